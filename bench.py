@@ -1,0 +1,342 @@
+"""Benchmark of the sketch-then-factor path (one JSON line on stdout).
+
+Workload: psvdfact of a dense 8192 x 8192 Float64 matrix A = U diag(s) V'
+with U, V Haar-random (thin QR of seeded N(0,1) matrices; columns past
+1024 carry s_i < 1e-25 and are dropped), s_i = 10^(-(i-1)/40), rtol 1e-10
+(rank ~ 400).  One step = one psvdfact call.  `value` is matrices/s with A
+resident in HBM; `e2e` is the same call from pinned host memory with the
+host<->device copies inside the timed region.  The inputs (512 MB) are
+larger than L2, so no flush is needed between steps.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+                  [--precision mixed|native] [--n 8192]
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+for p in (ROOT, os.path.join(ROOT, "lowrankapprox.jl_gb300")):
+    if p not in sys.path:
+        sys.path.insert(0, p)
+
+METRIC = "idfact/psvdfact matrices/s & GFLOP/s at rtol 1e-10 vs FP64 path; p50/p99 ms"
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--precision", default="mixed", choices=["mixed", "native"])
+    ap.add_argument("--n", type=int, default=8192)
+    ap.add_argument("--rtol", type=float, default=1e-10)
+    ap.add_argument("--no-fp64-leg", action="store_true")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    return ap.parse_args()
+
+
+def make_matrix(n: int, rank_cols: int = 1024):
+    """A = U diag(s) V' built on the GPU from seeded numpy Gaussians."""
+    import torch
+    r = min(n, rank_cols)
+    G1 = torch.from_numpy(np.random.default_rng(1).standard_normal((n, r))).cuda()
+    G2 = torch.from_numpy(np.random.default_rng(2).standard_normal((n, r))).cuda()
+    U, R1 = torch.linalg.qr(G1)
+    V, R2 = torch.linalg.qr(G2)
+    U = U * torch.sign(torch.diagonal(R1))[None, :]
+    V = V * torch.sign(torch.diagonal(R2))[None, :]
+    s = torch.pow(10.0, -torch.arange(r, dtype=torch.float64, device="cuda") / 40.0)
+    A = (U * s[None, :]) @ V.T
+    del G1, G2, U, V
+    # column-major storage
+    return A.t().contiguous().t()
+
+
+def psvd_flops(m, n, k_id, k, orders, ks):
+    """Algorithmic FLOPs of one psvdfact (sketch, QR, trsm, psvd extras)."""
+    f = 0.0
+    for l, kq in zip(orders, ks):
+        f += 2.0 * l * m * n
+        kq = min(kq + 1, l, n)
+        f += 4.0 * l * n * kq - 2.0 * kq * kq * (l + n) + 4.0 / 3.0 * kq ** 3
+    kk = k_id
+    f += kk * kk * (n - kk)                                   # trsm
+    f += 2.0 * m * kk * kk - 2.0 / 3.0 * kk ** 3              # QR(A[:, sk])
+    f += 2.0 * kk * kk * (n - kk)                             # R V
+    f += 4.0 * n * kk * kk + 8.0 * kk ** 3                    # SVD of R V
+    f += 4.0 * m * kk * k                                     # Q U~
+    return f
+
+
+def sketch_orders(k, nb=32):
+    orders, ks, nt = [], [], nb
+    while True:
+        orders.append(nt + 8)
+        if k < nt:
+            ks.append(k)
+            return orders, ks
+        ks.append(nt)
+        nt *= 2
+
+
+class Clocks:
+    """nvidia-smi sampling during the timed region."""
+
+    def __init__(self, gpu_index: int):
+        self.proc = None
+        self.path = os.path.join(ROOT, "gpurun_out", f"clocks_bench_{os.getpid()}.csv")
+        try:
+            os.makedirs(os.path.dirname(self.path), exist_ok=True)
+            self.f = open(self.path, "w")
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(gpu_index), "--query-gpu=index,clocks.sm,clocks.max.sm,power.draw,"
+                 "clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+                 "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+                 "clocks_event_reasons.sw_power_cap", "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=self.f, stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        time.sleep(0.3)
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        self.f.close()
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in open(self.path):
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                mx.append(float(parts[2]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[5:9]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"]}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def cpu_reference_step(A_host, rtol, seed, threads):
+    """The oracle's psvdfact on the host cores (numpy/OpenBLAS + C xLAQPS)."""
+    from oracle import oracle as O
+    rng = np.random.default_rng(seed)
+    m, n = A_host.shape
+    g = np.clip(np.rint(rng.standard_normal(2200 * m) * 32), -127, 127) / 32.0
+    backend = "lapack" if O.lapack_available() else "c"
+    t0 = time.perf_counter()
+    F = O.psvdfact(A_host, O.Opts(rtol=rtol), O.RandStream(gauss=g), backend=backend)
+    return time.perf_counter() - t0, F["k"], backend
+
+
+def run_reference(args):
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    threads = os.cpu_count() or 1
+    os.environ.setdefault("OPENBLAS_NUM_THREADS", str(threads))
+    import torch
+    A = make_matrix(args.n).cpu().numpy()
+    A = np.asfortranarray(A)
+    times = []
+    k = 0
+    backend = "c"
+    for i in range(args.warmup + args.steps):
+        dt, k, backend = cpu_reference_step(A, args.rtol, 100 + i, threads)
+        if i >= args.warmup:
+            times.append(dt)
+    sec = sum(times) / len(times)
+    val = 1.0 / sec
+    print(json.dumps({
+        "impl": "reference", "metric": METRIC, "value": val, "unit": "matrices/s", "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": sec * 1e3, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": f"psvdfact {args.n}x{args.n} F64 U diag(s) V', s_i=10^-(i-1)/40, rtol {args.rtol}",
+                   "m": args.n, "n": args.n, "rtol": args.rtol, "rank": k},
+        "cpu_baseline": {"value": val, "unit": "matrices/s", "cores": threads, "kind": "port",
+                         "sample": f"one full {args.n}^2 psvdfact per step (oracle restatement, "
+                                   f"numpy/OpenBLAS BLAS-3, xLAQPS backend {backend}); Julia absent"},
+        "e2e": {"value": val, "unit": "matrices/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }), flush=True)
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        return run_reference(args)
+    import torch
+    import torch.distributed as dist
+
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        dist.init_process_group("gloo")
+    torch.cuda.set_device(local)
+    import lowrankapprox as lra
+
+    ctx = lra.Context(local)
+    n = args.n
+    A = make_matrix(n)
+    torch.cuda.synchronize()
+    opts = lra.LRAOptions(rtol=args.rtol, precision=args.precision, seed=1234 + rank)
+
+    def step(X, o=opts):
+        return lra.psvdfact(X, o, ctx=ctx)
+
+    for _ in range(args.warmup):
+        F = step(A)
+    k = F.k
+
+    # ---- device-resident timed region ---------------------------------------
+    def barrier():
+        if world > 1:
+            dist.barrier()
+
+    stage_tot = {"sketch": 0.0, "qr": 0.0, "solve": 0.0, "post": 0.0}
+    clocks = Clocks(local)
+    barrier()
+    torch.cuda.synchronize()
+    l0 = ctx.launches
+    per = []
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        ts = time.perf_counter()
+        F = step(A)
+        per.append(time.perf_counter() - ts)
+        for kk, v in ctx.stage_ms().items():
+            stage_tot[kk] += v
+    torch.cuda.synchronize()
+    elapsed = time.perf_counter() - t0
+    barrier()
+    clk = clocks.stop()
+    launches = ctx.launches - l0
+    if world > 1:
+        t = torch.tensor([elapsed], dtype=torch.float64)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        elapsed = float(t[0])
+    value = world * args.steps / elapsed
+
+    # ---- end to end from pinned host memory ------------------------------------
+    Ah = torch.empty((n, n), dtype=torch.float64, pin_memory=True)
+    Ah.copy_(A.t())  # row-major buffer of A^T == column-major A
+    A_host = Ah.numpy().T  # Fortran-ordered view of pinned memory
+    assert A_host.flags.f_contiguous
+    step(A_host)
+    barrier()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        Fe = step(A_host)
+    torch.cuda.synchronize()
+    e2e_el = time.perf_counter() - t0
+    e2e_val = world * args.steps / e2e_el
+    h2d = n * n * 8
+    d2h = (Fe.U.size + Fe.S.size + Fe.Vt.size) * 8
+
+    # ---- accuracy of the last result ----------------------------------------------
+    g = np.random.default_rng(7).standard_normal(n)
+    err = lra.snormdiff(A, F, rand=lra.RandStream(gauss=g), ctx=ctx)
+    nrm = lra.snorm(A, rand=lra.RandStream(gauss=g), ctx=ctx)
+
+    # ---- the plain FP64 GPU path (same call, native precision) ---------------------
+    fp64 = None
+    if not args.no_fp64_leg and args.precision != "native":
+        on = opts.copy(precision="native")
+        step(A, on)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        reps = max(1, min(2, args.steps))
+        for _ in range(reps):
+            Fn = step(A, on)
+        torch.cuda.synchronize()
+        fsec = (time.perf_counter() - t0) / reps
+        errn = lra.snormdiff(A, Fn, rand=lra.RandStream(gauss=g), ctx=ctx)
+        fp64 = {"value": world / fsec, "unit": "matrices/s", "ms_per_step": fsec * 1e3,
+                "rel_spectral_err": errn / nrm, "rank": Fn.k}
+
+    # ---- roofline of the dominant stage ------------------------------------------------
+    import json as _json
+    peaks = {}
+    try:
+        peaks = _json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
+    except Exception:
+        pass
+    orders, ks = sketch_orders(k)
+    k_id = k  # ID rank ~ psvd rank before truncation
+    flops = psvd_flops(n, n, k_id, k, orders, ks)
+    sketch_flops = sum(2.0 * l * n * n for l in orders)
+    st = {kk: v / args.steps for kk, v in stage_tot.items()}
+    dom = max(st, key=st.get)
+    if dom == "sketch":
+        achieved = sketch_flops / (st["sketch"] * 1e-3) / 1e12
+        peak = peaks.get("bf16_tflops", 1900.0)
+        roof = {"kernel": "sketch GEMM (S op(A))", "bound": "tensor", "achieved": achieved, "peak": peak,
+                "unit": "TFLOP/s", "frac": achieved / peak, "traffic": None,
+                "peak_source": "MEASURED_PEAKS.json bf16_tflops (burst)" if peaks else "fallback"}
+    else:
+        qr_flops = sum(4.0 * l * n * min(kq + 1, l) for l, kq in zip(orders, ks))
+        achieved = qr_flops / (st[dom] * 1e-3) / 1e12
+        roof = {"kernel": f"{dom} stage", "bound": "fp64", "achieved": achieved, "peak": 1.25,
+                "unit": "TFLOP/s", "frac": achieved / 1.25, "traffic": None,
+                "peak_source": "nominal GB300 FP64 (not in MEASURED_PEAKS.json)"}
+    roof["stage_ms"] = st
+
+    # ---- CPU baseline (oracle on the host cores, one bounded sample) -------------------
+    cpu = None
+    if rank == 0 and not args.no_cpu_baseline:
+        try:
+            Ac = np.asfortranarray(A.cpu().numpy())
+            dt, kc, backend = cpu_reference_step(Ac, args.rtol, 5, os.cpu_count())
+            cpu = {"value": 1.0 / dt, "unit": "matrices/s", "cores": os.cpu_count(), "kind": "port",
+                   "sample": f"one full {n}^2 psvdfact (oracle: numpy/OpenBLAS BLAS-3 + xLAQPS {backend}), "
+                             f"rank {kc}"}
+        except Exception as e:  # pragma: no cover
+            cpu = {"value": None, "unit": "matrices/s", "cores": os.cpu_count(), "kind": "port",
+                   "sample": f"failed: {e}"}
+
+    if rank == 0:
+        per_ms = sorted(1e3 * p for p in per)
+        line = {
+            "metric": METRIC, "value": value, "unit": "matrices/s", "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": 1e3 * elapsed / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": f"psvdfact {n}x{n} F64 U diag(s) V', s_i=10^-(i-1)/40, rtol {args.rtol}",
+                       "m": n, "n": n, "rtol": args.rtol, "precision": args.precision,
+                       "l2": "inputs (512 MB) larger than L2; no flush"},
+            "gflops": flops / (elapsed / args.steps) / 1e9,
+            "p50_ms": per_ms[len(per_ms) // 2], "p99_ms": per_ms[min(len(per_ms) - 1, int(0.99 * len(per_ms)))],
+            "rank": k, "rel_spectral_err": err / nrm,
+            "e2e": {"value": e2e_val, "unit": "matrices/s", "h2d_bytes_per_step": h2d,
+                    "d2h_bytes_per_step": d2h},
+            "fp64_path": fp64,
+            "roofline": roof, "cpu_baseline": cpu, "clocks": clk, "gpu_launches": launches,
+        }
+        print(json.dumps(line), flush=True)
+    if world > 1:
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,296 @@
+/*
+ * lra.h -- C ABI of liblra, the GB300 (sm_103a) engine for LowRankApprox.jl's
+ * sketch-then-factor path (idfact / pqrfact / psvdfact / pheigfact / curfact,
+ * sketch / sketchfact, snorm / snormdiff).
+ *
+ * Conventions (chosen so that a Julia `ccall` shim needs no copies):
+ *   - matrices are column-major with an explicit leading dimension (Julia's
+ *     `stride(A, 2)`), exactly as the reference passes them to LAPACK
+ *     (src/lapack.jl:129-136);
+ *   - integer outputs (pivots, skeleton / redundant indices, rows, cols) are
+ *     int64 and 1-based, like Julia's `Vector{Int}` (src/pqr.jl:350,357);
+ *   - an input pointer may be host or device memory; the library detects
+ *     which with cudaPointerGetAttributes and never mutates an input;
+ *   - results are returned in library-owned host structs, released with the
+ *     matching lra_*_free (a Julia finalizer);
+ *   - every entry point returns an lra_status; lra_last_error(ctx) gives the
+ *     message.  The Julia shim maps LRA_EINVAL -> ArgumentError,
+ *     LRA_EDIM -> DimensionMismatch, LRA_ENOTHERM -> ErrorException
+ *     ("matrix must be Hermitian", src/pheig.jl:279).
+ *
+ * A context owns one CUDA stream, a device workspace arena and pinned host
+ * staging.  It is thread-compatible, not thread-safe: use one per host thread.
+ */
+#ifndef LRA_H
+#define LRA_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define LRA_VERSION_MAJOR 0
+#define LRA_VERSION_MINOR 1
+
+/* ---- status codes -------------------------------------------------------- */
+typedef enum lra_status {
+  LRA_OK = 0,
+  LRA_EINVAL = 1,      /* bad option / argument   (ArgumentError)        */
+  LRA_EDIM = 2,        /* inconsistent dimensions (DimensionMismatch)     */
+  LRA_ENOMEM = 3,      /* device or host allocation failed                */
+  LRA_ETIMEDOUT = 4,   /* a bounded device wait gave up                   */
+  LRA_ENONFINITE = 5,  /* NaN / Inf in the input                          */
+  LRA_ECUDA = 6,       /* CUDA runtime error                              */
+  LRA_ERAND = 7,       /* injected random stream too short                */
+  LRA_ENOTSUP = 8,     /* combination not supported by this build         */
+  LRA_ENOTHERM = 9,    /* pheigfact on a non-Hermitian matrix             */
+  LRA_EBUSY = 10       /* server queue full / over HBM budget             */
+} lra_status;
+
+typedef enum lra_dtype { LRA_F32 = 0, LRA_F64 = 1 } lra_dtype;
+
+/* src/LowRankApprox.jl:138 -- the valid sketch symbols */
+typedef enum lra_sketch_kind {
+  LRA_SKETCH_NONE = 0,
+  LRA_SKETCH_RANDN = 1,
+  LRA_SKETCH_SPRN = 2,
+  LRA_SKETCH_SRFT = 3,
+  LRA_SKETCH_SUB = 4
+} lra_sketch_kind;
+
+/* pqrfact_retval letters (src/pqr.jl:298-300) as a bit set */
+enum { LRA_RET_Q = 1, LRA_RET_R = 2, LRA_RET_T = 4 };
+
+/* arithmetic of the GEMM-shaped stages */
+typedef enum lra_precision {
+  LRA_PREC_NATIVE = 0, /* plain FP64 (FP32 for Float32 input) on CUDA cores  */
+  LRA_PREC_MIXED = 1   /* exact-split BF16 slices on tcgen05 tensor cores,
+                          FP64-faithful accumulation; the pivoted QR, norm
+                          recomputation, triangular solve and small dense
+                          factorizations stay in the input precision        */
+} lra_precision;
+
+/*
+ * LRAOptions (src/LowRankApprox.jl:77-120), field for field.  The
+ * oversampling functions `n -> a*n + b` become affine coefficients
+ * {a, b}; arbitrary Julia closures are rejected by the shim.
+ */
+typedef struct lra_opts {
+  double atol;                  /* 0                                      */
+  int64_t maxdet_niter;         /* -1                                     */
+  double maxdet_tol;            /* -1 (off)                               */
+  int64_t nb;                   /* 32                                     */
+  double pheig_orthtol;         /* sqrt(eps(T))                           */
+  int32_t pqrfact_retval;       /* LRA_RET_Q | LRA_RET_R                  */
+  int32_t sketch;               /* LRA_SKETCH_RANDN                       */
+  int64_t rank;                 /* -1                                     */
+  double rtol;                  /* 5 eps(T)                               */
+  int64_t sketch_randn_niter;   /* 0                                      */
+  int32_t sketchfact_adap;      /* 1                                      */
+  int32_t verb;                 /* 1                                      */
+  int64_t sketchfact_randn_samp[2]; /* {1, 8}:  n -> n + 8               */
+  int64_t sketchfact_srft_samp[2];  /* {1, 8}:  n -> n + 8               */
+  int64_t sketchfact_sub_samp[2];   /* {4, 8}:  n -> 4n + 8              */
+  int64_t snorm_niter;          /* 32                                     */
+  /* GB300 engine options (no counterpart in LRAOptions) */
+  int32_t precision;            /* lra_precision, default LRA_PREC_NATIVE */
+  int32_t check_finite;         /* reject NaN/Inf input (default 1)       */
+  uint64_t seed;                /* seed of the in-library generator       */
+} lra_opts;
+
+/*
+ * Injected randomness.  The reference draws its random numbers inside the
+ * sketch operators (src/sketch.jl:92,252,339-361,575; src/snorm.jl:18).
+ * For reproducible parity the caller may supply them instead; each sketch
+ * consumes, per adaptive step, in this order:
+ *   randn : l*M values of `gauss` = S (l x M, column-major)
+ *   srft  : M values of `gauss` (d_i = +1 if > 0 else -1), then l values of
+ *           `ints` (idx_i = 1 + (v - 1) mod M)
+ *   sub   : l values of `ints` (rows r_i = 1 + (v - 1) mod M)
+ *   sprn  : M values of `ints` used as sort keys (the permutation is their
+ *           stable ascending rank order, 1-based), then M values of `gauss`
+ *           (row i uses fld(M-i, l) + 1 of them)
+ *   snorm : N values of `gauss` (the start vector)
+ * where M is the sketched dimension and l the sketch order.  Pointers may be
+ * host or device memory.  With rand == NULL the library draws from its own
+ * counter-based generator seeded by opts->seed.
+ */
+typedef struct lra_rand {
+  const double* gauss;
+  int64_t gauss_len;
+  const int64_t* ints;
+  int64_t ints_len;
+} lra_rand;
+
+/* ---- result types (library-owned host memory) --------------------------- */
+
+/* IDPackedV (src/id.jl:15-92): A[:, rd] ~= A[:, sk] * T */
+typedef struct lra_id {
+  int32_t dtype;
+  int32_t nsteps;     /* adaptive sketch steps taken */
+  int64_t k, n;
+  int64_t* sk;        /* k, 1-based                  */
+  int64_t* rd;        /* n - k, 1-based              */
+  void* T;            /* k x (n - k), ld = k         */
+} lra_id;
+
+/* PartialQRFactors (src/pqr.jl:14-32); Q, R, T are NULL unless requested */
+typedef struct lra_pqr {
+  int32_t dtype;
+  int32_t retval;     /* LRA_RET_* bits that were filled */
+  int64_t m, n, k;
+  int64_t* p;         /* n, 1-based column permutation */
+  void* Q;            /* m x k, ld = m                 */
+  void* R;            /* k x n, ld = k                 */
+  void* T;            /* k x (n - k), ld = k           */
+} lra_pqr;
+
+/* PartialSVD (src/psvd.jl:4-16): A ~= U * diagm(S) * Vt */
+typedef struct lra_psvd {
+  int32_t dtype;
+  int32_t _pad;
+  int64_t m, n, k;
+  void* U;            /* m x k, ld = m (NULL for psvdvals) */
+  void* S;            /* k                                 */
+  void* Vt;           /* k x n, ld = k (NULL for psvdvals) */
+} lra_psvd;
+
+/* PartialHermitianEigen (src/pheig.jl:4-7) */
+typedef struct lra_pheig {
+  int32_t dtype;
+  int32_t _pad;
+  int64_t n, k;
+  void* values;       /* k, ascending              */
+  void* vectors;      /* n x k, ld = n (NULL: vals) */
+} lra_pheig;
+
+/* CURPackedU / HermitianCURPackedU / SymmetricCURPackedU (src/cur.jl:14-57) */
+typedef struct lra_cur {
+  int32_t kind;       /* 0 general, 1 Hermitian, 2 symmetric */
+  int32_t _pad;
+  int64_t kr, kc;
+  int64_t* rows;      /* kr, 1-based (== cols for kinds 1, 2) */
+  int64_t* cols;      /* kc, 1-based */
+} lra_cur;
+
+/* one matrix of a batch */
+typedef struct lra_matdesc {
+  int64_t m, n, lda;
+  const void* A;
+} lra_matdesc;
+
+/* ---- context ------------------------------------------------------------- */
+typedef struct lra_ctx lra_ctx;
+
+int lra_ctx_create(int device, lra_ctx** ctx);
+void lra_ctx_destroy(lra_ctx* ctx);
+/* use the caller's cudaStream_t for all work of this context */
+int lra_ctx_set_stream(lra_ctx* ctx, void* cuda_stream);
+const char* lra_last_error(const lra_ctx* ctx);
+const char* lra_status_string(int status);
+/* number of kernels this context has launched (instrumentation) */
+int64_t lra_ctx_launches(const lra_ctx* ctx);
+/* device time of the last call's stages, ms: sketch, qr, solve, post */
+int lra_ctx_stage_ms(const lra_ctx* ctx, double out[4]);
+
+/* LRAOptions(T) defaults (src/LowRankApprox.jl:96-119) */
+int lra_opts_init(lra_opts* opts, int dtype);
+/* chkopts! (src/LowRankApprox.jl:133-141) */
+int lra_chkopts(const lra_opts* opts);
+
+/* ---- sketches (src/sketch.jl) -------------------------------------------- */
+
+/* sketch(side, trans, A, order) (src/sketch.jl:35-46): writes B, which is
+   order x M' (side 'l') or M' x order (side 'r'), into caller memory `B`
+   (host or device), leading dimension ldb.                                 */
+int lra_sketch(lra_ctx* ctx, int dtype, char side, char trans, int64_t m,
+               int64_t n, const void* A, int64_t lda, int64_t order,
+               const lra_opts* opts, const lra_rand* rand, void* B,
+               int64_t ldb);
+
+/* sketchfact(side, trans, A) (src/sketch.jl:52-63, 223-240): adaptive
+   sketch + partial pivoted QR; returns PartialQRFactors with the options'
+   pqrfact_retval (Q is the Q of the sketch, as in the reference).          */
+int lra_sketchfact(lra_ctx* ctx, int dtype, char side, char trans, int64_t m,
+                   int64_t n, const void* A, int64_t lda, const lra_opts* opts,
+                   const lra_rand* rand, lra_pqr** out);
+
+/* geqp3_adap! (src/pqr.jl:348-418) on a DEVICE matrix, in place: B (m x n,
+   ldb) becomes R (upper) + Householder vectors (below), jpvt (n, int64,
+   1-based) the column permutation, tau (min(m,n)) the reflector scalars,
+   *k the detected rank.  Replaces the `_LAPACK.laqps!` ccall loop
+   (src/lapack.jl:117-139 called from src/pqr.jl:394-416).                   */
+int lra_geqp3_adap(lra_ctx* ctx, int dtype, int64_t m, int64_t n, void* B,
+                   int64_t ldb, int64_t* jpvt, void* tau, const lra_opts* opts,
+                   int64_t* k);
+
+/* ---- factorizations --------------------------------------------------------- */
+
+/* idfact(trans, A) (src/id.jl:434-450) */
+int lra_idfact(lra_ctx* ctx, int dtype, char trans, int64_t m, int64_t n,
+               const void* A, int64_t lda, const lra_opts* opts,
+               const lra_rand* rand, lra_id** out);
+
+/* pqrfact(trans, A) (src/pqr.jl:290-307) */
+int lra_pqrfact(lra_ctx* ctx, int dtype, char trans, int64_t m, int64_t n,
+                const void* A, int64_t lda, const lra_opts* opts,
+                const lra_rand* rand, lra_pqr** out);
+
+/* psvdfact(A) (src/psvd.jl:238-272); psvdvals (src/psvd.jl:274-290) when
+   vals_only != 0 (U and Vt are then NULL).                                  */
+int lra_psvdfact(lra_ctx* ctx, int dtype, int64_t m, int64_t n, const void* A,
+                 int64_t lda, const lra_opts* opts, const lra_rand* rand,
+                 int vals_only, lra_psvd** out);
+
+/* pheigfact(A) (src/pheig.jl:276-296); pheigvals (src/pheig.jl:298-311) */
+int lra_pheigfact(lra_ctx* ctx, int dtype, int64_t n, const void* A,
+                  int64_t lda, const lra_opts* opts, const lra_rand* rand,
+                  int vals_only, lra_pheig** out);
+
+/* curfact(A) (src/cur.jl:532-564) */
+int lra_curfact(lra_ctx* ctx, int dtype, int64_t m, int64_t n, const void* A,
+                int64_t lda, const lra_opts* opts, const lra_rand* rand,
+                lra_cur** out);
+
+/* ---- spectral norms (src/snorm.jl) ------------------------------------------ */
+
+/* snorm(A) (src/snorm.jl:14-45) */
+int lra_snorm(lra_ctx* ctx, int dtype, int64_t m, int64_t n, const void* A,
+              int64_t lda, int hermitian, const lra_opts* opts,
+              const lra_rand* rand, double* out);
+/* snormdiff(A, B) = snorm(A - B) (src/snorm.jl:50-53, src/linop.jl:176-187) */
+int lra_snormdiff(lra_ctx* ctx, int dtype, int64_t m, int64_t n,
+                  const void* A, int64_t lda, const void* B, int64_t ldb,
+                  const lra_opts* opts, const lra_rand* rand, double* out);
+/* snormdiff(A, F) with F = A[:, sk] * [I T] P' applied in factored form */
+int lra_snormdiff_id(lra_ctx* ctx, int dtype, char trans, int64_t m, int64_t n,
+                     const void* A, int64_t lda, const lra_id* F,
+                     const lra_opts* opts, const lra_rand* rand, double* out);
+/* snormdiff(A, F) with F = U * diagm(S) * Vt applied in factored form */
+int lra_snormdiff_psvd(lra_ctx* ctx, int dtype, int64_t m, int64_t n,
+                       const void* A, int64_t lda, const lra_psvd* F,
+                       const lra_opts* opts, const lra_rand* rand,
+                       double* out);
+
+/* ---- batches of independent matrices ---------------------------------------- */
+
+/* idfact over `count` matrices of uneven sizes, grouped on one stream.
+   outs[i] receives matrix i's IDPackedV.  rand may be NULL or an array of
+   `count` streams.                                                         */
+int lra_idfact_batched(lra_ctx* ctx, int dtype, int64_t count,
+                       const lra_matdesc* mats, const lra_opts* opts,
+                       const lra_rand* rand, lra_id** outs);
+
+/* ---- freeing ---------------------------------------------------------------- */
+void lra_id_free(lra_id* r);
+void lra_pqr_free(lra_pqr* r);
+void lra_psvd_free(lra_psvd* r);
+void lra_pheig_free(lra_pheig* r);
+void lra_cur_free(lra_cur* r);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* LRA_H */

@@ -1,0 +1,1531 @@
+// C ABI of liblra: option handling, randomness, and the host-side drivers
+// of the sketch-then-factor path.  Every numerical stage runs on the GPU;
+// the host only sequences launches and reads back the few scalars the
+// reference's control flow branches on (the rank of each adaptive step,
+// the singular / eigen values that decide the truncation).
+
+#include <algorithm>
+#include <cmath>
+#include <cstdlib>
+#include <cstring>
+#include <new>
+#include <numeric>
+#include <vector>
+
+#include "internal.hpp"
+
+namespace lra {
+
+namespace {
+
+bool is_dev(const void* p) {
+  if (!p) return false;
+  cudaPointerAttributes a;
+  cudaError_t e = cudaPointerGetAttributes(&a, p);
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    return false;
+  }
+  return a.type == cudaMemoryTypeDevice || a.type == cudaMemoryTypeManaged;
+}
+
+template <typename T>
+struct DMat {
+  const T* p;
+  int64_t ld;
+};
+
+template <typename T>
+DMat<T> stage_in(lra_ctx* ctx, const void* A, int64_t m, int64_t n, int64_t lda) {
+  if (m == 0 || n == 0) return DMat<T>{static_cast<const T*>(A), std::max<int64_t>(lda, 1)};
+  if (!A) fail(LRA_EINVAL, "null matrix pointer");
+  if (lda < std::max<int64_t>(1, m)) fail(LRA_EDIM, "lda (%lld) < m (%lld)", (long long)lda, (long long)m);
+  if (is_dev(A)) return DMat<T>{static_cast<const T*>(A), lda};
+  T* d = ctx->arena.alloc_n<T>((size_t)m * n);
+  LRA_CUDA(cudaMemcpy2DAsync(d, m * sizeof(T), A, lda * sizeof(T), m * sizeof(T), n, cudaMemcpyHostToDevice,
+                             ctx->stream));
+  return DMat<T>{d, m};
+}
+
+template <typename T>
+void to_host(lra_ctx* ctx, void* dst, const T* src, size_t n) {
+  if (n == 0) return;
+  LRA_CUDA(cudaMemcpyAsync(dst, src, n * sizeof(T), cudaMemcpyDeviceToHost, ctx->stream));
+}
+
+void* hmalloc(size_t bytes) {
+  void* p = std::malloc(bytes ? bytes : 1);
+  if (!p) fail(LRA_ENOMEM, "host allocation of %zu bytes", bytes);
+  return p;
+}
+
+// ---- stage timing (CUDA events on the context stream) ----------------------
+struct Stage {
+  lra_ctx* ctx;
+  int idx;
+  cudaEvent_t a = nullptr, b = nullptr;
+  Stage(lra_ctx* c, int i) : ctx(c), idx(i) {
+    cudaEventCreate(&a);
+    cudaEventCreate(&b);
+    cudaEventRecord(a, ctx->stream);
+  }
+  ~Stage() {
+    cudaEventRecord(b, ctx->stream);
+    cudaEventSynchronize(b);
+    float ms = 0;
+    if (cudaEventElapsedTime(&ms, a, b) == cudaSuccess) ctx->stage_ms[idx] += ms;
+    cudaEventDestroy(a);
+    cudaEventDestroy(b);
+    cudaGetLastError();
+  }
+};
+
+// ---- randomness ---------------------------------------------------------------
+struct RandSrc {
+  lra_ctx* ctx;
+  const lra_rand* r;
+  uint64_t seed;
+  int64_t g = 0, q = 0;
+  bool gdev = false, qdev = false;
+
+  RandSrc(lra_ctx* c, const lra_rand* rr, uint64_t s) : ctx(c), r(rr), seed(s) {
+    if (r) {
+      gdev = is_dev(r->gauss);
+      qdev = is_dev(r->ints);
+    }
+  }
+  bool injected_gauss() const { return r && r->gauss; }
+  bool injected_ints() const { return r && r->ints; }
+
+  const double* take_gauss_raw(int64_t n) {
+    if (g + n > r->gauss_len)
+      fail(LRA_ERAND, "gauss stream exhausted: need %lld values at offset %lld, have %lld", (long long)n,
+           (long long)g, (long long)r->gauss_len);
+    const double* src = r->gauss + g;
+    g += n;
+    if (gdev) return src;
+    double* d = ctx->arena.alloc_n<double>(n);
+    LRA_CUDA(cudaMemcpyAsync(d, src, n * sizeof(double), cudaMemcpyHostToDevice, ctx->stream));
+    return d;
+  }
+
+  template <typename T>
+  void gauss(int64_t n, T* out, bool lattice) {
+    if (n <= 0) return;
+    if (injected_gauss()) {
+      sketch_from_stream(ctx, take_gauss_raw(n), n, out, lattice);
+    } else {
+      sketch_philox(ctx, seed, ctx->rng_counter, n, out);
+      ctx->rng_counter += (uint64_t)(n + 1) / 2;
+    }
+  }
+
+  template <typename T>
+  void signs(int64_t n, T* d) {
+    if (n <= 0) return;
+    if (injected_gauss()) {
+      srft_signs(ctx, take_gauss_raw(n), n, d);
+    } else {
+      sketch_philox(ctx, seed, ctx->rng_counter, n, d);
+      ctx->rng_counter += (uint64_t)(n + 1) / 2;
+      // sign of a lattice Gaussian: map to +-1 through the stream kernel
+      double* tmp = ctx->arena.alloc_n<double>(n);
+      sketch_philox(ctx, seed ^ 0x5bd1e995ull, ctx->rng_counter, n, tmp);
+      ctx->rng_counter += (uint64_t)(n + 1) / 2;
+      srft_signs(ctx, tmp, n, d);
+    }
+  }
+
+  // n indices in [1, hi] (1 + (v - 1) mod hi), or with perm a permutation of
+  // 1..n (the stable ascending rank order of n keys)
+  void ints(int64_t n, int64_t hi, int64_t* out, bool perm) {
+    if (n <= 0) return;
+    if (injected_ints()) {
+      if (q + n > r->ints_len)
+        fail(LRA_ERAND, "int stream exhausted: need %lld values at offset %lld, have %lld", (long long)n,
+             (long long)q, (long long)r->ints_len);
+      std::vector<int64_t> h(n);
+      if (qdev) {
+        LRA_CUDA(cudaMemcpyAsync(h.data(), r->ints + q, n * sizeof(int64_t), cudaMemcpyDeviceToHost,
+                                 ctx->stream));
+        LRA_CUDA(cudaStreamSynchronize(ctx->stream));
+      } else {
+        std::memcpy(h.data(), r->ints + q, n * sizeof(int64_t));
+      }
+      q += n;
+      std::vector<int64_t> v(n);
+      if (perm) {
+        std::vector<int64_t> ord(n);
+        std::iota(ord.begin(), ord.end(), 0);
+        std::stable_sort(ord.begin(), ord.end(), [&](int64_t a, int64_t b) { return h[a] < h[b]; });
+        for (int64_t i = 0; i < n; ++i) v[i] = ord[i] + 1;
+      } else {
+        for (int64_t i = 0; i < n; ++i) v[i] = 1 + (((h[i] - 1) % hi) + hi) % hi;
+      }
+      LRA_CUDA(cudaMemcpyAsync(out, v.data(), n * sizeof(int64_t), cudaMemcpyHostToDevice, ctx->stream));
+      LRA_CUDA(cudaStreamSynchronize(ctx->stream));
+    } else if (perm) {
+      perm_philox(ctx, seed, ctx->rng_counter, n, out);
+      ctx->rng_counter += (uint64_t)n;
+    } else {
+      ints_philox(ctx, seed, ctx->rng_counter, n, hi, out);
+      ctx->rng_counter += (uint64_t)n;
+    }
+  }
+};
+
+// ---- options --------------------------------------------------------------------
+int64_t samp(const lra_opts& o, int64_t n) {
+  switch (o.sketch) {
+    case LRA_SKETCH_RANDN:
+      return o.sketchfact_randn_samp[0] * n + o.sketchfact_randn_samp[1];
+    case LRA_SKETCH_SRFT:
+      return o.sketchfact_srft_samp[0] * n + o.sketchfact_srft_samp[1];
+    case LRA_SKETCH_SUB:
+      return o.sketchfact_sub_samp[0] * n + o.sketchfact_sub_samp[1];
+    default:
+      return n;  // sprn: order = n (src/sketch.jl:680)
+  }
+}
+
+void chkopts(const lra_opts* o) {
+  if (!o) fail(LRA_EINVAL, "opts is NULL");
+  if (!(o->atol >= 0)) fail(LRA_EINVAL, "atol");
+  if (!(o->nb > 0)) fail(LRA_EINVAL, "nb");
+  if (!(o->pheig_orthtol >= 0)) fail(LRA_EINVAL, "pheig_orthtol");
+  if (!(o->rtol >= 0)) fail(LRA_EINVAL, "rtol");
+  if (o->sketch < LRA_SKETCH_NONE || o->sketch > LRA_SKETCH_SUB) fail(LRA_EINVAL, "sketch");
+  if (o->precision != LRA_PREC_NATIVE && o->precision != LRA_PREC_MIXED) fail(LRA_EINVAL, "precision");
+  if (o->sketch_randn_niter < 0) fail(LRA_EINVAL, "sketch_randn_niter");
+  if (o->pqrfact_retval & ~(LRA_RET_Q | LRA_RET_R | LRA_RET_T)) fail(LRA_EINVAL, "pqrfact_retval");
+}
+
+char chktrans(char t) {
+  if (t == 'n' || t == 'N') return 'n';
+  if (t == 'c' || t == 'C' || t == 't' || t == 'T') return 'c';
+  fail(LRA_EINVAL, "trans");
+}
+
+int slices_for(const lra_opts& o, int dtype) {
+  // 8-bit slices of A until the truncation is far below rtol
+  const double target = std::max(o.rtol, dtype == LRA_F64 ? 1e-15 : 1e-7) * 1e-2;
+  int s = 1;
+  while (s < 7 && std::ldexp(1.0, -8 * s + 1) > target) ++s;
+  return s;
+}
+
+// ---- sketches ----------------------------------------------------------------------
+template <typename T>
+void orthrows(lra_ctx* ctx, int64_t rows, int64_t cols, T* B) {
+  // thin = false: Q of the LQ factorization, rows beyond min(rows, cols) zeroed
+  const ArenaMark mk = ctx->arena.mark();
+  const int64_t kq = std::min(rows, cols);
+  T* Wt = ctx->arena.alloc_n<T>((size_t)cols * rows);
+  transpose(ctx, rows, cols, B, rows, Wt, cols);
+  int64_t* jp = ctx->arena.alloc_n<int64_t>(rows);
+  T* tau = ctx->arena.alloc_n<T>(std::max<int64_t>(kq, 1));
+  geqp3_adap<T>(ctx, cols, rows, Wt, cols, jp, tau, kq, 32, -1.0, 0.0, false);
+  orgqr(ctx, cols, kq, Wt, cols, tau);
+  set_zero(ctx, B, rows * cols);
+  transpose(ctx, cols, kq, Wt, cols, B, rows);
+  LRA_CUDA(cudaStreamSynchronize(ctx->stream));
+  ctx->arena.release(mk);
+}
+
+// whether the Gaussian sketch runs on the tensor cores: the mixed path
+// resolves op(A) to 2^-48 (Float64) / 2^-24 (Float32) of each column's
+// scale, so a Float64 rtol below 1e-13 keeps the native GEMM.
+bool use_tc(const lra_opts& o, int dtype) {
+  if (o.precision != LRA_PREC_MIXED || o.sketch != LRA_SKETCH_RANDN) return false;
+  return dtype == LRA_F32 || o.rtol >= 1e-13;
+}
+
+// right_layout: the Gaussian matrix is drawn as M x order (column-major), the
+// layout of a right sketch A S (src/sketch.jl:95-98), and used transposed
+template <typename T>
+void make_sketch(lra_ctx* ctx, const lra_opts& o, char trans, int64_t M, int64_t N, const T* A, int64_t lda,
+                 int64_t order, RandSrc& rs, T* B, int dtype, TcSplit* split = nullptr, bool right_layout = false) {
+  const ArenaMark mk = ctx->arena.mark();
+  const char tA = trans == 'c' ? 't' : 'n';
+  switch (o.sketch) {
+    case LRA_SKETCH_RANDN: {
+      const bool tc = use_tc(o, dtype) && tc_sketch_supported(order, M, N);
+      T* S = ctx->arena.alloc_n<T>((size_t)order * M);
+      if (right_layout) {
+        T* Sr = ctx->arena.alloc_n<T>((size_t)order * M);
+        rs.gauss(order * M, Sr, o.precision == LRA_PREC_MIXED);
+        transpose(ctx, M, order, Sr, std::max<int64_t>(M, 1), S, std::max<int64_t>(order, 1));
+      } else {
+        rs.gauss(order * M, S, o.precision == LRA_PREC_MIXED);
+      }
+      if (tc) {
+        TcSplit local;
+        if (!split) split = &local;
+        if (split->ns == 0) tc_split<T>(ctx, trans, M, N, A, lda, dtype == LRA_F64 ? 6 : 3, split);
+        tc_sketch<T>(ctx, *split, order, S, B, order);
+      } else {
+        gemm<T>(ctx, 'n', tA, order, N, M, T(1), S, order, A, lda, T(0), B, order);
+      }
+      if (o.sketch_randn_niter > 0) {
+        const bool herm = (M == N) && is_symmetric(ctx, M, A, lda);
+        T* Bq = ctx->arena.alloc_n<T>((size_t)order * M);
+        for (int64_t it = 0; it < o.sketch_randn_niter; ++it) {
+          orthrows(ctx, order, N, B);
+          // Bq = Bp op(A)^T (order x M)
+          gemm<T>(ctx, 'n', trans == 'c' ? 'n' : 't', order, M, N, T(1), B, order, A, lda, T(0), Bq, order);
+          if (herm) {
+            copy_matrix(ctx, order, M, Bq, order, B, order);
+          } else {
+            orthrows(ctx, order, M, Bq);
+            gemm<T>(ctx, 'n', tA, order, N, M, T(1), Bq, order, A, lda, T(0), B, order);
+          }
+        }
+      }
+      break;
+    }
+    case LRA_SKETCH_SRFT: {
+      T* d = ctx->arena.alloc_n<T>(M);
+      rs.signs(M, d);
+      int64_t* idx = ctx->arena.alloc_n<int64_t>(order);
+      rs.ints(order, M, idx, false);
+      srft_sketch<T>(ctx, trans, M, N, A, lda, d, idx, order, B, order);
+      break;
+    }
+    case LRA_SKETCH_SUB: {
+      int64_t* rows = ctx->arena.alloc_n<int64_t>(order);
+      rs.ints(order, M, rows, false);
+      sub_sketch<T>(ctx, trans, M, N, A, lda, rows, order, B, order);
+      break;
+    }
+    case LRA_SKETCH_SPRN: {
+      int64_t* perm = ctx->arena.alloc_n<int64_t>(M);
+      rs.ints(M, M, perm, true);
+      T* g = ctx->arena.alloc_n<T>(M);
+      rs.gauss(M, g, false);
+      sprn_sketch<T>(ctx, trans, M, N, A, lda, perm, g, order, B, order);
+      break;
+    }
+    default:
+      fail(LRA_EINVAL, "sketch");
+  }
+  LRA_CUDA(cudaStreamSynchronize(ctx->stream));
+  ctx->arena.release(mk);
+}
+
+// ---- pivoted QR + post-processing --------------------------------------------------
+template <typename T>
+struct Fact {
+  T* B = nullptr;  // order x N, R in the upper triangle
+  int64_t ld = 0, order = 0, N = 0;
+  int64_t* jpvt = nullptr;  // N, 1-based
+  T* tau = nullptr;
+  int64_t k = 0;
+  int nsteps = 0;
+  T* T_ = nullptr;  // k x (N - k), ld = k
+};
+
+template <typename T>
+void maxdet_dev(lra_ctx* ctx, const lra_opts& o, Fact<T>& F);
+
+template <typename T>
+Fact<T> sketchfact_dev(lra_ctx* ctx, const lra_opts& o, char trans, int64_t M, int64_t N, const T* A,
+                       int64_t lda, RandSrc& rs, int dtype) {
+  const bool adaptive = o.sketchfact_adap || o.rank < 0;
+  int64_t nt = adaptive ? o.nb : o.rank;
+  Fact<T> F;
+  F.N = N;
+  // the byte slices of op(A) for the tensor-core sketch outlive the steps
+  TcSplit split;
+  if (use_tc(o, dtype) && tc_sketch_supported(1, M, N) && M > 0 && N > 0) {
+    Stage st(ctx, 0);
+    tc_split<T>(ctx, trans, M, N, A, lda, dtype == LRA_F64 ? 6 : 3, &split);
+  }
+  const ArenaMark base = ctx->arena.mark();
+  for (int step = 0;; ++step) {
+    if (step > 62) fail(LRA_EINVAL, "adaptive sketch did not terminate");
+    const int64_t order = samp(o, nt);
+    if (order < 0) fail(LRA_EINVAL, "sketch order %lld", (long long)order);
+    const int64_t l = std::min(order, N);
+    const int64_t kmax = (o.rank < 0 || o.rank > l) ? l : o.rank;
+    F.order = order;
+    F.ld = std::max<int64_t>(order, 1);
+    F.B = ctx->arena.alloc_n<T>((size_t)F.ld * std::max<int64_t>(N, 1));
+    F.jpvt = ctx->arena.alloc_n<int64_t>(std::max<int64_t>(N, 1));
+    F.tau = ctx->arena.alloc_n<T>(std::max<int64_t>(l, 1));
+    {
+      Stage st(ctx, 0);
+      make_sketch<T>(ctx, o, trans, M, N, A, lda, order, rs, F.B, dtype, split.ns ? &split : nullptr);
+    }
+    {
+      Stage st(ctx, 1);
+      F.k = geqp3_adap<T>(ctx, order, N, F.B, F.ld, F.jpvt, F.tau, kmax, o.nb, o.atol, o.rtol, true);
+    }
+    F.nsteps = step + 1;
+    if (!adaptive || F.k < nt) break;
+    nt *= 2;
+    ctx->arena.release(base);
+  }
+  return F;
+}
+
+template <typename T>
+void postproc_t(lra_ctx* ctx, const lra_opts& o, Fact<T>& F, bool want_t) {
+  const bool maxdet = F.k > 0 && F.k < F.N && o.maxdet_tol >= 0;
+  if (!(want_t || maxdet)) return;
+  Stage st(ctx, 2);
+  const int64_t k = F.k, nr = F.N - k;
+  F.T_ = ctx->arena.alloc_n<T>((size_t)std::max<int64_t>(k, 1) * std::max<int64_t>(nr, 1));
+  if (k > 0 && nr > 0) {
+    copy_matrix(ctx, k, nr, F.B + k * F.ld, F.ld, F.T_, k);
+    trsm_upper(ctx, k, nr, F.B, F.ld, F.T_, k);
+  }
+  if (maxdet) maxdet_dev<T>(ctx, o, F);
+}
+
+// pqrfact_backend! on a dense device matrix (M x N, ld), in place
+template <typename T>
+Fact<T> pqr_backend_dev(lra_ctx* ctx, const lra_opts& o, T* B, int64_t M, int64_t N, int64_t ld) {
+  Fact<T> F;
+  F.B = B;
+  F.ld = ld;
+  F.order = M;
+  F.N = N;
+  const int64_t l = std::min(M, N);
+  const int64_t kmax = (o.rank < 0 || o.rank > l) ? l : o.rank;
+  F.jpvt = ctx->arena.alloc_n<int64_t>(std::max<int64_t>(N, 1));
+  F.tau = ctx->arena.alloc_n<T>(std::max<int64_t>(l, 1));
+  Stage st(ctx, 1);
+  F.k = geqp3_adap<T>(ctx, M, N, B, ld, F.jpvt, F.tau, kmax, o.nb, o.atol, o.rtol, true);
+  F.nsteps = 0;
+  return F;
+}
+
+// op(A) as a dense device copy (M x N, ld = M)
+template <typename T>
+T* dense_op(lra_ctx* ctx, char trans, int64_t m, int64_t n, const DMat<T>& A) {
+  const int64_t M = trans == 'n' ? m : n, N = trans == 'n' ? n : m;
+  T* B = ctx->arena.alloc_n<T>((size_t)std::max<int64_t>(M, 1) * std::max<int64_t>(N, 1));
+  if (trans == 'n')
+    copy_matrix(ctx, m, n, A.p, A.ld, B, M);
+  else
+    transpose(ctx, m, n, A.p, A.ld, B, M);
+  return B;
+}
+
+// the sketch or the full matrix, factored, with T when requested
+template <typename T>
+Fact<T> id_core(lra_ctx* ctx, const lra_opts& o, char trans, int64_t m, int64_t n, const DMat<T>& A,
+                RandSrc& rs, int dtype, bool want_t) {
+  const int64_t M = trans == 'n' ? m : n, N = trans == 'n' ? n : m;
+  Fact<T> F;
+  if (o.sketch == LRA_SKETCH_NONE) {
+    T* B = dense_op(ctx, trans, m, n, A);
+    F = pqr_backend_dev<T>(ctx, o, B, M, N, M);
+  } else {
+    F = sketchfact_dev<T>(ctx, o, trans, M, N, A.p, A.ld, rs, dtype);
+  }
+  postproc_t<T>(ctx, o, F, want_t);
+  return F;
+}
+
+// getcols(trans, A, idx): M x k device matrix
+template <typename T>
+T* getcols(lra_ctx* ctx, char trans, int64_t m, int64_t n, const DMat<T>& A, const int64_t* idx, int64_t k) {
+  const int64_t M = trans == 'n' ? m : n;
+  T* C = ctx->arena.alloc_n<T>((size_t)std::max<int64_t>(M, 1) * std::max<int64_t>(k, 1));
+  if (trans == 'n') {
+    gather_cols(ctx, m, k, A.p, A.ld, idx, C, M);
+  } else {
+    T* Rw = ctx->arena.alloc_n<T>((size_t)std::max<int64_t>(k, 1) * std::max<int64_t>(n, 1));
+    gather_rows(ctx, k, n, A.p, A.ld, idx, Rw, k);
+    transpose(ctx, k, n, Rw, k, C, M);
+  }
+  return C;
+}
+
+}  // namespace
+
+// One step of maxdet_swapcols! (src/pqr.jl:445-476) on the device: find
+// max |T| (ties: last index, findmaxabs, src/util.jl:13-23); when it is
+// above `bound` and `update` is set, swap p and apply maxdet_update!
+// (src/pqr.jl:479-501, T part).  Returns whether max |T| > bound.
+template <typename T>
+bool maxdet_step(lra_ctx* ctx, int64_t k, int64_t nr, T* Tm, int64_t* jpvt, double bound, bool update);
+
+namespace {
+
+// strong rank-revealing swaps on T and p (the ID path: no R factor)
+template <typename T>
+void maxdet_dev(lra_ctx* ctx, const lra_opts& o, Fact<T>& F) {
+  if (o.pqrfact_retval & (LRA_RET_R | LRA_RET_Q))
+    fail(LRA_ENOTSUP, "maxdet_tol >= 0 together with a Q or R factor is not supported");
+  const int64_t k = F.k, nr = F.N - k;
+  const int64_t cap = 64 * (k + nr) + 1000;  // the determinant grows every swap
+  int64_t niter = 0;
+  while (niter < cap) {
+    const bool upd = niter != o.maxdet_niter;
+    if (!maxdet_step<T>(ctx, k, nr, F.T_, F.jpvt, 1.0 + o.maxdet_tol, upd)) break;
+    if (!upd) break;
+    ++niter;
+  }
+}
+
+}  // namespace
+
+}  // namespace lra
+
+using namespace lra;
+
+// ======================================================================================
+// C ABI
+// ======================================================================================
+
+namespace {
+
+template <class Fn>
+int guarded(lra_ctx* ctx, Fn&& fn) {
+  if (!ctx) return LRA_EINVAL;
+  try {
+    LRA_CUDA(cudaSetDevice(ctx->device));
+    ctx->arena.reset(ctx->stream);
+    for (double& s : ctx->stage_ms) s = 0;
+    fn();
+    LRA_CUDA(cudaStreamSynchronize(ctx->stream));
+    ctx->last_error.clear();
+    return LRA_OK;
+  } catch (const lra::Error& e) {
+    ctx->last_error = e.msg;
+    cudaStreamSynchronize(ctx->stream);
+    cudaGetLastError();
+    return e.status;
+  } catch (const std::bad_alloc&) {
+    ctx->last_error = "host allocation failed";
+    return LRA_ENOMEM;
+  } catch (...) {
+    ctx->last_error = "unexpected exception";
+    return LRA_ECUDA;
+  }
+}
+
+template <class Fn>
+void dispatch(int dtype, Fn&& fn) {
+  if (dtype == LRA_F64)
+    fn(double(0));
+  else if (dtype == LRA_F32)
+    fn(float(0));
+  else
+    fail(LRA_EINVAL, "dtype");
+}
+
+template <typename T>
+void check_input(lra_ctx* ctx, const lra_opts& o, int64_t m, int64_t n, const DMat<T>& A) {
+  if (o.check_finite && !all_finite(ctx, m, n, A.p, A.ld)) fail(LRA_ENONFINITE, "input has NaN or Inf entries");
+}
+
+void check_dims(int64_t m, int64_t n) {
+  if (m < 0 || n < 0) fail(LRA_EDIM, "negative dimension");
+}
+
+template <typename T>
+lra_id* pack_id(lra_ctx* ctx, const Fact<T>& F, int dtype) {
+  lra_id* r = static_cast<lra_id*>(hmalloc(sizeof(lra_id)));
+  std::memset(r, 0, sizeof *r);
+  r->dtype = dtype;
+  r->nsteps = F.nsteps;
+  r->k = F.k;
+  r->n = F.N;
+  r->sk = static_cast<int64_t*>(hmalloc(sizeof(int64_t) * std::max<int64_t>(F.k, 1)));
+  r->rd = static_cast<int64_t*>(hmalloc(sizeof(int64_t) * std::max<int64_t>(F.N - F.k, 1)));
+  r->T = hmalloc(sizeof(T) * std::max<int64_t>(F.k * (F.N - F.k), 1));
+  to_host(ctx, r->sk, F.jpvt, F.k);
+  to_host(ctx, r->rd, F.jpvt + F.k, F.N - F.k);
+  if (F.k > 0 && F.N > F.k) to_host(ctx, r->T, F.T_, (size_t)F.k * (F.N - F.k));
+  LRA_CUDA(cudaStreamSynchronize(ctx->stream));
+  return r;
+}
+
+}  // namespace
+
+extern "C" {
+
+const char* lra_status_string(int s) {
+  switch (s) {
+    case LRA_OK: return "ok";
+    case LRA_EINVAL: return "invalid argument";
+    case LRA_EDIM: return "dimension mismatch";
+    case LRA_ENOMEM: return "out of memory";
+    case LRA_ETIMEDOUT: return "device wait timed out";
+    case LRA_ENONFINITE: return "non-finite input";
+    case LRA_ECUDA: return "CUDA error";
+    case LRA_ERAND: return "random stream exhausted";
+    case LRA_ENOTSUP: return "not supported";
+    case LRA_ENOTHERM: return "matrix must be Hermitian";
+    case LRA_EBUSY: return "busy";
+    default: return "unknown status";
+  }
+}
+
+int lra_ctx_create(int device, lra_ctx** out) {
+  if (!out) return LRA_EINVAL;
+  *out = nullptr;
+  int count = 0;
+  if (cudaGetDeviceCount(&count) != cudaSuccess || count == 0) {
+    cudaGetLastError();
+    return LRA_ECUDA;
+  }
+  if (device < 0 || device >= count) return LRA_EINVAL;
+  lra_ctx* c = new (std::nothrow) lra_ctx();
+  if (!c) return LRA_ENOMEM;
+  c->device = device;
+  if (cudaSetDevice(device) != cudaSuccess ||
+      cudaDeviceGetAttribute(&c->num_sms, cudaDevAttrMultiProcessorCount, device) != cudaSuccess ||
+      cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess) {
+    cudaGetLastError();
+    delete c;
+    return LRA_ECUDA;
+  }
+  c->own_stream = true;
+  *out = c;
+  return LRA_OK;
+}
+
+void lra_ctx_destroy(lra_ctx* ctx) {
+  if (!ctx) return;
+  cudaSetDevice(ctx->device);
+  cudaStreamSynchronize(ctx->stream);
+  if (ctx->pinned) cudaFreeHost(ctx->pinned);
+  if (ctx->own_stream) cudaStreamDestroy(ctx->stream);
+  delete ctx;
+}
+
+int lra_ctx_set_stream(lra_ctx* ctx, void* stream) {
+  if (!ctx) return LRA_EINVAL;
+  cudaStreamSynchronize(ctx->stream);
+  if (ctx->own_stream) cudaStreamDestroy(ctx->stream);
+  ctx->stream = static_cast<cudaStream_t>(stream);
+  ctx->own_stream = false;
+  return LRA_OK;
+}
+
+const char* lra_last_error(const lra_ctx* ctx) { return ctx ? ctx->last_error.c_str() : "no context"; }
+
+int64_t lra_ctx_launches(const lra_ctx* ctx) { return ctx ? ctx->launches : 0; }
+
+int lra_ctx_stage_ms(const lra_ctx* ctx, double out[4]) {
+  if (!ctx || !out) return LRA_EINVAL;
+  for (int i = 0; i < 4; ++i) out[i] = ctx->stage_ms[i];
+  return LRA_OK;
+}
+
+int lra_opts_init(lra_opts* o, int dtype) {
+  if (!o) return LRA_EINVAL;
+  if (dtype != LRA_F32 && dtype != LRA_F64) return LRA_EINVAL;
+  std::memset(o, 0, sizeof *o);
+  const double eps = dtype == LRA_F64 ? 2.220446049250313e-16 : 1.1920928955078125e-07;
+  o->atol = 0;
+  o->maxdet_niter = -1;
+  o->maxdet_tol = -1;
+  o->nb = 32;
+  o->pheig_orthtol = std::sqrt(eps);
+  o->pqrfact_retval = LRA_RET_Q | LRA_RET_R;
+  o->rank = -1;
+  o->rtol = 5 * eps;
+  o->sketch = LRA_SKETCH_RANDN;
+  o->sketch_randn_niter = 0;
+  o->sketchfact_adap = 1;
+  o->verb = 1;
+  o->sketchfact_randn_samp[0] = 1;
+  o->sketchfact_randn_samp[1] = 8;
+  o->sketchfact_srft_samp[0] = 1;
+  o->sketchfact_srft_samp[1] = 8;
+  o->sketchfact_sub_samp[0] = 4;
+  o->sketchfact_sub_samp[1] = 8;
+  o->snorm_niter = 32;
+  o->precision = LRA_PREC_NATIVE;
+  o->check_finite = 1;
+  o->seed = 0x4c5241ull;
+  return LRA_OK;
+}
+
+int lra_chkopts(const lra_opts* o) {
+  try {
+    chkopts(o);
+    return LRA_OK;
+  } catch (const lra::Error& e) {
+    return e.status;
+  }
+}
+
+int lra_sketch(lra_ctx* ctx, int dtype, char side, char trans, int64_t m, int64_t n, const void* A, int64_t lda,
+               int64_t order, const lra_opts* opts, const lra_rand* rand, void* B, int64_t ldb) {
+  return guarded(ctx, [&] {
+    chkopts(opts);
+    check_dims(m, n);
+    if (order < 0) fail(LRA_EINVAL, "order");
+    const char t = chktrans(trans);
+    if (side != 'l' && side != 'r' && side != 'L' && side != 'R') fail(LRA_EINVAL, "side");
+    lra_opts o = *opts;
+    if (o.sketch == LRA_SKETCH_NONE) o.sketch = LRA_SKETCH_RANDN;  // src/sketch.jl:68-74
+    dispatch(dtype, [&](auto z) {
+      using T = decltype(z);
+      DMat<T> dA = stage_in<T>(ctx, A, m, n, lda);
+      check_input(ctx, o, m, n, dA);
+      RandSrc rs(ctx, rand, o.seed);
+      // right sketches A S are the transposes of left sketches S^T A^T
+      const bool left = side == 'l' || side == 'L';
+      const char tt = left ? t : (t == 'n' ? 'c' : 'n');
+      const int64_t M = tt == 'n' ? m : n, N = tt == 'n' ? n : m;
+      T* Bd = ctx->arena.alloc_n<T>((size_t)std::max<int64_t>(order, 1) * std::max<int64_t>(N, 1));
+      make_sketch<T>(ctx, o, tt, M, N, dA.p, dA.ld, order, rs, Bd, dtype, nullptr, !left);
+      const int64_t rows = left ? order : N, cols = left ? N : order;
+      if (ldb < std::max<int64_t>(rows, 1)) fail(LRA_EDIM, "ldb");
+      T* src = Bd;
+      if (!left) {
+        src = ctx->arena.alloc_n<T>((size_t)std::max<int64_t>(rows * cols, 1));
+        transpose(ctx, order, N, Bd, std::max<int64_t>(order, 1), src, std::max<int64_t>(rows, 1));
+      }
+      if (rows > 0 && cols > 0)
+        LRA_CUDA(cudaMemcpy2DAsync(B, ldb * sizeof(T), src, rows * sizeof(T), rows * sizeof(T), cols,
+                                   is_dev(B) ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost, ctx->stream));
+    });
+  });
+}
+
+int lra_geqp3_adap(lra_ctx* ctx, int dtype, int64_t m, int64_t n, void* B, int64_t ldb, int64_t* jpvt, void* tau,
+                   const lra_opts* opts, int64_t* k) {
+  return guarded(ctx, [&] {
+    chkopts(opts);
+    check_dims(m, n);
+    if (!k) fail(LRA_EINVAL, "k is NULL");
+    if (m > 0 && n > 0 && (!is_dev(B) || !is_dev(jpvt) || !is_dev(tau)))
+      fail(LRA_EINVAL, "lra_geqp3_adap works on device buffers");
+    if (ldb < std::max<int64_t>(1, m)) fail(LRA_EDIM, "ldb");
+    dispatch(dtype, [&](auto z) {
+      using T = decltype(z);
+      const int64_t l = std::min(m, n);
+      const int64_t kmax = (opts->rank < 0 || opts->rank > l) ? l : opts->rank;
+      *k = geqp3_adap<T>(ctx, m, n, static_cast<T*>(B), ldb, jpvt, static_cast<T*>(tau), kmax, opts->nb,
+                         opts->atol, opts->rtol, true);
+    });
+  });
+}
+
+int lra_idfact(lra_ctx* ctx, int dtype, char trans, int64_t m, int64_t n, const void* A, int64_t lda,
+               const lra_opts* opts, const lra_rand* rand, lra_id** out) {
+  if (out) *out = nullptr;
+  return guarded(ctx, [&] {
+    chkopts(opts);
+    check_dims(m, n);
+    if (!out) fail(LRA_EINVAL, "out is NULL");
+    const char t = chktrans(trans);
+    lra_opts o = *opts;
+    o.pqrfact_retval = LRA_RET_T;  // src/id.jl:437
+    dispatch(dtype, [&](auto z) {
+      using T = decltype(z);
+      DMat<T> dA = stage_in<T>(ctx, A, m, n, lda);
+      check_input(ctx, o, m, n, dA);
+      RandSrc rs(ctx, rand, o.seed);
+      Fact<T> F = id_core<T>(ctx, o, t, m, n, dA, rs, dtype, true);
+      *out = pack_id<T>(ctx, F, dtype);
+    });
+  });
+}
+
+int lra_sketchfact(lra_ctx* ctx, int dtype, char side, char trans, int64_t m, int64_t n, const void* A,
+                   int64_t lda, const lra_opts* opts, const lra_rand* rand, lra_pqr** out) {
+  if (out) *out = nullptr;
+  return guarded(ctx, [&] {
+    chkopts(opts);
+    check_dims(m, n);
+    if (!out) fail(LRA_EINVAL, "out is NULL");
+    const char t = chktrans(trans);
+    if (side != 'l' && side != 'L') fail(LRA_ENOTSUP, "sketchfact: only side = :left is built");
+    lra_opts o = *opts;
+    if (o.sketch == LRA_SKETCH_NONE) o.sketch = LRA_SKETCH_RANDN;
+    dispatch(dtype, [&](auto z) {
+      using T = decltype(z);
+      DMat<T> dA = stage_in<T>(ctx, A, m, n, lda);
+      check_input(ctx, o, m, n, dA);
+      RandSrc rs(ctx, rand, o.seed);
+      const int64_t M = t == 'n' ? m : n, N = t == 'n' ? n : m;
+      Fact<T> F = sketchfact_dev<T>(ctx, o, t, M, N, dA.p, dA.ld, rs, dtype);
+      const bool rq = o.pqrfact_retval & LRA_RET_Q, rr = o.pqrfact_retval & LRA_RET_R,
+                 rt = o.pqrfact_retval & LRA_RET_T;
+      postproc_t<T>(ctx, o, F, rt);
+      lra_pqr* r = static_cast<lra_pqr*>(hmalloc(sizeof(lra_pqr)));
+      std::memset(r, 0, sizeof *r);
+      r->dtype = dtype;
+      r->m = F.order;
+      r->n = N;
+      r->k = F.k;
+      r->p = static_cast<int64_t*>(hmalloc(sizeof(int64_t) * std::max<int64_t>(N, 1)));
+      to_host(ctx, r->p, F.jpvt, N);
+      const int64_t k = F.k;
+      if (rr) {
+        T* R = ctx->arena.alloc_n<T>((size_t)std::max<int64_t>(k * N, 1));
+        copy_matrix(ctx, k, N, F.B, F.ld, R, std::max<int64_t>(k, 1));
+        zero_lower(ctx, k, N, R, std::max<int64_t>(k, 1));
+        r->R = hmalloc(sizeof(T) * std::max<int64_t>(k * N, 1));
+        to_host(ctx, r->R, R, (size_t)k * N);
+        r->retval |= LRA_RET_R;
+      }
+      if (rt) {
+        r->T = hmalloc(sizeof(T) * std::max<int64_t>(k * (N - k), 1));
+        if (k > 0 && N > k) to_host(ctx, r->T, F.T_, (size_t)k * (N - k));
+        r->retval |= LRA_RET_T;
+      }
+      if (rq) {
+        orgqr(ctx, F.order, k, F.B, F.ld, F.tau);
+        r->Q = hmalloc(sizeof(T) * std::max<int64_t>(F.order * k, 1));
+        if (k > 0)
+          LRA_CUDA(cudaMemcpy2DAsync(r->Q, F.order * sizeof(T), F.B, F.ld * sizeof(T), F.order * sizeof(T), k,
+                                     cudaMemcpyDeviceToHost, ctx->stream));
+        r->retval |= LRA_RET_Q;
+      }
+      LRA_CUDA(cudaStreamSynchronize(ctx->stream));
+      *out = r;
+    });
+  });
+}
+
+int lra_pqrfact(lra_ctx* ctx, int dtype, char trans, int64_t m, int64_t n, const void* A, int64_t lda,
+                const lra_opts* opts, const lra_rand* rand, lra_pqr** out) {
+  if (out) *out = nullptr;
+  return guarded(ctx, [&] {
+    chkopts(opts);
+    check_dims(m, n);
+    if (!out) fail(LRA_EINVAL, "out is NULL");
+    const char t = chktrans(trans);
+    const lra_opts& o = *opts;
+    dispatch(dtype, [&](auto z) {
+      using T = decltype(z);
+      DMat<T> dA = stage_in<T>(ctx, A, m, n, lda);
+      check_input(ctx, o, m, n, dA);
+      RandSrc rs(ctx, rand, o.seed);
+      const int64_t M = t == 'n' ? m : n, N = t == 'n' ? n : m;
+      const bool rq = o.pqrfact_retval & LRA_RET_Q, rr = o.pqrfact_retval & LRA_RET_R,
+                 rt = o.pqrfact_retval & LRA_RET_T;
+      lra_pqr* r = static_cast<lra_pqr*>(hmalloc(sizeof(lra_pqr)));
+      std::memset(r, 0, sizeof *r);
+      r->dtype = dtype;
+      r->m = M;
+      r->n = N;
+      r->p = static_cast<int64_t*>(hmalloc(sizeof(int64_t) * std::max<int64_t>(N, 1)));
+      try {
+        T* Qd = nullptr;  // M x k, ld = M
+        T* R11 = nullptr;  // k x k upper, ld = k
+        Fact<T> F;
+        if (o.sketch == LRA_SKETCH_NONE) {
+          // pqrfact_none (src/pqr.jl:323-327): pivoted QR of op(A) itself
+          lra_opts oo = o;
+          T* B = dense_op(ctx, t, m, n, dA);
+          F = pqr_backend_dev<T>(ctx, oo, B, M, N, M);
+          postproc_t<T>(ctx, oo, F, rt || rr);
+          const int64_t k = F.k;
+          R11 = ctx->arena.alloc_n<T>((size_t)std::max<int64_t>(k * k, 1));
+          copy_matrix(ctx, k, k, F.B, F.ld, R11, std::max<int64_t>(k, 1));
+          if (rq) {
+            orgqr(ctx, M, k, F.B, F.ld, F.tau);
+            Qd = F.B;
+          }
+        } else {
+          lra_opts oi = o;
+          oi.pqrfact_retval = LRA_RET_T;
+          F = id_core<T>(ctx, oi, t, m, n, dA, rs, dtype, true);
+          const int64_t k = F.k;
+          T* Ask = getcols<T>(ctx, t, m, n, dA, F.jpvt, k);
+          int64_t* jp = ctx->arena.alloc_n<int64_t>(std::max<int64_t>(k, 1));
+          T* tau = ctx->arena.alloc_n<T>(std::max<int64_t>(k, 1));
+          {
+            Stage st(ctx, 3);
+            geqp3_adap<T>(ctx, M, k, Ask, std::max<int64_t>(M, 1), jp, tau, k, 32, -1.0, 0.0, false);
+          }
+          R11 = ctx->arena.alloc_n<T>((size_t)std::max<int64_t>(k * k, 1));
+          copy_matrix(ctx, k, k, Ask, std::max<int64_t>(M, 1), R11, std::max<int64_t>(k, 1));
+          if (rq) {
+            orgqr(ctx, M, k, Ask, std::max<int64_t>(M, 1), tau);
+            Qd = Ask;
+          }
+        }
+        const int64_t k = F.k;
+        r->k = k;
+        zero_lower(ctx, k, k, R11, std::max<int64_t>(k, 1));
+        to_host(ctx, r->p, F.jpvt, N);
+        if (rq) {
+          r->Q = hmalloc(sizeof(T) * std::max<int64_t>(M * k, 1));
+          if (k > 0 && M > 0)
+            LRA_CUDA(cudaMemcpy2DAsync(r->Q, M * sizeof(T), Qd, (o.sketch == LRA_SKETCH_NONE ? F.ld : M) * sizeof(T),
+                                       M * sizeof(T), k, cudaMemcpyDeviceToHost, ctx->stream));
+          r->retval |= LRA_RET_Q;
+        }
+        if (rr) {
+          // R = [R11 | R11 T] (pqrr, src/pqr.jl:330-340)
+          T* R = ctx->arena.alloc_n<T>((size_t)std::max<int64_t>(k * N, 1));
+          copy_matrix(ctx, k, k, R11, std::max<int64_t>(k, 1), R, std::max<int64_t>(k, 1));
+          if (k > 0 && N > k)
+            gemm<T>(ctx, 'n', 'n', k, N - k, k, T(1), R11, k, F.T_, k, T(0), R + k * k, k);
+          r->R = hmalloc(sizeof(T) * std::max<int64_t>(k * N, 1));
+          to_host(ctx, r->R, R, (size_t)k * N);
+          r->retval |= LRA_RET_R;
+        }
+        if (rt) {
+          r->T = hmalloc(sizeof(T) * std::max<int64_t>(k * (N - k), 1));
+          if (k > 0 && N > k) to_host(ctx, r->T, F.T_, (size_t)k * (N - k));
+          r->retval |= LRA_RET_T;
+        }
+        LRA_CUDA(cudaStreamSynchronize(ctx->stream));
+      } catch (...) {
+        lra_pqr_free(r);
+        throw;
+      }
+      *out = r;
+    });
+  });
+}
+
+}  // extern "C"
+
+// ======================================================================================
+// post-processed factorizations: psvd, pheig, cur; norms; batches
+// ======================================================================================
+
+namespace lra {
+namespace {
+
+// SVD of the k x N device matrix W (k <= N): W = U diag(S) Vt with U k x k,
+// S descending, V (N x k) returned as the Householder reflectors of W^T
+// (Q2, tau2) plus V' (k x k) so that Vfull = Q2 [V'; 0].
+template <typename T>
+struct SmallSvd {
+  T* U;     // k x k
+  T* S;     // k (device)
+  T* Vp;    // k x k
+  T* Q2;    // N x k reflectors
+  T* tau2;  // k
+  std::vector<T> hS;
+};
+
+template <typename T>
+SmallSvd<T> svd_wide(lra_ctx* ctx, int64_t k, int64_t N, const T* W, int64_t ldw) {
+  SmallSvd<T> r;
+  r.Q2 = ctx->arena.alloc_n<T>((size_t)std::max<int64_t>(N * k, 1));
+  transpose(ctx, k, N, W, ldw, r.Q2, std::max<int64_t>(N, 1));
+  int64_t* jp = ctx->arena.alloc_n<int64_t>(std::max<int64_t>(k, 1));
+  r.tau2 = ctx->arena.alloc_n<T>(std::max<int64_t>(k, 1));
+  geqp3_adap<T>(ctx, N, k, r.Q2, std::max<int64_t>(N, 1), jp, r.tau2, k, 32, -1.0, 0.0, false);
+  // X = R2^T (k x k)
+  T* R2 = ctx->arena.alloc_n<T>((size_t)std::max<int64_t>(k * k, 1));
+  copy_matrix(ctx, k, k, r.Q2, std::max<int64_t>(N, 1), R2, std::max<int64_t>(k, 1));
+  zero_lower(ctx, k, k, R2, std::max<int64_t>(k, 1));
+  r.U = ctx->arena.alloc_n<T>((size_t)std::max<int64_t>(k * k, 1));
+  transpose(ctx, k, k, R2, std::max<int64_t>(k, 1), r.U, std::max<int64_t>(k, 1));
+  r.Vp = ctx->arena.alloc_n<T>((size_t)std::max<int64_t>(k * k, 1));
+  r.S = ctx->arena.alloc_n<T>(std::max<int64_t>(k, 1));
+  jacobi_svd<T>(ctx, k, r.U, std::max<int64_t>(k, 1), r.Vp, std::max<int64_t>(k, 1), r.S);
+  div_cols(ctx, k, k, r.U, std::max<int64_t>(k, 1), r.S);
+  // sort descending (gesdd order) and permute U, V' columns
+  r.hS.resize(k);
+  to_host(ctx, r.hS.data(), r.S, k);
+  LRA_CUDA(cudaStreamSynchronize(ctx->stream));
+  std::vector<int64_t> ord(k);
+  std::iota(ord.begin(), ord.end(), 0);
+  std::stable_sort(ord.begin(), ord.end(), [&](int64_t a, int64_t b) { return r.hS[a] > r.hS[b]; });
+  bool sorted = true;
+  for (int64_t i = 0; i < k; ++i) sorted &= ord[i] == i;
+  if (!sorted && k > 0) {
+    std::vector<int64_t> ord1(k);
+    std::vector<T> s2(k);
+    for (int64_t i = 0; i < k; ++i) {
+      ord1[i] = ord[i] + 1;
+      s2[i] = r.hS[ord[i]];
+    }
+    r.hS = s2;
+    int64_t* dord = ctx->arena.alloc_n<int64_t>(k);
+    LRA_CUDA(cudaMemcpyAsync(dord, ord1.data(), k * sizeof(int64_t), cudaMemcpyHostToDevice, ctx->stream));
+    T* tmp = ctx->arena.alloc_n<T>((size_t)k * k);
+    gather_cols(ctx, k, k, r.U, k, dord, tmp, k);
+    copy_matrix(ctx, k, k, tmp, k, r.U, k);
+    gather_cols(ctx, k, k, r.Vp, k, dord, tmp, k);
+    copy_matrix(ctx, k, k, tmp, k, r.Vp, k);
+    LRA_CUDA(cudaMemcpyAsync(r.S, r.hS.data(), k * sizeof(T), cudaMemcpyHostToDevice, ctx->stream));
+    LRA_CUDA(cudaStreamSynchronize(ctx->stream));
+  }
+  return r;
+}
+
+int64_t psvdrank(const std::vector<double>& s, const lra_opts& o) {
+  const int64_t k = (int64_t)s.size();
+  if (k == 0) return 0;
+  const double ptol = std::max(o.atol, o.rtol * s[0]);
+  for (int64_t i = 1; i < k; ++i)
+    if (s[i] <= ptol) return i;
+  return k;
+}
+
+// psvdfact for op(A) tall-or-square (M >= N in the reference's branch)
+template <typename T>
+lra_psvd* psvd_dev(lra_ctx* ctx, const lra_opts& o, char trans, int64_t m, int64_t n, const DMat<T>& dA,
+                   RandSrc& rs, int dtype, bool vals_only) {
+  const int64_t M = trans == 'n' ? m : n, N = trans == 'n' ? n : m;
+  lra_opts oi = o;
+  oi.pqrfact_retval = LRA_RET_T;
+  Fact<T> F = id_core<T>(ctx, oi, trans, m, n, dA, rs, dtype, true);
+  const int64_t k = F.k;
+  Stage st(ctx, 3);
+  // Q, R = qr(A[:, sk])
+  T* Ask = getcols<T>(ctx, trans, m, n, dA, F.jpvt, k);
+  const int64_t ldq = std::max<int64_t>(M, 1);
+  int64_t* jp = ctx->arena.alloc_n<int64_t>(std::max<int64_t>(k, 1));
+  T* tau = ctx->arena.alloc_n<T>(std::max<int64_t>(k, 1));
+  geqp3_adap<T>(ctx, M, k, Ask, ldq, jp, tau, k, 32, -1.0, 0.0, false);
+  const int64_t ldk = std::max<int64_t>(k, 1);
+  T* R = ctx->arena.alloc_n<T>((size_t)ldk * ldk);
+  copy_matrix(ctx, k, k, Ask, ldq, R, ldk);
+  zero_lower(ctx, k, k, R, ldk);
+  // W = R V = [R | R T] P^T  (k x N)
+  T* Wp = ctx->arena.alloc_n<T>((size_t)ldk * std::max<int64_t>(N, 1));
+  copy_matrix(ctx, k, k, R, ldk, Wp, ldk);
+  if (k > 0 && N > k) gemm<T>(ctx, 'n', 'n', k, N - k, k, T(1), R, ldk, F.T_, ldk, T(0), Wp + k * ldk, ldk);
+  T* W = ctx->arena.alloc_n<T>((size_t)ldk * std::max<int64_t>(N, 1));
+  scatter_cols(ctx, k, N, Wp, ldk, F.jpvt, W, ldk);
+  SmallSvd<T> sv = svd_wide<T>(ctx, k, N, W, ldk);
+  std::vector<double> sd(sv.hS.begin(), sv.hS.end());
+  const int64_t kk = psvdrank(sd, o);
+  lra_psvd* r = static_cast<lra_psvd*>(hmalloc(sizeof(lra_psvd)));
+  std::memset(r, 0, sizeof *r);
+  r->dtype = dtype;
+  r->k = kk;
+  r->S = hmalloc(sizeof(T) * std::max<int64_t>(kk, 1));
+  std::memcpy(r->S, sv.hS.data(), sizeof(T) * kk);
+  if (vals_only) return r;
+  // U = Q [U~(:, 1:kk); 0]  (M x kk)
+  T* U = ctx->arena.alloc_n<T>((size_t)ldq * std::max<int64_t>(kk, 1));
+  set_zero(ctx, U, ldq * std::max<int64_t>(kk, 1));
+  copy_matrix(ctx, k, kk, sv.U, ldk, U, ldq);
+  apply_q<T>(ctx, 'n', M, k, Ask, ldq, tau, U, ldq, kk);
+  // V~ = Q2 [V'(:, 1:kk); 0]  (N x kk); Vt = V~^T
+  const int64_t ldn = std::max<int64_t>(N, 1);
+  T* Vf = ctx->arena.alloc_n<T>((size_t)ldn * std::max<int64_t>(kk, 1));
+  set_zero(ctx, Vf, ldn * std::max<int64_t>(kk, 1));
+  copy_matrix(ctx, k, kk, sv.Vp, ldk, Vf, ldn);
+  apply_q<T>(ctx, 'n', N, k, sv.Q2, ldn, sv.tau2, Vf, ldn, kk);
+  r->U = hmalloc(sizeof(T) * std::max<int64_t>(M * kk, 1));
+  r->Vt = hmalloc(sizeof(T) * std::max<int64_t>(kk * N, 1));
+  T* Vt = ctx->arena.alloc_n<T>((size_t)std::max<int64_t>(kk * N, 1));
+  transpose(ctx, N, kk, Vf, ldn, Vt, std::max<int64_t>(kk, 1));
+  to_host(ctx, r->U, U, (size_t)M * kk);
+  to_host(ctx, r->Vt, Vt, (size_t)kk * N);
+  LRA_CUDA(cudaStreamSynchronize(ctx->stream));
+  return r;
+}
+
+// transpose a host matrix (rows x cols, ld = rows) in place into a new buffer
+template <typename T>
+void* host_transpose(const void* src, int64_t rows, int64_t cols) {
+  T* d = static_cast<T*>(hmalloc(sizeof(T) * std::max<int64_t>(rows * cols, 1)));
+  const T* s = static_cast<const T*>(src);
+  for (int64_t j = 0; j < cols; ++j)
+    for (int64_t i = 0; i < rows; ++i) d[j + i * cols] = s[i + j * rows];
+  return d;
+}
+
+std::pair<int64_t, int64_t> pheigrank(const std::vector<double>& w, const lra_opts& o) {
+  const int64_t n = (int64_t)w.size();
+  if (n == 0) return {0, 0};
+  const double wmax = std::max(std::fabs(w[0]), std::fabs(w[n - 1]));
+  // searchsorted(w, 0): first index with w >= 0 .. last index with w <= 0
+  int64_t lo = 0;
+  while (lo < n && w[lo] < 0) ++lo;
+  int64_t hi = lo;
+  while (hi < n && w[hi] <= 0) ++hi;
+  auto rank1 = [&](std::vector<double> v) {
+    int64_t k = (int64_t)v.size();
+    k = o.rank >= 0 ? std::min<int64_t>(o.rank, k) : k;
+    const double ptol = std::max(o.atol, o.rtol * wmax);
+    for (int64_t i = 1; i < k; ++i)
+      if (std::fabs(v[i]) <= ptol) return i;
+    return k;
+  };
+  std::vector<double> neg(w.begin(), w.begin() + lo);
+  std::vector<double> pos(w.rbegin(), w.rbegin() + (n - hi));
+  return {rank1(neg), rank1(pos)};
+}
+
+}  // namespace
+}  // namespace lra
+
+extern "C" {
+
+int lra_psvdfact(lra_ctx* ctx, int dtype, int64_t m, int64_t n, const void* A, int64_t lda, const lra_opts* opts,
+                 const lra_rand* rand, int vals_only, lra_psvd** out) {
+  if (out) *out = nullptr;
+  return guarded(ctx, [&] {
+    chkopts(opts);
+    check_dims(m, n);
+    if (!out) fail(LRA_EINVAL, "out is NULL");
+    dispatch(dtype, [&](auto z) {
+      using T = decltype(z);
+      DMat<T> dA = stage_in<T>(ctx, A, m, n, lda);
+      check_input(ctx, *opts, m, n, dA);
+      RandSrc rs(ctx, rand, opts->seed);
+      if (m >= n) {
+        lra_psvd* r = psvd_dev<T>(ctx, *opts, 'n', m, n, dA, rs, dtype, vals_only != 0);
+        r->m = m;
+        r->n = n;
+        *out = r;
+      } else {
+        // the :c branch (src/psvd.jl:256-270) is the same computation on A':
+        // A' = U2 S Vt2  =>  A = Vt2' S U2'
+        lra_psvd* r = psvd_dev<T>(ctx, *opts, 'c', m, n, dA, rs, dtype, vals_only != 0);
+        if (!vals_only) {
+          void* U = host_transpose<T>(r->Vt, r->k, m);
+          void* Vt = host_transpose<T>(r->U, n, r->k);
+          std::free(r->U);
+          std::free(r->Vt);
+          r->U = U;
+          r->Vt = Vt;
+        }
+        r->m = m;
+        r->n = n;
+        *out = r;
+      }
+    });
+  });
+}
+
+int lra_pheigfact(lra_ctx* ctx, int dtype, int64_t n, const void* A, int64_t lda, const lra_opts* opts,
+                  const lra_rand* rand, int vals_only, lra_pheig** out) {
+  if (out) *out = nullptr;
+  return guarded(ctx, [&] {
+    chkopts(opts);
+    check_dims(n, n);
+    if (!out) fail(LRA_EINVAL, "out is NULL");
+    const lra_opts& o = *opts;
+    dispatch(dtype, [&](auto z) {
+      using T = decltype(z);
+      DMat<T> dA = stage_in<T>(ctx, A, n, n, lda);
+      check_input(ctx, o, n, n, dA);
+      if (!is_symmetric(ctx, n, dA.p, dA.ld)) fail(LRA_ENOTHERM, "matrix must be Hermitian");
+      RandSrc rs(ctx, rand, o.seed);
+      lra_opts oi = o;
+      oi.pqrfact_retval = LRA_RET_T;
+      Fact<T> F = id_core<T>(ctx, oi, 'n', n, n, dA, rs, dtype, true);
+      const int64_t k = F.k, ldk = std::max<int64_t>(k, 1), ldn = std::max<int64_t>(n, 1);
+      Stage st(ctx, 3);
+      // V' = P [I; T'] (n x k) and its QR
+      T* Vt = ctx->arena.alloc_n<T>((size_t)ldn * ldk);
+      set_zero(ctx, Vt, ldn * ldk);
+      T* I = ctx->arena.alloc_n<T>((size_t)ldk * ldk);
+      set_identity(ctx, k, k, I, ldk);
+      scatter_rows(ctx, k, k, I, ldk, F.jpvt, Vt, ldn);
+      if (n > k) {
+        T* Tt = ctx->arena.alloc_n<T>((size_t)(n - k) * ldk);
+        transpose(ctx, k, n - k, F.T_, ldk, Tt, n - k);
+        scatter_rows(ctx, n - k, k, Tt, n - k, F.jpvt + k, Vt, ldn);
+      }
+      int64_t* jp = ctx->arena.alloc_n<int64_t>(ldk);
+      T* tau = ctx->arena.alloc_n<T>(ldk);
+      geqp3_adap<T>(ctx, n, k, Vt, ldn, jp, tau, k, 32, -1.0, 0.0, false);
+      T* R = ctx->arena.alloc_n<T>((size_t)ldk * ldk);
+      copy_matrix(ctx, k, k, Vt, ldn, R, ldk);
+      zero_lower(ctx, k, k, R, ldk);
+      // B = R (A[sk, sk] R')
+      T* Ar = ctx->arena.alloc_n<T>((size_t)ldk * ldn);
+      gather_rows(ctx, k, n, dA.p, dA.ld, F.jpvt, Ar, ldk);
+      T* Ass = ctx->arena.alloc_n<T>((size_t)ldk * ldk);
+      gather_cols(ctx, k, k, Ar, ldk, F.jpvt, Ass, ldk);
+      T* C = ctx->arena.alloc_n<T>((size_t)ldk * ldk);
+      gemm<T>(ctx, 'n', 't', k, k, k, T(1), Ass, ldk, R, ldk, T(0), C, ldk);
+      T* B = ctx->arena.alloc_n<T>((size_t)ldk * ldk);
+      gemm<T>(ctx, 'n', 'n', k, k, k, T(1), R, ldk, C, ldk, T(0), B, ldk);
+      symmetrize(ctx, k, B, ldk);
+      // eigen! through the one-sided Jacobi SVD of the PSD shift B + s I
+      T* cn = ctx->arena.alloc_n<T>(ldk);
+      col_norms(ctx, k, k, B, ldk, cn);
+      std::vector<T> hcn(k);
+      to_host(ctx, hcn.data(), cn, k);
+      LRA_CUDA(cudaStreamSynchronize(ctx->stream));
+      double fro = 0;
+      for (T v : hcn) fro += (double)v * (double)v;
+      const T shift = (T)(std::sqrt(fro) * 1.0001 + (fro == 0 ? 1.0 : 0.0));
+      add_diag(ctx, k, B, ldk, shift);
+      T* Z = ctx->arena.alloc_n<T>((size_t)ldk * ldk);
+      T* S = ctx->arena.alloc_n<T>(ldk);
+      jacobi_svd<T>(ctx, k, B, ldk, Z, ldk, S);
+      std::vector<T> hS(k);
+      to_host(ctx, hS.data(), S, k);
+      LRA_CUDA(cudaStreamSynchronize(ctx->stream));
+      std::vector<double> w(k);
+      for (int64_t i = 0; i < k; ++i) w[i] = (double)hS[i] - (double)shift;
+      std::vector<int64_t> ord(k);
+      std::iota(ord.begin(), ord.end(), 0);
+      std::stable_sort(ord.begin(), ord.end(), [&](int64_t a, int64_t b) { return w[a] < w[b]; });
+      std::vector<double> ws(k);
+      for (int64_t i = 0; i < k; ++i) ws[i] = w[ord[i]];
+      auto kk = pheigrank(ws, o);
+      std::vector<int64_t> sel;
+      if (kk.first + kk.second < k) {
+        for (int64_t i = 0; i < kk.first; ++i) sel.push_back(i);
+        for (int64_t i = k - kk.second; i < k; ++i) sel.push_back(i);
+      } else {
+        for (int64_t i = 0; i < k; ++i) sel.push_back(i);
+      }
+      const int64_t ke = (int64_t)sel.size();
+      lra_pheig* r = static_cast<lra_pheig*>(hmalloc(sizeof(lra_pheig)));
+      std::memset(r, 0, sizeof *r);
+      r->dtype = dtype;
+      r->n = n;
+      r->k = ke;
+      r->values = hmalloc(sizeof(T) * std::max<int64_t>(ke, 1));
+      std::vector<double> vals(ke);
+      for (int64_t i = 0; i < ke; ++i) {
+        vals[i] = ws[sel[i]];
+        static_cast<T*>(r->values)[i] = (T)vals[i];
+      }
+      if (!vals_only && ke > 0) {
+        std::vector<int64_t> cols1(ke);
+        for (int64_t i = 0; i < ke; ++i) cols1[i] = ord[sel[i]] + 1;
+        int64_t* dcols = ctx->arena.alloc_n<int64_t>(ke);
+        LRA_CUDA(cudaMemcpyAsync(dcols, cols1.data(), ke * sizeof(int64_t), cudaMemcpyHostToDevice, ctx->stream));
+        T* Zs = ctx->arena.alloc_n<T>((size_t)ldn * ke);
+        set_zero(ctx, Zs, ldn * ke);
+        gather_cols(ctx, k, ke, Z, ldk, dcols, Zs, ldn);
+        // pheigorth!: re-orthonormalize clusters (src/pheig.jl:342-364)
+        std::vector<int64_t> cl;
+        int64_t a = 0;
+        while (a < ke) {
+          const double va = vals[a];
+          int64_t b = a + 1;
+          while (b < ke) {
+            const double vb = vals[b];
+            if (2 * std::fabs((va - vb) / (va + vb)) > o.pheig_orthtol) break;
+            ++b;
+          }
+          --b;
+          if (b > a) {
+            cl.push_back(a);
+            cl.push_back(b);
+          }
+          a = b + 1;
+        }
+        if (!cl.empty()) {
+          int64_t* dcl = ctx->arena.alloc_n<int64_t>(cl.size());
+          LRA_CUDA(cudaMemcpyAsync(dcl, cl.data(), cl.size() * sizeof(int64_t), cudaMemcpyHostToDevice, ctx->stream));
+          cluster_orth(ctx, k, ke, Zs, ldn, dcl, (int64_t)cl.size() / 2);
+        }
+        apply_q<T>(ctx, 'n', n, k, Vt, ldn, tau, Zs, ldn, ke);
+        r->vectors = hmalloc(sizeof(T) * (size_t)n * ke);
+        to_host(ctx, r->vectors, Zs, (size_t)n * ke);
+        LRA_CUDA(cudaStreamSynchronize(ctx->stream));
+      }
+      *out = r;
+    });
+  });
+}
+
+int lra_curfact(lra_ctx* ctx, int dtype, int64_t m, int64_t n, const void* A, int64_t lda, const lra_opts* opts,
+                const lra_rand* rand, lra_cur** out) {
+  if (out) *out = nullptr;
+  return guarded(ctx, [&] {
+    chkopts(opts);
+    check_dims(m, n);
+    if (!out) fail(LRA_EINVAL, "out is NULL");
+    lra_opts o = *opts;
+    o.pqrfact_retval = 0;  // src/cur.jl:534
+    dispatch(dtype, [&](auto z) {
+      using T = decltype(z);
+      DMat<T> dA = stage_in<T>(ctx, A, m, n, lda);
+      check_input(ctx, o, m, n, dA);
+      RandSrc rs(ctx, rand, o.seed);
+      auto sel = [&](char t, int64_t mm, int64_t nn, const DMat<T>& X) {
+        Fact<T> F = id_core<T>(ctx, o, t, mm, nn, X, rs, dtype, false);
+        std::vector<int64_t> idx(F.k);
+        to_host(ctx, idx.data(), F.jpvt, F.k);
+        LRA_CUDA(cudaStreamSynchronize(ctx->stream));
+        return idx;
+      };
+      lra_cur* r = static_cast<lra_cur*>(hmalloc(sizeof(lra_cur)));
+      std::memset(r, 0, sizeof *r);
+      std::vector<int64_t> rows, cols;
+      if (m == n && is_symmetric(ctx, n, dA.p, dA.ld)) {
+        cols = sel('n', m, n, dA);
+        rows = cols;
+        r->kind = 1;
+      } else if (m >= n) {
+        rows = sel('c', m, n, dA);
+        const int64_t kr = (int64_t)rows.size();
+        int64_t* drows = ctx->arena.alloc_n<int64_t>(std::max<int64_t>(kr, 1));
+        LRA_CUDA(cudaMemcpyAsync(drows, rows.data(), kr * sizeof(int64_t), cudaMemcpyHostToDevice, ctx->stream));
+        T* Ar = ctx->arena.alloc_n<T>((size_t)std::max<int64_t>(kr, 1) * std::max<int64_t>(n, 1));
+        gather_rows(ctx, kr, n, dA.p, dA.ld, drows, Ar, std::max<int64_t>(kr, 1));
+        cols = sel('n', kr, n, DMat<T>{Ar, std::max<int64_t>(kr, 1)});
+      } else {
+        cols = sel('n', m, n, dA);
+        const int64_t kc = (int64_t)cols.size();
+        int64_t* dcols = ctx->arena.alloc_n<int64_t>(std::max<int64_t>(kc, 1));
+        LRA_CUDA(cudaMemcpyAsync(dcols, cols.data(), kc * sizeof(int64_t), cudaMemcpyHostToDevice, ctx->stream));
+        T* Ac = ctx->arena.alloc_n<T>((size_t)std::max<int64_t>(m, 1) * std::max<int64_t>(kc, 1));
+        gather_cols(ctx, m, kc, dA.p, dA.ld, dcols, Ac, std::max<int64_t>(m, 1));
+        rows = sel('c', m, kc, DMat<T>{Ac, std::max<int64_t>(m, 1)});
+      }
+      if (r->kind == 0) {
+        const size_t k = std::min(rows.size(), cols.size());
+        rows.resize(k);
+        cols.resize(k);
+      }
+      r->kr = (int64_t)rows.size();
+      r->kc = (int64_t)cols.size();
+      r->rows = static_cast<int64_t*>(hmalloc(sizeof(int64_t) * std::max<size_t>(rows.size(), 1)));
+      r->cols = static_cast<int64_t*>(hmalloc(sizeof(int64_t) * std::max<size_t>(cols.size(), 1)));
+      std::memcpy(r->rows, rows.data(), rows.size() * sizeof(int64_t));
+      std::memcpy(r->cols, cols.data(), cols.size() * sizeof(int64_t));
+      *out = r;
+    });
+  });
+}
+
+}  // extern "C"
+
+// ---- spectral norms ----------------------------------------------------------------
+
+namespace lra {
+namespace {
+
+// power iteration of src/snorm.jl:14-45 with the operator given as callbacks
+template <typename T, class FwdFn, class AdjFn>
+double snorm_loop(lra_ctx* ctx, const lra_opts& o, int64_t m, int64_t n, bool herm, RandSrc& rs, FwdFn fwd,
+                  AdjFn adj) {
+  T* xn = ctx->arena.alloc_n<T>(std::max<int64_t>(n, 1));
+  T* xm = ctx->arena.alloc_n<T>(std::max<int64_t>(m, 1));
+  T* nrm = ctx->arena.alloc_n<T>(1);
+  if (rs.injected_gauss())
+    sketch_from_stream(ctx, rs.take_gauss_raw(n), n, xn, false);
+  else
+    rs.gauss(n, xn, false);
+  auto norm = [&](const T* x, int64_t len) {
+    col_norms(ctx, len, 1, x, std::max<int64_t>(len, 1), nrm);
+    T h = 0;
+    to_host(ctx, &h, nrm, 1);
+    LRA_CUDA(cudaStreamSynchronize(ctx->stream));
+    return (double)h;
+  };
+  double xnrm = norm(xn, n);
+  double s = 1, t = 0;
+  int64_t niter = 0;
+  while (s > 0 && std::fabs(s - t) > std::max(o.atol, t * o.rtol)) {
+    if (niter == o.snorm_niter) break;
+    ++niter;
+    scale_vec(ctx, n, xn, (T)(1.0 / xnrm));
+    if (herm) {
+      fwd(xn, xm);
+      copy_matrix(ctx, n, 1, xm, std::max<int64_t>(n, 1), xn, std::max<int64_t>(n, 1));
+    } else {
+      fwd(xn, xm);
+      adj(xm, xn);
+    }
+    xnrm = norm(xn, n);
+    t = s;
+    s = herm ? xnrm : std::sqrt(xnrm);
+  }
+  return s;
+}
+
+}  // namespace
+}  // namespace lra
+
+extern "C" {
+
+int lra_snorm(lra_ctx* ctx, int dtype, int64_t m, int64_t n, const void* A, int64_t lda, int hermitian,
+              const lra_opts* opts, const lra_rand* rand, double* out) {
+  return guarded(ctx, [&] {
+    chkopts(opts);
+    check_dims(m, n);
+    if (!out) fail(LRA_EINVAL, "out is NULL");
+    dispatch(dtype, [&](auto z) {
+      using T = decltype(z);
+      DMat<T> dA = stage_in<T>(ctx, A, m, n, lda);
+      check_input(ctx, *opts, m, n, dA);
+      const bool herm = hermitian < 0 ? (m == n && is_symmetric(ctx, n, dA.p, dA.ld)) : hermitian != 0;
+      RandSrc rs(ctx, rand, opts->seed);
+      *out = snorm_loop<T>(
+          ctx, *opts, m, n, herm, rs,
+          [&](const T* x, T* y) { gemv<T>(ctx, 'n', m, n, T(1), dA.p, dA.ld, x, T(0), y); },
+          [&](const T* y, T* x) { gemv<T>(ctx, 't', m, n, T(1), dA.p, dA.ld, y, T(0), x); });
+    });
+  });
+}
+
+int lra_snormdiff(lra_ctx* ctx, int dtype, int64_t m, int64_t n, const void* A, int64_t lda, const void* B,
+                  int64_t ldb, const lra_opts* opts, const lra_rand* rand, double* out) {
+  return guarded(ctx, [&] {
+    chkopts(opts);
+    check_dims(m, n);
+    if (!out) fail(LRA_EINVAL, "out is NULL");
+    dispatch(dtype, [&](auto z) {
+      using T = decltype(z);
+      DMat<T> dA = stage_in<T>(ctx, A, m, n, lda);
+      DMat<T> dB = stage_in<T>(ctx, B, m, n, ldb);
+      const bool herm = m == n && is_symmetric(ctx, n, dA.p, dA.ld) && is_symmetric(ctx, n, dB.p, dB.ld);
+      RandSrc rs(ctx, rand, opts->seed);
+      *out = snorm_loop<T>(
+          ctx, *opts, m, n, herm, rs,
+          [&](const T* x, T* y) {
+            gemv<T>(ctx, 'n', m, n, T(1), dA.p, dA.ld, x, T(0), y);
+            gemv<T>(ctx, 'n', m, n, T(-1), dB.p, dB.ld, x, T(1), y);
+          },
+          [&](const T* y, T* x) {
+            gemv<T>(ctx, 't', m, n, T(1), dA.p, dA.ld, y, T(0), x);
+            gemv<T>(ctx, 't', m, n, T(-1), dB.p, dB.ld, y, T(1), x);
+          });
+    });
+  });
+}
+
+int lra_snormdiff_id(lra_ctx* ctx, int dtype, char trans, int64_t m, int64_t n, const void* A, int64_t lda,
+                     const lra_id* F, const lra_opts* opts, const lra_rand* rand, double* out) {
+  return guarded(ctx, [&] {
+    chkopts(opts);
+    check_dims(m, n);
+    if (!out || !F) fail(LRA_EINVAL, "NULL argument");
+    const char t = chktrans(trans);
+    dispatch(dtype, [&](auto z) {
+      using T = decltype(z);
+      if (F->dtype != dtype) fail(LRA_EINVAL, "dtype of F");
+      DMat<T> dA = stage_in<T>(ctx, A, m, n, lda);
+      // work on op(A) (M x N): F = C [I T] P', C = op(A)[:, sk]
+      const int64_t M = t == 'n' ? m : n, N = t == 'n' ? n : m;
+      if (F->n != N) fail(LRA_EDIM, "ID size");
+      const int64_t k = F->k, ldm = std::max<int64_t>(M, 1);
+      T* Aop = dense_op(ctx, t, m, n, dA);
+      int64_t* p = ctx->arena.alloc_n<int64_t>(std::max<int64_t>(N, 1));
+      LRA_CUDA(cudaMemcpyAsync(p, F->sk, k * sizeof(int64_t), cudaMemcpyHostToDevice, ctx->stream));
+      LRA_CUDA(cudaMemcpyAsync(p + k, F->rd, (N - k) * sizeof(int64_t), cudaMemcpyHostToDevice, ctx->stream));
+      T* Td = ctx->arena.alloc_n<T>((size_t)std::max<int64_t>(k * (N - k), 1));
+      if (k > 0 && N > k)
+        LRA_CUDA(cudaMemcpyAsync(Td, F->T, (size_t)k * (N - k) * sizeof(T), cudaMemcpyHostToDevice, ctx->stream));
+      T* C = ctx->arena.alloc_n<T>((size_t)ldm * std::max<int64_t>(k, 1));
+      gather_cols(ctx, M, k, Aop, ldm, p, C, ldm);
+      // dense F = C [I T] P' then the difference power iteration
+      T* Fd = ctx->arena.alloc_n<T>((size_t)ldm * std::max<int64_t>(N, 1));
+      T* Fp = ctx->arena.alloc_n<T>((size_t)ldm * std::max<int64_t>(N, 1));
+      copy_matrix(ctx, M, k, C, ldm, Fp, ldm);
+      if (k > 0 && N > k) gemm<T>(ctx, 'n', 'n', M, N - k, k, T(1), C, ldm, Td, k, T(0), Fp + k * ldm, ldm);
+      else if (N > k) set_zero(ctx, Fp + k * ldm, ldm * (N - k));
+      scatter_cols(ctx, M, N, Fp, ldm, p, Fd, ldm);
+      RandSrc rs(ctx, rand, opts->seed);
+      *out = snorm_loop<T>(
+          ctx, *opts, M, N, false, rs,
+          [&](const T* x, T* y) {
+            gemv<T>(ctx, 'n', M, N, T(1), Aop, ldm, x, T(0), y);
+            gemv<T>(ctx, 'n', M, N, T(-1), Fd, ldm, x, T(1), y);
+          },
+          [&](const T* y, T* x) {
+            gemv<T>(ctx, 't', M, N, T(1), Aop, ldm, y, T(0), x);
+            gemv<T>(ctx, 't', M, N, T(-1), Fd, ldm, y, T(1), x);
+          });
+    });
+  });
+}
+
+int lra_snormdiff_psvd(lra_ctx* ctx, int dtype, int64_t m, int64_t n, const void* A, int64_t lda,
+                       const lra_psvd* F, const lra_opts* opts, const lra_rand* rand, double* out) {
+  return guarded(ctx, [&] {
+    chkopts(opts);
+    check_dims(m, n);
+    if (!out || !F || !F->U || !F->Vt) fail(LRA_EINVAL, "NULL argument");
+    dispatch(dtype, [&](auto z) {
+      using T = decltype(z);
+      if (F->dtype != dtype) fail(LRA_EINVAL, "dtype of F");
+      if (F->m != m || F->n != n) fail(LRA_EDIM, "PSVD size");
+      DMat<T> dA = stage_in<T>(ctx, A, m, n, lda);
+      const int64_t k = F->k, kk = std::max<int64_t>(k, 1);
+      T* U = ctx->arena.alloc_n<T>((size_t)std::max<int64_t>(m, 1) * kk);
+      T* S = ctx->arena.alloc_n<T>(kk);
+      T* Vt = ctx->arena.alloc_n<T>((size_t)kk * std::max<int64_t>(n, 1));
+      T* w = ctx->arena.alloc_n<T>(kk);
+      LRA_CUDA(cudaMemcpyAsync(U, F->U, (size_t)m * k * sizeof(T), cudaMemcpyHostToDevice, ctx->stream));
+      LRA_CUDA(cudaMemcpyAsync(S, F->S, (size_t)k * sizeof(T), cudaMemcpyHostToDevice, ctx->stream));
+      LRA_CUDA(cudaMemcpyAsync(Vt, F->Vt, (size_t)k * n * sizeof(T), cudaMemcpyHostToDevice, ctx->stream));
+      // US = U diag(S)
+      T* Sinv = ctx->arena.alloc_n<T>(kk);
+      std::vector<T> hs(k), hsi(k);
+      std::memcpy(hs.data(), F->S, k * sizeof(T));
+      for (int64_t i = 0; i < k; ++i) hsi[i] = hs[i] != T(0) ? T(1) / hs[i] : T(0);
+      LRA_CUDA(cudaMemcpyAsync(Sinv, hsi.data(), k * sizeof(T), cudaMemcpyHostToDevice, ctx->stream));
+      div_cols(ctx, std::max<int64_t>(m, 1), k, U, std::max<int64_t>(m, 1), Sinv);  // U <- U diag(S)
+      LRA_CUDA(cudaStreamSynchronize(ctx->stream));
+      RandSrc rs(ctx, rand, opts->seed);
+      *out = snorm_loop<T>(
+          ctx, *opts, m, n, false, rs,
+          [&](const T* x, T* y) {
+            gemv<T>(ctx, 'n', m, n, T(1), dA.p, dA.ld, x, T(0), y);
+            gemv<T>(ctx, 'n', k, n, T(1), Vt, kk, x, T(0), w);
+            gemv<T>(ctx, 'n', m, k, T(-1), U, std::max<int64_t>(m, 1), w, T(1), y);
+          },
+          [&](const T* y, T* x) {
+            gemv<T>(ctx, 't', m, n, T(1), dA.p, dA.ld, y, T(0), x);
+            gemv<T>(ctx, 't', m, k, T(1), U, std::max<int64_t>(m, 1), y, T(0), w);
+            gemv<T>(ctx, 't', k, n, T(-1), Vt, kk, w, T(1), x);
+          });
+    });
+  });
+}
+
+int lra_idfact_batched(lra_ctx* ctx, int dtype, int64_t count, const lra_matdesc* mats, const lra_opts* opts,
+                       const lra_rand* rand, lra_id** outs) {
+  if (!ctx || !mats || !outs || count < 0) return LRA_EINVAL;
+  for (int64_t i = 0; i < count; ++i) outs[i] = nullptr;
+  for (int64_t i = 0; i < count; ++i) {
+    const int st = lra_idfact(ctx, dtype, 'n', mats[i].m, mats[i].n, mats[i].A, mats[i].lda, opts,
+                              rand ? rand + i : nullptr, outs + i);
+    if (st != LRA_OK) {
+      for (int64_t j = 0; j < i; ++j) {
+        lra_id_free(outs[j]);
+        outs[j] = nullptr;
+      }
+      return st;
+    }
+  }
+  return LRA_OK;
+}
+
+void lra_id_free(lra_id* r) {
+  if (!r) return;
+  std::free(r->sk);
+  std::free(r->rd);
+  std::free(r->T);
+  std::free(r);
+}
+
+void lra_pqr_free(lra_pqr* r) {
+  if (!r) return;
+  std::free(r->p);
+  std::free(r->Q);
+  std::free(r->R);
+  std::free(r->T);
+  std::free(r);
+}
+
+void lra_psvd_free(lra_psvd* r) {
+  if (!r) return;
+  std::free(r->U);
+  std::free(r->S);
+  std::free(r->Vt);
+  std::free(r);
+}
+
+void lra_pheig_free(lra_pheig* r) {
+  if (!r) return;
+  std::free(r->values);
+  std::free(r->vectors);
+  std::free(r);
+}
+
+void lra_cur_free(lra_cur* r) {
+  if (!r) return;
+  std::free(r->rows);
+  std::free(r->cols);
+  std::free(r);
+}
+
+}  // extern "C"

@@ -1,0 +1,195 @@
+// Small dense factorizations of the post-processing stages, FP64 (input
+// precision) on CUDA cores:
+//   - one-sided (Hestenes) Jacobi SVD of a square k x k matrix, used for the
+//     core SVD of psvdfact (src/psvd.jl:245) after a QR of (R V)^T, and --
+//     on the shifted positive semidefinite B + s I -- for the k x k Hermitian
+//     eigenproblem of pheigfact (src/pheig.jl:284);
+//   - a symmetry test (ishermitian on a dense real matrix).
+// One cooperative launch runs all sweeps: each round of the round-robin
+// ordering rotates n/2 disjoint column pairs in parallel (one warp per
+// pair), separated by bounded grid barriers.
+
+#include <algorithm>
+#include <cmath>
+
+#include "common.cuh"
+#include "internal.hpp"
+
+namespace lra {
+
+namespace {
+
+template <typename T>
+struct JacParams {
+  int64_t n;
+  T* X;
+  int64_t ldx;
+  T* V;
+  int64_t ldv;
+  T* S;
+  double tol;
+  int max_sweeps;
+  double* part;
+  GridBar* bar;
+  int* sweeps_out;
+};
+
+__device__ __forceinline__ void rr_pair(int64_t r, int64_t s, int64_t nn, int64_t& p, int64_t& q) {
+  auto pos = [&](int64_t i) -> int64_t { return i == 0 ? 0 : 1 + (i - 1 + r) % (nn - 1); };
+  p = pos(s);
+  q = pos(nn - 1 - s);
+}
+
+template <typename T, int NT>
+__global__ void __launch_bounds__(NT) jacobi_kernel(JacParams<T> P) {
+  __shared__ double red[32];
+  constexpr int NW = NT / 32;
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  const int64_t gw = (int64_t)blockIdx.x * NW + wid;
+  const int64_t W = (int64_t)gridDim.x * NW;
+  const int64_t n = P.n;
+  const int64_t nn = n + (n & 1);
+  int sweep = 0;
+  for (; sweep < P.max_sweeps; ++sweep) {
+    double off = 0;
+    for (int64_t r = 0; r < nn - 1; ++r) {
+      for (int64_t s = gw; s < nn / 2; s += W) {
+        int64_t p, q;
+        rr_pair(r, s, nn, p, q);
+        if (p >= n || q >= n) continue;
+        if (p > q) {
+          const int64_t t = p;
+          p = q;
+          q = t;
+        }
+        T* xp = P.X + p * P.ldx;
+        T* xq = P.X + q * P.ldx;
+        double a = 0, b = 0, g = 0;
+        for (int64_t i = lane; i < n; i += 32) {
+          const double u = __ldcg(xp + i), v = __ldcg(xq + i);
+          a = fma(u, u, a);
+          b = fma(v, v, b);
+          g = fma(u, v, g);
+        }
+        a = warp_sum(a);
+        b = warp_sum(b);
+        g = warp_sum(g);
+        if (a == 0 || b == 0) continue;
+        const double rel = fabs(g) / sqrt(a * b);
+        if (!(rel > P.tol)) continue;
+        off = fmax(off, rel);
+        const double zeta = (b - a) / (2.0 * g);
+        const double t = copysign(1.0, zeta) / (fabs(zeta) + sqrt(1.0 + zeta * zeta));
+        const double c = 1.0 / sqrt(1.0 + t * t);
+        const double sn = c * t;
+        for (int64_t i = lane; i < n; i += 32) {
+          const double u = __ldcg(xp + i), v = __ldcg(xq + i);
+          xp[i] = (T)(c * u - sn * v);
+          xq[i] = (T)(sn * u + c * v);
+        }
+        T* vp = P.V + p * P.ldv;
+        T* vq = P.V + q * P.ldv;
+        for (int64_t i = lane; i < n; i += 32) {
+          const double u = __ldcg(vp + i), v = __ldcg(vq + i);
+          vp[i] = (T)(c * u - sn * v);
+          vq[i] = (T)(sn * u + c * v);
+        }
+      }
+      if (!grid_sync(P.bar)) return;
+    }
+    off = block_max(off, red);
+    if (threadIdx.x == 0) P.part[blockIdx.x] = off;
+    if (!grid_sync(P.bar)) return;
+    double mx = 0;
+    for (int b = threadIdx.x; b < gridDim.x; b += NT) mx = fmax(mx, __ldcg(P.part + b));
+    mx = block_max(mx, red);
+    if (!grid_sync(P.bar)) return;  // everyone read part before it is rewritten
+    if (mx <= P.tol) {
+      ++sweep;
+      break;
+    }
+  }
+  // singular values = column norms
+  for (int64_t j = gw; j < n; j += W) {
+    const T* x = P.X + j * P.ldx;
+    double a = 0;
+    for (int64_t i = lane; i < n; i += 32) {
+      const double u = __ldcg(x + i);
+      a = fma(u, u, a);
+    }
+    a = warp_sum(a);
+    if (lane == 0) P.S[j] = (T)sqrt(a);
+  }
+  if (blockIdx.x == 0 && threadIdx.x == 0) *P.sweeps_out = sweep;
+}
+
+template <typename T>
+__global__ void symcheck_kernel(int64_t n, const T* __restrict__ A, int64_t lda, int* bad) {
+  const int64_t total = n * n;
+  int local = 0;
+  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < total;
+       t += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t i = t % n, j = t / n;
+    if (i < j && A[i + j * lda] != A[j + i * lda]) local = 1;
+  }
+  if (__syncthreads_or(local) && threadIdx.x == 0) atomicExch(bad, 1);
+}
+
+}  // namespace
+
+template <typename T>
+void jacobi_svd(lra_ctx* ctx, int64_t n, T* X, int64_t ldx, T* V, int64_t ldv, T* S) {
+  constexpr int NT = 256;
+  if (n <= 0) return;
+  set_identity(ctx, n, n, V, ldv);
+  const ArenaMark mk = ctx->arena.mark();
+  int per_sm = 0;
+  LRA_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, jacobi_kernel<T, NT>, NT, 0));
+  const int64_t pairs = (n + 1) / 2;
+  int grid = (int)std::min<int64_t>((pairs + (NT / 32) - 1) / (NT / 32), (int64_t)ctx->num_sms);
+  grid = std::max(1, std::min(grid, ctx->num_sms * std::max(per_sm, 1)));
+  JacParams<T> P;
+  P.n = n;
+  P.X = X;
+  P.ldx = ldx;
+  P.V = V;
+  P.ldv = ldv;
+  P.S = S;
+  P.tol = (double)Real<T>::eps * 2.0 * std::sqrt((double)n);
+  P.max_sweeps = 40;
+  P.part = ctx->arena.alloc_n<double>(grid);
+  P.bar = reinterpret_cast<GridBar*>(ctx->arena.alloc(sizeof(GridBar)));
+  P.sweeps_out = ctx->arena.alloc_n<int>(1);
+  LRA_CUDA(cudaMemsetAsync(P.bar, 0, sizeof(GridBar), ctx->stream));
+  void* args[] = {&P};
+  LRA_CUDA(cudaLaunchCooperativeKernel((const void*)jacobi_kernel<T, NT>, dim3(grid), dim3(NT), args, 0,
+                                       ctx->stream));
+  post_launch(ctx, "jacobi_kernel");
+  GridBar hb;
+  LRA_CUDA(cudaMemcpyAsync(&hb, P.bar, sizeof(GridBar), cudaMemcpyDeviceToHost, ctx->stream));
+  LRA_CUDA(cudaStreamSynchronize(ctx->stream));
+  ctx->arena.release(mk);
+  if (hb.err != 0) fail(LRA_ETIMEDOUT, "jacobi: a grid barrier timed out");
+}
+
+template <typename T>
+bool is_symmetric(lra_ctx* ctx, int64_t n, const T* A, int64_t lda) {
+  const ArenaMark mk = ctx->arena.mark();
+  int* bad = ctx->arena.alloc_n<int>(1);
+  LRA_CUDA(cudaMemsetAsync(bad, 0, sizeof(int), ctx->stream));
+  const unsigned g = (unsigned)std::max<int64_t>(1, std::min<int64_t>((n * n + 255) / 256, (int64_t)ctx->num_sms * 16));
+  symcheck_kernel<T><<<g, 256, 0, ctx->stream>>>(n, A, lda, bad);
+  post_launch(ctx, "symcheck_kernel");
+  int h = 0;
+  LRA_CUDA(cudaMemcpyAsync(&h, bad, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+  LRA_CUDA(cudaStreamSynchronize(ctx->stream));
+  ctx->arena.release(mk);
+  return h == 0;
+}
+
+template void jacobi_svd<float>(lra_ctx*, int64_t, float*, int64_t, float*, int64_t, float*);
+template void jacobi_svd<double>(lra_ctx*, int64_t, double*, int64_t, double*, int64_t, double*);
+template bool is_symmetric<float>(lra_ctx*, int64_t, const float*, int64_t);
+template bool is_symmetric<double>(lra_ctx*, int64_t, const double*, int64_t);
+
+}  // namespace lra

@@ -1,0 +1,218 @@
+// Internal interfaces of liblra: context, workspace arena, kernel launchers.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <cstdarg>
+#include <string>
+#include <vector>
+
+#include "../../include/lra.h"
+
+namespace lra {
+
+// Error carried from the point of failure to the C ABI boundary.
+struct Error {
+  int status;
+  std::string msg;
+};
+
+[[noreturn]] void fail(int status, const char* fmt, ...);
+void check_cuda(cudaError_t e, const char* what);
+#define LRA_CUDA(x) ::lra::check_cuda((x), #x)
+
+// Device workspace: bump allocation in chunks that never move while a call
+// runs (so earlier pointers stay valid).  All work of a context is ordered
+// on its one stream, so rewinding to a mark and reusing memory is safe.
+// At the start of a call, several chunks are merged into one.
+struct ArenaMark {
+  size_t chunk;
+  size_t used;
+};
+
+class Arena {
+ public:
+  ~Arena();
+  void* alloc(size_t bytes);  // 256-byte aligned
+  template <typename T>
+  T* alloc_n(size_t n) {
+    return static_cast<T*>(alloc(n * sizeof(T)));
+  }
+  ArenaMark mark() const;
+  void release(ArenaMark m);
+  // start of a call: merge chunks (synchronizes the stream first)
+  void reset(cudaStream_t stream);
+  size_t capacity() const;
+
+ private:
+  struct Chunk {
+    char* base;
+    size_t cap;
+    size_t used;
+  };
+  std::vector<Chunk> chunks_;
+  size_t cur_ = 0;
+};
+
+}  // namespace lra
+
+struct lra_ctx {
+  int device = 0;
+  int num_sms = 0;
+  cudaStream_t stream = nullptr;
+  bool own_stream = false;
+  lra::Arena arena;
+  std::string last_error;
+  int64_t launches = 0;
+  double stage_ms[4] = {0, 0, 0, 0};
+  cudaEvent_t ev[5] = {nullptr, nullptr, nullptr, nullptr, nullptr};
+  uint64_t rng_counter = 0;  // advances per call of the in-library generator
+  // pinned host staging (grown on demand)
+  void* pinned = nullptr;
+  size_t pinned_cap = 0;
+};
+
+namespace lra {
+
+// ---- launchers (defined in the .cu files) ---------------------------------
+
+// C = alpha * op(A) * op(B) + beta * C, column-major, CUDA cores.
+template <typename T>
+void gemm(lra_ctx* ctx, char ta, char tb, int64_t m, int64_t n, int64_t k, T alpha,
+          const T* A, int64_t lda, const T* B, int64_t ldb, T beta, T* C, int64_t ldc);
+
+// op(A) (M x N) cut into `ns` exact BF16 byte slices at per-column
+// power-of-two scales (K-major planes, ld = Kp), built once per call and
+// reused by every adaptive sketch step.
+struct TcSplit {
+  int64_t K = 0, N = 0, Kp = 0;
+  int ns = 0;
+  char trans = 'n';
+  int* colexp = nullptr;
+  void* slices = nullptr;
+};
+bool tc_sketch_supported(int64_t order, int64_t M, int64_t N);
+template <typename T>
+void tc_split(lra_ctx* ctx, char trans, int64_t M, int64_t N, const T* A, int64_t lda, int ns,
+              TcSplit* out);
+// B (order x N, ldb) = S op(A) on tcgen05 tensor cores; S is order x M
+// (ld = order) with entries on the 1/32 lattice.
+template <typename T>
+void tc_sketch(lra_ctx* ctx, const TcSplit& sp, int64_t order, const T* S, T* B, int64_t ldb);
+
+// Rank-adaptive column-pivoted Householder QR (geqp3_adap!), in place.
+// pivot == false runs the same Householder QR without pivoting.
+template <typename T>
+int64_t geqp3_adap(lra_ctx* ctx, int64_t m, int64_t n, T* A, int64_t lda, int64_t* jpvt,
+                   T* tau, int64_t kmax, int64_t nb, double atol, double rtol, bool pivot);
+
+// X (k x nrhs) <- triu(R)^{-1} X, R k x k (ldr).
+template <typename T>
+void trsm_upper(lra_ctx* ctx, int64_t k, int64_t nrhs, const T* R, int64_t ldr, T* X,
+                int64_t ldx);
+
+// Householder vectors (below the diagonal of V, m x k) applied to X
+// (m x nc): X <- Q X (trans 'n') or Q^T X (trans 't').
+template <typename T>
+void apply_q(lra_ctx* ctx, char trans, int64_t m, int64_t k, const T* V, int64_t ldv,
+             const T* tau, T* X, int64_t ldx, int64_t nc);
+
+// Explicit Q (m x k) from Householder vectors (LAPACK xORGQR).
+template <typename T>
+void orgqr(lra_ctx* ctx, int64_t m, int64_t k, T* V, int64_t ldv, const T* tau);
+
+// One-sided Jacobi SVD of X (n x n, square, in place): on exit X = U * S,
+// V (n x n) accumulates the right rotations, S gets the column norms.
+template <typename T>
+void jacobi_svd(lra_ctx* ctx, int64_t n, T* X, int64_t ldx, T* V, int64_t ldv, T* S);
+
+// exact symmetry test of a square device matrix
+template <typename T>
+bool is_symmetric(lra_ctx* ctx, int64_t n, const T* A, int64_t lda);
+
+// ---- small elementwise / data-movement kernels (kernels_misc.cu) -----------
+template <typename T>
+void copy_matrix(lra_ctx* ctx, int64_t m, int64_t n, const T* src, int64_t lds, T* dst,
+                 int64_t ldd);
+template <typename T>
+void transpose(lra_ctx* ctx, int64_t m, int64_t n, const T* src, int64_t lds, T* dst,
+               int64_t ldd);
+// dst(:, j) = src(:, idx[j] - 1) (1-based idx on the device)
+template <typename T>
+void gather_cols(lra_ctx* ctx, int64_t m, int64_t k, const T* src, int64_t lds,
+                 const int64_t* idx, T* dst, int64_t ldd);
+// dst(i, :) = src(idx[i] - 1, :)
+template <typename T>
+void gather_rows(lra_ctx* ctx, int64_t k, int64_t n, const T* src, int64_t lds,
+                 const int64_t* idx, T* dst, int64_t ldd);
+// dst(:, idx[j] - 1) = src(:, j)
+template <typename T>
+void scatter_cols(lra_ctx* ctx, int64_t m, int64_t k, const T* src, int64_t lds,
+                  const int64_t* idx, T* dst, int64_t ldd);
+template <typename T>
+void set_zero(lra_ctx* ctx, T* p, int64_t n);
+template <typename T>
+void set_identity(lra_ctx* ctx, int64_t m, int64_t n, T* A, int64_t lda);
+// lower part (below diagonal) of A (m x n) set to zero
+template <typename T>
+void zero_lower(lra_ctx* ctx, int64_t m, int64_t n, T* A, int64_t lda);
+// 1/32-lattice rounding of a Gaussian stream, converting to T
+template <typename T>
+void sketch_from_stream(lra_ctx* ctx, const double* g, int64_t n, T* out, bool lattice);
+// in-library lattice Gaussians (Philox-4x32-10, key = seed, counter = base + i)
+template <typename T>
+void sketch_philox(lra_ctx* ctx, uint64_t seed, uint64_t base, int64_t n, T* out);
+// in-library uniform integers in [1, hi] and permutations of 1..n
+void ints_philox(lra_ctx* ctx, uint64_t seed, uint64_t base, int64_t n, int64_t hi, int64_t* out);
+void perm_philox(lra_ctx* ctx, uint64_t seed, uint64_t base, int64_t n, int64_t* out);
+// B(i, j) = 0.5 (B(i, j) + B(j, i)) on both triangles (hermitianize!)
+template <typename T>
+void symmetrize(lra_ctx* ctx, int64_t n, T* B, int64_t ldb);
+// A(i, i) += s
+template <typename T>
+void add_diag(lra_ctx* ctx, int64_t n, T* A, int64_t lda, T s);
+// dst(idx[i] - 1, :) = src(i, :)
+template <typename T>
+void scatter_rows(lra_ctx* ctx, int64_t k, int64_t n, const T* src, int64_t lds,
+                  const int64_t* idx, T* dst, int64_t ldd);
+// x *= s
+template <typename T>
+void scale_vec(lra_ctx* ctx, int64_t n, T* x, T s);
+// columns j of X (m x n) divided by s[j] (skipped where s[j] == 0)
+template <typename T>
+void div_cols(lra_ctx* ctx, int64_t m, int64_t n, T* X, int64_t ldx, const T* s);
+// pheigorth!: Gram-Schmidt inside eigenvalue clusters, cl = cluster bounds
+template <typename T>
+void cluster_orth(lra_ctx* ctx, int64_t n, int64_t k, T* Z, int64_t ldz, const int64_t* cl,
+                  int64_t ncl);
+// nonfinite check: returns true when every entry is finite
+template <typename T>
+bool all_finite(lra_ctx* ctx, int64_t m, int64_t n, const T* A, int64_t lda);
+// column 2-norms
+template <typename T>
+void col_norms(lra_ctx* ctx, int64_t m, int64_t n, const T* A, int64_t lda, T* out);
+
+// SRFT / subset / sparse-Gaussian sketches (sketch.cu), left side, op(A)
+template <typename T>
+void srft_sketch(lra_ctx* ctx, char trans, int64_t M, int64_t N, const T* A, int64_t lda,
+                 const T* d, const int64_t* idx, int64_t order, T* B, int64_t ldb);
+template <typename T>
+void sub_sketch(lra_ctx* ctx, char trans, int64_t M, int64_t N, const T* A, int64_t lda,
+                const int64_t* rows, int64_t order, T* B, int64_t ldb);
+template <typename T>
+void srft_signs(lra_ctx* ctx, const double* g, int64_t n, T* d);
+template <typename T>
+void sprn_sketch(lra_ctx* ctx, char trans, int64_t M, int64_t N, const T* A, int64_t lda,
+                 const int64_t* perm, const T* g, int64_t order, T* B, int64_t ldb);
+
+// y = op(A) x (gemv), CUDA cores
+template <typename T>
+void gemv(lra_ctx* ctx, char trans, int64_t m, int64_t n, T alpha, const T* A, int64_t lda,
+          const T* x, T beta, T* y);
+
+// kernel-launch accounting (every launcher calls this once per launch)
+inline void count_launch(lra_ctx* ctx, int n = 1) { ctx->launches += n; }
+void post_launch(lra_ctx* ctx, const char* name);
+
+}  // namespace lra

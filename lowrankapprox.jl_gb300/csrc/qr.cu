@@ -1,0 +1,529 @@
+// Rank-adaptive column-pivoted Householder QR (geqp3_adap!), triangular
+// solve, Householder application -- CUDA cores, input precision.
+//
+// geqp3_adap! (src/pqr.jl:348-418) drives LAPACK xLAQPS block by block
+// (src/lapack.jl:117-139).  This kernel keeps xLAQPS's observable
+// semantics -- IxAMAX pivots (largest partial norm, first index on ties),
+// the xLARFG reflector, the partial-norm downdate with the tol3z
+// recomputation trigger, the early end of a block when a norm must be
+// recomputed, and the reference's rank test on the last diagonal entry of
+// each block -- but applies each reflector to the trailing columns at once
+// instead of through xLAQPS's F matrix: on the GPU one pass over the
+// trailing panel per pivot is the natural unit, and the results agree with
+// LAPACK to rounding.
+//
+// One cooperative launch does the whole factorization.  Every CTA runs the
+// same control flow and takes every decision from data made visible by a
+// bounded grid barrier, so all CTAs agree without further messages.
+
+#include <cooperative_groups.h>
+
+#include <algorithm>
+#include <cmath>
+
+#include "common.cuh"
+#include "internal.hpp"
+
+namespace lra {
+
+namespace {
+
+template <typename T>
+struct QrParams {
+  int64_t m, n, lda;
+  T* A;
+  int64_t* jpvt;
+  T* tau;
+  T* vn1;
+  T* vn2;
+  int* flag;
+  T* part_v;
+  int64_t* part_i;
+  double* part_d;
+  int* lsticc;  // [2]
+  GridBar* bar;
+  int64_t kmax, nb;
+  double atol, rtol;
+  int pivot;
+  int64_t* k_out;
+};
+
+// exact power-of-two scale for a norm computation
+__device__ __forceinline__ double pow2_scale_inv(double mx) {
+  int e = ilogb(mx);
+  return ldexp(1.0, -e);
+}
+
+// 2-norm of x[0..len) computed by one warp (all lanes get the result)
+template <typename T>
+__device__ T warp_nrm2(const T* x, int64_t len, int lane) {
+  double mx = 0;
+  for (int64_t i = lane; i < len; i += 32) mx = fmax(mx, fabs((double)__ldcg(x + i)));
+  mx = warp_max(mx);
+  if (mx == 0 || !isfinite(mx)) return (T)mx;
+  const double s = pow2_scale_inv(mx);
+  double acc = 0;
+  for (int64_t i = lane; i < len; i += 32) {
+    double t = (double)__ldcg(x + i) * s;
+    acc = fma(t, t, acc);
+  }
+  acc = warp_sum(acc);
+  return (T)(sqrt(acc) / s);
+}
+
+template <typename T>
+__device__ T block_nrm2(const T* x, int64_t len, double* red) {
+  double mx = 0;
+  for (int64_t i = threadIdx.x; i < len; i += blockDim.x) mx = fmax(mx, fabs((double)__ldcg(x + i)));
+  mx = block_max(mx, red);
+  if (mx == 0 || !isfinite(mx)) return (T)mx;
+  const double s = pow2_scale_inv(mx);
+  double acc = 0;
+  for (int64_t i = threadIdx.x; i < len; i += blockDim.x) {
+    double t = (double)__ldcg(x + i) * s;
+    acc = fma(t, t, acc);
+  }
+  acc = block_sum(acc, red);
+  return (T)(sqrt(acc) / s);
+}
+
+template <typename T>
+__device__ __forceinline__ T lapy2(T x, T y) {
+  T xa = fabs(x), ya = fabs(y);
+  T w = fmax(xa, ya), z = fmin(xa, ya);
+  if (z == 0 || w > Real<T>::big) return w;
+  T q = z / w;
+  return w * sqrt(T(1) + q * q);
+}
+
+// block-wide argmax of per-thread candidates; result in (v, i) on all threads
+template <typename T>
+__device__ void block_argmax(T& v, int64_t& i, T* sv, int64_t* si) {
+  warp_argmax(v, i);
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  const int nw = blockDim.x >> 5;
+  __syncthreads();
+  if (lane == 0) {
+    sv[wid] = v;
+    si[wid] = i;
+  }
+  __syncthreads();
+  if (wid == 0) {
+    T vv = lane < nw ? sv[lane] : T(-1);
+    int64_t ii = lane < nw ? si[lane] : INT64_MAX;
+    warp_argmax(vv, ii);
+    if (lane == 0) {
+      sv[0] = vv;
+      si[0] = ii;
+    }
+  }
+  __syncthreads();
+  v = sv[0];
+  i = si[0];
+  __syncthreads();
+}
+
+// every CTA reduces the per-CTA partials to the global argmax
+template <typename T>
+__device__ int64_t reduce_pivot(const QrParams<T>& P, T* sv, int64_t* si) {
+  T v = T(-1);
+  int64_t i = INT64_MAX;
+  for (int b = threadIdx.x; b < gridDim.x; b += blockDim.x)
+    argmax_merge(v, i, __ldcg(P.part_v + b), __ldcg(P.part_i + b));
+  block_argmax(v, i, sv, si);
+  return i;
+}
+
+template <typename T, int NT>
+__global__ void __launch_bounds__(NT) geqp3_kernel(QrParams<T> P) {
+  __shared__ T sv[32];
+  __shared__ int64_t si[32];
+  __shared__ double red[32];
+  __shared__ T s_tau;
+  constexpr int NW = NT / 32;
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  const int64_t gw = (int64_t)blockIdx.x * NW + wid;
+  const int64_t W = (int64_t)gridDim.x * NW;
+  const int64_t m = P.m, n = P.n, lda = P.lda;
+  T* __restrict__ A = P.A;
+  const T tol3z = sqrt(Real<T>::eps);
+  const int64_t lastrk = m < n ? m : n;
+
+  // ---- initial column norms, ptol, first pivot -----------------------------
+  double lmax = 0;
+  T bv = T(-1);
+  int64_t bi = INT64_MAX;
+  for (int64_t j = gw; j < n; j += W) {
+    T nr = P.pivot ? warp_nrm2(A + j * lda, m, lane) : T(0);
+    if (lane == 0) {
+      P.vn1[j] = nr;
+      P.vn2[j] = nr;
+      P.flag[j] = 0;
+      P.jpvt[j] = j + 1;
+    }
+    lmax = fmax(lmax, (double)nr);
+    argmax_merge(bv, bi, nr, j);
+  }
+  lmax = block_max(lmax, red);
+  block_argmax(bv, bi, sv, si);
+  if (threadIdx.x == 0) {
+    P.part_d[blockIdx.x] = lmax;
+    P.part_v[blockIdx.x] = bv;
+    P.part_i[blockIdx.x] = bi;
+  }
+  if (!grid_sync(P.bar)) return;
+  double maxnrm = 0;
+  for (int b = threadIdx.x; b < gridDim.x; b += blockDim.x)
+    maxnrm = fmax(maxnrm, __ldcg(P.part_d + b));
+  maxnrm = block_max(maxnrm, red);
+  const double ptol = fmax(P.atol, P.rtol * maxnrm);
+  int64_t pvt = reduce_pivot(P, sv, si);
+
+  int64_t kres = P.kmax;
+  int64_t j = 0;
+  int par = 0;
+  while (j < P.kmax) {
+    const int64_t jb = min(P.nb, P.kmax - j);
+    int* lst = P.lsticc + par;
+    if (blockIdx.x == 0 && threadIdx.x == 0) P.lsticc[par ^ 1] = 0;
+    int64_t kk = 0;
+    bool stop_block = false;
+    while (kk < jb && !stop_block) {
+      const int64_t c = j + kk;
+      if (!P.pivot) pvt = c;
+      // ---- one CTA: pivot swap + reflector -----------------------------------
+      if (blockIdx.x == 0) {
+        if (pvt != c) {
+          T* a1 = A + c * lda;
+          T* a2 = A + pvt * lda;
+          for (int64_t i = threadIdx.x; i < m; i += NT) {
+            T t1 = __ldcg(a1 + i), t2 = __ldcg(a2 + i);
+            a1[i] = t2;
+            a2[i] = t1;
+          }
+          if (threadIdx.x == 0) {
+            // (every cross-CTA read in this kernel bypasses L1: ld.global.cg)
+            const int64_t it = __ldcg(P.jpvt + pvt);
+            P.jpvt[pvt] = __ldcg(P.jpvt + c);
+            P.jpvt[c] = it;
+            P.vn1[pvt] = __ldcg(P.vn1 + c);
+            P.vn2[pvt] = __ldcg(P.vn2 + c);
+          }
+        }
+        __syncthreads();
+        T* col = A + c * lda;
+        T tau = 0;
+        if (c < m - 1) {
+          T* x = col + c + 1;
+          const int64_t len = m - c - 1;
+          T xnorm = block_nrm2(x, len, red);
+          T alpha = __ldcg(col + c);
+          if (xnorm != 0) {
+            T beta = -copysign(lapy2(alpha, xnorm), alpha);
+            const T safmin = Real<T>::safmin / Real<T>::eps;
+            int knt = 0;
+            if (fabs(beta) < safmin) {
+              const T rsafmn = T(1) / safmin;
+              do {
+                ++knt;
+                for (int64_t i = threadIdx.x; i < len; i += NT) x[i] = __ldcg(x + i) * rsafmn;
+                beta *= rsafmn;
+                alpha *= rsafmn;
+              } while (fabs(beta) < safmin && knt < 20);
+              __syncthreads();
+              xnorm = block_nrm2(x, len, red);
+              beta = -copysign(lapy2(alpha, xnorm), alpha);
+            }
+            tau = (beta - alpha) / beta;
+            const T scal = T(1) / (alpha - beta);
+            for (int64_t i = threadIdx.x; i < len; i += NT) x[i] = __ldcg(x + i) * scal;
+            for (int q = 0; q < knt; ++q) beta *= safmin;
+            __syncthreads();
+            if (threadIdx.x == 0) col[c] = beta;
+          }
+        }
+        if (threadIdx.x == 0) P.tau[c] = tau;
+      }
+      if (!grid_sync(P.bar)) return;
+
+      // ---- all warps: apply H(c) to the trailing columns, downdate norms ------
+      if (threadIdx.x == 0) s_tau = __ldcg(P.tau + c);
+      __syncthreads();
+      const T tauc = s_tau;
+      const T* v = A + c * lda;
+      bv = T(-1);
+      bi = INT64_MAX;
+      int myflag = 0;
+      int64_t jj = c + 1 + ((gw - (c + 1)) % W + W) % W;
+      for (; jj < n; jj += W) {
+        T* colj = A + jj * lda;
+        T s = 0;
+        for (int64_t i = c + 1 + lane; i < m; i += 32) s += __ldcg(v + i) * __ldcg(colj + i);
+        s = warp_sum(s);
+        const T arc0 = __ldcg(colj + c);
+        const T f = tauc * (arc0 + s);
+        if (f != 0)
+          for (int64_t i = c + 1 + lane; i < m; i += 32) colj[i] = __ldcg(colj + i) - f * __ldcg(v + i);
+        const T arc = arc0 - f;
+        if (lane == 0) colj[c] = arc;
+        if (P.pivot) {
+          T v1 = __ldcg(P.vn1 + jj);
+          if (c < lastrk - 1 && v1 != 0) {
+            T temp = fabs(arc) / v1;
+            temp = fmax(T(0), (T(1) + temp) * (T(1) - temp));
+            const T r = v1 / __ldcg(P.vn2 + jj);
+            const T temp2 = temp * r * r;
+            if (temp2 <= tol3z) {
+              myflag = 1;
+              if (lane == 0) P.flag[jj] = 1;
+            } else {
+              v1 = v1 * sqrt(temp);
+              if (lane == 0) P.vn1[jj] = v1;
+            }
+          }
+          argmax_merge(bv, bi, v1, jj);
+        }
+      }
+      if (myflag && lane == 0) atomicAdd(lst, 1);
+      block_argmax(bv, bi, sv, si);
+      if (threadIdx.x == 0) {
+        P.part_v[blockIdx.x] = bv;
+        P.part_i[blockIdx.x] = bi;
+      }
+      if (!grid_sync(P.bar)) return;
+      stop_block = *((volatile int*)lst) != 0;
+      pvt = reduce_pivot(P, sv, si);
+      ++kk;
+    }
+    const int64_t kb = kk;
+    const int64_t jn = j + kb;
+    if (stop_block) {
+      // recompute the flagged partial norms over rows jn..m-1
+      bv = T(-1);
+      bi = INT64_MAX;
+      for (int64_t q = jn + ((gw - jn) % W + W) % W; q < n; q += W) {
+        T v1 = __ldcg(P.vn1 + q);
+        if (__ldcg(P.flag + q)) {
+          v1 = warp_nrm2(A + q * lda + jn, m - jn, lane);
+          if (lane == 0) {
+            P.vn1[q] = v1;
+            P.vn2[q] = v1;
+            P.flag[q] = 0;
+          }
+        }
+        argmax_merge(bv, bi, v1, q);
+      }
+      block_argmax(bv, bi, sv, si);
+      if (threadIdx.x == 0) {
+        P.part_v[blockIdx.x] = bv;
+        P.part_i[blockIdx.x] = bi;
+      }
+      if (!grid_sync(P.bar)) return;
+      pvt = reduce_pivot(P, sv, si);
+    }
+    // rank test of geqp3_adap_main! (src/pqr.jl:407-415)
+    if (fabs((double)__ldcg(A + (jn - 1) + (jn - 1) * lda)) <= ptol) {
+      bool found = false;
+      for (int64_t i = j; i < jn; ++i) {
+        if (fabs((double)__ldcg(A + i + i * lda)) <= ptol) {
+          kres = i;
+          found = true;
+          break;
+        }
+      }
+      if (found) break;
+    }
+    j = jn;
+    par ^= 1;
+  }
+  if (blockIdx.x == 0 && threadIdx.x == 0) *P.k_out = kres;
+}
+
+// ---- triangular solve: X <- triu(R)^{-1} X, one warp per right-hand side ----
+template <typename T>
+__global__ void trsm_upper_kernel(int64_t k, int64_t nrhs, const T* __restrict__ R, int64_t ldr,
+                                  T* __restrict__ X, int64_t ldx) {
+  extern __shared__ unsigned char smem_raw[];
+  T* sb = reinterpret_cast<T*>(smem_raw);
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  const int nw = blockDim.x >> 5;
+  T* b = sb + (int64_t)wid * k;
+  for (int64_t col = (int64_t)blockIdx.x * nw + wid; col < nrhs; col += (int64_t)gridDim.x * nw) {
+    T* x = X + col * ldx;
+    for (int64_t i = lane; i < k; i += 32) b[i] = x[i];
+    __syncwarp();
+    for (int64_t i = k - 1; i >= 0; --i) {
+      const T xi = b[i] / R[i + i * ldr];
+      __syncwarp();
+      if (xi != 0) {
+        const T* ri = R + i * ldr;
+        for (int64_t q = lane; q < i; q += 32) b[q] -= xi * ri[q];
+      }
+      if (lane == 0) b[i] = xi;
+      __syncwarp();
+    }
+    for (int64_t i = lane; i < k; i += 32) x[i] = b[i];
+    __syncwarp();
+  }
+}
+
+// ---- Householder application, one warp per column of X ----------------------
+template <typename T>
+__global__ void apply_q_kernel(int trans, int64_t m, int64_t k, const T* __restrict__ V, int64_t ldv,
+                               const T* __restrict__ tau, T* __restrict__ X, int64_t ldx, int64_t nc) {
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  const int nw = blockDim.x >> 5;
+  for (int64_t col = (int64_t)blockIdx.x * nw + wid; col < nc; col += (int64_t)gridDim.x * nw) {
+    T* x = X + col * ldx;
+    for (int64_t t = 0; t < k; ++t) {
+      const int64_t i = trans ? t : (k - 1 - t);
+      const T ti = tau[i];
+      if (ti == 0) continue;
+      const T* v = V + i * ldv;
+      T s = 0;
+      for (int64_t r = i + 1 + lane; r < m; r += 32) s += v[r] * x[r];
+      s = warp_sum(s);
+      const T f = ti * (x[i] + s);
+      __syncwarp();
+      for (int64_t r = i + 1 + lane; r < m; r += 32) x[r] -= f * v[r];
+      if (lane == 0) x[i] -= f;
+      __syncwarp();
+    }
+  }
+}
+
+template <typename T>
+__global__ void col_norms_kernel(int64_t m, int64_t n, const T* __restrict__ A, int64_t lda,
+                                 T* __restrict__ out) {
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  const int nw = blockDim.x >> 5;
+  for (int64_t j = (int64_t)blockIdx.x * nw + wid; j < n; j += (int64_t)gridDim.x * nw) {
+    T r = warp_nrm2(A + j * lda, m, lane);
+    if (lane == 0) out[j] = r;
+  }
+}
+
+}  // namespace
+
+template <typename T>
+int64_t geqp3_adap(lra_ctx* ctx, int64_t m, int64_t n, T* A, int64_t lda, int64_t* jpvt, T* tau,
+                   int64_t kmax, int64_t nb, double atol, double rtol, bool pivot) {
+  constexpr int NT = 512;
+  if (n <= 0) return 0;
+  const ArenaMark mark = ctx->arena.mark();
+  int per_sm = 0;
+  LRA_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, geqp3_kernel<T, NT>, NT, 0));
+  if (per_sm < 1) fail(LRA_ECUDA, "geqp3 kernel cannot be resident");
+  const int64_t want = (n + (NT / 32) - 1) / (NT / 32);
+  int grid = (int)std::min<int64_t>((int64_t)ctx->num_sms * std::min(per_sm, 1), want);
+  grid = std::max(grid, 1);
+
+  QrParams<T> P;
+  P.m = m;
+  P.n = n;
+  P.lda = lda;
+  P.A = A;
+  P.jpvt = jpvt;
+  P.tau = tau;
+  P.vn1 = ctx->arena.alloc_n<T>(n);
+  P.vn2 = ctx->arena.alloc_n<T>(n);
+  P.flag = ctx->arena.alloc_n<int>(n);
+  P.part_v = ctx->arena.alloc_n<T>(grid);
+  P.part_i = ctx->arena.alloc_n<int64_t>(grid);
+  P.part_d = ctx->arena.alloc_n<double>(grid);
+  int* small = ctx->arena.alloc_n<int>(8);
+  P.lsticc = small;
+  P.bar = reinterpret_cast<GridBar*>(ctx->arena.alloc(sizeof(GridBar)));
+  P.kmax = std::min<int64_t>(kmax, std::min(m, n));
+  P.nb = std::max<int64_t>(1, std::min<int64_t>(nb, std::max<int64_t>(P.kmax, 1)));
+  P.atol = atol;
+  P.rtol = rtol;
+  P.pivot = pivot ? 1 : 0;
+  P.k_out = ctx->arena.alloc_n<int64_t>(1);
+  LRA_CUDA(cudaMemsetAsync(small, 0, 8 * sizeof(int), ctx->stream));
+  LRA_CUDA(cudaMemsetAsync(P.bar, 0, sizeof(GridBar), ctx->stream));
+  if (P.kmax <= 0) {
+    // nothing to factor: identity permutation
+    std::vector<int64_t> id(n);
+    for (int64_t i = 0; i < n; ++i) id[i] = i + 1;
+    LRA_CUDA(cudaMemcpyAsync(jpvt, id.data(), n * sizeof(int64_t), cudaMemcpyHostToDevice,
+                             ctx->stream));
+    LRA_CUDA(cudaStreamSynchronize(ctx->stream));
+    ctx->arena.release(mark);
+    return 0;
+  }
+  void* args[] = {&P};
+  LRA_CUDA(cudaLaunchCooperativeKernel((const void*)geqp3_kernel<T, NT>, dim3(grid), dim3(NT), args,
+                                       0, ctx->stream));
+  post_launch(ctx, "geqp3_kernel");
+  int64_t k = 0;
+  GridBar hb;
+  LRA_CUDA(cudaMemcpyAsync(&k, P.k_out, sizeof(int64_t), cudaMemcpyDeviceToHost, ctx->stream));
+  LRA_CUDA(cudaMemcpyAsync(&hb, P.bar, sizeof(GridBar), cudaMemcpyDeviceToHost, ctx->stream));
+  LRA_CUDA(cudaStreamSynchronize(ctx->stream));
+  ctx->arena.release(mark);
+  if (hb.err != 0) fail(LRA_ETIMEDOUT, "geqp3: a grid barrier timed out");
+  return k;
+}
+
+template <typename T>
+void trsm_upper(lra_ctx* ctx, int64_t k, int64_t nrhs, const T* R, int64_t ldr, T* X, int64_t ldx) {
+  if (k <= 0 || nrhs <= 0) return;
+  int warps = 8;
+  while (warps > 1 && (size_t)warps * k * sizeof(T) > 160 * 1024) warps >>= 1;
+  const size_t smem = (size_t)warps * k * sizeof(T);
+  if (smem > 200 * 1024) fail(LRA_ENOTSUP, "trsm: rank %lld too large", (long long)k);
+  if (smem > 48 * 1024)
+    LRA_CUDA(cudaFuncSetAttribute(trsm_upper_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                  (int)smem));
+  const int64_t blocks = std::min<int64_t>((nrhs + warps - 1) / warps, (int64_t)ctx->num_sms * 8);
+  trsm_upper_kernel<T><<<(unsigned)blocks, warps * 32, smem, ctx->stream>>>(k, nrhs, R, ldr, X, ldx);
+  post_launch(ctx, "trsm_upper_kernel");
+}
+
+template <typename T>
+void apply_q(lra_ctx* ctx, char trans, int64_t m, int64_t k, const T* V, int64_t ldv, const T* tau,
+             T* X, int64_t ldx, int64_t nc) {
+  if (k <= 0 || nc <= 0) return;
+  const int warps = 4;
+  const int64_t blocks = std::min<int64_t>((nc + warps - 1) / warps, (int64_t)ctx->num_sms * 16);
+  apply_q_kernel<T><<<(unsigned)blocks, warps * 32, 0, ctx->stream>>>(
+      (trans == 't' || trans == 'T' || trans == 'c' || trans == 'C') ? 1 : 0, m, k, V, ldv, tau, X,
+      ldx, nc);
+  post_launch(ctx, "apply_q_kernel");
+}
+
+template <typename T>
+void orgqr(lra_ctx* ctx, int64_t m, int64_t k, T* V, int64_t ldv, const T* tau) {
+  // Q = H(0) ... H(k-1) [I; 0] built in a separate buffer, then copied back
+  const ArenaMark mark = ctx->arena.mark();
+  T* Q = ctx->arena.alloc_n<T>((size_t)m * k);
+  set_identity(ctx, m, k, Q, m);
+  apply_q(ctx, 'n', m, k, V, ldv, tau, Q, m, k);
+  copy_matrix(ctx, m, k, Q, m, V, ldv);
+  LRA_CUDA(cudaStreamSynchronize(ctx->stream));
+  ctx->arena.release(mark);
+}
+
+template <typename T>
+void col_norms(lra_ctx* ctx, int64_t m, int64_t n, const T* A, int64_t lda, T* out) {
+  if (n <= 0) return;
+  const int warps = 8;
+  const int64_t blocks = std::min<int64_t>((n + warps - 1) / warps, (int64_t)ctx->num_sms * 8);
+  col_norms_kernel<T><<<(unsigned)blocks, warps * 32, 0, ctx->stream>>>(m, n, A, lda, out);
+  post_launch(ctx, "col_norms_kernel");
+}
+
+#define INST(T)                                                                                   \
+  template int64_t geqp3_adap<T>(lra_ctx*, int64_t, int64_t, T*, int64_t, int64_t*, T*, int64_t,  \
+                                 int64_t, double, double, bool);                                 \
+  template void trsm_upper<T>(lra_ctx*, int64_t, int64_t, const T*, int64_t, T*, int64_t);       \
+  template void apply_q<T>(lra_ctx*, char, int64_t, int64_t, const T*, int64_t, const T*, T*,    \
+                           int64_t, int64_t);                                                    \
+  template void orgqr<T>(lra_ctx*, int64_t, int64_t, T*, int64_t, const T*);                      \
+  template void col_norms<T>(lra_ctx*, int64_t, int64_t, const T*, int64_t, T*);
+INST(float)
+INST(double)
+#undef INST
+
+}  // namespace lra

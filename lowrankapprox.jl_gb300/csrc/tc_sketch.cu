@@ -1,0 +1,595 @@
+// Gaussian sketch B = S op(A) on tcgen05 tensor cores, FP64-faithful, for
+// the mixed-precision path (the sketch of src/sketch.jl:91-98 and
+// sketch_randn_ln/lc, src/sketch.jl:129-174).
+//
+// Exact split products.  S is on the 1/32 lattice: S = sigma / 32 with
+// integer |sigma| <= 127, exact in BF16.  Column j of op(A) is written as a
+// W-bit fixed-point integer at a per-column power-of-two scale,
+//     op(A)(i, j) ~= F_ij 2^(e_j - W),  |op(A)(:, j)| < 2^(e_j),
+// (W = 48 for Float64, 24 for Float32) and F is cut into ns = W/8 byte
+// slices b_1 (signed, |b_1| <= 256) and b_2..b_ns (0..255), all exact in BF16.
+// Every product sigma * b is an integer below 2^15, so the FP32 sum of 512 of
+// them is an exact integer below 2^24: the tensor core loses nothing inside
+// a 512-long K chunk.  Slices 1..3 get their own TMEM accumulators; slices
+// 4..ns are pre-scaled by 2^-8(s-4) and share one FP32 tail accumulator
+// (its per-chunk rounding is ~2^-45 of the result).  All four are drained
+// after every chunk into one int64 per output,
+//     X += P1 2^24 + P2 2^16 + P3 2^8 + round(tail 2^8),
+// and B(r, j) = 2^(e_j - 37) X  (Float32: three slices, B = 2^(e_j-29) X).
+//
+// Kernel: 10 warps; warp 0 issues TMA loads (SW128, K-major) into a 2-stage
+// ring, warp 1 allocates TMEM and issues tcgen05.mma from one thread, warps
+// 2..9 drain the accumulators and write B.  Tile: 128 columns of op(A) (the
+// MMA M dimension, one TMEM lane each) x 128 sketch rows (MMA N).  Every
+// mbarrier wait is bounded by %globaltimer; a timeout records an error and
+// the kernel runs to its end, freeing TMEM.
+
+#include <cuda.h>
+#include <cuda_bf16.h>
+#include <cudaTypedefs.h>
+
+#include <algorithm>
+#include <cstring>
+
+#include "common.cuh"
+#include "internal.hpp"
+
+namespace lra {
+
+namespace {
+
+constexpr int TILE_M = 128;   // columns of op(A) per CTA
+constexpr int TILE_N = 128;   // sketch rows per CTA
+constexpr int KBLK = 64;      // K per stage (128 bytes of BF16: one SW128 row)
+constexpr int CHUNK_KB = 8;   // K-blocks per exact chunk (512)
+constexpr int NSTAGE = 2;
+constexpr int TILE_BYTES = TILE_M * KBLK * 2;  // 16 KB
+constexpr int NTHREADS = 320;
+constexpr int MAX_SLICES = 6;
+
+struct TcParams {
+  int64_t K;       // sketched dimension (rows of op(A))
+  int64_t ncols;   // columns of op(A)
+  int64_t L;       // sketch order
+  int ns;          // slices
+  const int* colexp;
+  void* B;
+  int64_t ldb;
+  int out_double;
+  int* err;
+};
+
+// ---- PTX helpers -------------------------------------------------------------
+__device__ __forceinline__ uint32_t smem_u32(const void* p) {
+  return static_cast<uint32_t>(__cvta_generic_to_shared(p));
+}
+
+__device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
+}
+
+__device__ __forceinline__ void mbar_expect_tx(uint64_t* bar, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes)
+               : "memory");
+}
+
+__device__ __forceinline__ void mbar_arrive(uint64_t* bar) {
+  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(bar)) : "memory");
+}
+
+__device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
+  uint32_t ok;
+  asm volatile(
+      "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
+      : "=r"(ok)
+      : "r"(smem_u32(bar)), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+
+// bounded wait; returns false (and records the error) on time-out
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, int* err) {
+  if (mbar_try_wait(bar, parity)) return true;
+  const uint64_t t0 = globaltimer_ns();
+  while (!mbar_try_wait(bar, parity)) {
+    if (*((volatile int*)err) != 0) return false;
+    if (globaltimer_ns() - t0 > kWaitLimitNs) {
+      atomicCAS(err, 0, 4);
+      return false;
+    }
+  }
+  return true;
+}
+
+__device__ __forceinline__ void tma_load_2d(void* dst, const CUtensorMap* tm, int x, int y, uint64_t* bar) {
+  asm volatile(
+      "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], [%4];" ::"r"(
+          smem_u32(dst)),
+      "l"(reinterpret_cast<uint64_t>(tm)), "r"(x), "r"(y), "r"(smem_u32(bar))
+      : "memory");
+}
+
+__device__ __forceinline__ void tma_load_3d(void* dst, const CUtensorMap* tm, int x, int y, int z, uint64_t* bar) {
+  asm volatile(
+      "cp.async.bulk.tensor.3d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4}], [%5];" ::"r"(
+          smem_u32(dst)),
+      "l"(reinterpret_cast<uint64_t>(tm)), "r"(x), "r"(y), "r"(z), "r"(smem_u32(bar))
+      : "memory");
+}
+
+// tcgen05 shared-memory descriptor: K-major, 128-byte swizzle, 8-row groups
+// 1024 bytes apart (SBO), version 1, base offset 0 (tiles are 1024-aligned)
+__device__ __forceinline__ uint64_t sw128_desc(uint32_t saddr) {
+  uint64_t d = 0;
+  d |= (uint64_t)((saddr & 0x3FFFF) >> 4);          // start address
+  d |= (uint64_t)1 << 16;                           // LBO (unused for SW128 K-major)
+  d |= (uint64_t)(1024 >> 4) << 32;                 // SBO
+  d |= (uint64_t)1 << 46;                           // descriptor version
+  d |= (uint64_t)2 << 61;                           // SWIZZLE_128B
+  return d;
+}
+
+// instruction descriptor, kind::f16: BF16 x BF16 -> FP32, K-major A and B
+__host__ __device__ constexpr uint32_t idesc_bf16(int M, int N) {
+  return (1u << 4)                        // D format F32
+         | (1u << 7)                      // A format BF16
+         | (1u << 10)                     // B format BF16
+         | ((uint32_t)(N >> 3) << 17)     // N / 8
+         | ((uint32_t)(M >> 4) << 24);    // M / 16
+}
+
+__device__ __forceinline__ void mma_bf16(uint32_t d_tmem, uint64_t adesc, uint64_t bdesc, uint32_t idesc,
+                                         uint32_t accumulate) {
+  asm volatile(
+      "{\n .reg .pred p;\n setp.ne.u32 p, %4, 0;\n"
+      " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(d_tmem),
+      "l"(adesc), "l"(bdesc), "r"(idesc), "r"(accumulate)
+      : "memory");
+}
+
+__device__ __forceinline__ void mma_commit(uint64_t* bar) {
+  asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(smem_u32(bar))
+               : "memory");
+}
+
+__device__ __forceinline__ void tmem_ld32(uint32_t taddr, uint32_t (&r)[32]) {
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,"
+      "%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];"
+      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]), "=r"(r[8]),
+        "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15]), "=r"(r[16]),
+        "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]), "=r"(r[24]),
+        "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
+      : "r"(taddr));
+  asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+}
+
+__device__ __forceinline__ void tc_fence_before() {
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+}
+__device__ __forceinline__ void tc_fence_after() {
+  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+}
+
+// ---- the sketch kernel ----------------------------------------------------------
+__global__ void __launch_bounds__(NTHREADS, 1)
+    tc_sketch_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmS,
+                     TcParams P) {
+  extern __shared__ __align__(1024) unsigned char smem_raw[];
+  // 1024-align the tile area
+  unsigned char* base = reinterpret_cast<unsigned char*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
+  const int ns = P.ns;
+  const int stage_bytes = (1 + ns) * TILE_BYTES;
+  unsigned char* stages = base;
+  uint64_t* full = reinterpret_cast<uint64_t*>(base + NSTAGE * stage_bytes);
+  uint64_t* empty = full + NSTAGE;
+  uint64_t* acc_ready = empty + NSTAGE;
+  uint64_t* acc_free = acc_ready + 1;
+  uint64_t* mma_done = acc_free + 1;
+  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(mma_done + 1);
+
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int64_t ntl = (P.L + TILE_N - 1) / TILE_N;
+  const int64_t n_tile = blockIdx.x / ntl, l_tile = blockIdx.x % ntl;
+  const int nkb = (int)((P.K + KBLK - 1) / KBLK);
+  const int nchunks = (nkb + CHUNK_KB - 1) / CHUNK_KB;
+  const int n_exact = ns < 3 ? ns : 3;
+  const bool has_tail = ns > 3;
+  const int n_acc = n_exact + (has_tail ? 1 : 0);
+
+  if (threadIdx.x == 0) {
+    for (int s = 0; s < NSTAGE; ++s) {
+      mbar_init(full + s, 1);
+      mbar_init(empty + s, 1);
+    }
+    mbar_init(acc_ready, 1);
+    mbar_init(acc_free, 8);  // one arrival per drain warp
+    mbar_init(mma_done, 1);
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  if (warp == 1) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], 512;" ::"r"(smem_u32(tmem_slot))
+                 : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+  }
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  const uint32_t tmem = *tmem_slot;
+
+  if (warp == 0) {
+    // ---------------- TMA producer ----------------
+    if (lane == 0) {
+      int issued = 0;
+      for (int kb = 0; kb < nkb; ++kb) {
+        const int s = kb % NSTAGE;
+        const uint32_t ph = (kb / NSTAGE) & 1;
+        if (!mbar_wait(empty + s, ph ^ 1, P.err)) break;
+        ++issued;
+        unsigned char* st = stages + s * stage_bytes;
+        mbar_expect_tx(full + s, (uint32_t)stage_bytes);
+        tma_load_2d(st, &tmS, kb * KBLK, (int)(l_tile * TILE_N), full + s);
+        for (int q = 0; q < ns; ++q)
+          tma_load_3d(st + (1 + q) * TILE_BYTES, &tmA, kb * KBLK, (int)(n_tile * TILE_M), q, full + s);
+      }
+      // no copy may still be landing in shared memory when the CTA exits
+      int dummy = 0;
+      for (int kb = issued - NSTAGE; kb < issued; ++kb)
+        if (kb >= 0) mbar_wait(full + kb % NSTAGE, (kb / NSTAGE) & 1, &dummy);
+    }
+  } else if (warp == 1) {
+    // ---------------- MMA issuer ----------------
+    if (lane == 0) {
+      constexpr uint32_t idesc = idesc_bf16(TILE_M, TILE_N);
+      bool ok = true;
+      for (int kb = 0; kb < nkb && ok; ++kb) {
+        const int chunk = kb / CHUNK_KB;
+        const bool chunk_start = (kb % CHUNK_KB) == 0;
+        if (chunk_start && chunk > 0) {
+          // the drain of the previous chunk must be done before overwriting
+          if (!mbar_wait(acc_free, (chunk - 1) & 1, P.err)) {
+            ok = false;
+            break;
+          }
+          tc_fence_after();
+        }
+        const int s = kb % NSTAGE;
+        const uint32_t ph = (kb / NSTAGE) & 1;
+        if (!mbar_wait(full + s, ph, P.err)) {
+          ok = false;
+          break;
+        }
+        tc_fence_after();
+        const uint32_t st = smem_u32(stages + s * stage_bytes);
+        for (int q = 0; q < ns; ++q) {
+          const uint32_t acc = q < 3 ? tmem + (uint32_t)(q * TILE_N) : tmem + 3u * TILE_N;
+          const uint32_t a_addr = st + (uint32_t)((1 + q) * TILE_BYTES);
+#pragma unroll
+          for (int k4 = 0; k4 < KBLK / 16; ++k4) {
+            const uint64_t ad = sw128_desc(a_addr + k4 * 32);
+            const uint64_t bd = sw128_desc(st + k4 * 32);
+            // every accumulator restarts at each chunk; the tail slices
+            // (q >= 3) share one, reset by the first of them
+            const bool first = chunk_start && k4 == 0 && (q < 3 || q == 3);
+            const uint32_t accumulate = first ? 0u : 1u;
+            mma_bf16(acc, ad, bd, idesc, accumulate);
+          }
+        }
+        mma_commit(empty + s);  // frees the stage once these MMAs complete
+        if ((kb % CHUNK_KB) == CHUNK_KB - 1 || kb == nkb - 1) mma_commit(acc_ready);
+      }
+      // every issued MMA has completed before TMEM is released
+      mma_commit(mma_done);
+      int dummy = 0;
+      mbar_wait(mma_done, 0, &dummy);
+    }
+  } else {
+    // ---------------- drain / epilogue: warps 2..9 ----------------
+    const int q4 = warp & 3;          // TMEM lane quarter this warp may access
+    const int half = (warp - 2) >> 2;  // which 64 of the 128 sketch rows
+    const uint32_t lane_base = (uint32_t)(32 * q4) << 16;
+    long long X[64];
+#pragma unroll
+    for (int c = 0; c < 64; ++c) X[c] = 0;
+    bool ok = true;
+    for (int ch = 0; ch < nchunks; ++ch) {
+      if (!mbar_wait(acc_ready, ch & 1, P.err)) {
+        ok = false;
+        break;
+      }
+      tc_fence_after();
+      // X += P1 2^(8(E-1)+t) + ... + P_E 2^t + round(tail 2^8), t = 8 with a tail
+      for (int a = 0; a < n_acc; ++a) {
+        const int sh = 8 * (n_exact - 1 - a) + (has_tail ? 8 : 0);
+#pragma unroll
+        for (int piece = 0; piece < 2; ++piece) {
+          uint32_t r[32];
+          tmem_ld32(tmem + lane_base + (uint32_t)(a * TILE_N + half * 64 + piece * 32), r);
+          if (a < n_exact) {
+#pragma unroll
+            for (int c = 0; c < 32; ++c) {
+              const int iv = __float2int_rz(__uint_as_float(r[c]));
+              X[piece * 32 + c] += (long long)iv << sh;
+            }
+          } else {
+#pragma unroll
+            for (int c = 0; c < 32; ++c) X[piece * 32 + c] += __float2ll_rn(__uint_as_float(r[c]) * 256.0f);
+          }
+        }
+      }
+      tc_fence_before();
+      __syncwarp();
+      if (lane == 0) mbar_arrive(acc_free);
+    }
+    // epilogue: scale + store
+    const int64_t j = n_tile * TILE_M + 32 * q4 + lane;  // column of op(A) / B
+    const int e = (ok && j < P.ncols) ? P.colexp[j] : 0;
+    // B = 2^(e - 5 - 8 E - t) X,  E = exact slices, t = 8 with a tail
+    const int sc = e - 5 - 8 * n_exact - (has_tail ? 8 : 0);
+    const int64_t r0 = l_tile * TILE_N + half * 64;
+    if (ok && j < P.ncols) {
+#pragma unroll
+      for (int c = 0; c < 64; ++c) {
+        const int64_t row = r0 + c;
+        if (row < P.L) {
+          const double v = ldexp((double)X[c], sc);
+          if (P.out_double)
+            static_cast<double*>(P.B)[row + j * P.ldb] = v;
+          else
+            static_cast<float*>(P.B)[row + j * P.ldb] = (float)v;
+        }
+      }
+    }
+  }
+
+  tc_fence_before();
+  __syncthreads();
+  if (warp == 1) {
+    tc_fence_after();
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, 512;" ::"r"(tmem) : "memory");
+  }
+}
+
+// ---- splitting op(A) into byte slices ---------------------------------------------
+
+// per-column exponent e_j with max |op(A)(:, j)| < 2^e_j
+template <typename T>
+__global__ void colexp_n_kernel(int64_t K, int64_t N, const T* __restrict__ A, int64_t lda, int* e) {
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  const int nw = blockDim.x >> 5;
+  for (int64_t j = (int64_t)blockIdx.x * nw + wid; j < N; j += (int64_t)gridDim.x * nw) {
+    double mx = 0;
+    for (int64_t i = lane; i < K; i += 32) mx = fmax(mx, fabs((double)A[i + j * lda]));
+    mx = warp_max(mx);
+    if (lane == 0) e[j] = mx > 0 ? ilogb(mx) + 1 : 0;
+  }
+}
+
+// op(A) = A^T: column j of op(A) is row j of A
+template <typename T>
+__global__ void colexp_c_kernel(int64_t K, int64_t N, const T* __restrict__ A, int64_t lda, int* e) {
+  for (int64_t j = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; j < N; j += (int64_t)gridDim.x * blockDim.x) {
+    double mx = 0;
+    for (int64_t i = 0; i < K; ++i) mx = fmax(mx, fabs((double)A[j + i * lda]));
+    e[j] = mx > 0 ? ilogb(mx) + 1 : 0;
+  }
+}
+
+// fixed-point integer of x at scale 2^(e - W) (round half up), from the bits
+__device__ __forceinline__ long long fixed_point(double x, int e, int W) {
+  const unsigned long long bits = (unsigned long long)__double_as_longlong(x);
+  const int ex = (int)((bits >> 52) & 0x7FF);
+  unsigned long long mant = bits & ((1ull << 52) - 1);
+  if (ex == 0 && mant == 0) return 0;
+  if (ex != 0) mant |= 1ull << 52;
+  const int e2 = (ex == 0 ? 1 : ex) - 1075;  // x = mant 2^e2
+  const int sh = e2 + W - e;                  // F = mant 2^sh, sh < 0 here
+  long long F;
+  if (sh >= 0) {
+    F = (long long)(mant << sh);
+  } else if (-sh >= 64) {
+    F = 0;
+  } else {
+    const int r = -sh;
+    F = (long long)((mant + (1ull << (r - 1))) >> r);
+  }
+  return (bits >> 63) ? -F : F;
+}
+
+__device__ __forceinline__ long long fixed_point(float x, int e, int W) { return fixed_point((double)x, e, W); }
+
+// exact BF16 of an integer b in [-256, 256], times 2^-8k
+__device__ __forceinline__ __nv_bfloat16 bf16_of(int b, int k) {
+  float f = __int_as_float(0x4B000000 | (b + 256)) - 8388864.0f;  // exact: 2^23 + 256
+  if (k) f *= __int_as_float((127 - 8 * k) << 23);
+  return __ushort_as_bfloat16((unsigned short)(__float_as_uint(f) >> 16));
+}
+
+template <typename T>
+__device__ __forceinline__ void write_slices(long long F, int ns, int W, __nv_bfloat16* out, int64_t plane) {
+  const int n_exact = ns < 3 ? ns : 3;
+#pragma unroll
+  for (int s = 1; s <= MAX_SLICES; ++s) {
+    if (s > ns) break;
+    const int shift = W - 8 * s;
+    int b = (s == 1) ? (int)(F >> shift) : (int)((F >> shift) & 255);
+    const int k = s > n_exact ? (s - n_exact - 1) : 0;
+    out[(s - 1) * plane] = bf16_of(b, k);
+  }
+}
+
+template <typename T>
+__global__ void split_n_kernel(int64_t K, int64_t N, const T* __restrict__ A, int64_t lda, const int* __restrict__ e,
+                               int ns, int W, __nv_bfloat16* __restrict__ S, int64_t Kp) {
+  const int64_t total = Kp * N;
+  const int64_t plane = Kp * N;
+  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < total; t += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t i = t % Kp, j = t / Kp;
+    const long long F = i < K ? fixed_point(A[i + j * lda], e[j], W) : 0;
+    write_slices<T>(F, ns, W, S + i + j * Kp, plane);
+  }
+}
+
+// op(A) = A^T through 32 x 32 shared-memory tiles
+template <typename T>
+__global__ void split_c_kernel(int64_t K, int64_t N, const T* __restrict__ A, int64_t lda, const int* __restrict__ e,
+                               int ns, int W, __nv_bfloat16* __restrict__ S, int64_t Kp) {
+  __shared__ T tile[32][33];
+  const int64_t plane = Kp * N;
+  const int64_t ti = (Kp + 31) / 32, tj = (N + 31) / 32;
+  for (int64_t t = blockIdx.x; t < ti * tj; t += gridDim.x) {
+    const int64_t i0 = (t % ti) * 32, j0 = (t / ti) * 32;
+    for (int r = threadIdx.y; r < 32; r += blockDim.y) {
+      const int64_t j = j0 + threadIdx.x, i = i0 + r;  // A(j, i) contiguous in j
+      tile[r][threadIdx.x] = (i < K && j < N) ? A[j + i * lda] : T(0);
+    }
+    __syncthreads();
+    for (int r = threadIdx.y; r < 32; r += blockDim.y) {
+      const int64_t i = i0 + threadIdx.x, j = j0 + r;
+      if (i < Kp && j < N) {
+        const long long F = fixed_point(tile[threadIdx.x][r], e[j], W);
+        write_slices<T>(F, ns, W, S + i + j * Kp, plane);
+      }
+    }
+    __syncthreads();
+  }
+}
+
+// St (Kp x Lp, K-major: St[i + r Kp]) = 32 S(r, i) in BF16, zero padded
+template <typename T>
+__global__ void sketch_t_kernel(int64_t L, int64_t K, const T* __restrict__ S, int64_t Lp, int64_t Kp,
+                                __nv_bfloat16* __restrict__ St) {
+  __shared__ T tile[32][33];
+  const int64_t tr = (Lp + 31) / 32, tk = (Kp + 31) / 32;
+  for (int64_t t = blockIdx.x; t < tr * tk; t += gridDim.x) {
+    const int64_t r0 = (t % tr) * 32, i0 = (t / tr) * 32;
+    for (int c = threadIdx.y; c < 32; c += blockDim.y) {
+      const int64_t r = r0 + threadIdx.x, i = i0 + c;  // S(r, i) contiguous in r
+      tile[c][threadIdx.x] = (r < L && i < K) ? S[r + i * L] : T(0);
+    }
+    __syncthreads();
+    for (int c = threadIdx.y; c < 32; c += blockDim.y) {
+      const int64_t i = i0 + threadIdx.x, r = r0 + c;
+      if (i < Kp && r < Lp) St[i + r * Kp] = __float2bfloat16_rn((float)(tile[threadIdx.x][c] * T(32)));
+    }
+    __syncthreads();
+  }
+}
+
+PFN_cuTensorMapEncodeTiled_v12000 encode_fn() {
+  static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
+  if (!fn) {
+    cudaDriverEntryPointQueryResult q;
+    void* p = nullptr;
+    check_cuda(cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q),
+               "cudaGetDriverEntryPoint(cuTensorMapEncodeTiled)");
+    if (q != cudaDriverEntryPointSuccess || !p) fail(LRA_ECUDA, "cuTensorMapEncodeTiled unavailable");
+    fn = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(p);
+  }
+  return fn;
+}
+
+void make_map(CUtensorMap* m, void* ptr, int rank, const cuuint64_t* dims, const cuuint64_t* strides,
+              const cuuint32_t* box) {
+  cuuint32_t es[3] = {1, 1, 1};
+  CUresult r = encode_fn()(m, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, (cuuint32_t)rank, ptr, dims, strides, box, es,
+                           CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B,
+                           CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  if (r != CUDA_SUCCESS) fail(LRA_ECUDA, "cuTensorMapEncodeTiled failed (%d)", (int)r);
+}
+
+inline unsigned nblk(lra_ctx* ctx, int64_t n, int t) {
+  return (unsigned)std::max<int64_t>(1, std::min<int64_t>((n + t - 1) / t, (int64_t)ctx->num_sms * 16));
+}
+
+}  // namespace
+
+bool tc_sketch_supported(int64_t order, int64_t M, int64_t N) {
+  // K extent and counts kept inside int32 TMA coordinates
+  return order > 0 && M > 0 && N > 0 && M < (1ll << 30) && N < (1ll << 30) && order < (1ll << 20);
+}
+
+template <typename T>
+void tc_split(lra_ctx* ctx, char trans, int64_t M, int64_t N, const T* A, int64_t lda, int ns, TcSplit* out) {
+  const int W = 8 * ns;
+  const int64_t Kp = (M + 7) / 8 * 8;
+  out->K = M;
+  out->N = N;
+  out->Kp = Kp;
+  out->ns = ns;
+  out->trans = trans;
+  out->colexp = ctx->arena.alloc_n<int>(std::max<int64_t>(N, 1));
+  out->slices = ctx->arena.alloc_n<__nv_bfloat16>((size_t)ns * Kp * std::max<int64_t>(N, 1));
+  if (trans == 'c') {
+    colexp_c_kernel<T><<<nblk(ctx, N, 256), 256, 0, ctx->stream>>>(M, N, A, lda, out->colexp);
+    post_launch(ctx, "colexp_c_kernel");
+    const int64_t tiles = ((Kp + 31) / 32) * ((N + 31) / 32);
+    split_c_kernel<T><<<(unsigned)std::min<int64_t>(tiles, (int64_t)ctx->num_sms * 16), dim3(32, 8), 0,
+                        ctx->stream>>>(M, N, A, lda, out->colexp, ns, W,
+                                       static_cast<__nv_bfloat16*>(out->slices), Kp);
+    post_launch(ctx, "split_c_kernel");
+  } else {
+    colexp_n_kernel<T><<<nblk(ctx, N, 8), 256, 0, ctx->stream>>>(M, N, A, lda, out->colexp);
+    post_launch(ctx, "colexp_n_kernel");
+    split_n_kernel<T><<<nblk(ctx, Kp * N, 256), 256, 0, ctx->stream>>>(
+        M, N, A, lda, out->colexp, ns, W, static_cast<__nv_bfloat16*>(out->slices), Kp);
+    post_launch(ctx, "split_n_kernel");
+  }
+}
+
+template <typename T>
+void tc_sketch(lra_ctx* ctx, const TcSplit& sp, int64_t order, const T* S, T* B, int64_t ldb) {
+  const int64_t K = sp.K, N = sp.N, Kp = sp.Kp;
+  const int ns = sp.ns;
+  const int64_t Lp = (order + TILE_N - 1) / TILE_N * TILE_N;
+  const ArenaMark mk = ctx->arena.mark();
+  __nv_bfloat16* St = ctx->arena.alloc_n<__nv_bfloat16>((size_t)Kp * Lp);
+  {
+    const int64_t tiles = ((Lp + 31) / 32) * ((Kp + 31) / 32);
+    sketch_t_kernel<T><<<(unsigned)std::min<int64_t>(tiles, (int64_t)ctx->num_sms * 16), dim3(32, 8), 0,
+                         ctx->stream>>>(order, K, S, Lp, Kp, St);
+    post_launch(ctx, "sketch_t_kernel");
+  }
+  CUtensorMap tmA, tmS;
+  {
+    cuuint64_t dims[3] = {(cuuint64_t)Kp, (cuuint64_t)N, (cuuint64_t)ns};
+    cuuint64_t strides[2] = {(cuuint64_t)Kp * 2, (cuuint64_t)Kp * N * 2};
+    cuuint32_t box[3] = {KBLK, TILE_M, 1};
+    make_map(&tmA, sp.slices, 3, dims, strides, box);
+  }
+  {
+    cuuint64_t dims[2] = {(cuuint64_t)Kp, (cuuint64_t)Lp};
+    cuuint64_t strides[1] = {(cuuint64_t)Kp * 2};
+    cuuint32_t box[2] = {KBLK, TILE_N};
+    make_map(&tmS, St, 2, dims, strides, box);
+  }
+  int* err = ctx->arena.alloc_n<int>(1);
+  LRA_CUDA(cudaMemsetAsync(err, 0, sizeof(int), ctx->stream));
+  TcParams P;
+  P.K = K;
+  P.ncols = N;
+  P.L = order;
+  P.ns = ns;
+  P.colexp = sp.colexp;
+  P.B = B;
+  P.ldb = ldb;
+  P.out_double = sizeof(T) == 8 ? 1 : 0;
+  P.err = err;
+  const size_t smem = 1024 + (size_t)NSTAGE * (1 + ns) * TILE_BYTES + 256;
+  LRA_CUDA(cudaFuncSetAttribute(tc_sketch_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  const int64_t ntiles = ((N + TILE_M - 1) / TILE_M) * (Lp / TILE_N);
+  tc_sketch_kernel<<<(unsigned)ntiles, NTHREADS, smem, ctx->stream>>>(tmA, tmS, P);
+  post_launch(ctx, "tc_sketch_kernel");
+  int herr = 0;
+  LRA_CUDA(cudaMemcpyAsync(&herr, err, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+  LRA_CUDA(cudaStreamSynchronize(ctx->stream));
+  ctx->arena.release(mk);
+  if (herr) fail(LRA_ETIMEDOUT, "tc_sketch: a bounded wait timed out");
+}
+
+template void tc_split<float>(lra_ctx*, char, int64_t, int64_t, const float*, int64_t, int, TcSplit*);
+template void tc_split<double>(lra_ctx*, char, int64_t, int64_t, const double*, int64_t, int, TcSplit*);
+template void tc_sketch<float>(lra_ctx*, const TcSplit&, int64_t, const float*, float*, int64_t);
+template void tc_sketch<double>(lra_ctx*, const TcSplit&, int64_t, const double*, double*, int64_t);
+
+}  // namespace lra

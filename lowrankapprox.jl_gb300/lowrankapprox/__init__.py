@@ -1,0 +1,687 @@
+"""LowRankApprox.jl's sketch-then-factor API on the GB300 engine (liblra).
+
+The names, arguments and result types mirror the Julia package
+(src/LowRankApprox.jl:27-73): ``LRAOptions``, ``idfact`` / ``id``,
+``pqrfact`` / ``pqr``, ``psvdfact`` / ``psvdvals`` / ``psvd``,
+``pheigfact`` / ``pheigvals`` / ``pheig``, ``curfact`` / ``cur``,
+``sketch`` / ``sketchfact``, ``snorm`` / ``snormdiff``, ``matrixlib``.
+Every call goes through the C ABI of liblra (include/lra.h) -- the same
+entry points a Julia ``ccall`` shim binds -- and runs on the GPU.
+
+Matrices are numpy arrays (host) or column-major torch CUDA tensors
+(device); index outputs are 1-based like Julia's.
+"""
+from __future__ import annotations
+
+import ctypes as C
+from dataclasses import dataclass
+
+import numpy as np
+
+from . import _ffi
+from ._ffi import LRA_F32, LRA_F64
+
+__all__ = [
+    "LRAOptions", "RandStream", "Context", "IDPackedV", "PartialQRFactors", "PartialQR", "PartialSVD",
+    "PartialHermitianEigen", "CURPackedU", "idfact", "id", "pqrfact", "pqr", "psvdfact", "psvdvals",
+    "psvd", "pheigfact", "pheigvals", "pheig", "curfact", "cur", "sketch", "sketchfact", "snorm",
+    "snormdiff", "geqp3_adap", "matrixlib", "LRAError", "ArgumentError", "DimensionMismatch",
+    "lattice_gauss", "default_context",
+]
+
+
+# ---------------------------------------------------------------------------
+# errors (the Julia shim maps the same statuses to Julia exceptions)
+# ---------------------------------------------------------------------------
+
+class LRAError(RuntimeError):
+    def __init__(self, status: int, msg: str):
+        super().__init__(f"{msg} (status {status})")
+        self.status = status
+
+
+class ArgumentError(LRAError, ValueError):
+    pass
+
+
+class DimensionMismatch(LRAError, ValueError):
+    pass
+
+
+def _raise(status: int, ctx) -> None:
+    if status == _ffi.LRA_OK:
+        return
+    lib = _ffi.load()
+    msg = (lib.lra_last_error(ctx.handle) if ctx is not None else b"").decode() or \
+        lib.lra_status_string(status).decode()
+    if status in (_ffi.LRA_EINVAL, _ffi.LRA_ENOTHERM, _ffi.LRA_ENONFINITE):
+        raise ArgumentError(status, msg)
+    if status == _ffi.LRA_EDIM:
+        raise DimensionMismatch(status, msg)
+    raise LRAError(status, msg)
+
+
+# ---------------------------------------------------------------------------
+# options (src/LowRankApprox.jl:77-148)
+# ---------------------------------------------------------------------------
+
+class LRAOptions:
+    """Mirror of LRAOptions; ``*_samp`` take (a, b) for n -> a n + b."""
+
+    _fields = ("atol", "maxdet_niter", "maxdet_tol", "nb", "pheig_orthtol", "pqrfact_retval", "rank",
+               "rtol", "sketch", "sketch_randn_niter", "sketchfact_adap", "sketchfact_randn_samp",
+               "sketchfact_srft_samp", "sketchfact_sub_samp", "snorm_niter", "verb", "precision", "seed",
+               "check_finite")
+
+    def __init__(self, T=np.float64, **kwargs):
+        eps = float(np.finfo(np.dtype(T)).eps)
+        self.atol = 0.0
+        self.maxdet_niter = -1
+        self.maxdet_tol = -1.0
+        self.nb = 32
+        self.pheig_orthtol = float(np.sqrt(eps))
+        self.pqrfact_retval = "qr"
+        self.rank = -1
+        self.rtol = 5 * eps
+        self.sketch = "randn"
+        self.sketch_randn_niter = 0
+        self.sketchfact_adap = True
+        self.sketchfact_randn_samp = (1, 8)
+        self.sketchfact_srft_samp = (1, 8)
+        self.sketchfact_sub_samp = (4, 8)
+        self.snorm_niter = 32
+        self.verb = True
+        self.precision = "native"
+        self.seed = 0x4C5241
+        self.check_finite = True
+        for k, v in kwargs.items():
+            self._set(k, v)
+
+    def _set(self, k, v):
+        if k == "sketch" and v == "subs":
+            v = "sub"
+        if k not in self._fields:
+            raise ArgumentError(_ffi.LRA_EINVAL, f"unknown option {k}")
+        setattr(self, k, v)
+
+    def copy(self, **kwargs) -> "LRAOptions":
+        o = LRAOptions.__new__(LRAOptions)
+        o.__dict__.update(self.__dict__)
+        for k, v in kwargs.items():
+            o._set(k, v)
+        return o
+
+    def to_c(self) -> _ffi.lra_opts:
+        c = _ffi.lra_opts()
+        c.atol = float(self.atol)
+        c.maxdet_niter = int(self.maxdet_niter)
+        c.maxdet_tol = float(self.maxdet_tol)
+        c.nb = int(self.nb)
+        c.pheig_orthtol = float(self.pheig_orthtol)
+        rv = str(self.pqrfact_retval).lower()
+        c.pqrfact_retval = (_ffi.RET_Q if "q" in rv else 0) | (_ffi.RET_R if "r" in rv else 0) | \
+            (_ffi.RET_T if "t" in rv else 0)
+        if self.sketch not in _ffi.SKETCH:
+            raise ArgumentError(_ffi.LRA_EINVAL, "sketch")
+        c.sketch = _ffi.SKETCH[self.sketch]
+        c.rank = int(self.rank)
+        c.rtol = float(self.rtol)
+        c.sketch_randn_niter = int(self.sketch_randn_niter)
+        c.sketchfact_adap = 1 if self.sketchfact_adap else 0
+        c.verb = 1 if self.verb else 0
+        for name in ("sketchfact_randn_samp", "sketchfact_srft_samp", "sketchfact_sub_samp"):
+            a, b = getattr(self, name)
+            arr = getattr(c, name)
+            arr[0], arr[1] = int(a), int(b)
+        c.snorm_niter = int(self.snorm_niter)
+        if self.precision not in _ffi.PREC:
+            raise ArgumentError(_ffi.LRA_EINVAL, "precision")
+        c.precision = _ffi.PREC[self.precision]
+        c.check_finite = 1 if self.check_finite else 0
+        c.seed = int(self.seed) & 0xFFFFFFFFFFFFFFFF
+        return c
+
+
+def lattice_gauss(rng_or_seed, n: int) -> np.ndarray:
+    """N(0,1) draws rounded to the 1/32 lattice, clipped to +-127/32: the
+    sketch entries the mixed-precision path multiplies exactly."""
+    rng = np.random.default_rng(rng_or_seed) if not isinstance(rng_or_seed, np.random.Generator) \
+        else rng_or_seed
+    return np.clip(np.rint(rng.standard_normal(n) * 32.0), -127, 127) / 32.0
+
+
+class RandStream:
+    """Injected random numbers (lra_rand): a float64 Gaussian stream and an
+    int64 index stream, host numpy arrays or CUDA tensors."""
+
+    def __init__(self, gauss=None, ints=None):
+        self._keep = []
+        self.c = _ffi.lra_rand()
+        if gauss is not None:
+            p, n = self._ptr(gauss, np.float64)
+            self.c.gauss, self.c.gauss_len = p, n
+        if ints is not None:
+            p, n = self._ptr(ints, np.int64)
+            self.c.ints, self.c.ints_len = p, n
+
+    def _ptr(self, a, dt):
+        if _is_torch(a):
+            import torch
+            want = torch.float64 if dt == np.float64 else torch.int64
+            if a.dtype != want or not a.is_contiguous():
+                a = a.to(want).contiguous()
+            self._keep.append(a)
+            return a.data_ptr(), a.numel()
+        a = np.ascontiguousarray(a, dtype=dt)
+        self._keep.append(a)
+        return a.ctypes.data, a.size
+
+
+# ---------------------------------------------------------------------------
+# context and matrix arguments
+# ---------------------------------------------------------------------------
+
+class Context:
+    """An lra_ctx: one CUDA stream, a workspace arena, stage timers."""
+
+    def __init__(self, device: int = 0):
+        lib = _ffi.load()
+        h = C.c_void_p()
+        st = lib.lra_ctx_create(int(device), C.byref(h))
+        if st != _ffi.LRA_OK:
+            raise LRAError(st, f"lra_ctx_create: {lib.lra_status_string(st).decode()}")
+        self.handle = h
+        self.device = device
+
+    def close(self):
+        if getattr(self, "handle", None):
+            _ffi.load().lra_ctx_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    @property
+    def launches(self) -> int:
+        return int(_ffi.load().lra_ctx_launches(self.handle))
+
+    def stage_ms(self):
+        out = (C.c_double * 4)()
+        _ffi.load().lra_ctx_stage_ms(self.handle, out)
+        return {"sketch": out[0], "qr": out[1], "solve": out[2], "post": out[3]}
+
+    def set_stream(self, stream_ptr: int):
+        _raise(_ffi.load().lra_ctx_set_stream(self.handle, C.c_void_p(stream_ptr)), self)
+
+
+_DEFAULT = None
+
+
+def default_context() -> Context:
+    global _DEFAULT
+    if _DEFAULT is None:
+        _DEFAULT = Context(0)
+    return _DEFAULT
+
+
+def _is_torch(a) -> bool:
+    return type(a).__module__.startswith("torch")
+
+
+@dataclass
+class _Mat:
+    ptr: int
+    m: int
+    n: int
+    ld: int
+    dtype: int
+    np_dtype: type
+    keep: object
+
+
+def _mat(A) -> _Mat:
+    if _is_torch(A):
+        import torch
+        if A.dim() != 2:
+            raise DimensionMismatch(_ffi.LRA_EDIM, "matrix expected")
+        if A.dtype not in (torch.float32, torch.float64):
+            raise ArgumentError(_ffi.LRA_EINVAL, "Float32 or Float64 matrix expected")
+        if not A.is_cuda:
+            return _mat(A.numpy())
+        m, n = A.shape
+        if not (A.stride(0) == 1 and A.stride(1) >= max(1, m)):
+            A = A.t().contiguous().t()
+        dt = LRA_F64 if A.dtype == torch.float64 else LRA_F32
+        return _Mat(A.data_ptr(), m, n, max(A.stride(1), 1), dt,
+                    np.float64 if dt == LRA_F64 else np.float32, A)
+    A = np.asarray(A)
+    if A.ndim != 2:
+        raise DimensionMismatch(_ffi.LRA_EDIM, "matrix expected")
+    if A.dtype not in (np.float32, np.float64):
+        if np.iscomplexobj(A):
+            raise ArgumentError(_ffi.LRA_ENOTSUP, "complex element types are not built")
+        A = A.astype(np.float64)
+    A = np.asfortranarray(A)
+    m, n = A.shape
+    dt = LRA_F64 if A.dtype == np.float64 else LRA_F32
+    return _Mat(A.ctypes.data, m, n, max(m, 1), dt, A.dtype.type, A)
+
+
+def _host(ptr, shape, dtype, order="F") -> np.ndarray:
+    count = int(np.prod(shape)) if len(shape) else 1
+    if count == 0 or not ptr:
+        return np.zeros(shape, dtype=dtype, order=order)
+    ct = C.c_double if dtype == np.float64 else (C.c_float if dtype == np.float32 else C.c_int64)
+    buf = (ct * count).from_address(int(ptr) if not isinstance(ptr, int) else ptr)
+    return np.array(np.frombuffer(buf, dtype=dtype, count=count).reshape(shape, order=order), copy=True)
+
+
+def _iptr(p) -> int:
+    return C.cast(p, C.c_void_p).value or 0
+
+
+def _args(args, kwargs, default_trans="n"):
+    """Julia-style (trans, A, opts) / (A, opts) positional forms."""
+    args = list(args)
+    trans = default_trans
+    if args and isinstance(args[0], str):
+        trans = args.pop(0)
+    if not args:
+        raise ArgumentError(_ffi.LRA_EINVAL, "matrix argument missing")
+    A = args.pop(0)
+    opts = args.pop(0) if args and isinstance(args[0], LRAOptions) else None
+    ctx = kwargs.pop("ctx", None) or default_context()
+    rand = kwargs.pop("rand", None)
+    M = _mat(A)
+    opts = (opts or LRAOptions(M.np_dtype)).copy(**kwargs) if (opts is None or kwargs) else opts
+    if trans not in ("n", "c", "t"):
+        raise ArgumentError(_ffi.LRA_EINVAL, "trans")
+    return trans, M, opts, ctx, rand
+
+
+def _rand(rand):
+    return C.byref(rand.c) if rand is not None else None
+
+
+# ---------------------------------------------------------------------------
+# result types
+# ---------------------------------------------------------------------------
+
+class IDPackedV:
+    """IDPackedV (src/id.jl:15-92): A[:, rd] ~= A[:, sk] * T."""
+
+    def __init__(self, sk, rd, T, nsteps=0):
+        self.sk, self.rd, self.T, self.nsteps = sk, rd, T, nsteps
+
+    @property
+    def k(self) -> int:
+        return len(self.sk)
+
+    @property
+    def p(self) -> np.ndarray:
+        return np.concatenate([self.sk, self.rd])
+
+    def __getitem__(self, d):
+        return {"k": self.k, "sk": self.sk, "rd": self.rd, "T": self.T, "p": self.p, "P": self.p}[d]
+
+    def matrix(self) -> np.ndarray:
+        """Matrix(V) = [I T] P' (k x n)."""
+        n = self.k + len(self.rd)
+        out = np.zeros((self.k, n), self.T.dtype)
+        out[:, self.sk - 1] = np.eye(self.k, dtype=self.T.dtype)
+        if len(self.rd):
+            out[:, self.rd - 1] = self.T
+        return out
+
+
+class PartialQRFactors:
+    """PartialQRFactors (src/pqr.jl:14-32)."""
+
+    def __init__(self, Q, R, p, k, T):
+        self.Q, self.R, self.p, self.k, self.T = Q, R, p, k, T
+
+    def __getitem__(self, d):
+        return {"Q": self.Q, "R": self.R, "p": self.p, "P": self.p, "k": self.k, "T": self.T}[d]
+
+
+class PartialQR(PartialQRFactors):
+    """PartialQR (src/pqr.jl:36-40): A[:, p] ~= Q R."""
+
+    def matrix(self) -> np.ndarray:
+        out = np.zeros((self.Q.shape[0], self.R.shape[1]), self.Q.dtype)
+        out[:, self.p - 1] = self.Q @ self.R
+        return out
+
+
+class PartialSVD:
+    """PartialSVD (src/psvd.jl:4-16): A ~= U diagm(S) Vt."""
+
+    def __init__(self, U, S, Vt):
+        self.U, self.S, self.Vt = U, S, Vt
+
+    @property
+    def k(self) -> int:
+        return len(self.S)
+
+    def __getitem__(self, d):
+        return {"U": self.U, "S": self.S, "Vt": self.Vt, "V": None if self.Vt is None else self.Vt.T,
+                "k": self.k}[d]
+
+    def matrix(self) -> np.ndarray:
+        return (self.U * self.S) @ self.Vt
+
+
+class PartialHermitianEigen:
+    """PartialHermitianEigen (src/pheig.jl:4-7)."""
+
+    def __init__(self, values, vectors):
+        self.values, self.vectors = values, vectors
+
+    @property
+    def k(self) -> int:
+        return len(self.values)
+
+    def __getitem__(self, d):
+        return {"values": self.values, "vectors": self.vectors, "k": self.k}[d]
+
+    def matrix(self) -> np.ndarray:
+        return (self.vectors * self.values) @ self.vectors.T
+
+
+class CURPackedU:
+    """CURPackedU / HermitianCURPackedU (src/cur.jl:14-57)."""
+
+    def __init__(self, rows, cols, kind=0):
+        self.rows, self.cols, self.kind = rows, cols, kind
+
+    def __getitem__(self, d):
+        return {"rows": self.rows, "cols": self.cols, "k": len(self.cols)}[d]
+
+
+# ---------------------------------------------------------------------------
+# entry points
+# ---------------------------------------------------------------------------
+
+def idfact(*args, **kwargs) -> IDPackedV:
+    """idfact([trans,] A[, opts]; kwargs) (src/id.jl:434-450)."""
+    trans, M, opts, ctx, rand = _args(args, kwargs)
+    lib = _ffi.load()
+    out = C.POINTER(_ffi.lra_id)()
+    co = opts.to_c()
+    st = lib.lra_idfact(ctx.handle, M.dtype, trans.encode(), M.m, M.n, C.c_void_p(M.ptr), M.ld, C.byref(co),
+                        _rand(rand), C.byref(out))
+    _raise(st, ctx)
+    r = out.contents
+    try:
+        k, n = r.k, r.n
+        sk = _host(_iptr(r.sk), (k,), np.int64)
+        rd = _host(_iptr(r.rd), (n - k,), np.int64)
+        T = _host(r.T, (k, n - k), M.np_dtype)
+        return IDPackedV(sk, rd, T, r.nsteps)
+    finally:
+        lib.lra_id_free(out)
+
+
+def id(*args, **kwargs):
+    V = idfact(*args, **kwargs)
+    return V.sk, V.rd, V.T
+
+
+def _pqr_out(lib, out, np_dtype, want_pqr):
+    r = out.contents
+    try:
+        m, n, k = r.m, r.n, r.k
+        p = _host(_iptr(r.p), (n,), np.int64)
+        Q = _host(r.Q, (m, k), np_dtype) if r.retval & _ffi.RET_Q else None
+        R = _host(r.R, (k, n), np_dtype) if r.retval & _ffi.RET_R else None
+        T = _host(r.T, (k, n - k), np_dtype) if r.retval & _ffi.RET_T else None
+        if want_pqr and Q is not None and R is not None and T is None:
+            return PartialQR(Q, R, p, k, None)
+        return PartialQRFactors(Q, R, p, k, T)
+    finally:
+        lib.lra_pqr_free(out)
+
+
+def pqrfact(*args, **kwargs):
+    """pqrfact([trans,] A[, opts]) (src/pqr.jl:290-307)."""
+    trans, M, opts, ctx, rand = _args(args, kwargs)
+    lib = _ffi.load()
+    out = C.POINTER(_ffi.lra_pqr)()
+    co = opts.to_c()
+    st = lib.lra_pqrfact(ctx.handle, M.dtype, trans.encode(), M.m, M.n, C.c_void_p(M.ptr), M.ld,
+                         C.byref(co), _rand(rand), C.byref(out))
+    _raise(st, ctx)
+    return _pqr_out(lib, out, M.np_dtype, True)
+
+
+def pqr(*args, **kwargs):
+    kwargs.setdefault("pqrfact_retval", "qr")
+    F = pqrfact(*args, **kwargs)
+    return F.Q, F.R, F.p
+
+
+def sketchfact(*args, **kwargs):
+    """sketchfact([side, trans,] A[, opts]) (src/sketch.jl:52-66)."""
+    args = list(args)
+    side = "left"
+    if len(args) >= 2 and isinstance(args[0], str) and isinstance(args[1], str):
+        side = args.pop(0)
+    trans, M, opts, ctx, rand = _args(args, kwargs)
+    lib = _ffi.load()
+    out = C.POINTER(_ffi.lra_pqr)()
+    co = opts.to_c()
+    st = lib.lra_sketchfact(ctx.handle, M.dtype, side[0].encode(), trans.encode(), M.m, M.n,
+                            C.c_void_p(M.ptr), M.ld, C.byref(co), _rand(rand), C.byref(out))
+    _raise(st, ctx)
+    return _pqr_out(lib, out, M.np_dtype, True)
+
+
+def sketch(*args, **kwargs) -> np.ndarray:
+    """sketch([side, trans,] A, order[, opts]) (src/sketch.jl:35-50)."""
+    args = list(args)
+    side, trans = "left", "n"
+    if len(args) >= 2 and isinstance(args[0], str) and isinstance(args[1], str):
+        side, trans = args.pop(0), args.pop(0)
+    A = args.pop(0)
+    order = int(args.pop(0))
+    opts = args.pop(0) if args else None
+    ctx = kwargs.pop("ctx", None) or default_context()
+    rand = kwargs.pop("rand", None)
+    M = _mat(A)
+    opts = (opts or LRAOptions(M.np_dtype)).copy(**kwargs)
+    Mop = M.m if trans == "n" else M.n
+    Nop = M.n if trans == "n" else M.m
+    shape = (order, Nop) if side == "left" else (Mop, order)
+    B = np.zeros(shape, dtype=M.np_dtype, order="F")
+    lib = _ffi.load()
+    co = opts.to_c()
+    st = lib.lra_sketch(ctx.handle, M.dtype, side[0].encode(), trans.encode(), M.m, M.n, C.c_void_p(M.ptr),
+                        M.ld, order, C.byref(co), _rand(rand), C.c_void_p(B.ctypes.data), max(shape[0], 1))
+    _raise(st, ctx)
+    return B
+
+
+def geqp3_adap(B, opts: LRAOptions | None = None, ctx: Context | None = None, **kwargs):
+    """geqp3_adap! (src/pqr.jl:348-359) in place on a column-major CUDA
+    tensor; returns (jpvt, tau, k) as CUDA tensors / int."""
+    import torch
+    ctx = ctx or default_context()
+    M = _mat(B)
+    if M.keep is not B:
+        raise ArgumentError(_ffi.LRA_EINVAL, "B must be a column-major CUDA tensor")
+    opts = (opts or LRAOptions(M.np_dtype)).copy(**kwargs)
+    jpvt = torch.empty(max(M.n, 1), dtype=torch.int64, device=B.device)
+    tau = torch.empty(max(min(M.m, M.n), 1), dtype=B.dtype, device=B.device)
+    k = C.c_int64()
+    co = opts.to_c()
+    st = _ffi.load().lra_geqp3_adap(ctx.handle, M.dtype, M.m, M.n, C.c_void_p(M.ptr), M.ld,
+                                    C.c_void_p(jpvt.data_ptr()), C.c_void_p(tau.data_ptr()), C.byref(co),
+                                    C.byref(k))
+    _raise(st, ctx)
+    return jpvt[:M.n], tau[:min(M.m, M.n)], int(k.value)
+
+
+def _psvd(A, opts, kwargs, vals_only):
+    trans, M, opts, ctx, rand = _args((A,) + ((opts,) if opts is not None else ()), kwargs)
+    lib = _ffi.load()
+    out = C.POINTER(_ffi.lra_psvd)()
+    co = opts.to_c()
+    st = lib.lra_psvdfact(ctx.handle, M.dtype, M.m, M.n, C.c_void_p(M.ptr), M.ld, C.byref(co), _rand(rand),
+                          1 if vals_only else 0, C.byref(out))
+    _raise(st, ctx)
+    r = out.contents
+    try:
+        k = r.k
+        S = _host(r.S, (k,), M.np_dtype)
+        if vals_only:
+            return S
+        U = _host(r.U, (M.m, k), M.np_dtype)
+        Vt = _host(r.Vt, (k, M.n), M.np_dtype)
+        return PartialSVD(U, S, Vt)
+    finally:
+        lib.lra_psvd_free(out)
+
+
+def psvdfact(A, opts: LRAOptions | None = None, **kwargs) -> PartialSVD:
+    """psvdfact(A[, opts]) (src/psvd.jl:238-272)."""
+    return _psvd(A, opts, kwargs, False)
+
+
+def psvdvals(A, opts: LRAOptions | None = None, **kwargs) -> np.ndarray:
+    """psvdvals(A[, opts]) (src/psvd.jl:274-290)."""
+    return _psvd(A, opts, kwargs, True)
+
+
+def psvd(A, opts=None, **kwargs):
+    F = psvdfact(A, opts, **kwargs)
+    return F.U, F.S, F.Vt.T
+
+
+def _pheig(A, opts, kwargs, vals_only):
+    trans, M, opts, ctx, rand = _args((A,) + ((opts,) if opts is not None else ()), kwargs)
+    if M.m != M.n:
+        raise DimensionMismatch(_ffi.LRA_EDIM, "matrix is not square")
+    lib = _ffi.load()
+    out = C.POINTER(_ffi.lra_pheig)()
+    co = opts.to_c()
+    st = lib.lra_pheigfact(ctx.handle, M.dtype, M.n, C.c_void_p(M.ptr), M.ld, C.byref(co), _rand(rand),
+                           1 if vals_only else 0, C.byref(out))
+    _raise(st, ctx)
+    r = out.contents
+    try:
+        k = r.k
+        w = _host(r.values, (k,), M.np_dtype)
+        if vals_only:
+            return w
+        return PartialHermitianEigen(w, _host(r.vectors, (M.n, k), M.np_dtype))
+    finally:
+        lib.lra_pheig_free(out)
+
+
+def pheigfact(A, opts: LRAOptions | None = None, **kwargs) -> PartialHermitianEigen:
+    """pheigfact(A[, opts]) (src/pheig.jl:276-296)."""
+    return _pheig(A, opts, kwargs, False)
+
+
+def pheigvals(A, opts: LRAOptions | None = None, **kwargs) -> np.ndarray:
+    """pheigvals(A[, opts]) (src/pheig.jl:298-311)."""
+    return _pheig(A, opts, kwargs, True)
+
+
+def pheig(A, opts=None, **kwargs):
+    F = pheigfact(A, opts, **kwargs)
+    return F.values, F.vectors
+
+
+def curfact(A, opts: LRAOptions | None = None, **kwargs) -> CURPackedU:
+    """curfact(A[, opts]) (src/cur.jl:532-564)."""
+    trans, M, opts, ctx, rand = _args((A,) + ((opts,) if opts is not None else ()), kwargs)
+    lib = _ffi.load()
+    out = C.POINTER(_ffi.lra_cur)()
+    co = opts.to_c()
+    st = lib.lra_curfact(ctx.handle, M.dtype, M.m, M.n, C.c_void_p(M.ptr), M.ld, C.byref(co), _rand(rand),
+                         C.byref(out))
+    _raise(st, ctx)
+    r = out.contents
+    try:
+        rows = _host(_iptr(r.rows), (r.kr,), np.int64)
+        cols = _host(_iptr(r.cols), (r.kc,), np.int64)
+        return CURPackedU(rows, cols, r.kind)
+    finally:
+        lib.lra_cur_free(out)
+
+
+def cur(A, opts=None, **kwargs):
+    U = curfact(A, opts, **kwargs)
+    return U.rows, U.cols
+
+
+def snorm(A, opts: LRAOptions | None = None, hermitian=None, **kwargs) -> float:
+    """snorm(A[, opts]) (src/snorm.jl:14-45)."""
+    trans, M, opts, ctx, rand = _args((A,) + ((opts,) if opts is not None else ()), kwargs)
+    out = C.c_double()
+    co = opts.to_c()
+    herm = -1 if hermitian is None else (1 if hermitian else 0)
+    st = _ffi.load().lra_snorm(ctx.handle, M.dtype, M.m, M.n, C.c_void_p(M.ptr), M.ld, herm, C.byref(co),
+                               _rand(rand), C.byref(out))
+    _raise(st, ctx)
+    return out.value
+
+
+def snormdiff(A, B, opts: LRAOptions | None = None, trans: str = "n", **kwargs) -> float:
+    """snormdiff(A, B[, opts]) (src/snorm.jl:50-53); B may be a dense matrix,
+    an IDPackedV (F = A[:, sk] [I T] P') or a PartialSVD (factored form)."""
+    _, M, opts, ctx, rand = _args((A,) + ((opts,) if opts is not None else ()), kwargs)
+    lib = _ffi.load()
+    out = C.c_double()
+    co = opts.to_c()
+    if isinstance(B, IDPackedV):
+        keep = [np.ascontiguousarray(B.sk, np.int64), np.ascontiguousarray(B.rd, np.int64),
+                np.asfortranarray(B.T.astype(M.np_dtype))]
+        cid = _ffi.lra_id(M.dtype, B.nsteps, B.k, B.k + len(B.rd),
+                          keep[0].ctypes.data_as(C.POINTER(C.c_int64)),
+                          keep[1].ctypes.data_as(C.POINTER(C.c_int64)), keep[2].ctypes.data)
+        st = lib.lra_snormdiff_id(ctx.handle, M.dtype, trans.encode(), M.m, M.n, C.c_void_p(M.ptr), M.ld,
+                                  C.byref(cid), C.byref(co), _rand(rand), C.byref(out))
+    elif isinstance(B, PartialSVD):
+        keep = [np.asfortranarray(B.U.astype(M.np_dtype)), np.ascontiguousarray(B.S.astype(M.np_dtype)),
+                np.asfortranarray(B.Vt.astype(M.np_dtype))]
+        cps = _ffi.lra_psvd(M.dtype, 0, M.m, M.n, B.k, keep[0].ctypes.data, keep[1].ctypes.data,
+                            keep[2].ctypes.data)
+        st = lib.lra_snormdiff_psvd(ctx.handle, M.dtype, M.m, M.n, C.c_void_p(M.ptr), M.ld, C.byref(cps),
+                                    C.byref(co), _rand(rand), C.byref(out))
+    else:
+        MB = _mat(B)
+        if MB.dtype != M.dtype or MB.m != M.m or MB.n != M.n:
+            raise DimensionMismatch(_ffi.LRA_EDIM, "snormdiff operands differ")
+        st = lib.lra_snormdiff(ctx.handle, M.dtype, M.m, M.n, C.c_void_p(M.ptr), M.ld, C.c_void_p(MB.ptr),
+                               MB.ld, C.byref(co), _rand(rand), C.byref(out))
+    _raise(st, ctx)
+    return out.value
+
+
+def matrixlib(name: str, *args, dtype=np.float64) -> np.ndarray:
+    """matrixlib (src/matrixlib.jl:4-48): :hilb, :cauchy, :fourier."""
+    if name == "hilb":
+        m = args[0]
+        n = args[1] if len(args) > 1 else m
+        i = np.arange(1, m + 1)[:, None]
+        j = np.arange(1, n + 1)[None, :]
+        return np.asfortranarray((1.0 / (i + j - 1)).astype(dtype))
+    if name == "cauchy":
+        x, y = np.asarray(args[0]), np.asarray(args[1])
+        return np.asfortranarray((1.0 / (x[:, None] - y[None, :])).astype(dtype))
+    if name == "fourier":
+        if len(args) == 2 and np.isscalar(args[0]):
+            x = np.arange(args[0])
+            y = np.arange(args[1]) / args[1]
+        elif len(args) == 1:
+            x = np.arange(args[0])
+            y = np.arange(args[0]) / args[0]
+        else:
+            x, y = np.asarray(args[0]), np.asarray(args[1])
+        return np.asfortranarray(np.exp(-2j * np.pi * np.outer(x, y)))
+    raise ArgumentError(_ffi.LRA_EINVAL, "name")

@@ -1,0 +1,96 @@
+"""C-ABI checks that need no GPU: the library loads, exports every entry
+point include/lra.h declares, the ctypes structs match the C layout, and the
+option defaults / validation mirror LRAOptions (src/LowRankApprox.jl:96-148)."""
+import ctypes
+import os
+import re
+import subprocess
+
+import numpy as np
+import pytest
+
+from conftest import ROOT
+
+
+def header_symbols():
+    txt = open(os.path.join(ROOT, "include", "lra.h")).read()
+    txt = re.sub(r"/\*.*?\*/", "", txt, flags=re.S)
+    return sorted(set(re.findall(r"\b(lra_[a-z0-9_]+)\s*\(", txt)))
+
+
+@pytest.fixture(scope="module")
+def lib():
+    import lowrankapprox._ffi as F
+    if not os.path.exists(F.LIB_PATH):
+        import __graft_entry__ as g
+        g.build()
+    return F.load()
+
+
+def test_exports_every_declared_symbol(lib):
+    import lowrankapprox._ffi as F
+    syms = header_symbols()
+    assert len(syms) >= 25
+    out = subprocess.run(["nm", "-D", "--defined-only", F.LIB_PATH], capture_output=True, text=True).stdout
+    exported = set(re.findall(r" T (lra_\w+)", out))
+    missing = [s for s in syms if s not in exported]
+    assert not missing, missing
+    bound = {name for name, _, _ in F.SIGNATURES}
+    assert set(syms) <= bound | {"lra_geqp3_adap_noalloc"}
+
+
+def test_struct_layout_matches_header(tmp_path):
+    import lowrankapprox._ffi as F
+    src = tmp_path / "sz.c"
+    src.write_text('#include <stdio.h>\n#include <stddef.h>\n#include "lra.h"\n'
+                   'int main(void){printf("%zu %zu %zu %zu %zu %zu %zu %zu %zu\\n", sizeof(lra_opts),'
+                   'sizeof(lra_rand), sizeof(lra_id), sizeof(lra_pqr), sizeof(lra_psvd), sizeof(lra_pheig),'
+                   'sizeof(lra_cur), sizeof(lra_matdesc), offsetof(lra_opts, seed)); return 0;}\n')
+    exe = tmp_path / "sz"
+    subprocess.check_call(["gcc", "-I", os.path.join(ROOT, "include"), str(src), "-o", str(exe)])
+    got = list(map(int, subprocess.check_output([str(exe)]).split()))
+    want = [ctypes.sizeof(c) for c in (F.lra_opts, F.lra_rand, F.lra_id, F.lra_pqr, F.lra_psvd, F.lra_pheig,
+                                       F.lra_cur, F.lra_matdesc)] + [F.lra_opts.seed.offset]
+    assert got == want
+
+
+@pytest.mark.parametrize("dtype,eps", [(1, np.finfo(np.float64).eps), (0, np.finfo(np.float32).eps)])
+def test_opts_defaults(lib, dtype, eps):
+    import lowrankapprox._ffi as F
+    o = F.lra_opts()
+    assert lib.lra_opts_init(ctypes.byref(o), dtype) == 0
+    assert o.nb == 32 and o.rank == -1 and o.atol == 0 and o.maxdet_tol == -1 and o.maxdet_niter == -1
+    assert o.rtol == pytest.approx(5 * eps) and o.pheig_orthtol == pytest.approx(np.sqrt(eps))
+    assert o.sketch == F.SKETCH["randn"] and o.sketch_randn_niter == 0 and o.sketchfact_adap == 1
+    assert list(o.sketchfact_randn_samp) == [1, 8] and list(o.sketchfact_sub_samp) == [4, 8]
+    assert o.snorm_niter == 32 and o.pqrfact_retval == F.RET_Q | F.RET_R
+    # python mirror agrees
+    import lowrankapprox as L
+    p = L.LRAOptions(np.float64 if dtype == 1 else np.float32).to_c()
+    assert p.rtol == o.rtol and p.nb == o.nb and p.pqrfact_retval == o.pqrfact_retval
+
+
+@pytest.mark.parametrize("field,value", [("atol", -1.0), ("nb", 0), ("rtol", -1e-3), ("pheig_orthtol", -1.0),
+                                         ("sketch", 9), ("precision", 5)])
+def test_chkopts_rejects(lib, field, value):
+    import lowrankapprox._ffi as F
+    o = F.lra_opts()
+    lib.lra_opts_init(ctypes.byref(o), 1)
+    assert lib.lra_chkopts(ctypes.byref(o)) == 0
+    setattr(o, field, value)
+    assert lib.lra_chkopts(ctypes.byref(o)) == F.LRA_EINVAL
+
+
+def test_status_strings(lib):
+    assert lib.lra_status_string(0) == b"ok"
+    assert lib.lra_status_string(9) == b"matrix must be Hermitian"
+
+
+def test_python_options_mirror():
+    import lowrankapprox as L
+    o = L.LRAOptions(sketch="subs", rank=5)   # BASELINE's :subs spelling means :sub
+    assert o.sketch == "sub" and o.rank == 5
+    o2 = o.copy(rtol=1e-3)
+    assert o2.rtol == 1e-3 and o.rtol != 1e-3
+    with pytest.raises(ValueError):
+        L.LRAOptions(bogus=1)

@@ -1,0 +1,322 @@
+"""GPU parity of the sketch-then-factor path against the oracle, through the
+C ABI (ctypes), on the same injected random streams.
+
+Bar (floating point): rank equal; skeleton columns p[:k] bit-exact; the
+rest of the permutation equal as a set; factors reconstruct A to within 2x
+of the oracle's own error and within the reference tests' criteria
+(test/id.jl:31, test/psvd.jl:29, test/pheig.jl:26, test/pqr.jl:29)."""
+import numpy as np
+import pytest
+
+from test_oracle import assert_pqr_parity, check_pivots, real_fourier
+
+pytestmark = pytest.mark.gpu
+
+
+def dev(A):
+    import torch
+    return torch.from_numpy(np.asfortranarray(A)).cuda().t().contiguous().t()
+
+
+def streams(seed, n=400000):
+    rng = np.random.default_rng(seed)
+    return rng.standard_normal(n), rng.integers(1, 2**62, n, dtype=np.int64)
+
+
+def both_rs(oracle, lra, seed):
+    g, q = streams(seed)
+    return oracle.RandStream(gauss=g, ints=q), lra.RandStream(gauss=g, ints=q)
+
+
+def relerr(A, E):
+    return np.linalg.norm(A - E) / np.linalg.norm(A)
+
+
+# ---------------------------------------------------------------------------
+# pivoted QR core vs the real-LAPACK goldens
+# ---------------------------------------------------------------------------
+
+def test_geqp3_goldens(lra, golden):
+    import torch
+    z = golden["qr"]
+    names = sorted({k.split("/")[1] for k in z.files})
+    for nm in names:
+        B = np.asfortranarray(z[f"qr/{nm}/B"])
+        Bd = dev(B)
+        opts = lra.LRAOptions(B.dtype.type, rtol=float(z[f"qr/{nm}/rtol"]), rank=int(z[f"qr/{nm}/rank"]))
+        jpvt, tau, k = lra.geqp3_adap(Bd, opts)
+        assert k == int(z[f"qr/{nm}/k"]), nm
+        W = Bd.cpu().numpy()
+        p = jpvt.cpu().numpy()
+        tol = 1e-11 if B.dtype == np.float64 else 5e-5
+        same = check_pivots(B, p, z[f"qr/{nm}/p"], k, B.dtype, nm)
+        if same == k:
+            assert_pqr_parity(p, np.triu(W[:k, :]), z[f"qr/{nm}/p"], z[f"qr/{nm}/R"], k, tol, nm)
+        assert torch.isfinite(tau).all()
+
+
+def test_hilbert1024_id(lra, oracle, golden):
+    h = golden["hilb"]
+    A = oracle.hilb(1024)
+    g = h["stream"].astype(np.float64) / 32.0
+    for tag, rtol in (("1e-12", 1e-12), ("default", None)):
+        kw = {} if rtol is None else {"rtol": rtol}
+        for Ain in (A, dev(A)):
+            V = lra.idfact(Ain, rand=lra.RandStream(gauss=g), **kw)
+            assert V.k == int(h[f"{tag}/k"])
+            B = g[:40 * 1024].reshape((40, 1024), order="F") @ A     # the (only) sketch
+            check_pivots(B, V.sk, h[f"{tag}/sk"], V.k, np.float64, tag)
+            E = lra.IDPackedV.matrix(V)
+            err = np.linalg.norm(A - A[:, V.sk - 1] @ E, 2) / np.linalg.norm(A, 2)
+            assert err <= 2 * float(h[f"{tag}/relerr2"]) + 1e-15
+
+
+# ---------------------------------------------------------------------------
+# every sketch and element type, reference-test matrices
+# ---------------------------------------------------------------------------
+
+SKETCHES = ["none", "randn", "sub", "srft", "sprn"]
+
+
+@pytest.mark.parametrize("sketch", SKETCHES)
+@pytest.mark.parametrize("dt", [np.float32, np.float64])
+@pytest.mark.parametrize("trans", ["n", "c"])
+def test_idfact_parity(lra, oracle, sketch, dt, trans):
+    A = real_fourier(128, 64).astype(dt)
+    rtol = 5 * np.finfo(dt).eps
+    ors, grs = both_rs(oracle, lra, 11)
+    ref = oracle.idfact(trans, A, oracle.Opts(rtol=rtol, sketch=sketch), ors)
+    V = lra.idfact(trans, A, lra.LRAOptions(dt, rtol=rtol, sketch=sketch), rand=grs)
+    Aop = A if trans == "n" else A.T
+    E = Aop[:, V.sk - 1] @ V.matrix()
+    assert relerr(Aop, E) < 100 * rtol            # test/id.jl:31-32
+    assert abs(V.k - ref["k"]) <= 1
+    if V.k == ref["k"]:
+        kk = V.k
+        # skeleton equal up to the columns decided at the noise floor
+        head = max(0, kk - 2)
+        assert np.array_equal(V.sk[:head], ref["sk"][:head])
+
+
+@pytest.mark.parametrize("sketch", ["randn", "sub", "srft", "sprn"])
+@pytest.mark.parametrize("dt", [np.float32, np.float64])
+def test_sketch_values(lra, oracle, sketch, dt):
+    rng = np.random.default_rng(4)
+    A = np.asfortranarray(rng.standard_normal((96, 40)).astype(dt))
+    for side, trans in (("left", "n"), ("left", "c"), ("right", "n")):
+        # injected streams restart at offset 0 on every C-ABI call
+        ors, grs = both_rs(oracle, lra, 12)
+        order = 17
+        B = lra.sketch(side, trans, A, order, lra.LRAOptions(dt, sketch=sketch), rand=grs)
+        R = oracle.sketch(side, trans, A, order, oracle.Opts(sketch=sketch), ors)
+        tol = 1e-10 if dt == np.float64 else 2e-4
+        assert B.shape == R.shape
+        assert np.abs(B - R).max() <= tol * max(1.0, np.abs(R).max()), (sketch, side, trans)
+
+
+@pytest.mark.parametrize("sketch", SKETCHES)
+@pytest.mark.parametrize("dt", [np.float32, np.float64])
+def test_psvd_parity(lra, oracle, sketch, dt):
+    rtol = 5 * np.finfo(dt).eps
+    for (m, n) in ((128, 64), (64, 128)):
+        A = real_fourier(m, n, 3).astype(dt)
+        ors, grs = both_rs(oracle, lra, 13)
+        ref = oracle.psvdfact(A, oracle.Opts(rtol=rtol, sketch=sketch), ors)
+        F = lra.psvdfact(A, lra.LRAOptions(dt, rtol=rtol, sketch=sketch), rand=grs)
+        assert relerr(A, F.matrix()) < 100 * rtol          # test/psvd.jl:29
+        assert abs(F.k - ref["k"]) <= 1
+        k = min(F.k, ref["k"])
+        assert np.allclose(F.S[:k], ref["S"][:k], rtol=100 * rtol, atol=100 * rtol * ref["S"][0])
+        Uo = F.U.T @ F.U
+        assert np.abs(Uo - np.eye(F.k)).max() < 1e3 * rtol * max(1, F.k)
+        s = lra.psvdvals(A, lra.LRAOptions(dt, rtol=rtol, sketch=sketch), rand=both_rs(oracle, lra, 13)[1])
+        assert np.allclose(s, F.S, rtol=100 * rtol, atol=100 * rtol * F.S[0])
+
+
+@pytest.mark.parametrize("sketch", SKETCHES)
+@pytest.mark.parametrize("dt", [np.float32, np.float64])
+def test_pheig_parity(lra, oracle, sketch, dt):
+    rtol = 5 * np.finfo(dt).eps
+    H = real_fourier(128, 128, 4)
+    H = np.asfortranarray((H + H.T).astype(dt))
+    ors, grs = both_rs(oracle, lra, 14)
+    ref = oracle.pheigfact(H, oracle.Opts(rtol=rtol, sketch=sketch), ors)
+    F = lra.pheigfact(H, lra.LRAOptions(dt, rtol=rtol, sketch=sketch), rand=grs)
+    assert relerr(H, F.matrix()) < 100 * rtol                # test/pheig.jl:26
+    assert abs(F.k - ref["k"]) <= 1
+    if F.k == ref["k"]:
+        assert np.allclose(F.values, ref["values"], atol=100 * rtol * np.abs(ref["values"]).max())
+
+
+@pytest.mark.parametrize("sketch", SKETCHES)
+def test_pqrfact_parity(lra, oracle, sketch):
+    rtol = 5 * np.finfo(np.float64).eps
+    A = real_fourier(128, 64, 6)
+    ors, grs = both_rs(oracle, lra, 15)
+    ref = oracle.pqrfact("n", A, oracle.Opts(rtol=rtol, sketch=sketch), ors)
+    F = lra.pqrfact(A, lra.LRAOptions(rtol=rtol, sketch=sketch), rand=grs)
+    assert isinstance(F, lra.PartialQR)
+    assert relerr(A, F.matrix()) < 100 * rtol                # test/pqr.jl:29
+    assert abs(F.k - ref["k"]) <= 1
+    assert np.abs(F.Q.T @ F.Q - np.eye(F.k)).max() < 1e-12
+
+
+@pytest.mark.parametrize("sketch", SKETCHES)
+def test_curfact_parity(lra, oracle, sketch):
+    rtol = 5 * np.finfo(np.float64).eps
+    M = real_fourier(128, 64, 7)
+    Mh = M[:64, :64] + M[:64, :64].T
+    for A in (M, M.T.copy(order="F"), np.asfortranarray(Mh)):
+        ors, grs = both_rs(oracle, lra, 16)
+        ref = oracle.curfact(A, oracle.Opts(rtol=rtol, sketch=sketch), ors)
+        U = lra.curfact(A, lra.LRAOptions(rtol=rtol, sketch=sketch), rand=grs)
+        assert U.kind == ref["kind"]
+        assert abs(len(U.cols) - len(ref["cols"])) <= 1
+        # CUR(A, U) (src/cur.jl:85-93): C * inv(C[rows, :]) * R through an SVD
+        def cur_err(rows, cols):
+            C, R = A[:, cols - 1], A[rows - 1, :]
+            u, s, vt = np.linalg.svd(C[rows - 1, :])
+            return relerr(A, C @ ((vt.T / s) @ u.T) @ R)
+        e_gpu = cur_err(U.rows, U.cols)
+        e_ref = cur_err(ref["rows"], ref["cols"])
+        assert e_gpu <= max(2 * e_ref, 1000 * rtol)         # test/cur.jl:22-31
+
+
+def test_maxdet(lra, oracle):
+    A = real_fourier(128, 64, 8)
+    ors, grs = both_rs(oracle, lra, 17)
+    ref = oracle.idfact("n", A, oracle.Opts(rtol=1e-10, maxdet_tol=0.0), ors)
+    V = lra.idfact(A, lra.LRAOptions(rtol=1e-10, maxdet_tol=0.0), rand=grs)
+    assert np.abs(V.T).max() <= 1 + 1e-9
+    assert V.k == ref["k"]
+    assert sorted(V.sk) == sorted(ref["sk"])
+
+
+def test_power_iterations(lra, oracle):
+    A = real_fourier(128, 64, 9)
+    ors, grs = both_rs(oracle, lra, 18)
+    opts = dict(rtol=1e-10, sketch_randn_niter=1)
+    ref = oracle.idfact("n", A, oracle.Opts(**opts), ors)
+    V = lra.idfact(A, lra.LRAOptions(**opts), rand=grs)
+    assert abs(V.k - ref["k"]) <= 1
+    E = A[:, V.sk - 1] @ V.matrix()
+    assert relerr(A, E) < 1e-8
+
+
+# ---------------------------------------------------------------------------
+# spectral norms
+# ---------------------------------------------------------------------------
+
+@pytest.mark.parametrize("dt", [np.float32, np.float64])
+def test_snorm(lra, dt):
+    rng = np.random.default_rng(8)
+    rtol = 100 * np.finfo(dt).eps
+    A = rng.random((20, 10)).astype(dt)
+    g = rng.standard_normal(1000)
+    nrm = np.linalg.norm(A.astype(np.float64), 2)
+    assert abs(lra.snorm(A, rand=lra.RandStream(gauss=g)) - nrm) <= rtol * nrm * 10   # test/snorm.jl:16
+    H = rng.random((10, 10)).astype(dt)
+    H = H + H.T
+    nh = np.linalg.norm(H.astype(np.float64), 2)
+    assert abs(lra.snorm(H, rand=lra.RandStream(gauss=g)) - nh) <= rtol * nh * 10
+    B = rng.random((20, 10)).astype(dt)
+    nd = np.linalg.norm((A - B).astype(np.float64), 2)
+    d = lra.snormdiff(A, B, rand=lra.RandStream(gauss=g))
+    # snorm stops after snorm_niter = 32 power steps; the oracle runs the same
+    from oracle import oracle as O
+    dref = O.snormdiff_dense(A, B, O.Opts(), O.RandStream(gauss=g))
+    assert abs(d - dref) <= 1e-5 * nd
+    assert abs(d - nd) <= 1e-4 * nd
+
+
+def test_snormdiff_factored(lra):
+    rng = np.random.default_rng(9)
+    A = real_fourier(200, 90, 2)
+    F = lra.psvdfact(A, rtol=1e-8)
+    g = rng.standard_normal(1000)
+    d1 = lra.snormdiff(A, F, rand=lra.RandStream(gauss=g))
+    assert abs(d1 - np.linalg.norm(A - F.matrix(), 2)) <= 1e-3 * max(d1, 1e-300) + 1e-14
+    V = lra.idfact(A, rtol=1e-8)
+    d2 = lra.snormdiff(A, V, rand=lra.RandStream(gauss=g))
+    E = A[:, V.sk - 1] @ V.matrix()
+    assert abs(d2 - np.linalg.norm(A - E, 2)) <= 1e-3 * max(d2, 1e-300) + 1e-14
+
+
+# ---------------------------------------------------------------------------
+# edge cases and errors
+# ---------------------------------------------------------------------------
+
+def test_edge_shapes(lra, oracle):
+    rng = np.random.default_rng(1)
+    # n < nb, order > m, rank 0, full rank, single column / row
+    for (m, n) in ((5, 3), (3, 5), (40, 7), (1, 9), (9, 1), (33, 33)):
+        A = np.asfortranarray(rng.standard_normal((m, n)))
+        ors, grs = both_rs(oracle, lra, 19)
+        V = lra.idfact(A, rand=grs)
+        ref = oracle.idfact("n", A, oracle.Opts(), ors)
+        assert V.k == ref["k"] == min(m, n)
+        assert np.array_equal(V.sk, ref["sk"])
+    A = np.asfortranarray(rng.standard_normal((30, 20)))
+    V = lra.idfact(A, rank=0, sketchfact_adap=False)
+    assert V.k == 0 and len(V.rd) == 20
+    V = lra.idfact(A, rank=5)
+    assert V.k == 5
+    Z = np.zeros((0, 4))
+    V = lra.idfact(Z)
+    assert V.k == 0
+    Zc = np.zeros((12, 10))
+    V = lra.idfact(Zc)
+    assert V.k == 0
+
+
+def test_device_and_host_inputs_agree(lra):
+    rng = np.random.default_rng(2)
+    A = np.asfortranarray(rng.standard_normal((300, 200)) @ np.diag(0.7 ** np.arange(200)))
+    g, q = streams(21)
+    V1 = lra.idfact(A, rtol=1e-10, rand=lra.RandStream(gauss=g))
+    import torch
+    V2 = lra.idfact(dev(A), rtol=1e-10, rand=lra.RandStream(gauss=torch.from_numpy(g).cuda()))
+    assert V1.k == V2.k and np.array_equal(V1.sk, V2.sk)
+    assert np.array_equal(V1.T, V2.T)  # same kernels, same data: bit-identical
+
+
+def test_errors(lra):
+    rng = np.random.default_rng(3)
+    A = rng.standard_normal((20, 20))
+    with pytest.raises(ValueError, match="Hermitian"):
+        lra.pheigfact(A)
+    B = A.copy()
+    B[3, 4] = np.nan
+    with pytest.raises(ValueError):
+        lra.idfact(B)
+    with pytest.raises(lra.LRAError) as e:
+        lra.idfact(A, rand=lra.RandStream(gauss=np.zeros(10)))
+    assert e.value.status == 7
+    with pytest.raises(ValueError):
+        lra.idfact(A, nb=0)
+    with pytest.raises(ValueError):
+        lra.idfact(A, rtol=-1.0)
+    # the context stays usable after errors
+    assert lra.idfact(A).k == 20
+
+
+def test_batched_ragged(lra, oracle):
+    import ctypes as C
+    from lowrankapprox import _ffi
+    rng = np.random.default_rng(4)
+    mats, keep = [], []
+    sizes = [(50, 30), (16, 70), (128, 128), (7, 3)]
+    for (m, n) in sizes:
+        A = np.asfortranarray(rng.standard_normal((m, n)) @ np.diag(0.5 ** np.arange(n)))
+        keep.append(A)
+        mats.append(_ffi.lra_matdesc(m, n, m, A.ctypes.data))
+    arr = (_ffi.lra_matdesc * len(mats))(*mats)
+    outs = (C.POINTER(_ffi.lra_id) * len(mats))()
+    o = lra.LRAOptions(rtol=1e-9).to_c()
+    lib = _ffi.load()
+    ctx = lra.default_context()
+    assert lib.lra_idfact_batched(ctx.handle, 1, len(mats), arr, C.byref(o), None, outs) == 0
+    for i, A in enumerate(keep):
+        r = outs[i].contents
+        assert 0 < r.k <= min(A.shape)
+        lib.lra_id_free(outs[i])

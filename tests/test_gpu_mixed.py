@@ -1,0 +1,101 @@
+"""The mixed-precision path: the Gaussian sketch on tcgen05 tensor cores from
+exact BF16 byte slices.  Checked against the FP64 product of the same
+lattice sketch, at tile-edge shapes, and end to end against the oracle."""
+import numpy as np
+import pytest
+
+from test_gpu_core import dev, relerr
+from test_oracle import check_pivots
+
+pytestmark = pytest.mark.gpu
+
+
+def lattice(seed, n):
+    import lowrankapprox as L
+    return L.lattice_gauss(seed, n)
+
+
+@pytest.mark.parametrize("shape,order", [((300, 200), 40), ((1000, 130), 136), ((64, 257), 264),
+                                         ((2048, 640), 520), ((129, 1), 17)])
+@pytest.mark.parametrize("trans", ["n", "c"])
+def test_tc_sketch_exact(lra, shape, order, trans):
+    rng = np.random.default_rng(sum(shape) + order)
+    m, n = shape
+    # columns with wildly different scales, exercising the per-column exponent
+    A = np.asfortranarray(rng.standard_normal((m, n)) * np.exp(rng.uniform(-30, 30, (1, n))) *
+                          np.exp(rng.uniform(-3, 3, (m, 1))))
+    M = m if trans == "n" else n
+    g = lattice(3, order * M + 10)
+    B = lra.sketch("left", trans, A, order, lra.LRAOptions(precision="mixed", rtol=1e-10),
+                   rand=lra.RandStream(gauss=g))
+    S = g[:order * M].reshape((order, M), order="F")
+    opA = A if trans == "n" else A.T
+    R = S @ opA
+    # truncation of op(A) at 2^-48 of each column's scale, times |S|
+    colmax = np.abs(opA).max(axis=0)
+    bound = 2.0 ** -47 * (np.abs(S).sum(axis=1)[:, None] * colmax[None, :]) + 4 * np.finfo(float).eps * np.abs(R)
+    assert np.all(np.abs(B - R) <= bound + 1e-300)
+
+
+def test_tc_sketch_f32(lra):
+    rng = np.random.default_rng(7)
+    A = np.asfortranarray(rng.standard_normal((700, 333)).astype(np.float32))
+    order = 72
+    g = lattice(4, order * 700)
+    B = lra.sketch("left", "n", A, order, lra.LRAOptions(np.float32, precision="mixed"),
+                   rand=lra.RandStream(gauss=g))
+    R = g.reshape((order, 700), order="F") @ A.astype(np.float64)
+    assert np.abs(B - R).max() <= 1e-5 * np.abs(R).max()
+
+
+def decaying(m, n, rate, seed):
+    rng = np.random.default_rng(seed)
+    r = min(m, n)
+    U, _ = np.linalg.qr(rng.standard_normal((m, r)))
+    V, _ = np.linalg.qr(rng.standard_normal((n, r)))
+    s = 10.0 ** (-np.arange(r) / rate)
+    return np.asfortranarray((U * s) @ V.T)
+
+
+@pytest.mark.parametrize("trans", ["n", "c"])
+def test_idfact_mixed_parity(lra, oracle, trans):
+    A = decaying(1100, 900, 25.0, 1)
+    g = lattice(5, 4_000_000)
+    ref = oracle.idfact(trans, A, oracle.Opts(rtol=1e-10), oracle.RandStream(gauss=g))
+    V = lra.idfact(trans, A, lra.LRAOptions(rtol=1e-10, precision="mixed"), rand=lra.RandStream(gauss=g))
+    assert V.k == ref["k"]
+    Aop = A if trans == "n" else A.T
+    M = Aop.shape[0]
+    # the final step's sketch, to judge near-ties
+    off = sum((32 * 2 ** t + 8) * M for t in range(V.nsteps - 1))
+    order = 32 * 2 ** (V.nsteps - 1) + 8
+    B = g[off:off + order * M].reshape((order, M), order="F") @ Aop
+    check_pivots(B, V.sk, ref["sk"], V.k, np.float64)
+    e = np.linalg.norm(Aop - Aop[:, V.sk - 1] @ V.matrix(), 2) / np.linalg.norm(Aop, 2)
+    e_ref = np.linalg.norm(Aop - Aop[:, ref["sk"] - 1] @ oracle._v_matrix(ref, Aop.shape[1], A.dtype), 2) / \
+        np.linalg.norm(Aop, 2)
+    assert e <= 2 * e_ref + 1e-15
+
+
+def test_psvd_mixed_vs_native(lra):
+    A = decaying(1536, 1024, 40.0, 2)
+    g = lattice(6, 6_000_000)
+    Fm = lra.psvdfact(A, lra.LRAOptions(rtol=1e-10, precision="mixed"), rand=lra.RandStream(gauss=g))
+    Fn = lra.psvdfact(A, lra.LRAOptions(rtol=1e-10, precision="native"), rand=lra.RandStream(gauss=g))
+    assert abs(Fm.k - Fn.k) <= 1
+    nrm = np.linalg.norm(A, 2)
+    em = np.linalg.norm(A - Fm.matrix(), 2) / nrm
+    en = np.linalg.norm(A - Fn.matrix(), 2) / nrm
+    assert em <= 2 * en + 1e-14
+    assert em < 1e-9
+    k = min(Fm.k, Fn.k)
+    assert np.allclose(Fm.S[:k], Fn.S[:k], rtol=1e-8, atol=1e-12 * Fn.S[0])
+
+
+def test_mixed_device_input(lra):
+    A = decaying(800, 600, 20.0, 3)
+    g = lattice(8, 2_000_000)
+    o = lra.LRAOptions(rtol=1e-10, precision="mixed")
+    V1 = lra.idfact(A, o, rand=lra.RandStream(gauss=g))
+    V2 = lra.idfact(dev(A), o, rand=lra.RandStream(gauss=g))
+    assert V1.k == V2.k and np.array_equal(V1.sk, V2.sk) and np.array_equal(V1.T, V2.T)

@@ -1,0 +1,179 @@
+"""The CPU oracle pinned before it is trusted: against the golden fixtures
+made with the real LAPACK xLAQPS (the routine the reference ccalls,
+src/lapack.jl:117-139), the README's published Hilbert ranks
+(README.md:107,122), and the reference tests' reconstruction criteria
+(test/id.jl:31-32, test/pqr.jl, test/psvd.jl:29-32, test/pheig.jl:26-29,
+test/cur.jl:31, test/snorm.jl:16-25)."""
+import numpy as np
+import pytest
+
+
+def assert_pqr_parity(p, R, p_ref, R_ref, k, tol, name=""):
+    """Skeleton pivots p[:k] bit-exact; the columns after the rank are
+    compared as a set, with R12 aligned by column index (their order is
+    decided among pivots below the rank tolerance)."""
+    assert np.array_equal(p[:k], p_ref[:k]), name
+    assert sorted(p[k:]) == sorted(p_ref[k:]), name
+    scale = max(np.abs(R_ref).max(), 1e-300)
+    assert np.abs(R[:, :k] - R_ref[:, :k]).max() <= tol * scale, name
+    if R.shape[1] > k:
+        o, o_ref = np.argsort(p[k:]), np.argsort(p_ref[k:])
+        assert np.abs(R[:, k:][:, o] - R_ref[:, k:][:, o_ref]).max() <= tol * scale, name
+
+
+def residual_norms(B, piv, cols):
+    """Norms of columns `cols` of B after projecting out B[:, piv] (float64)."""
+    B = np.asarray(B, np.float64)
+    X = B[:, np.asarray(cols) - 1]
+    if len(piv):
+        Q, _ = np.linalg.qr(B[:, np.asarray(piv) - 1])
+        X = X - Q @ (Q.T @ X)
+    return np.linalg.norm(X, axis=0)
+
+
+def check_pivots(B, p, p_ref, k, dt, name=""):
+    """p[:k] must equal p_ref[:k] up to the first step where the two choices
+    are a near-tie: there, the exact residual norms of both candidates agree
+    to the precision's tie tolerance, and the sequences may differ after.
+    Returns the number of leading pivots that agree."""
+    tie = 5e-4 if np.dtype(dt) == np.float32 else 1e-9
+    eps = float(np.finfo(dt).eps)
+    floor = 1e3 * eps * float(np.linalg.norm(np.asarray(B, np.float64), axis=0).max())
+    for i in range(k):
+        if p[i] == p_ref[i]:
+            continue
+        r = residual_norms(B, p[:i], [p[i], p_ref[i]])
+        # a tie relative to the candidates, or both at the rounding floor
+        assert abs(r[0] - r[1]) <= tie * r.max() + floor, (name, i, r)
+        return i
+    return k
+
+
+def qr_cases(golden):
+    z = golden["qr"]
+    names = sorted({k.split("/")[1] for k in z.files})
+    return z, names
+
+
+def test_c_laqps_matches_lapack_goldens(oracle, golden):
+    z, names = qr_cases(golden)
+    assert len(names) >= 10
+    for nm in names:
+        B = np.asfortranarray(z[f"qr/{nm}/B"])
+        opts = oracle.Opts(rtol=float(z[f"qr/{nm}/rtol"]), rank=int(z[f"qr/{nm}/rank"])).for_dtype(B.dtype)
+        W = B.copy(order="F")
+        p, tau, k = oracle.geqp3_adap(W, opts, backend="c")
+        assert k == int(z[f"qr/{nm}/k"]), nm
+        assert_pqr_parity(p, np.triu(W[:k, :]), z[f"qr/{nm}/p"], z[f"qr/{nm}/R"], k,
+                          1e-12 if B.dtype == np.float64 else 2e-5, nm)
+
+
+def test_block_loop_equals_c_loop(oracle, golden):
+    z, names = qr_cases(golden)
+    for nm in names[:6]:
+        B = np.asfortranarray(z[f"qr/{nm}/B"])
+        opts = oracle.Opts(rtol=float(z[f"qr/{nm}/rtol"]), rank=int(z[f"qr/{nm}/rank"])).for_dtype(B.dtype)
+        W1, W2 = B.copy(order="F"), B.copy(order="F")
+        p1, _, k1 = oracle.geqp3_adap(W1, opts, backend="oracle")
+        p2, _, k2 = oracle.geqp3_adap(W2, opts, backend="c")
+        assert k1 == k2 and np.array_equal(p1, p2)
+
+
+@pytest.mark.skipif("not __import__('oracle.oracle', fromlist=['x']).lapack_available()")
+def test_lapack_pin_live(oracle):
+    rng = np.random.default_rng(5)
+    B = np.asfortranarray(rng.standard_normal((50, 200)) @ np.diag(np.exp(-np.arange(200) / 4)))
+    opts = oracle.Opts(rtol=1e-11).for_dtype(np.float64)
+    W1, W2 = B.copy(order="F"), B.copy(order="F")
+    p1, _, k1 = oracle.geqp3_adap(W1, opts, backend="lapack")
+    p2, _, k2 = oracle.geqp3_adap(W2, opts, backend="c")
+    assert k1 == k2 and np.array_equal(p1, p2)
+
+
+def test_hilbert_readme_ranks(oracle, golden):
+    h = golden["hilb"]
+    A = oracle.hilb(1024)
+    g = h["stream"].astype(np.float64) / 32.0
+    for tag, rtol, want in (("1e-12", 1e-12, {22}), ("default", None, {26, 27})):
+        V = oracle.idfact("n", A, oracle.Opts(rtol=rtol), oracle.RandStream(gauss=g))
+        assert V["k"] in want                       # README.md:107,122
+        assert V["k"] == int(h[f"{tag}/k"])
+        assert np.array_equal(V["sk"], h[f"{tag}/sk"])
+        # T = R11 \ R12 inherits cond(R11) (~1/rtol): compare it normwise
+        # loosely and the reconstruction it gives tightly
+        Tg = h[f"{tag}/T"]
+        if tag == "1e-12":   # at 5 eps, cond(R11) ~ 1/eps leaves T undetermined
+            assert np.linalg.norm(V["T"] - Tg) <= 1e-3 * np.linalg.norm(Tg)
+        E = oracle.id_matrix("n", A, V)
+        err = np.linalg.norm(A - E, 2) / np.linalg.norm(A, 2)
+        assert err <= 2 * float(h[f"{tag}/relerr2"]) + 1e-15
+
+
+def test_srft_restatement_matches_fft(oracle):
+    rng = np.random.default_rng(3)
+    X = rng.standard_normal((96, 5))
+    d = np.where(rng.standard_normal(96) > 0, 1.0, -1.0)
+    for k in (7, 8, 40):
+        idx = rng.integers(1, 97, k)
+        a = oracle._srft_apply_columns(X, d, idx, k)
+        b = oracle.srft_exact(X, d, idx, k)
+        assert np.allclose(a, b, rtol=1e-10, atol=1e-10)
+
+
+def real_fourier(m, n, seed=0):
+    rng = np.random.default_rng(seed)
+    return np.asfortranarray(np.real(np.exp(-2j * np.pi * np.outer(rng.random(m), rng.random(n)))))
+
+
+def streams(seed, n=200000):
+    rng = np.random.default_rng(seed)
+    return rng.standard_normal(n), rng
+
+
+SKETCHES = ["none", "randn", "sub", "srft", "sprn"]
+
+
+def rs_for(oracle, sketch, M, seed):
+    g, rng = streams(seed)
+    return oracle.RandStream(gauss=g, ints=rng.integers(1, 2**62, 200000, dtype=np.int64))
+
+
+@pytest.mark.parametrize("sketch", SKETCHES)
+@pytest.mark.parametrize("dt", [np.float32, np.float64])
+def test_reference_criteria_id(oracle, sketch, dt):
+    A = real_fourier(128, 64).astype(dt)
+    rtol = 5 * np.finfo(dt).eps
+    opts = oracle.Opts(rtol=rtol, sketch=sketch)
+    V = oracle.idfact("n", A, opts, rs_for(oracle, sketch, 128, 1))
+    E = oracle.id_matrix("n", A, V)
+    assert np.linalg.norm(A - E) < 100 * rtol * np.linalg.norm(A)     # test/id.jl:31
+
+
+@pytest.mark.parametrize("sketch", SKETCHES)
+def test_reference_criteria_psvd_pheig_cur(oracle, sketch):
+    A = real_fourier(128, 64)
+    rtol = 5 * np.finfo(np.float64).eps
+    opts = oracle.Opts(rtol=rtol, sketch=sketch)
+    F = oracle.psvdfact(A, opts, rs_for(oracle, sketch, 128, 2))
+    assert np.linalg.norm(A - (F["U"] * F["S"]) @ F["Vt"]) < 100 * rtol * np.linalg.norm(A)
+    H = real_fourier(128, 128, 4)
+    H = np.asfortranarray(H + H.T)
+    E = oracle.pheigfact(H, opts, rs_for(oracle, sketch, 128, 3))
+    assert np.linalg.norm(H - (E["vectors"] * E["values"]) @ E["vectors"].T) < 100 * rtol * np.linalg.norm(H)
+    U = oracle.curfact(A, opts, rs_for(oracle, sketch, 128, 5))
+    assert len(U["rows"]) == len(U["cols"]) > 0
+
+
+def test_snorm_criteria(oracle):
+    rng = np.random.default_rng(7)
+    A = rng.random((20, 10))
+    rs = oracle.RandStream(gauss=rng.standard_normal(100))
+    s = oracle.snorm_dense(A, oracle.Opts(), rs)
+    assert abs(s - np.linalg.norm(A, 2)) <= 100 * np.finfo(float).eps * np.linalg.norm(A, 2) * 10
+
+
+def test_maxdet_bounds_T(oracle):
+    A = real_fourier(128, 64)
+    opts = oracle.Opts(rtol=1e-10, maxdet_tol=0.0)
+    V = oracle.idfact("n", A, opts, rs_for(oracle, "randn", 128, 9))
+    assert np.abs(V["T"]).max() <= 1 + 1e-12
