@@ -193,3 +193,164 @@ template bool is_symmetric<float>(lra_ctx*, int64_t, const float*, int64_t);
 template bool is_symmetric<double>(lra_ctx*, int64_t, const double*, int64_t);
 
 }  // namespace lra
+
+// ---- blocked Cholesky and right triangular solve ----------------------------------
+// Used by the sketch-preconditioned Cholesky QR of the post-processing: the
+// skeleton columns A[:, sk] times R11^{-1} (R11 from the pivoted QR of the
+// sketch) are well conditioned, so their Gram matrix factors stably.
+
+namespace lra {
+
+namespace {
+
+constexpr int CB = 32;  // diagonal block size
+
+// upper Cholesky of the jb x jb diagonal block in place (one CTA); sets *bad
+// when the block is not positive definite
+template <typename T>
+__global__ void potrf_diag_kernel(int jb, T* G, int64_t ldg, int* bad) {
+  __shared__ T a[CB][CB + 1];
+  for (int t = threadIdx.x; t < jb * jb; t += blockDim.x) {
+    const int i = t % jb, j = t / jb;
+    a[i][j] = G[i + j * ldg];
+  }
+  __syncthreads();
+  for (int c = 0; c < jb; ++c) {
+    // a[c][c] <- sqrt(a[c][c] - sum_{r<c} a[r][c]^2); a[c][j] <- (...)/a[c][c]
+    if (threadIdx.x == 0) {
+      T d = a[c][c];
+      for (int r = 0; r < c; ++r) d -= a[r][c] * a[r][c];
+      if (!(d > T(0))) {
+        atomicExch(bad, 1);
+        d = T(1);
+      }
+      a[c][c] = sqrt(d);
+    }
+    __syncthreads();
+    for (int j = c + 1 + threadIdx.x; j < jb; j += blockDim.x) {
+      T s = a[c][j];
+      for (int r = 0; r < c; ++r) s -= a[r][c] * a[r][j];
+      a[c][j] = s / a[c][c];
+    }
+    __syncthreads();
+  }
+  for (int t = threadIdx.x; t < jb * jb; t += blockDim.x) {
+    const int i = t % jb, j = t / jb;
+    G[i + j * ldg] = i <= j ? a[i][j] : T(0);
+  }
+}
+
+// panel: R_{b, >b} = R_bb^{-T} G_{b, >b} (jb x nc), one thread per column
+template <typename T>
+__global__ void potrf_panel_kernel(int jb, int64_t nc, const T* Rbb, int64_t ldr, T* P, int64_t ldp) {
+  __shared__ T r[CB][CB + 1];
+  for (int t = threadIdx.x; t < jb * jb; t += blockDim.x) {
+    const int i = t % jb, j = t / jb;
+    r[i][j] = Rbb[i + j * ldr];
+  }
+  __syncthreads();
+  for (int64_t col = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; col < nc; col += (int64_t)gridDim.x * blockDim.x) {
+    T* p = P + col * ldp;
+    T x[CB];
+#pragma unroll
+    for (int i = 0; i < CB; ++i)
+      if (i < jb) x[i] = p[i];
+#pragma unroll
+    for (int i = 0; i < CB; ++i) {
+      if (i < jb) {
+        T s = x[i];
+#pragma unroll
+        for (int q = 0; q < CB; ++q)
+          if (q < i) s -= r[q][i] * x[q];
+        x[i] = s / r[i][i];
+      }
+    }
+#pragma unroll
+    for (int i = 0; i < CB; ++i)
+      if (i < jb) p[i] = x[i];
+  }
+}
+
+// X_b <- X_b R_bb^{-1} (m x jb), one thread per row
+template <typename T>
+__global__ void trsm_right_diag_kernel(int64_t m, int jb, const T* Rbb, int64_t ldr, T* X, int64_t ldx) {
+  __shared__ T r[CB][CB + 1];
+  for (int t = threadIdx.x; t < jb * jb; t += blockDim.x) {
+    const int i = t % jb, j = t / jb;
+    r[i][j] = Rbb[i + j * ldr];
+  }
+  __syncthreads();
+  for (int64_t row = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; row < m; row += (int64_t)gridDim.x * blockDim.x) {
+    T x[CB];
+#pragma unroll
+    for (int j = 0; j < CB; ++j)
+      if (j < jb) x[j] = X[row + j * ldx];
+    // x R = b: x_j = (b_j - sum_{i<j} x_i R_ij) / R_jj
+#pragma unroll
+    for (int j = 0; j < CB; ++j) {
+      if (j < jb) {
+        T s = x[j];
+#pragma unroll
+        for (int i = 0; i < CB; ++i)
+          if (i < j) s -= x[i] * r[i][j];
+        x[j] = s / r[j][j];
+      }
+    }
+#pragma unroll
+    for (int j = 0; j < CB; ++j)
+      if (j < jb) X[row + j * ldx] = x[j];
+  }
+}
+
+}  // namespace
+
+template <typename T>
+bool potrf_upper(lra_ctx* ctx, int64_t k, T* G, int64_t ldg) {
+  if (k <= 0) return true;
+  const ArenaMark mk = ctx->arena.mark();
+  int* bad = ctx->arena.alloc_n<int>(1);
+  LRA_CUDA(cudaMemsetAsync(bad, 0, sizeof(int), ctx->stream));
+  for (int64_t j0 = 0; j0 < k; j0 += CB) {
+    const int jb = (int)std::min<int64_t>(CB, k - j0);
+    T* Gjj = G + j0 + j0 * ldg;
+    potrf_diag_kernel<T><<<1, 256, 0, ctx->stream>>>(jb, Gjj, ldg, bad);
+    post_launch(ctx, "potrf_diag_kernel");
+    const int64_t rest = k - j0 - jb;
+    if (rest > 0) {
+      T* P = G + j0 + (j0 + jb) * ldg;
+      const unsigned g = (unsigned)std::max<int64_t>(1, std::min<int64_t>((rest + 127) / 128, ctx->num_sms * 4));
+      potrf_panel_kernel<T><<<g, 128, 0, ctx->stream>>>(jb, rest, Gjj, ldg, P, ldg);
+      post_launch(ctx, "potrf_panel_kernel");
+      // trailing: G_{>b,>b} -= P^T P
+      T* Gt = G + (j0 + jb) + (j0 + jb) * ldg;
+      gemm<T>(ctx, 't', 'n', rest, rest, jb, T(-1), P, ldg, P, ldg, T(1), Gt, ldg);
+    }
+  }
+  int h = 0;
+  LRA_CUDA(cudaMemcpyAsync(&h, bad, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+  LRA_CUDA(cudaStreamSynchronize(ctx->stream));
+  ctx->arena.release(mk);
+  return h == 0;
+}
+
+template <typename T>
+void trsm_right_upper(lra_ctx* ctx, int64_t m, int64_t k, const T* R, int64_t ldr, T* X, int64_t ldx) {
+  if (m <= 0 || k <= 0) return;
+  for (int64_t j0 = 0; j0 < k; j0 += CB) {
+    const int jb = (int)std::min<int64_t>(CB, k - j0);
+    const unsigned g = (unsigned)std::max<int64_t>(1, std::min<int64_t>((m + 127) / 128, ctx->num_sms * 8));
+    trsm_right_diag_kernel<T><<<g, 128, 0, ctx->stream>>>(m, jb, R + j0 + j0 * ldr, ldr, X + j0 * ldx, ldx);
+    post_launch(ctx, "trsm_right_diag_kernel");
+    const int64_t rest = k - j0 - jb;
+    if (rest > 0)  // X[:, >b] -= X_b R_{b, >b}
+      gemm<T>(ctx, 'n', 'n', m, rest, jb, T(-1), X + j0 * ldx, ldx, R + j0 + (j0 + jb) * ldr, ldr, T(1),
+              X + (j0 + jb) * ldx, ldx);
+  }
+}
+
+template bool potrf_upper<float>(lra_ctx*, int64_t, float*, int64_t);
+template bool potrf_upper<double>(lra_ctx*, int64_t, double*, int64_t);
+template void trsm_right_upper<float>(lra_ctx*, int64_t, int64_t, const float*, int64_t, float*, int64_t);
+template void trsm_right_upper<double>(lra_ctx*, int64_t, int64_t, const double*, int64_t, double*, int64_t);
+
+}  // namespace lra

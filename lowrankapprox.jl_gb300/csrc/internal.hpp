@@ -127,6 +127,14 @@ void orgqr(lra_ctx* ctx, int64_t m, int64_t k, T* V, int64_t ldv, const T* tau);
 template <typename T>
 void jacobi_svd(lra_ctx* ctx, int64_t n, T* X, int64_t ldx, T* V, int64_t ldv, T* S);
 
+// G = R^T R in place (upper R, lower part zeroed), blocked; false when G is
+// not numerically positive definite
+template <typename T>
+bool potrf_upper(lra_ctx* ctx, int64_t k, T* G, int64_t ldg);
+// X (m x k) <- X triu(R)^{-1}, blocked
+template <typename T>
+void trsm_right_upper(lra_ctx* ctx, int64_t m, int64_t k, const T* R, int64_t ldr, T* X, int64_t ldx);
+
 // exact symmetry test of a square device matrix
 template <typename T>
 bool is_symmetric(lra_ctx* ctx, int64_t n, const T* A, int64_t lda);

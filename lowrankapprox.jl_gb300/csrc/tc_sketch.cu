@@ -10,19 +10,22 @@
 // slices b_1 (signed, |b_1| <= 256) and b_2..b_ns (0..255), all exact in BF16.
 // Every product sigma * b is an integer below 2^15, so the FP32 sum of 512 of
 // them is an exact integer below 2^24: the tensor core loses nothing inside
-// a 512-long K chunk.  Slices 1..3 get their own TMEM accumulators; slices
-// 4..ns are pre-scaled by 2^-8(s-4) and share one FP32 tail accumulator
-// (its per-chunk rounding is ~2^-45 of the result).  All four are drained
-// after every chunk into one int64 per output,
-//     X += P1 2^24 + P2 2^16 + P3 2^8 + round(tail 2^8),
-// and B(r, j) = 2^(e_j - 37) X  (Float32: three slices, B = 2^(e_j-29) X).
+// a 512-long K chunk.  Slices 1..4 (E = min(ns, 4)) get their own TMEM
+// accumulators; slices 5..6 are pre-scaled by 2^-8(s-5) and share one FP32
+// tail accumulator, whose per-chunk rounding (~half a unit of P5) sits near
+// 2^-48 of the result.  All are drained after every chunk into one int64
+// per output,
+//     X += sum_a P_a 2^(8(E-a)+t) + round(tail 2^(t-8)),
+//     B(r, j) = 2^(e_j - 5 - 8E - t) X,
+// with t = 8 while |X| stays below 2^62 (K <= 32768), else t = 0.
 //
 // Kernel: 10 warps; warp 0 issues TMA loads (SW128, K-major) into a 2-stage
 // ring, warp 1 allocates TMEM and issues tcgen05.mma from one thread, warps
 // 2..9 drain the accumulators and write B.  Tile: 128 columns of op(A) (the
-// MMA M dimension, one TMEM lane each) x 128 sketch rows (MMA N).  Every
-// mbarrier wait is bounded by %globaltimer; a timeout records an error and
-// the kernel runs to its end, freeing TMEM.
+// MMA M dimension, one TMEM lane each) x 96 sketch rows (MMA N; five
+// accumulators of 96 columns fit the 512 TMEM columns).  Every mbarrier wait
+// is bounded by %globaltimer; a timeout records an error and the kernel runs
+// to its end, freeing TMEM.
 
 #include <cuda.h>
 #include <cuda_bf16.h>
@@ -39,19 +42,23 @@ namespace lra {
 namespace {
 
 constexpr int TILE_M = 128;   // columns of op(A) per CTA
-constexpr int TILE_N = 128;   // sketch rows per CTA
+constexpr int TILE_N = 96;    // sketch rows per CTA
 constexpr int KBLK = 64;      // K per stage (128 bytes of BF16: one SW128 row)
 constexpr int CHUNK_KB = 8;   // K-blocks per exact chunk (512)
 constexpr int NSTAGE = 2;
-constexpr int TILE_BYTES = TILE_M * KBLK * 2;  // 16 KB
+constexpr int TILE_BYTES = TILE_M * KBLK * 2;  // 16 KB (one slice tile)
+constexpr int S_BYTES = TILE_N * KBLK * 2;     // 12 KB (a 1024 multiple)
 constexpr int NTHREADS = 320;
 constexpr int MAX_SLICES = 6;
+constexpr int MAX_EXACT = 4;
+constexpr int COLS = TILE_N / 2;               // sketch rows per drain thread
 
 struct TcParams {
   int64_t K;       // sketched dimension (rows of op(A))
   int64_t ncols;   // columns of op(A)
   int64_t L;       // sketch order
   int ns;          // slices
+  int tshift;      // t above
   const int* colexp;
   void* B;
   int64_t ldb;
@@ -164,6 +171,15 @@ __device__ __forceinline__ void tmem_ld32(uint32_t taddr, uint32_t (&r)[32]) {
   asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
 }
 
+__device__ __forceinline__ void tmem_ld16(uint32_t taddr, uint32_t (&r)[16]) {
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
+      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]), "=r"(r[8]),
+        "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+      : "r"(taddr));
+  asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+}
+
 __device__ __forceinline__ void tc_fence_before() {
   asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
 }
@@ -179,7 +195,7 @@ __global__ void __launch_bounds__(NTHREADS, 1)
   // 1024-align the tile area
   unsigned char* base = reinterpret_cast<unsigned char*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
   const int ns = P.ns;
-  const int stage_bytes = (1 + ns) * TILE_BYTES;
+  const int stage_bytes = S_BYTES + ns * TILE_BYTES;
   unsigned char* stages = base;
   uint64_t* full = reinterpret_cast<uint64_t*>(base + NSTAGE * stage_bytes);
   uint64_t* empty = full + NSTAGE;
@@ -193,9 +209,10 @@ __global__ void __launch_bounds__(NTHREADS, 1)
   const int64_t n_tile = blockIdx.x / ntl, l_tile = blockIdx.x % ntl;
   const int nkb = (int)((P.K + KBLK - 1) / KBLK);
   const int nchunks = (nkb + CHUNK_KB - 1) / CHUNK_KB;
-  const int n_exact = ns < 3 ? ns : 3;
-  const bool has_tail = ns > 3;
+  const int n_exact = ns < MAX_EXACT ? ns : MAX_EXACT;
+  const bool has_tail = ns > MAX_EXACT;
   const int n_acc = n_exact + (has_tail ? 1 : 0);
+  const int t = has_tail ? P.tshift : 0;
 
   if (threadIdx.x == 0) {
     for (int s = 0; s < NSTAGE; ++s) {
@@ -230,7 +247,7 @@ __global__ void __launch_bounds__(NTHREADS, 1)
         mbar_expect_tx(full + s, (uint32_t)stage_bytes);
         tma_load_2d(st, &tmS, kb * KBLK, (int)(l_tile * TILE_N), full + s);
         for (int q = 0; q < ns; ++q)
-          tma_load_3d(st + (1 + q) * TILE_BYTES, &tmA, kb * KBLK, (int)(n_tile * TILE_M), q, full + s);
+          tma_load_3d(st + S_BYTES + q * TILE_BYTES, &tmA, kb * KBLK, (int)(n_tile * TILE_M), q, full + s);
       }
       // no copy may still be landing in shared memory when the CTA exits
       int dummy = 0;
@@ -241,38 +258,31 @@ __global__ void __launch_bounds__(NTHREADS, 1)
     // ---------------- MMA issuer ----------------
     if (lane == 0) {
       constexpr uint32_t idesc = idesc_bf16(TILE_M, TILE_N);
-      bool ok = true;
-      for (int kb = 0; kb < nkb && ok; ++kb) {
+      for (int kb = 0; kb < nkb; ++kb) {
         const int chunk = kb / CHUNK_KB;
         const bool chunk_start = (kb % CHUNK_KB) == 0;
         if (chunk_start && chunk > 0) {
           // the drain of the previous chunk must be done before overwriting
-          if (!mbar_wait(acc_free, (chunk - 1) & 1, P.err)) {
-            ok = false;
-            break;
-          }
+          if (!mbar_wait(acc_free, (chunk - 1) & 1, P.err)) break;
           tc_fence_after();
         }
         const int s = kb % NSTAGE;
         const uint32_t ph = (kb / NSTAGE) & 1;
-        if (!mbar_wait(full + s, ph, P.err)) {
-          ok = false;
-          break;
-        }
+        if (!mbar_wait(full + s, ph, P.err)) break;
         tc_fence_after();
         const uint32_t st = smem_u32(stages + s * stage_bytes);
         for (int q = 0; q < ns; ++q) {
-          const uint32_t acc = q < 3 ? tmem + (uint32_t)(q * TILE_N) : tmem + 3u * TILE_N;
-          const uint32_t a_addr = st + (uint32_t)((1 + q) * TILE_BYTES);
+          const int a = q < MAX_EXACT ? q : MAX_EXACT;  // accumulator
+          const uint32_t acc = tmem + (uint32_t)(a * TILE_N);
+          const uint32_t a_addr = st + (uint32_t)(S_BYTES + q * TILE_BYTES);
 #pragma unroll
           for (int k4 = 0; k4 < KBLK / 16; ++k4) {
             const uint64_t ad = sw128_desc(a_addr + k4 * 32);
             const uint64_t bd = sw128_desc(st + k4 * 32);
             // every accumulator restarts at each chunk; the tail slices
-            // (q >= 3) share one, reset by the first of them
-            const bool first = chunk_start && k4 == 0 && (q < 3 || q == 3);
-            const uint32_t accumulate = first ? 0u : 1u;
-            mma_bf16(acc, ad, bd, idesc, accumulate);
+            // share one, reset by the first of them
+            const bool first = chunk_start && k4 == 0 && q <= MAX_EXACT;
+            mma_bf16(acc, ad, bd, idesc, first ? 0u : 1u);
           }
         }
         mma_commit(empty + s);  // frees the stage once these MMAs complete
@@ -285,12 +295,12 @@ __global__ void __launch_bounds__(NTHREADS, 1)
     }
   } else {
     // ---------------- drain / epilogue: warps 2..9 ----------------
-    const int q4 = warp & 3;          // TMEM lane quarter this warp may access
-    const int half = (warp - 2) >> 2;  // which 64 of the 128 sketch rows
+    const int q4 = warp & 3;           // TMEM lane quarter this warp may access
+    const int half = (warp - 2) >> 2;  // which COLS of the TILE_N sketch rows
     const uint32_t lane_base = (uint32_t)(32 * q4) << 16;
-    long long X[64];
+    long long X[COLS];
 #pragma unroll
-    for (int c = 0; c < 64; ++c) X[c] = 0;
+    for (int c = 0; c < COLS; ++c) X[c] = 0;
     bool ok = true;
     for (int ch = 0; ch < nchunks; ++ch) {
       if (!mbar_wait(acc_ready, ch & 1, P.err)) {
@@ -298,22 +308,22 @@ __global__ void __launch_bounds__(NTHREADS, 1)
         break;
       }
       tc_fence_after();
-      // X += P1 2^(8(E-1)+t) + ... + P_E 2^t + round(tail 2^8), t = 8 with a tail
       for (int a = 0; a < n_acc; ++a) {
-        const int sh = 8 * (n_exact - 1 - a) + (has_tail ? 8 : 0);
+        const int sh = 8 * (n_exact - 1 - a) + t;
 #pragma unroll
-        for (int piece = 0; piece < 2; ++piece) {
-          uint32_t r[32];
-          tmem_ld32(tmem + lane_base + (uint32_t)(a * TILE_N + half * 64 + piece * 32), r);
+        for (int piece = 0; piece < COLS / 16; ++piece) {
+          uint32_t r[16];
+          tmem_ld16(tmem + lane_base + (uint32_t)(a * TILE_N + half * COLS + piece * 16), r);
           if (a < n_exact) {
 #pragma unroll
-            for (int c = 0; c < 32; ++c) {
+            for (int c = 0; c < 16; ++c) {
               const int iv = __float2int_rz(__uint_as_float(r[c]));
-              X[piece * 32 + c] += (long long)iv << sh;
+              X[piece * 16 + c] += (long long)iv << sh;
             }
           } else {
+            const float tsc = t ? 1.0f : (1.0f / 256.0f);  // tail weight 2^(t-8)
 #pragma unroll
-            for (int c = 0; c < 32; ++c) X[piece * 32 + c] += __float2ll_rn(__uint_as_float(r[c]) * 256.0f);
+            for (int c = 0; c < 16; ++c) X[piece * 16 + c] += __float2ll_rn(__uint_as_float(r[c]) * tsc);
           }
         }
       }
@@ -324,12 +334,11 @@ __global__ void __launch_bounds__(NTHREADS, 1)
     // epilogue: scale + store
     const int64_t j = n_tile * TILE_M + 32 * q4 + lane;  // column of op(A) / B
     const int e = (ok && j < P.ncols) ? P.colexp[j] : 0;
-    // B = 2^(e - 5 - 8 E - t) X,  E = exact slices, t = 8 with a tail
-    const int sc = e - 5 - 8 * n_exact - (has_tail ? 8 : 0);
-    const int64_t r0 = l_tile * TILE_N + half * 64;
+    const int sc = e - 5 - 8 * n_exact - t;  // B = 2^(e - 5 - 8E - t) X
+    const int64_t r0 = l_tile * TILE_N + half * COLS;
     if (ok && j < P.ncols) {
 #pragma unroll
-      for (int c = 0; c < 64; ++c) {
+      for (int c = 0; c < COLS; ++c) {
         const int64_t row = r0 + c;
         if (row < P.L) {
           const double v = ldexp((double)X[c], sc);
@@ -407,7 +416,7 @@ __device__ __forceinline__ __nv_bfloat16 bf16_of(int b, int k) {
 
 template <typename T>
 __device__ __forceinline__ void write_slices(long long F, int ns, int W, __nv_bfloat16* out, int64_t plane) {
-  const int n_exact = ns < 3 ? ns : 3;
+  const int n_exact = ns < MAX_EXACT ? ns : MAX_EXACT;
 #pragma unroll
   for (int s = 1; s <= MAX_SLICES; ++s) {
     if (s > ns) break;
@@ -570,12 +579,14 @@ void tc_sketch(lra_ctx* ctx, const TcSplit& sp, int64_t order, const T* S, T* B,
   P.ncols = N;
   P.L = order;
   P.ns = ns;
+  // |X| < 2^(24 + 8(E-1) + t + log2(chunks)): keep t = 8 while that is < 2^62
+  P.tshift = ((K + 511) / 512 <= 64) ? 8 : 0;
   P.colexp = sp.colexp;
   P.B = B;
   P.ldb = ldb;
   P.out_double = sizeof(T) == 8 ? 1 : 0;
   P.err = err;
-  const size_t smem = 1024 + (size_t)NSTAGE * (1 + ns) * TILE_BYTES + 256;
+  const size_t smem = 1024 + (size_t)NSTAGE * (S_BYTES + ns * TILE_BYTES) + 256;
   LRA_CUDA(cudaFuncSetAttribute(tc_sketch_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
   const int64_t ntiles = ((N + TILE_M - 1) / TILE_M) * (Lp / TILE_N);
   tc_sketch_kernel<<<(unsigned)ntiles, NTHREADS, smem, ctx->stream>>>(tmA, tmS, P);

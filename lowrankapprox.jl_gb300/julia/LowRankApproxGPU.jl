@@ -1,0 +1,218 @@
+#= LowRankApproxGPU.jl -- LowRankApprox.jl's sketch-then-factor entry points on
+   liblra (GB300, sm_103a) through `ccall`.
+
+   Drop-in for the path idfact / pqrfact / psvdfact / pheigfact / curfact /
+   sketch / sketchfact / snorm / snormdiff of LowRankApprox.jl: same names,
+   same LRAOptions fields, same result types (PartialQR, IDPackedV,
+   PartialSVD, PartialHermitianEigen, CURPackedU) -- the LowRankApprox
+   package provides the types and their algebra; this module only replaces
+   the factorization routines.  Every call lands in one C entry point of
+   include/lra.h; there is no Julia-side numerics and no CPU fallback.
+
+   Usage:
+     using LowRankApprox, LowRankApproxGPU
+     V = LowRankApproxGPU.idfact(A; rtol=1e-10, precision=:mixed)
+=#
+module LowRankApproxGPU
+
+using LinearAlgebra
+import LowRankApprox
+using LowRankApprox: LRAOptions, IDPackedV, PartialQR, PartialSVD, PartialHermitianEigen, CURPackedU,
+                     HermitianCURPackedU, PartialQRFactors
+
+const liblra = get(ENV, "LIBLRA", joinpath(@__DIR__, "..", "lowrankapprox", "liblra.so"))
+
+# ---- C structs (include/lra.h) ------------------------------------------------
+struct lra_opts
+  atol::Float64; maxdet_niter::Int64; maxdet_tol::Float64; nb::Int64; pheig_orthtol::Float64
+  pqrfact_retval::Int32; sketch::Int32; rank::Int64; rtol::Float64; sketch_randn_niter::Int64
+  sketchfact_adap::Int32; verb::Int32
+  randn_samp::NTuple{2,Int64}; srft_samp::NTuple{2,Int64}; sub_samp::NTuple{2,Int64}
+  snorm_niter::Int64; precision::Int32; check_finite::Int32; seed::UInt64
+end
+struct lra_rand;  gauss::Ptr{Float64}; gauss_len::Int64; ints::Ptr{Int64}; ints_len::Int64; end
+struct lra_id;    dtype::Int32; nsteps::Int32; k::Int64; n::Int64; sk::Ptr{Int64}; rd::Ptr{Int64}; T::Ptr{Cvoid}; end
+struct lra_pqr;   dtype::Int32; retval::Int32; m::Int64; n::Int64; k::Int64; p::Ptr{Int64}
+                  Q::Ptr{Cvoid}; R::Ptr{Cvoid}; T::Ptr{Cvoid}; end
+struct lra_psvd;  dtype::Int32; pad::Int32; m::Int64; n::Int64; k::Int64; U::Ptr{Cvoid}; S::Ptr{Cvoid}; Vt::Ptr{Cvoid}; end
+struct lra_pheig; dtype::Int32; pad::Int32; n::Int64; k::Int64; values::Ptr{Cvoid}; vectors::Ptr{Cvoid}; end
+struct lra_cur;   kind::Int32; pad::Int32; kr::Int64; kc::Int64; rows::Ptr{Int64}; cols::Ptr{Int64}; end
+
+const SKETCH = Dict(:none => 0, :randn => 1, :sprn => 2, :srft => 3, :sub => 4, :subs => 4)
+dtype(::Type{Float64}) = Int32(1)
+dtype(::Type{Float32}) = Int32(0)
+
+# an affine n -> a n + b, read off the option's function (src/LowRankApprox.jl:109-111)
+function affine(f)
+  b = f(0); a = f(1) - b
+  all(f(n) == a*n + b for n in (2, 7, 32, 1000)) || throw(ArgumentError("oversampling must be affine"))
+  (Int64(a), Int64(b))
+end
+
+function c_opts(o::LRAOptions; precision::Symbol=:native, seed::Integer=0x4c5241)
+  rv = lowercase(o.pqrfact_retval)
+  bits = Int32((occursin('q', rv) ? 1 : 0) | (occursin('r', rv) ? 2 : 0) | (occursin('t', rv) ? 4 : 0))
+  lra_opts(o.atol, o.maxdet_niter, o.maxdet_tol, o.nb, o.pheig_orthtol, bits, SKETCH[o.sketch], o.rank, o.rtol,
+           o.sketch_randn_niter, Int32(o.sketchfact_adap), Int32(o.verb), affine(o.sketchfact_randn_samp),
+           affine(o.sketchfact_srft_samp), affine(o.sketchfact_sub_samp), o.snorm_niter,
+           Int32(precision == :mixed), Int32(1), UInt64(seed))
+end
+
+# ---- context and errors ---------------------------------------------------------
+mutable struct Context
+  h::Ptr{Cvoid}
+  function Context(device::Integer=0)
+    r = Ref{Ptr{Cvoid}}(C_NULL)
+    st = ccall((:lra_ctx_create, liblra), Cint, (Cint, Ref{Ptr{Cvoid}}), device, r)
+    st == 0 || error("lra_ctx_create: ", unsafe_string(ccall((:lra_status_string, liblra), Cstring, (Cint,), st)))
+    c = new(r[])
+    finalizer(c -> ccall((:lra_ctx_destroy, liblra), Cvoid, (Ptr{Cvoid},), c.h), c)
+  end
+end
+const CTX = Ref{Context}()
+ctx() = (isassigned(CTX) || (CTX[] = Context()); CTX[])
+
+function check(st::Cint, c::Context)
+  st == 0 && return
+  msg = unsafe_string(ccall((:lra_last_error, liblra), Cstring, (Ptr{Cvoid},), c.h))
+  st == 1 && throw(ArgumentError(msg))               # LRA_EINVAL  (chkopts!, src/LowRankApprox.jl:133-148)
+  st == 2 && throw(DimensionMismatch(msg))           # LRA_EDIM
+  st == 9 && error("matrix must be Hermitian")       # LRA_ENOTHERM (src/pheig.jl:279)
+  error("liblra: ", msg, " (status ", st, ")")
+end
+
+opts_of(::Type{T}, opts, kw) where T = isempty(kw) ? (opts === nothing ? LRAOptions(T) : opts) :
+                                      copy(opts === nothing ? LRAOptions(T) : opts; kw...)
+
+take(ptr::Ptr{T}, n) where T = n == 0 ? T[] : copy(unsafe_wrap(Array, ptr, n))
+takem(ptr::Ptr{Cvoid}, ::Type{T}, m, n) where T = (m*n == 0 ? zeros(T, m, n) :
+                                                   copy(unsafe_wrap(Array, Ptr{T}(ptr), (m, n))))
+
+# ---- entry points --------------------------------------------------------------
+"idfact(trans, A[, opts]; precision=:native) -- src/id.jl:434-450 on the GPU."
+function idfact(trans::Symbol, A::StridedMatrix{T}, opts::Union{LRAOptions,Nothing}=nothing;
+                precision::Symbol=:native, kw...) where T<:Union{Float32,Float64}
+  o = opts_of(T, opts, kw); c = ctx(); out = Ref{Ptr{lra_id}}(C_NULL)
+  co = Ref(c_opts(o; precision))
+  st = ccall((:lra_idfact, liblra), Cint,
+             (Ptr{Cvoid}, Cint, Cchar, Int64, Int64, Ptr{T}, Int64, Ref{lra_opts}, Ptr{lra_rand}, Ref{Ptr{lra_id}}),
+             c.h, dtype(T), trans == :n ? 'n' : 'c', size(A,1), size(A,2), A, stride(A,2), co, C_NULL, out)
+  check(st, c)
+  r = unsafe_load(out[])
+  try
+    IDPackedV(take(r.sk, r.k), take(r.rd, r.n - r.k), takem(r.T, T, r.k, r.n - r.k))
+  finally
+    ccall((:lra_id_free, liblra), Cvoid, (Ptr{lra_id},), out[])
+  end
+end
+idfact(A::StridedMatrix, args...; kw...) = idfact(:n, A, args...; kw...)
+
+"pqrfact(trans, A[, opts]) -- src/pqr.jl:290-307 on the GPU."
+function pqrfact(trans::Symbol, A::StridedMatrix{T}, opts::Union{LRAOptions,Nothing}=nothing;
+                 precision::Symbol=:native, kw...) where T<:Union{Float32,Float64}
+  o = opts_of(T, opts, kw); c = ctx(); out = Ref{Ptr{lra_pqr}}(C_NULL)
+  co = Ref(c_opts(o; precision))
+  st = ccall((:lra_pqrfact, liblra), Cint,
+             (Ptr{Cvoid}, Cint, Cchar, Int64, Int64, Ptr{T}, Int64, Ref{lra_opts}, Ptr{lra_rand}, Ref{Ptr{lra_pqr}}),
+             c.h, dtype(T), trans == :n ? 'n' : 'c', size(A,1), size(A,2), A, stride(A,2), co, C_NULL, out)
+  check(st, c)
+  r = unsafe_load(out[])
+  try
+    p = take(r.p, r.n)
+    Q = (r.retval & 1) != 0 ? takem(r.Q, T, r.m, r.k) : nothing
+    R = (r.retval & 2) != 0 ? takem(r.R, T, r.k, r.n) : nothing
+    Tm = (r.retval & 4) != 0 ? takem(r.T, T, r.k, r.n - r.k) : nothing
+    Q !== nothing && R !== nothing && Tm === nothing && return PartialQR(Q, R, p)
+    PartialQRFactors(Q, R, p, r.k, Tm)
+  finally
+    ccall((:lra_pqr_free, liblra), Cvoid, (Ptr{lra_pqr},), out[])
+  end
+end
+pqrfact(A::StridedMatrix, args...; kw...) = pqrfact(:n, A, args...; kw...)
+
+function _psvd(A::StridedMatrix{T}, opts, vals::Bool; precision::Symbol=:native, kw...) where T
+  o = opts_of(T, opts, kw); c = ctx(); out = Ref{Ptr{lra_psvd}}(C_NULL)
+  co = Ref(c_opts(o; precision))
+  st = ccall((:lra_psvdfact, liblra), Cint,
+             (Ptr{Cvoid}, Cint, Int64, Int64, Ptr{T}, Int64, Ref{lra_opts}, Ptr{lra_rand}, Cint, Ref{Ptr{lra_psvd}}),
+             c.h, dtype(T), size(A,1), size(A,2), A, stride(A,2), co, C_NULL, Cint(vals), out)
+  check(st, c)
+  r = unsafe_load(out[])
+  try
+    S = take(Ptr{T}(r.S), r.k)
+    vals && return S
+    PartialSVD(takem(r.U, T, r.m, r.k), S, takem(r.Vt, T, r.k, r.n))
+  finally
+    ccall((:lra_psvd_free, liblra), Cvoid, (Ptr{lra_psvd},), out[])
+  end
+end
+"psvdfact(A[, opts]) -- src/psvd.jl:238-272 on the GPU."
+psvdfact(A::StridedMatrix{T}, opts::Union{LRAOptions,Nothing}=nothing; kw...) where T = _psvd(A, opts, false; kw...)
+"psvdvals(A[, opts]) -- src/psvd.jl:274-290 on the GPU."
+psvdvals(A::StridedMatrix{T}, opts::Union{LRAOptions,Nothing}=nothing; kw...) where T = _psvd(A, opts, true; kw...)
+psvd(A, args...; kw...) = (F = psvdfact(A, args...; kw...); (F.U, F.S, F.Vt'))
+
+function _pheig(A::StridedMatrix{T}, opts, vals::Bool; precision::Symbol=:native, kw...) where T
+  LinearAlgebra.checksquare(A)
+  o = opts_of(T, opts, kw); c = ctx(); out = Ref{Ptr{lra_pheig}}(C_NULL)
+  co = Ref(c_opts(o; precision))
+  st = ccall((:lra_pheigfact, liblra), Cint,
+             (Ptr{Cvoid}, Cint, Int64, Ptr{T}, Int64, Ref{lra_opts}, Ptr{lra_rand}, Cint, Ref{Ptr{lra_pheig}}),
+             c.h, dtype(T), size(A,1), A, stride(A,2), co, C_NULL, Cint(vals), out)
+  check(st, c)
+  r = unsafe_load(out[])
+  try
+    w = take(Ptr{T}(r.values), r.k)
+    vals && return w
+    PartialHermitianEigen(w, takem(r.vectors, T, r.n, r.k))
+  finally
+    ccall((:lra_pheig_free, liblra), Cvoid, (Ptr{lra_pheig},), out[])
+  end
+end
+"pheigfact(A[, opts]) -- src/pheig.jl:276-296 on the GPU."
+pheigfact(A::StridedMatrix{T}, opts::Union{LRAOptions,Nothing}=nothing; kw...) where T = _pheig(A, opts, false; kw...)
+pheigvals(A::StridedMatrix{T}, opts::Union{LRAOptions,Nothing}=nothing; kw...) where T = _pheig(A, opts, true; kw...)
+pheig(A, args...; kw...) = (F = pheigfact(A, args...; kw...); (F.values, F.vectors))
+
+"curfact(A[, opts]) -- src/cur.jl:532-564 on the GPU."
+function curfact(A::StridedMatrix{T}, opts::Union{LRAOptions,Nothing}=nothing; precision::Symbol=:native,
+                 kw...) where T<:Union{Float32,Float64}
+  o = opts_of(T, opts, kw); c = ctx(); out = Ref{Ptr{lra_cur}}(C_NULL)
+  co = Ref(c_opts(o; precision))
+  st = ccall((:lra_curfact, liblra), Cint,
+             (Ptr{Cvoid}, Cint, Int64, Int64, Ptr{T}, Int64, Ref{lra_opts}, Ptr{lra_rand}, Ref{Ptr{lra_cur}}),
+             c.h, dtype(T), size(A,1), size(A,2), A, stride(A,2), co, C_NULL, out)
+  check(st, c)
+  r = unsafe_load(out[])
+  try
+    rows = take(r.rows, r.kr); cols = take(r.cols, r.kc)
+    r.kind == 1 ? HermitianCURPackedU(cols) : CURPackedU(rows, cols)
+  finally
+    ccall((:lra_cur_free, liblra), Cvoid, (Ptr{lra_cur},), out[])
+  end
+end
+
+"snorm(A[, opts]) -- src/snorm.jl:14-45 on the GPU."
+function snorm(A::StridedMatrix{T}, opts::Union{LRAOptions,Nothing}=nothing; kw...) where T<:Union{Float32,Float64}
+  o = opts_of(T, opts, kw); c = ctx(); s = Ref{Float64}(0)
+  co = Ref(c_opts(o))
+  st = ccall((:lra_snorm, liblra), Cint,
+             (Ptr{Cvoid}, Cint, Int64, Int64, Ptr{T}, Int64, Cint, Ref{lra_opts}, Ptr{lra_rand}, Ref{Float64}),
+             c.h, dtype(T), size(A,1), size(A,2), A, stride(A,2), Cint(-1), co, C_NULL, s)
+  check(st, c)
+  s[]
+end
+
+"snormdiff(A, B[, opts]) -- src/snorm.jl:50-53 on the GPU."
+function snormdiff(A::StridedMatrix{T}, B::StridedMatrix{T}, opts::Union{LRAOptions,Nothing}=nothing;
+                   kw...) where T<:Union{Float32,Float64}
+  o = opts_of(T, opts, kw); c = ctx(); s = Ref{Float64}(0)
+  co = Ref(c_opts(o))
+  st = ccall((:lra_snormdiff, liblra), Cint,
+             (Ptr{Cvoid}, Cint, Int64, Int64, Ptr{T}, Int64, Ptr{T}, Int64, Ref{lra_opts}, Ptr{lra_rand}, Ref{Float64}),
+             c.h, dtype(T), size(A,1), size(A,2), A, stride(A,2), B, stride(B,2), co, C_NULL, s)
+  check(st, c)
+  s[]
+end
+
+end # module
