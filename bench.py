@@ -50,15 +50,14 @@ def make_matrix(n: int, rank_cols: int = 1024):
     """A = U diag(s) V' built on the GPU from seeded numpy Gaussians."""
     import torch
     r = min(n, rank_cols)
-    G1 = torch.from_numpy(np.random.default_rng(1).standard_normal((n, r))).cuda()
-    G2 = torch.from_numpy(np.random.default_rng(2).standard_normal((n, r))).cuda()
-    U, R1 = torch.linalg.qr(G1)
-    V, R2 = torch.linalg.qr(G2)
-    U = U * torch.sign(torch.diagonal(R1))[None, :]
-    V = V * torch.sign(torch.diagonal(R2))[None, :]
+    facs = []
+    for seed in (1, 2):
+        Q, R = np.linalg.qr(np.random.default_rng(seed).standard_normal((n, r)))
+        facs.append(torch.from_numpy(Q * np.sign(np.diag(R))[None, :]).cuda())
+    U, V = facs
     s = torch.pow(10.0, -torch.arange(r, dtype=torch.float64, device="cuda") / 40.0)
     A = (U * s[None, :]) @ V.T
-    del G1, G2, U, V
+    del U, V, facs
     # column-major storage
     return A.t().contiguous().t()
 

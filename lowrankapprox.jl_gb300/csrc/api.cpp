@@ -322,6 +322,8 @@ struct Fact {
   int64_t k = 0;
   int nsteps = 0;
   T* T_ = nullptr;  // k x (N - k), ld = k
+  int64_t swaps = 0;  // maxdet swaps: when > 0, R11 no longer matches sk
+  bool embed = true;  // B = S op(A) with S a subspace embedding (randn/srft)
 };
 
 template <typename T>
@@ -423,9 +425,29 @@ Fact<T> id_core(lra_ctx* ctx, const lra_opts& o, char trans, int64_t m, int64_t 
     F = pqr_backend_dev<T>(ctx, o, B, M, N, M);
   } else {
     F = sketchfact_dev<T>(ctx, o, trans, M, N, A.p, A.ld, rs, dtype);
+    F.embed = o.sketch == LRA_SKETCH_RANDN || o.sketch == LRA_SKETCH_SRFT;
   }
   postproc_t<T>(ctx, o, F, want_t);
   return F;
+}
+
+// A[:, sk] = Q R_A through the sketch-preconditioned Cholesky QR; Ask (M x k,
+// ld M) becomes Q.  False when R11 does not precondition A[:, sk] (maxdet
+// swaps) or a Cholesky factorization broke down; Ask is then left damaged
+// and the caller regathers it.
+template <typename T>
+bool skeleton_qr(lra_ctx* ctx, const Fact<T>& F, int64_t M, T* Ask, T* RA, int dtype) {
+  const int64_t k = F.k, kk = std::max<int64_t>(k, 1);
+  if (F.swaps > 0) return false;
+  const int passes = (dtype == LRA_F64 && F.embed) ? 1 : 2;
+  T* Rc = ctx->arena.alloc_n<T>((size_t)kk * kk);
+  if (!cholqr_pre<T>(ctx, M, k, Ask, std::max<int64_t>(M, 1), F.B, F.ld, passes, Rc)) return false;
+  // R_A = Rc R11
+  T* R11 = ctx->arena.alloc_n<T>((size_t)kk * kk);
+  copy_matrix(ctx, k, k, F.B, F.ld, R11, kk);
+  zero_lower(ctx, k, k, R11, kk);
+  gemm<T>(ctx, 'n', 'n', k, k, k, T(1), Rc, kk, R11, kk, T(0), RA, kk);
+  return true;
 }
 
 // getcols(trans, A, idx): M x k device matrix
@@ -468,6 +490,7 @@ void maxdet_dev(lra_ctx* ctx, const lra_opts& o, Fact<T>& F) {
     if (!upd) break;
     ++niter;
   }
+  F.swaps = niter;
 }
 
 }  // namespace
@@ -834,17 +857,20 @@ int lra_pqrfact(lra_ctx* ctx, int dtype, char trans, int64_t m, int64_t n, const
           F = id_core<T>(ctx, oi, t, m, n, dA, rs, dtype, true);
           const int64_t k = F.k;
           T* Ask = getcols<T>(ctx, t, m, n, dA, F.jpvt, k);
-          int64_t* jp = ctx->arena.alloc_n<int64_t>(std::max<int64_t>(k, 1));
-          T* tau = ctx->arena.alloc_n<T>(std::max<int64_t>(k, 1));
-          {
-            Stage st(ctx, 3);
-            geqp3_adap<T>(ctx, M, k, Ask, std::max<int64_t>(M, 1), jp, tau, k, 32, -1.0, 0.0, false);
-          }
           R11 = ctx->arena.alloc_n<T>((size_t)std::max<int64_t>(k * k, 1));
-          copy_matrix(ctx, k, k, Ask, std::max<int64_t>(M, 1), R11, std::max<int64_t>(k, 1));
-          if (rq) {
-            orgqr(ctx, M, k, Ask, std::max<int64_t>(M, 1), tau);
-            Qd = Ask;
+          Stage st(ctx, 3);
+          if (skeleton_qr<T>(ctx, F, M, Ask, R11, dtype)) {
+            Qd = Ask;  // Cholesky QR preconditioned by the sketch's R11
+          } else {
+            Ask = getcols<T>(ctx, t, m, n, dA, F.jpvt, k);
+            int64_t* jp = ctx->arena.alloc_n<int64_t>(std::max<int64_t>(k, 1));
+            T* tau = ctx->arena.alloc_n<T>(std::max<int64_t>(k, 1));
+            geqp3_adap<T>(ctx, M, k, Ask, std::max<int64_t>(M, 1), jp, tau, k, 32, -1.0, 0.0, false);
+            copy_matrix(ctx, k, k, Ask, std::max<int64_t>(M, 1), R11, std::max<int64_t>(k, 1));
+            if (rq) {
+              orgqr(ctx, M, k, Ask, std::max<int64_t>(M, 1), tau);
+              Qd = Ask;
+            }
           }
         }
         const int64_t k = F.k;
@@ -972,13 +998,54 @@ lra_psvd* psvd_dev(lra_ctx* ctx, const lra_opts& o, char trans, int64_t m, int64
   Fact<T> F = id_core<T>(ctx, oi, trans, m, n, dA, rs, dtype, true);
   const int64_t k = F.k;
   Stage st(ctx, 3);
-  // Q, R = qr(A[:, sk])
+  const int64_t ldq = std::max<int64_t>(M, 1), ldk = std::max<int64_t>(k, 1);
+  {
+    // GEMM-shaped route: A[:, sk] = Q R_A, V^T = Q_v R_v, SVD(R_A R_v^T)
+    const ArenaMark mk = ctx->arena.mark();
+    T* Q = getcols<T>(ctx, trans, m, n, dA, F.jpvt, k);
+    T* RA = ctx->arena.alloc_n<T>((size_t)ldk * ldk);
+    T* Rv = ctx->arena.alloc_n<T>((size_t)ldk * ldk);
+    if (skeleton_qr<T>(ctx, F, M, Q, RA, dtype) && chol_v<T>(ctx, k, N - k, F.T_, Rv)) {
+      T* Mm = ctx->arena.alloc_n<T>((size_t)ldk * ldk);
+      gemm<T>(ctx, 'n', 't', k, k, k, T(1), RA, ldk, Rv, ldk, T(0), Mm, ldk);
+      T* UM = ctx->arena.alloc_n<T>((size_t)ldk * ldk);
+      T* VM = ctx->arena.alloc_n<T>((size_t)ldk * ldk);
+      T* S = ctx->arena.alloc_n<T>(ldk);
+      std::vector<T> hS = small_svd<T>(ctx, k, Mm, UM, VM, S);
+      std::vector<double> sd(hS.begin(), hS.end());
+      const int64_t kk = psvdrank(sd, o), lkk = std::max<int64_t>(kk, 1);
+      lra_psvd* r = static_cast<lra_psvd*>(hmalloc(sizeof(lra_psvd)));
+      std::memset(r, 0, sizeof *r);
+      r->dtype = dtype;
+      r->k = kk;
+      r->S = hmalloc(sizeof(T) * lkk);
+      std::memcpy(r->S, hS.data(), sizeof(T) * kk);
+      if (vals_only) return r;
+      // U = Q U_M(:, 1:kk)
+      T* U = ctx->arena.alloc_n<T>((size_t)ldq * lkk);
+      gemm<T>(ctx, 'n', 'n', M, kk, k, T(1), Q, ldq, UM, ldk, T(0), U, ldq);
+      // Vt = Z^T V,  Z = R_v^{-1} V_M(:, 1:kk):  Vt[:, p] = [Z^T | Z^T T]
+      trsm_upper(ctx, k, kk, Rv, ldk, VM, ldk);
+      T* Vp = ctx->arena.alloc_n<T>((size_t)lkk * std::max<int64_t>(N, 1));
+      transpose(ctx, k, kk, VM, ldk, Vp, lkk);
+      if (N > k) gemm<T>(ctx, 't', 'n', kk, N - k, k, T(1), VM, ldk, F.T_, ldk, T(0), Vp + k * lkk, lkk);
+      T* Vt = ctx->arena.alloc_n<T>((size_t)lkk * std::max<int64_t>(N, 1));
+      scatter_cols(ctx, kk, N, Vp, lkk, F.jpvt, Vt, lkk);
+      r->U = hmalloc(sizeof(T) * std::max<int64_t>(M * kk, 1));
+      r->Vt = hmalloc(sizeof(T) * std::max<int64_t>(kk * N, 1));
+      to_host(ctx, r->U, U, (size_t)M * kk);
+      to_host(ctx, r->Vt, Vt, (size_t)kk * N);
+      LRA_CUDA(cudaStreamSynchronize(ctx->stream));
+      return r;
+    }
+    ctx->arena.release(mk);
+  }
+  // Householder route (the skeleton moved under maxdet, or a Cholesky broke
+  // down): Q, R = qr(A[:, sk])
   T* Ask = getcols<T>(ctx, trans, m, n, dA, F.jpvt, k);
-  const int64_t ldq = std::max<int64_t>(M, 1);
   int64_t* jp = ctx->arena.alloc_n<int64_t>(std::max<int64_t>(k, 1));
   T* tau = ctx->arena.alloc_n<T>(std::max<int64_t>(k, 1));
   geqp3_adap<T>(ctx, M, k, Ask, ldq, jp, tau, k, 32, -1.0, 0.0, false);
-  const int64_t ldk = std::max<int64_t>(k, 1);
   T* R = ctx->arena.alloc_n<T>((size_t)ldk * ldk);
   copy_matrix(ctx, k, k, Ask, ldq, R, ldk);
   zero_lower(ctx, k, k, R, ldk);
@@ -1112,23 +1179,29 @@ int lra_pheigfact(lra_ctx* ctx, int dtype, int64_t n, const void* A, int64_t lda
       Fact<T> F = id_core<T>(ctx, oi, 'n', n, n, dA, rs, dtype, true);
       const int64_t k = F.k, ldk = std::max<int64_t>(k, 1), ldn = std::max<int64_t>(n, 1);
       Stage st(ctx, 3);
-      // V' = P [I; T'] (n x k) and its QR
-      T* Vt = ctx->arena.alloc_n<T>((size_t)ldn * ldk);
-      set_zero(ctx, Vt, ldn * ldk);
-      T* I = ctx->arena.alloc_n<T>((size_t)ldk * ldk);
-      set_identity(ctx, k, k, I, ldk);
-      scatter_rows(ctx, k, k, I, ldk, F.jpvt, Vt, ldn);
-      if (n > k) {
-        T* Tt = ctx->arena.alloc_n<T>((size_t)(n - k) * ldk);
-        transpose(ctx, k, n - k, F.T_, ldk, Tt, n - k);
-        scatter_rows(ctx, n - k, k, Tt, n - k, F.jpvt + k, Vt, ldn);
-      }
-      int64_t* jp = ctx->arena.alloc_n<int64_t>(ldk);
-      T* tau = ctx->arena.alloc_n<T>(ldk);
-      geqp3_adap<T>(ctx, n, k, Vt, ldn, jp, tau, k, 32, -1.0, 0.0, false);
+      // V' = P [I; T'] (n x k) = Q_v R: R = chol(I + T T') (V V' = I + T T'),
+      // Q_v = V' R^{-1} is applied in factored form below; the Householder
+      // QR of V' remains for a (theoretical) Cholesky breakdown
       T* R = ctx->arena.alloc_n<T>((size_t)ldk * ldk);
-      copy_matrix(ctx, k, k, Vt, ldn, R, ldk);
-      zero_lower(ctx, k, k, R, ldk);
+      T* Vt = nullptr;
+      T* tau = nullptr;
+      if (!chol_v<T>(ctx, k, n - k, F.T_, R)) {
+        Vt = ctx->arena.alloc_n<T>((size_t)ldn * ldk);
+        set_zero(ctx, Vt, ldn * ldk);
+        T* I = ctx->arena.alloc_n<T>((size_t)ldk * ldk);
+        set_identity(ctx, k, k, I, ldk);
+        scatter_rows(ctx, k, k, I, ldk, F.jpvt, Vt, ldn);
+        if (n > k) {
+          T* Tt = ctx->arena.alloc_n<T>((size_t)(n - k) * ldk);
+          transpose(ctx, k, n - k, F.T_, ldk, Tt, n - k);
+          scatter_rows(ctx, n - k, k, Tt, n - k, F.jpvt + k, Vt, ldn);
+        }
+        int64_t* jp = ctx->arena.alloc_n<int64_t>(ldk);
+        tau = ctx->arena.alloc_n<T>(ldk);
+        geqp3_adap<T>(ctx, n, k, Vt, ldn, jp, tau, k, 32, -1.0, 0.0, false);
+        copy_matrix(ctx, k, k, Vt, ldn, R, ldk);
+        zero_lower(ctx, k, k, R, ldk);
+      }
       // B = R (A[sk, sk] R')
       T* Ar = ctx->arena.alloc_n<T>((size_t)ldk * ldn);
       gather_rows(ctx, k, n, dA.p, dA.ld, F.jpvt, Ar, ldk);
@@ -1213,7 +1286,21 @@ int lra_pheigfact(lra_ctx* ctx, int dtype, int64_t n, const void* A, int64_t lda
           LRA_CUDA(cudaMemcpyAsync(dcl, cl.data(), cl.size() * sizeof(int64_t), cudaMemcpyHostToDevice, ctx->stream));
           cluster_orth(ctx, k, ke, Zs, ldn, dcl, (int64_t)cl.size() / 2);
         }
-        apply_q<T>(ctx, 'n', n, k, Vt, ldn, tau, Zs, ldn, ke);
+        if (Vt) {
+          apply_q<T>(ctx, 'n', n, k, Vt, ldn, tau, Zs, ldn, ke);
+        } else {
+          // Q_v Z = P [I; T'] (R^{-1} Z): rows sk <- Y, rows rd <- T' Y
+          T* Y = ctx->arena.alloc_n<T>((size_t)ldk * ke);
+          copy_matrix(ctx, k, ke, Zs, ldn, Y, ldk);
+          trsm_upper(ctx, k, ke, R, ldk, Y, ldk);
+          set_zero(ctx, Zs, ldn * ke);
+          scatter_rows(ctx, k, ke, Y, ldk, F.jpvt, Zs, ldn);
+          if (n > k) {
+            T* TY = ctx->arena.alloc_n<T>((size_t)(n - k) * ke);
+            gemm<T>(ctx, 't', 'n', n - k, ke, k, T(1), F.T_, ldk, Y, ldk, T(0), TY, n - k);
+            scatter_rows(ctx, n - k, ke, TY, n - k, F.jpvt + k, Zs, ldn);
+          }
+        }
         r->vectors = hmalloc(sizeof(T) * (size_t)n * ke);
         to_host(ctx, r->vectors, Zs, (size_t)n * ke);
         LRA_CUDA(cudaStreamSynchronize(ctx->stream));

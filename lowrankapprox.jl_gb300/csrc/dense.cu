@@ -34,6 +34,8 @@ struct JacParams {
   int* sweeps_out;
 };
 
+constexpr int JCH = 16;  // rows per lane per register chunk (512 rows)
+
 __device__ __forceinline__ void rr_pair(int64_t r, int64_t s, int64_t nn, int64_t& p, int64_t& q) {
   auto pos = [&](int64_t i) -> int64_t { return i == 0 ? 0 : 1 + (i - 1 + r) % (nn - 1); };
   p = pos(s);
@@ -64,12 +66,24 @@ __global__ void __launch_bounds__(NT) jacobi_kernel(JacParams<T> P) {
         }
         T* xp = P.X + p * P.ldx;
         T* xq = P.X + q * P.ldx;
+        // both columns are pulled into registers with independent loads
+        // (one L2 round trip per chunk), reduced, rotated and stored
         double a = 0, b = 0, g = 0;
-        for (int64_t i = lane; i < n; i += 32) {
-          const double u = __ldcg(xp + i), v = __ldcg(xq + i);
-          a = fma(u, u, a);
-          b = fma(v, v, b);
-          g = fma(u, v, g);
+        double u[JCH], w[JCH];
+        const bool one = n <= 32 * JCH;
+        for (int64_t b0 = 0; b0 < n; b0 += 32 * JCH) {
+#pragma unroll
+          for (int t = 0; t < JCH; ++t) {
+            const int64_t i = b0 + lane + 32 * t;
+            u[t] = i < n ? (double)__ldcg(xp + i) : 0.0;
+            w[t] = i < n ? (double)__ldcg(xq + i) : 0.0;
+          }
+#pragma unroll
+          for (int t = 0; t < JCH; ++t) {
+            a = fma(u[t], u[t], a);
+            b = fma(w[t], w[t], b);
+            g = fma(u[t], w[t], g);
+          }
         }
         a = warp_sum(a);
         b = warp_sum(b);
@@ -82,17 +96,41 @@ __global__ void __launch_bounds__(NT) jacobi_kernel(JacParams<T> P) {
         const double t = copysign(1.0, zeta) / (fabs(zeta) + sqrt(1.0 + zeta * zeta));
         const double c = 1.0 / sqrt(1.0 + t * t);
         const double sn = c * t;
-        for (int64_t i = lane; i < n; i += 32) {
-          const double u = __ldcg(xp + i), v = __ldcg(xq + i);
-          xp[i] = (T)(c * u - sn * v);
-          xq[i] = (T)(sn * u + c * v);
+        for (int64_t b0 = 0; b0 < n; b0 += 32 * JCH) {
+          if (!one) {
+#pragma unroll
+            for (int tt = 0; tt < JCH; ++tt) {
+              const int64_t i = b0 + lane + 32 * tt;
+              u[tt] = i < n ? (double)__ldcg(xp + i) : 0.0;
+              w[tt] = i < n ? (double)__ldcg(xq + i) : 0.0;
+            }
+          }
+#pragma unroll
+          for (int tt = 0; tt < JCH; ++tt) {
+            const int64_t i = b0 + lane + 32 * tt;
+            if (i < n) {
+              xp[i] = (T)(c * u[tt] - sn * w[tt]);
+              xq[i] = (T)(sn * u[tt] + c * w[tt]);
+            }
+          }
         }
         T* vp = P.V + p * P.ldv;
         T* vq = P.V + q * P.ldv;
-        for (int64_t i = lane; i < n; i += 32) {
-          const double u = __ldcg(vp + i), v = __ldcg(vq + i);
-          vp[i] = (T)(c * u - sn * v);
-          vq[i] = (T)(sn * u + c * v);
+        for (int64_t b0 = 0; b0 < n; b0 += 32 * JCH) {
+#pragma unroll
+          for (int tt = 0; tt < JCH; ++tt) {
+            const int64_t i = b0 + lane + 32 * tt;
+            u[tt] = i < n ? (double)__ldcg(vp + i) : 0.0;
+            w[tt] = i < n ? (double)__ldcg(vq + i) : 0.0;
+          }
+#pragma unroll
+          for (int tt = 0; tt < JCH; ++tt) {
+            const int64_t i = b0 + lane + 32 * tt;
+            if (i < n) {
+              vp[i] = (T)(c * u[tt] - sn * w[tt]);
+              vq[i] = (T)(sn * u[tt] + c * w[tt]);
+            }
+          }
         }
       }
       if (!grid_sync(P.bar)) return;
@@ -139,7 +177,7 @@ __global__ void symcheck_kernel(int64_t n, const T* __restrict__ A, int64_t lda,
 
 template <typename T>
 void jacobi_svd(lra_ctx* ctx, int64_t n, T* X, int64_t ldx, T* V, int64_t ldv, T* S) {
-  constexpr int NT = 256;
+  constexpr int NT = 128;
   if (n <= 0) return;
   set_identity(ctx, n, n, V, ldv);
   const ArenaMark mk = ctx->arena.mark();
@@ -326,6 +364,7 @@ bool potrf_upper(lra_ctx* ctx, int64_t k, T* G, int64_t ldg) {
       gemm<T>(ctx, 't', 'n', rest, rest, jb, T(-1), P, ldg, P, ldg, T(1), Gt, ldg);
     }
   }
+  zero_lower(ctx, k, k, G, ldg);  // the factor is used as a dense matrix later
   int h = 0;
   LRA_CUDA(cudaMemcpyAsync(&h, bad, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
   LRA_CUDA(cudaStreamSynchronize(ctx->stream));

@@ -15,11 +15,21 @@ namespace {
 constexpr int BM = 64, BN = 64, BK = 16, TM = 4, TN = 4;
 constexpr int NT = (BM / TM) * (BN / TN);  // 256
 
+// blockIdx.y selects a K slice of length kchunk; with gridDim.y > 1 each
+// slice writes its own partial product to C + y * ldc * N (split-K)
 template <typename T, bool TA, bool TB>
 __global__ void __launch_bounds__(NT) gemm_kernel(int64_t M, int64_t N, int64_t K, T alpha,
                                                   const T* __restrict__ A, int64_t lda,
                                                   const T* __restrict__ B, int64_t ldb, T beta,
-                                                  T* __restrict__ C, int64_t ldc) {
+                                                  T* __restrict__ C, int64_t ldc, int64_t kchunk) {
+  {
+    const int64_t k0 = (int64_t)blockIdx.y * kchunk;
+    if (k0 >= K) return;
+    K = min(K - k0, kchunk);
+    A += TA ? k0 : k0 * lda;
+    B += TB ? k0 * ldb : k0;
+    C += (int64_t)blockIdx.y * ldc * N;
+  }
   __shared__ T As[2][BK][BM + 1];
   __shared__ T Bs[2][BK][BN + 1];
   const int tid = threadIdx.x;
@@ -136,6 +146,20 @@ __global__ void __launch_bounds__(NT) gemm_kernel(int64_t M, int64_t N, int64_t 
 }
 
 template <typename T>
+__global__ void splitk_reduce_kernel(int64_t m, int64_t n, int64_t nsplit, const T* __restrict__ W, T alpha, T beta,
+                                     T* __restrict__ C, int64_t ldc) {
+  const int64_t total = m * n;
+  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < total;
+       t += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t i = t % m, j = t / m;
+    T s = 0;
+    for (int64_t q = 0; q < nsplit; ++q) s += W[q * total + t];
+    T* c = C + i + j * ldc;
+    *c = (beta == T(0)) ? alpha * s : alpha * s + beta * *c;
+  }
+}
+
+template <typename T>
 __global__ void scale_kernel(int64_t m, int64_t n, T beta, T* C, int64_t ldc) {
   const int64_t total = m * n;
   for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < total;
@@ -161,14 +185,39 @@ void gemm(lra_ctx* ctx, char ta, char tb, int64_t m, int64_t n, int64_t k, T alp
   const bool TB = (tb == 't' || tb == 'T' || tb == 'c' || tb == 'C');
   const int64_t tiles = ((m + BM - 1) / BM) * ((n + BN - 1) / BN);
   const unsigned g = (unsigned)std::min<int64_t>(tiles, (int64_t)ctx->num_sms * 4);
+  // split K when the tiles alone leave most SMs idle
+  int64_t nsplit = 1;
+  if (tiles < ctx->num_sms && k >= 1024)
+    nsplit = std::min<int64_t>((2 * ctx->num_sms + tiles - 1) / tiles, k / 256);
+  const int64_t kchunk = (k + nsplit - 1) / nsplit;
+  nsplit = (k + kchunk - 1) / kchunk;
+  T* out = C;
+  int64_t ldo = ldc;
+  T al = alpha, be = beta;
+  const ArenaMark mk = ctx->arena.mark();
+  if (nsplit > 1) {
+    out = ctx->arena.alloc_n<T>((size_t)nsplit * m * n);
+    ldo = m;
+    al = T(1);
+    be = T(0);
+  }
+  const dim3 grid(g, (unsigned)nsplit);
   if (!TA && !TB)
-    gemm_kernel<T, false, false><<<g, NT, 0, ctx->stream>>>(m, n, k, alpha, A, lda, B, ldb, beta, C, ldc);
+    gemm_kernel<T, false, false><<<grid, NT, 0, ctx->stream>>>(m, n, k, al, A, lda, B, ldb, be, out, ldo, kchunk);
   else if (TA && !TB)
-    gemm_kernel<T, true, false><<<g, NT, 0, ctx->stream>>>(m, n, k, alpha, A, lda, B, ldb, beta, C, ldc);
+    gemm_kernel<T, true, false><<<grid, NT, 0, ctx->stream>>>(m, n, k, al, A, lda, B, ldb, be, out, ldo, kchunk);
   else if (!TA && TB)
-    gemm_kernel<T, false, true><<<g, NT, 0, ctx->stream>>>(m, n, k, alpha, A, lda, B, ldb, beta, C, ldc);
+    gemm_kernel<T, false, true><<<grid, NT, 0, ctx->stream>>>(m, n, k, al, A, lda, B, ldb, be, out, ldo, kchunk);
   else
-    gemm_kernel<T, true, true><<<g, NT, 0, ctx->stream>>>(m, n, k, alpha, A, lda, B, ldb, beta, C, ldc);
+    gemm_kernel<T, true, true><<<grid, NT, 0, ctx->stream>>>(m, n, k, al, A, lda, B, ldb, be, out, ldo, kchunk);
+  if (nsplit > 1) {
+    post_launch(ctx, "gemm_kernel");
+    const unsigned gr = (unsigned)std::max<int64_t>(1, std::min<int64_t>((m * n + 255) / 256, ctx->num_sms * 8));
+    splitk_reduce_kernel<T><<<gr, 256, 0, ctx->stream>>>(m, n, nsplit, out, alpha, beta, C, ldc);
+    ctx->arena.release(mk);  // stream-ordered reuse
+    post_launch(ctx, "splitk_reduce_kernel");
+    return;
+  }
   post_launch(ctx, "gemm_kernel");
 }
 

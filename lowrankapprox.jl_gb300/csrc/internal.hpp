@@ -135,6 +135,21 @@ bool potrf_upper(lra_ctx* ctx, int64_t k, T* G, int64_t ldg);
 template <typename T>
 void trsm_right_upper(lra_ctx* ctx, int64_t m, int64_t k, const T* R, int64_t ldr, T* X, int64_t ldx);
 
+// post.cu: X (m x k) <- X Rpre^{-1} (if Rpre), then `passes` Cholesky QR
+// passes; on exit X is orthonormal and the input equals X Rc Rpre.  False
+// on a Cholesky breakdown.
+template <typename T>
+bool cholqr_pre(lra_ctx* ctx, int64_t m, int64_t k, T* X, int64_t ldx, const T* Rpre, int64_t ldr,
+                int passes, T* Rc);
+// Rv = chol(I + T T^T) for the k x nr matrix T (ld k)
+template <typename T>
+bool chol_v(lra_ctx* ctx, int64_t k, int64_t nr, const T* Tm, T* Rv);
+// SVD of the k x k matrix Mm (ld k): U diag(S) V^T, S descending (returned)
+template <typename T>
+std::vector<T> small_svd(lra_ctx* ctx, int64_t k, const T* Mm, T* U, T* V, T* S);
+template <typename T>
+std::vector<T> sort_desc(lra_ctx* ctx, int64_t k, T* S, T* U, T* V);
+
 // exact symmetry test of a square device matrix
 template <typename T>
 bool is_symmetric(lra_ctx* ctx, int64_t n, const T* A, int64_t lda);

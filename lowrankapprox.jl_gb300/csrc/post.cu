@@ -1,0 +1,122 @@
+// Post-processing of the ID into PSVD / PHEIG / PQR factors (src/psvd.jl:238-272,
+// src/pheig.jl:276-296, src/pqr.jl:297-307) as GEMM-shaped work.
+//
+// The reference takes Householder QRs of the tall skeleton matrix A[:, sk]
+// (m x k) and of (R V)^T (n x k).  Here both become Cholesky QRs that are
+// stable because their inputs are well conditioned:
+//   * A[:, sk] R11^{-1}, with R11 the triangular factor of the sketch's own
+//     pivoted QR on the skeleton columns (S A[:, sk] = Q_B R11), is the
+//     preimage of the orthonormal Q_B under the subspace embedding S, so its
+//     condition number is that of S on range(A[:, sk]) -- O(10) for a
+//     Gaussian sketch -- and its Gram matrix factors stably;
+//   * V V^T = I + T T^T, so V^T = P [I; T^T] factors as Q_v R_v with
+//     R_v = chol(I + T T^T) without forming Q_v.
+// The factorizations of the reference are then recovered exactly:
+//   A[:, sk] = Q R_A,  R_A = R_c R11,
+//   R V = R_A R_v^T Q_v^T,  SVD(R_A R_v^T) = U_M S V_M^T,
+//   U = Q U_M,  Vt = (R_v^{-1} V_M)^T V.
+// Every large operation is a GEMM or a blocked triangular solve; only the
+// k x k SVD / eigenproblem is iterative.
+
+#include <algorithm>
+#include <cmath>
+#include <numeric>
+#include <vector>
+
+#include "common.cuh"
+#include "internal.hpp"
+
+namespace lra {
+
+template <typename T>
+bool cholqr_pre(lra_ctx* ctx, int64_t m, int64_t k, T* X, int64_t ldx, const T* Rpre, int64_t ldr, int passes,
+                T* Rc) {
+  const int64_t kk = std::max<int64_t>(k, 1);
+  set_identity(ctx, k, k, Rc, kk);
+  if (k == 0) return true;
+  if (Rpre) trsm_right_upper(ctx, m, k, Rpre, ldr, X, ldx);
+  const ArenaMark mk = ctx->arena.mark();
+  T* G = ctx->arena.alloc_n<T>((size_t)kk * kk);
+  T* tmp = ctx->arena.alloc_n<T>((size_t)kk * kk);
+  bool ok = true;
+  for (int p = 0; p < passes && ok; ++p) {
+    gemm<T>(ctx, 't', 'n', k, k, m, T(1), X, ldx, X, ldx, T(0), G, kk);
+    ok = potrf_upper(ctx, k, G, kk);
+    if (!ok) break;
+    trsm_right_upper(ctx, m, k, G, kk, X, ldx);
+    // Rc <- G Rc (both upper triangular)
+    gemm<T>(ctx, 'n', 'n', k, k, k, T(1), G, kk, Rc, kk, T(0), tmp, kk);
+    copy_matrix(ctx, k, k, tmp, kk, Rc, kk);
+  }
+  LRA_CUDA(cudaStreamSynchronize(ctx->stream));
+  ctx->arena.release(mk);
+  return ok;
+}
+
+// R_v = chol(I + T T^T), T k x nr (ld k); false on breakdown
+template <typename T>
+bool chol_v(lra_ctx* ctx, int64_t k, int64_t nr, const T* Tm, T* Rv) {
+  const int64_t kk = std::max<int64_t>(k, 1);
+  set_identity(ctx, k, k, Rv, kk);
+  if (k == 0) return true;
+  if (nr > 0) gemm<T>(ctx, 'n', 't', k, k, nr, T(1), Tm, kk, Tm, kk, T(1), Rv, kk);
+  return potrf_upper(ctx, k, Rv, kk);
+}
+
+// descending sort of S with the matching columns of U and V (k x k, ld k)
+template <typename T>
+std::vector<T> sort_desc(lra_ctx* ctx, int64_t k, T* S, T* U, T* V) {
+  std::vector<T> hS(k);
+  if (k == 0) return hS;
+  LRA_CUDA(cudaMemcpyAsync(hS.data(), S, k * sizeof(T), cudaMemcpyDeviceToHost, ctx->stream));
+  LRA_CUDA(cudaStreamSynchronize(ctx->stream));
+  std::vector<int64_t> ord(k);
+  std::iota(ord.begin(), ord.end(), 0);
+  std::stable_sort(ord.begin(), ord.end(), [&](int64_t a, int64_t b) { return hS[a] > hS[b]; });
+  bool sorted = true;
+  for (int64_t i = 0; i < k; ++i) sorted &= ord[i] == i;
+  if (sorted) return hS;
+  std::vector<int64_t> o1(k);
+  std::vector<T> s2(k);
+  for (int64_t i = 0; i < k; ++i) {
+    o1[i] = ord[i] + 1;
+    s2[i] = hS[ord[i]];
+  }
+  const ArenaMark mk = ctx->arena.mark();
+  int64_t* d = ctx->arena.alloc_n<int64_t>(k);
+  T* tmp = ctx->arena.alloc_n<T>((size_t)k * k);
+  LRA_CUDA(cudaMemcpyAsync(d, o1.data(), k * sizeof(int64_t), cudaMemcpyHostToDevice, ctx->stream));
+  for (T* X : {U, V}) {
+    gather_cols(ctx, k, k, X, k, d, tmp, k);
+    copy_matrix(ctx, k, k, tmp, k, X, k);
+  }
+  LRA_CUDA(cudaMemcpyAsync(S, s2.data(), k * sizeof(T), cudaMemcpyHostToDevice, ctx->stream));
+  LRA_CUDA(cudaStreamSynchronize(ctx->stream));
+  ctx->arena.release(mk);
+  return s2;
+}
+
+// SVD of a k x k matrix Mm = U_M diag(S) V_M^T (S descending) by one-sided
+// Jacobi on Mm^T, whose columns (the rows of Mm) carry the grading of the
+// pivoted factors.  U, V, S are k x k / k device buffers.
+template <typename T>
+std::vector<T> small_svd(lra_ctx* ctx, int64_t k, const T* Mm, T* U, T* V, T* S) {
+  if (k == 0) return {};
+  // X = Mm^T; Jacobi: X W = Y diag(S) -> Mm = W diag(S) Y^T: U_M = W, V_M = Y
+  transpose(ctx, k, k, Mm, k, V, k);
+  jacobi_svd<T>(ctx, k, V, k, U, k, S);
+  div_cols(ctx, k, k, V, k, S);
+  return sort_desc(ctx, k, S, U, V);
+}
+
+template bool cholqr_pre<float>(lra_ctx*, int64_t, int64_t, float*, int64_t, const float*, int64_t, int, float*);
+template bool cholqr_pre<double>(lra_ctx*, int64_t, int64_t, double*, int64_t, const double*, int64_t, int,
+                                 double*);
+template bool chol_v<float>(lra_ctx*, int64_t, int64_t, const float*, float*);
+template bool chol_v<double>(lra_ctx*, int64_t, int64_t, const double*, double*);
+template std::vector<float> small_svd<float>(lra_ctx*, int64_t, const float*, float*, float*, float*);
+template std::vector<double> small_svd<double>(lra_ctx*, int64_t, const double*, double*, double*, double*);
+template std::vector<float> sort_desc<float>(lra_ctx*, int64_t, float*, float*, float*);
+template std::vector<double> sort_desc<double>(lra_ctx*, int64_t, double*, double*, double*);
+
+}  // namespace lra

@@ -46,7 +46,10 @@ struct QrParams {
   double atol, rtol;
   int pivot;
   int64_t* k_out;
+  int64_t vcap;  // reflector rows that fit the dynamic shared memory
 };
+
+constexpr int CH = 16;  // rows per lane held in registers per column chunk
 
 // exact power-of-two scale for a norm computation
 __device__ __forceinline__ double pow2_scale_inv(double mx) {
@@ -140,6 +143,8 @@ __global__ void __launch_bounds__(NT) geqp3_kernel(QrParams<T> P) {
   __shared__ int64_t si[32];
   __shared__ double red[32];
   __shared__ T s_tau;
+  extern __shared__ unsigned char qr_dyn[];
+  T* vs = reinterpret_cast<T*>(qr_dyn);
   constexpr int NW = NT / 32;
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
   const int64_t gw = (int64_t)blockIdx.x * NW + wid;
@@ -247,23 +252,76 @@ __global__ void __launch_bounds__(NT) geqp3_kernel(QrParams<T> P) {
       if (!grid_sync(P.bar)) return;
 
       // ---- all warps: apply H(c) to the trailing columns, downdate norms ------
+      // The reflector (rows c+1..m-1) is staged once per CTA in shared memory
+      // and each column is pulled into registers with independent loads, so
+      // a column costs one L2 round trip instead of one per row.
       if (threadIdx.x == 0) s_tau = __ldcg(P.tau + c);
+      const int64_t len = m - c - 1;
+      const T* vsrc = A + c * lda + c + 1;
+      const bool vsm = len <= P.vcap;
+      if (vsm)
+        for (int64_t i = threadIdx.x; i < len; i += NT) vs[i] = __ldcg(vsrc + i);
       __syncthreads();
       const T tauc = s_tau;
-      const T* v = A + c * lda;
       bv = T(-1);
       bi = INT64_MAX;
       int myflag = 0;
       int64_t jj = c + 1 + ((gw - (c + 1)) % W + W) % W;
       for (; jj < n; jj += W) {
         T* colj = A + jj * lda;
+        T* cj = colj + c + 1;
         T s = 0;
-        for (int64_t i = c + 1 + lane; i < m; i += 32) s += __ldcg(v + i) * __ldcg(colj + i);
+        T x[CH];
+        if (len <= 32 * CH) {
+#pragma unroll
+          for (int t = 0; t < CH; ++t) {
+            const int64_t i = lane + 32 * t;
+            x[t] = i < len ? __ldcg(cj + i) : T(0);
+          }
+#pragma unroll
+          for (int t = 0; t < CH; ++t) {
+            const int64_t i = lane + 32 * t;
+            if (i < len) s += (vsm ? vs[i] : __ldcg(vsrc + i)) * x[t];
+          }
+        } else {
+          for (int64_t b0 = 0; b0 < len; b0 += 32 * CH) {
+#pragma unroll
+            for (int t = 0; t < CH; ++t) {
+              const int64_t i = b0 + lane + 32 * t;
+              x[t] = i < len ? __ldcg(cj + i) : T(0);
+            }
+#pragma unroll
+            for (int t = 0; t < CH; ++t) {
+              const int64_t i = b0 + lane + 32 * t;
+              if (i < len) s += (vsm ? vs[i] : __ldcg(vsrc + i)) * x[t];
+            }
+          }
+        }
         s = warp_sum(s);
         const T arc0 = __ldcg(colj + c);
         const T f = tauc * (arc0 + s);
-        if (f != 0)
-          for (int64_t i = c + 1 + lane; i < m; i += 32) colj[i] = __ldcg(colj + i) - f * __ldcg(v + i);
+        if (f != 0) {
+          if (len <= 32 * CH) {
+#pragma unroll
+            for (int t = 0; t < CH; ++t) {
+              const int64_t i = lane + 32 * t;
+              if (i < len) cj[i] = x[t] - f * (vsm ? vs[i] : __ldcg(vsrc + i));
+            }
+          } else {
+            for (int64_t b0 = 0; b0 < len; b0 += 32 * CH) {
+#pragma unroll
+              for (int t = 0; t < CH; ++t) {
+                const int64_t i = b0 + lane + 32 * t;
+                x[t] = i < len ? __ldcg(cj + i) : T(0);
+              }
+#pragma unroll
+              for (int t = 0; t < CH; ++t) {
+                const int64_t i = b0 + lane + 32 * t;
+                if (i < len) cj[i] = x[t] - f * (vsm ? vs[i] : __ldcg(vsrc + i));
+              }
+            }
+          }
+        }
         const T arc = arc0 - f;
         if (lane == 0) colj[c] = arc;
         if (P.pivot) {
@@ -411,8 +469,13 @@ int64_t geqp3_adap(lra_ctx* ctx, int64_t m, int64_t n, T* A, int64_t lda, int64_
   constexpr int NT = 512;
   if (n <= 0) return 0;
   const ArenaMark mark = ctx->arena.mark();
+  // the reflector of each pivot is staged in shared memory when it fits
+  const int64_t vcap = std::min<int64_t>(m, (int64_t)(160 * 1024 / sizeof(T)));
+  const size_t dyn_smem = (size_t)vcap * sizeof(T);
+  LRA_CUDA(cudaFuncSetAttribute(geqp3_kernel<T, NT>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                (int)std::max<size_t>(dyn_smem, 1)));
   int per_sm = 0;
-  LRA_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, geqp3_kernel<T, NT>, NT, 0));
+  LRA_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, geqp3_kernel<T, NT>, NT, dyn_smem));
   if (per_sm < 1) fail(LRA_ECUDA, "geqp3 kernel cannot be resident");
   const int64_t want = (n + (NT / 32) - 1) / (NT / 32);
   int grid = (int)std::min<int64_t>((int64_t)ctx->num_sms * std::min(per_sm, 1), want);
@@ -440,6 +503,7 @@ int64_t geqp3_adap(lra_ctx* ctx, int64_t m, int64_t n, T* A, int64_t lda, int64_
   P.rtol = rtol;
   P.pivot = pivot ? 1 : 0;
   P.k_out = ctx->arena.alloc_n<int64_t>(1);
+  P.vcap = vcap;
   LRA_CUDA(cudaMemsetAsync(small, 0, 8 * sizeof(int), ctx->stream));
   LRA_CUDA(cudaMemsetAsync(P.bar, 0, sizeof(GridBar), ctx->stream));
   if (P.kmax <= 0) {
@@ -454,7 +518,7 @@ int64_t geqp3_adap(lra_ctx* ctx, int64_t m, int64_t n, T* A, int64_t lda, int64_
   }
   void* args[] = {&P};
   LRA_CUDA(cudaLaunchCooperativeKernel((const void*)geqp3_kernel<T, NT>, dim3(grid), dim3(NT), args,
-                                       0, ctx->stream));
+                                       dyn_smem, ctx->stream));
   post_launch(ctx, "geqp3_kernel");
   int64_t k = 0;
   GridBar hb;
