@@ -225,6 +225,22 @@ int lra_geqp3_adap(lra_ctx* ctx, int dtype, int64_t m, int64_t n, void* B,
                    int64_t ldb, int64_t* jpvt, void* tau, const lra_opts* opts,
                    int64_t* k);
 
+/* The same pivoted QR as lra_geqp3_adap, for callers that cannot allocate
+   device memory while they factor: code inside a CUDA stream capture, a
+   serving loop that reserved all of its memory up front, or a host whose
+   device allocator is owned by another framework.  It has no counterpart in
+   the reference.  Its scratch (partial norms, pivot candidates, counters,
+   grid barrier) is one fixed 1 MiB device array inside liblra, so the matrix
+   may have at most 32768 columns (larger n returns LRA_EINVAL); B, jpvt and
+   tau are caller-owned device buffers as above.  The first call on a device
+   resolves the array's device address (cudaGetSymbolAddress) and should
+   come before any stream capture.  All calls on a device share the array:
+   calls that overlap on the GPU race and must be serialized by the caller.
+   No cudaMalloc / cudaFree or allocating library routine is called.        */
+int lra_geqp3_adap_noalloc(lra_ctx* ctx, int dtype, int64_t m, int64_t n, void* B,
+                           int64_t ldb, int64_t* jpvt, void* tau,
+                           const lra_opts* opts, int64_t* k);
+
 /* ---- factorizations --------------------------------------------------------- */
 
 /* idfact(trans, A) (src/id.jl:434-450) */

@@ -733,6 +733,38 @@ int lra_geqp3_adap(lra_ctx* ctx, int dtype, int64_t m, int64_t n, void* B, int64
   });
 }
 
+int lra_geqp3_adap_noalloc(lra_ctx* ctx, int dtype, int64_t m, int64_t n, void* B, int64_t ldb, int64_t* jpvt,
+                           void* tau, const lra_opts* opts, int64_t* k) {
+  // No arena reset and no workspace: this entry point allocates nothing.
+  if (!ctx) return LRA_EINVAL;
+  try {
+    chkopts(opts);
+    check_dims(m, n);
+    if (!k) fail(LRA_EINVAL, "k is NULL");
+    if (n > noalloc_max_cols())
+      fail(LRA_EINVAL, "lra_geqp3_adap_noalloc: n = %lld exceeds its limit of %lld columns", (long long)n,
+           (long long)noalloc_max_cols());
+    if (m <= 0 || n <= 0) fail(LRA_EINVAL, "lra_geqp3_adap_noalloc: empty matrix");
+    if (!is_dev(B) || !is_dev(jpvt) || !is_dev(tau)) fail(LRA_EINVAL, "lra_geqp3_adap_noalloc works on device buffers");
+    if (ldb < m) fail(LRA_EDIM, "ldb");
+    LRA_CUDA(cudaSetDevice(ctx->device));
+    dispatch(dtype, [&](auto z) {
+      using T = decltype(z);
+      const int64_t l = std::min(m, n);
+      const int64_t kmax = (opts->rank < 0 || opts->rank > l) ? l : opts->rank;
+      *k = geqp3_adap_noalloc<T>(ctx, m, n, static_cast<T*>(B), ldb, jpvt, static_cast<T*>(tau), kmax, opts->nb,
+                                 opts->atol, opts->rtol);
+    });
+    ctx->last_error.clear();
+    return LRA_OK;
+  } catch (const lra::Error& e) {
+    ctx->last_error = e.msg;
+    cudaStreamSynchronize(ctx->stream);
+    cudaGetLastError();
+    return e.status;
+  }
+}
+
 int lra_idfact(lra_ctx* ctx, int dtype, char trans, int64_t m, int64_t n, const void* A, int64_t lda,
                const lra_opts* opts, const lra_rand* rand, lra_id** out) {
   if (out) *out = nullptr;

@@ -107,6 +107,13 @@ template <typename T>
 int64_t geqp3_adap(lra_ctx* ctx, int64_t m, int64_t n, T* A, int64_t lda, int64_t* jpvt,
                    T* tau, int64_t kmax, int64_t nb, double atol, double rtol, bool pivot);
 
+// The same pivoted QR with its scratch in a fixed device array instead of
+// the context arena (no device allocation); n <= noalloc_max_cols().
+template <typename T>
+int64_t geqp3_adap_noalloc(lra_ctx* ctx, int64_t m, int64_t n, T* A, int64_t lda, int64_t* jpvt, T* tau,
+                           int64_t kmax, int64_t nb, double atol, double rtol);
+int64_t noalloc_max_cols();
+
 // X (k x nrhs) <- triu(R)^{-1} X, R k x k (ldr).
 template <typename T>
 void trsm_upper(lra_ctx* ctx, int64_t k, int64_t nrhs, const T* R, int64_t ldr, T* X,

@@ -20,6 +20,7 @@
 
 #include <algorithm>
 #include <cmath>
+#include <mutex>
 
 #include "common.cuh"
 #include "internal.hpp"
@@ -577,6 +578,126 @@ void col_norms(lra_ctx* ctx, int64_t m, int64_t n, const T* A, int64_t lda, T* o
   col_norms_kernel<T><<<(unsigned)blocks, warps * 32, 0, ctx->stream>>>(m, n, A, lda, out);
   post_launch(ctx, "col_norms_kernel");
 }
+
+// ---- pivoted QR without any device allocation --------------------------------------
+//
+// Some callers cannot allocate device memory while they factor: code that
+// runs between the begin and end of a CUDA stream capture, a serving loop
+// that has reserved all of its device memory up front, or a host framework
+// that owns the device allocator (a Julia or Python memory pool) and does
+// not let a library call cudaMalloc behind its back.  For them the pivoted
+// QR's scratch -- the partial column norms, the per-CTA pivot candidates,
+// the block-stop counters and the grid barrier -- lives in one fixed device
+// array of this file, sized for at most kNoAllocMaxCols columns.  Every GPU
+// that loads the library keeps the array until the process exits.
+//
+// The array's host-side name is not a device address; its address is taken
+// once per device with cudaGetSymbolAddress, with that device current, on
+// the first call that runs on the device.  That first call should therefore
+// happen before any stream capture begins.  All calls on a device share the
+// array: calls that overlap on the GPU (different streams, threads or
+// contexts) race on it and must be serialized by the caller.
+
+constexpr int64_t kNoAllocMaxCols = 32768;
+constexpr int kNoAllocMaxGrid = 1024;
+constexpr size_t kNoAllocBytes = 1u << 20;  // 1 MiB
+static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocBytes];
+
+namespace {
+
+std::mutex g_noalloc_mu;
+void* g_noalloc_ptr[128] = {};
+
+// device address of the scratch array on the current device (set up once)
+void* noalloc_scratch(int device) {
+  if (device < 0 || device >= 128) fail(LRA_EINVAL, "device index %d out of range", device);
+  std::lock_guard<std::mutex> lk(g_noalloc_mu);
+  if (!g_noalloc_ptr[device]) {
+    void* p = nullptr;
+    check_cuda(cudaGetSymbolAddress(&p, g_noalloc_scratch), "cudaGetSymbolAddress(no-alloc scratch)");
+    if (!p) fail(LRA_ECUDA, "no-alloc scratch has no device address");
+    g_noalloc_ptr[device] = p;
+  }
+  return g_noalloc_ptr[device];
+}
+
+inline unsigned char* carve(unsigned char*& cur, size_t bytes) {
+  unsigned char* p = cur;
+  cur += (bytes + 255) / 256 * 256;
+  return p;
+}
+
+}  // namespace
+
+int64_t noalloc_max_cols() { return kNoAllocMaxCols; }
+
+template <typename T>
+int64_t geqp3_adap_noalloc(lra_ctx* ctx, int64_t m, int64_t n, T* A, int64_t lda, int64_t* jpvt, T* tau,
+                           int64_t kmax, int64_t nb, double atol, double rtol) {
+  constexpr int NT = 512;
+  if (n <= 0) return 0;
+  if (n > kNoAllocMaxCols)
+    fail(LRA_EINVAL, "lra_geqp3_adap_noalloc: n = %lld exceeds its limit of %lld columns", (long long)n,
+         (long long)kNoAllocMaxCols);
+  unsigned char* base = static_cast<unsigned char*>(noalloc_scratch(ctx->device));
+  const int64_t vcap = std::min<int64_t>(m, (int64_t)(160 * 1024 / sizeof(T)));
+  const size_t dyn_smem = (size_t)vcap * sizeof(T);
+  LRA_CUDA(cudaFuncSetAttribute(geqp3_kernel<T, NT>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                (int)std::max<size_t>(dyn_smem, 1)));
+  int per_sm = 0;
+  LRA_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, geqp3_kernel<T, NT>, NT, dyn_smem));
+  if (per_sm < 1) fail(LRA_ECUDA, "geqp3 kernel cannot be resident");
+  const int64_t want = (n + (NT / 32) - 1) / (NT / 32);
+  int grid = (int)std::min<int64_t>(std::min<int64_t>((int64_t)ctx->num_sms, want), kNoAllocMaxGrid);
+  grid = std::max(grid, 1);
+
+  unsigned char* cur = base;
+  QrParams<T> P;
+  P.m = m;
+  P.n = n;
+  P.lda = lda;
+  P.A = A;
+  P.jpvt = jpvt;
+  P.tau = tau;
+  P.vn1 = reinterpret_cast<T*>(carve(cur, n * sizeof(T)));
+  P.vn2 = reinterpret_cast<T*>(carve(cur, n * sizeof(T)));
+  P.flag = reinterpret_cast<int*>(carve(cur, n * sizeof(int)));
+  P.part_v = reinterpret_cast<T*>(carve(cur, grid * sizeof(T)));
+  P.part_i = reinterpret_cast<int64_t*>(carve(cur, grid * sizeof(int64_t)));
+  P.part_d = reinterpret_cast<double*>(carve(cur, grid * sizeof(double)));
+  int* small = reinterpret_cast<int*>(carve(cur, 8 * sizeof(int)));
+  P.lsticc = small;
+  P.bar = reinterpret_cast<GridBar*>(carve(cur, sizeof(GridBar)));
+  P.k_out = reinterpret_cast<int64_t*>(carve(cur, sizeof(int64_t)));
+  if ((size_t)(cur - base) > kNoAllocBytes) fail(LRA_EINVAL, "no-alloc scratch overflow");
+  P.kmax = std::min<int64_t>(kmax, std::min(m, n));
+  P.nb = std::max<int64_t>(1, std::min<int64_t>(nb, std::max<int64_t>(P.kmax, 1)));
+  P.atol = atol;
+  P.rtol = rtol;
+  P.pivot = 1;
+  P.vcap = vcap;
+  // the array keeps the previous call's contents: clear the counters and
+  // the barrier, which must start at zero (the kernel initializes the rest)
+  LRA_CUDA(cudaMemsetAsync(small, 0, 8 * sizeof(int), ctx->stream));
+  LRA_CUDA(cudaMemsetAsync(P.bar, 0, sizeof(GridBar), ctx->stream));
+  if (P.kmax <= 0) fail(LRA_EINVAL, "lra_geqp3_adap_noalloc: nothing to factor (rank 0 or empty)");
+  void* args[] = {&P};
+  LRA_CUDA(cudaLaunchCooperativeKernel((const void*)geqp3_kernel<T, NT>, dim3(grid), dim3(NT), args,
+                                       dyn_smem, ctx->stream));
+  post_launch(ctx, "geqp3_kernel");
+  int64_t k = 0;
+  GridBar hb;
+  LRA_CUDA(cudaMemcpyAsync(&k, P.k_out, sizeof(int64_t), cudaMemcpyDeviceToHost, ctx->stream));
+  LRA_CUDA(cudaMemcpyAsync(&hb, P.bar, sizeof(GridBar), cudaMemcpyDeviceToHost, ctx->stream));
+  LRA_CUDA(cudaStreamSynchronize(ctx->stream));
+  if (hb.err != 0) fail(LRA_ETIMEDOUT, "geqp3: a grid barrier timed out");
+  return k;
+}
+
+template int64_t geqp3_adap_noalloc<float>(lra_ctx*, int64_t, int64_t, float*, int64_t, int64_t*, float*, int64_t,
+                                           int64_t, double, double);
+template int64_t geqp3_adap_noalloc<double>(lra_ctx*, int64_t, int64_t, double*, int64_t, int64_t*, double*,
+                                            int64_t, int64_t, double, double);
 
 #define INST(T)                                                                                   \
   template int64_t geqp3_adap<T>(lra_ctx*, int64_t, int64_t, T*, int64_t, int64_t*, T*, int64_t,  \
