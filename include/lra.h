@@ -241,6 +241,17 @@ int lra_geqp3_adap_noalloc(lra_ctx* ctx, int dtype, int64_t m, int64_t n, void* 
                            int64_t ldb, int64_t* jpvt, void* tau,
                            const lra_opts* opts, int64_t* k);
 
+/* C = alpha op(A) op(B) + beta C in Float64 (column-major device arrays;
+   trans 'n' or 't'), computed the way the factorizations compute their
+   GEMMs: precision LRA_PREC_MIXED runs the tensor-core product of six
+   exact BF16 byte slices per operand (error near 2^-45 of the rows' and
+   columns' largest magnitudes), LRA_PREC_NATIVE the FP64 CUDA-core kernel.
+   No counterpart in the reference, whose GEMMs are BLAS calls; exported so
+   that the product the mixed path relies on can be checked directly.      */
+int lra_dgemm(lra_ctx* ctx, int precision, char transa, char transb, int64_t m,
+              int64_t n, int64_t k, double alpha, const double* A, int64_t lda,
+              const double* B, int64_t ldb, double beta, double* C, int64_t ldc);
+
 /* ---- factorizations --------------------------------------------------------- */
 
 /* idfact(trans, A) (src/id.jl:434-450) */

@@ -240,6 +240,12 @@ bool use_tc(const lra_opts& o, int dtype) {
   return dtype == LRA_F32 || o.rtol >= 1e-13;
 }
 
+// whether the large Float64 GEMMs of a factorization run on the tensor
+// cores (tc_gemm: 2^-45 of the operands' row / column scales)
+bool use_tc_gemm(const lra_opts& o, int dtype) {
+  return o.precision == LRA_PREC_MIXED && dtype == LRA_F64 && o.rtol >= 1e-13;
+}
+
 // right_layout: the Gaussian matrix is drawn as M x order (column-major), the
 // layout of a right sketch A S (src/sketch.jl:95-98), and used transposed
 template <typename T>
@@ -288,7 +294,8 @@ void make_sketch(lra_ctx* ctx, const lra_opts& o, char trans, int64_t M, int64_t
       rs.signs(M, d);
       int64_t* idx = ctx->arena.alloc_n<int64_t>(order);
       rs.ints(order, M, idx, false);
-      srft_sketch<T>(ctx, trans, M, N, A, lda, d, idx, order, B, order);
+      if (!srft_sketch_fft<T>(ctx, trans, M, N, A, lda, d, idx, order, B, order))
+        srft_sketch<T>(ctx, trans, M, N, A, lda, d, idx, order, B, order);
       break;
     }
     case LRA_SKETCH_SUB: {
@@ -512,11 +519,14 @@ int guarded(lra_ctx* ctx, Fn&& fn) {
     LRA_CUDA(cudaSetDevice(ctx->device));
     ctx->arena.reset(ctx->stream);
     for (double& s : ctx->stage_ms) s = 0;
+    ctx->gemm_tc = false;
     fn();
+    ctx->gemm_tc = false;
     LRA_CUDA(cudaStreamSynchronize(ctx->stream));
     ctx->last_error.clear();
     return LRA_OK;
   } catch (const lra::Error& e) {
+    ctx->gemm_tc = false;
     ctx->last_error = e.msg;
     cudaStreamSynchronize(ctx->stream);
     cudaGetLastError();
@@ -758,6 +768,7 @@ int lra_geqp3_adap_noalloc(lra_ctx* ctx, int dtype, int64_t m, int64_t n, void* 
     ctx->last_error.clear();
     return LRA_OK;
   } catch (const lra::Error& e) {
+    ctx->gemm_tc = false;
     ctx->last_error = e.msg;
     cudaStreamSynchronize(ctx->stream);
     cudaGetLastError();
@@ -765,11 +776,33 @@ int lra_geqp3_adap_noalloc(lra_ctx* ctx, int dtype, int64_t m, int64_t n, void* 
   }
 }
 
+int lra_dgemm(lra_ctx* ctx, int precision, char transa, char transb, int64_t m, int64_t n, int64_t k,
+              double alpha, const double* A, int64_t lda, const double* B, int64_t ldb, double beta, double* C,
+              int64_t ldc) {
+  return guarded(ctx, [&] {
+    auto tr = [](char t) { return t == 'n' || t == 'N' || t == 't' || t == 'T' || t == 'c' || t == 'C'; };
+    if (!tr(transa) || !tr(transb)) fail(LRA_EINVAL, "trans must be 'n' or 't'");
+    if (m < 0 || n < 0 || k < 0) fail(LRA_EDIM, "negative dimension");
+    if (precision != LRA_PREC_NATIVE && precision != LRA_PREC_MIXED) fail(LRA_EINVAL, "precision");
+    if (m == 0 || n == 0) return;
+    const bool ta = transa != 'n' && transa != 'N', tb = transb != 'n' && transb != 'N';
+    if (lda < std::max<int64_t>(1, ta ? k : m) || ldb < std::max<int64_t>(1, tb ? n : k) ||
+        ldc < std::max<int64_t>(1, m))
+      fail(LRA_EDIM, "leading dimension too small");
+    if ((k > 0 && (!is_dev(A) || !is_dev(B))) || !is_dev(C)) fail(LRA_EINVAL, "lra_dgemm takes device arrays");
+    if (precision == LRA_PREC_MIXED && k > 0)
+      tc_gemm(ctx, transa, transb, m, n, k, alpha, A, lda, B, ldb, beta, C, ldc);
+    else
+      gemm<double>(ctx, transa, transb, m, n, k, alpha, A, lda, B, ldb, beta, C, ldc);
+  });
+}
+
 int lra_idfact(lra_ctx* ctx, int dtype, char trans, int64_t m, int64_t n, const void* A, int64_t lda,
                const lra_opts* opts, const lra_rand* rand, lra_id** out) {
   if (out) *out = nullptr;
   return guarded(ctx, [&] {
     chkopts(opts);
+    ctx->gemm_tc = use_tc_gemm(*opts, dtype);
     check_dims(m, n);
     if (!out) fail(LRA_EINVAL, "out is NULL");
     const char t = chktrans(trans);
@@ -791,6 +824,7 @@ int lra_sketchfact(lra_ctx* ctx, int dtype, char side, char trans, int64_t m, in
   if (out) *out = nullptr;
   return guarded(ctx, [&] {
     chkopts(opts);
+    ctx->gemm_tc = use_tc_gemm(*opts, dtype);
     check_dims(m, n);
     if (!out) fail(LRA_EINVAL, "out is NULL");
     const char t = chktrans(trans);
@@ -848,6 +882,7 @@ int lra_pqrfact(lra_ctx* ctx, int dtype, char trans, int64_t m, int64_t n, const
   if (out) *out = nullptr;
   return guarded(ctx, [&] {
     chkopts(opts);
+    ctx->gemm_tc = use_tc_gemm(*opts, dtype);
     check_dims(m, n);
     if (!out) fail(LRA_EINVAL, "out is NULL");
     const char t = chktrans(trans);
@@ -1160,6 +1195,7 @@ int lra_psvdfact(lra_ctx* ctx, int dtype, int64_t m, int64_t n, const void* A, i
   if (out) *out = nullptr;
   return guarded(ctx, [&] {
     chkopts(opts);
+    ctx->gemm_tc = use_tc_gemm(*opts, dtype);
     check_dims(m, n);
     if (!out) fail(LRA_EINVAL, "out is NULL");
     dispatch(dtype, [&](auto z) {
@@ -1197,6 +1233,7 @@ int lra_pheigfact(lra_ctx* ctx, int dtype, int64_t n, const void* A, int64_t lda
   if (out) *out = nullptr;
   return guarded(ctx, [&] {
     chkopts(opts);
+    ctx->gemm_tc = use_tc_gemm(*opts, dtype);
     check_dims(n, n);
     if (!out) fail(LRA_EINVAL, "out is NULL");
     const lra_opts& o = *opts;
@@ -1256,7 +1293,7 @@ int lra_pheigfact(lra_ctx* ctx, int dtype, int64_t n, const void* A, int64_t lda
       add_diag(ctx, k, B, ldk, shift);
       T* Z = ctx->arena.alloc_n<T>((size_t)ldk * ldk);
       T* S = ctx->arena.alloc_n<T>(ldk);
-      jacobi_svd<T>(ctx, k, B, ldk, Z, ldk, S);
+      jacobi_svd_fast<T>(ctx, k, B, ldk, Z, ldk, S);
       std::vector<T> hS(k);
       to_host(ctx, hS.data(), S, k);
       LRA_CUDA(cudaStreamSynchronize(ctx->stream));
@@ -1347,6 +1384,7 @@ int lra_curfact(lra_ctx* ctx, int dtype, int64_t m, int64_t n, const void* A, in
   if (out) *out = nullptr;
   return guarded(ctx, [&] {
     chkopts(opts);
+    ctx->gemm_tc = use_tc_gemm(*opts, dtype);
     check_dims(m, n);
     if (!out) fail(LRA_EINVAL, "out is NULL");
     lra_opts o = *opts;

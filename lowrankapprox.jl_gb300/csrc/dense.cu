@@ -28,6 +28,7 @@ struct JacParams {
   int64_t ldv;
   T* S;
   double tol;
+  double stop;  // a sweep whose largest rotated cosine is below this is the last
   int max_sweeps;
   double* part;
   GridBar* bar;
@@ -68,15 +69,15 @@ __global__ void __launch_bounds__(NT) jacobi_kernel(JacParams<T> P) {
         T* xq = P.X + q * P.ldx;
         // both columns are pulled into registers with independent loads
         // (one L2 round trip per chunk), reduced, rotated and stored
-        double a = 0, b = 0, g = 0;
-        double u[JCH], w[JCH];
+        T a = 0, b = 0, g = 0;
+        T u[JCH], w[JCH];
         const bool one = n <= 32 * JCH;
         for (int64_t b0 = 0; b0 < n; b0 += 32 * JCH) {
 #pragma unroll
           for (int t = 0; t < JCH; ++t) {
             const int64_t i = b0 + lane + 32 * t;
-            u[t] = i < n ? (double)__ldcg(xp + i) : 0.0;
-            w[t] = i < n ? (double)__ldcg(xq + i) : 0.0;
+            u[t] = i < n ? __ldcg(xp + i) : T(0);
+            w[t] = i < n ? __ldcg(xq + i) : T(0);
           }
 #pragma unroll
           for (int t = 0; t < JCH; ++t) {
@@ -89,28 +90,28 @@ __global__ void __launch_bounds__(NT) jacobi_kernel(JacParams<T> P) {
         b = warp_sum(b);
         g = warp_sum(g);
         if (a == 0 || b == 0) continue;
-        const double rel = fabs(g) / sqrt(a * b);
-        if (!(rel > P.tol)) continue;
-        off = fmax(off, rel);
-        const double zeta = (b - a) / (2.0 * g);
-        const double t = copysign(1.0, zeta) / (fabs(zeta) + sqrt(1.0 + zeta * zeta));
-        const double c = 1.0 / sqrt(1.0 + t * t);
-        const double sn = c * t;
+        const T rel = fabs(g) / sqrt(a * b);
+        if (!(rel > (T)P.tol)) continue;
+        off = fmax(off, (double)rel);
+        const T zeta = (b - a) / (T(2) * g);
+        const T t = copysign(T(1), zeta) / (fabs(zeta) + sqrt(T(1) + zeta * zeta));
+        const T c = T(1) / sqrt(T(1) + t * t);
+        const T sn = c * t;
         for (int64_t b0 = 0; b0 < n; b0 += 32 * JCH) {
           if (!one) {
 #pragma unroll
             for (int tt = 0; tt < JCH; ++tt) {
               const int64_t i = b0 + lane + 32 * tt;
-              u[tt] = i < n ? (double)__ldcg(xp + i) : 0.0;
-              w[tt] = i < n ? (double)__ldcg(xq + i) : 0.0;
+              u[tt] = i < n ? __ldcg(xp + i) : T(0);
+              w[tt] = i < n ? __ldcg(xq + i) : T(0);
             }
           }
 #pragma unroll
           for (int tt = 0; tt < JCH; ++tt) {
             const int64_t i = b0 + lane + 32 * tt;
             if (i < n) {
-              xp[i] = (T)(c * u[tt] - sn * w[tt]);
-              xq[i] = (T)(sn * u[tt] + c * w[tt]);
+              xp[i] = c * u[tt] - sn * w[tt];
+              xq[i] = sn * u[tt] + c * w[tt];
             }
           }
         }
@@ -120,15 +121,15 @@ __global__ void __launch_bounds__(NT) jacobi_kernel(JacParams<T> P) {
 #pragma unroll
           for (int tt = 0; tt < JCH; ++tt) {
             const int64_t i = b0 + lane + 32 * tt;
-            u[tt] = i < n ? (double)__ldcg(vp + i) : 0.0;
-            w[tt] = i < n ? (double)__ldcg(vq + i) : 0.0;
+            u[tt] = i < n ? __ldcg(vp + i) : T(0);
+            w[tt] = i < n ? __ldcg(vq + i) : T(0);
           }
 #pragma unroll
           for (int tt = 0; tt < JCH; ++tt) {
             const int64_t i = b0 + lane + 32 * tt;
             if (i < n) {
-              vp[i] = (T)(c * u[tt] - sn * w[tt]);
-              vq[i] = (T)(sn * u[tt] + c * w[tt]);
+              vp[i] = c * u[tt] - sn * w[tt];
+              vq[i] = sn * u[tt] + c * w[tt];
             }
           }
         }
@@ -142,7 +143,7 @@ __global__ void __launch_bounds__(NT) jacobi_kernel(JacParams<T> P) {
     for (int b = threadIdx.x; b < gridDim.x; b += NT) mx = fmax(mx, __ldcg(P.part + b));
     mx = block_max(mx, red);
     if (!grid_sync(P.bar)) return;  // everyone read part before it is rewritten
-    if (mx <= P.tol) {
+    if (mx <= P.stop) {
       ++sweep;
       break;
     }
@@ -157,6 +158,163 @@ __global__ void __launch_bounds__(NT) jacobi_kernel(JacParams<T> P) {
     }
     a = warp_sum(a);
     if (lane == 0) P.S[j] = (T)sqrt(a);
+  }
+  if (blockIdx.x == 0 && threadIdx.x == 0) *P.sweeps_out = sweep;
+}
+
+// One CTA per column pair for Float64: the rows of the two columns are
+// spread over all threads of the CTA (a warp-wide FP64 instruction costs
+// tens of cycles on this part, so fewer rows per thread shorten every
+// dependent chain), the three dot products are reduced through shared
+// memory, and the rotation test g^2 > tol^2 a b needs no division or
+// square root.
+constexpr int JP_RCH = 8;  // rows per thread per register chunk
+
+template <typename T, int NT>
+__global__ void __launch_bounds__(NT) jacobi_pair_kernel(JacParams<T> P) {
+  constexpr int NW = NT / 32;
+  __shared__ T red[2][NW][3];
+  __shared__ int s_flag;
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  const int64_t n = P.n;
+  const int64_t nn = n + (n & 1);
+  const T tol2 = (T)(P.tol * P.tol), stop2 = (T)(P.stop * P.stop);
+  int sweep = 0;
+  int buf = 0;
+  for (; sweep < P.max_sweeps; ++sweep) {
+    int above = 0;  // a pair of this CTA had a cosine above the stopping level
+    for (int64_t r = 0; r < nn - 1; ++r) {
+      for (int64_t s = blockIdx.x; s < nn / 2; s += gridDim.x) {
+        int64_t p, q;
+        rr_pair(r, s, nn, p, q);
+        if (p >= n || q >= n) continue;
+        if (p > q) {
+          const int64_t t = p;
+          p = q;
+          q = t;
+        }
+        T* xp = P.X + p * P.ldx;
+        T* xq = P.X + q * P.ldx;
+        T a = 0, b = 0, g = 0;
+        T u[JP_RCH], w[JP_RCH];
+        const bool one = n <= (int64_t)NT * JP_RCH;
+        for (int64_t b0 = 0; b0 < n; b0 += (int64_t)NT * JP_RCH) {
+#pragma unroll
+          for (int c = 0; c < JP_RCH; ++c) {
+            if (b0 + (int64_t)NT * c >= n) break;
+            const int64_t i = b0 + threadIdx.x + (int64_t)NT * c;
+            u[c] = i < n ? __ldcg(xp + i) : T(0);
+            w[c] = i < n ? __ldcg(xq + i) : T(0);
+          }
+#pragma unroll
+          for (int c = 0; c < JP_RCH; ++c) {
+            if (b0 + (int64_t)NT * c >= n) break;
+            a = fma(u[c], u[c], a);
+            b = fma(w[c], w[c], b);
+            g = fma(u[c], w[c], g);
+          }
+        }
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+          a += __shfl_xor_sync(0xffffffffu, a, o);
+          b += __shfl_xor_sync(0xffffffffu, b, o);
+          g += __shfl_xor_sync(0xffffffffu, g, o);
+        }
+        if (lane == 0) {
+          red[buf][wid][0] = a;
+          red[buf][wid][1] = b;
+          red[buf][wid][2] = g;
+        }
+        __syncthreads();
+        a = red[buf][0][0];
+        b = red[buf][0][1];
+        g = red[buf][0][2];
+#pragma unroll
+        for (int k = 1; k < NW; ++k) {
+          a += red[buf][k][0];
+          b += red[buf][k][1];
+          g += red[buf][k][2];
+        }
+        buf ^= 1;  // the next pair reduces through the other buffer
+        if (a == 0 || b == 0) continue;
+        const T g2 = g * g, ab = a * b;
+        if (!(g2 > tol2 * ab)) continue;
+        if (g2 > stop2 * ab) above = 1;
+        // t = tan of the rotation angle, the smaller root of t^2 + 2 zeta t - 1
+        const T d = b - a;
+        const T t = (T(2) * g) / (d + copysign(sqrt(fma(d, d, T(4) * g2)), d));
+        const T c = T(1) / sqrt(fma(t, t, T(1)));
+        const T sn = c * t;
+        for (int64_t b0 = 0; b0 < n; b0 += (int64_t)NT * JP_RCH) {
+          if (!one) {
+#pragma unroll
+            for (int cc = 0; cc < JP_RCH; ++cc) {
+              if (b0 + (int64_t)NT * cc >= n) break;
+              const int64_t i = b0 + threadIdx.x + (int64_t)NT * cc;
+              u[cc] = i < n ? __ldcg(xp + i) : T(0);
+              w[cc] = i < n ? __ldcg(xq + i) : T(0);
+            }
+          }
+#pragma unroll
+          for (int cc = 0; cc < JP_RCH; ++cc) {
+            if (b0 + (int64_t)NT * cc >= n) break;
+            const int64_t i = b0 + threadIdx.x + (int64_t)NT * cc;
+            if (i < n) {
+              xp[i] = c * u[cc] - sn * w[cc];
+              xq[i] = sn * u[cc] + c * w[cc];
+            }
+          }
+        }
+        T* vp = P.V + p * P.ldv;
+        T* vq = P.V + q * P.ldv;
+        for (int64_t b0 = 0; b0 < n; b0 += (int64_t)NT * JP_RCH) {
+#pragma unroll
+          for (int cc = 0; cc < JP_RCH; ++cc) {
+            if (b0 + (int64_t)NT * cc >= n) break;
+            const int64_t i = b0 + threadIdx.x + (int64_t)NT * cc;
+            u[cc] = i < n ? __ldcg(vp + i) : T(0);
+            w[cc] = i < n ? __ldcg(vq + i) : T(0);
+          }
+#pragma unroll
+          for (int cc = 0; cc < JP_RCH; ++cc) {
+            if (b0 + (int64_t)NT * cc >= n) break;
+            const int64_t i = b0 + threadIdx.x + (int64_t)NT * cc;
+            if (i < n) {
+              vp[i] = c * u[cc] - sn * w[cc];
+              vq[i] = sn * u[cc] + c * w[cc];
+            }
+          }
+        }
+      }
+      if (!grid_sync(P.bar)) return;
+    }
+    // any CTA above the stopping level keeps the sweeps going
+    if (threadIdx.x == 0) P.part[blockIdx.x] = above ? 1.0 : 0.0;
+    if (!grid_sync(P.bar)) return;
+    if (threadIdx.x == 0) {
+      int any = 0;
+      for (int k = 0; k < (int)gridDim.x; ++k) any |= __ldcg(P.part + k) != 0.0;
+      s_flag = any;
+    }
+    __syncthreads();
+    const int any = s_flag;
+    if (!grid_sync(P.bar)) return;  // everyone read part before it is rewritten
+    if (!any) {
+      ++sweep;
+      break;
+    }
+  }
+  // singular values = column norms, a warp per column
+  const int64_t gw = (int64_t)blockIdx.x * NW + wid, W = (int64_t)gridDim.x * NW;
+  for (int64_t j = gw; j < n; j += W) {
+    const T* x = P.X + j * P.ldx;
+    double acc = 0;
+    for (int64_t i = lane; i < n; i += 32) {
+      const double v = __ldcg(x + i);
+      acc = fma(v, v, acc);
+    }
+    acc = warp_sum(acc);
+    if (lane == 0) P.S[j] = (T)sqrt(acc);
   }
   if (blockIdx.x == 0 && threadIdx.x == 0) *P.sweeps_out = sweep;
 }
@@ -176,15 +334,19 @@ __global__ void symcheck_kernel(int64_t n, const T* __restrict__ A, int64_t lda,
 }  // namespace
 
 template <typename T>
-void jacobi_svd(lra_ctx* ctx, int64_t n, T* X, int64_t ldx, T* V, int64_t ldv, T* S) {
+void jacobi_svd(lra_ctx* ctx, int64_t n, T* X, int64_t ldx, T* V, int64_t ldv, T* S, bool quadratic_stop) {
+  // Float64: a CTA of 128 threads per pair; Float32: a warp per pair
+  constexpr bool pair_cta = sizeof(T) == 8;
   constexpr int NT = 128;
   if (n <= 0) return;
   set_identity(ctx, n, n, V, ldv);
   const ArenaMark mk = ctx->arena.mark();
+  const void* kern = pair_cta ? (const void*)jacobi_pair_kernel<T, NT> : (const void*)jacobi_kernel<T, NT>;
   int per_sm = 0;
-  LRA_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, jacobi_kernel<T, NT>, NT, 0));
+  LRA_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, NT, 0));
   const int64_t pairs = (n + 1) / 2;
-  int grid = (int)std::min<int64_t>((pairs + (NT / 32) - 1) / (NT / 32), (int64_t)ctx->num_sms);
+  const int64_t per_cta = pair_cta ? 1 : NT / 32;
+  int grid = (int)std::min<int64_t>((pairs + per_cta - 1) / per_cta, (int64_t)ctx->num_sms);
   grid = std::max(1, std::min(grid, ctx->num_sms * std::max(per_sm, 1)));
   JacParams<T> P;
   P.n = n;
@@ -194,15 +356,19 @@ void jacobi_svd(lra_ctx* ctx, int64_t n, T* X, int64_t ldx, T* V, int64_t ldv, T
   P.ldv = ldv;
   P.S = S;
   P.tol = (double)Real<T>::eps * 2.0 * std::sqrt((double)n);
+  // Started from columns already orthogonal to about 1e-7 (the FP32 sweeps
+  // of jacobi_svd_fast), the FP64 sweeps converge quadratically: a sweep
+  // whose cosines were all below sqrt(tol)/10 leaves them near tol^2/100
+  // times a modest gap factor, so no further sweep is needed.
+  P.stop = quadratic_stop ? std::sqrt(P.tol) * 0.1 : P.tol;
   P.max_sweeps = 40;
   P.part = ctx->arena.alloc_n<double>(grid);
   P.bar = reinterpret_cast<GridBar*>(ctx->arena.alloc(sizeof(GridBar)));
   P.sweeps_out = ctx->arena.alloc_n<int>(1);
   LRA_CUDA(cudaMemsetAsync(P.bar, 0, sizeof(GridBar), ctx->stream));
   void* args[] = {&P};
-  LRA_CUDA(cudaLaunchCooperativeKernel((const void*)jacobi_kernel<T, NT>, dim3(grid), dim3(NT), args, 0,
-                                       ctx->stream));
-  post_launch(ctx, "jacobi_kernel");
+  LRA_CUDA(cudaLaunchCooperativeKernel(kern, dim3(grid), dim3(NT), args, 0, ctx->stream));
+  post_launch(ctx, pair_cta ? "jacobi_pair_kernel" : "jacobi_kernel");
   GridBar hb;
   LRA_CUDA(cudaMemcpyAsync(&hb, P.bar, sizeof(GridBar), cudaMemcpyDeviceToHost, ctx->stream));
   LRA_CUDA(cudaStreamSynchronize(ctx->stream));
@@ -225,8 +391,8 @@ bool is_symmetric(lra_ctx* ctx, int64_t n, const T* A, int64_t lda) {
   return h == 0;
 }
 
-template void jacobi_svd<float>(lra_ctx*, int64_t, float*, int64_t, float*, int64_t, float*);
-template void jacobi_svd<double>(lra_ctx*, int64_t, double*, int64_t, double*, int64_t, double*);
+template void jacobi_svd<float>(lra_ctx*, int64_t, float*, int64_t, float*, int64_t, float*, bool);
+template void jacobi_svd<double>(lra_ctx*, int64_t, double*, int64_t, double*, int64_t, double*, bool);
 template bool is_symmetric<float>(lra_ctx*, int64_t, const float*, int64_t);
 template bool is_symmetric<double>(lra_ctx*, int64_t, const double*, int64_t);
 
@@ -340,6 +506,39 @@ __global__ void trsm_right_diag_kernel(int64_t m, int jb, const T* Rbb, int64_t 
   }
 }
 
+// X[0:jb, :] <- Rbb^{-1} X[0:jb, :] for an upper-triangular jb x jb block
+template <typename T>
+__global__ void trsm_left_diag_kernel(int jb, int64_t nrhs, const T* Rbb, int64_t ldr, T* X, int64_t ldx) {
+  __shared__ T r[CB][CB + 1];
+  for (int t = threadIdx.x; t < jb * jb; t += blockDim.x) {
+    const int i = t % jb, j = t / jb;
+    r[i][j] = Rbb[i + j * ldr];
+  }
+  __syncthreads();
+  for (int64_t col = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; col < nrhs;
+       col += (int64_t)gridDim.x * blockDim.x) {
+    T* xc = X + col * ldx;
+    T x[CB];
+#pragma unroll
+    for (int i = 0; i < CB; ++i)
+      if (i < jb) x[i] = xc[i];
+    // R x = b: x_i = (b_i - sum_{q>i} R_iq x_q) / R_ii, bottom up
+#pragma unroll
+    for (int i = CB - 1; i >= 0; --i) {
+      if (i < jb) {
+        T s = x[i];
+#pragma unroll
+        for (int q = CB - 1; q > i; --q)
+          if (q < jb) s -= r[i][q] * x[q];
+        x[i] = s / r[i][i];
+      }
+    }
+#pragma unroll
+    for (int i = 0; i < CB; ++i)
+      if (i < jb) xc[i] = x[i];
+  }
+}
+
 }  // namespace
 
 template <typename T>
@@ -373,23 +572,34 @@ bool potrf_upper(lra_ctx* ctx, int64_t k, T* G, int64_t ldg) {
 }
 
 template <typename T>
+void trsm_left_diag(lra_ctx* ctx, int jb, int64_t nrhs, const T* R, int64_t ldr, T* X, int64_t ldx) {
+  const unsigned g = (unsigned)std::max<int64_t>(1, std::min<int64_t>((nrhs + 127) / 128, ctx->num_sms * 8));
+  trsm_left_diag_kernel<T><<<g, 128, 0, ctx->stream>>>(jb, nrhs, R, ldr, X, ldx);
+  post_launch(ctx, "trsm_left_diag_kernel");
+}
+
+// X <- X triu(R)^{-1}, recursive like trsm_upper: the leading half, a GEMM
+// update of the trailing columns, the trailing half
+template <typename T>
 void trsm_right_upper(lra_ctx* ctx, int64_t m, int64_t k, const T* R, int64_t ldr, T* X, int64_t ldx) {
   if (m <= 0 || k <= 0) return;
-  for (int64_t j0 = 0; j0 < k; j0 += CB) {
-    const int jb = (int)std::min<int64_t>(CB, k - j0);
+  if (k <= CB) {
     const unsigned g = (unsigned)std::max<int64_t>(1, std::min<int64_t>((m + 127) / 128, ctx->num_sms * 8));
-    trsm_right_diag_kernel<T><<<g, 128, 0, ctx->stream>>>(m, jb, R + j0 + j0 * ldr, ldr, X + j0 * ldx, ldx);
+    trsm_right_diag_kernel<T><<<g, 128, 0, ctx->stream>>>(m, (int)k, R, ldr, X, ldx);
     post_launch(ctx, "trsm_right_diag_kernel");
-    const int64_t rest = k - j0 - jb;
-    if (rest > 0)  // X[:, >b] -= X_b R_{b, >b}
-      gemm<T>(ctx, 'n', 'n', m, rest, jb, T(-1), X + j0 * ldx, ldx, R + j0 + (j0 + jb) * ldr, ldr, T(1),
-              X + (j0 + jb) * ldx, ldx);
+    return;
   }
+  const int64_t k1 = (k / 2 + CB - 1) / CB * CB, k2 = k - k1;
+  trsm_right_upper(ctx, m, k1, R, ldr, X, ldx);
+  gemm<T>(ctx, 'n', 'n', m, k2, k1, T(-1), X, ldx, R + k1 * ldr, ldr, T(1), X + k1 * ldx, ldx);
+  trsm_right_upper(ctx, m, k2, R + k1 + k1 * ldr, ldr, X + k1 * ldx, ldx);
 }
 
 template bool potrf_upper<float>(lra_ctx*, int64_t, float*, int64_t);
 template bool potrf_upper<double>(lra_ctx*, int64_t, double*, int64_t);
 template void trsm_right_upper<float>(lra_ctx*, int64_t, int64_t, const float*, int64_t, float*, int64_t);
 template void trsm_right_upper<double>(lra_ctx*, int64_t, int64_t, const double*, int64_t, double*, int64_t);
+template void trsm_left_diag<float>(lra_ctx*, int, int64_t, const float*, int64_t, float*, int64_t);
+template void trsm_left_diag<double>(lra_ctx*, int, int64_t, const double*, int64_t, double*, int64_t);
 
 }  // namespace lra

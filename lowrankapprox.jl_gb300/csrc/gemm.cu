@@ -181,6 +181,12 @@ void gemm(lra_ctx* ctx, char ta, char tb, int64_t m, int64_t n, int64_t k, T alp
     post_launch(ctx, "scale_kernel");
     return;
   }
+  if constexpr (sizeof(T) == 8) {
+    if (ctx->gemm_tc && tc_gemm_worthwhile(m, n, k)) {
+      tc_gemm(ctx, ta, tb, m, n, k, alpha, A, lda, B, ldb, beta, C, ldc);
+      return;
+    }
+  }
   const bool TA = (ta == 't' || ta == 'T' || ta == 'c' || ta == 'C');
   const bool TB = (tb == 't' || tb == 'T' || tb == 'c' || tb == 'C');
   const int64_t tiles = ((m + BM - 1) / BM) * ((n + BN - 1) / BN);

@@ -68,6 +68,8 @@ struct lra_ctx {
   double stage_ms[4] = {0, 0, 0, 0};
   cudaEvent_t ev[5] = {nullptr, nullptr, nullptr, nullptr, nullptr};
   uint64_t rng_counter = 0;  // advances per call of the in-library generator
+  // the mixed-precision path sends large Float64 GEMMs to tc_gemm
+  bool gemm_tc = false;
   // pinned host staging (grown on demand)
   void* pinned = nullptr;
   size_t pinned_cap = 0;
@@ -95,11 +97,29 @@ struct TcSplit {
 bool tc_sketch_supported(int64_t order, int64_t M, int64_t N);
 template <typename T>
 void tc_split(lra_ctx* ctx, char trans, int64_t M, int64_t N, const T* A, int64_t lda, int ns,
-              TcSplit* out);
+              TcSplit* out, bool balanced = false);
 // B (order x N, ldb) = S op(A) on tcgen05 tensor cores; S is order x M
 // (ld = order) with entries on the 1/32 lattice.
 template <typename T>
 void tc_sketch(lra_ctx* ctx, const TcSplit& sp, int64_t order, const T* S, T* B, int64_t ldb);
+
+// Keeps a stretch of work on the FP64 CUDA-core GEMM (products whose
+// result must be orthonormal to working precision).
+struct NativeGemmScope {
+  lra_ctx* ctx;
+  bool saved;
+  explicit NativeGemmScope(lra_ctx* c) : ctx(c), saved(c->gemm_tc) { c->gemm_tc = false; }
+  ~NativeGemmScope() { ctx->gemm_tc = saved; }
+  NativeGemmScope(const NativeGemmScope&) = delete;
+  NativeGemmScope& operator=(const NativeGemmScope&) = delete;
+};
+
+// C = alpha op(A) op(B) + beta C in Float64 on tcgen05 tensor cores from
+// six exact BF16 byte slices of each operand (error near 2^-45 of the
+// row / column scales); used by the mixed-precision path.
+bool tc_gemm_worthwhile(int64_t m, int64_t n, int64_t k);
+void tc_gemm(lra_ctx* ctx, char ta, char tb, int64_t m, int64_t n, int64_t k, double alpha, const double* A,
+             int64_t lda, const double* B, int64_t ldb, double beta, double* C, int64_t ldc);
 
 // Rank-adaptive column-pivoted Householder QR (geqp3_adap!), in place.
 // pivot == false runs the same Householder QR without pivoting.
@@ -115,6 +135,8 @@ int64_t geqp3_adap_noalloc(lra_ctx* ctx, int64_t m, int64_t n, T* A, int64_t lda
 int64_t noalloc_max_cols();
 
 // X (k x nrhs) <- triu(R)^{-1} X, R k x k (ldr).
+template <typename T>
+void trsm_left_diag(lra_ctx* ctx, int jb, int64_t nrhs, const T* R, int64_t ldr, T* X, int64_t ldx);
 template <typename T>
 void trsm_upper(lra_ctx* ctx, int64_t k, int64_t nrhs, const T* R, int64_t ldr, T* X,
                 int64_t ldx);
@@ -132,7 +154,7 @@ void orgqr(lra_ctx* ctx, int64_t m, int64_t k, T* V, int64_t ldv, const T* tau);
 // One-sided Jacobi SVD of X (n x n, square, in place): on exit X = U * S,
 // V (n x n) accumulates the right rotations, S gets the column norms.
 template <typename T>
-void jacobi_svd(lra_ctx* ctx, int64_t n, T* X, int64_t ldx, T* V, int64_t ldv, T* S);
+void jacobi_svd(lra_ctx* ctx, int64_t n, T* X, int64_t ldx, T* V, int64_t ldv, T* S, bool quadratic_stop = false);
 
 // G = R^T R in place (upper R, lower part zeroed), blocked; false when G is
 // not numerically positive definite
@@ -156,6 +178,10 @@ template <typename T>
 std::vector<T> small_svd(lra_ctx* ctx, int64_t k, const T* Mm, T* U, T* V, T* S);
 template <typename T>
 std::vector<T> sort_desc(lra_ctx* ctx, int64_t k, T* S, T* U, T* V);
+
+// jacobi_svd for Float64 with the bulk of the sweeps in FP32 and FP64 polish
+template <typename T>
+void jacobi_svd_fast(lra_ctx* ctx, int64_t n, T* X, int64_t ldx, T* V, int64_t ldv, T* S);
 
 // exact symmetry test of a square device matrix
 template <typename T>
@@ -232,6 +258,10 @@ void sub_sketch(lra_ctx* ctx, char trans, int64_t M, int64_t N, const T* A, int6
                 const int64_t* rows, int64_t order, T* B, int64_t ldb);
 template <typename T>
 void srft_signs(lra_ctx* ctx, const double* g, int64_t n, T* d);
+// FFT-based SRFT (srft.cu); false when the shape needs srft_sketch
+template <typename T>
+bool srft_sketch_fft(lra_ctx* ctx, char trans, int64_t M, int64_t N, const T* A, int64_t lda, const T* d,
+                     const int64_t* idx, int64_t order, T* B, int64_t ldb);
 template <typename T>
 void sprn_sketch(lra_ctx* ctx, char trans, int64_t M, int64_t N, const T* A, int64_t lda,
                  const int64_t* perm, const T* g, int64_t order, T* B, int64_t ldb);

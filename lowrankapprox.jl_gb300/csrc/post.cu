@@ -20,6 +20,7 @@
 
 #include <algorithm>
 #include <cmath>
+#include <cstring>
 #include <numeric>
 #include <vector>
 
@@ -104,7 +105,7 @@ std::vector<T> small_svd(lra_ctx* ctx, int64_t k, const T* Mm, T* U, T* V, T* S)
   if (k == 0) return {};
   // X = Mm^T; Jacobi: X W = Y diag(S) -> Mm = W diag(S) Y^T: U_M = W, V_M = Y
   transpose(ctx, k, k, Mm, k, V, k);
-  jacobi_svd<T>(ctx, k, V, k, U, k, S);
+  jacobi_svd_fast<T>(ctx, k, V, k, U, k, S);
   div_cols(ctx, k, k, V, k, S);
   return sort_desc(ctx, k, S, U, V);
 }
@@ -118,5 +119,110 @@ template std::vector<float> small_svd<float>(lra_ctx*, int64_t, const float*, fl
 template std::vector<double> small_svd<double>(lra_ctx*, int64_t, const double*, double*, double*, double*);
 template std::vector<float> sort_desc<float>(lra_ctx*, int64_t, float*, float*, float*);
 template std::vector<double> sort_desc<double>(lra_ctx*, int64_t, double*, double*, double*);
+
+}  // namespace lra
+
+// ---- mixed-precision one-sided Jacobi -------------------------------------------
+// FP64 runs at 1/64 of the FP32 rate on GB300, so the sweeps that only need to
+// bring the columns close to orthogonal run in FP32; the accumulated FP32
+// rotation is re-orthonormalized in FP64 (Cholesky QR of a near-identity
+// Gram matrix), applied to X in FP64, and FP64 sweeps finish from there --
+// they converge quadratically from the FP32 level in one or two sweeps.
+
+namespace lra {
+
+namespace {
+
+template <typename S, typename D>
+__global__ void cast_kernel(int64_t m, int64_t n, const S* __restrict__ a, int64_t lda, D* __restrict__ b,
+                            int64_t ldb, double scale) {
+  const int64_t total = m * n;
+  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < total; t += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t i = t % m, j = t / m;
+    b[i + j * ldb] = (D)((double)a[i + j * lda] * scale);
+  }
+}
+
+template <typename S, typename D>
+void cast(lra_ctx* ctx, int64_t m, int64_t n, const S* a, int64_t lda, D* b, int64_t ldb, double scale = 1.0) {
+  const unsigned g = (unsigned)std::max<int64_t>(1, std::min<int64_t>((m * n + 255) / 256, ctx->num_sms * 8));
+  cast_kernel<S, D><<<g, 256, 0, ctx->stream>>>(m, n, a, lda, b, ldb, scale);
+  post_launch(ctx, "cast_kernel");
+}
+
+// max |a| as the bit pattern of a nonnegative double (NaN / Inf as +Inf)
+template <typename T>
+__global__ void absmax_bits_kernel(int64_t m, int64_t n, const T* __restrict__ a, int64_t lda,
+                                   unsigned long long* __restrict__ out) {
+  double mx = 0;
+  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < m * n; t += (int64_t)gridDim.x * blockDim.x) {
+    const double v = fabs((double)a[t % m + (t / m) * lda]);
+    mx = v <= 1.7976931348623157e308 ? fmax(mx, v) : INFINITY;
+  }
+  mx = warp_max(mx);
+  if ((threadIdx.x & 31) == 0 && mx > 0) atomicMax(out, (unsigned long long)__double_as_longlong(mx));
+}
+
+}  // namespace
+
+template <typename T>
+void jacobi_svd_fast(lra_ctx* ctx, int64_t n, T* X, int64_t ldx, T* V, int64_t ldv, T* S) {
+  if (sizeof(T) != 8 || n < 64) {
+    jacobi_svd<T>(ctx, n, X, ldx, V, ldv, S);
+    return;
+  }
+  const NativeGemmScope native(ctx);  // W must come out orthonormal to FP64 rounding
+  const ArenaMark mk = ctx->arena.mark();
+  // 1. FP32 sweeps on X scaled by a power of two into FP32's range (the
+  //    rotations do not depend on the scale)
+  double scale = 1.0;
+  {
+    unsigned long long* mx = ctx->arena.alloc_n<unsigned long long>(1);
+    LRA_CUDA(cudaMemsetAsync(mx, 0, sizeof(unsigned long long), ctx->stream));
+    const unsigned g = (unsigned)std::max<int64_t>(1, std::min<int64_t>((n * n + 255) / 256, ctx->num_sms * 4));
+    absmax_bits_kernel<T><<<g, 256, 0, ctx->stream>>>(n, n, X, ldx, mx);
+    post_launch(ctx, "absmax_bits_kernel");
+    unsigned long long hb = 0;
+    LRA_CUDA(cudaMemcpyAsync(&hb, mx, sizeof(hb), cudaMemcpyDeviceToHost, ctx->stream));
+    LRA_CUDA(cudaStreamSynchronize(ctx->stream));
+    double hm;
+    std::memcpy(&hm, &hb, sizeof(hm));
+    if (!(hm > 0) || !std::isfinite(hm)) {
+      // nothing to rotate, or not a finite matrix: the FP64 sweeps handle it
+      ctx->arena.release(mk);
+      jacobi_svd<T>(ctx, n, X, ldx, V, ldv, S);
+      return;
+    }
+    scale = std::ldexp(1.0, -std::ilogb(hm));
+  }
+  float* X32 = ctx->arena.alloc_n<float>((size_t)n * n);
+  float* V32 = ctx->arena.alloc_n<float>((size_t)n * n);
+  float* S32 = ctx->arena.alloc_n<float>(n);
+  cast<T, float>(ctx, n, n, X, ldx, X32, n, scale);
+  jacobi_svd<float>(ctx, n, X32, n, V32, n, S32);
+  // 2. the rotation in FP64, re-orthonormalized: W = V32 chol(V32' V32)^{-1}
+  T* W = ctx->arena.alloc_n<T>((size_t)n * n);
+  T* G = ctx->arena.alloc_n<T>((size_t)n * n);
+  cast<float, T>(ctx, n, n, V32, n, W, n);
+  gemm<T>(ctx, 't', 'n', n, n, n, T(1), W, n, W, n, T(0), G, n);
+  if (!potrf_upper(ctx, n, G, n)) {
+    // cannot happen for a near-orthogonal W; fall back to the FP64 sweeps
+    ctx->arena.release(mk);
+    jacobi_svd<T>(ctx, n, X, ldx, V, ldv, S);
+    return;
+  }
+  trsm_right_upper(ctx, n, n, G, n, W, n);
+  // 3. X <- X W, FP64 sweeps, V = W V2
+  T* Y = ctx->arena.alloc_n<T>((size_t)n * n);
+  gemm<T>(ctx, 'n', 'n', n, n, n, T(1), X, ldx, W, n, T(0), Y, n);
+  copy_matrix(ctx, n, n, Y, n, X, ldx);
+  jacobi_svd<T>(ctx, n, X, ldx, Y, n, S, true);  // Y <- V2
+  gemm<T>(ctx, 'n', 'n', n, n, n, T(1), W, n, Y, n, T(0), V, ldv);
+  LRA_CUDA(cudaStreamSynchronize(ctx->stream));
+  ctx->arena.release(mk);
+}
+
+template void jacobi_svd_fast<float>(lra_ctx*, int64_t, float*, int64_t, float*, int64_t, float*);
+template void jacobi_svd_fast<double>(lra_ctx*, int64_t, double*, int64_t, double*, int64_t, double*);
 
 }  // namespace lra

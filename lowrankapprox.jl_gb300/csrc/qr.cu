@@ -398,32 +398,480 @@ __global__ void __launch_bounds__(NT) geqp3_kernel(QrParams<T> P) {
   if (blockIdx.x == 0 && threadIdx.x == 0) *P.k_out = kres;
 }
 
-// ---- triangular solve: X <- triu(R)^{-1} X, one warp per right-hand side ----
-template <typename T>
-__global__ void trsm_upper_kernel(int64_t k, int64_t nrhs, const T* __restrict__ R, int64_t ldr,
-                                  T* __restrict__ X, int64_t ldx) {
-  extern __shared__ unsigned char smem_raw[];
-  T* sb = reinterpret_cast<T*>(smem_raw);
+// ---- geqp3_adap!, one grid barrier per pivot ---------------------------------------
+//
+// Columns never move during the factorization: pivot c is the physical
+// column piv[c], R's row c sits in row c of every column, the reflector of
+// pivot c below it in column piv[c].  Every CTA computes the xLARFG
+// reflector of the pivot column itself, into its own shared memory, with
+// the same block reductions (so the values agree bit for bit); CTA 0 writes
+// it back.  Each warp owns the columns gw, gw + W, ... and keeps their partial
+// norms in registers, one lane per column.  A pivot thus needs one bounded
+// grid barrier, after which every CTA reduces the per-CTA candidates.
+// LAPACK's column swaps are replayed afterwards (geqp3_permute) so that A,
+// jpvt and the order of the non-pivot columns come out as xLAQPS leaves
+// them.  Exactly equal partial norms go to the lowest physical index.
+
+struct QrV2Extra {
+  int64_t* piv;     // pivot c -> physical column
+  int64_t* nfac;    // number of pivots performed
+  long long* part_k;  // per-CTA pivot candidate keys
+};
+
+// Column state lives in shared memory, one slot per column the CTA owns:
+// column j belongs to warp j mod W (W warps in the grid), and its slot in
+// the owning CTA is (j div W) * NW + warp-in-CTA.  The dot products and
+// updates run a warp per column, two columns at a time so that their load
+// and reduction latencies overlap; the norm downdates, which cost two FP64
+// divisions and a square root per column, run a thread per slot.  The
+// reflector's scalars are computed once per CTA by warp 0, and pivot
+// candidates are compared as integer keys (the bit patterns of nonnegative
+// floating-point norms order like the norms).
+constexpr int QCH = 16;  // rows per lane per register chunk (512 rows)
+constexpr int QG = 4;    // rows per lane issued between uniform range checks
+constexpr unsigned char ST_LIVE = 1, ST_DONE = 2, ST_FLAG = 4;
+
+__device__ __forceinline__ long long norm_key(double v) {
+  const long long b = __double_as_longlong(v);
+  return b < 0 ? -1 : b;
+}
+__device__ __forceinline__ long long norm_key(float v) {
+  const int b = __float_as_int(v);
+  return b < 0 ? -1 : (long long)b;
+}
+
+__device__ __forceinline__ void key_merge(long long& k, int64_t& i, long long k2, int64_t i2) {
+  if (k2 > k || (k2 == k && i2 < i)) {
+    k = k2;
+    i = i2;
+  }
+}
+
+// block-wide argmax of (key, index); the index of the winner on all threads
+__device__ int64_t block_argmax_key(long long k, int64_t i, long long* sk, int64_t* si) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    const long long k2 = __shfl_xor_sync(0xffffffffu, k, o);
+    const int64_t i2 = __shfl_xor_sync(0xffffffffu, i, o);
+    key_merge(k, i, k2, i2);
+  }
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
   const int nw = blockDim.x >> 5;
-  T* b = sb + (int64_t)wid * k;
-  for (int64_t col = (int64_t)blockIdx.x * nw + wid; col < nrhs; col += (int64_t)gridDim.x * nw) {
-    T* x = X + col * ldx;
-    for (int64_t i = lane; i < k; i += 32) b[i] = x[i];
-    __syncwarp();
-    for (int64_t i = k - 1; i >= 0; --i) {
-      const T xi = b[i] / R[i + i * ldr];
-      __syncwarp();
-      if (xi != 0) {
-        const T* ri = R + i * ldr;
-        for (int64_t q = lane; q < i; q += 32) b[q] -= xi * ri[q];
-      }
-      if (lane == 0) b[i] = xi;
-      __syncwarp();
-    }
-    for (int64_t i = lane; i < k; i += 32) x[i] = b[i];
-    __syncwarp();
+  __syncthreads();
+  if (lane == 0) {
+    sk[wid] = k;
+    si[wid] = i;
   }
+  __syncthreads();
+  if (wid == 0) {
+    long long kk = lane < nw ? sk[lane] : -2;
+    int64_t ii = lane < nw ? si[lane] : INT64_MAX;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      const long long k2 = __shfl_xor_sync(0xffffffffu, kk, o);
+      const int64_t i2 = __shfl_xor_sync(0xffffffffu, ii, o);
+      key_merge(kk, ii, k2, i2);
+    }
+    if (lane == 0) si[0] = ii;
+  }
+  __syncthreads();
+  const int64_t r = si[0];
+  __syncthreads();
+  return r;
+}
+
+// 2-norm of the reflector tail x[0..len) in shared memory, by one warp:
+// an unscaled sum of squares when it is safely inside the exponent range,
+// else LAPACK's scaled form
+template <typename T>
+__device__ T warp_nrm2_smem(const T* x, int64_t len, int lane) {
+  double a0 = 0, a1 = 0;
+  int64_t i = lane;
+  for (; i + 32 < len; i += 64) {
+    const double u = (double)x[i], w = (double)x[i + 32];
+    a0 = fma(u, u, a0);
+    a1 = fma(w, w, a1);
+  }
+  if (i < len) {
+    const double u = (double)x[i];
+    a0 = fma(u, u, a0);
+  }
+  double ssq = warp_sum(a0 + a1);
+  if (ssq > 1e-280 && ssq < 1e280) return (T)sqrt(ssq);
+  double mx = 0;
+  for (int64_t q = lane; q < len; q += 32) mx = fmax(mx, fabs((double)x[q]));
+  mx = warp_max(mx);
+  if (mx == 0 || !isfinite(mx)) return (T)mx;
+  const double s = pow2_scale_inv(mx);
+  double acc = 0;
+  for (int64_t q = lane; q < len; q += 32) {
+    const double t = (double)x[q] * s;
+    acc = fma(t, t, acc);
+  }
+  acc = warp_sum(acc);
+  return (T)(sqrt(acc) / s);
+}
+
+template <typename T>
+struct QrShared {
+  long long sk[32];
+  int64_t si[32];
+  double red[32];
+  T alpha, tau, beta, scal;
+  int knt;
+};
+
+template <typename T, int NT>
+__global__ void __launch_bounds__(NT) geqp3_v2_kernel(QrParams<T> P, QrV2Extra X) {
+  __shared__ QrShared<T> sh;
+  extern __shared__ unsigned char qr_dyn[];
+  constexpr int NW = NT / 32;
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  const int64_t gw = (int64_t)blockIdx.x * NW + wid;
+  const int64_t W = (int64_t)gridDim.x * NW;
+  const int64_t m = P.m, n = P.n, lda = P.lda;
+  T* __restrict__ A = P.A;
+  const T tol3z = sqrt(Real<T>::eps);
+  const int64_t lastrk = m < n ? m : n;
+  const int64_t ncol = gw < n ? (n - 1 - gw) / W + 1 : 0;  // columns of this warp
+  const int64_t ncmax = (n + W - 1) / W;
+  const int nslot = (int)(ncmax * NW);
+  T* vs = reinterpret_cast<T*>(qr_dyn);
+  T* s_vn1 = vs + P.vcap;
+  T* s_vn2 = s_vn1 + nslot;
+  T* s_arc = s_vn2 + nslot;
+  unsigned char* s_st = reinterpret_cast<unsigned char*>(s_arc + nslot);
+  // slot -> column of this CTA
+  auto slot_col = [&](int s) -> int64_t {
+    return (int64_t)blockIdx.x * NW + (s % NW) + (int64_t)(s / NW) * W;
+  };
+  // every CTA reduces the per-CTA candidates to the global pivot
+  auto reduce_pivot_key = [&]() -> int64_t {
+    long long k = -2;
+    int64_t i = INT64_MAX;
+    for (int b = threadIdx.x; b < gridDim.x; b += NT) key_merge(k, i, __ldcg(X.part_k + b), __ldcg(P.part_i + b));
+    return block_argmax_key(k, i, sh.sk, sh.si);
+  };
+
+  // per-CTA winner (key and index) to the grid-wide partials
+  auto publish = [&](long long k, int64_t i) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      const long long k2 = __shfl_xor_sync(0xffffffffu, k, o);
+      const int64_t i2 = __shfl_xor_sync(0xffffffffu, i, o);
+      key_merge(k, i, k2, i2);
+    }
+    __syncthreads();
+    if (lane == 0) {
+      sh.sk[wid] = k;
+      sh.si[wid] = i;
+    }
+    __syncthreads();
+    if (wid == 0) {
+      long long k0 = lane < NW ? sh.sk[lane] : -2;
+      int64_t i0 = lane < NW ? sh.si[lane] : INT64_MAX;
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) {
+        const long long k2 = __shfl_xor_sync(0xffffffffu, k0, o);
+        const int64_t i2 = __shfl_xor_sync(0xffffffffu, i0, o);
+        key_merge(k0, i0, k2, i2);
+      }
+      if (lane == 0) {
+        X.part_k[blockIdx.x] = k0;
+        P.part_i[blockIdx.x] = i0;
+      }
+    }
+  };
+
+  // ---- initial column norms, ptol, first pivot -----------------------------
+  for (int64_t t = 0; t < ncol; ++t) {
+    const int64_t j = gw + t * W;
+    const T nr = P.pivot ? warp_nrm2(A + j * lda, m, lane) : T(0);
+    if (lane == 0) {
+      const int s = (int)(t * NW + wid);
+      s_vn1[s] = s_vn2[s] = nr;
+    }
+  }
+  for (int s = threadIdx.x; s < nslot; s += NT) s_st[s] = slot_col(s) < n ? ST_LIVE : 0;
+  __syncthreads();
+  double lmax = 0;
+  long long bk = -2;
+  int64_t bi = INT64_MAX;
+  for (int s = threadIdx.x; s < nslot; s += NT)
+    if (s_st[s] & ST_LIVE) {
+      lmax = fmax(lmax, (double)s_vn1[s]);
+      key_merge(bk, bi, norm_key(s_vn1[s]), slot_col(s));
+    }
+  lmax = block_max(lmax, sh.red);
+  publish(bk, bi);
+  if (threadIdx.x == 0) P.part_d[blockIdx.x] = lmax;
+  if (!grid_sync(P.bar)) return;
+  double maxnrm = 0;
+  for (int b = threadIdx.x; b < gridDim.x; b += blockDim.x) maxnrm = fmax(maxnrm, __ldcg(P.part_d + b));
+  maxnrm = block_max(maxnrm, sh.red);
+  const double ptol = fmax(P.atol, P.rtol * maxnrm);
+  int64_t pvt = reduce_pivot_key();
+
+  int64_t kres = P.kmax, nfac = 0;
+  int64_t j = 0;
+  int par = 0;
+  while (j < P.kmax) {
+    const int64_t jb = min(P.nb, P.kmax - j);
+    int* lst = P.lsticc + par;
+    if (blockIdx.x == 0 && threadIdx.x == 0) P.lsticc[par ^ 1] = 0;
+    int64_t kk = 0;
+    bool stop_block = false;
+    while (kk < jb && !stop_block) {
+      const int64_t c = j + kk;
+      if (!P.pivot) pvt = c;
+      // ---- every CTA: the reflector of column pvt, rows c..m-1 ---------------
+      const int64_t len = m - c - 1;
+      T* pc = A + pvt * lda;
+      for (int64_t i = threadIdx.x; i < len; i += NT) vs[i] = __ldcg(pc + c + 1 + i);
+      if (threadIdx.x == 0) sh.alpha = __ldcg(pc + c);
+      __syncthreads();
+      if (wid == 0) {
+        // xLARFG: scalars by warp 0, broadcast through shared memory
+        T alpha = sh.alpha, tau = 0, beta = alpha, scal = 1;
+        int knt = 0;
+        if (len > 0) {
+          T xnorm = warp_nrm2_smem(vs, len, lane);
+          if (xnorm != 0) {
+            beta = -copysign(lapy2(alpha, xnorm), alpha);
+            const T safmin = Real<T>::safmin / Real<T>::eps;
+            if (fabs(beta) < safmin) {
+              const T rsafmn = T(1) / safmin;
+              do {
+                ++knt;
+                for (int64_t i = lane; i < len; i += 32) vs[i] *= rsafmn;
+                __syncwarp();
+                beta *= rsafmn;
+                alpha *= rsafmn;
+              } while (fabs(beta) < safmin && knt < 20);
+              xnorm = warp_nrm2_smem(vs, len, lane);
+              beta = -copysign(lapy2(alpha, xnorm), alpha);
+            }
+            tau = (beta - alpha) / beta;
+            scal = T(1) / (alpha - beta);
+            for (int q = 0; q < knt; ++q) beta *= safmin;
+          }
+        }
+        if (lane == 0) {
+          sh.tau = tau;
+          sh.beta = beta;
+          sh.scal = scal;
+        }
+      }
+      __syncthreads();
+      const T tau = sh.tau;
+      if (tau != 0) {
+        const T scal = sh.scal;
+        for (int64_t i = threadIdx.x; i < len; i += NT) vs[i] *= scal;
+      }
+      __syncthreads();
+      if (blockIdx.x == 0) {
+        if (tau != 0)
+          for (int64_t i = threadIdx.x; i < len; i += NT) pc[c + 1 + i] = vs[i];
+        if (threadIdx.x == 0) {
+          pc[c] = sh.beta;
+          P.tau[c] = tau;
+          X.piv[c] = pvt;
+        }
+      }
+      // ---- each warp: apply H(c) to its live columns, two at a time -----------
+      auto dead = [&](int64_t t) {
+        return (s_st[t * NW + wid] & ST_DONE) || gw + t * W == pvt;
+      };
+      int64_t t = 0;
+      while (true) {
+        while (t < ncol && dead(t)) ++t;
+        if (t >= ncol) break;
+        const int64_t ta = t++;
+        while (t < ncol && dead(t)) ++t;
+        const bool two = t < ncol;
+        const int64_t tb = two ? t++ : ta;
+        T* ca = A + (gw + ta * W) * lda;
+        T* cb = A + (gw + tb * W) * lda;
+        const T arca0 = __ldcg(ca + c);
+        const T arcb0 = two ? __ldcg(cb + c) : T(0);
+        T* ya = ca + c + 1;
+        T* yb = cb + c + 1;
+        T sa = 0, sb = 0;
+        T xa[QCH], xb[QCH];
+        if (tau != 0) {
+          for (int64_t b0 = 0; b0 < len; b0 += 32 * QCH) {
+            const int64_t rem = len - b0;
+#pragma unroll
+            for (int q = 0; q < QCH; ++q) {
+              if (q % QG == 0 && 32 * q >= rem) break;
+              const int64_t i = b0 + lane + 32 * q;
+              xa[q] = i < len ? __ldcg(ya + i) : T(0);
+              xb[q] = (two && i < len) ? __ldcg(yb + i) : T(0);
+            }
+#pragma unroll
+            for (int q = 0; q < QCH; ++q) {
+              if (q % QG == 0 && 32 * q >= rem) break;
+              const int64_t i = b0 + lane + 32 * q;
+              const T v = i < len ? vs[i] : T(0);
+              sa = fma(v, xa[q], sa);
+              sb = fma(v, xb[q], sb);
+            }
+          }
+        }
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+          sa += __shfl_xor_sync(0xffffffffu, sa, o);
+          sb += __shfl_xor_sync(0xffffffffu, sb, o);
+        }
+        const T fa = tau * (arca0 + sa);
+        const T fb = two ? tau * (arcb0 + sb) : T(0);
+        if (fa != 0 || fb != 0) {
+          for (int64_t b0 = 0; b0 < len; b0 += 32 * QCH) {
+            const int64_t rem = len - b0;
+            if (len > 32 * QCH) {
+#pragma unroll
+              for (int q = 0; q < QCH; ++q) {
+                if (q % QG == 0 && 32 * q >= rem) break;
+                const int64_t i = b0 + lane + 32 * q;
+                xa[q] = i < len ? __ldcg(ya + i) : T(0);
+                xb[q] = (two && i < len) ? __ldcg(yb + i) : T(0);
+              }
+            }
+#pragma unroll
+            for (int q = 0; q < QCH; ++q) {
+              if (q % QG == 0 && 32 * q >= rem) break;
+              const int64_t i = b0 + lane + 32 * q;
+              if (i < len) {
+                const T v = vs[i];
+                if (fa != 0) ya[i] = xa[q] - fa * v;
+                if (two && fb != 0) yb[i] = xb[q] - fb * v;
+              }
+            }
+          }
+        }
+        if (lane == 0) {
+          const T arca = arca0 - fa;
+          ca[c] = arca;
+          s_arc[ta * NW + wid] = arca;
+          if (two) {
+            const T arcb = arcb0 - fb;
+            cb[c] = arcb;
+            s_arc[tb * NW + wid] = arcb;
+          }
+        }
+      }
+      __syncthreads();
+      // ---- a thread per slot: norm downdate and the pivot candidate -----------
+      bk = -2;
+      bi = INT64_MAX;
+      int myflag = 0;
+      for (int s = threadIdx.x; s < nslot; s += NT) {
+        const unsigned char st = s_st[s];
+        if (!(st & ST_LIVE) || (st & ST_DONE)) continue;
+        const int64_t jj = slot_col(s);
+        if (jj == pvt) {
+          s_st[s] = st | ST_DONE;
+          continue;
+        }
+        if (!P.pivot) continue;
+        T v1 = s_vn1[s];
+        if (c < lastrk - 1 && v1 != 0) {
+          T temp = fabs(s_arc[s]) / v1;
+          temp = fmax(T(0), (T(1) + temp) * (T(1) - temp));
+          const T r = v1 / s_vn2[s];
+          const T temp2 = temp * r * r;
+          if (temp2 <= tol3z) {
+            myflag = 1;
+            s_st[s] = st | ST_FLAG;
+          } else {
+            v1 = v1 * sqrt(temp);
+            s_vn1[s] = v1;
+          }
+        }
+        key_merge(bk, bi, norm_key(v1), jj);
+      }
+      if (myflag) atomicAdd(lst, 1);
+      publish(bk, bi);
+      if (!grid_sync(P.bar)) return;
+      stop_block = *((volatile int*)lst) != 0;
+      pvt = reduce_pivot_key();
+      ++kk;
+    }
+    const int64_t kb = kk;
+    const int64_t jn = j + kb;
+    nfac = jn;
+    if (stop_block) {
+      // recompute the flagged partial norms over rows jn..m-1
+      for (int64_t t = 0; t < ncol; ++t) {
+        const int s = (int)(t * NW + wid);
+        if (!(s_st[s] & ST_FLAG) || (s_st[s] & ST_DONE)) continue;
+        const T v1 = warp_nrm2(A + (gw + t * W) * lda + jn, m - jn, lane);
+        __syncwarp();
+        if (lane == 0) {
+          s_vn1[s] = s_vn2[s] = v1;
+          s_st[s] = s_st[s] & (unsigned char)~ST_FLAG;
+        }
+      }
+      __syncthreads();
+      bk = -2;
+      bi = INT64_MAX;
+      for (int s = threadIdx.x; s < nslot; s += NT) {
+        const unsigned char st = s_st[s];
+        if (!(st & ST_LIVE) || (st & ST_DONE)) continue;
+        key_merge(bk, bi, norm_key(s_vn1[s]), slot_col(s));
+      }
+      publish(bk, bi);
+      if (!grid_sync(P.bar)) return;
+      pvt = reduce_pivot_key();
+    }
+    // rank test of geqp3_adap_main! (src/pqr.jl:407-415): R(i, i) lives in
+    // row i of the pivot column piv[i]
+    auto rdiag = [&](int64_t i) { return fabs((double)__ldcg(A + i + __ldcg(X.piv + i) * lda)); };
+    if (rdiag(jn - 1) <= ptol) {
+      bool found = false;
+      for (int64_t i = j; i < jn; ++i) {
+        if (rdiag(i) <= ptol) {
+          kres = i;
+          found = true;
+          break;
+        }
+      }
+      if (found) break;
+    }
+    j = jn;
+    par ^= 1;
+  }
+  if (blockIdx.x == 0 && threadIdx.x == 0) {
+    *P.k_out = kres;
+    *X.nfac = nfac;
+  }
+}
+
+// LAPACK's column order after pivots piv[0..nfac): replay the swaps of
+// position c with the position holding piv[c] (one thread; nfac is small)
+__global__ void geqp3_replay_kernel(int64_t n, const int64_t* piv, const int64_t* nfac_p, int64_t* col_at,
+                                    int64_t* pos) {
+  if (blockIdx.x != 0 || threadIdx.x != 0) return;
+  const int64_t nfac = *nfac_p;
+  for (int64_t c = 0; c < nfac; ++c) {
+    const int64_t pc = piv[c];
+    const int64_t p = pos[pc];
+    const int64_t other = col_at[c];
+    col_at[p] = other;
+    pos[other] = p;
+    col_at[c] = pc;
+    pos[pc] = c;
+  }
+}
+
+__global__ void iota_kernel(int64_t n, int64_t* a, int64_t* b) {
+  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < n; t += (int64_t)gridDim.x * blockDim.x)
+    a[t] = b[t] = t;
+}
+
+__global__ void jpvt_kernel(int64_t n, const int64_t* col_at, int64_t* jpvt) {
+  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < n; t += (int64_t)gridDim.x * blockDim.x)
+    jpvt[t] = col_at[t] + 1;
 }
 
 // ---- Householder application, one warp per column of X ----------------------
@@ -517,10 +965,49 @@ int64_t geqp3_adap(lra_ctx* ctx, int64_t m, int64_t n, T* A, int64_t lda, int64_
     ctx->arena.release(mark);
     return 0;
   }
-  void* args[] = {&P};
-  LRA_CUDA(cudaLaunchCooperativeKernel((const void*)geqp3_kernel<T, NT>, dim3(grid), dim3(NT), args,
-                                       dyn_smem, ctx->stream));
-  post_launch(ctx, "geqp3_kernel");
+  // one barrier per pivot when the reflector and the per-column state of
+  // each CTA fit shared memory
+  const int64_t nwarps = (int64_t)grid * (NT / 32);
+  const int64_t nslot = (n + nwarps - 1) / nwarps * (NT / 32);
+  const size_t smem2 = dyn_smem + (size_t)nslot * (3 * sizeof(T) + 1);
+  const bool v2 = (m - 1) <= vcap && smem2 <= 200 * 1024;
+  if (v2) {
+    LRA_CUDA(cudaFuncSetAttribute(geqp3_v2_kernel<T, NT>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                  (int)smem2));
+    int per_sm2 = 0;
+    LRA_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm2, geqp3_v2_kernel<T, NT>, NT, smem2));
+    if (per_sm2 < 1) fail(LRA_ECUDA, "geqp3 kernel cannot be resident");
+    QrV2Extra X;
+    X.piv = ctx->arena.alloc_n<int64_t>(std::max<int64_t>(P.kmax, 1));
+    X.nfac = ctx->arena.alloc_n<int64_t>(1);
+    X.part_k = ctx->arena.alloc_n<long long>(grid);
+    int64_t* col_at = ctx->arena.alloc_n<int64_t>(n);
+    int64_t* pos = ctx->arena.alloc_n<int64_t>(n);
+    const unsigned gi = (unsigned)std::max<int64_t>(1, std::min<int64_t>((n + 255) / 256, ctx->num_sms * 4));
+    iota_kernel<<<gi, 256, 0, ctx->stream>>>(n, col_at, pos);
+    post_launch(ctx, "iota_kernel");
+    void* args[] = {&P, &X};
+    LRA_CUDA(cudaLaunchCooperativeKernel((const void*)geqp3_v2_kernel<T, NT>, dim3(grid), dim3(NT), args,
+                                         smem2, ctx->stream));
+    post_launch(ctx, "geqp3_v2_kernel");
+    if (pivot) {
+      // xLAQPS's swaps, replayed: jpvt and the column order of A
+      geqp3_replay_kernel<<<1, 32, 0, ctx->stream>>>(n, X.piv, X.nfac, col_at, pos);
+      post_launch(ctx, "geqp3_replay_kernel");
+    }
+    jpvt_kernel<<<gi, 256, 0, ctx->stream>>>(n, col_at, jpvt);
+    post_launch(ctx, "jpvt_kernel");
+    if (pivot) {
+      T* tmp = ctx->arena.alloc_n<T>((size_t)m * n);
+      gather_cols(ctx, m, n, A, lda, jpvt, tmp, m);
+      copy_matrix(ctx, m, n, tmp, m, A, lda);
+    }
+  } else {
+    void* args[] = {&P};
+    LRA_CUDA(cudaLaunchCooperativeKernel((const void*)geqp3_kernel<T, NT>, dim3(grid), dim3(NT), args,
+                                         dyn_smem, ctx->stream));
+    post_launch(ctx, "geqp3_kernel");
+  }
   int64_t k = 0;
   GridBar hb;
   LRA_CUDA(cudaMemcpyAsync(&k, P.k_out, sizeof(int64_t), cudaMemcpyDeviceToHost, ctx->stream));
@@ -531,19 +1018,21 @@ int64_t geqp3_adap(lra_ctx* ctx, int64_t m, int64_t n, T* A, int64_t lda, int64_
   return k;
 }
 
+// X <- triu(R)^{-1} X, recursive: the solve with the trailing half, a GEMM
+// update of the leading rows, the solve with the leading half; blocks of at
+// most 32 rows are solved by trsm_left_diag_kernel (a thread per right-hand
+// side, back substitution in registers)
 template <typename T>
 void trsm_upper(lra_ctx* ctx, int64_t k, int64_t nrhs, const T* R, int64_t ldr, T* X, int64_t ldx) {
   if (k <= 0 || nrhs <= 0) return;
-  int warps = 8;
-  while (warps > 1 && (size_t)warps * k * sizeof(T) > 160 * 1024) warps >>= 1;
-  const size_t smem = (size_t)warps * k * sizeof(T);
-  if (smem > 200 * 1024) fail(LRA_ENOTSUP, "trsm: rank %lld too large", (long long)k);
-  if (smem > 48 * 1024)
-    LRA_CUDA(cudaFuncSetAttribute(trsm_upper_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                  (int)smem));
-  const int64_t blocks = std::min<int64_t>((nrhs + warps - 1) / warps, (int64_t)ctx->num_sms * 8);
-  trsm_upper_kernel<T><<<(unsigned)blocks, warps * 32, smem, ctx->stream>>>(k, nrhs, R, ldr, X, ldx);
-  post_launch(ctx, "trsm_upper_kernel");
+  if (k <= 32) {
+    trsm_left_diag(ctx, (int)k, nrhs, R, ldr, X, ldx);
+    return;
+  }
+  const int64_t k1 = (k / 2 + 31) / 32 * 32, k2 = k - k1;
+  trsm_upper(ctx, k2, nrhs, R + k1 + k1 * ldr, ldr, X + k1, ldx);
+  gemm<T>(ctx, 'n', 'n', k1, nrhs, k2, T(-1), R + k1 * ldr, ldr, X + k1, ldx, T(1), X, ldx);
+  trsm_upper(ctx, k1, nrhs, R, ldr, X, ldx);
 }
 
 template <typename T>

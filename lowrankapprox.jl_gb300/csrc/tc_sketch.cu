@@ -32,6 +32,7 @@
 #include <cudaTypedefs.h>
 
 #include <algorithm>
+#include <cfloat>
 #include <cstring>
 
 #include "common.cuh"
@@ -52,6 +53,7 @@ constexpr int NTHREADS = 320;
 constexpr int MAX_SLICES = 6;
 constexpr int MAX_EXACT = 4;
 constexpr int COLS = TILE_N / 2;               // sketch rows per drain thread
+constexpr int kNonFinite = 1 << 20;            // exponent of a column holding NaN / Inf
 
 struct TcParams {
   int64_t K;       // sketched dimension (rows of op(A))
@@ -341,7 +343,7 @@ __global__ void __launch_bounds__(NTHREADS, 1)
       for (int c = 0; c < COLS; ++c) {
         const int64_t row = r0 + c;
         if (row < P.L) {
-          const double v = ldexp((double)X[c], sc);
+          const double v = e >= kNonFinite ? __longlong_as_double(0x7FF8000000000000ll) : ldexp((double)X[c], sc);
           if (P.out_double)
             static_cast<double*>(P.B)[row + j * P.ldb] = v;
           else
@@ -361,27 +363,52 @@ __global__ void __launch_bounds__(NTHREADS, 1)
 
 // ---- splitting op(A) into byte slices ---------------------------------------------
 
-// per-column exponent e_j with max |op(A)(:, j)| < 2^e_j
+// per-column exponent e_j with max |op(A)(:, j)| < 2^e_j; a column holding
+// a NaN or an infinity gets kNonFinite, and every output it touches is NaN
+__device__ __forceinline__ int colexp_of(double mx) {
+  if (!(mx <= DBL_MAX)) return kNonFinite;
+  return mx > 0 ? ilogb(mx) + 1 : 0;
+}
+
 template <typename T>
 __global__ void colexp_n_kernel(int64_t K, int64_t N, const T* __restrict__ A, int64_t lda, int* e) {
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
   const int nw = blockDim.x >> 5;
   for (int64_t j = (int64_t)blockIdx.x * nw + wid; j < N; j += (int64_t)gridDim.x * nw) {
     double mx = 0;
-    for (int64_t i = lane; i < K; i += 32) mx = fmax(mx, fabs((double)A[i + j * lda]));
+    for (int64_t i = lane; i < K; i += 32) {
+      const double a = fabs((double)A[i + j * lda]);
+      mx = a <= DBL_MAX ? fmax(mx, a) : INFINITY;  // NaN and Inf mark the column
+    }
     mx = warp_max(mx);
-    if (lane == 0) e[j] = mx > 0 ? ilogb(mx) + 1 : 0;
+    if (lane == 0) e[j] = colexp_of(mx);
   }
 }
 
-// op(A) = A^T: column j of op(A) is row j of A
+// op(A) = A^T: column j of op(A) is row j of A.  Tiles of 32 rows of A x
+// 256 of its columns: coalesced partial maxima per row, merged with an
+// atomic max on the bit patterns (nonnegative doubles order like their
+// bits; NaN / Inf are entered as +Inf), then turned into exponents.
 template <typename T>
-__global__ void colexp_c_kernel(int64_t K, int64_t N, const T* __restrict__ A, int64_t lda, int* e) {
-  for (int64_t j = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; j < N; j += (int64_t)gridDim.x * blockDim.x) {
-    double mx = 0;
-    for (int64_t i = 0; i < K; ++i) mx = fmax(mx, fabs((double)A[j + i * lda]));
-    e[j] = mx > 0 ? ilogb(mx) + 1 : 0;
+__global__ void rowmax_kernel(int64_t K, int64_t N, const T* __restrict__ A, int64_t lda,
+                              unsigned long long* __restrict__ mx) {
+  const int64_t tn = (N + 31) / 32, tk = (K + 255) / 256;
+  for (int64_t t = blockIdx.x; t < tn * tk; t += gridDim.x) {
+    const int64_t j = (t % tn) * 32 + threadIdx.x;
+    const int64_t i0 = (t / tn) * 256;
+    double m = 0;
+    if (j < N)
+      for (int64_t i = i0 + threadIdx.y; i < min(K, i0 + 256); i += blockDim.y) {
+        const double a = fabs((double)A[j + i * lda]);
+        m = a <= DBL_MAX ? fmax(m, a) : INFINITY;
+      }
+    if (j < N && m > 0) atomicMax(mx + j, (unsigned long long)__double_as_longlong(m));
   }
+}
+
+__global__ void rowmax_exp_kernel(int64_t N, const unsigned long long* __restrict__ mx, int* __restrict__ e) {
+  for (int64_t j = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; j < N; j += (int64_t)gridDim.x * blockDim.x)
+    e[j] = colexp_of(__longlong_as_double((long long)mx[j]));
 }
 
 // fixed-point integer of x at scale 2^(e - W) (round half up), from the bits
@@ -389,7 +416,7 @@ __device__ __forceinline__ long long fixed_point(double x, int e, int W) {
   const unsigned long long bits = (unsigned long long)__double_as_longlong(x);
   const int ex = (int)((bits >> 52) & 0x7FF);
   unsigned long long mant = bits & ((1ull << 52) - 1);
-  if (ex == 0 && mant == 0) return 0;
+  if ((ex == 0 && mant == 0) || ex == 0x7FF || e >= kNonFinite) return 0;
   if (ex != 0) mant |= 1ull << 52;
   const int e2 = (ex == 0 ? 1 : ex) - 1075;  // x = mant 2^e2
   const int sh = e2 + W - e;                  // F = mant 2^sh, sh < 0 here
@@ -414,9 +441,25 @@ __device__ __forceinline__ __nv_bfloat16 bf16_of(int b, int k) {
   return __ushort_as_bfloat16((unsigned short)(__float_as_uint(f) >> 16));
 }
 
+// n_exact > 0: slices b_1 (signed) and b_2.. (bytes 0..255) of F, those
+// after the first n_exact pre-scaled by 2^-8(s - n_exact - 1) for a shared
+// tail accumulator.  n_exact == 0: balanced digits, F = sum_s b_s 2^(W - 8s)
+// with every b_s rounded to nearest (|b_1| <= 256, |b_s| <= 128 after), so
+// that the products a GEMM drops average to zero instead of piling up.
 template <typename T>
-__device__ __forceinline__ void write_slices(long long F, int ns, int W, __nv_bfloat16* out, int64_t plane) {
-  const int n_exact = ns < MAX_EXACT ? ns : MAX_EXACT;
+__device__ __forceinline__ void write_slices(long long F, int ns, int n_exact, int W, __nv_bfloat16* out,
+                                             int64_t plane) {
+  if (n_exact == 0) {
+#pragma unroll
+    for (int s = 1; s <= MAX_SLICES; ++s) {
+      if (s > ns) break;
+      const int shift = W - 8 * s;
+      const long long b = shift > 0 ? (F + (1ll << (shift - 1))) >> shift : F;
+      F -= b << shift;
+      out[(s - 1) * plane] = bf16_of((int)b, 0);
+    }
+    return;
+  }
 #pragma unroll
   for (int s = 1; s <= MAX_SLICES; ++s) {
     if (s > ns) break;
@@ -429,20 +472,20 @@ __device__ __forceinline__ void write_slices(long long F, int ns, int W, __nv_bf
 
 template <typename T>
 __global__ void split_n_kernel(int64_t K, int64_t N, const T* __restrict__ A, int64_t lda, const int* __restrict__ e,
-                               int ns, int W, __nv_bfloat16* __restrict__ S, int64_t Kp) {
+                               int ns, int n_exact, int W, __nv_bfloat16* __restrict__ S, int64_t Kp) {
   const int64_t total = Kp * N;
   const int64_t plane = Kp * N;
   for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < total; t += (int64_t)gridDim.x * blockDim.x) {
     const int64_t i = t % Kp, j = t / Kp;
     const long long F = i < K ? fixed_point(A[i + j * lda], e[j], W) : 0;
-    write_slices<T>(F, ns, W, S + i + j * Kp, plane);
+    write_slices<T>(F, ns, n_exact, W, S + i + j * Kp, plane);
   }
 }
 
 // op(A) = A^T through 32 x 32 shared-memory tiles
 template <typename T>
 __global__ void split_c_kernel(int64_t K, int64_t N, const T* __restrict__ A, int64_t lda, const int* __restrict__ e,
-                               int ns, int W, __nv_bfloat16* __restrict__ S, int64_t Kp) {
+                               int ns, int n_exact, int W, __nv_bfloat16* __restrict__ S, int64_t Kp) {
   __shared__ T tile[32][33];
   const int64_t plane = Kp * N;
   const int64_t ti = (Kp + 31) / 32, tj = (N + 31) / 32;
@@ -457,7 +500,7 @@ __global__ void split_c_kernel(int64_t K, int64_t N, const T* __restrict__ A, in
       const int64_t i = i0 + threadIdx.x, j = j0 + r;
       if (i < Kp && j < N) {
         const long long F = fixed_point(tile[threadIdx.x][r], e[j], W);
-        write_slices<T>(F, ns, W, S + i + j * Kp, plane);
+        write_slices<T>(F, ns, n_exact, W, S + i + j * Kp, plane);
       }
     }
     __syncthreads();
@@ -482,6 +525,205 @@ __global__ void sketch_t_kernel(int64_t L, int64_t K, const T* __restrict__ S, i
       if (i < Kp && r < Lp) St[i + r * Kp] = __float2bfloat16_rn((float)(tile[threadIdx.x][c] * T(32)));
     }
     __syncthreads();
+  }
+}
+
+// ---- FP64 GEMM from two-sided byte slices -------------------------------------------
+//
+// C = alpha op(A) op(B) + beta C for Float64.  Row i of op(A) and column j of
+// op(B) are 48-bit fixed-point integers at power-of-two scales 2^(ea_i - 48)
+// and 2^(eb_j - 48), each cut into six balanced BF16 digits a_1..a_6,
+// b_1..b_6 (|a_1|, |b_1| <= 256, the rest <= 128; all exact in BF16).  The
+// product is
+//     sum_{s,t} a_s b_t 2^(8(12 - s - t)) 2^(ea_i + eb_j - 96),
+// kept for s + t <= 7 (21 digit products; the dropped ones weigh below
+// 2^-46 of the leading term and, the digits being balanced, average to
+// zero).  The products of one diagonal d = s + t - 2 share a TMEM
+// accumulator whose 64-long K block sums stay below 2^23, so the FP32
+// accumulation is exact.  After every K block the six accumulators are
+// drained into one int64 per output,
+//     X += sum_d acc_d 2^(8(5 - d) - t),   C = 2^(ea_i + eb_j - 56 + t) X,
+// with t = ceil(log2(K blocks)) keeping |X| below 2^63.
+//
+// Same warp roles as the sketch kernel; one 144 KB stage (six 128 x 64 A
+// digit tiles, six 64 x 64 B digit tiles), so the loads of block k + 1
+// overlap the drain of block k.  blockIdx.y selects a range of K blocks;
+// with several, each writes its unscaled partial product to a workspace.
+constexpr int G_TILE_M = 128, G_TILE_N = 64, G_NS = 6;
+constexpr int G_A_BYTES = G_TILE_M * KBLK * 2;               // 16 KB
+constexpr int G_B_BYTES = G_TILE_N * KBLK * 2;               // 8 KB
+constexpr int G_STAGE = G_NS * (G_A_BYTES + G_B_BYTES);      // 144 KB
+constexpr int G_COLS = G_TILE_N / 2;                         // columns per drain thread
+
+struct TgParams {
+  int64_t M, N;
+  int nkb;          // K blocks in all
+  int kb_per;       // K blocks per split
+  int tshift;
+  const int* ea;    // per row of op(A)
+  const int* eb;    // per column of op(B)
+  double* C;
+  int64_t ldc;
+  double alpha, beta;
+  int to_ws;        // write 2^(...) X to C + y M N (ld M), no alpha / beta
+  int* err;
+};
+
+__global__ void __launch_bounds__(NTHREADS, 1)
+    tc_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB, TgParams P) {
+  extern __shared__ __align__(1024) unsigned char smem_raw[];
+  unsigned char* base = reinterpret_cast<unsigned char*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
+  unsigned char* stA = base;
+  unsigned char* stB = base + G_NS * G_A_BYTES;
+  uint64_t* full = reinterpret_cast<uint64_t*>(base + G_STAGE);
+  uint64_t* empty = full + 1;
+  uint64_t* acc_ready = empty + 1;
+  uint64_t* acc_free = acc_ready + 1;
+  uint64_t* mma_done = acc_free + 1;
+  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(mma_done + 1);
+
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int64_t tiles_m = (P.M + G_TILE_M - 1) / G_TILE_M;
+  const int64_t m_tile = blockIdx.x % tiles_m, n_tile = blockIdx.x / tiles_m;
+  const int kb0 = blockIdx.y * P.kb_per;
+  const int nloc = min(P.nkb, kb0 + P.kb_per) - kb0;
+  const int t = P.tshift;
+
+  if (threadIdx.x == 0) {
+    mbar_init(full, 1);
+    mbar_init(empty, 1);
+    mbar_init(acc_ready, 1);
+    mbar_init(acc_free, 8);
+    mbar_init(mma_done, 1);
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  if (warp == 1) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], 512;" ::"r"(smem_u32(tmem_slot))
+                 : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+  }
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  const uint32_t tmem = *tmem_slot;
+
+  if (warp == 0) {
+    if (lane == 0) {
+      int issued = 0;
+      for (int it = 0; it < nloc; ++it) {
+        if (!mbar_wait(empty, (it & 1) ^ 1, P.err)) break;
+        ++issued;
+        const int kx = (kb0 + it) * KBLK;
+        mbar_expect_tx(full, (uint32_t)G_STAGE);
+        for (int q = 0; q < G_NS; ++q) {
+          tma_load_3d(stA + q * G_A_BYTES, &tmA, kx, (int)(m_tile * G_TILE_M), q, full);
+          tma_load_3d(stB + q * G_B_BYTES, &tmB, kx, (int)(n_tile * G_TILE_N), q, full);
+        }
+      }
+      int dummy = 0;
+      if (issued > 0) mbar_wait(full, (issued - 1) & 1, &dummy);
+    }
+  } else if (warp == 1) {
+    if (lane == 0) {
+      constexpr uint32_t idesc = idesc_bf16(G_TILE_M, G_TILE_N);
+      for (int it = 0; it < nloc; ++it) {
+        if (it > 0) {
+          if (!mbar_wait(acc_free, (it - 1) & 1, P.err)) break;
+          tc_fence_after();
+        }
+        if (!mbar_wait(full, it & 1, P.err)) break;
+        tc_fence_after();
+        const uint32_t a0 = smem_u32(stA), b0 = smem_u32(stB);
+        for (int s = 0; s < G_NS; ++s) {
+          for (int u = 0; u + s < G_NS; ++u) {
+            const uint32_t acc = tmem + (uint32_t)((s + u) * G_TILE_N);
+#pragma unroll
+            for (int k4 = 0; k4 < KBLK / 16; ++k4) {
+              const uint64_t ad = sw128_desc(a0 + s * G_A_BYTES + k4 * 32);
+              const uint64_t bd = sw128_desc(b0 + u * G_B_BYTES + k4 * 32);
+              // each diagonal restarts with its (1, d + 1) product
+              mma_bf16(acc, ad, bd, idesc, (s == 0 && k4 == 0) ? 0u : 1u);
+            }
+          }
+        }
+        mma_commit(empty);
+        mma_commit(acc_ready);
+      }
+      mma_commit(mma_done);
+      int dummy = 0;
+      mbar_wait(mma_done, 0, &dummy);
+    }
+  } else {
+    const int q4 = warp & 3;
+    const int half = (warp - 2) >> 2;
+    const uint32_t lane_base = (uint32_t)(32 * q4) << 16;
+    long long X[G_COLS];
+#pragma unroll
+    for (int c = 0; c < G_COLS; ++c) X[c] = 0;
+    bool ok = true;
+    for (int it = 0; it < nloc; ++it) {
+      if (!mbar_wait(acc_ready, it & 1, P.err)) {
+        ok = false;
+        break;
+      }
+      tc_fence_after();
+#pragma unroll 1
+      for (int d = 0; d < G_NS; ++d) {
+        uint32_t r[32];
+        tmem_ld32(tmem + lane_base + (uint32_t)(d * G_TILE_N + half * G_COLS), r);
+        const int w = 8 * (G_NS - 1 - d) - t;
+        if (w >= 0) {
+#pragma unroll
+          for (int c = 0; c < G_COLS; ++c) X[c] += __float2ll_rn(__uint_as_float(r[c])) << w;
+        } else {
+          const float sc = __int_as_float((127 + w) << 23);  // 2^w
+#pragma unroll
+          for (int c = 0; c < G_COLS; ++c) X[c] += __float2ll_rn(__uint_as_float(r[c]) * sc);
+        }
+      }
+      tc_fence_before();
+      __syncwarp();
+      if (lane == 0) mbar_arrive(acc_free);
+    }
+    const int64_t i = m_tile * G_TILE_M + 32 * q4 + lane;
+    if (ok && i < P.M) {
+      const int ea = P.ea[i];
+      const int64_t j0 = n_tile * G_TILE_N + half * G_COLS;
+#pragma unroll
+      for (int c = 0; c < G_COLS; ++c) {
+        const int64_t j = j0 + c;
+        if (j < P.N) {
+          const int eb = P.eb[j];
+          const double v = (ea >= kNonFinite || eb >= kNonFinite) ? __longlong_as_double(0x7FF8000000000000ll)
+                                                                   : ldexp((double)X[c], ea + eb - 56 + t);
+          if (P.to_ws) {
+            P.C[(int64_t)blockIdx.y * P.M * P.N + i + j * P.M] = v;
+          } else {
+            double* cp = P.C + i + j * P.ldc;
+            *cp = P.beta == 0.0 ? P.alpha * v : P.alpha * v + P.beta * *cp;
+          }
+        }
+      }
+    }
+  }
+
+  tc_fence_before();
+  __syncthreads();
+  if (warp == 1) {
+    tc_fence_after();
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, 512;" ::"r"(tmem) : "memory");
+  }
+}
+
+__global__ void tc_gemm_reduce_kernel(int64_t m, int64_t n, int64_t nsplit, const double* __restrict__ W,
+                                      double alpha, double beta, double* __restrict__ C, int64_t ldc) {
+  const int64_t total = m * n;
+  for (int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; q < total; q += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t i = q % m, j = q / m;
+    double s = 0;
+    for (int64_t z = 0; z < nsplit; ++z) s += W[z * total + q];
+    double* c = C + i + j * ldc;
+    *c = beta == 0.0 ? alpha * s : alpha * s + beta * *c;
   }
 }
 
@@ -519,8 +761,10 @@ bool tc_sketch_supported(int64_t order, int64_t M, int64_t N) {
 }
 
 template <typename T>
-void tc_split(lra_ctx* ctx, char trans, int64_t M, int64_t N, const T* A, int64_t lda, int ns, TcSplit* out) {
+void tc_split(lra_ctx* ctx, char trans, int64_t M, int64_t N, const T* A, int64_t lda, int ns, TcSplit* out,
+              bool balanced) {
   const int W = 8 * ns;
+  const int n_exact = balanced ? 0 : std::min(ns, MAX_EXACT);
   const int64_t Kp = (M + 7) / 8 * 8;
   out->K = M;
   out->N = N;
@@ -530,18 +774,28 @@ void tc_split(lra_ctx* ctx, char trans, int64_t M, int64_t N, const T* A, int64_
   out->colexp = ctx->arena.alloc_n<int>(std::max<int64_t>(N, 1));
   out->slices = ctx->arena.alloc_n<__nv_bfloat16>((size_t)ns * Kp * std::max<int64_t>(N, 1));
   if (trans == 'c') {
-    colexp_c_kernel<T><<<nblk(ctx, N, 256), 256, 0, ctx->stream>>>(M, N, A, lda, out->colexp);
-    post_launch(ctx, "colexp_c_kernel");
+    {
+      const ArenaMark mk = ctx->arena.mark();
+      unsigned long long* mx = ctx->arena.alloc_n<unsigned long long>(std::max<int64_t>(N, 1));
+      LRA_CUDA(cudaMemsetAsync(mx, 0, std::max<int64_t>(N, 1) * sizeof(unsigned long long), ctx->stream));
+      const int64_t tiles = ((N + 31) / 32) * ((M + 255) / 256);
+      rowmax_kernel<T><<<(unsigned)std::min<int64_t>(tiles, (int64_t)ctx->num_sms * 16), dim3(32, 8), 0,
+                         ctx->stream>>>(M, N, A, lda, mx);
+      post_launch(ctx, "rowmax_kernel");
+      rowmax_exp_kernel<<<nblk(ctx, N, 256), 256, 0, ctx->stream>>>(N, mx, out->colexp);
+      post_launch(ctx, "rowmax_exp_kernel");
+      ctx->arena.release(mk);  // stream-ordered reuse
+    }
     const int64_t tiles = ((Kp + 31) / 32) * ((N + 31) / 32);
     split_c_kernel<T><<<(unsigned)std::min<int64_t>(tiles, (int64_t)ctx->num_sms * 16), dim3(32, 8), 0,
-                        ctx->stream>>>(M, N, A, lda, out->colexp, ns, W,
+                        ctx->stream>>>(M, N, A, lda, out->colexp, ns, n_exact, W,
                                        static_cast<__nv_bfloat16*>(out->slices), Kp);
     post_launch(ctx, "split_c_kernel");
   } else {
     colexp_n_kernel<T><<<nblk(ctx, N, 8), 256, 0, ctx->stream>>>(M, N, A, lda, out->colexp);
     post_launch(ctx, "colexp_n_kernel");
     split_n_kernel<T><<<nblk(ctx, Kp * N, 256), 256, 0, ctx->stream>>>(
-        M, N, A, lda, out->colexp, ns, W, static_cast<__nv_bfloat16*>(out->slices), Kp);
+        M, N, A, lda, out->colexp, ns, n_exact, W, static_cast<__nv_bfloat16*>(out->slices), Kp);
     post_launch(ctx, "split_n_kernel");
   }
 }
@@ -598,8 +852,85 @@ void tc_sketch(lra_ctx* ctx, const TcSplit& sp, int64_t order, const T* S, T* B,
   if (herr) fail(LRA_ETIMEDOUT, "tc_sketch: a bounded wait timed out");
 }
 
-template void tc_split<float>(lra_ctx*, char, int64_t, int64_t, const float*, int64_t, int, TcSplit*);
-template void tc_split<double>(lra_ctx*, char, int64_t, int64_t, const double*, int64_t, int, TcSplit*);
+bool tc_gemm_worthwhile(int64_t m, int64_t n, int64_t k) {
+  return m > 0 && n > 0 && k > 0 && (double)m * n * k >= 16.0 * 1024 * 1024 && m < (1ll << 30) &&
+         n < (1ll << 30) && k < (1ll << 30);
+}
+
+void tc_gemm(lra_ctx* ctx, char ta, char tb, int64_t m, int64_t n, int64_t k, double alpha, const double* A,
+             int64_t lda, const double* B, int64_t ldb, double beta, double* C, int64_t ldc) {
+  const bool TA = (ta == 't' || ta == 'T' || ta == 'c' || ta == 'C');
+  const bool TB = (tb == 't' || tb == 'T' || tb == 'c' || tb == 'C');
+  const ArenaMark mk = ctx->arena.mark();
+  // X_A = op(A)^T (k x m) and X_B = op(B) (k x n), split by columns
+  TcSplit sa, sb;
+  tc_split<double>(ctx, TA ? 'n' : 'c', k, m, A, lda, G_NS, &sa, true);
+  tc_split<double>(ctx, TB ? 'c' : 'n', k, n, B, ldb, G_NS, &sb, true);
+  const int64_t Kp = sa.Kp;
+  CUtensorMap tmA, tmB;
+  {
+    cuuint64_t dims[3] = {(cuuint64_t)Kp, (cuuint64_t)m, (cuuint64_t)G_NS};
+    cuuint64_t strides[2] = {(cuuint64_t)Kp * 2, (cuuint64_t)Kp * m * 2};
+    cuuint32_t box[3] = {KBLK, G_TILE_M, 1};
+    make_map(&tmA, sa.slices, 3, dims, strides, box);
+  }
+  {
+    cuuint64_t dims[3] = {(cuuint64_t)Kp, (cuuint64_t)n, (cuuint64_t)G_NS};
+    cuuint64_t strides[2] = {(cuuint64_t)Kp * 2, (cuuint64_t)Kp * n * 2};
+    cuuint32_t box[3] = {KBLK, G_TILE_N, 1};
+    make_map(&tmB, sb.slices, 3, dims, strides, box);
+  }
+  const int nkb = (int)((k + KBLK - 1) / KBLK);
+  const int64_t tiles = ((m + G_TILE_M - 1) / G_TILE_M) * ((n + G_TILE_N - 1) / G_TILE_N);
+  // split K while the tiles alone leave SMs idle, at least 4 K blocks each
+  int64_t nsplit = 1;
+  if (tiles < ctx->num_sms) nsplit = std::max<int64_t>(1, std::min<int64_t>((ctx->num_sms + tiles - 1) / tiles, nkb / 4));
+  const int kb_per = (int)((nkb + nsplit - 1) / nsplit);
+  nsplit = (nkb + kb_per - 1) / kb_per;
+  int tsh = 0;
+  while ((1 << tsh) < kb_per) ++tsh;
+  int* err = ctx->arena.alloc_n<int>(1);
+  LRA_CUDA(cudaMemsetAsync(err, 0, sizeof(int), ctx->stream));
+  TgParams P;
+  P.M = m;
+  P.N = n;
+  P.nkb = nkb;
+  P.kb_per = kb_per;
+  P.tshift = tsh;
+  P.ea = sa.colexp;
+  P.eb = sb.colexp;
+  P.alpha = alpha;
+  P.beta = beta;
+  P.err = err;
+  double* ws = nullptr;
+  if (nsplit > 1) {
+    ws = ctx->arena.alloc_n<double>((size_t)nsplit * m * n);
+    P.C = ws;
+    P.ldc = m;
+    P.to_ws = 1;
+  } else {
+    P.C = C;
+    P.ldc = ldc;
+    P.to_ws = 0;
+  }
+  const size_t smem = 1024 + (size_t)G_STAGE + 256;
+  LRA_CUDA(cudaFuncSetAttribute(tc_gemm_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  tc_gemm_kernel<<<dim3((unsigned)tiles, (unsigned)nsplit), NTHREADS, smem, ctx->stream>>>(tmA, tmB, P);
+  post_launch(ctx, "tc_gemm_kernel");
+  if (nsplit > 1) {
+    const unsigned g = nblk(ctx, m * n, 256);
+    tc_gemm_reduce_kernel<<<g, 256, 0, ctx->stream>>>(m, n, nsplit, ws, alpha, beta, C, ldc);
+    post_launch(ctx, "tc_gemm_reduce_kernel");
+  }
+  int herr = 0;
+  LRA_CUDA(cudaMemcpyAsync(&herr, err, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+  LRA_CUDA(cudaStreamSynchronize(ctx->stream));
+  ctx->arena.release(mk);
+  if (herr) fail(LRA_ETIMEDOUT, "tc_gemm: a bounded wait timed out");
+}
+
+template void tc_split<float>(lra_ctx*, char, int64_t, int64_t, const float*, int64_t, int, TcSplit*, bool);
+template void tc_split<double>(lra_ctx*, char, int64_t, int64_t, const double*, int64_t, int, TcSplit*, bool);
 template void tc_sketch<float>(lra_ctx*, const TcSplit&, int64_t, const float*, float*, int64_t);
 template void tc_sketch<double>(lra_ctx*, const TcSplit&, int64_t, const double*, double*, int64_t);
 

@@ -619,6 +619,34 @@ def cur(A, opts=None, **kwargs):
     return U.rows, U.cols
 
 
+def dgemm(transa: str, transb: str, A, B, alpha: float = 1.0, beta: float = 0.0, C_=None,
+          precision: str = "mixed", ctx: "Context | None" = None):
+    """C = alpha op(A) op(B) + beta C on CUDA Float64 tensors, as the
+    factorizations compute their GEMMs ("mixed": tensor-core split product;
+    "native": FP64 CUDA cores).  No counterpart in the reference."""
+    import torch
+    ctx = ctx or default_context()
+    MA, MB = _mat(A), _mat(B)
+    if MA.dtype != LRA_F64 or MB.dtype != LRA_F64 or not (_is_torch(A) and A.is_cuda and _is_torch(B) and B.is_cuda):
+        raise ArgumentError(_ffi.LRA_EINVAL, "dgemm takes CUDA Float64 tensors")
+    m = MA.n if transa == "t" else MA.m
+    k = MA.m if transa == "t" else MA.n
+    n = MB.m if transb == "t" else MB.n
+    if (MB.n if transb == "t" else MB.m) != k:
+        raise DimensionMismatch(_ffi.LRA_EDIM, "inner dimensions differ")
+    if C_ is None:
+        C_ = torch.zeros((n, m), dtype=torch.float64, device=A.device).t()
+        beta = 0.0
+    MC = _mat(C_)
+    if MC.keep is not C_:
+        raise ArgumentError(_ffi.LRA_EINVAL, "C must be a column-major CUDA tensor")
+    st = _ffi.load().lra_dgemm(ctx.handle, _ffi.PREC[precision], transa.encode(), transb.encode(), m, n, k,
+                               float(alpha), C.c_void_p(MA.ptr), MA.ld, C.c_void_p(MB.ptr), MB.ld, float(beta),
+                               C.c_void_p(MC.ptr), MC.ld)
+    _raise(st, ctx)
+    return C_
+
+
 def snorm(A, opts: LRAOptions | None = None, hermitian=None, **kwargs) -> float:
     """snorm(A[, opts]) (src/snorm.jl:14-45)."""
     trans, M, opts, ctx, rand = _args((A,) + ((opts,) if opts is not None else ()), kwargs)

@@ -103,3 +103,20 @@ def test_mixed_device_input(lra):
     V1 = lra.idfact(A, o, rand=lra.RandStream(gauss=g))
     V2 = lra.idfact(dev(A), o, rand=lra.RandStream(gauss=g))
     assert V1.k == V2.k and np.array_equal(V1.sk, V2.sk) and np.array_equal(V1.T, V2.T)
+
+
+@pytest.mark.parametrize("dt", [np.float32, np.float64])
+@pytest.mark.parametrize("M,order", [(4096, 72), (2048, 520), (1536, 136)])
+def test_srft_fft_path(lra, oracle, dt, M, order):
+    """SRFT through l'-point FFTs (l' a power of two: 64, 512, 128) against
+    the full-length FFT of the same signs and frequencies."""
+    rng = np.random.default_rng(M + order)
+    A = np.asfortranarray(rng.standard_normal((M, 300)).astype(dt))
+    g = rng.standard_normal(M + 10)
+    q = rng.integers(1, 2**62, order + 10, dtype=np.int64)
+    B = lra.sketch("left", "n", A, order, lra.LRAOptions(dt, sketch="srft"), rand=lra.RandStream(gauss=g, ints=q))
+    d = np.where(g[:M] > 0, 1.0, -1.0)
+    idx = (q[:order] - 1) % M + 1
+    R = oracle.srft_exact(A.astype(np.float64), d, idx, order)
+    tol = 1e-10 if dt == np.float64 else 2e-5
+    assert np.abs(B - R).max() <= tol * np.abs(R).max()
