@@ -1,5 +1,6 @@
 // Context runtime of liblra: errors, device workspace arena, launch hooks.
 
+#include <cstdlib>
 #include <cstdio>
 #include <cstring>
 
@@ -101,6 +102,14 @@ size_t Arena::capacity() const {
   size_t s = 0;
   for (auto& c : chunks_) s += c.cap;
   return s;
+}
+
+bool trace_on() {
+  static const bool on = [] {
+    const char* e = std::getenv("LRA_TRACE");
+    return e && *e && *e != '0';
+  }();
+  return on;
 }
 
 }  // namespace lra

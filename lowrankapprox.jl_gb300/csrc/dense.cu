@@ -10,6 +10,7 @@
 // pair), separated by bounded grid barriers.
 
 #include <algorithm>
+#include <cstdio>
 #include <cmath>
 
 #include "common.cuh"
@@ -173,7 +174,9 @@ constexpr int JP_RCH = 8;  // rows per thread per register chunk
 template <typename T, int NT>
 __global__ void __launch_bounds__(NT) jacobi_pair_kernel(JacParams<T> P) {
   constexpr int NW = NT / 32;
-  __shared__ T red[2][NW][3];
+  __shared__ T red[2][NT][3];
+  __shared__ T rot_c[2], rot_s[2];
+  __shared__ int rot_on[2];
   __shared__ int s_flag;
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
   const int64_t n = P.n;
@@ -214,37 +217,52 @@ __global__ void __launch_bounds__(NT) jacobi_pair_kernel(JacParams<T> P) {
             g = fma(u[c], w[c], g);
           }
         }
+        // partial dot products to shared memory; warp 0 alone reduces them
+        // and computes the rotation (FP64 instructions cost tens of cycles
+        // each here, so they are not repeated in every warp)
+        red[buf][threadIdx.x][0] = a;
+        red[buf][threadIdx.x][1] = b;
+        red[buf][threadIdx.x][2] = g;
+        __syncthreads();
+        if (wid == 0) {
+          T ra = 0, rb = 0, rg = 0;
 #pragma unroll
-        for (int o = 16; o > 0; o >>= 1) {
-          a += __shfl_xor_sync(0xffffffffu, a, o);
-          b += __shfl_xor_sync(0xffffffffu, b, o);
-          g += __shfl_xor_sync(0xffffffffu, g, o);
-        }
-        if (lane == 0) {
-          red[buf][wid][0] = a;
-          red[buf][wid][1] = b;
-          red[buf][wid][2] = g;
+          for (int k = 0; k < NW; ++k) {
+            ra += red[buf][lane + 32 * k][0];
+            rb += red[buf][lane + 32 * k][1];
+            rg += red[buf][lane + 32 * k][2];
+          }
+#pragma unroll
+          for (int o = 16; o > 0; o >>= 1) {
+            ra += __shfl_xor_sync(0xffffffffu, ra, o);
+            rb += __shfl_xor_sync(0xffffffffu, rb, o);
+            rg += __shfl_xor_sync(0xffffffffu, rg, o);
+          }
+          T cs = 1, sn = 0;
+          int rot = 0;
+          if (ra != 0 && rb != 0) {
+            const T g2 = rg * rg, ab = ra * rb;
+            if (g2 > tol2 * ab) {
+              rot = 1;
+              if (g2 > stop2 * ab) above = 1;
+              // t = tan of the rotation angle, the smaller root of t^2 + 2 zeta t - 1
+              const T d = rb - ra;
+              const T t = (T(2) * rg) / (d + copysign(sqrt(fma(d, d, T(4) * g2)), d));
+              cs = T(1) / sqrt(fma(t, t, T(1)));
+              sn = cs * t;
+            }
+          }
+          if (lane == 0) {
+            rot_c[buf] = cs;
+            rot_s[buf] = sn;
+            rot_on[buf] = rot;
+          }
         }
         __syncthreads();
-        a = red[buf][0][0];
-        b = red[buf][0][1];
-        g = red[buf][0][2];
-#pragma unroll
-        for (int k = 1; k < NW; ++k) {
-          a += red[buf][k][0];
-          b += red[buf][k][1];
-          g += red[buf][k][2];
-        }
+        const int on = rot_on[buf];
+        const T c = rot_c[buf], sn = rot_s[buf];
         buf ^= 1;  // the next pair reduces through the other buffer
-        if (a == 0 || b == 0) continue;
-        const T g2 = g * g, ab = a * b;
-        if (!(g2 > tol2 * ab)) continue;
-        if (g2 > stop2 * ab) above = 1;
-        // t = tan of the rotation angle, the smaller root of t^2 + 2 zeta t - 1
-        const T d = b - a;
-        const T t = (T(2) * g) / (d + copysign(sqrt(fma(d, d, T(4) * g2)), d));
-        const T c = T(1) / sqrt(fma(t, t, T(1)));
-        const T sn = c * t;
+        if (!on) continue;
         for (int64_t b0 = 0; b0 < n; b0 += (int64_t)NT * JP_RCH) {
           if (!one) {
 #pragma unroll
@@ -288,7 +306,8 @@ __global__ void __launch_bounds__(NT) jacobi_pair_kernel(JacParams<T> P) {
       }
       if (!grid_sync(P.bar)) return;
     }
-    // any CTA above the stopping level keeps the sweeps going
+    // any CTA above the stopping level keeps the sweeps going (warp 0 holds
+    // the flag of this CTA)
     if (threadIdx.x == 0) P.part[blockIdx.x] = above ? 1.0 : 0.0;
     if (!grid_sync(P.bar)) return;
     if (threadIdx.x == 0) {
@@ -319,6 +338,142 @@ __global__ void __launch_bounds__(NT) jacobi_pair_kernel(JacParams<T> P) {
   if (blockIdx.x == 0 && threadIdx.x == 0) *P.sweeps_out = sweep;
 }
 
+// Block one-sided Jacobi for the FP32 sweeps: the columns are grouped in
+// blocks of JB; each grid-wide round pairs the blocks round-robin, and the
+// CTA holding a block pair loads its 2 JB columns of X and V into shared
+// memory and rotates every pair among them there (2 JB - 1 local rounds of
+// JB pairs, a warp per pair) before writing them back.  A sweep then costs
+// about n / JB grid barriers instead of n, and the local rotations also
+// reach the pairs inside each block.
+constexpr int JB = 8;
+
+__device__ __forceinline__ void cp_async4(float* dst, const float* src) {
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 4;" ::"r"((uint32_t)__cvta_generic_to_shared(dst)), "l"(src)
+               : "memory");
+}
+
+__global__ void __launch_bounds__(JB * 32) jacobi_block_kernel(JacParams<float> P) {
+  extern __shared__ float jb_smem[];
+  __shared__ double red[32];
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  const int64_t n = P.n;
+  float* Xs = jb_smem;                       // [2 JB][n]
+  float* Vs = jb_smem + (size_t)2 * JB * n;  // [2 JB][n]
+  const int64_t nblk = (n + JB - 1) / JB;
+  const int64_t nbb = nblk + (nblk & 1);
+  const float tol = (float)P.tol;
+  int sweep = 0;
+  for (; sweep < P.max_sweeps; ++sweep) {
+    float off = 0;
+    for (int64_t r = 0; r < nbb - 1; ++r) {
+      for (int64_t s = blockIdx.x; s < nbb / 2; s += gridDim.x) {
+        int64_t b1, b2;
+        rr_pair(r, s, nbb, b1, b2);
+        // local column k < JB is column b1 JB + k, k >= JB is b2 JB + k - JB
+        auto gcol = [&](int k) -> int64_t {
+          const int64_t b = k < JB ? b1 : b2;
+          if (b >= nblk) return -1;
+          const int64_t j = b * JB + (k % JB);
+          return j < n ? j : -1;
+        };
+        // all 4 JB n elements in flight at once (asynchronous copies)
+        for (int k = 0; k < 2 * JB; ++k) {
+          const int64_t j = gcol(k);
+          for (int64_t i = threadIdx.x; i < n; i += JB * 32) {
+            if (j >= 0) {
+              cp_async4(Xs + k * n + i, P.X + i + j * P.ldx);
+              cp_async4(Vs + k * n + i, P.V + i + j * P.ldv);
+            } else {
+              Xs[k * n + i] = 0.0f;
+              Vs[k * n + i] = 0.0f;
+            }
+          }
+        }
+        asm volatile("cp.async.wait_all;" ::: "memory");
+        __syncthreads();
+        for (int lr = 0; lr < 2 * JB - 1; ++lr) {
+          int64_t p, q;
+          rr_pair(lr, wid, 2 * JB, p, q);
+          if (p > q) {
+            const int64_t t = p;
+            p = q;
+            q = t;
+          }
+          if (gcol((int)p) >= 0 && gcol((int)q) >= 0) {
+            float* xp = Xs + p * n;
+            float* xq = Xs + q * n;
+            float a = 0, b = 0, g = 0;
+            for (int64_t i = lane; i < n; i += 32) {
+              const float u = xp[i], w = xq[i];
+              a = fmaf(u, u, a);
+              b = fmaf(w, w, b);
+              g = fmaf(u, w, g);
+            }
+            a = warp_sum(a);
+            b = warp_sum(b);
+            g = warp_sum(g);
+            if (a != 0 && b != 0) {
+              const float rel = fabsf(g) / sqrtf(a * b);
+              if (rel > tol) {
+                off = fmaxf(off, rel);
+                const float zeta = (b - a) / (2.0f * g);
+                const float t = copysignf(1.0f, zeta) / (fabsf(zeta) + sqrtf(1.0f + zeta * zeta));
+                const float c = 1.0f / sqrtf(1.0f + t * t);
+                const float sn = c * t;
+                float* vp = Vs + p * n;
+                float* vq = Vs + q * n;
+                for (int64_t i = lane; i < n; i += 32) {
+                  const float u = xp[i], w = xq[i];
+                  xp[i] = c * u - sn * w;
+                  xq[i] = sn * u + c * w;
+                  const float vu = vp[i], vw = vq[i];
+                  vp[i] = c * vu - sn * vw;
+                  vq[i] = sn * vu + c * vw;
+                }
+              }
+            }
+          }
+          __syncthreads();
+        }
+        for (int k = 0; k < 2 * JB; ++k) {
+          const int64_t j = gcol(k);
+          if (j < 0) continue;
+          for (int64_t i = threadIdx.x; i < n; i += JB * 32) {
+            P.X[i + j * P.ldx] = Xs[k * n + i];
+            P.V[i + j * P.ldv] = Vs[k * n + i];
+          }
+        }
+        __syncthreads();
+      }
+      if (!grid_sync(P.bar)) return;
+    }
+    const double offd = block_max((double)off, red);
+    if (threadIdx.x == 0) P.part[blockIdx.x] = offd;
+    if (!grid_sync(P.bar)) return;
+    double mx = 0;
+    for (int b = threadIdx.x; b < gridDim.x; b += JB * 32) mx = fmax(mx, __ldcg(P.part + b));
+    mx = block_max(mx, red);
+    if (!grid_sync(P.bar)) return;
+    if (mx <= P.stop) {
+      ++sweep;
+      break;
+    }
+  }
+  // singular values = column norms, a warp per column
+  const int64_t gw = (int64_t)blockIdx.x * JB + wid, W = (int64_t)gridDim.x * JB;
+  for (int64_t j = gw; j < n; j += W) {
+    const float* x = P.X + j * P.ldx;
+    double acc = 0;
+    for (int64_t i = lane; i < n; i += 32) {
+      const double v = __ldcg(x + i);
+      acc = fma(v, v, acc);
+    }
+    acc = warp_sum(acc);
+    if (lane == 0) P.S[j] = (float)sqrt(acc);
+  }
+  if (blockIdx.x == 0 && threadIdx.x == 0) *P.sweeps_out = sweep;
+}
+
 template <typename T>
 __global__ void symcheck_kernel(int64_t n, const T* __restrict__ A, int64_t lda, int* bad) {
   const int64_t total = n * n;
@@ -335,18 +490,30 @@ __global__ void symcheck_kernel(int64_t n, const T* __restrict__ A, int64_t lda,
 
 template <typename T>
 void jacobi_svd(lra_ctx* ctx, int64_t n, T* X, int64_t ldx, T* V, int64_t ldv, T* S, bool quadratic_stop) {
-  // Float64: a CTA of 128 threads per pair; Float32: a warp per pair
+  // Float64: a CTA of 128 threads per pair; Float32: block Jacobi with the
+  // block pair in shared memory when it fits, else a warp per pair
   constexpr bool pair_cta = sizeof(T) == 8;
   constexpr int NT = 128;
   if (n <= 0) return;
   set_identity(ctx, n, n, V, ldv);
   const ArenaMark mk = ctx->arena.mark();
-  const void* kern = pair_cta ? (const void*)jacobi_pair_kernel<T, NT> : (const void*)jacobi_kernel<T, NT>;
+  const size_t blk_smem = (size_t)4 * JB * n * sizeof(float);
+  const bool block = !pair_cta && n >= 4 * JB && blk_smem <= 200 * 1024;
+  const void* kern = pair_cta ? (const void*)jacobi_pair_kernel<T, NT>
+                              : (block ? (const void*)jacobi_block_kernel : (const void*)jacobi_kernel<T, NT>);
+  const int nt = block ? JB * 32 : NT;
+  const size_t smem = block ? blk_smem : 0;
+  if (block) LRA_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
   int per_sm = 0;
-  LRA_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, NT, 0));
+  LRA_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, nt, smem));
   const int64_t pairs = (n + 1) / 2;
-  const int64_t per_cta = pair_cta ? 1 : NT / 32;
-  int grid = (int)std::min<int64_t>((pairs + per_cta - 1) / per_cta, (int64_t)ctx->num_sms);
+  int64_t units = pair_cta ? pairs : (pairs + NT / 32 - 1) / (NT / 32);
+  if (block) {
+    const int64_t nblk = (n + JB - 1) / JB;
+    units = (nblk + 1) / 2;
+  }
+  // the FP64 pairs all at once (up to two CTAs per SM), the rest one CTA per SM
+  int grid = (int)std::min<int64_t>(units, (int64_t)ctx->num_sms * (pair_cta ? 2 : 1));
   grid = std::max(1, std::min(grid, ctx->num_sms * std::max(per_sm, 1)));
   JacParams<T> P;
   P.n = n;
@@ -356,10 +523,9 @@ void jacobi_svd(lra_ctx* ctx, int64_t n, T* X, int64_t ldx, T* V, int64_t ldv, T
   P.ldv = ldv;
   P.S = S;
   P.tol = (double)Real<T>::eps * 2.0 * std::sqrt((double)n);
-  // Started from columns already orthogonal to about 1e-7 (the FP32 sweeps
-  // of jacobi_svd_fast), the FP64 sweeps converge quadratically: a sweep
-  // whose cosines were all below sqrt(tol)/10 leaves them near tol^2/100
-  // times a modest gap factor, so no further sweep is needed.
+  // A sweep whose cosines were all below sqrt(tol)/10 leaves them near
+  // tol^2/100 times a modest gap factor (quadratic convergence), so the
+  // sweep that would only confirm it is skipped.
   P.stop = quadratic_stop ? std::sqrt(P.tol) * 0.1 : P.tol;
   P.max_sweeps = 40;
   P.part = ctx->arena.alloc_n<double>(grid);
@@ -367,13 +533,19 @@ void jacobi_svd(lra_ctx* ctx, int64_t n, T* X, int64_t ldx, T* V, int64_t ldv, T
   P.sweeps_out = ctx->arena.alloc_n<int>(1);
   LRA_CUDA(cudaMemsetAsync(P.bar, 0, sizeof(GridBar), ctx->stream));
   void* args[] = {&P};
-  LRA_CUDA(cudaLaunchCooperativeKernel(kern, dim3(grid), dim3(NT), args, 0, ctx->stream));
-  post_launch(ctx, pair_cta ? "jacobi_pair_kernel" : "jacobi_kernel");
+  LRA_CUDA(cudaLaunchCooperativeKernel(kern, dim3(grid), dim3(nt), args, smem, ctx->stream));
+  post_launch(ctx, pair_cta ? "jacobi_pair_kernel" : (block ? "jacobi_block_kernel" : "jacobi_kernel"));
   GridBar hb;
+  int sweeps = 0;
   LRA_CUDA(cudaMemcpyAsync(&hb, P.bar, sizeof(GridBar), cudaMemcpyDeviceToHost, ctx->stream));
+  if (trace_on())
+    LRA_CUDA(cudaMemcpyAsync(&sweeps, P.sweeps_out, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
   LRA_CUDA(cudaStreamSynchronize(ctx->stream));
   ctx->arena.release(mk);
   if (hb.err != 0) fail(LRA_ETIMEDOUT, "jacobi: a grid barrier timed out");
+  if (trace_on())
+    std::fprintf(stderr, "[lra] jacobi %s%s n=%lld sweeps=%d grid=%d\n", sizeof(T) == 8 ? "f64" : "f32",
+                 block ? " block" : "", (long long)n, sweeps, grid);
 }
 
 template <typename T>
@@ -411,30 +583,38 @@ constexpr int CB = 32;  // diagonal block size
 
 // upper Cholesky of the jb x jb diagonal block in place (one CTA); sets *bad
 // when the block is not positive definite
+// Right-looking Cholesky of one jb x jb diagonal block in shared memory, as
+// LAPACK xPOTF2 orders it: R(c, c) = sqrt(.), row c scaled by 1 / R(c, c),
+// then the trailing block updated in parallel.
 template <typename T>
 __global__ void potrf_diag_kernel(int jb, T* G, int64_t ldg, int* bad) {
   __shared__ T a[CB][CB + 1];
+  __shared__ T s_inv;
   for (int t = threadIdx.x; t < jb * jb; t += blockDim.x) {
     const int i = t % jb, j = t / jb;
     a[i][j] = G[i + j * ldg];
   }
   __syncthreads();
   for (int c = 0; c < jb; ++c) {
-    // a[c][c] <- sqrt(a[c][c] - sum_{r<c} a[r][c]^2); a[c][j] <- (...)/a[c][c]
     if (threadIdx.x == 0) {
       T d = a[c][c];
-      for (int r = 0; r < c; ++r) d -= a[r][c] * a[r][c];
       if (!(d > T(0))) {
         atomicExch(bad, 1);
         d = T(1);
       }
-      a[c][c] = sqrt(d);
+      const T r = sqrt(d);
+      a[c][c] = r;
+      s_inv = T(1) / r;
     }
     __syncthreads();
-    for (int j = c + 1 + threadIdx.x; j < jb; j += blockDim.x) {
-      T s = a[c][j];
-      for (int r = 0; r < c; ++r) s -= a[r][c] * a[r][j];
-      a[c][j] = s / a[c][c];
+    const T inv = s_inv;
+    for (int j = c + 1 + threadIdx.x; j < jb; j += blockDim.x) a[c][j] *= inv;
+    __syncthreads();
+    // a[i][j] -= a[c][i] a[c][j] for c < i <= j < jb
+    const int w = jb - c - 1;
+    for (int t = threadIdx.x; t < w * w; t += blockDim.x) {
+      const int i = c + 1 + t % w, j = c + 1 + t / w;
+      if (i <= j) a[i][j] -= a[c][i] * a[c][j];
     }
     __syncthreads();
   }
@@ -448,10 +628,12 @@ __global__ void potrf_diag_kernel(int jb, T* G, int64_t ldg, int* bad) {
 template <typename T>
 __global__ void potrf_panel_kernel(int jb, int64_t nc, const T* Rbb, int64_t ldr, T* P, int64_t ldp) {
   __shared__ T r[CB][CB + 1];
+  __shared__ T rinv[CB];
   for (int t = threadIdx.x; t < jb * jb; t += blockDim.x) {
     const int i = t % jb, j = t / jb;
     r[i][j] = Rbb[i + j * ldr];
   }
+  if (threadIdx.x < jb) rinv[threadIdx.x] = T(1) / Rbb[threadIdx.x + threadIdx.x * ldr];
   __syncthreads();
   for (int64_t col = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; col < nc; col += (int64_t)gridDim.x * blockDim.x) {
     T* p = P + col * ldp;
@@ -466,7 +648,7 @@ __global__ void potrf_panel_kernel(int jb, int64_t nc, const T* Rbb, int64_t ldr
 #pragma unroll
         for (int q = 0; q < CB; ++q)
           if (q < i) s -= r[q][i] * x[q];
-        x[i] = s / r[i][i];
+        x[i] = s * rinv[i];
       }
     }
 #pragma unroll
@@ -479,10 +661,12 @@ __global__ void potrf_panel_kernel(int jb, int64_t nc, const T* Rbb, int64_t ldr
 template <typename T>
 __global__ void trsm_right_diag_kernel(int64_t m, int jb, const T* Rbb, int64_t ldr, T* X, int64_t ldx) {
   __shared__ T r[CB][CB + 1];
+  __shared__ T rinv[CB];
   for (int t = threadIdx.x; t < jb * jb; t += blockDim.x) {
     const int i = t % jb, j = t / jb;
     r[i][j] = Rbb[i + j * ldr];
   }
+  if (threadIdx.x < jb) rinv[threadIdx.x] = T(1) / Rbb[threadIdx.x + threadIdx.x * ldr];
   __syncthreads();
   for (int64_t row = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; row < m; row += (int64_t)gridDim.x * blockDim.x) {
     T x[CB];
@@ -497,7 +681,7 @@ __global__ void trsm_right_diag_kernel(int64_t m, int jb, const T* Rbb, int64_t 
 #pragma unroll
         for (int i = 0; i < CB; ++i)
           if (i < j) s -= x[i] * r[i][j];
-        x[j] = s / r[j][j];
+        x[j] = s * rinv[j];
       }
     }
 #pragma unroll
@@ -510,10 +694,12 @@ __global__ void trsm_right_diag_kernel(int64_t m, int jb, const T* Rbb, int64_t 
 template <typename T>
 __global__ void trsm_left_diag_kernel(int jb, int64_t nrhs, const T* Rbb, int64_t ldr, T* X, int64_t ldx) {
   __shared__ T r[CB][CB + 1];
+  __shared__ T rinv[CB];
   for (int t = threadIdx.x; t < jb * jb; t += blockDim.x) {
     const int i = t % jb, j = t / jb;
     r[i][j] = Rbb[i + j * ldr];
   }
+  if (threadIdx.x < jb) rinv[threadIdx.x] = T(1) / Rbb[threadIdx.x + threadIdx.x * ldr];
   __syncthreads();
   for (int64_t col = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; col < nrhs;
        col += (int64_t)gridDim.x * blockDim.x) {
@@ -530,7 +716,7 @@ __global__ void trsm_left_diag_kernel(int jb, int64_t nrhs, const T* Rbb, int64_
 #pragma unroll
         for (int q = CB - 1; q > i; --q)
           if (q < jb) s -= r[i][q] * x[q];
-        x[i] = s / r[i][i];
+        x[i] = s * rinv[i];
       }
     }
 #pragma unroll

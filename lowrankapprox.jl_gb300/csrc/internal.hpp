@@ -103,6 +103,10 @@ void tc_split(lra_ctx* ctx, char trans, int64_t M, int64_t N, const T* A, int64_
 template <typename T>
 void tc_sketch(lra_ctx* ctx, const TcSplit& sp, int64_t order, const T* S, T* B, int64_t ldb);
 
+// LRA_TRACE=1 in the environment: iteration counts of the iterative
+// kernels (Jacobi sweeps, pivots) on stderr.
+bool trace_on();
+
 // Keeps a stretch of work on the FP64 CUDA-core GEMM (products whose
 // result must be orthonormal to working precision).
 struct NativeGemmScope {

@@ -199,7 +199,7 @@ void jacobi_svd_fast(lra_ctx* ctx, int64_t n, T* X, int64_t ldx, T* V, int64_t l
   float* V32 = ctx->arena.alloc_n<float>((size_t)n * n);
   float* S32 = ctx->arena.alloc_n<float>(n);
   cast<T, float>(ctx, n, n, X, ldx, X32, n, scale);
-  jacobi_svd<float>(ctx, n, X32, n, V32, n, S32);
+  jacobi_svd<float>(ctx, n, X32, n, V32, n, S32, true);
   // 2. the rotation in FP64, re-orthonormalized: W = V32 chol(V32' V32)^{-1}
   T* W = ctx->arena.alloc_n<T>((size_t)n * n);
   T* G = ctx->arena.alloc_n<T>((size_t)n * n);

@@ -19,6 +19,7 @@
 #include <cooperative_groups.h>
 
 #include <algorithm>
+#include <cstring>
 #include <cmath>
 #include <mutex>
 
@@ -416,6 +417,7 @@ struct QrV2Extra {
   int64_t* piv;     // pivot c -> physical column
   int64_t* nfac;    // number of pivots performed
   long long* part_k;  // per-CTA pivot candidate keys
+  double* beta;     // R(c, c) of each pivot, for the rank test
 };
 
 // Column state lives in shared memory, one slot per column the CTA owns:
@@ -669,14 +671,12 @@ __global__ void __launch_bounds__(NT) geqp3_v2_kernel(QrParams<T> P, QrV2Extra X
         for (int64_t i = threadIdx.x; i < len; i += NT) vs[i] *= scal;
       }
       __syncthreads();
-      if (blockIdx.x == 0) {
-        if (tau != 0)
-          for (int64_t i = threadIdx.x; i < len; i += NT) pc[c + 1 + i] = vs[i];
-        if (threadIdx.x == 0) {
-          pc[c] = sh.beta;
-          P.tau[c] = tau;
-          X.piv[c] = pvt;
-        }
+      // the reflector goes back into column pvt only after the barrier that
+      // ends this step: other CTAs may still be reading the column until then
+      if (blockIdx.x == 0 && threadIdx.x == 0) {
+        P.tau[c] = tau;
+        X.piv[c] = pvt;
+        X.beta[c] = (double)sh.beta;
       }
       // ---- each warp: apply H(c) to its live columns, two at a time -----------
       auto dead = [&](int64_t t) {
@@ -793,8 +793,13 @@ __global__ void __launch_bounds__(NT) geqp3_v2_kernel(QrParams<T> P, QrV2Extra X
       if (myflag) atomicAdd(lst, 1);
       publish(bk, bi);
       if (!grid_sync(P.bar)) return;
+      if (blockIdx.x == 0) {
+        if (tau != 0)
+          for (int64_t i = threadIdx.x; i < len; i += NT) pc[c + 1 + i] = vs[i];
+        if (threadIdx.x == 0) pc[c] = sh.beta;
+      }
       stop_block = *((volatile int*)lst) != 0;
-      pvt = reduce_pivot_key();
+      pvt = reduce_pivot_key();  // its block reduction orders the writes above before vs is reloaded
       ++kk;
     }
     const int64_t kb = kk;
@@ -826,7 +831,7 @@ __global__ void __launch_bounds__(NT) geqp3_v2_kernel(QrParams<T> P, QrV2Extra X
     }
     // rank test of geqp3_adap_main! (src/pqr.jl:407-415): R(i, i) lives in
     // row i of the pivot column piv[i]
-    auto rdiag = [&](int64_t i) { return fabs((double)__ldcg(A + i + __ldcg(X.piv + i) * lda)); };
+    auto rdiag = [&](int64_t i) { return fabs(__ldcg(X.beta + i)); };
     if (rdiag(jn - 1) <= ptol) {
       bool found = false;
       for (int64_t i = j; i < jn; ++i) {
@@ -844,6 +849,531 @@ __global__ void __launch_bounds__(NT) geqp3_v2_kernel(QrParams<T> P, QrV2Extra X
   if (blockIdx.x == 0 && threadIdx.x == 0) {
     *P.k_out = kres;
     *X.nfac = nfac;
+  }
+}
+
+// ---- double-float variant for the mixed-precision path -----------------------------
+// The sketch is held as pairs of floats, x = h + l with |l| <= ulp(h) / 2
+// (48 significant bits, the resolution of the tensor-core sketch that
+// produced it), at one power-of-two scale for the whole matrix.  The dot
+// products and rank-1 updates, which dominate the factorization, run as
+// compensated FP32 arithmetic (error-free products by FMA, two-sum
+// accumulation) on the FP32 pipes, 64x wider than FP64 on this part; pivot
+// decisions, norm downdates and the reflector scalars stay in FP64.
+struct Df {
+  float h, l;
+};
+
+__device__ __forceinline__ double df_val(float h, float l) { return (double)h + (double)l; }
+
+__device__ __forceinline__ Df df_split(double x) {
+  const float h = (float)x;
+  return Df{h, (float)(x - (double)h)};
+}
+
+__device__ __forceinline__ void two_sum(float a, float b, float& s, float& e) {
+  s = a + b;
+  const float bb = s - a;
+  e = (a - (s - bb)) + (b - bb);
+}
+
+__device__ __forceinline__ Df quick_two_sum(float a, float b) {
+  const float s = a + b;
+  return Df{s, b - (s - a)};
+}
+
+__device__ __forceinline__ Df df_add(Df a, Df b) {
+  float s, e;
+  two_sum(a.h, b.h, s, e);
+  e += a.l + b.l;
+  return quick_two_sum(s, e);
+}
+
+__device__ __forceinline__ Df df_mul(Df a, Df b) {
+  const float p = a.h * b.h;
+  float e = fmaf(a.h, b.h, -p);
+  e = fmaf(a.h, b.l, fmaf(a.l, b.h, e));
+  return quick_two_sum(p, e);
+}
+
+// acc += v x, the high parts by two-sum, every lower-order term into acc.l
+__device__ __forceinline__ void df_fma_acc(Df& acc, float vh, float vl, float xh, float xl) {
+  const float p = vh * xh;
+  float pe = fmaf(vh, xh, -p);
+  pe = fmaf(vh, xl, fmaf(vl, xh, pe));
+  float s, e;
+  two_sum(acc.h, p, s, e);
+  acc.h = s;
+  acc.l += e + pe;
+}
+
+// y = x - f v
+__device__ __forceinline__ Df df_axpy_neg(float xh, float xl, Df f, float vh, float vl) {
+  const float p = f.h * vh;
+  float pe = fmaf(f.h, vh, -p);
+  pe = fmaf(f.h, vl, fmaf(f.l, vh, pe));
+  float s, e;
+  two_sum(xh, -p, s, e);
+  return quick_two_sum(s, (xl - pe) + e);
+}
+
+__device__ __forceinline__ Df df_shfl_xor(Df a, int o) {
+  return Df{__shfl_xor_sync(0xffffffffu, a.h, o), __shfl_xor_sync(0xffffffffu, a.l, o)};
+}
+
+struct QrDf {
+  float* Bh;            // high parts, ld = lda of the params
+  float* Bl;            // low parts
+  const double* vn0;    // initial column norms (scaled)
+  const double* scale;  // 2^-E: the factorization sees B * scale
+};
+
+template <int NT>
+__global__ void __launch_bounds__(NT) geqp3_df_kernel(QrParams<double> P, QrV2Extra X, QrDf D) {
+  __shared__ QrShared<double> sh;
+  __shared__ Df s_f;  // reflector scale / tau in df form
+  __shared__ Df s_tau;
+  extern __shared__ unsigned char qr_dyn[];
+  constexpr int NW = NT / 32;
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  const int64_t gw = (int64_t)blockIdx.x * NW + wid;
+  const int64_t W = (int64_t)gridDim.x * NW;
+  const int64_t m = P.m, n = P.n, lda = P.lda;
+  float* __restrict__ Bh = D.Bh;
+  float* __restrict__ Bl = D.Bl;
+  const double tol3z = sqrt(Real<double>::eps);
+  const int64_t lastrk = m < n ? m : n;
+  const int64_t ncol = gw < n ? (n - 1 - gw) / W + 1 : 0;
+  const int64_t ncmax = (n + W - 1) / W;
+  const int nslot = (int)(ncmax * NW);
+  float* vh = reinterpret_cast<float*>(qr_dyn);
+  float* vl = vh + P.vcap;
+  double* s_vn1 = reinterpret_cast<double*>(vl + P.vcap);
+  double* s_vn2 = s_vn1 + nslot;
+  double* s_arc = s_vn2 + nslot;
+  unsigned char* s_st = reinterpret_cast<unsigned char*>(s_arc + nslot);
+  auto slot_col = [&](int s) -> int64_t {
+    return (int64_t)blockIdx.x * NW + (s % NW) + (int64_t)(s / NW) * W;
+  };
+  auto reduce_pivot_key = [&]() -> int64_t {
+    long long k = -2;
+    int64_t i = INT64_MAX;
+    for (int b = threadIdx.x; b < gridDim.x; b += NT) key_merge(k, i, __ldcg(X.part_k + b), __ldcg(P.part_i + b));
+    return block_argmax_key(k, i, sh.sk, sh.si);
+  };
+  auto publish = [&](long long k, int64_t i) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      const long long k2 = __shfl_xor_sync(0xffffffffu, k, o);
+      const int64_t i2 = __shfl_xor_sync(0xffffffffu, i, o);
+      key_merge(k, i, k2, i2);
+    }
+    __syncthreads();
+    if (lane == 0) {
+      sh.sk[wid] = k;
+      sh.si[wid] = i;
+    }
+    __syncthreads();
+    if (wid == 0) {
+      long long k0 = lane < NW ? sh.sk[lane] : -2;
+      int64_t i0 = lane < NW ? sh.si[lane] : INT64_MAX;
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) {
+        const long long k2 = __shfl_xor_sync(0xffffffffu, k0, o);
+        const int64_t i2 = __shfl_xor_sync(0xffffffffu, i0, o);
+        key_merge(k0, i0, k2, i2);
+      }
+      if (lane == 0) {
+        X.part_k[blockIdx.x] = k0;
+        P.part_i[blockIdx.x] = i0;
+      }
+    }
+  };
+  // 2-norm of a column segment held as (h, l), by one warp, in FP64
+  auto warp_nrm2_df = [&](const float* h, const float* l, int64_t len) -> double {
+    double mx = 0;
+    for (int64_t i = lane; i < len; i += 32) mx = fmax(mx, fabs(df_val(__ldcg(h + i), __ldcg(l + i))));
+    mx = warp_max(mx);
+    if (mx == 0 || !isfinite(mx)) return mx;
+    const double sc = pow2_scale_inv(mx);
+    double acc = 0;
+    for (int64_t i = lane; i < len; i += 32) {
+      const double t = df_val(__ldcg(h + i), __ldcg(l + i)) * sc;
+      acc = fma(t, t, acc);
+    }
+    acc = warp_sum(acc);
+    return sqrt(acc) / sc;
+  };
+
+  // ---- initial column norms (precomputed), ptol, first pivot ---------------
+  for (int s = threadIdx.x; s < nslot; s += NT) {
+    const int64_t j = slot_col(s);
+    s_st[s] = j < n ? ST_LIVE : 0;
+    const double nr = (j < n && P.pivot) ? D.vn0[j] : 0.0;
+    s_vn1[s] = s_vn2[s] = nr;
+  }
+  __syncthreads();
+  double lmax = 0;
+  long long bk = -2;
+  int64_t bi = INT64_MAX;
+  for (int s = threadIdx.x; s < nslot; s += NT)
+    if (s_st[s] & ST_LIVE) {
+      lmax = fmax(lmax, s_vn1[s]);
+      key_merge(bk, bi, norm_key(s_vn1[s]), slot_col(s));
+    }
+  lmax = block_max(lmax, sh.red);
+  publish(bk, bi);
+  if (threadIdx.x == 0) P.part_d[blockIdx.x] = lmax;
+  if (!grid_sync(P.bar)) return;
+  double maxnrm = 0;
+  for (int b = threadIdx.x; b < gridDim.x; b += blockDim.x) maxnrm = fmax(maxnrm, __ldcg(P.part_d + b));
+  maxnrm = block_max(maxnrm, sh.red);
+  const double ptol = fmax(P.atol * *D.scale, P.rtol * maxnrm);
+  int64_t pvt = reduce_pivot_key();
+
+  int64_t kres = P.kmax, nfac = 0;
+  int64_t j = 0;
+  int par = 0;
+  while (j < P.kmax) {
+    const int64_t jb = min(P.nb, P.kmax - j);
+    int* lst = P.lsticc + par;
+    if (blockIdx.x == 0 && threadIdx.x == 0) P.lsticc[par ^ 1] = 0;
+    int64_t kk = 0;
+    bool stop_block = false;
+    while (kk < jb && !stop_block) {
+      const int64_t c = j + kk;
+      if (!P.pivot) pvt = c;
+      // ---- every CTA: the reflector of column pvt, rows c..m-1 ---------------
+      const int64_t len = m - c - 1;
+      const float* ph = Bh + pvt * lda;
+      const float* pl = Bl + pvt * lda;
+      for (int64_t i = threadIdx.x; i < len; i += NT) {
+        vh[i] = __ldcg(ph + c + 1 + i);
+        vl[i] = __ldcg(pl + c + 1 + i);
+      }
+      if (threadIdx.x == 0) sh.alpha = df_val(__ldcg(ph + c), __ldcg(pl + c));
+      __syncthreads();
+      if (wid == 0) {
+        double alpha = sh.alpha, tau = 0, beta = alpha, scal = 1;
+        int knt = 0;
+        if (len > 0) {
+          // sum of squares in double-float, then FP64
+          Df acc{0.f, 0.f};
+          for (int64_t i = lane; i < len; i += 32) df_fma_acc(acc, vh[i], vl[i], vh[i], vl[i]);
+#pragma unroll
+          for (int o = 16; o > 0; o >>= 1) acc = df_add(acc, df_shfl_xor(acc, o));
+          const double ssq = df_val(acc.h, acc.l);
+          double xnorm;
+          if (ssq > 1e-280 && ssq < 1e280) {
+            xnorm = sqrt(ssq);
+          } else {
+            double mx = 0;
+            for (int64_t i = lane; i < len; i += 32) mx = fmax(mx, fabs(df_val(vh[i], vl[i])));
+            mx = warp_max(mx);
+            xnorm = mx;
+            if (mx != 0 && isfinite(mx)) {
+              const double sc = pow2_scale_inv(mx);
+              double a2 = 0;
+              for (int64_t i = lane; i < len; i += 32) {
+                const double t = df_val(vh[i], vl[i]) * sc;
+                a2 = fma(t, t, a2);
+              }
+              xnorm = sqrt(warp_sum(a2)) / sc;
+            }
+          }
+          if (xnorm != 0) {
+            beta = -copysign(lapy2(alpha, xnorm), alpha);
+            const double safmin = Real<double>::safmin / Real<double>::eps;
+            // the matrix is scaled to max |B| in [1, 2): |beta| < safmin
+            // would need entries below 2^-1000, which the float pairs do not
+            // hold; xLARFG's rescaling loop is therefore not reached here
+            tau = (beta - alpha) / beta;
+            scal = 1.0 / (alpha - beta);
+            (void)safmin;
+          }
+        }
+        if (lane == 0) {
+          sh.tau = tau;
+          sh.beta = beta;
+          sh.scal = scal;
+          s_f = df_split(scal);
+          s_tau = df_split(tau);
+        }
+        (void)knt;
+      }
+      __syncthreads();
+      const double tau = sh.tau;
+      if (tau != 0) {
+        const Df sc = s_f;
+        for (int64_t i = threadIdx.x; i < len; i += NT) {
+          const Df y = df_mul(Df{vh[i], vl[i]}, sc);
+          vh[i] = y.h;
+          vl[i] = y.l;
+        }
+      }
+      __syncthreads();
+      // the reflector goes back into column pvt only after the barrier that
+      // ends this step: other CTAs may still be reading the column until then
+      if (blockIdx.x == 0 && threadIdx.x == 0) {
+        P.tau[c] = tau;
+        X.piv[c] = pvt;
+        X.beta[c] = sh.beta;
+      }
+      const Df tdf = s_tau;
+      // ---- each warp: apply H(c) to its live columns, two at a time -----------
+      auto dead = [&](int64_t t) {
+        return (s_st[t * NW + wid] & ST_DONE) || gw + t * W == pvt;
+      };
+      int64_t t = 0;
+      while (true) {
+        while (t < ncol && dead(t)) ++t;
+        if (t >= ncol) break;
+        const int64_t ta = t++;
+        while (t < ncol && dead(t)) ++t;
+        const bool two = t < ncol;
+        const int64_t tb = two ? t++ : ta;
+        const int64_t ja = gw + ta * W, jbb = gw + tb * W;
+        float* ah = Bh + ja * lda;
+        float* al = Bl + ja * lda;
+        float* bh = Bh + jbb * lda;
+        float* bl = Bl + jbb * lda;
+        const Df arca0{__ldcg(ah + c), __ldcg(al + c)};
+        const Df arcb0 = two ? Df{__ldcg(bh + c), __ldcg(bl + c)} : Df{0.f, 0.f};
+        Df sa{0.f, 0.f}, sb{0.f, 0.f};
+        float xah[QCH], xal[QCH], xbh[QCH], xbl[QCH];
+        const int64_t o = c + 1;
+        if (tau != 0) {
+          for (int64_t b0 = 0; b0 < len; b0 += 32 * QCH) {
+            const int64_t rem = len - b0;
+#pragma unroll
+            for (int q = 0; q < QCH; ++q) {
+              if (q % QG == 0 && 32 * q >= rem) break;
+              const int64_t i = b0 + lane + 32 * q;
+              const bool in = i < len;
+              xah[q] = in ? __ldcg(ah + o + i) : 0.f;
+              xal[q] = in ? __ldcg(al + o + i) : 0.f;
+              xbh[q] = (two && in) ? __ldcg(bh + o + i) : 0.f;
+              xbl[q] = (two && in) ? __ldcg(bl + o + i) : 0.f;
+            }
+#pragma unroll
+            for (int q = 0; q < QCH; ++q) {
+              if (q % QG == 0 && 32 * q >= rem) break;
+              const int64_t i = b0 + lane + 32 * q;
+              const float wh = i < len ? vh[i] : 0.f, wl = i < len ? vl[i] : 0.f;
+              df_fma_acc(sa, wh, wl, xah[q], xal[q]);
+              if (two) df_fma_acc(sb, wh, wl, xbh[q], xbl[q]);
+            }
+          }
+        }
+#pragma unroll
+        for (int off = 16; off > 0; off >>= 1) {
+          sa = df_add(sa, df_shfl_xor(sa, off));
+          sb = df_add(sb, df_shfl_xor(sb, off));
+        }
+        const Df fa = df_mul(tdf, df_add(arca0, sa));
+        const Df fb = two ? df_mul(tdf, df_add(arcb0, sb)) : Df{0.f, 0.f};
+        const bool ua = fa.h != 0.f, ub = two && fb.h != 0.f;
+        if (ua || ub) {
+          for (int64_t b0 = 0; b0 < len; b0 += 32 * QCH) {
+            const int64_t rem = len - b0;
+            if (len > 32 * QCH) {
+#pragma unroll
+              for (int q = 0; q < QCH; ++q) {
+                if (q % QG == 0 && 32 * q >= rem) break;
+                const int64_t i = b0 + lane + 32 * q;
+                const bool in = i < len;
+                xah[q] = in ? __ldcg(ah + o + i) : 0.f;
+                xal[q] = in ? __ldcg(al + o + i) : 0.f;
+                xbh[q] = (two && in) ? __ldcg(bh + o + i) : 0.f;
+                xbl[q] = (two && in) ? __ldcg(bl + o + i) : 0.f;
+              }
+            }
+#pragma unroll
+            for (int q = 0; q < QCH; ++q) {
+              if (q % QG == 0 && 32 * q >= rem) break;
+              const int64_t i = b0 + lane + 32 * q;
+              if (i < len) {
+                const float wh = vh[i], wl = vl[i];
+                if (ua) {
+                  const Df y = df_axpy_neg(xah[q], xal[q], fa, wh, wl);
+                  ah[o + i] = y.h;
+                  al[o + i] = y.l;
+                }
+                if (ub) {
+                  const Df y = df_axpy_neg(xbh[q], xbl[q], fb, wh, wl);
+                  bh[o + i] = y.h;
+                  bl[o + i] = y.l;
+                }
+              }
+            }
+          }
+        }
+        if (lane == 0) {
+          const Df arca = df_add(arca0, Df{-fa.h, -fa.l});
+          ah[c] = arca.h;
+          al[c] = arca.l;
+          s_arc[ta * NW + wid] = df_val(arca.h, arca.l);
+          if (two) {
+            const Df arcb = df_add(arcb0, Df{-fb.h, -fb.l});
+            bh[c] = arcb.h;
+            bl[c] = arcb.l;
+            s_arc[tb * NW + wid] = df_val(arcb.h, arcb.l);
+          }
+        }
+      }
+      __syncthreads();
+      // ---- a thread per slot: norm downdate and the pivot candidate -----------
+      bk = -2;
+      bi = INT64_MAX;
+      int myflag = 0;
+      for (int s = threadIdx.x; s < nslot; s += NT) {
+        const unsigned char st = s_st[s];
+        if (!(st & ST_LIVE) || (st & ST_DONE)) continue;
+        const int64_t jj = slot_col(s);
+        if (jj == pvt) {
+          s_st[s] = st | ST_DONE;
+          continue;
+        }
+        if (!P.pivot) continue;
+        double v1 = s_vn1[s];
+        if (c < lastrk - 1 && v1 != 0) {
+          double temp = fabs(s_arc[s]) / v1;
+          temp = fmax(0.0, (1.0 + temp) * (1.0 - temp));
+          const double r = v1 / s_vn2[s];
+          const double temp2 = temp * r * r;
+          if (temp2 <= tol3z) {
+            myflag = 1;
+            s_st[s] = st | ST_FLAG;
+          } else {
+            v1 = v1 * sqrt(temp);
+            s_vn1[s] = v1;
+          }
+        }
+        key_merge(bk, bi, norm_key(v1), jj);
+      }
+      if (myflag) atomicAdd(lst, 1);
+      publish(bk, bi);
+      if (!grid_sync(P.bar)) return;
+      if (blockIdx.x == 0) {
+        float* wh = Bh + pvt * lda;
+        float* wl = Bl + pvt * lda;
+        if (tau != 0)
+          for (int64_t i = threadIdx.x; i < len; i += NT) {
+            wh[c + 1 + i] = vh[i];
+            wl[c + 1 + i] = vl[i];
+          }
+        if (threadIdx.x == 0) {
+          const Df b = df_split(sh.beta);
+          wh[c] = b.h;
+          wl[c] = b.l;
+        }
+      }
+      stop_block = *((volatile int*)lst) != 0;
+      pvt = reduce_pivot_key();  // its block reduction orders the writes above before vs is reloaded
+      ++kk;
+    }
+    const int64_t kb = kk;
+    const int64_t jn = j + kb;
+    nfac = jn;
+    if (stop_block) {
+      for (int64_t t = 0; t < ncol; ++t) {
+        const int s = (int)(t * NW + wid);
+        if (!(s_st[s] & ST_FLAG) || (s_st[s] & ST_DONE)) continue;
+        const int64_t jj = gw + t * W;
+        const double v1 = warp_nrm2_df(Bh + jj * lda + jn, Bl + jj * lda + jn, m - jn);
+        __syncwarp();
+        if (lane == 0) {
+          s_vn1[s] = s_vn2[s] = v1;
+          s_st[s] = s_st[s] & (unsigned char)~ST_FLAG;
+        }
+      }
+      __syncthreads();
+      bk = -2;
+      bi = INT64_MAX;
+      for (int s = threadIdx.x; s < nslot; s += NT) {
+        const unsigned char st = s_st[s];
+        if (!(st & ST_LIVE) || (st & ST_DONE)) continue;
+        key_merge(bk, bi, norm_key(s_vn1[s]), slot_col(s));
+      }
+      publish(bk, bi);
+      if (!grid_sync(P.bar)) return;
+      pvt = reduce_pivot_key();
+    }
+    auto rdiag = [&](int64_t i) { return fabs(__ldcg(X.beta + i)); };
+    if (rdiag(jn - 1) <= ptol) {
+      bool found = false;
+      for (int64_t i = j; i < jn; ++i) {
+        if (rdiag(i) <= ptol) {
+          kres = i;
+          found = true;
+          break;
+        }
+      }
+      if (found) break;
+    }
+    j = jn;
+    par ^= 1;
+  }
+  if (blockIdx.x == 0 && threadIdx.x == 0) {
+    *P.k_out = kres;
+    *X.nfac = nfac;
+  }
+}
+
+// max |B| as the bit pattern of a nonnegative double
+__global__ void df_absmax_kernel(int64_t m, int64_t n, const double* __restrict__ B, int64_t ldb,
+                                 unsigned long long* __restrict__ out) {
+  double mx = 0;
+  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < m * n; t += (int64_t)gridDim.x * blockDim.x)
+    mx = fmax(mx, fabs(B[t % m + (t / m) * ldb]));
+  mx = warp_max(mx);
+  if ((threadIdx.x & 31) == 0 && mx > 0) atomicMax(out, (unsigned long long)__double_as_longlong(mx));
+}
+
+// scale = 2^-E with max |B| in [2^(E-1), 2^E)
+__global__ void df_scale_kernel(const unsigned long long* mx, double* scale) {
+  const double m = __longlong_as_double((long long)*mx);
+  *scale = m > 0 ? ldexp(1.0, -(ilogb(m) + 1)) : 1.0;
+}
+
+// (h, l) = split(B * scale); a warp per column also writes its norm
+__global__ void df_split_kernel(int64_t m, int64_t n, const double* __restrict__ B, int64_t ldb,
+                                const double* __restrict__ scale, float* __restrict__ Bh, float* __restrict__ Bl,
+                                int64_t ldh, double* __restrict__ vn0) {
+  const int lane = threadIdx.x & 31;
+  const int64_t w0 = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
+  const int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
+  const double sc = *scale;
+  for (int64_t j = w0; j < n; j += nw) {
+    double mx = 0;
+    for (int64_t i = lane; i < m; i += 32) {
+      const double x = B[i + j * ldb] * sc;
+      const Df d = df_split(x);
+      Bh[i + j * ldh] = d.h;
+      Bl[i + j * ldh] = d.l;
+      mx = fmax(mx, fabs(x));
+    }
+    mx = warp_max(mx);
+    double acc = 0;
+    if (mx > 0) {
+      const double s = pow2_scale_inv(mx);
+      for (int64_t i = lane; i < m; i += 32) {
+        const double t = df_val(Bh[i + j * ldh], Bl[i + j * ldh]) * s;
+        acc = fma(t, t, acc);
+      }
+      acc = sqrt(warp_sum(acc)) / s;
+    }
+    if (lane == 0) vn0[j] = acc;
+  }
+}
+
+// B = (h + l) / scale
+__global__ void df_join_kernel(int64_t m, int64_t n, const float* __restrict__ Bh, const float* __restrict__ Bl,
+                               int64_t ldh, const double* __restrict__ scale, double* __restrict__ B, int64_t ldb) {
+  const double inv = 1.0 / *scale;
+  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < m * n; t += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t i = t % m, j = t / m;
+    B[i + j * ldb] = df_val(Bh[i + j * ldh], Bl[i + j * ldh]) * inv;
   }
 }
 
@@ -981,15 +1511,50 @@ int64_t geqp3_adap(lra_ctx* ctx, int64_t m, int64_t n, T* A, int64_t lda, int64_
     X.piv = ctx->arena.alloc_n<int64_t>(std::max<int64_t>(P.kmax, 1));
     X.nfac = ctx->arena.alloc_n<int64_t>(1);
     X.part_k = ctx->arena.alloc_n<long long>(grid);
+    X.beta = ctx->arena.alloc_n<double>(std::max<int64_t>(P.kmax, 1));
     int64_t* col_at = ctx->arena.alloc_n<int64_t>(n);
     int64_t* pos = ctx->arena.alloc_n<int64_t>(n);
     const unsigned gi = (unsigned)std::max<int64_t>(1, std::min<int64_t>((n + 255) / 256, ctx->num_sms * 4));
     iota_kernel<<<gi, 256, 0, ctx->stream>>>(n, col_at, pos);
     post_launch(ctx, "iota_kernel");
-    void* args[] = {&P, &X};
-    LRA_CUDA(cudaLaunchCooperativeKernel((const void*)geqp3_v2_kernel<T, NT>, dim3(grid), dim3(NT), args,
-                                         smem2, ctx->stream));
-    post_launch(ctx, "geqp3_v2_kernel");
+    // the mixed-precision path factors Float64 sketches in double-float
+    const bool dfq = sizeof(T) == 8 && ctx->gemm_tc && pivot;
+    if (dfq) {
+      float* Bh = ctx->arena.alloc_n<float>((size_t)m * n);
+      float* Bl = ctx->arena.alloc_n<float>((size_t)m * n);
+      double* vn0 = ctx->arena.alloc_n<double>(n);
+      double* scale = ctx->arena.alloc_n<double>(1);
+      unsigned long long* mx = ctx->arena.alloc_n<unsigned long long>(1);
+      LRA_CUDA(cudaMemsetAsync(mx, 0, sizeof(unsigned long long), ctx->stream));
+      const double* Bd = reinterpret_cast<const double*>(A);
+      const unsigned gm = (unsigned)std::max<int64_t>(1, std::min<int64_t>((m * n + 255) / 256, ctx->num_sms * 8));
+      df_absmax_kernel<<<gm, 256, 0, ctx->stream>>>(m, n, Bd, lda, mx);
+      post_launch(ctx, "df_absmax_kernel");
+      df_scale_kernel<<<1, 1, 0, ctx->stream>>>(mx, scale);
+      post_launch(ctx, "df_scale_kernel");
+      const unsigned gs = (unsigned)std::max<int64_t>(1, std::min<int64_t>((n + 7) / 8, ctx->num_sms * 8));
+      df_split_kernel<<<gs, 256, 0, ctx->stream>>>(m, n, Bd, lda, scale, Bh, Bl, m, vn0);
+      post_launch(ctx, "df_split_kernel");
+      QrDf D{Bh, Bl, vn0, scale};
+      QrParams<double> Pd;
+      std::memcpy(&Pd, &P, sizeof(Pd));
+      Pd.lda = m;
+      LRA_CUDA(cudaFuncSetAttribute(geqp3_df_kernel<NT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem2));
+      int per_df = 0;
+      LRA_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_df, geqp3_df_kernel<NT>, NT, smem2));
+      if (per_df < 1) fail(LRA_ECUDA, "geqp3 kernel cannot be resident");
+      void* args[] = {&Pd, &X, &D};
+      LRA_CUDA(cudaLaunchCooperativeKernel((const void*)geqp3_df_kernel<NT>, dim3(grid), dim3(NT), args, smem2,
+                                           ctx->stream));
+      post_launch(ctx, "geqp3_df_kernel");
+      df_join_kernel<<<gm, 256, 0, ctx->stream>>>(m, n, Bh, Bl, m, scale, reinterpret_cast<double*>(A), lda);
+      post_launch(ctx, "df_join_kernel");
+    } else {
+      void* args[] = {&P, &X};
+      LRA_CUDA(cudaLaunchCooperativeKernel((const void*)geqp3_v2_kernel<T, NT>, dim3(grid), dim3(NT), args,
+                                           smem2, ctx->stream));
+      post_launch(ctx, "geqp3_v2_kernel");
+    }
     if (pivot) {
       // xLAQPS's swaps, replayed: jpvt and the column order of A
       geqp3_replay_kernel<<<1, 32, 0, ctx->stream>>>(n, X.piv, X.nfac, col_at, pos);

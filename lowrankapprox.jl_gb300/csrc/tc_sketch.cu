@@ -539,11 +539,13 @@ __global__ void sketch_t_kernel(int64_t L, int64_t K, const T* __restrict__ S, i
 // kept for s + t <= 7 (21 digit products; the dropped ones weigh below
 // 2^-46 of the leading term and, the digits being balanced, average to
 // zero).  The products of one diagonal d = s + t - 2 share a TMEM
-// accumulator whose 64-long K block sums stay below 2^23, so the FP32
-// accumulation is exact.  After every K block the six accumulators are
-// drained into one int64 per output,
+// accumulator; a digit product is at most 2^16 (2^15, 2^14 for the later
+// digits), so the sums of a diagonal over a 128-long K chunk stay within
+// 2^24 and the FP32 accumulation is exact.  After every chunk the six
+// accumulators are drained, through 32-bit conversions, into one int64
+// per output,
 //     X += sum_d acc_d 2^(8(5 - d) - t),   C = 2^(ea_i + eb_j - 56 + t) X,
-// with t = ceil(log2(K blocks)) keeping |X| below 2^63.
+// with t = ceil(log2(K chunks)) + 1 keeping |X| below 2^63.
 //
 // Same warp roles as the sketch kernel; one 144 KB stage (six 128 x 64 A
 // digit tiles, six 64 x 64 B digit tiles), so the loads of block k + 1
@@ -554,6 +556,7 @@ constexpr int G_A_BYTES = G_TILE_M * KBLK * 2;               // 16 KB
 constexpr int G_B_BYTES = G_TILE_N * KBLK * 2;               // 8 KB
 constexpr int G_STAGE = G_NS * (G_A_BYTES + G_B_BYTES);      // 144 KB
 constexpr int G_COLS = G_TILE_N / 2;                         // columns per drain thread
+constexpr int G_CHUNK = 2;                                   // K blocks per drain (128)
 
 struct TgParams {
   int64_t M, N;
@@ -627,8 +630,10 @@ __global__ void __launch_bounds__(NTHREADS, 1)
     if (lane == 0) {
       constexpr uint32_t idesc = idesc_bf16(G_TILE_M, G_TILE_N);
       for (int it = 0; it < nloc; ++it) {
-        if (it > 0) {
-          if (!mbar_wait(acc_free, (it - 1) & 1, P.err)) break;
+        const int ch = it / G_CHUNK;  // drain chunk
+        const bool first = (it % G_CHUNK) == 0;
+        if (first && ch > 0) {
+          if (!mbar_wait(acc_free, (ch - 1) & 1, P.err)) break;
           tc_fence_after();
         }
         if (!mbar_wait(full, it & 1, P.err)) break;
@@ -642,12 +647,12 @@ __global__ void __launch_bounds__(NTHREADS, 1)
               const uint64_t ad = sw128_desc(a0 + s * G_A_BYTES + k4 * 32);
               const uint64_t bd = sw128_desc(b0 + u * G_B_BYTES + k4 * 32);
               // each diagonal restarts with its (1, d + 1) product
-              mma_bf16(acc, ad, bd, idesc, (s == 0 && k4 == 0) ? 0u : 1u);
+              mma_bf16(acc, ad, bd, idesc, (first && s == 0 && k4 == 0) ? 0u : 1u);
             }
           }
         }
         mma_commit(empty);
-        mma_commit(acc_ready);
+        if ((it % G_CHUNK) == G_CHUNK - 1 || it == nloc - 1) mma_commit(acc_ready);
       }
       mma_commit(mma_done);
       int dummy = 0;
@@ -661,8 +666,9 @@ __global__ void __launch_bounds__(NTHREADS, 1)
 #pragma unroll
     for (int c = 0; c < G_COLS; ++c) X[c] = 0;
     bool ok = true;
-    for (int it = 0; it < nloc; ++it) {
-      if (!mbar_wait(acc_ready, it & 1, P.err)) {
+    const int nch = (nloc + G_CHUNK - 1) / G_CHUNK;
+    for (int ch = 0; ch < nch; ++ch) {
+      if (!mbar_wait(acc_ready, ch & 1, P.err)) {
         ok = false;
         break;
       }
@@ -672,13 +678,16 @@ __global__ void __launch_bounds__(NTHREADS, 1)
         uint32_t r[32];
         tmem_ld32(tmem + lane_base + (uint32_t)(d * G_TILE_N + half * G_COLS), r);
         const int w = 8 * (G_NS - 1 - d) - t;
+        // |acc| <= 2^24: exact through a 32-bit conversion
         if (w >= 0) {
 #pragma unroll
-          for (int c = 0; c < G_COLS; ++c) X[c] += __float2ll_rn(__uint_as_float(r[c])) << w;
+          for (int c = 0; c < G_COLS; ++c) X[c] += (long long)__float2int_rn(__uint_as_float(r[c])) << w;
         } else {
-          const float sc = __int_as_float((127 + w) << 23);  // 2^w
 #pragma unroll
-          for (int c = 0; c < G_COLS; ++c) X[c] += __float2ll_rn(__uint_as_float(r[c]) * sc);
+          for (int c = 0; c < G_COLS; ++c) {
+            const long long v = __float2int_rn(__uint_as_float(r[c]));
+            X[c] += (v + (1ll << (-w - 1))) >> (-w);  // round half up at weight 2^w
+          }
         }
       }
       tc_fence_before();
@@ -887,8 +896,10 @@ void tc_gemm(lra_ctx* ctx, char ta, char tb, int64_t m, int64_t n, int64_t k, do
   if (tiles < ctx->num_sms) nsplit = std::max<int64_t>(1, std::min<int64_t>((ctx->num_sms + tiles - 1) / tiles, nkb / 4));
   const int kb_per = (int)((nkb + nsplit - 1) / nsplit);
   nsplit = (nkb + kb_per - 1) / kb_per;
-  int tsh = 0;
-  while ((1 << tsh) < kb_per) ++tsh;
+  // |X| <= chunks * 2^(24 + 40 - t) (1 + 2^-7 + ...): t = ceil(log2(chunks)) + 1
+  const int chunks = (kb_per + G_CHUNK - 1) / G_CHUNK;
+  int tsh = 1;
+  while ((1 << (tsh - 1)) < chunks) ++tsh;
   int* err = ctx->arena.alloc_n<int>(1);
   LRA_CUDA(cudaMemsetAsync(err, 0, sizeof(int), ctx->stream));
   TgParams P;
