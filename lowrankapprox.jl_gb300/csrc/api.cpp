@@ -11,6 +11,9 @@
 #include <new>
 #include <numeric>
 #include <vector>
+#include <unordered_map>
+#include <map>
+#include <mutex>
 
 #include "internal.hpp"
 
@@ -53,10 +56,59 @@ void to_host(lra_ctx* ctx, void* dst, const T* src, size_t n) {
   LRA_CUDA(cudaMemcpyAsync(dst, src, n * sizeof(T), cudaMemcpyDeviceToHost, ctx->stream));
 }
 
+// Result arrays of 1 MiB and more live in page-locked host memory, so that
+// the device-to-host copies run at the link's speed (the driver stages a
+// pageable copy at a fraction of it: 19 vs 180 GB/s measured on a GB300
+// node).  Blocks freed through lra_*_free are kept for reuse, up to 2 GiB.
+std::mutex g_pin_mu;
+std::multimap<size_t, void*> g_pin_free;
+std::unordered_map<void*, size_t> g_pin_live;
+size_t g_pin_cached = 0;
+constexpr size_t kPinMin = (size_t)1 << 20;
+constexpr size_t kPinCacheCap = (size_t)2 << 30;
+
 void* hmalloc(size_t bytes) {
+  if (bytes >= kPinMin) {
+    std::lock_guard<std::mutex> lk(g_pin_mu);
+    auto it = g_pin_free.lower_bound(bytes);
+    if (it != g_pin_free.end() && it->first <= 2 * bytes) {
+      void* p = it->second;
+      const size_t sz = it->first;
+      g_pin_free.erase(it);
+      g_pin_cached -= sz;
+      g_pin_live[p] = sz;
+      return p;
+    }
+    void* p = nullptr;
+    if (cudaHostAlloc(&p, bytes, cudaHostAllocPortable) == cudaSuccess && p) {
+      g_pin_live[p] = bytes;
+      return p;
+    }
+    cudaGetLastError();  // no page-locked memory left: pageable below
+  }
   void* p = std::malloc(bytes ? bytes : 1);
   if (!p) fail(LRA_ENOMEM, "host allocation of %zu bytes", bytes);
   return p;
+}
+
+void hfree(void* p) {
+  if (!p) return;
+  {
+    std::lock_guard<std::mutex> lk(g_pin_mu);
+    auto it = g_pin_live.find(p);
+    if (it != g_pin_live.end()) {
+      const size_t sz = it->second;
+      g_pin_live.erase(it);
+      if (g_pin_cached + sz <= kPinCacheCap) {
+        g_pin_free.emplace(sz, p);
+        g_pin_cached += sz;
+      } else {
+        cudaFreeHost(p);
+      }
+      return;
+    }
+  }
+  std::free(p);
 }
 
 // ---- stage timing (CUDA events on the context stream) ----------------------
@@ -1215,8 +1267,8 @@ int lra_psvdfact(lra_ctx* ctx, int dtype, int64_t m, int64_t n, const void* A, i
         if (!vals_only) {
           void* U = host_transpose<T>(r->Vt, r->k, m);
           void* Vt = host_transpose<T>(r->U, n, r->k);
-          std::free(r->U);
-          std::free(r->Vt);
+          hfree(r->U);
+          hfree(r->Vt);
           r->U = U;
           r->Vt = Vt;
         }
@@ -1648,41 +1700,41 @@ int lra_idfact_batched(lra_ctx* ctx, int dtype, int64_t count, const lra_matdesc
 
 void lra_id_free(lra_id* r) {
   if (!r) return;
-  std::free(r->sk);
-  std::free(r->rd);
-  std::free(r->T);
-  std::free(r);
+  hfree(r->sk);
+  hfree(r->rd);
+  hfree(r->T);
+  hfree(r);
 }
 
 void lra_pqr_free(lra_pqr* r) {
   if (!r) return;
-  std::free(r->p);
-  std::free(r->Q);
-  std::free(r->R);
-  std::free(r->T);
-  std::free(r);
+  hfree(r->p);
+  hfree(r->Q);
+  hfree(r->R);
+  hfree(r->T);
+  hfree(r);
 }
 
 void lra_psvd_free(lra_psvd* r) {
   if (!r) return;
-  std::free(r->U);
-  std::free(r->S);
-  std::free(r->Vt);
-  std::free(r);
+  hfree(r->U);
+  hfree(r->S);
+  hfree(r->Vt);
+  hfree(r);
 }
 
 void lra_pheig_free(lra_pheig* r) {
   if (!r) return;
-  std::free(r->values);
-  std::free(r->vectors);
-  std::free(r);
+  hfree(r->values);
+  hfree(r->vectors);
+  hfree(r);
 }
 
 void lra_cur_free(lra_cur* r) {
   if (!r) return;
-  std::free(r->rows);
-  std::free(r->cols);
-  std::free(r);
+  hfree(r->rows);
+  hfree(r->cols);
+  hfree(r);
 }
 
 }  // extern "C"

@@ -346,6 +346,7 @@ __global__ void __launch_bounds__(NT) jacobi_pair_kernel(JacParams<T> P) {
 // about n / JB grid barriers instead of n, and the local rotations also
 // reach the pairs inside each block.
 constexpr int JB = 8;
+constexpr int JB_RPL = 16;  // rows per lane in registers (columns up to 512 long)
 
 __device__ __forceinline__ void cp_async4(float* dst, const float* src) {
   asm volatile("cp.async.ca.shared.global [%0], [%1], 4;" ::"r"((uint32_t)__cvta_generic_to_shared(dst)), "l"(src)
@@ -391,44 +392,103 @@ __global__ void __launch_bounds__(JB * 32) jacobi_block_kernel(JacParams<float> 
         }
         asm volatile("cp.async.wait_all;" ::: "memory");
         __syncthreads();
+        unsigned vmask = 0;  // local columns that exist
+#pragma unroll
+        for (int k = 0; k < 2 * JB; ++k) vmask |= (gcol(k) >= 0 ? 1u : 0u) << k;
+        const int ni = (int)n;
         for (int lr = 0; lr < 2 * JB - 1; ++lr) {
-          int64_t p, q;
-          rr_pair(lr, wid, 2 * JB, p, q);
+          // round-robin pair of this warp among the 2 JB local columns
+          auto lpos = [&](int i) { return i == 0 ? 0 : 1 + (i - 1 + lr) % (2 * JB - 1); };
+          int p = lpos(wid), q = lpos(2 * JB - 1 - wid);
           if (p > q) {
-            const int64_t t = p;
+            const int t = p;
             p = q;
             q = t;
           }
-          if (gcol((int)p) >= 0 && gcol((int)q) >= 0) {
-            float* xp = Xs + p * n;
-            float* xq = Xs + q * n;
+          if (((vmask >> p) & 1u) && ((vmask >> q) & 1u)) {
+            float* xp = Xs + p * ni;
+            float* xq = Xs + q * ni;
             float a = 0, b = 0, g = 0;
-            for (int64_t i = lane; i < n; i += 32) {
-              const float u = xp[i], w = xq[i];
-              a = fmaf(u, u, a);
-              b = fmaf(w, w, b);
-              g = fmaf(u, w, g);
-            }
-            a = warp_sum(a);
-            b = warp_sum(b);
-            g = warp_sum(g);
-            if (a != 0 && b != 0) {
-              const float rel = fabsf(g) / sqrtf(a * b);
-              if (rel > tol) {
-                off = fmaxf(off, rel);
-                const float zeta = (b - a) / (2.0f * g);
-                const float t = copysignf(1.0f, zeta) / (fabsf(zeta) + sqrtf(1.0f + zeta * zeta));
-                const float c = 1.0f / sqrtf(1.0f + t * t);
-                const float sn = c * t;
-                float* vp = Vs + p * n;
-                float* vq = Vs + q * n;
-                for (int64_t i = lane; i < n; i += 32) {
-                  const float u = xp[i], w = xq[i];
-                  xp[i] = c * u - sn * w;
-                  xq[i] = sn * u + c * w;
-                  const float vu = vp[i], vw = vq[i];
-                  vp[i] = c * vu - sn * vw;
-                  vq[i] = sn * vu + c * vw;
+            if (ni <= 32 * JB_RPL) {
+              // both columns in registers for the dots and the update
+              float u[JB_RPL], w[JB_RPL];
+#pragma unroll
+              for (int t = 0; t < JB_RPL; ++t) {
+                const int i = lane + 32 * t;
+                u[t] = i < ni ? xp[i] : 0.0f;
+                w[t] = i < ni ? xq[i] : 0.0f;
+              }
+#pragma unroll
+              for (int t = 0; t < JB_RPL; ++t) {
+                a = fmaf(u[t], u[t], a);
+                b = fmaf(w[t], w[t], b);
+                g = fmaf(u[t], w[t], g);
+              }
+              a = warp_sum(a);
+              b = warp_sum(b);
+              g = warp_sum(g);
+              if (a != 0 && b != 0) {
+                const float rel = fabsf(g) * rsqrtf(a * b);
+                if (rel > tol) {
+                  off = fmaxf(off, rel);
+                  const float zeta = (b - a) / (2.0f * g);
+                  const float t = copysignf(1.0f, zeta) / (fabsf(zeta) + sqrtf(1.0f + zeta * zeta));
+                  const float c = rsqrtf(1.0f + t * t);
+                  const float sn = c * t;
+#pragma unroll
+                  for (int tt = 0; tt < JB_RPL; ++tt) {
+                    const int i = lane + 32 * tt;
+                    if (i < ni) {
+                      xp[i] = c * u[tt] - sn * w[tt];
+                      xq[i] = sn * u[tt] + c * w[tt];
+                    }
+                  }
+                  float* vp = Vs + p * ni;
+                  float* vq = Vs + q * ni;
+#pragma unroll
+                  for (int tt = 0; tt < JB_RPL; ++tt) {
+                    const int i = lane + 32 * tt;
+                    u[tt] = i < ni ? vp[i] : 0.0f;
+                    w[tt] = i < ni ? vq[i] : 0.0f;
+                  }
+#pragma unroll
+                  for (int tt = 0; tt < JB_RPL; ++tt) {
+                    const int i = lane + 32 * tt;
+                    if (i < ni) {
+                      vp[i] = c * u[tt] - sn * w[tt];
+                      vq[i] = sn * u[tt] + c * w[tt];
+                    }
+                  }
+                }
+              }
+            } else {
+              for (int i = lane; i < ni; i += 32) {
+                const float u = xp[i], w = xq[i];
+                a = fmaf(u, u, a);
+                b = fmaf(w, w, b);
+                g = fmaf(u, w, g);
+              }
+              a = warp_sum(a);
+              b = warp_sum(b);
+              g = warp_sum(g);
+              if (a != 0 && b != 0) {
+                const float rel = fabsf(g) * rsqrtf(a * b);
+                if (rel > tol) {
+                  off = fmaxf(off, rel);
+                  const float zeta = (b - a) / (2.0f * g);
+                  const float t = copysignf(1.0f, zeta) / (fabsf(zeta) + sqrtf(1.0f + zeta * zeta));
+                  const float c = rsqrtf(1.0f + t * t);
+                  const float sn = c * t;
+                  float* vp = Vs + p * ni;
+                  float* vq = Vs + q * ni;
+                  for (int i = lane; i < ni; i += 32) {
+                    const float u = xp[i], w = xq[i];
+                    xp[i] = c * u - sn * w;
+                    xq[i] = sn * u + c * w;
+                    const float vu = vp[i], vw = vq[i];
+                    vp[i] = c * vu - sn * vw;
+                    vq[i] = sn * vu + c * vw;
+                  }
                 }
               }
             }

@@ -115,6 +115,12 @@ __device__ __forceinline__ double lattice(double g) {
   return r * (1.0 / 32.0);
 }
 
+// the same rounding in FP32 (exact: the lattice values are k / 32, |k| <= 127)
+__device__ __forceinline__ float lattice_f(float g) {
+  const float r = fminf(127.0f, fmaxf(-127.0f, rintf(g * 32.0f)));
+  return r * 0.03125f;
+}
+
 template <typename T>
 __global__ void from_stream_kernel(const double* __restrict__ g, int64_t n, T* __restrict__ out,
                                    int lat) {
@@ -149,14 +155,16 @@ __global__ void philox_kernel(uint64_t seed, uint64_t base, int64_t n, T* __rest
        t += (int64_t)gridDim.x * blockDim.x) {
     const uint64_t ctr = base + (uint64_t)t;
     U4 r = philox(U4{(unsigned)ctr, (unsigned)(ctr >> 32), 0x6c72u, 0x61u}, k0, k1);
-    // Box-Muller on two uniforms in (0, 1]
-    const double u1 = ((double)r.x + 1.0) * 2.3283064365386963e-10;
-    const double u2 = ((double)r.y + 0.5) * 2.3283064365386963e-10;
-    const double rad = sqrt(-2.0 * log(u1));
-    double s, c;
-    sincospi(2.0 * u2, &s, &c);
-    out[2 * t] = (T)lattice(rad * c);
-    if (2 * t + 1 < n) out[2 * t + 1] = (T)lattice(rad * s);
+    // Box-Muller on two uniforms in (0, 1], in FP32: the draws are rounded
+    // to the 1/32 lattice, far coarser than FP32's resolution, and FP64
+    // transcendentals are slow on this part
+    const float u1 = ((float)r.x + 1.0f) * 2.3283064365386963e-10f;
+    const float u2 = ((float)r.y + 0.5f) * 2.3283064365386963e-10f;
+    const float rad = sqrtf(-2.0f * logf(u1));
+    float s, c;
+    sincospif(2.0f * u2, &s, &c);
+    out[2 * t] = (T)lattice_f(rad * c);
+    if (2 * t + 1 < n) out[2 * t + 1] = (T)lattice_f(rad * s);
   }
 }
 
@@ -167,7 +175,12 @@ __global__ void finite_kernel(int64_t m, int64_t n, const T* __restrict__ A, int
   for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < total;
        t += (int64_t)gridDim.x * blockDim.x) {
     const int64_t i = t % m, j = t / m;
-    if (!isfinite(A[i + j * lda])) local = 1;
+    // an all-ones exponent field (Inf / NaN), tested on the bits
+    if constexpr (sizeof(T) == 8) {
+      if ((((unsigned long long)__double_as_longlong((double)A[i + j * lda]) >> 52) & 0x7FF) == 0x7FF) local = 1;
+    } else {
+      if (((__float_as_uint((float)A[i + j * lda]) >> 23) & 0xFF) == 0xFF) local = 1;
+    }
   }
   if (__syncthreads_or(local) && threadIdx.x == 0) atomicExch(bad, 1);
 }

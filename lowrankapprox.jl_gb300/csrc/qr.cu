@@ -928,11 +928,39 @@ struct QrDf {
   const double* scale;  // 2^-E: the factorization sees B * scale
 };
 
+__device__ __forceinline__ Df df_neg(Df a) { return Df{-a.h, -a.l}; }
+
+__device__ __forceinline__ Df df_div(Df a, Df b) {
+  const float q1 = a.h / b.h;
+  const Df r = df_add(a, df_neg(df_mul(Df{q1, 0.f}, b)));
+  const float q2 = r.h / b.h;
+  return quick_two_sum(q1, q2);
+}
+
+__device__ __forceinline__ Df df_sqrt(Df a) {
+  if (!(a.h > 0.f)) return Df{0.f, 0.f};
+  const float y = sqrtf(a.h);
+  const float p = y * y;
+  const float pe = fmaf(y, y, -p);
+  const float d = ((a.h - p) - pe) + a.l;
+  return quick_two_sum(y, d / (2.f * y));
+}
+
+// orderable key of a nonnegative double-float (h >= 0, |l| <= ulp(h) / 2):
+// h's bits, then l mapped to an unsigned order
+__device__ __forceinline__ long long df_key(Df a) {
+  if (a.h < 0.f) return -1;
+  const unsigned int lb = __float_as_uint(a.l);
+  const unsigned int lo = (lb & 0x80000000u) ? ~lb : (lb | 0x80000000u);
+  return (long long)(((unsigned long long)__float_as_uint(a.h) << 32) | lo);
+}
+
 template <int NT>
 __global__ void __launch_bounds__(NT) geqp3_df_kernel(QrParams<double> P, QrV2Extra X, QrDf D) {
   __shared__ QrShared<double> sh;
-  __shared__ Df s_f;  // reflector scale / tau in df form
+  __shared__ Df s_f;  // reflector scale / tau / beta in df form
   __shared__ Df s_tau;
+  __shared__ Df s_beta;
   extern __shared__ unsigned char qr_dyn[];
   constexpr int NW = NT / 32;
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
@@ -948,18 +976,30 @@ __global__ void __launch_bounds__(NT) geqp3_df_kernel(QrParams<double> P, QrV2Ex
   const int nslot = (int)(ncmax * NW);
   float* vh = reinterpret_cast<float*>(qr_dyn);
   float* vl = vh + P.vcap;
-  double* s_vn1 = reinterpret_cast<double*>(vl + P.vcap);
-  double* s_vn2 = s_vn1 + nslot;
-  double* s_arc = s_vn2 + nslot;
+  Df* s_vn1 = reinterpret_cast<Df*>(vl + P.vcap);
+  Df* s_vn2 = s_vn1 + nslot;
+  Df* s_arc = s_vn2 + nslot;
   unsigned char* s_st = reinterpret_cast<unsigned char*>(s_arc + nslot);
   auto slot_col = [&](int s) -> int64_t {
     return (int64_t)blockIdx.x * NW + (s % NW) + (int64_t)(s / NW) * W;
   };
+  // warp 0 alone reduces the per-CTA candidates; one block barrier
   auto reduce_pivot_key = [&]() -> int64_t {
-    long long k = -2;
-    int64_t i = INT64_MAX;
-    for (int b = threadIdx.x; b < gridDim.x; b += NT) key_merge(k, i, __ldcg(X.part_k + b), __ldcg(P.part_i + b));
-    return block_argmax_key(k, i, sh.sk, sh.si);
+    if (wid == 0) {
+      long long k = -2;
+      int64_t i = INT64_MAX;
+      for (int b = lane; b < gridDim.x; b += 32) key_merge(k, i, __ldcg(X.part_k + b), __ldcg(P.part_i + b));
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) {
+        const long long k2 = __shfl_xor_sync(0xffffffffu, k, o);
+        const int64_t i2 = __shfl_xor_sync(0xffffffffu, i, o);
+        key_merge(k, i, k2, i2);
+      }
+      if (lane == 0) sh.si[0] = i;
+    }
+    __syncthreads();
+    const int64_t r = sh.si[0];
+    return r;
   };
   auto publish = [&](long long k, int64_t i) {
 #pragma unroll
@@ -1009,7 +1049,7 @@ __global__ void __launch_bounds__(NT) geqp3_df_kernel(QrParams<double> P, QrV2Ex
   for (int s = threadIdx.x; s < nslot; s += NT) {
     const int64_t j = slot_col(s);
     s_st[s] = j < n ? ST_LIVE : 0;
-    const double nr = (j < n && P.pivot) ? D.vn0[j] : 0.0;
+    const Df nr = (j < n && P.pivot) ? df_split(D.vn0[j]) : Df{0.f, 0.f};
     s_vn1[s] = s_vn2[s] = nr;
   }
   __syncthreads();
@@ -1018,8 +1058,8 @@ __global__ void __launch_bounds__(NT) geqp3_df_kernel(QrParams<double> P, QrV2Ex
   int64_t bi = INT64_MAX;
   for (int s = threadIdx.x; s < nslot; s += NT)
     if (s_st[s] & ST_LIVE) {
-      lmax = fmax(lmax, s_vn1[s]);
-      key_merge(bk, bi, norm_key(s_vn1[s]), slot_col(s));
+      lmax = fmax(lmax, D.vn0[slot_col(s)]);
+      key_merge(bk, bi, df_key(s_vn1[s]), slot_col(s));
     }
   lmax = block_max(lmax, sh.red);
   publish(bk, bi);
@@ -1051,55 +1091,35 @@ __global__ void __launch_bounds__(NT) geqp3_df_kernel(QrParams<double> P, QrV2Ex
         vh[i] = __ldcg(ph + c + 1 + i);
         vl[i] = __ldcg(pl + c + 1 + i);
       }
-      if (threadIdx.x == 0) sh.alpha = df_val(__ldcg(ph + c), __ldcg(pl + c));
+      __shared__ Df s_alpha;
+      if (threadIdx.x == 0) s_alpha = Df{__ldcg(ph + c), __ldcg(pl + c)};
       __syncthreads();
       if (wid == 0) {
-        double alpha = sh.alpha, tau = 0, beta = alpha, scal = 1;
-        int knt = 0;
-        if (len > 0) {
-          // sum of squares in double-float, then FP64
-          Df acc{0.f, 0.f};
-          for (int64_t i = lane; i < len; i += 32) df_fma_acc(acc, vh[i], vl[i], vh[i], vl[i]);
+        // xLARFG in double-float: beta = -sign(alpha) sqrt(alpha^2 + |x|^2),
+        // tau = (beta - alpha) / beta, x <- x / (alpha - beta).  The matrix
+        // is scaled to max |B| < 1, so no intermediate overflows, and the
+        // rescaling loop of xLARFG (|beta| < safmin / eps, i.e. entries below
+        // 2^-970) cannot arise: a float pair holds nothing below 2^-149.
+        const Df alpha = s_alpha;
+        Df acc{0.f, 0.f};
+        for (int64_t i = lane; i < len; i += 32) df_fma_acc(acc, vh[i], vl[i], vh[i], vl[i]);
+        acc = quick_two_sum(acc.h, acc.l);
 #pragma unroll
-          for (int o = 16; o > 0; o >>= 1) acc = df_add(acc, df_shfl_xor(acc, o));
-          const double ssq = df_val(acc.h, acc.l);
-          double xnorm;
-          if (ssq > 1e-280 && ssq < 1e280) {
-            xnorm = sqrt(ssq);
-          } else {
-            double mx = 0;
-            for (int64_t i = lane; i < len; i += 32) mx = fmax(mx, fabs(df_val(vh[i], vl[i])));
-            mx = warp_max(mx);
-            xnorm = mx;
-            if (mx != 0 && isfinite(mx)) {
-              const double sc = pow2_scale_inv(mx);
-              double a2 = 0;
-              for (int64_t i = lane; i < len; i += 32) {
-                const double t = df_val(vh[i], vl[i]) * sc;
-                a2 = fma(t, t, a2);
-              }
-              xnorm = sqrt(warp_sum(a2)) / sc;
-            }
-          }
-          if (xnorm != 0) {
-            beta = -copysign(lapy2(alpha, xnorm), alpha);
-            const double safmin = Real<double>::safmin / Real<double>::eps;
-            // the matrix is scaled to max |B| in [1, 2): |beta| < safmin
-            // would need entries below 2^-1000, which the float pairs do not
-            // hold; xLARFG's rescaling loop is therefore not reached here
-            tau = (beta - alpha) / beta;
-            scal = 1.0 / (alpha - beta);
-            (void)safmin;
-          }
+        for (int o = 16; o > 0; o >>= 1) acc = df_add(acc, df_shfl_xor(acc, o));
+        Df tau{0.f, 0.f}, beta = alpha, scal{1.f, 0.f};
+        if (len > 0 && acc.h > 0.f) {
+          const Df r = df_sqrt(df_add(df_mul(alpha, alpha), acc));
+          beta = alpha.h >= 0.f ? df_neg(r) : r;
+          tau = df_div(df_add(beta, df_neg(alpha)), beta);
+          scal = df_div(Df{1.f, 0.f}, df_add(alpha, df_neg(beta)));
         }
         if (lane == 0) {
-          sh.tau = tau;
-          sh.beta = beta;
-          sh.scal = scal;
-          s_f = df_split(scal);
-          s_tau = df_split(tau);
+          sh.tau = df_val(tau.h, tau.l);
+          sh.beta = df_val(beta.h, beta.l);
+          s_f = scal;
+          s_tau = tau;
+          s_beta = beta;
         }
-        (void)knt;
       }
       __syncthreads();
       const double tau = sh.tau;
@@ -1212,12 +1232,12 @@ __global__ void __launch_bounds__(NT) geqp3_df_kernel(QrParams<double> P, QrV2Ex
           const Df arca = df_add(arca0, Df{-fa.h, -fa.l});
           ah[c] = arca.h;
           al[c] = arca.l;
-          s_arc[ta * NW + wid] = df_val(arca.h, arca.l);
+          s_arc[ta * NW + wid] = arca;
           if (two) {
             const Df arcb = df_add(arcb0, Df{-fb.h, -fb.l});
             bh[c] = arcb.h;
             bl[c] = arcb.l;
-            s_arc[tb * NW + wid] = df_val(arcb.h, arcb.l);
+            s_arc[tb * NW + wid] = arcb;
           }
         }
       }
@@ -1235,21 +1255,24 @@ __global__ void __launch_bounds__(NT) geqp3_df_kernel(QrParams<double> P, QrV2Ex
           continue;
         }
         if (!P.pivot) continue;
-        double v1 = s_vn1[s];
-        if (c < lastrk - 1 && v1 != 0) {
-          double temp = fabs(s_arc[s]) / v1;
-          temp = fmax(0.0, (1.0 + temp) * (1.0 - temp));
-          const double r = v1 / s_vn2[s];
-          const double temp2 = temp * r * r;
-          if (temp2 <= tol3z) {
+        Df v1 = s_vn1[s];
+        if (c < lastrk - 1 && v1.h != 0.f) {
+          // LAPACK's partial-norm downdate, in double-float
+          const Df a = s_arc[s];
+          Df temp = df_div(a.h < 0.f ? df_neg(a) : a, v1);
+          temp = df_mul(df_add(Df{1.f, 0.f}, temp), df_add(Df{1.f, 0.f}, df_neg(temp)));
+          if (temp.h < 0.f) temp = Df{0.f, 0.f};
+          const Df r = df_div(v1, s_vn2[s]);
+          const Df temp2 = df_mul(temp, df_mul(r, r));
+          if (temp2.h <= (float)tol3z) {
             myflag = 1;
             s_st[s] = st | ST_FLAG;
           } else {
-            v1 = v1 * sqrt(temp);
+            v1 = df_mul(v1, df_sqrt(temp));
             s_vn1[s] = v1;
           }
         }
-        key_merge(bk, bi, norm_key(v1), jj);
+        key_merge(bk, bi, df_key(v1), jj);
       }
       if (myflag) atomicAdd(lst, 1);
       publish(bk, bi);
@@ -1263,9 +1286,8 @@ __global__ void __launch_bounds__(NT) geqp3_df_kernel(QrParams<double> P, QrV2Ex
             wl[c + 1 + i] = vl[i];
           }
         if (threadIdx.x == 0) {
-          const Df b = df_split(sh.beta);
-          wh[c] = b.h;
-          wl[c] = b.l;
+          wh[c] = s_beta.h;
+          wl[c] = s_beta.l;
         }
       }
       stop_block = *((volatile int*)lst) != 0;
@@ -1280,7 +1302,7 @@ __global__ void __launch_bounds__(NT) geqp3_df_kernel(QrParams<double> P, QrV2Ex
         const int s = (int)(t * NW + wid);
         if (!(s_st[s] & ST_FLAG) || (s_st[s] & ST_DONE)) continue;
         const int64_t jj = gw + t * W;
-        const double v1 = warp_nrm2_df(Bh + jj * lda + jn, Bl + jj * lda + jn, m - jn);
+        const Df v1 = df_split(warp_nrm2_df(Bh + jj * lda + jn, Bl + jj * lda + jn, m - jn));
         __syncwarp();
         if (lane == 0) {
           s_vn1[s] = s_vn2[s] = v1;
@@ -1293,7 +1315,7 @@ __global__ void __launch_bounds__(NT) geqp3_df_kernel(QrParams<double> P, QrV2Ex
       for (int s = threadIdx.x; s < nslot; s += NT) {
         const unsigned char st = s_st[s];
         if (!(st & ST_LIVE) || (st & ST_DONE)) continue;
-        key_merge(bk, bi, norm_key(s_vn1[s]), slot_col(s));
+        key_merge(bk, bi, df_key(s_vn1[s]), slot_col(s));
       }
       publish(bk, bi);
       if (!grid_sync(P.bar)) return;

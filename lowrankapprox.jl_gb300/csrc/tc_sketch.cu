@@ -370,39 +370,63 @@ __device__ __forceinline__ int colexp_of(double mx) {
   return mx > 0 ? ilogb(mx) + 1 : 0;
 }
 
+// |x| as an orderable bit pattern (nonnegative floating-point numbers order
+// like their bits); NaN and Inf map to +Inf.  Integer operations only: the
+// FP64 pipe is narrow on this part.
+__device__ __forceinline__ unsigned long long abs_bits(double x) {
+  const unsigned long long b = (unsigned long long)__double_as_longlong(x) & 0x7FFFFFFFFFFFFFFFull;
+  return b >= 0x7FF0000000000000ull ? 0x7FF0000000000000ull : b;
+}
+__device__ __forceinline__ unsigned int abs_bits(float x) {
+  const unsigned int b = __float_as_uint(x) & 0x7FFFFFFFu;
+  return b >= 0x7F800000u ? 0x7F800000u : b;
+}
+__device__ __forceinline__ double bits_value(unsigned long long b) { return __longlong_as_double((long long)b); }
+__device__ __forceinline__ double bits_value(unsigned int b) { return (double)__uint_as_float(b); }
+template <typename K>
+__device__ __forceinline__ K warp_max_bits(K v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    const K w = __shfl_xor_sync(0xffffffffu, v, o);
+    v = w > v ? w : v;
+  }
+  return v;
+}
+
 template <typename T>
 __global__ void colexp_n_kernel(int64_t K, int64_t N, const T* __restrict__ A, int64_t lda, int* e) {
+  using Key = decltype(abs_bits(T(0)));
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
   const int nw = blockDim.x >> 5;
   for (int64_t j = (int64_t)blockIdx.x * nw + wid; j < N; j += (int64_t)gridDim.x * nw) {
-    double mx = 0;
+    Key mx = 0;
     for (int64_t i = lane; i < K; i += 32) {
-      const double a = fabs((double)A[i + j * lda]);
-      mx = a <= DBL_MAX ? fmax(mx, a) : INFINITY;  // NaN and Inf mark the column
+      const Key a = abs_bits(A[i + j * lda]);
+      mx = a > mx ? a : mx;
     }
-    mx = warp_max(mx);
-    if (lane == 0) e[j] = colexp_of(mx);
+    mx = warp_max_bits(mx);
+    if (lane == 0) e[j] = colexp_of(bits_value(mx));  // NaN and Inf mark the column
   }
 }
 
 // op(A) = A^T: column j of op(A) is row j of A.  Tiles of 32 rows of A x
 // 256 of its columns: coalesced partial maxima per row, merged with an
-// atomic max on the bit patterns (nonnegative doubles order like their
-// bits; NaN / Inf are entered as +Inf), then turned into exponents.
+// atomic max on the bit patterns of the doubles, then turned into exponents.
 template <typename T>
 __global__ void rowmax_kernel(int64_t K, int64_t N, const T* __restrict__ A, int64_t lda,
                               unsigned long long* __restrict__ mx) {
+  using Key = decltype(abs_bits(T(0)));
   const int64_t tn = (N + 31) / 32, tk = (K + 255) / 256;
   for (int64_t t = blockIdx.x; t < tn * tk; t += gridDim.x) {
     const int64_t j = (t % tn) * 32 + threadIdx.x;
     const int64_t i0 = (t / tn) * 256;
-    double m = 0;
+    Key m = 0;
     if (j < N)
       for (int64_t i = i0 + threadIdx.y; i < min(K, i0 + 256); i += blockDim.y) {
-        const double a = fabs((double)A[j + i * lda]);
-        m = a <= DBL_MAX ? fmax(m, a) : INFINITY;
+        const Key a = abs_bits(A[j + i * lda]);
+        m = a > m ? a : m;
       }
-    if (j < N && m > 0) atomicMax(mx + j, (unsigned long long)__double_as_longlong(m));
+    if (j < N && m > 0) atomicMax(mx + j, abs_bits(bits_value(m)));
   }
 }
 
