@@ -572,13 +572,16 @@ int guarded(lra_ctx* ctx, Fn&& fn) {
     ctx->arena.reset(ctx->stream);
     for (double& s : ctx->stage_ms) s = 0;
     ctx->gemm_tc = false;
+    ctx->mixed_rtol = 0;
     fn();
     ctx->gemm_tc = false;
+    ctx->mixed_rtol = 0;
     LRA_CUDA(cudaStreamSynchronize(ctx->stream));
     ctx->last_error.clear();
     return LRA_OK;
   } catch (const lra::Error& e) {
     ctx->gemm_tc = false;
+    ctx->mixed_rtol = 0;
     ctx->last_error = e.msg;
     cudaStreamSynchronize(ctx->stream);
     cudaGetLastError();
@@ -821,6 +824,7 @@ int lra_geqp3_adap_noalloc(lra_ctx* ctx, int dtype, int64_t m, int64_t n, void* 
     return LRA_OK;
   } catch (const lra::Error& e) {
     ctx->gemm_tc = false;
+    ctx->mixed_rtol = 0;
     ctx->last_error = e.msg;
     cudaStreamSynchronize(ctx->stream);
     cudaGetLastError();
@@ -855,6 +859,7 @@ int lra_idfact(lra_ctx* ctx, int dtype, char trans, int64_t m, int64_t n, const 
   return guarded(ctx, [&] {
     chkopts(opts);
     ctx->gemm_tc = use_tc_gemm(*opts, dtype);
+    ctx->mixed_rtol = ctx->gemm_tc ? opts->rtol : 0.0;
     check_dims(m, n);
     if (!out) fail(LRA_EINVAL, "out is NULL");
     const char t = chktrans(trans);
@@ -877,6 +882,7 @@ int lra_sketchfact(lra_ctx* ctx, int dtype, char side, char trans, int64_t m, in
   return guarded(ctx, [&] {
     chkopts(opts);
     ctx->gemm_tc = use_tc_gemm(*opts, dtype);
+    ctx->mixed_rtol = ctx->gemm_tc ? opts->rtol : 0.0;
     check_dims(m, n);
     if (!out) fail(LRA_EINVAL, "out is NULL");
     const char t = chktrans(trans);
@@ -935,6 +941,7 @@ int lra_pqrfact(lra_ctx* ctx, int dtype, char trans, int64_t m, int64_t n, const
   return guarded(ctx, [&] {
     chkopts(opts);
     ctx->gemm_tc = use_tc_gemm(*opts, dtype);
+    ctx->mixed_rtol = ctx->gemm_tc ? opts->rtol : 0.0;
     check_dims(m, n);
     if (!out) fail(LRA_EINVAL, "out is NULL");
     const char t = chktrans(trans);
@@ -1248,6 +1255,7 @@ int lra_psvdfact(lra_ctx* ctx, int dtype, int64_t m, int64_t n, const void* A, i
   return guarded(ctx, [&] {
     chkopts(opts);
     ctx->gemm_tc = use_tc_gemm(*opts, dtype);
+    ctx->mixed_rtol = ctx->gemm_tc ? opts->rtol : 0.0;
     check_dims(m, n);
     if (!out) fail(LRA_EINVAL, "out is NULL");
     dispatch(dtype, [&](auto z) {
@@ -1286,6 +1294,7 @@ int lra_pheigfact(lra_ctx* ctx, int dtype, int64_t n, const void* A, int64_t lda
   return guarded(ctx, [&] {
     chkopts(opts);
     ctx->gemm_tc = use_tc_gemm(*opts, dtype);
+    ctx->mixed_rtol = ctx->gemm_tc ? opts->rtol : 0.0;
     check_dims(n, n);
     if (!out) fail(LRA_EINVAL, "out is NULL");
     const lra_opts& o = *opts;
@@ -1437,6 +1446,7 @@ int lra_curfact(lra_ctx* ctx, int dtype, int64_t m, int64_t n, const void* A, in
   return guarded(ctx, [&] {
     chkopts(opts);
     ctx->gemm_tc = use_tc_gemm(*opts, dtype);
+    ctx->mixed_rtol = ctx->gemm_tc ? opts->rtol : 0.0;
     check_dims(m, n);
     if (!out) fail(LRA_EINVAL, "out is NULL");
     lra_opts o = *opts;

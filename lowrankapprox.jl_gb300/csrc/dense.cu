@@ -14,6 +14,7 @@
 #include <cmath>
 
 #include "common.cuh"
+#include "df64.cuh"
 #include "internal.hpp"
 
 namespace lra {
@@ -534,6 +535,227 @@ __global__ void __launch_bounds__(JB * 32) jacobi_block_kernel(JacParams<float> 
   if (blockIdx.x == 0 && threadIdx.x == 0) *P.sweeps_out = sweep;
 }
 
+// Double-float block Jacobi: the polish sweeps of the mixed-precision path,
+// the same block-pair schedule as jacobi_block_kernel with X and V held as
+// float pairs (df64.cuh) and every dot, rotation and update done in
+// double-float arithmetic on the FP32 pipes.  Columns are kept orthogonal
+// to about 1e-13, ample for the tolerances the mixed path accepts.
+struct JacDf {
+  int64_t n;
+  float* Xh;
+  float* Xl;
+  float* Vh;
+  float* Vl;  // all with leading dimension n
+  double* S;
+  double tol, stop;
+  int max_sweeps;
+  double* part;
+  GridBar* bar;
+  int* sweeps_out;
+};
+
+__device__ __forceinline__ bool df_gt(Df x, Df y) { return x.h > y.h || (x.h == y.h && x.l > y.l); }
+
+__device__ __forceinline__ Df df_rot_a(Df c, Df s, Df u, Df w) { return df_add(df_mul(c, u), df_neg(df_mul(s, w))); }
+__device__ __forceinline__ Df df_rot_b(Df c, Df s, Df u, Df w) { return df_add(df_mul(s, u), df_mul(c, w)); }
+
+__global__ void __launch_bounds__(JB * 32) jacobi_block_df_kernel(JacDf P) {
+  extern __shared__ float jd_smem[];
+  __shared__ int s_any;
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  const int ni = (int)P.n;
+  const size_t plane = (size_t)2 * JB * ni;
+  float* Xh = jd_smem;
+  float* Xl = Xh + plane;
+  float* Vh = Xl + plane;
+  float* Vl = Vh + plane;
+  const int nblk = (ni + JB - 1) / JB;
+  const int nbb = nblk + (nblk & 1);
+  const Df tol2 = df_split(P.tol * P.tol), stop2 = df_split(P.stop * P.stop);
+  int sweep = 0;
+  for (; sweep < P.max_sweeps; ++sweep) {
+    int above = 0;
+    for (int r = 0; r < nbb - 1; ++r) {
+      for (int s = blockIdx.x; s < nbb / 2; s += gridDim.x) {
+        auto bpos = [&](int i) { return i == 0 ? 0 : 1 + (i - 1 + r) % (nbb - 1); };
+        const int b1 = bpos(s), b2 = bpos(nbb - 1 - s);
+        auto gcol = [&](int k) -> int {
+          const int b = k < JB ? b1 : b2;
+          if (b >= nblk) return -1;
+          const int j = b * JB + (k % JB);
+          return j < ni ? j : -1;
+        };
+        for (int k = 0; k < 2 * JB; ++k) {
+          const int j = gcol(k);
+          for (int i = threadIdx.x; i < ni; i += JB * 32) {
+            const size_t o = (size_t)k * ni + i;
+            if (j >= 0) {
+              const size_t g = (size_t)j * ni + i;
+              cp_async4(Xh + o, P.Xh + g);
+              cp_async4(Xl + o, P.Xl + g);
+              cp_async4(Vh + o, P.Vh + g);
+              cp_async4(Vl + o, P.Vl + g);
+            } else {
+              Xh[o] = Xl[o] = Vh[o] = Vl[o] = 0.0f;
+            }
+          }
+        }
+        asm volatile("cp.async.wait_all;" ::: "memory");
+        __syncthreads();
+        unsigned vmask = 0;
+#pragma unroll
+        for (int k = 0; k < 2 * JB; ++k) vmask |= (gcol(k) >= 0 ? 1u : 0u) << k;
+        for (int lr = 0; lr < 2 * JB - 1; ++lr) {
+          auto lpos = [&](int i) { return i == 0 ? 0 : 1 + (i - 1 + lr) % (2 * JB - 1); };
+          int p = lpos(wid), q = lpos(2 * JB - 1 - wid);
+          if (p > q) {
+            const int t = p;
+            p = q;
+            q = t;
+          }
+          if (((vmask >> p) & 1u) && ((vmask >> q) & 1u)) {
+            float* xph = Xh + p * ni;
+            float* xpl = Xl + p * ni;
+            float* xqh = Xh + q * ni;
+            float* xql = Xl + q * ni;
+            Df u[JB_RPL], w[JB_RPL];
+            Df a{0.f, 0.f}, b{0.f, 0.f}, g{0.f, 0.f};
+#pragma unroll
+            for (int t = 0; t < JB_RPL; ++t) {
+              const int i = lane + 32 * t;
+              u[t] = i < ni ? Df{xph[i], xpl[i]} : Df{0.f, 0.f};
+              w[t] = i < ni ? Df{xqh[i], xql[i]} : Df{0.f, 0.f};
+            }
+#pragma unroll
+            for (int t = 0; t < JB_RPL; ++t) {
+              df_fma_acc(a, u[t].h, u[t].l, u[t].h, u[t].l);
+              df_fma_acc(b, w[t].h, w[t].l, w[t].h, w[t].l);
+              df_fma_acc(g, u[t].h, u[t].l, w[t].h, w[t].l);
+            }
+            a = quick_two_sum(a.h, a.l);
+            b = quick_two_sum(b.h, b.l);
+            g = quick_two_sum(g.h, g.l);
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) {
+              a = df_add(a, df_shfl_xor(a, o));
+              b = df_add(b, df_shfl_xor(b, o));
+              g = df_add(g, df_shfl_xor(g, o));
+            }
+            if (a.h != 0.f && b.h != 0.f) {
+              const Df g2 = df_mul(g, g), ab = df_mul(a, b);
+              if (df_gt(g2, df_mul(tol2, ab))) {
+                if (df_gt(g2, df_mul(stop2, ab))) above = 1;
+                // t = tan of the rotation angle, the smaller root of t^2 + 2 zeta t - 1
+                const Df d = df_add(b, df_neg(a));
+                const Df rt = df_sqrt(df_add(df_mul(d, d), df_mul(Df{4.f, 0.f}, g2)));
+                const Df den = df_add(d, d.h >= 0.f ? rt : df_neg(rt));
+                const Df t = df_div(df_mul(Df{2.f, 0.f}, g), den);
+                const Df c = df_div(Df{1.f, 0.f}, df_sqrt(df_add(Df{1.f, 0.f}, df_mul(t, t))));
+                const Df sn = df_mul(c, t);
+#pragma unroll
+                for (int tt = 0; tt < JB_RPL; ++tt) {
+                  const int i = lane + 32 * tt;
+                  if (i < ni) {
+                    const Df x1 = df_rot_a(c, sn, u[tt], w[tt]), x2 = df_rot_b(c, sn, u[tt], w[tt]);
+                    xph[i] = x1.h;
+                    xpl[i] = x1.l;
+                    xqh[i] = x2.h;
+                    xql[i] = x2.l;
+                  }
+                }
+                float* vph = Vh + p * ni;
+                float* vpl = Vl + p * ni;
+                float* vqh = Vh + q * ni;
+                float* vql = Vl + q * ni;
+#pragma unroll
+                for (int tt = 0; tt < JB_RPL; ++tt) {
+                  const int i = lane + 32 * tt;
+                  u[tt] = i < ni ? Df{vph[i], vpl[i]} : Df{0.f, 0.f};
+                  w[tt] = i < ni ? Df{vqh[i], vql[i]} : Df{0.f, 0.f};
+                }
+#pragma unroll
+                for (int tt = 0; tt < JB_RPL; ++tt) {
+                  const int i = lane + 32 * tt;
+                  if (i < ni) {
+                    const Df v1 = df_rot_a(c, sn, u[tt], w[tt]), v2 = df_rot_b(c, sn, u[tt], w[tt]);
+                    vph[i] = v1.h;
+                    vpl[i] = v1.l;
+                    vqh[i] = v2.h;
+                    vql[i] = v2.l;
+                  }
+                }
+              }
+            }
+          }
+          __syncthreads();
+        }
+        for (int k = 0; k < 2 * JB; ++k) {
+          const int j = gcol(k);
+          if (j < 0) continue;
+          for (int i = threadIdx.x; i < ni; i += JB * 32) {
+            const size_t o = (size_t)k * ni + i, g = (size_t)j * ni + i;
+            P.Xh[g] = Xh[o];
+            P.Xl[g] = Xl[o];
+            P.Vh[g] = Vh[o];
+            P.Vl[g] = Vl[o];
+          }
+        }
+        __syncthreads();
+      }
+      if (!grid_sync(P.bar)) return;
+    }
+    // any rotation above the stopping level, over the grid
+    above = __syncthreads_or(above);
+    if (threadIdx.x == 0) P.part[blockIdx.x] = above ? 1.0 : 0.0;
+    if (!grid_sync(P.bar)) return;
+    if (threadIdx.x == 0) {
+      int any = 0;
+      for (int k = 0; k < (int)gridDim.x; ++k) any |= __ldcg(P.part + k) != 0.0;
+      s_any = any;
+    }
+    __syncthreads();
+    const int any = s_any;
+    if (!grid_sync(P.bar)) return;
+    if (!any) {
+      ++sweep;
+      break;
+    }
+  }
+  // singular values = column norms, a warp per column
+  const int gw = blockIdx.x * JB + wid, W = gridDim.x * JB;
+  for (int j = gw; j < ni; j += W) {
+    Df acc{0.f, 0.f};
+    for (int i = lane; i < ni; i += 32) {
+      const float h = __ldcg(P.Xh + (size_t)j * ni + i), l = __ldcg(P.Xl + (size_t)j * ni + i);
+      df_fma_acc(acc, h, l, h, l);
+    }
+    acc = quick_two_sum(acc.h, acc.l);
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) acc = df_add(acc, df_shfl_xor(acc, o));
+    if (lane == 0) P.S[j] = sqrt(df_val(acc.h, acc.l));
+  }
+  if (blockIdx.x == 0 && threadIdx.x == 0) *P.sweeps_out = sweep;
+}
+
+__global__ void df_from_double_kernel(int64_t m, int64_t n, const double* __restrict__ A, int64_t lda,
+                                      float* __restrict__ H, float* __restrict__ L, int identity) {
+  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < m * n; t += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t i = t % m, j = t / m;
+    const double x = identity ? (i == j ? 1.0 : 0.0) : A[i + j * lda];
+    const Df d = df_split(x);
+    H[t] = d.h;
+    L[t] = d.l;
+  }
+}
+
+__global__ void df_to_double_kernel(int64_t m, int64_t n, const float* __restrict__ H, const float* __restrict__ L,
+                                    double* __restrict__ A, int64_t lda) {
+  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < m * n; t += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t i = t % m, j = t / m;
+    A[i + j * lda] = df_val(H[t], L[t]);
+  }
+}
+
 template <typename T>
 __global__ void symcheck_kernel(int64_t n, const T* __restrict__ A, int64_t lda, int* bad) {
   const int64_t total = n * n;
@@ -606,6 +828,58 @@ void jacobi_svd(lra_ctx* ctx, int64_t n, T* X, int64_t ldx, T* V, int64_t ldv, T
   if (trace_on())
     std::fprintf(stderr, "[lra] jacobi %s%s n=%lld sweeps=%d grid=%d\n", sizeof(T) == 8 ? "f64" : "f32",
                  block ? " block" : "", (long long)n, sweeps, grid);
+}
+
+bool jacobi_svd_df(lra_ctx* ctx, int64_t n, double* X, int64_t ldx, double* V, int64_t ldv, double* S) {
+  if (n < 2 || n > 32 * JB_RPL) return false;
+  const size_t smem = (size_t)8 * JB * n * sizeof(float);
+  if (smem > 200 * 1024) return false;
+  LRA_CUDA(cudaFuncSetAttribute(jacobi_block_df_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  int per_sm = 0;
+  LRA_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, jacobi_block_df_kernel, JB * 32, smem));
+  if (per_sm < 1) return false;
+  const ArenaMark mk = ctx->arena.mark();
+  const int64_t nblk = (n + JB - 1) / JB;
+  const int grid = (int)std::max<int64_t>(1, std::min<int64_t>((nblk + 1) / 2, (int64_t)ctx->num_sms * per_sm));
+  JacDf P;
+  P.n = n;
+  P.Xh = ctx->arena.alloc_n<float>((size_t)n * n);
+  P.Xl = ctx->arena.alloc_n<float>((size_t)n * n);
+  P.Vh = ctx->arena.alloc_n<float>((size_t)n * n);
+  P.Vl = ctx->arena.alloc_n<float>((size_t)n * n);
+  P.S = S;
+  // double-float resolves cosines down to a few units of 2^-46 sqrt(n)
+  P.tol = std::max((double)Real<double>::eps * 2.0 * std::sqrt((double)n), 8.0 * std::ldexp(1.0, -46) * std::sqrt((double)n));
+  P.stop = std::sqrt(P.tol) * 0.1;  // quadratic convergence from the FP32 sweeps
+  P.max_sweeps = 40;
+  P.part = ctx->arena.alloc_n<double>(grid);
+  P.bar = reinterpret_cast<GridBar*>(ctx->arena.alloc(sizeof(GridBar)));
+  P.sweeps_out = ctx->arena.alloc_n<int>(1);
+  LRA_CUDA(cudaMemsetAsync(P.bar, 0, sizeof(GridBar), ctx->stream));
+  const unsigned g = (unsigned)std::max<int64_t>(1, std::min<int64_t>((n * n + 255) / 256, ctx->num_sms * 8));
+  df_from_double_kernel<<<g, 256, 0, ctx->stream>>>(n, n, X, ldx, P.Xh, P.Xl, 0);
+  post_launch(ctx, "df_from_double_kernel");
+  df_from_double_kernel<<<g, 256, 0, ctx->stream>>>(n, n, nullptr, n, P.Vh, P.Vl, 1);
+  post_launch(ctx, "df_from_double_kernel");
+  void* args[] = {&P};
+  LRA_CUDA(cudaLaunchCooperativeKernel((const void*)jacobi_block_df_kernel, dim3(grid), dim3(JB * 32), args, smem,
+                                       ctx->stream));
+  post_launch(ctx, "jacobi_block_df_kernel");
+  df_to_double_kernel<<<g, 256, 0, ctx->stream>>>(n, n, P.Xh, P.Xl, X, ldx);
+  post_launch(ctx, "df_to_double_kernel");
+  df_to_double_kernel<<<g, 256, 0, ctx->stream>>>(n, n, P.Vh, P.Vl, V, ldv);
+  post_launch(ctx, "df_to_double_kernel");
+  GridBar hb;
+  int sweeps = 0;
+  LRA_CUDA(cudaMemcpyAsync(&hb, P.bar, sizeof(GridBar), cudaMemcpyDeviceToHost, ctx->stream));
+  if (trace_on())
+    LRA_CUDA(cudaMemcpyAsync(&sweeps, P.sweeps_out, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+  LRA_CUDA(cudaStreamSynchronize(ctx->stream));
+  ctx->arena.release(mk);
+  if (hb.err != 0) fail(LRA_ETIMEDOUT, "jacobi: a grid barrier timed out");
+  if (trace_on())
+    std::fprintf(stderr, "[lra] jacobi df block n=%lld sweeps=%d grid=%d\n", (long long)n, sweeps, grid);
+  return true;
 }
 
 template <typename T>
@@ -681,6 +955,101 @@ __global__ void potrf_diag_kernel(int jb, T* G, int64_t ldg, int* bad) {
   for (int t = threadIdx.x; t < jb * jb; t += blockDim.x) {
     const int i = t % jb, j = t / jb;
     G[i + j * ldg] = i <= j ? a[i][j] : T(0);
+  }
+}
+
+// The whole blocked right-looking Cholesky in one cooperative launch: for
+// each 32-wide diagonal block, CTA 0 factors the block in shared memory (as
+// potrf_diag_kernel), the grid solves the block row with a thread per column
+// (as potrf_panel_kernel) and updates the upper trailing triangle, with a
+// bounded grid barrier between the phases.  Three barriers per block
+// instead of three launches and a GEMM.
+template <typename T>
+__global__ void __launch_bounds__(256) potrf_coop_kernel(int64_t k, T* G, int64_t ldg, int* bad, GridBar* bar) {
+  __shared__ T a[CB][CB + 1];
+  __shared__ T rinv[CB];
+  __shared__ T s_inv;
+  const int64_t gt = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const int64_t GT = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t j0 = 0; j0 < k; j0 += CB) {
+    const int jb = (int)min((int64_t)CB, k - j0);
+    T* Gjj = G + j0 + j0 * ldg;
+    // ---- 1. the diagonal block, CTA 0 ----
+    if (blockIdx.x == 0) {
+      // every read of G goes around L1: other CTAs wrote it in earlier phases
+      for (int t = threadIdx.x; t < jb * jb; t += blockDim.x)
+        a[t % jb][t / jb] = __ldcg(Gjj + t % jb + (t / jb) * ldg);
+      __syncthreads();
+      for (int c = 0; c < jb; ++c) {
+        if (threadIdx.x == 0) {
+          T d = a[c][c];
+          if (!(d > T(0))) {
+            atomicExch(bad, 1);
+            d = T(1);
+          }
+          const T r = sqrt(d);
+          a[c][c] = r;
+          s_inv = T(1) / r;
+        }
+        __syncthreads();
+        const T inv = s_inv;
+        for (int j = c + 1 + threadIdx.x; j < jb; j += blockDim.x) a[c][j] *= inv;
+        __syncthreads();
+        const int w = jb - c - 1;
+        for (int t = threadIdx.x; t < w * w; t += blockDim.x) {
+          const int i = c + 1 + t % w, j = c + 1 + t / w;
+          if (i <= j) a[i][j] -= a[c][i] * a[c][j];
+        }
+        __syncthreads();
+      }
+      for (int t = threadIdx.x; t < jb * jb; t += blockDim.x) {
+        const int i = t % jb, j = t / jb;
+        if (i <= j) Gjj[i + j * ldg] = a[i][j];
+      }
+    }
+    if (!grid_sync(bar)) return;
+    const int64_t rest = k - j0 - jb;
+    if (rest <= 0) break;
+    // ---- 2. the block row: R_{b,>b} = R_bb^{-T} G_{b,>b}, a thread per column ----
+    for (int t = threadIdx.x; t < jb * jb; t += blockDim.x) a[t % jb][t / jb] = __ldcg(Gjj + t % jb + (t / jb) * ldg);
+    __syncthreads();
+    if (threadIdx.x < jb) rinv[threadIdx.x] = T(1) / a[threadIdx.x][threadIdx.x];
+    __syncthreads();
+    for (int64_t col = gt; col < rest; col += GT) {
+      T* p = G + j0 + (j0 + jb + col) * ldg;
+      T x[CB];
+#pragma unroll
+      for (int i = 0; i < CB; ++i)
+        if (i < jb) x[i] = __ldcg(p + i);
+#pragma unroll
+      for (int i = 0; i < CB; ++i) {
+        if (i < jb) {
+          T s = x[i];
+#pragma unroll
+          for (int q = 0; q < CB; ++q)
+            if (q < i) s -= a[q][i] * x[q];
+          x[i] = s * rinv[i];
+        }
+      }
+#pragma unroll
+      for (int i = 0; i < CB; ++i)
+        if (i < jb) p[i] = x[i];
+    }
+    if (!grid_sync(bar)) return;
+    // ---- 3. trailing upper triangle: G(i, j) -= sum_q R(q, i) R(q, j), j0+jb <= i <= j ----
+    const int64_t o = j0 + jb;
+    for (int64_t t = gt; t < rest * rest; t += GT) {
+      const int64_t i = t % rest, j = t / rest;
+      if (i > j) continue;
+      const T* ri = G + j0 + (o + i) * ldg;
+      const T* rj = G + j0 + (o + j) * ldg;
+      T s = 0;
+#pragma unroll 8
+      for (int q = 0; q < jb; ++q) s = fma(__ldcg(ri + q), __ldcg(rj + q), s);
+      T* gij = G + (o + i) + (o + j) * ldg;
+      *gij = __ldcg(gij) - s;
+    }
+    if (!grid_sync(bar)) return;
   }
 }
 
@@ -793,6 +1162,26 @@ bool potrf_upper(lra_ctx* ctx, int64_t k, T* G, int64_t ldg) {
   const ArenaMark mk = ctx->arena.mark();
   int* bad = ctx->arena.alloc_n<int>(1);
   LRA_CUDA(cudaMemsetAsync(bad, 0, sizeof(int), ctx->stream));
+  if (k > CB) {
+    int per_sm = 0;
+    LRA_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, potrf_coop_kernel<T>, 256, 0));
+    const int grid = std::max(1, std::min(ctx->num_sms, ctx->num_sms * per_sm));
+    GridBar* bar = reinterpret_cast<GridBar*>(ctx->arena.alloc(sizeof(GridBar)));
+    LRA_CUDA(cudaMemsetAsync(bar, 0, sizeof(GridBar), ctx->stream));
+    void* args[] = {&k, &G, &ldg, &bad, &bar};
+    LRA_CUDA(cudaLaunchCooperativeKernel((const void*)potrf_coop_kernel<T>, dim3(grid), dim3(256), args, 0,
+                                         ctx->stream));
+    post_launch(ctx, "potrf_coop_kernel");
+    zero_lower(ctx, k, k, G, ldg);
+    int h = 0;
+    GridBar hb;
+    LRA_CUDA(cudaMemcpyAsync(&h, bad, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+    LRA_CUDA(cudaMemcpyAsync(&hb, bar, sizeof(GridBar), cudaMemcpyDeviceToHost, ctx->stream));
+    LRA_CUDA(cudaStreamSynchronize(ctx->stream));
+    ctx->arena.release(mk);
+    if (hb.err != 0) fail(LRA_ETIMEDOUT, "potrf: a grid barrier timed out");
+    return h == 0;
+  }
   for (int64_t j0 = 0; j0 < k; j0 += CB) {
     const int jb = (int)std::min<int64_t>(CB, k - j0);
     T* Gjj = G + j0 + j0 * ldg;

@@ -70,6 +70,8 @@ struct lra_ctx {
   uint64_t rng_counter = 0;  // advances per call of the in-library generator
   // the mixed-precision path sends large Float64 GEMMs to tc_gemm
   bool gemm_tc = false;
+  // rtol of the current mixed-precision call (0 otherwise)
+  double mixed_rtol = 0;
   // pinned host staging (grown on demand)
   void* pinned = nullptr;
   size_t pinned_cap = 0;
@@ -183,6 +185,9 @@ std::vector<T> small_svd(lra_ctx* ctx, int64_t k, const T* Mm, T* U, T* V, T* S)
 template <typename T>
 std::vector<T> sort_desc(lra_ctx* ctx, int64_t k, T* S, T* U, T* V);
 
+// Polish sweeps of the mixed-precision path in double-float (X and V
+// Float64 in and out, V overwritten); false when n does not fit.
+bool jacobi_svd_df(lra_ctx* ctx, int64_t n, double* X, int64_t ldx, double* V, int64_t ldv, double* S);
 // jacobi_svd for Float64 with the bulk of the sweeps in FP32 and FP64 polish
 template <typename T>
 void jacobi_svd_fast(lra_ctx* ctx, int64_t n, T* X, int64_t ldx, T* V, int64_t ldv, T* S);

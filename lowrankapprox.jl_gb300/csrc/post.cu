@@ -171,7 +171,18 @@ void jacobi_svd_fast(lra_ctx* ctx, int64_t n, T* X, int64_t ldx, T* V, int64_t l
     jacobi_svd<T>(ctx, n, X, ldx, V, ldv, S);
     return;
   }
-  const NativeGemmScope native(ctx);  // W must come out orthonormal to FP64 rounding
+  // The polish runs in double-float on the mixed path when its rtol leaves
+  // room for the ~1e-13 orthogonality that gives; there the GEMMs below may
+  // use the tensor cores.  Otherwise W must come out orthonormal to FP64
+  // rounding and the GEMMs stay in FP64.
+  const bool df_polish = sizeof(T) == 8 && ctx->mixed_rtol >= 1e-12;
+  const bool saved_tc = ctx->gemm_tc;
+  if (!df_polish) ctx->gemm_tc = false;
+  struct Restore {
+    lra_ctx* c;
+    bool v;
+    ~Restore() { c->gemm_tc = v; }
+  } restore{ctx, saved_tc};
   const ArenaMark mk = ctx->arena.mark();
   // 1. FP32 sweeps on X scaled by a power of two into FP32's range (the
   //    rotations do not depend on the scale)
@@ -200,23 +211,29 @@ void jacobi_svd_fast(lra_ctx* ctx, int64_t n, T* X, int64_t ldx, T* V, int64_t l
   float* S32 = ctx->arena.alloc_n<float>(n);
   cast<T, float>(ctx, n, n, X, ldx, X32, n, scale);
   jacobi_svd<float>(ctx, n, X32, n, V32, n, S32, true);
-  // 2. the rotation in FP64, re-orthonormalized: W = V32 chol(V32' V32)^{-1}
+  // 2. the rotation in FP64, re-orthonormalized by two Newton-Schulz steps
+  //    W <- W (3 I - W'W) / 2: with |I - W'W| near 1e-6 from the FP32
+  //    sweeps the error squares each step, to rounding level after two
   T* W = ctx->arena.alloc_n<T>((size_t)n * n);
   T* G = ctx->arena.alloc_n<T>((size_t)n * n);
+  T* W2 = ctx->arena.alloc_n<T>((size_t)n * n);
   cast<float, T>(ctx, n, n, V32, n, W, n);
-  gemm<T>(ctx, 't', 'n', n, n, n, T(1), W, n, W, n, T(0), G, n);
-  if (!potrf_upper(ctx, n, G, n)) {
-    // cannot happen for a near-orthogonal W; fall back to the FP64 sweeps
-    ctx->arena.release(mk);
-    jacobi_svd<T>(ctx, n, X, ldx, V, ldv, S);
-    return;
+  for (int it = 0; it < 2; ++it) {
+    gemm<T>(ctx, 't', 'n', n, n, n, T(1), W, n, W, n, T(0), G, n);
+    copy_matrix(ctx, n, n, W, n, W2, n);
+    gemm<T>(ctx, 'n', 'n', n, n, n, T(-0.5), W, n, G, n, T(1.5), W2, n);
+    std::swap(W, W2);
   }
-  trsm_right_upper(ctx, n, n, G, n, W, n);
   // 3. X <- X W, FP64 sweeps, V = W V2
   T* Y = ctx->arena.alloc_n<T>((size_t)n * n);
   gemm<T>(ctx, 'n', 'n', n, n, n, T(1), X, ldx, W, n, T(0), Y, n);
   copy_matrix(ctx, n, n, Y, n, X, ldx);
-  jacobi_svd<T>(ctx, n, X, ldx, Y, n, S, true);  // Y <- V2
+  // Y <- V2
+  bool done = false;
+  if constexpr (sizeof(T) == 8)
+    if (df_polish) done = jacobi_svd_df(ctx, n, reinterpret_cast<double*>(X), ldx, reinterpret_cast<double*>(Y), n,
+                                        reinterpret_cast<double*>(S));
+  if (!done) jacobi_svd<T>(ctx, n, X, ldx, Y, n, S, true);
   gemm<T>(ctx, 'n', 'n', n, n, n, T(1), W, n, Y, n, T(0), V, ldv);
   LRA_CUDA(cudaStreamSynchronize(ctx->stream));
   ctx->arena.release(mk);

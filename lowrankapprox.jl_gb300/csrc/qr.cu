@@ -24,6 +24,7 @@
 #include <mutex>
 
 #include "common.cuh"
+#include "df64.cuh"
 #include "internal.hpp"
 
 namespace lra {
@@ -860,66 +861,6 @@ __global__ void __launch_bounds__(NT) geqp3_v2_kernel(QrParams<T> P, QrV2Extra X
 // compensated FP32 arithmetic (error-free products by FMA, two-sum
 // accumulation) on the FP32 pipes, 64x wider than FP64 on this part; pivot
 // decisions, norm downdates and the reflector scalars stay in FP64.
-struct Df {
-  float h, l;
-};
-
-__device__ __forceinline__ double df_val(float h, float l) { return (double)h + (double)l; }
-
-__device__ __forceinline__ Df df_split(double x) {
-  const float h = (float)x;
-  return Df{h, (float)(x - (double)h)};
-}
-
-__device__ __forceinline__ void two_sum(float a, float b, float& s, float& e) {
-  s = a + b;
-  const float bb = s - a;
-  e = (a - (s - bb)) + (b - bb);
-}
-
-__device__ __forceinline__ Df quick_two_sum(float a, float b) {
-  const float s = a + b;
-  return Df{s, b - (s - a)};
-}
-
-__device__ __forceinline__ Df df_add(Df a, Df b) {
-  float s, e;
-  two_sum(a.h, b.h, s, e);
-  e += a.l + b.l;
-  return quick_two_sum(s, e);
-}
-
-__device__ __forceinline__ Df df_mul(Df a, Df b) {
-  const float p = a.h * b.h;
-  float e = fmaf(a.h, b.h, -p);
-  e = fmaf(a.h, b.l, fmaf(a.l, b.h, e));
-  return quick_two_sum(p, e);
-}
-
-// acc += v x, the high parts by two-sum, every lower-order term into acc.l
-__device__ __forceinline__ void df_fma_acc(Df& acc, float vh, float vl, float xh, float xl) {
-  const float p = vh * xh;
-  float pe = fmaf(vh, xh, -p);
-  pe = fmaf(vh, xl, fmaf(vl, xh, pe));
-  float s, e;
-  two_sum(acc.h, p, s, e);
-  acc.h = s;
-  acc.l += e + pe;
-}
-
-// y = x - f v
-__device__ __forceinline__ Df df_axpy_neg(float xh, float xl, Df f, float vh, float vl) {
-  const float p = f.h * vh;
-  float pe = fmaf(f.h, vh, -p);
-  pe = fmaf(f.h, vl, fmaf(f.l, vh, pe));
-  float s, e;
-  two_sum(xh, -p, s, e);
-  return quick_two_sum(s, (xl - pe) + e);
-}
-
-__device__ __forceinline__ Df df_shfl_xor(Df a, int o) {
-  return Df{__shfl_xor_sync(0xffffffffu, a.h, o), __shfl_xor_sync(0xffffffffu, a.l, o)};
-}
 
 struct QrDf {
   float* Bh;            // high parts, ld = lda of the params
@@ -928,32 +869,6 @@ struct QrDf {
   const double* scale;  // 2^-E: the factorization sees B * scale
 };
 
-__device__ __forceinline__ Df df_neg(Df a) { return Df{-a.h, -a.l}; }
-
-__device__ __forceinline__ Df df_div(Df a, Df b) {
-  const float q1 = a.h / b.h;
-  const Df r = df_add(a, df_neg(df_mul(Df{q1, 0.f}, b)));
-  const float q2 = r.h / b.h;
-  return quick_two_sum(q1, q2);
-}
-
-__device__ __forceinline__ Df df_sqrt(Df a) {
-  if (!(a.h > 0.f)) return Df{0.f, 0.f};
-  const float y = sqrtf(a.h);
-  const float p = y * y;
-  const float pe = fmaf(y, y, -p);
-  const float d = ((a.h - p) - pe) + a.l;
-  return quick_two_sum(y, d / (2.f * y));
-}
-
-// orderable key of a nonnegative double-float (h >= 0, |l| <= ulp(h) / 2):
-// h's bits, then l mapped to an unsigned order
-__device__ __forceinline__ long long df_key(Df a) {
-  if (a.h < 0.f) return -1;
-  const unsigned int lb = __float_as_uint(a.l);
-  const unsigned int lo = (lb & 0x80000000u) ? ~lb : (lb | 0x80000000u);
-  return (long long)(((unsigned long long)__float_as_uint(a.h) << 32) | lo);
-}
 
 template <int NT>
 __global__ void __launch_bounds__(NT) geqp3_df_kernel(QrParams<double> P, QrV2Extra X, QrDf D) {
@@ -1416,6 +1331,32 @@ __global__ void geqp3_replay_kernel(int64_t n, const int64_t* piv, const int64_t
   }
 }
 
+// the same replay with the permutation in shared memory (n <= 24576):
+// the swaps are a chain of dependent reads, which shared memory serves in
+// tens of cycles instead of an L2 round trip each
+__global__ void __launch_bounds__(1024) geqp3_replay_smem_kernel(int64_t n, const int64_t* piv, const int64_t* nfac_p,
+                                                                 int64_t* col_at) {
+  extern __shared__ int rp_smem[];
+  int* ca = rp_smem;      // column at position
+  int* ps = rp_smem + n;  // position of column
+  for (int64_t i = threadIdx.x; i < n; i += blockDim.x) ca[i] = ps[i] = (int)i;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    const int64_t nfac = *nfac_p;
+    for (int64_t c = 0; c < nfac; ++c) {
+      const int pc = (int)piv[c];
+      const int p = ps[pc];
+      const int other = ca[c];
+      ca[p] = other;
+      ps[other] = p;
+      ca[c] = pc;
+      ps[pc] = (int)c;
+    }
+  }
+  __syncthreads();
+  for (int64_t i = threadIdx.x; i < n; i += blockDim.x) col_at[i] = ca[i];
+}
+
 __global__ void iota_kernel(int64_t n, int64_t* a, int64_t* b) {
   for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < n; t += (int64_t)gridDim.x * blockDim.x)
     a[t] = b[t] = t;
@@ -1579,8 +1520,16 @@ int64_t geqp3_adap(lra_ctx* ctx, int64_t m, int64_t n, T* A, int64_t lda, int64_
     }
     if (pivot) {
       // xLAQPS's swaps, replayed: jpvt and the column order of A
-      geqp3_replay_kernel<<<1, 32, 0, ctx->stream>>>(n, X.piv, X.nfac, col_at, pos);
-      post_launch(ctx, "geqp3_replay_kernel");
+      if (n <= 24576) {
+        const size_t rs = (size_t)2 * n * sizeof(int);
+        LRA_CUDA(cudaFuncSetAttribute(geqp3_replay_smem_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                      (int)std::max<size_t>(rs, 1)));
+        geqp3_replay_smem_kernel<<<1, 1024, rs, ctx->stream>>>(n, X.piv, X.nfac, col_at);
+        post_launch(ctx, "geqp3_replay_smem_kernel");
+      } else {
+        geqp3_replay_kernel<<<1, 32, 0, ctx->stream>>>(n, X.piv, X.nfac, col_at, pos);
+        post_launch(ctx, "geqp3_replay_kernel");
+      }
     }
     jpvt_kernel<<<gi, 256, 0, ctx->stream>>>(n, col_at, jpvt);
     post_launch(ctx, "jpvt_kernel");
