@@ -57,7 +57,7 @@ void to_host(lra_ctx* ctx, void* dst, const T* src, size_t n) {
 }
 
 // Result arrays of 1 MiB and more live in page-locked host memory, so that
-// the device-to-host copies run at the link's speed (the driver stages a
+// the device-to-host copies run at the link's speed (the CUDA runtime stages a
 // pageable copy at a fraction of it: 19 vs 180 GB/s measured on a GB300
 // node).  Blocks freed through lra_*_free are kept for reuse, up to 2 GiB.
 std::mutex g_pin_mu;

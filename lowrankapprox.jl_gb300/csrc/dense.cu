@@ -354,14 +354,15 @@ __device__ __forceinline__ void cp_async4(float* dst, const float* src) {
                : "memory");
 }
 
-__global__ void __launch_bounds__(JB * 32) jacobi_block_kernel(JacParams<float> P) {
+template <int JBT>
+__global__ void __launch_bounds__(JBT * 32) jacobi_block_kernel(JacParams<float> P) {
   extern __shared__ float jb_smem[];
   __shared__ double red[32];
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
   const int64_t n = P.n;
-  float* Xs = jb_smem;                       // [2 JB][n]
-  float* Vs = jb_smem + (size_t)2 * JB * n;  // [2 JB][n]
-  const int64_t nblk = (n + JB - 1) / JB;
+  float* Xs = jb_smem;                       // [2 JBT][n]
+  float* Vs = jb_smem + (size_t)2 * JBT * n;  // [2 JBT][n]
+  const int64_t nblk = (n + JBT - 1) / JBT;
   const int64_t nbb = nblk + (nblk & 1);
   const float tol = (float)P.tol;
   int sweep = 0;
@@ -371,17 +372,17 @@ __global__ void __launch_bounds__(JB * 32) jacobi_block_kernel(JacParams<float> 
       for (int64_t s = blockIdx.x; s < nbb / 2; s += gridDim.x) {
         int64_t b1, b2;
         rr_pair(r, s, nbb, b1, b2);
-        // local column k < JB is column b1 JB + k, k >= JB is b2 JB + k - JB
+        // local column k < JBT is column b1 JBT + k, k >= JBT is b2 JBT + k - JBT
         auto gcol = [&](int k) -> int64_t {
-          const int64_t b = k < JB ? b1 : b2;
+          const int64_t b = k < JBT ? b1 : b2;
           if (b >= nblk) return -1;
-          const int64_t j = b * JB + (k % JB);
+          const int64_t j = b * JBT + (k % JBT);
           return j < n ? j : -1;
         };
-        // all 4 JB n elements in flight at once (asynchronous copies)
-        for (int k = 0; k < 2 * JB; ++k) {
+        // all 4 JBT n elements in flight at once (asynchronous copies)
+        for (int k = 0; k < 2 * JBT; ++k) {
           const int64_t j = gcol(k);
-          for (int64_t i = threadIdx.x; i < n; i += JB * 32) {
+          for (int64_t i = threadIdx.x; i < n; i += JBT * 32) {
             if (j >= 0) {
               cp_async4(Xs + k * n + i, P.X + i + j * P.ldx);
               cp_async4(Vs + k * n + i, P.V + i + j * P.ldv);
@@ -395,12 +396,12 @@ __global__ void __launch_bounds__(JB * 32) jacobi_block_kernel(JacParams<float> 
         __syncthreads();
         unsigned vmask = 0;  // local columns that exist
 #pragma unroll
-        for (int k = 0; k < 2 * JB; ++k) vmask |= (gcol(k) >= 0 ? 1u : 0u) << k;
+        for (int k = 0; k < 2 * JBT; ++k) vmask |= (gcol(k) >= 0 ? 1u : 0u) << k;
         const int ni = (int)n;
-        for (int lr = 0; lr < 2 * JB - 1; ++lr) {
-          // round-robin pair of this warp among the 2 JB local columns
-          auto lpos = [&](int i) { return i == 0 ? 0 : 1 + (i - 1 + lr) % (2 * JB - 1); };
-          int p = lpos(wid), q = lpos(2 * JB - 1 - wid);
+        for (int lr = 0; lr < 2 * JBT - 1; ++lr) {
+          // round-robin pair of this warp among the 2 JBT local columns
+          auto lpos = [&](int i) { return i == 0 ? 0 : 1 + (i - 1 + lr) % (2 * JBT - 1); };
+          int p = lpos(wid), q = lpos(2 * JBT - 1 - wid);
           if (p > q) {
             const int t = p;
             p = q;
@@ -496,10 +497,10 @@ __global__ void __launch_bounds__(JB * 32) jacobi_block_kernel(JacParams<float> 
           }
           __syncthreads();
         }
-        for (int k = 0; k < 2 * JB; ++k) {
+        for (int k = 0; k < 2 * JBT; ++k) {
           const int64_t j = gcol(k);
           if (j < 0) continue;
-          for (int64_t i = threadIdx.x; i < n; i += JB * 32) {
+          for (int64_t i = threadIdx.x; i < n; i += JBT * 32) {
             P.X[i + j * P.ldx] = Xs[k * n + i];
             P.V[i + j * P.ldv] = Vs[k * n + i];
           }
@@ -512,7 +513,7 @@ __global__ void __launch_bounds__(JB * 32) jacobi_block_kernel(JacParams<float> 
     if (threadIdx.x == 0) P.part[blockIdx.x] = offd;
     if (!grid_sync(P.bar)) return;
     double mx = 0;
-    for (int b = threadIdx.x; b < gridDim.x; b += JB * 32) mx = fmax(mx, __ldcg(P.part + b));
+    for (int b = threadIdx.x; b < gridDim.x; b += JBT * 32) mx = fmax(mx, __ldcg(P.part + b));
     mx = block_max(mx, red);
     if (!grid_sync(P.bar)) return;
     if (mx <= P.stop) {
@@ -521,7 +522,7 @@ __global__ void __launch_bounds__(JB * 32) jacobi_block_kernel(JacParams<float> 
     }
   }
   // singular values = column norms, a warp per column
-  const int64_t gw = (int64_t)blockIdx.x * JB + wid, W = (int64_t)gridDim.x * JB;
+  const int64_t gw = (int64_t)blockIdx.x * JBT + wid, W = (int64_t)gridDim.x * JBT;
   for (int64_t j = gw; j < n; j += W) {
     const float* x = P.X + j * P.ldx;
     double acc = 0;
@@ -559,19 +560,20 @@ __device__ __forceinline__ bool df_gt(Df x, Df y) { return x.h > y.h || (x.h == 
 __device__ __forceinline__ Df df_rot_a(Df c, Df s, Df u, Df w) { return df_add(df_mul(c, u), df_neg(df_mul(s, w))); }
 __device__ __forceinline__ Df df_rot_b(Df c, Df s, Df u, Df w) { return df_add(df_mul(s, u), df_mul(c, w)); }
 
-__global__ void __launch_bounds__(JB * 32) jacobi_block_df_kernel(JacDf P) {
+template <int JBT>
+__global__ void __launch_bounds__(JBT * 32) jacobi_block_df_kernel(JacDf P) {
   extern __shared__ float jd_smem[];
   __shared__ int s_any;
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
   const int ni = (int)P.n;
-  const size_t plane = (size_t)2 * JB * ni;
+  const size_t plane = (size_t)2 * JBT * ni;
   float* Xh = jd_smem;
   float* Xl = Xh + plane;
   float* Vh = Xl + plane;
   float* Vl = Vh + plane;
-  const int nblk = (ni + JB - 1) / JB;
+  const int nblk = (ni + JBT - 1) / JBT;
   const int nbb = nblk + (nblk & 1);
-  const Df tol2 = df_split(P.tol * P.tol), stop2 = df_split(P.stop * P.stop);
+  const float ftol = (float)P.tol, fstop = (float)P.stop;
   int sweep = 0;
   for (; sweep < P.max_sweeps; ++sweep) {
     int above = 0;
@@ -580,14 +582,14 @@ __global__ void __launch_bounds__(JB * 32) jacobi_block_df_kernel(JacDf P) {
         auto bpos = [&](int i) { return i == 0 ? 0 : 1 + (i - 1 + r) % (nbb - 1); };
         const int b1 = bpos(s), b2 = bpos(nbb - 1 - s);
         auto gcol = [&](int k) -> int {
-          const int b = k < JB ? b1 : b2;
+          const int b = k < JBT ? b1 : b2;
           if (b >= nblk) return -1;
-          const int j = b * JB + (k % JB);
+          const int j = b * JBT + (k % JBT);
           return j < ni ? j : -1;
         };
-        for (int k = 0; k < 2 * JB; ++k) {
+        for (int k = 0; k < 2 * JBT; ++k) {
           const int j = gcol(k);
-          for (int i = threadIdx.x; i < ni; i += JB * 32) {
+          for (int i = threadIdx.x; i < ni; i += JBT * 32) {
             const size_t o = (size_t)k * ni + i;
             if (j >= 0) {
               const size_t g = (size_t)j * ni + i;
@@ -604,10 +606,10 @@ __global__ void __launch_bounds__(JB * 32) jacobi_block_df_kernel(JacDf P) {
         __syncthreads();
         unsigned vmask = 0;
 #pragma unroll
-        for (int k = 0; k < 2 * JB; ++k) vmask |= (gcol(k) >= 0 ? 1u : 0u) << k;
-        for (int lr = 0; lr < 2 * JB - 1; ++lr) {
-          auto lpos = [&](int i) { return i == 0 ? 0 : 1 + (i - 1 + lr) % (2 * JB - 1); };
-          int p = lpos(wid), q = lpos(2 * JB - 1 - wid);
+        for (int k = 0; k < 2 * JBT; ++k) vmask |= (gcol(k) >= 0 ? 1u : 0u) << k;
+        for (int lr = 0; lr < 2 * JBT - 1; ++lr) {
+          auto lpos = [&](int i) { return i == 0 ? 0 : 1 + (i - 1 + lr) % (2 * JBT - 1); };
+          int p = lpos(wid), q = lpos(2 * JBT - 1 - wid);
           if (p > q) {
             const int t = p;
             p = q;
@@ -641,47 +643,93 @@ __global__ void __launch_bounds__(JB * 32) jacobi_block_df_kernel(JacDf P) {
               b = df_add(b, df_shfl_xor(b, o));
               g = df_add(g, df_shfl_xor(g, o));
             }
-            if (a.h != 0.f && b.h != 0.f) {
-              const Df g2 = df_mul(g, g), ab = df_mul(a, b);
-              if (df_gt(g2, df_mul(tol2, ab))) {
-                if (df_gt(g2, df_mul(stop2, ab))) above = 1;
-                // t = tan of the rotation angle, the smaller root of t^2 + 2 zeta t - 1
-                const Df d = df_add(b, df_neg(a));
-                const Df rt = df_sqrt(df_add(df_mul(d, d), df_mul(Df{4.f, 0.f}, g2)));
-                const Df den = df_add(d, d.h >= 0.f ? rt : df_neg(rt));
-                const Df t = df_div(df_mul(Df{2.f, 0.f}, g), den);
-                const Df c = df_div(Df{1.f, 0.f}, df_sqrt(df_add(Df{1.f, 0.f}, df_mul(t, t))));
-                const Df sn = df_mul(c, t);
-#pragma unroll
-                for (int tt = 0; tt < JB_RPL; ++tt) {
-                  const int i = lane + 32 * tt;
-                  if (i < ni) {
-                    const Df x1 = df_rot_a(c, sn, u[tt], w[tt]), x2 = df_rot_b(c, sn, u[tt], w[tt]);
-                    xph[i] = x1.h;
-                    xpl[i] = x1.l;
-                    xqh[i] = x2.h;
-                    xql[i] = x2.l;
-                  }
-                }
+            if (a.h > 0.f && b.h > 0.f) {
+              const float rel = fabsf(g.h) * rsqrtf(a.h) * rsqrtf(b.h);
+              if (rel > ftol) {
+                if (rel > fstop) above = 1;
+                // tan of the rotation angle from zeta = (b - a) / (2 g) in
+                // double-float; t itself in FP32: a rotation by an angle off
+                // by 1e-7 relative still shrinks g by 1e-7, and the rotation
+                // matrix below is orthogonal to double-float precision
+                const Df zeta = df_div(df_add(b, df_neg(a)), df_mul(Df{2.f, 0.f}, g));
+                const float z = zeta.h;
+                const float t = copysignf(1.0f, z) / (fabsf(z) + sqrtf(fmaf(z, z, 1.0f)));
                 float* vph = Vh + p * ni;
                 float* vpl = Vl + p * ni;
                 float* vqh = Vh + q * ni;
                 float* vql = Vl + q * ni;
+                if (fabsf(t) < 9.5367431640625e-07f) {
+                  // small angle: x' = x + delta, delta = -eps x -/+ s y in FP32
+                  // (c = 1 - eps, eps = t^2 / (r (1 + r)), r = sqrt(1 + t^2))
+                  const float r = sqrtf(fmaf(t, t, 1.0f));
+                  const float eps = t * t / (r * (1.0f + r));
+                  const float sn = t / r;
+                  auto bump = [&](Df x, float d) {
+                    float hs, e;
+                    two_sum(x.h, d, hs, e);
+                    return quick_two_sum(hs, x.l + e);
+                  };
 #pragma unroll
-                for (int tt = 0; tt < JB_RPL; ++tt) {
-                  const int i = lane + 32 * tt;
-                  u[tt] = i < ni ? Df{vph[i], vpl[i]} : Df{0.f, 0.f};
-                  w[tt] = i < ni ? Df{vqh[i], vql[i]} : Df{0.f, 0.f};
-                }
+                  for (int tt = 0; tt < JB_RPL; ++tt) {
+                    const int i = lane + 32 * tt;
+                    if (i < ni) {
+                      const Df x1 = bump(u[tt], fmaf(-sn, w[tt].l, fmaf(-sn, w[tt].h, -eps * u[tt].h)));
+                      const Df x2 = bump(w[tt], fmaf(sn, u[tt].l, fmaf(sn, u[tt].h, -eps * w[tt].h)));
+                      xph[i] = x1.h;
+                      xpl[i] = x1.l;
+                      xqh[i] = x2.h;
+                      xql[i] = x2.l;
+                    }
+                  }
 #pragma unroll
-                for (int tt = 0; tt < JB_RPL; ++tt) {
-                  const int i = lane + 32 * tt;
-                  if (i < ni) {
-                    const Df v1 = df_rot_a(c, sn, u[tt], w[tt]), v2 = df_rot_b(c, sn, u[tt], w[tt]);
-                    vph[i] = v1.h;
-                    vpl[i] = v1.l;
-                    vqh[i] = v2.h;
-                    vql[i] = v2.l;
+                  for (int tt = 0; tt < JB_RPL; ++tt) {
+                    const int i = lane + 32 * tt;
+                    u[tt] = i < ni ? Df{vph[i], vpl[i]} : Df{0.f, 0.f};
+                    w[tt] = i < ni ? Df{vqh[i], vql[i]} : Df{0.f, 0.f};
+                  }
+#pragma unroll
+                  for (int tt = 0; tt < JB_RPL; ++tt) {
+                    const int i = lane + 32 * tt;
+                    if (i < ni) {
+                      const Df v1 = bump(u[tt], fmaf(-sn, w[tt].l, fmaf(-sn, w[tt].h, -eps * u[tt].h)));
+                      const Df v2 = bump(w[tt], fmaf(sn, u[tt].l, fmaf(sn, u[tt].h, -eps * w[tt].h)));
+                      vph[i] = v1.h;
+                      vpl[i] = v1.l;
+                      vqh[i] = v2.h;
+                      vql[i] = v2.l;
+                    }
+                  }
+                } else {
+                  const Df td{t, 0.f};
+                  const Df c = df_div(Df{1.f, 0.f}, df_sqrt(df_add(Df{1.f, 0.f}, df_mul(td, td))));
+                  const Df sn = df_mul(c, td);
+#pragma unroll
+                  for (int tt = 0; tt < JB_RPL; ++tt) {
+                    const int i = lane + 32 * tt;
+                    if (i < ni) {
+                      const Df x1 = df_rot_a(c, sn, u[tt], w[tt]), x2 = df_rot_b(c, sn, u[tt], w[tt]);
+                      xph[i] = x1.h;
+                      xpl[i] = x1.l;
+                      xqh[i] = x2.h;
+                      xql[i] = x2.l;
+                    }
+                  }
+#pragma unroll
+                  for (int tt = 0; tt < JB_RPL; ++tt) {
+                    const int i = lane + 32 * tt;
+                    u[tt] = i < ni ? Df{vph[i], vpl[i]} : Df{0.f, 0.f};
+                    w[tt] = i < ni ? Df{vqh[i], vql[i]} : Df{0.f, 0.f};
+                  }
+#pragma unroll
+                  for (int tt = 0; tt < JB_RPL; ++tt) {
+                    const int i = lane + 32 * tt;
+                    if (i < ni) {
+                      const Df v1 = df_rot_a(c, sn, u[tt], w[tt]), v2 = df_rot_b(c, sn, u[tt], w[tt]);
+                      vph[i] = v1.h;
+                      vpl[i] = v1.l;
+                      vqh[i] = v2.h;
+                      vql[i] = v2.l;
+                    }
                   }
                 }
               }
@@ -689,10 +737,10 @@ __global__ void __launch_bounds__(JB * 32) jacobi_block_df_kernel(JacDf P) {
           }
           __syncthreads();
         }
-        for (int k = 0; k < 2 * JB; ++k) {
+        for (int k = 0; k < 2 * JBT; ++k) {
           const int j = gcol(k);
           if (j < 0) continue;
-          for (int i = threadIdx.x; i < ni; i += JB * 32) {
+          for (int i = threadIdx.x; i < ni; i += JBT * 32) {
             const size_t o = (size_t)k * ni + i, g = (size_t)j * ni + i;
             P.Xh[g] = Xh[o];
             P.Xl[g] = Xl[o];
@@ -722,7 +770,7 @@ __global__ void __launch_bounds__(JB * 32) jacobi_block_df_kernel(JacDf P) {
     }
   }
   // singular values = column norms, a warp per column
-  const int gw = blockIdx.x * JB + wid, W = gridDim.x * JB;
+  const int gw = blockIdx.x * JBT + wid, W = gridDim.x * JBT;
   for (int j = gw; j < ni; j += W) {
     Df acc{0.f, 0.f};
     for (int i = lane; i < ni; i += 32) {
@@ -779,11 +827,16 @@ void jacobi_svd(lra_ctx* ctx, int64_t n, T* X, int64_t ldx, T* V, int64_t ldv, T
   if (n <= 0) return;
   set_identity(ctx, n, n, V, ldv);
   const ArenaMark mk = ctx->arena.mark();
-  const size_t blk_smem = (size_t)4 * JB * n * sizeof(float);
-  const bool block = !pair_cta && n >= 4 * JB && blk_smem <= 200 * 1024;
+  // FP32: 16-column blocks (half the grid barriers per sweep) when two
+  // block columns of X and V fit shared memory, else 8
+  const int jbt = (size_t)4 * 16 * n * sizeof(float) <= 200 * 1024 ? 16 : 8;
+  const size_t blk_smem = (size_t)4 * jbt * n * sizeof(float);
+  const bool block = !pair_cta && n >= 4 * jbt && blk_smem <= 200 * 1024;
   const void* kern = pair_cta ? (const void*)jacobi_pair_kernel<T, NT>
-                              : (block ? (const void*)jacobi_block_kernel : (const void*)jacobi_kernel<T, NT>);
-  const int nt = block ? JB * 32 : NT;
+                              : (block ? (jbt == 16 ? (const void*)jacobi_block_kernel<16>
+                                                    : (const void*)jacobi_block_kernel<8>)
+                                       : (const void*)jacobi_kernel<T, NT>);
+  const int nt = block ? jbt * 32 : NT;
   const size_t smem = block ? blk_smem : 0;
   if (block) LRA_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
   int per_sm = 0;
@@ -791,7 +844,7 @@ void jacobi_svd(lra_ctx* ctx, int64_t n, T* X, int64_t ldx, T* V, int64_t ldv, T
   const int64_t pairs = (n + 1) / 2;
   int64_t units = pair_cta ? pairs : (pairs + NT / 32 - 1) / (NT / 32);
   if (block) {
-    const int64_t nblk = (n + JB - 1) / JB;
+    const int64_t nblk = (n + jbt - 1) / jbt;
     units = (nblk + 1) / 2;
   }
   // the FP64 pairs all at once (up to two CTAs per SM), the rest one CTA per SM
@@ -831,15 +884,18 @@ void jacobi_svd(lra_ctx* ctx, int64_t n, T* X, int64_t ldx, T* V, int64_t ldv, T
 }
 
 bool jacobi_svd_df(lra_ctx* ctx, int64_t n, double* X, int64_t ldx, double* V, int64_t ldv, double* S) {
+  // 4-column blocks: the double-float rotations are issue-bound, so the work
+  // is spread over as many SMs as the block pairs allow
+  constexpr int JDF = 4;
   if (n < 2 || n > 32 * JB_RPL) return false;
-  const size_t smem = (size_t)8 * JB * n * sizeof(float);
+  const size_t smem = (size_t)8 * JDF * n * sizeof(float);
   if (smem > 200 * 1024) return false;
-  LRA_CUDA(cudaFuncSetAttribute(jacobi_block_df_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  LRA_CUDA(cudaFuncSetAttribute(jacobi_block_df_kernel<JDF>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
   int per_sm = 0;
-  LRA_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, jacobi_block_df_kernel, JB * 32, smem));
+  LRA_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, jacobi_block_df_kernel<JDF>, JDF * 32, smem));
   if (per_sm < 1) return false;
   const ArenaMark mk = ctx->arena.mark();
-  const int64_t nblk = (n + JB - 1) / JB;
+  const int64_t nblk = (n + JDF - 1) / JDF;
   const int grid = (int)std::max<int64_t>(1, std::min<int64_t>((nblk + 1) / 2, (int64_t)ctx->num_sms * per_sm));
   JacDf P;
   P.n = n;
@@ -862,9 +918,9 @@ bool jacobi_svd_df(lra_ctx* ctx, int64_t n, double* X, int64_t ldx, double* V, i
   df_from_double_kernel<<<g, 256, 0, ctx->stream>>>(n, n, nullptr, n, P.Vh, P.Vl, 1);
   post_launch(ctx, "df_from_double_kernel");
   void* args[] = {&P};
-  LRA_CUDA(cudaLaunchCooperativeKernel((const void*)jacobi_block_df_kernel, dim3(grid), dim3(JB * 32), args, smem,
+  LRA_CUDA(cudaLaunchCooperativeKernel((const void*)jacobi_block_df_kernel<JDF>, dim3(grid), dim3(JDF * 32), args, smem,
                                        ctx->stream));
-  post_launch(ctx, "jacobi_block_df_kernel");
+  post_launch(ctx, "jacobi_block_df_kernel<JDF>");
   df_to_double_kernel<<<g, 256, 0, ctx->stream>>>(n, n, P.Xh, P.Xl, X, ldx);
   post_launch(ctx, "df_to_double_kernel");
   df_to_double_kernel<<<g, 256, 0, ctx->stream>>>(n, n, P.Vh, P.Vl, V, ldv);

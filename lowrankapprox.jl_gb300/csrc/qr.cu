@@ -19,6 +19,8 @@
 #include <cooperative_groups.h>
 
 #include <algorithm>
+#include <vector>
+#include <cstdio>
 #include <cstring>
 #include <cmath>
 #include <mutex>
@@ -534,6 +536,7 @@ __global__ void __launch_bounds__(NT) geqp3_v2_kernel(QrParams<T> P, QrV2Extra X
   const int64_t W = (int64_t)gridDim.x * NW;
   const int64_t m = P.m, n = P.n, lda = P.lda;
   T* __restrict__ A = P.A;
+  auto ldown = [](const T* p) { return *p; };
   const T tol3z = sqrt(Real<T>::eps);
   const int64_t lastrk = m < n ? m : n;
   const int64_t ncol = gw < n ? (n - 1 - gw) / W + 1 : 0;  // columns of this warp
@@ -680,6 +683,7 @@ __global__ void __launch_bounds__(NT) geqp3_v2_kernel(QrParams<T> P, QrV2Extra X
         X.beta[c] = (double)sh.beta;
       }
       // ---- each warp: apply H(c) to its live columns, two at a time -----------
+      // (loaded through L1: a warp's columns are written by that warp alone)
       auto dead = [&](int64_t t) {
         return (s_st[t * NW + wid] & ST_DONE) || gw + t * W == pvt;
       };
@@ -693,8 +697,8 @@ __global__ void __launch_bounds__(NT) geqp3_v2_kernel(QrParams<T> P, QrV2Extra X
         const int64_t tb = two ? t++ : ta;
         T* ca = A + (gw + ta * W) * lda;
         T* cb = A + (gw + tb * W) * lda;
-        const T arca0 = __ldcg(ca + c);
-        const T arcb0 = two ? __ldcg(cb + c) : T(0);
+        const T arca0 = ldown(ca + c);
+        const T arcb0 = two ? ldown(cb + c) : T(0);
         T* ya = ca + c + 1;
         T* yb = cb + c + 1;
         T sa = 0, sb = 0;
@@ -706,8 +710,8 @@ __global__ void __launch_bounds__(NT) geqp3_v2_kernel(QrParams<T> P, QrV2Extra X
             for (int q = 0; q < QCH; ++q) {
               if (q % QG == 0 && 32 * q >= rem) break;
               const int64_t i = b0 + lane + 32 * q;
-              xa[q] = i < len ? __ldcg(ya + i) : T(0);
-              xb[q] = (two && i < len) ? __ldcg(yb + i) : T(0);
+              xa[q] = i < len ? ldown(ya + i) : T(0);
+              xb[q] = (two && i < len) ? ldown(yb + i) : T(0);
             }
 #pragma unroll
             for (int q = 0; q < QCH; ++q) {
@@ -734,8 +738,8 @@ __global__ void __launch_bounds__(NT) geqp3_v2_kernel(QrParams<T> P, QrV2Extra X
               for (int q = 0; q < QCH; ++q) {
                 if (q % QG == 0 && 32 * q >= rem) break;
                 const int64_t i = b0 + lane + 32 * q;
-                xa[q] = i < len ? __ldcg(ya + i) : T(0);
-                xb[q] = (two && i < len) ? __ldcg(yb + i) : T(0);
+                xa[q] = i < len ? ldown(ya + i) : T(0);
+                xb[q] = (two && i < len) ? ldown(yb + i) : T(0);
               }
             }
 #pragma unroll
@@ -867,6 +871,7 @@ struct QrDf {
   float* Bl;            // low parts
   const double* vn0;    // initial column norms (scaled)
   const double* scale;  // 2^-E: the factorization sees B * scale
+  unsigned long long* stamps;  // LRA_TRACE: %globaltimer at 8 points of each pivot (CTA 0), or null
 };
 
 
@@ -882,6 +887,10 @@ __global__ void __launch_bounds__(NT) geqp3_df_kernel(QrParams<double> P, QrV2Ex
   const int64_t gw = (int64_t)blockIdx.x * NW + wid;
   const int64_t W = (int64_t)gridDim.x * NW;
   const int64_t m = P.m, n = P.n, lda = P.lda;
+  auto ldown = [](const float* p) { return *p; };
+  auto stamp = [&](int64_t c, int ph) {
+    if (D.stamps && blockIdx.x == 0 && threadIdx.x == 0 && c < P.kmax) D.stamps[c * 16 + ph] = globaltimer_ns();
+  };
   float* __restrict__ Bh = D.Bh;
   float* __restrict__ Bl = D.Bl;
   const double tol3z = sqrt(Real<double>::eps);
@@ -899,8 +908,10 @@ __global__ void __launch_bounds__(NT) geqp3_df_kernel(QrParams<double> P, QrV2Ex
     return (int64_t)blockIdx.x * NW + (s % NW) + (int64_t)(s / NW) * W;
   };
   // warp 0 alone reduces the per-CTA candidates; one block barrier
-  auto reduce_pivot_key = [&]() -> int64_t {
+  __shared__ int s_lst;
+  auto reduce_pivot_key = [&](const int* lstp = nullptr) -> int64_t {
     if (wid == 0) {
+      if (lane == 0 && lstp) s_lst = *((const volatile int*)lstp);
       long long k = -2;
       int64_t i = INT64_MAX;
       for (int b = lane; b < gridDim.x; b += 32) key_merge(k, i, __ldcg(X.part_k + b), __ldcg(P.part_i + b));
@@ -998,6 +1009,7 @@ __global__ void __launch_bounds__(NT) geqp3_df_kernel(QrParams<double> P, QrV2Ex
     while (kk < jb && !stop_block) {
       const int64_t c = j + kk;
       if (!P.pivot) pvt = c;
+      stamp(c, 0);
       // ---- every CTA: the reflector of column pvt, rows c..m-1 ---------------
       const int64_t len = m - c - 1;
       const float* ph = Bh + pvt * lda;
@@ -1009,6 +1021,7 @@ __global__ void __launch_bounds__(NT) geqp3_df_kernel(QrParams<double> P, QrV2Ex
       __shared__ Df s_alpha;
       if (threadIdx.x == 0) s_alpha = Df{__ldcg(ph + c), __ldcg(pl + c)};
       __syncthreads();
+      stamp(c, 1);
       if (wid == 0) {
         // xLARFG in double-float: beta = -sign(alpha) sqrt(alpha^2 + |x|^2),
         // tau = (beta - alpha) / beta, x <- x / (alpha - beta).  The matrix
@@ -1037,6 +1050,7 @@ __global__ void __launch_bounds__(NT) geqp3_df_kernel(QrParams<double> P, QrV2Ex
         }
       }
       __syncthreads();
+      stamp(c, 2);
       const double tau = sh.tau;
       if (tau != 0) {
         const Df sc = s_f;
@@ -1054,12 +1068,19 @@ __global__ void __launch_bounds__(NT) geqp3_df_kernel(QrParams<double> P, QrV2Ex
         X.piv[c] = pvt;
         X.beta[c] = sh.beta;
       }
+      stamp(c, 3);
       const Df tdf = s_tau;
       // ---- each warp: apply H(c) to its live columns, two at a time -----------
+      // A warp's columns are read and written by that warp alone, so they
+      // are loaded through L1: a CTA's columns fit there for sketches of up
+      // to a few hundred rows, and a hit costs tens of cycles, not an L2
+      // round trip.  (The pivot column, written by another SM, is read
+      // around L1 above.)
       auto dead = [&](int64_t t) {
         return (s_st[t * NW + wid] & ST_DONE) || gw + t * W == pvt;
       };
       int64_t t = 0;
+      int pass = 0;
       while (true) {
         while (t < ncol && dead(t)) ++t;
         if (t >= ncol) break;
@@ -1072,8 +1093,8 @@ __global__ void __launch_bounds__(NT) geqp3_df_kernel(QrParams<double> P, QrV2Ex
         float* al = Bl + ja * lda;
         float* bh = Bh + jbb * lda;
         float* bl = Bl + jbb * lda;
-        const Df arca0{__ldcg(ah + c), __ldcg(al + c)};
-        const Df arcb0 = two ? Df{__ldcg(bh + c), __ldcg(bl + c)} : Df{0.f, 0.f};
+        const Df arca0{ldown(ah + c), ldown(al + c)};
+        const Df arcb0 = two ? Df{ldown(bh + c), ldown(bl + c)} : Df{0.f, 0.f};
         Df sa{0.f, 0.f}, sb{0.f, 0.f};
         float xah[QCH], xal[QCH], xbh[QCH], xbl[QCH];
         const int64_t o = c + 1;
@@ -1085,10 +1106,10 @@ __global__ void __launch_bounds__(NT) geqp3_df_kernel(QrParams<double> P, QrV2Ex
               if (q % QG == 0 && 32 * q >= rem) break;
               const int64_t i = b0 + lane + 32 * q;
               const bool in = i < len;
-              xah[q] = in ? __ldcg(ah + o + i) : 0.f;
-              xal[q] = in ? __ldcg(al + o + i) : 0.f;
-              xbh[q] = (two && in) ? __ldcg(bh + o + i) : 0.f;
-              xbl[q] = (two && in) ? __ldcg(bl + o + i) : 0.f;
+              xah[q] = in ? ldown(ah + o + i) : 0.f;
+              xal[q] = in ? ldown(al + o + i) : 0.f;
+              xbh[q] = (two && in) ? ldown(bh + o + i) : 0.f;
+              xbl[q] = (two && in) ? ldown(bl + o + i) : 0.f;
             }
 #pragma unroll
             for (int q = 0; q < QCH; ++q) {
@@ -1100,6 +1121,7 @@ __global__ void __launch_bounds__(NT) geqp3_df_kernel(QrParams<double> P, QrV2Ex
             }
           }
         }
+        if (pass < 2) stamp(c, 8 + 3 * pass);
 #pragma unroll
         for (int off = 16; off > 0; off >>= 1) {
           sa = df_add(sa, df_shfl_xor(sa, off));
@@ -1107,6 +1129,7 @@ __global__ void __launch_bounds__(NT) geqp3_df_kernel(QrParams<double> P, QrV2Ex
         }
         const Df fa = df_mul(tdf, df_add(arca0, sa));
         const Df fb = two ? df_mul(tdf, df_add(arcb0, sb)) : Df{0.f, 0.f};
+        if (pass < 2) stamp(c, 9 + 3 * pass);
         const bool ua = fa.h != 0.f, ub = two && fb.h != 0.f;
         if (ua || ub) {
           for (int64_t b0 = 0; b0 < len; b0 += 32 * QCH) {
@@ -1117,10 +1140,10 @@ __global__ void __launch_bounds__(NT) geqp3_df_kernel(QrParams<double> P, QrV2Ex
                 if (q % QG == 0 && 32 * q >= rem) break;
                 const int64_t i = b0 + lane + 32 * q;
                 const bool in = i < len;
-                xah[q] = in ? __ldcg(ah + o + i) : 0.f;
-                xal[q] = in ? __ldcg(al + o + i) : 0.f;
-                xbh[q] = (two && in) ? __ldcg(bh + o + i) : 0.f;
-                xbl[q] = (two && in) ? __ldcg(bl + o + i) : 0.f;
+                xah[q] = in ? ldown(ah + o + i) : 0.f;
+                xal[q] = in ? ldown(al + o + i) : 0.f;
+                xbh[q] = (two && in) ? ldown(bh + o + i) : 0.f;
+                xbl[q] = (two && in) ? ldown(bl + o + i) : 0.f;
               }
             }
 #pragma unroll
@@ -1143,6 +1166,8 @@ __global__ void __launch_bounds__(NT) geqp3_df_kernel(QrParams<double> P, QrV2Ex
             }
           }
         }
+        if (pass < 2) stamp(c, 10 + 3 * pass);
+        ++pass;
         if (lane == 0) {
           const Df arca = df_add(arca0, Df{-fa.h, -fa.l});
           ah[c] = arca.h;
@@ -1157,6 +1182,7 @@ __global__ void __launch_bounds__(NT) geqp3_df_kernel(QrParams<double> P, QrV2Ex
         }
       }
       __syncthreads();
+      stamp(c, 4);
       // ---- a thread per slot: norm downdate and the pivot candidate -----------
       bk = -2;
       bi = INT64_MAX;
@@ -1190,8 +1216,11 @@ __global__ void __launch_bounds__(NT) geqp3_df_kernel(QrParams<double> P, QrV2Ex
         key_merge(bk, bi, df_key(v1), jj);
       }
       if (myflag) atomicAdd(lst, 1);
+      stamp(c, 5);
       publish(bk, bi);
+      stamp(c, 6);
       if (!grid_sync(P.bar)) return;
+      stamp(c, 7);
       if (blockIdx.x == 0) {
         float* wh = Bh + pvt * lda;
         float* wl = Bl + pvt * lda;
@@ -1205,8 +1234,8 @@ __global__ void __launch_bounds__(NT) geqp3_df_kernel(QrParams<double> P, QrV2Ex
           wl[c] = s_beta.l;
         }
       }
-      stop_block = *((volatile int*)lst) != 0;
-      pvt = reduce_pivot_key();  // its block reduction orders the writes above before vs is reloaded
+      pvt = reduce_pivot_key(lst);  // its block barrier also orders the writes above before vs is reloaded
+      stop_block = s_lst != 0;
       ++kk;
     }
     const int64_t kb = kk;
@@ -1467,6 +1496,8 @@ int64_t geqp3_adap(lra_ctx* ctx, int64_t m, int64_t n, T* A, int64_t lda, int64_
   if (v2) {
     LRA_CUDA(cudaFuncSetAttribute(geqp3_v2_kernel<T, NT>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                   (int)smem2));
+    LRA_CUDA(cudaFuncSetAttribute(geqp3_v2_kernel<T, NT>, cudaFuncAttributePreferredSharedMemoryCarveout,
+                                  cudaSharedmemCarveoutMaxL1));
     int per_sm2 = 0;
     LRA_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm2, geqp3_v2_kernel<T, NT>, NT, smem2));
     if (per_sm2 < 1) fail(LRA_ECUDA, "geqp3 kernel cannot be resident");
@@ -1498,11 +1529,18 @@ int64_t geqp3_adap(lra_ctx* ctx, int64_t m, int64_t n, T* A, int64_t lda, int64_
       const unsigned gs = (unsigned)std::max<int64_t>(1, std::min<int64_t>((n + 7) / 8, ctx->num_sms * 8));
       df_split_kernel<<<gs, 256, 0, ctx->stream>>>(m, n, Bd, lda, scale, Bh, Bl, m, vn0);
       post_launch(ctx, "df_split_kernel");
-      QrDf D{Bh, Bl, vn0, scale};
+      QrDf D{Bh, Bl, vn0, scale, nullptr};
+      if (trace_on()) {
+        D.stamps = ctx->arena.alloc_n<unsigned long long>((size_t)16 * std::max<int64_t>(P.kmax, 1));
+        LRA_CUDA(cudaMemsetAsync(D.stamps, 0, (size_t)16 * std::max<int64_t>(P.kmax, 1) * 8, ctx->stream));
+      }
       QrParams<double> Pd;
       std::memcpy(&Pd, &P, sizeof(Pd));
       Pd.lda = m;
       LRA_CUDA(cudaFuncSetAttribute(geqp3_df_kernel<NT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem2));
+      // as much L1 as the shared memory leaves: the warps' columns live there
+      LRA_CUDA(cudaFuncSetAttribute(geqp3_df_kernel<NT>, cudaFuncAttributePreferredSharedMemoryCarveout,
+                                    cudaSharedmemCarveoutMaxL1));
       int per_df = 0;
       LRA_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_df, geqp3_df_kernel<NT>, NT, smem2));
       if (per_df < 1) fail(LRA_ECUDA, "geqp3 kernel cannot be resident");
@@ -1510,6 +1548,45 @@ int64_t geqp3_adap(lra_ctx* ctx, int64_t m, int64_t n, T* A, int64_t lda, int64_
       LRA_CUDA(cudaLaunchCooperativeKernel((const void*)geqp3_df_kernel<NT>, dim3(grid), dim3(NT), args, smem2,
                                            ctx->stream));
       post_launch(ctx, "geqp3_df_kernel");
+      if (D.stamps) {
+        std::vector<unsigned long long> h((size_t)16 * P.kmax);
+        LRA_CUDA(cudaMemcpyAsync(h.data(), D.stamps, h.size() * 8, cudaMemcpyDeviceToHost, ctx->stream));
+        LRA_CUDA(cudaStreamSynchronize(ctx->stream));
+        double ph[7] = {0}, cyc = 0;
+        int64_t cnt = 0;
+        double sub[6] = {0};
+        int64_t nsub = 0;
+        for (int64_t c = 0; c + 1 < P.kmax; ++c) {
+          const unsigned long long* t = h.data() + 16 * c;
+          if (!t[0] || !t[7] || !h[16 * (c + 1)]) continue;
+          for (int q = 0; q < 7; ++q) ph[q] += (double)(t[q + 1] - t[q]);
+          cyc += (double)(h[16 * (c + 1)] - t[0]);
+          ++cnt;
+          if (t[8] && t[9] && t[10] && t[11] && t[12] && t[13]) {
+            sub[0] += (double)(t[8] - t[3]);
+            sub[1] += (double)(t[9] - t[8]);
+            sub[2] += (double)(t[10] - t[9]);
+            sub[3] += (double)(t[11] - t[10]);
+            sub[4] += (double)(t[12] - t[11]);
+            sub[5] += (double)(t[13] - t[12]);
+            ++nsub;
+          }
+        }
+        if (nsub)
+          std::fprintf(stderr,
+                       "[lra] geqp3_df warp-0 passes (us): load+dots %.2f reduce+f %.2f update %.2f | load+dots %.2f "
+                       "reduce+f %.2f update %.2f\n",
+                       sub[0] / nsub / 1e3, sub[1] / nsub / 1e3, sub[2] / nsub / 1e3, sub[3] / nsub / 1e3,
+                       sub[4] / nsub / 1e3, sub[5] / nsub / 1e3);
+        if (cnt)
+          std::fprintf(stderr,
+                       "[lra] geqp3_df m=%lld n=%lld pivots=%lld us/pivot %.2f: vs-load %.2f reflector %.2f scale %.2f "
+                       "columns %.2f downdate %.2f publish %.2f barrier %.2f write-back+pivot %.2f\n",
+                       (long long)m, (long long)n, (long long)cnt, cyc / cnt / 1e3, ph[0] / cnt / 1e3,
+                       ph[1] / cnt / 1e3, ph[2] / cnt / 1e3, ph[3] / cnt / 1e3, ph[4] / cnt / 1e3, ph[5] / cnt / 1e3,
+                       ph[6] / cnt / 1e3,
+                       (cyc - ph[0] - ph[1] - ph[2] - ph[3] - ph[4] - ph[5] - ph[6]) / cnt / 1e3);
+      }
       df_join_kernel<<<gm, 256, 0, ctx->stream>>>(m, n, Bh, Bl, m, scale, reinterpret_cast<double*>(A), lda);
       post_launch(ctx, "df_join_kernel");
     } else {

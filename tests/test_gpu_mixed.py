@@ -70,7 +70,7 @@ def test_idfact_mixed_parity(lra, oracle, trans):
     assert V.k == ref["k"]
     Aop = A if trans == "n" else A.T
     M = Aop.shape[0]
-    # the final step's sketch, to judge near-ties
+    # the final step's sketch, to assess near-ties
     off = sum((32 * 2 ** t + 8) * M for t in range(V.nsteps - 1))
     order = 32 * 2 ** (V.nsteps - 1) + 8
     B = g[off:off + order * M].reshape((order, M), order="F") @ Aop
