@@ -44,6 +44,10 @@ def parse():
     ap.add_argument("--rtol", type=float, default=1e-10)
     ap.add_argument("--no-fp64-leg", action="store_true")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--serve-requests", type=int, default=64,
+                    help="requests per precision in the serving measurement (0: skip)")
+    ap.add_argument("--batch", type=int, default=256,
+                    help="kernel matrices per precision in the batched measurement (0: skip)")
     return ap.parse_args()
 
 
@@ -88,6 +92,94 @@ def sketch_orders(k, nb=32):
             return orders, ks
         ks.append(nt)
         nt *= 2
+
+
+def serving_workload(count: int, seed: int = 5):
+    """Requests shaped like the serving config, scaled to a bounded sample:
+    70 % idfact / 30 % psvdfact, m and n log-uniform in [256, 4096], F32 / F64
+    half and half, s_i = 10^(-(i-1)/r) with r ~ U[20, 200], rtol 1e-6 (F32)
+    and 1e-10 (F64).  A = (G1 diag(s)) G2' from Gaussian G1, G2 on the GPU."""
+    import torch
+    rng = np.random.default_rng(seed)
+    out = []
+    for i in range(count):
+        m, n = (int(round(np.exp(rng.uniform(np.log(256), np.log(4096))))) for _ in range(2))
+        dt = torch.float64 if rng.random() < 0.5 else torch.float32
+        kind = "idfact" if rng.random() < 0.7 else "psvdfact"
+        r = rng.uniform(20, 200)
+        k = min(m, n)
+        g = torch.Generator(device="cuda").manual_seed(int(rng.integers(1 << 31)))
+        G1 = torch.randn(m, k, generator=g, device="cuda", dtype=torch.float64) / np.sqrt(m)
+        G2 = torch.randn(n, k, generator=g, device="cuda", dtype=torch.float64) / np.sqrt(n)
+        sv = torch.pow(10.0, -torch.arange(k, dtype=torch.float64, device="cuda") / r)
+        A = ((G1 * sv[None, :]) @ G2.T).to(dt).t().contiguous().t()
+        out.append((kind, A, 1e-10 if dt == torch.float64 else 1e-6))
+    return out
+
+
+def kernel_matrices(count: int, seed: int = 4):
+    """Batched config sample: K(x, y) = 1 / (1 + |x - y|^2) between x ~ U[0,1]^2 and
+    y ~ U[1.5,2.5] x U[0,1] (gap 0.5 in x1), m, n ~ U{128..2048}, Float64."""
+    import torch
+    rng = np.random.default_rng(seed)
+    out = []
+    for _ in range(count):
+        m, n = int(rng.integers(128, 2049)), int(rng.integers(128, 2049))
+        x = rng.uniform(0, 1, (m, 2))
+        y = np.column_stack([rng.uniform(1.5, 2.5, n), rng.uniform(0, 1, n)])
+        d2 = ((x[:, None, :] - y[None, :, :]) ** 2).sum(-1)
+        out.append(torch.from_numpy(np.asfortranarray(1.0 / (1.0 + d2))).cuda().t().contiguous().t())
+    return out
+
+
+def measure_serving(lra, work, precision: str, slots: int = 8):
+    """Poisson arrivals at about 80 % of the rate the server sustains when the
+    requests arrive all at once; p50 / p99 of submit -> done."""
+    import torch
+    opts = [lra.LRAOptions(np.float64 if A.dtype == torch.float64 else np.float32, rtol=rt,
+                           precision=precision, seed=11 + i) for i, (_, A, rt) in enumerate(work)]
+    srv = lra.Server(slots=slots, hbm_budget_bytes=150 << 30)
+    try:
+        t0 = time.perf_counter()
+        ts = [srv.submit(kind, A, o) for (kind, A, _), o in zip(work, opts)]
+        for t in ts:
+            srv.result(t)
+        burst = len(work) / (time.perf_counter() - t0)
+    finally:
+        srv.close()
+    rate = 0.8 * burst
+    gaps = np.random.default_rng(9).exponential(1.0 / rate, len(work))
+    srv = lra.Server(slots=slots, hbm_budget_bytes=150 << 30)
+    try:
+        t0 = time.perf_counter()
+        ts = []
+        due = t0
+        for (kind, A, _), o, gap in zip(work, opts, gaps):
+            due += gap
+            while time.perf_counter() < due:
+                time.sleep(min(1e-3, max(0.0, due - time.perf_counter())))
+            ts.append(srv.submit(kind, A, o))
+        for t in ts:
+            srv.result(t)
+        wall = time.perf_counter() - t0
+        st = srv.stats()
+    finally:
+        srv.close()
+    return {"requests": len(work), "slots": slots, "arrival_rate_per_s": rate, "matrices_s": len(work) / wall,
+            "p50_ms": st["p50_ms"], "p99_ms": st["p99_ms"], "burst_matrices_s": burst}
+
+
+def measure_batched(lra, mats, precision: str, ctx):
+    """lra_idfact_batched over the kernel matrices (rtol 1e-10)."""
+    import torch
+    o = lra.LRAOptions(rtol=1e-10, precision=precision, seed=3)
+    lra.idfact_batched(mats[:4], o, ctx=ctx)  # warm-up
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    Vs = lra.idfact_batched(mats, o, ctx=ctx)
+    torch.cuda.synchronize()
+    el = time.perf_counter() - t0
+    return {"matrices": len(mats), "matrices_s": len(mats) / el, "mean_rank": float(np.mean([V.k for V in Vs]))}
 
 
 class Clocks:
@@ -332,6 +424,30 @@ def main():
             cpu = {"value": None, "unit": "matrices/s", "cores": os.cpu_count(), "kind": "port",
                    "sample": f"failed: {e}"}
 
+    # ---- serving loop and batched idfact (bounded samples of those configs) ------------
+    serving, batched = None, None
+    if rank == 0 and args.serve_requests > 0:
+        try:
+            work = serving_workload(args.serve_requests)
+            serving = {"mixed": measure_serving(lra, work, "mixed"),
+                       "native": measure_serving(lra, work, "native"),
+                       "sample": f"{args.serve_requests} requests: 70% idfact / 30% psvdfact, m, n log-uniform "
+                                 "[256, 4096], F32/F64 half each, rtol 1e-6 / 1e-10, Poisson arrivals at 80% "
+                                 "of the burst rate, 8 slots, 150 GB budget"}
+            del work
+        except Exception as e:  # pragma: no cover
+            serving = {"failed": str(e)}
+    if rank == 0 and args.batch > 0:
+        try:
+            mats = kernel_matrices(args.batch)
+            batched = {"mixed": measure_batched(lra, mats, "mixed", ctx),
+                       "native": measure_batched(lra, mats, "native", ctx),
+                       "sample": f"{args.batch} kernel matrices 1/(1+|x-y|^2), m, n ~ U{{128..2048}}, F64, "
+                                 "rtol 1e-10, lra_idfact_batched"}
+            del mats
+        except Exception as e:  # pragma: no cover
+            batched = {"failed": str(e)}
+
     if rank == 0:
         per_ms = sorted(1e3 * p for p in per)
         line = {
@@ -346,7 +462,7 @@ def main():
             "rank": k, "rel_spectral_err": err / nrm,
             "e2e": {"value": e2e_val, "unit": "matrices/s", "h2d_bytes_per_step": h2d,
                     "d2h_bytes_per_step": d2h},
-            "fp64_path": fp64,
+            "fp64_path": fp64, "serving": serving, "batched": batched,
             "roofline": roof, "roofline_sketch": roof_sketch, "cpu_baseline": cpu, "clocks": clk, "gpu_launches": launches,
         }
         print(json.dumps(line), flush=True)

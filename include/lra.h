@@ -302,12 +302,72 @@ int lra_snormdiff_psvd(lra_ctx* ctx, int dtype, int64_t m, int64_t n,
 
 /* ---- batches of independent matrices ---------------------------------------- */
 
-/* idfact over `count` matrices of uneven sizes, grouped on one stream.
-   outs[i] receives matrix i's IDPackedV.  rand may be NULL or an array of
-   `count` streams.                                                         */
+/* idfact over `count` matrices of uneven sizes (many independent idfact
+   calls, src/id.jl:434-450).  The matrices are spread over up to eight
+   worker streams of a private server (below), so that their work overlaps
+   on the device; outs[i] receives matrix i's IDPackedV, identical to a
+   single lra_idfact call on it.  rand may be NULL or an array of `count`
+   streams.                                                                 */
 int lra_idfact_batched(lra_ctx* ctx, int dtype, int64_t count,
                        const lra_matdesc* mats, const lra_opts* opts,
                        const lra_rand* rand, lra_id** outs);
+
+/* ---- serving loop (continuous batching) --------------------------------------
+   No counterpart in the reference, which factors one matrix per call.  A
+   server owns `slots` workers (host thread + context + stream each) on one
+   device.  Submitted requests are admitted in arrival order as soon as a
+   slot is free and their estimated device memory fits `hbm_budget_bytes`
+   beside the requests already running; admitted requests run concurrently.
+   Each request runs as a fresh idfact / psvdfact call (the in-library
+   generator restarts from opts.seed), so its result is the same whichever
+   slot runs it and whatever runs beside it.  A request's A and rand must
+   stay valid until its result has been polled.                             */
+typedef struct lra_server lra_server;
+
+enum { LRA_REQ_IDFACT = 0, LRA_REQ_PSVDFACT = 1 };
+
+typedef struct lra_request {
+  int32_t kind;          /* LRA_REQ_* */
+  int32_t dtype;         /* LRA_F32 / LRA_F64 */
+  char trans;            /* idfact: 'n' or 'c' (0 means 'n') */
+  char _pad[7];
+  int64_t m, n, lda;
+  const void* A;         /* host or device, column-major */
+  lra_opts opts;
+  const lra_rand* rand;  /* optional injected randomness */
+} lra_request;
+
+typedef struct lra_result {
+  int32_t kind;          /* LRA_REQ_* of the request */
+  int32_t status;        /* LRA_* status of the factorization */
+  lra_id* id;            /* LRA_REQ_IDFACT: free with lra_id_free */
+  lra_psvd* psvd;        /* LRA_REQ_PSVDFACT: free with lra_psvd_free */
+  double queue_ms;       /* submit -> start */
+  double run_ms;         /* start -> done */
+  double total_ms;       /* submit -> done */
+  int32_t slot;
+  int32_t _pad;
+  char error[160];       /* lra_last_error text when status != LRA_OK */
+} lra_result;
+
+typedef struct lra_server_stats {
+  int64_t submitted, completed, rejected, in_flight, queued;
+  double p50_ms, p99_ms, mean_ms;  /* submit -> done, completed requests */
+  double matrices_per_s;           /* completed / (last done - first submit) */
+  int64_t hbm_budget, hbm_in_use;  /* bytes, by the admission estimates */
+} lra_server_stats;
+
+int lra_server_create(int device, int slots, int64_t hbm_budget_bytes,
+                      lra_server** out);
+/* LRA_ENOMEM (and nothing queued) when the request alone exceeds the budget */
+int lra_server_submit(lra_server* s, const lra_request* req, uint64_t* ticket);
+/* wait_ms < 0 waits for completion, 0 only checks.  LRA_OK: done, *out
+   filled and the ticket released; LRA_EBUSY: not done yet.                 */
+int lra_server_poll(lra_server* s, uint64_t ticket, int64_t wait_ms,
+                    lra_result* out);
+int lra_server_get_stats(lra_server* s, lra_server_stats* out);
+/* running requests finish, queued ones are dropped, unpolled results freed */
+void lra_server_destroy(lra_server* s);
 
 /* ---- freeing ---------------------------------------------------------------- */
 void lra_id_free(lra_id* r);

@@ -1690,24 +1690,6 @@ int lra_snormdiff_psvd(lra_ctx* ctx, int dtype, int64_t m, int64_t n, const void
   });
 }
 
-int lra_idfact_batched(lra_ctx* ctx, int dtype, int64_t count, const lra_matdesc* mats, const lra_opts* opts,
-                       const lra_rand* rand, lra_id** outs) {
-  if (!ctx || !mats || !outs || count < 0) return LRA_EINVAL;
-  for (int64_t i = 0; i < count; ++i) outs[i] = nullptr;
-  for (int64_t i = 0; i < count; ++i) {
-    const int st = lra_idfact(ctx, dtype, 'n', mats[i].m, mats[i].n, mats[i].A, mats[i].lda, opts,
-                              rand ? rand + i : nullptr, outs + i);
-    if (st != LRA_OK) {
-      for (int64_t j = 0; j < i; ++j) {
-        lra_id_free(outs[j]);
-        outs[j] = nullptr;
-      }
-      return st;
-    }
-  }
-  return LRA_OK;
-}
-
 void lra_id_free(lra_id* r) {
   if (!r) return;
   hfree(r->sk);

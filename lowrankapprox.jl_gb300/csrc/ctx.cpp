@@ -34,6 +34,13 @@ void post_launch(lra_ctx* ctx, const char* name) {
 
 static constexpr size_t kAlign = 256;
 
+void Arena::free_all(cudaStream_t stream) {
+  cudaStreamSynchronize(stream);
+  for (auto& c : chunks_) cudaFree(c.base);
+  chunks_.clear();
+  cur_ = 0;
+}
+
 Arena::~Arena() {
   for (auto& c : chunks_) cudaFree(c.base);
 }
@@ -102,6 +109,17 @@ size_t Arena::capacity() const {
   size_t s = 0;
   for (auto& c : chunks_) s += c.cap;
   return s;
+}
+
+void raise_smem_limit(lra_ctx* ctx, const void* kernel) {
+  int optin = 0;
+  check_cuda(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, ctx->device),
+             "cudaDeviceGetAttribute(MaxSharedMemoryPerBlockOptin)");
+  cudaFuncAttributes fa;
+  check_cuda(cudaFuncGetAttributes(&fa, kernel), "cudaFuncGetAttributes");
+  check_cuda(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                  optin - (int)fa.sharedSizeBytes),
+             "cudaFuncSetAttribute(MaxDynamicSharedMemorySize)");
 }
 
 bool trace_on() {

@@ -827,9 +827,9 @@ void jacobi_svd(lra_ctx* ctx, int64_t n, T* X, int64_t ldx, T* V, int64_t ldv, T
   if (n <= 0) return;
   set_identity(ctx, n, n, V, ldv);
   const ArenaMark mk = ctx->arena.mark();
-  // FP32: 16-column blocks (half the grid barriers per sweep) when two
-  // block columns of X and V fit shared memory, else 8
-  const int jbt = (size_t)4 * 16 * n * sizeof(float) <= 200 * 1024 ? 16 : 8;
+  // FP32: 8-column blocks (16-column blocks halve the grid barriers but
+  // measured slower: the local sweeps become issue-bound on half the SMs)
+  const int jbt = 8;
   const size_t blk_smem = (size_t)4 * jbt * n * sizeof(float);
   const bool block = !pair_cta && n >= 4 * jbt && blk_smem <= 200 * 1024;
   const void* kern = pair_cta ? (const void*)jacobi_pair_kernel<T, NT>
@@ -838,7 +838,7 @@ void jacobi_svd(lra_ctx* ctx, int64_t n, T* X, int64_t ldx, T* V, int64_t ldv, T
                                        : (const void*)jacobi_kernel<T, NT>);
   const int nt = block ? jbt * 32 : NT;
   const size_t smem = block ? blk_smem : 0;
-  if (block) LRA_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  if (block) raise_smem_limit(ctx, (const void*)kern);
   int per_sm = 0;
   LRA_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, nt, smem));
   const int64_t pairs = (n + 1) / 2;
@@ -890,7 +890,7 @@ bool jacobi_svd_df(lra_ctx* ctx, int64_t n, double* X, int64_t ldx, double* V, i
   if (n < 2 || n > 32 * JB_RPL) return false;
   const size_t smem = (size_t)8 * JDF * n * sizeof(float);
   if (smem > 200 * 1024) return false;
-  LRA_CUDA(cudaFuncSetAttribute(jacobi_block_df_kernel<JDF>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  raise_smem_limit(ctx, (const void*)jacobi_block_df_kernel<JDF>);
   int per_sm = 0;
   LRA_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, jacobi_block_df_kernel<JDF>, JDF * 32, smem));
   if (per_sm < 1) return false;

@@ -43,6 +43,8 @@ class Arena {
   void release(ArenaMark m);
   // start of a call: merge chunks (synchronizes the stream first)
   void reset(cudaStream_t stream);
+  // give every chunk back to the device (synchronizes the stream first)
+  void free_all(cudaStream_t stream);
   size_t capacity() const;
 
  private:
@@ -104,6 +106,12 @@ void tc_split(lra_ctx* ctx, char trans, int64_t M, int64_t N, const T* A, int64_
 // (ld = order) with entries on the 1/32 lattice.
 template <typename T>
 void tc_sketch(lra_ctx* ctx, const TcSplit& sp, int64_t order, const T* S, T* B, int64_t ldb);
+
+// Raises a kernel's dynamic shared memory limit to the most the device
+// allows beside its static shared memory.  Always the same value per kernel:
+// the attribute is global to the kernel, and a per-call value set by one
+// host thread could undercut another thread's launch in between.
+void raise_smem_limit(lra_ctx* ctx, const void* kernel);
 
 // LRA_TRACE=1 in the environment: iteration counts of the iterative
 // kernels (Jacobi sweeps, pivots) on stderr.

@@ -1443,8 +1443,7 @@ int64_t geqp3_adap(lra_ctx* ctx, int64_t m, int64_t n, T* A, int64_t lda, int64_
   // the reflector of each pivot is staged in shared memory when it fits
   const int64_t vcap = std::min<int64_t>(m, (int64_t)(160 * 1024 / sizeof(T)));
   const size_t dyn_smem = (size_t)vcap * sizeof(T);
-  LRA_CUDA(cudaFuncSetAttribute(geqp3_kernel<T, NT>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                (int)std::max<size_t>(dyn_smem, 1)));
+  raise_smem_limit(ctx, (const void*)geqp3_kernel<T, NT>);
   int per_sm = 0;
   LRA_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, geqp3_kernel<T, NT>, NT, dyn_smem));
   if (per_sm < 1) fail(LRA_ECUDA, "geqp3 kernel cannot be resident");
@@ -1494,8 +1493,7 @@ int64_t geqp3_adap(lra_ctx* ctx, int64_t m, int64_t n, T* A, int64_t lda, int64_
   const size_t smem2 = dyn_smem + (size_t)nslot * (3 * sizeof(T) + 1);
   const bool v2 = (m - 1) <= vcap && smem2 <= 200 * 1024;
   if (v2) {
-    LRA_CUDA(cudaFuncSetAttribute(geqp3_v2_kernel<T, NT>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                  (int)smem2));
+    raise_smem_limit(ctx, (const void*)geqp3_v2_kernel<T, NT>);
     LRA_CUDA(cudaFuncSetAttribute(geqp3_v2_kernel<T, NT>, cudaFuncAttributePreferredSharedMemoryCarveout,
                                   cudaSharedmemCarveoutMaxL1));
     int per_sm2 = 0;
@@ -1537,7 +1535,7 @@ int64_t geqp3_adap(lra_ctx* ctx, int64_t m, int64_t n, T* A, int64_t lda, int64_
       QrParams<double> Pd;
       std::memcpy(&Pd, &P, sizeof(Pd));
       Pd.lda = m;
-      LRA_CUDA(cudaFuncSetAttribute(geqp3_df_kernel<NT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem2));
+      raise_smem_limit(ctx, (const void*)geqp3_df_kernel<NT>);
       // as much L1 as the shared memory leaves: the warps' columns live there
       LRA_CUDA(cudaFuncSetAttribute(geqp3_df_kernel<NT>, cudaFuncAttributePreferredSharedMemoryCarveout,
                                     cudaSharedmemCarveoutMaxL1));
@@ -1599,8 +1597,7 @@ int64_t geqp3_adap(lra_ctx* ctx, int64_t m, int64_t n, T* A, int64_t lda, int64_
       // xLAQPS's swaps, replayed: jpvt and the column order of A
       if (n <= 24576) {
         const size_t rs = (size_t)2 * n * sizeof(int);
-        LRA_CUDA(cudaFuncSetAttribute(geqp3_replay_smem_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                      (int)std::max<size_t>(rs, 1)));
+        raise_smem_limit(ctx, (const void*)geqp3_replay_smem_kernel);
         geqp3_replay_smem_kernel<<<1, 1024, rs, ctx->stream>>>(n, X.piv, X.nfac, col_at);
         post_launch(ctx, "geqp3_replay_smem_kernel");
       } else {
@@ -1744,8 +1741,7 @@ int64_t geqp3_adap_noalloc(lra_ctx* ctx, int64_t m, int64_t n, T* A, int64_t lda
   unsigned char* base = static_cast<unsigned char*>(noalloc_scratch(ctx->device));
   const int64_t vcap = std::min<int64_t>(m, (int64_t)(160 * 1024 / sizeof(T)));
   const size_t dyn_smem = (size_t)vcap * sizeof(T);
-  LRA_CUDA(cudaFuncSetAttribute(geqp3_kernel<T, NT>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                (int)std::max<size_t>(dyn_smem, 1)));
+  raise_smem_limit(ctx, (const void*)geqp3_kernel<T, NT>);
   int per_sm = 0;
   LRA_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, geqp3_kernel<T, NT>, NT, dyn_smem));
   if (per_sm < 1) fail(LRA_ECUDA, "geqp3 kernel cannot be resident");

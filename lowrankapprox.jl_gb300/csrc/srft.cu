@@ -177,7 +177,7 @@ bool srft_sketch_fft(lra_ctx* ctx, char trans, int64_t M, int64_t N, const T* A,
   cis_table_kernel<T><<<g1, 256, 0, ctx->stream>>>(M, tw_M);
   post_launch(ctx, "cis_table_kernel");
   const size_t smem = per * kcp;
-  LRA_CUDA(cudaFuncSetAttribute(srft_fft_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  raise_smem_limit(ctx, (const void*)srft_fft_kernel<T>);
   const unsigned grid = (unsigned)std::min<int64_t>(N, (int64_t)ctx->num_sms * 8);
   srft_fft_kernel<T><<<grid, SRFT_NT, smem, ctx->stream>>>(M, N, X, ldx, d, idx, order, lbits, (int)kcp, tw_l,
                                                            tw_M, B, ldb);

@@ -32,6 +32,7 @@
 #include <cudaTypedefs.h>
 
 #include <algorithm>
+#include <atomic>
 #include <cfloat>
 #include <cstring>
 
@@ -761,16 +762,19 @@ __global__ void tc_gemm_reduce_kernel(int64_t m, int64_t n, int64_t nsplit, cons
 }
 
 PFN_cuTensorMapEncodeTiled_v12000 encode_fn() {
-  static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
-  if (!fn) {
+  // looked up once per process, safely under concurrent first calls
+  static std::atomic<PFN_cuTensorMapEncodeTiled_v12000> fn{nullptr};
+  PFN_cuTensorMapEncodeTiled_v12000 f = fn.load(std::memory_order_acquire);
+  if (!f) {
     cudaDriverEntryPointQueryResult q;
     void* p = nullptr;
     check_cuda(cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q),
                "cudaGetDriverEntryPoint(cuTensorMapEncodeTiled)");
     if (q != cudaDriverEntryPointSuccess || !p) fail(LRA_ECUDA, "cuTensorMapEncodeTiled unavailable");
-    fn = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(p);
+    f = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(p);
+    fn.store(f, std::memory_order_release);
   }
-  return fn;
+  return f;
 }
 
 void make_map(CUtensorMap* m, void* ptr, int rank, const cuuint64_t* dims, const cuuint64_t* strides,
@@ -874,7 +878,7 @@ void tc_sketch(lra_ctx* ctx, const TcSplit& sp, int64_t order, const T* S, T* B,
   P.out_double = sizeof(T) == 8 ? 1 : 0;
   P.err = err;
   const size_t smem = 1024 + (size_t)NSTAGE * (S_BYTES + ns * TILE_BYTES) + 256;
-  LRA_CUDA(cudaFuncSetAttribute(tc_sketch_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  raise_smem_limit(ctx, (const void*)tc_sketch_kernel);
   const int64_t ntiles = ((N + TILE_M - 1) / TILE_M) * (Lp / TILE_N);
   tc_sketch_kernel<<<(unsigned)ntiles, NTHREADS, smem, ctx->stream>>>(tmA, tmS, P);
   post_launch(ctx, "tc_sketch_kernel");
@@ -949,7 +953,7 @@ void tc_gemm(lra_ctx* ctx, char ta, char tb, int64_t m, int64_t n, int64_t k, do
     P.to_ws = 0;
   }
   const size_t smem = 1024 + (size_t)G_STAGE + 256;
-  LRA_CUDA(cudaFuncSetAttribute(tc_gemm_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  raise_smem_limit(ctx, (const void*)tc_gemm_kernel);
   tc_gemm_kernel<<<dim3((unsigned)tiles, (unsigned)nsplit), NTHREADS, smem, ctx->stream>>>(tmA, tmB, P);
   post_launch(ctx, "tc_gemm_kernel");
   if (nsplit > 1) {

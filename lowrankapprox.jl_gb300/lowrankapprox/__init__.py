@@ -26,7 +26,7 @@ __all__ = [
     "PartialHermitianEigen", "CURPackedU", "idfact", "id", "pqrfact", "pqr", "psvdfact", "psvdvals",
     "psvd", "pheigfact", "pheigvals", "pheig", "curfact", "cur", "sketch", "sketchfact", "snorm",
     "snormdiff", "geqp3_adap", "matrixlib", "LRAError", "ArgumentError", "DimensionMismatch",
-    "lattice_gauss", "default_context",
+    "lattice_gauss", "default_context", "Server", "idfact_batched",
 ]
 
 
@@ -425,6 +425,38 @@ def idfact(*args, **kwargs) -> IDPackedV:
         lib.lra_id_free(out)
 
 
+def idfact_batched(mats, opts: LRAOptions | None = None, rands=None, ctx: "Context | None" = None):
+    """idfact of many independent matrices of one element type
+    (lra_idfact_batched): their work overlaps on the device; each result is
+    identical to an idfact call on that matrix."""
+    ctx = ctx or default_context()
+    Ms = [_mat(A) for A in mats]
+    if not Ms:
+        return []
+    if len({M.dtype for M in Ms}) != 1:
+        raise ArgumentError(_ffi.LRA_EINVAL, "idfact_batched needs one element type")
+    opts = opts or LRAOptions(Ms[0].np_dtype)
+    lib = _ffi.load()
+    arr = (_ffi.lra_matdesc * len(Ms))(*[_ffi.lra_matdesc(M.m, M.n, M.ld, M.ptr) for M in Ms])
+    outs = (C.POINTER(_ffi.lra_id) * len(Ms))()
+    rarr = None
+    if rands is not None:
+        rarr = (_ffi.lra_rand * len(Ms))(*[r.c for r in rands])
+    co = opts.to_c()
+    st = lib.lra_idfact_batched(ctx.handle, Ms[0].dtype, len(Ms), arr, C.byref(co), rarr, outs)
+    _raise(st, ctx)
+    res = []
+    for M, p in zip(Ms, outs):
+        r = p.contents
+        try:
+            k, n = r.k, r.n
+            res.append(IDPackedV(_host(_iptr(r.sk), (k,), np.int64), _host(_iptr(r.rd), (n - k,), np.int64),
+                                 _host(r.T, (k, n - k), M.np_dtype), r.nsteps))
+        finally:
+            lib.lra_id_free(p)
+    return res
+
+
 def id(*args, **kwargs):
     V = idfact(*args, **kwargs)
     return V.sk, V.rd, V.T
@@ -543,6 +575,92 @@ def _psvd(A, opts, kwargs, vals_only):
         return PartialSVD(U, S, Vt)
     finally:
         lib.lra_psvd_free(out)
+
+
+class Server:
+    """Serving loop (lra_server_*): continuous batching of idfact / psvdfact
+    requests over `slots` worker streams under an HBM budget.  No
+    counterpart in the reference.  submit() returns a ticket; result()
+    waits for it and returns an IDPackedV or PartialSVD."""
+
+    def __init__(self, slots: int = 4, hbm_budget_bytes: int = 64 << 30, device: int = 0):
+        lib = _ffi.load()
+        h = C.c_void_p()
+        st = lib.lra_server_create(int(device), int(slots), int(hbm_budget_bytes), C.byref(h))
+        if st != _ffi.LRA_OK:
+            raise LRAError(st, f"lra_server_create: {lib.lra_status_string(st).decode()}")
+        self.handle = h
+        self._keep = {}
+
+    def submit(self, kind: str, A, opts: LRAOptions | None = None, rand: "RandStream | None" = None,
+               trans: str = "n") -> int:
+        M = _mat(A)
+        opts = opts or LRAOptions(M.np_dtype)
+        req = _ffi.lra_request()
+        req.kind = {"idfact": _ffi.LRA_REQ_IDFACT, "psvdfact": _ffi.LRA_REQ_PSVDFACT}[kind]
+        req.dtype = M.dtype
+        req.trans = trans.encode()
+        req.m, req.n, req.lda = M.m, M.n, M.ld
+        req.A = M.ptr
+        req.opts = opts.to_c()
+        if rand is not None:
+            req.rand = C.pointer(rand.c)
+        t = C.c_uint64()
+        st = _ffi.load().lra_server_submit(self.handle, C.byref(req), C.byref(t))
+        if st != _ffi.LRA_OK:
+            raise LRAError(st, f"lra_server_submit: {_ffi.load().lra_status_string(st).decode()}")
+        # the input and the random streams must outlive the request
+        self._keep[t.value] = (M, rand, req, kind)
+        return t.value
+
+    def result(self, ticket: int, wait_ms: int = -1):
+        """The factorization of `ticket` (None if not done within wait_ms),
+        with .queue_ms / .run_ms / .total_ms / .slot attached."""
+        lib = _ffi.load()
+        res = _ffi.lra_result()
+        st = lib.lra_server_poll(self.handle, C.c_uint64(ticket), int(wait_ms), C.byref(res))
+        if st == _ffi.LRA_EBUSY:
+            return None
+        if st != _ffi.LRA_OK:
+            raise LRAError(st, "lra_server_poll: unknown ticket")
+        M, rand, req, kind = self._keep.pop(ticket)
+        try:
+            if res.status != _ffi.LRA_OK:
+                raise LRAError(res.status, f"{kind} in the server: {res.error.decode(errors='replace')}")
+            if kind == "idfact":
+                r = res.id.contents
+                k, n = r.k, r.n
+                out = IDPackedV(_host(_iptr(r.sk), (k,), np.int64), _host(_iptr(r.rd), (n - k,), np.int64),
+                                _host(r.T, (k, n - k), M.np_dtype), r.nsteps)
+            else:
+                r = res.psvd.contents
+                k = r.k
+                out = PartialSVD(_host(r.U, (M.m, k), M.np_dtype), _host(r.S, (k,), M.np_dtype),
+                                 _host(r.Vt, (k, M.n), M.np_dtype))
+        finally:
+            if res.id:
+                lib.lra_id_free(res.id)
+            if res.psvd:
+                lib.lra_psvd_free(res.psvd)
+        out.queue_ms, out.run_ms, out.total_ms, out.slot = res.queue_ms, res.run_ms, res.total_ms, res.slot
+        return out
+
+    def stats(self) -> dict:
+        s = _ffi.lra_server_stats()
+        _ffi.load().lra_server_get_stats(self.handle, C.byref(s))
+        return {f: getattr(s, f) for f, _ in s._fields_}
+
+    def close(self):
+        if getattr(self, "handle", None):
+            _ffi.load().lra_server_destroy(self.handle)
+            self.handle = None
+            self._keep.clear()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
 
 
 def psvdfact(A, opts: LRAOptions | None = None, **kwargs) -> PartialSVD:

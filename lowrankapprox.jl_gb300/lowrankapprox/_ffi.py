@@ -79,6 +79,29 @@ class lra_matdesc(C.Structure):
     _fields_ = [("m", C.c_int64), ("n", C.c_int64), ("lda", C.c_int64), ("A", C.c_void_p)]
 
 
+LRA_REQ_IDFACT, LRA_REQ_PSVDFACT = 0, 1
+
+
+class lra_request(C.Structure):
+    _fields_ = [("kind", C.c_int32), ("dtype", C.c_int32), ("trans", C.c_char), ("_pad", C.c_char * 7),
+                ("m", C.c_int64), ("n", C.c_int64), ("lda", C.c_int64), ("A", C.c_void_p),
+                ("opts", lra_opts), ("rand", C.POINTER(lra_rand))]
+
+
+class lra_result(C.Structure):
+    _fields_ = [("kind", C.c_int32), ("status", C.c_int32), ("id", C.POINTER(lra_id)),
+                ("psvd", C.POINTER(lra_psvd)), ("queue_ms", C.c_double), ("run_ms", C.c_double),
+                ("total_ms", C.c_double), ("slot", C.c_int32), ("_pad", C.c_int32),
+                ("error", C.c_char * 160)]
+
+
+class lra_server_stats(C.Structure):
+    _fields_ = [("submitted", C.c_int64), ("completed", C.c_int64), ("rejected", C.c_int64),
+                ("in_flight", C.c_int64), ("queued", C.c_int64), ("p50_ms", C.c_double),
+                ("p99_ms", C.c_double), ("mean_ms", C.c_double), ("matrices_per_s", C.c_double),
+                ("hbm_budget", C.c_int64), ("hbm_in_use", C.c_int64)]
+
+
 # every exported entry point: (name, restype, argtypes)
 _vp, _i64, _i32, _d, _ch = C.c_void_p, C.c_int64, C.c_int, C.c_double, C.c_char
 _P = C.POINTER
@@ -120,6 +143,11 @@ SIGNATURES = [
                                   _P(lra_rand), _P(_d)]),
     ("lra_idfact_batched", _i32, [_vp, _i32, _i64, _P(lra_matdesc), _P(lra_opts), _P(lra_rand),
                                   _P(_P(lra_id))]),
+    ("lra_server_create", _i32, [_i32, _i32, _i64, _P(_vp)]),
+    ("lra_server_submit", _i32, [_vp, _P(lra_request), _P(C.c_uint64)]),
+    ("lra_server_poll", _i32, [_vp, C.c_uint64, _i64, _P(lra_result)]),
+    ("lra_server_get_stats", _i32, [_vp, _P(lra_server_stats)]),
+    ("lra_server_destroy", None, [_vp]),
     ("lra_id_free", None, [_P(lra_id)]),
     ("lra_pqr_free", None, [_P(lra_pqr)]),
     ("lra_psvd_free", None, [_P(lra_psvd)]),

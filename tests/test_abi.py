@@ -43,14 +43,18 @@ def test_struct_layout_matches_header(tmp_path):
     import lowrankapprox._ffi as F
     src = tmp_path / "sz.c"
     src.write_text('#include <stdio.h>\n#include <stddef.h>\n#include "lra.h"\n'
-                   'int main(void){printf("%zu %zu %zu %zu %zu %zu %zu %zu %zu\\n", sizeof(lra_opts),'
+                   'int main(void){printf("%zu %zu %zu %zu %zu %zu %zu %zu %zu %zu %zu %zu %zu %zu\\n", sizeof(lra_opts),'
                    'sizeof(lra_rand), sizeof(lra_id), sizeof(lra_pqr), sizeof(lra_psvd), sizeof(lra_pheig),'
-                   'sizeof(lra_cur), sizeof(lra_matdesc), offsetof(lra_opts, seed)); return 0;}\n')
+                   'sizeof(lra_cur), sizeof(lra_matdesc), offsetof(lra_opts, seed), sizeof(lra_request),'
+                   'offsetof(lra_request, opts), offsetof(lra_request, rand), sizeof(lra_result),'
+                   'sizeof(lra_server_stats)); return 0;}\n')
     exe = tmp_path / "sz"
     subprocess.check_call(["gcc", "-I", os.path.join(ROOT, "include"), str(src), "-o", str(exe)])
     got = list(map(int, subprocess.check_output([str(exe)]).split()))
     want = [ctypes.sizeof(c) for c in (F.lra_opts, F.lra_rand, F.lra_id, F.lra_pqr, F.lra_psvd, F.lra_pheig,
-                                       F.lra_cur, F.lra_matdesc)] + [F.lra_opts.seed.offset]
+                                       F.lra_cur, F.lra_matdesc)] + [F.lra_opts.seed.offset] + \
+        [ctypes.sizeof(F.lra_request), F.lra_request.opts.offset, F.lra_request.rand.offset,
+         ctypes.sizeof(F.lra_result), ctypes.sizeof(F.lra_server_stats)]
     assert got == want
 
 
