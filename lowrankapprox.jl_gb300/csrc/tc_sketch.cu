@@ -325,8 +325,11 @@ __global__ void __launch_bounds__(NTHREADS, 1)
             }
           } else {
             const float tsc = t ? 1.0f : (1.0f / 256.0f);  // tail weight 2^(t-8)
+            // |tail| < 2^25 here: a 32-bit conversion is exact and stays off
+            // the FP64 pipe, which runs the 64-bit ones on this part
 #pragma unroll
-            for (int c = 0; c < 16; ++c) X[piece * 16 + c] += __float2ll_rn(__uint_as_float(r[c]) * tsc);
+            for (int c = 0; c < 16; ++c)
+              X[piece * 16 + c] += (long long)__float2int_rn(__uint_as_float(r[c]) * tsc);
           }
         }
       }

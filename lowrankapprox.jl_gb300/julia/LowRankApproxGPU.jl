@@ -37,6 +37,18 @@ struct lra_pqr;   dtype::Int32; retval::Int32; m::Int64; n::Int64; k::Int64; p::
 struct lra_psvd;  dtype::Int32; pad::Int32; m::Int64; n::Int64; k::Int64; U::Ptr{Cvoid}; S::Ptr{Cvoid}; Vt::Ptr{Cvoid}; end
 struct lra_pheig; dtype::Int32; pad::Int32; n::Int64; k::Int64; values::Ptr{Cvoid}; vectors::Ptr{Cvoid}; end
 struct lra_cur;   kind::Int32; pad::Int32; kr::Int64; kc::Int64; rows::Ptr{Int64}; cols::Ptr{Int64}; end
+struct lra_request
+  kind::Int32; dtype::Int32; trans::UInt8; pad::NTuple{7,UInt8}
+  m::Int64; n::Int64; lda::Int64; A::Ptr{Cvoid}; opts::lra_opts; rand::Ptr{lra_rand}
+end
+struct lra_result
+  kind::Int32; status::Int32; id::Ptr{lra_id}; psvd::Ptr{lra_psvd}
+  queue_ms::Float64; run_ms::Float64; total_ms::Float64; slot::Int32; pad::Int32; error::NTuple{160,UInt8}
+end
+struct lra_server_stats
+  submitted::Int64; completed::Int64; rejected::Int64; in_flight::Int64; queued::Int64
+  p50_ms::Float64; p99_ms::Float64; mean_ms::Float64; matrices_per_s::Float64; hbm_budget::Int64; hbm_in_use::Int64
+end
 
 const SKETCH = Dict(:none => 0, :randn => 1, :sprn => 2, :srft => 3, :sub => 4, :subs => 4)
 dtype(::Type{Float64}) = Int32(1)
@@ -213,6 +225,69 @@ function snormdiff(A::StridedMatrix{T}, B::StridedMatrix{T}, opts::Union{LRAOpti
              c.h, dtype(T), size(A,1), size(A,2), A, stride(A,2), B, stride(B,2), co, C_NULL, s)
   check(st, c)
   s[]
+end
+
+# ---- serving loop (lra_server_*; no counterpart in LowRankApprox.jl) ----------------
+"""
+    Server(; slots=8, hbm_budget=150 << 30, device=0)
+
+Continuous batching of idfact / psvdfact requests on one GPU: `submit` returns
+a ticket, `fetch(srv, t)` waits and returns the factorization.  Inputs stay
+referenced by the server until their result is fetched.
+"""
+mutable struct Server
+  h::Ptr{Cvoid}
+  keep::Dict{UInt64,Any}
+  function Server(; slots::Integer=8, hbm_budget::Integer=150 << 30, device::Integer=0)
+    r = Ref{Ptr{Cvoid}}(C_NULL)
+    st = ccall((:lra_server_create, liblra), Cint, (Cint, Cint, Int64, Ref{Ptr{Cvoid}}), device, slots,
+               hbm_budget, r)
+    st == 0 || error("lra_server_create failed with status $st")
+    s = new(r[], Dict{UInt64,Any}())
+    finalizer(x -> ccall((:lra_server_destroy, liblra), Cvoid, (Ptr{Cvoid},), x.h), s)
+  end
+end
+
+function submit(s::Server, kind::Symbol, A::StridedMatrix{T}, opts::Union{LRAOptions,Nothing}=nothing;
+                precision::Symbol=:native, trans::Symbol=:n, kw...) where T<:Union{Float32,Float64}
+  o = c_opts(opts_of(T, opts, kw); precision)
+  req = lra_request(kind == :psvdfact ? 1 : 0, dtype(T), UInt8(trans == :n ? 'n' : 'c'), ntuple(_ -> 0x0, 7),
+                    size(A,1), size(A,2), stride(A,2), Ptr{Cvoid}(pointer(A)), o, C_NULL)
+  t = Ref{UInt64}(0)
+  st = ccall((:lra_server_submit, liblra), Cint, (Ptr{Cvoid}, Ref{lra_request}, Ref{UInt64}), s.h, req, t)
+  st == 0 || error("lra_server_submit failed with status $st")
+  s.keep[t[]] = (A, T, kind)
+  t[]
+end
+
+function Base.fetch(s::Server, t::UInt64)
+  res = Ref{lra_result}()
+  st = ccall((:lra_server_poll, liblra), Cint, (Ptr{Cvoid}, UInt64, Int64, Ref{lra_result}), s.h, t, -1, res)
+  st == 0 || error("lra_server_poll failed with status $st")
+  A, T, kind = pop!(s.keep, t)
+  r = res[]
+  r.status == 0 || error(unsafe_string(pointer(collect(r.error))))
+  if kind == :psvdfact
+    p = unsafe_load(r.psvd)
+    try
+      return PartialSVD(takem(p.U, T, p.m, p.k), take(Ptr{T}(p.S), p.k), takem(p.Vt, T, p.k, p.n))
+    finally
+      ccall((:lra_psvd_free, liblra), Cvoid, (Ptr{lra_psvd},), r.psvd)
+    end
+  else
+    v = unsafe_load(r.id)
+    try
+      return IDPackedV(take(v.sk, v.k), take(v.rd, v.n - v.k), takem(v.T, T, v.k, v.n - v.k))
+    finally
+      ccall((:lra_id_free, liblra), Cvoid, (Ptr{lra_id},), r.id)
+    end
+  end
+end
+
+function stats(s::Server)
+  r = Ref{lra_server_stats}()
+  ccall((:lra_server_get_stats, liblra), Cint, (Ptr{Cvoid}, Ref{lra_server_stats}), s.h, r)
+  r[]
 end
 
 end # module
