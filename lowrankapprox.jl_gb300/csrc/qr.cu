@@ -21,6 +21,7 @@
 #include <algorithm>
 #include <vector>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <cmath>
 #include <mutex>
@@ -1286,6 +1287,533 @@ __global__ void __launch_bounds__(NT) geqp3_df_kernel(QrParams<double> P, QrV2Ex
   }
 }
 
+// ---- shared-memory-resident double-float variant ------------------------------
+// When a CTA's share of the sketch fits in shared memory the columns never
+// leave the SM: CTA b owns the contiguous columns [n b / G, n (b + 1) / G),
+// held as (h, l) float pairs, and applies every reflector to them there.
+// The only traffic between CTAs per pivot is one 64-bit word per CTA and
+// the winning candidate's column: each CTA stages its best candidate's
+// remaining rows in global memory, then publishes (norm key, column, stop
+// flag, sequence bit) as one word.  Readers poll the G words of the
+// exchange (one L2 round trip once they are written), take the argmax and
+// load the winner's staged rows; this replaces the grid barrier and the
+// separate read of the per-CTA partials.  Words and staged columns are
+// double-buffered by exchange parity, so a CTA that runs ahead never
+// overwrites what a slower CTA still reads, and the sequence bit tells
+// this exchange from the one two steps earlier.  The key keeps the 38
+// leading bits of the double-float norm (relative resolution 2^-30, far
+// below the error of the downdated norms); ties go to the smaller column
+// index, as with xLAQPS's idamax.
+struct QrSm {
+  unsigned long long* xw;    // [2][G] exchange words, zeroed before the launch
+  float2* stage;             // [2][G][m] staged candidate columns
+  unsigned long long* pubt;  // LRA_TRACE: %globaltimer of each CTA's word per pivot, [kmax][G], or null
+};
+
+constexpr unsigned long long XW_IDX = 0xFFFFFFull;  // 24-bit column field, stored as XW_IDX - j
+constexpr unsigned long long XW_LOW = (1ull << 62) - 1;
+
+__device__ __forceinline__ unsigned long long xw_pack(Df v, int64_t j) {
+  // 38 bits of the key (df_key < 2^63 for h > 0); zero, negative zero and
+  // NaN norms rank lowest
+  const unsigned long long k = v.h > 0.f ? (unsigned long long)df_key(v) >> 25 : 0ull;
+  return (k << 24) | (XW_IDX - (unsigned long long)j);
+}
+
+// Warp 0 computes the reflector's scalars while warps 1..NW-1 take the dot
+// products of their columns with the (unscaled) reflector tail x; with
+// v = [1; scal x] the update of column a is f = tau (a_c + scal (x . a)),
+// a_c -= f, a_i -= (f scal) x_i.  A warp takes its columns four at a time:
+// one load of x serves four accumulators, and the four dot products are
+// reduced together (each butterfly level halves the values a lane holds, so
+// the four totals cost about as much as one).  The warp that updates a
+// column also downdates its norm, recomputes it when the downdate is
+// unreliable (LAPACK's tol3z test), and forms its candidate word.
+template <int NT>
+__global__ void __launch_bounds__(NT) geqp3_df_smem_kernel(QrParams<double> P, QrV2Extra X, QrDf D, QrSm S) {
+  constexpr int NW = NT / 32;
+  constexpr int NCW = NW - 1;  // column warps
+  __shared__ Df s_part[NW];
+  __shared__ unsigned long long s_w[NW];
+  __shared__ int s_fl[NW];
+  __shared__ Df s_alpha, s_f, s_tau, s_beta;
+  __shared__ double s_red[32];
+  __shared__ unsigned long long s_win;
+  __shared__ int s_owner, s_stop, s_ok;
+  __shared__ double s_taud, s_betad;
+  extern __shared__ unsigned char qr_dyn[];
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  const int G = gridDim.x, b = blockIdx.x;
+  const int64_t m = P.m, n = P.n, lda = P.lda;
+  const int64_t c0 = n * b / G, c1 = n * (b + 1) / G;
+  const int nloc = (int)(c1 - c0);
+  const int64_t ncap = (n + G - 1) / G;
+  float2* V = reinterpret_cast<float2*>(qr_dyn);  // rows c..m-1 of the pivot column
+  float2* C = V + m;                              // the CTA's columns, slot s = column c0 + s
+  Df* s_vn1 = reinterpret_cast<Df*>(C + ncap * m);
+  Df* s_vn2 = s_vn1 + ncap;
+  Df* s_dot = s_vn2 + ncap;
+  unsigned char* s_st = reinterpret_cast<unsigned char*>(s_dot + ncap);
+  float* __restrict__ Bh = D.Bh;
+  float* __restrict__ Bl = D.Bl;
+  const float tol3z = (float)sqrt(Real<double>::eps);
+  const int64_t lastrk = m < n ? m : n;
+  auto stamp = [&](int64_t c, int ph) {
+    if (D.stamps && b == 0 && threadIdx.x == 0 && c < P.kmax) D.stamps[c * 16 + ph] = globaltimer_ns();
+  };
+  // the CTA's candidate: max of the warps' words (s_w) and OR of their
+  // stop flags (s_fl), into s_win / s_stop
+  auto cta_word = [&]() {
+    __syncthreads();
+    if (wid == 0) {
+      unsigned long long w0 = lane < NW ? s_w[lane] : 0ull;
+      int f0 = lane < NW ? s_fl[lane] : 0;
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) {
+        const unsigned long long w2 = __shfl_xor_sync(0xffffffffu, w0, o);
+        w0 = w2 > w0 ? w2 : w0;
+        f0 |= __shfl_xor_sync(0xffffffffu, f0, o);
+      }
+      if (lane == 0) {
+        s_win = w0;
+        s_stop = f0;
+      }
+    }
+    __syncthreads();
+  };
+  auto warp_word = [&](unsigned long long w, int fl) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      const unsigned long long w2 = __shfl_xor_sync(0xffffffffu, w, o);
+      w = w2 > w ? w2 : w;
+      fl |= __shfl_xor_sync(0xffffffffu, fl, o);
+    }
+    if (lane == 0) {
+      s_w[wid] = w;
+      s_fl[wid] = fl;
+    }
+  };
+  // stage the CTA's candidate (rows r0..m-1) and publish its word for
+  // exchange e; the word goes out after every thread's staged rows
+  auto publish = [&](unsigned e, int64_t r0) {
+    const unsigned long long w = s_win;
+    if (w & XW_LOW) {
+      const int64_t jc = (int64_t)(XW_IDX - (w & XW_IDX));
+      const float2* src = C + (jc - c0) * m;
+      float2* dst = S.stage + ((size_t)(e & 1) * G + b) * m;
+      for (int64_t i = r0 + threadIdx.x; i < m; i += NT) dst[i] = src[i];
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      const unsigned long long seq = (unsigned long long)(((e >> 1) & 1) ^ 1) << 63;
+      const unsigned long long fl = s_stop ? (1ull << 62) : 0ull;
+      __threadfence();
+      if (S.pubt && r0 >= 1 && r0 - 1 < P.kmax) S.pubt[(r0 - 1) * G + b] = globaltimer_ns();
+      *((volatile unsigned long long*)(S.xw + (size_t)(e & 1) * G + b)) = seq | fl | (w & XW_LOW);
+    }
+  };
+  // wait for all G words of exchange e (bounded), reduce them: the winning
+  // word, its CTA and the OR of the stop flags, in shared memory
+  auto collect = [&](unsigned e) -> bool {
+    if (wid == 0) {
+      const unsigned long long* xw = S.xw + (size_t)(e & 1) * G;
+      const unsigned long long want = ((e >> 1) & 1) ^ 1;
+      constexpr int PB = 8;  // G <= 256
+      unsigned long long w[PB];
+      unsigned pending = 0;
+#pragma unroll
+      for (int q = 0; q < PB; ++q) {
+        const int bb = lane + 32 * q;
+        w[q] = 0;
+        if (bb < G) {
+          w[q] = *((const volatile unsigned long long*)(xw + bb));
+          if ((w[q] >> 63) != want) pending |= 1u << q;
+        }
+      }
+      bool ok = true;
+      if (__any_sync(0xffffffffu, pending != 0)) {
+        const uint64_t t0 = globaltimer_ns();
+        for (unsigned it = 1;; ++it) {
+#pragma unroll
+          for (int q = 0; q < PB; ++q)
+            if (pending & (1u << q)) {
+              w[q] = *((const volatile unsigned long long*)(xw + lane + 32 * q));
+              if ((w[q] >> 63) == want) pending &= ~(1u << q);
+            }
+          if (!__any_sync(0xffffffffu, pending != 0)) break;
+          // the error word and the clock every 16th round: a poll round is
+          // one L2 round trip, and a dependent second load would double it
+          if (it & 15) continue;
+          int bad = 0;
+          if (lane == 0) {
+            bad = *((volatile int*)&P.bar->err) != 0;
+            if (!bad && globaltimer_ns() - t0 > kWaitLimitNs) {
+              atomicCAS(&P.bar->err, 0, 4);
+              bad = 1;
+            }
+          }
+          if (__shfl_sync(0xffffffffu, bad, 0)) {
+            ok = false;
+            break;
+          }
+        }
+      }
+      __threadfence();
+      unsigned long long best = 0;
+      int own = 0, fl = 0;
+#pragma unroll
+      for (int q = 0; q < PB; ++q) {
+        const int bb = lane + 32 * q;
+        if (bb < G) {
+          const unsigned long long lw = w[q] & XW_LOW;
+          fl |= (int)((w[q] >> 62) & 1);
+          if (lw > best) {
+            best = lw;
+            own = bb;
+          }
+        }
+      }
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) {
+        const unsigned long long b2 = __shfl_xor_sync(0xffffffffu, best, o);
+        const int o2 = __shfl_xor_sync(0xffffffffu, own, o);
+        if (b2 > best || (b2 == best && o2 < own)) {
+          best = b2;
+          own = o2;
+        }
+        fl |= __shfl_xor_sync(0xffffffffu, fl, o);
+      }
+      if (lane == 0) {
+        s_win = best;
+        s_owner = own;
+        s_stop = fl;
+        s_ok = ok ? 1 : 0;
+      }
+    }
+    __syncthreads();
+    return s_ok != 0;
+  };
+  // the next four live slots of this warp from slot s on (-1: absent)
+  auto next_live = [&](int s) {
+    while (s < nloc && (s_st[s] & ST_DONE)) s += NCW;
+    return s;
+  };
+  auto quad = [&](int& s, int* q) {
+    int cnt = 0;
+#pragma unroll
+    for (int g = 0; g < 4; ++g) {
+      s = next_live(s);
+      if (s < nloc) {
+        q[g] = s;
+        ++cnt;
+        s += NCW;
+      } else {
+        q[g] = -1;
+      }
+    }
+    return cnt;
+  };
+  // 2-norm of rows r0..m-1 of a shared-memory column, by one warp, in FP64
+  auto col_nrm2 = [&](const float2* col, int64_t r0) -> double {
+    double mx = 0;
+    for (int64_t i = r0 + lane; i < m; i += 32) mx = fmax(mx, fabs(df_val(col[i].x, col[i].y)));
+    mx = warp_max(mx);
+    if (mx == 0 || !isfinite(mx)) return mx;
+    const double sc = pow2_scale_inv(mx);
+    double acc = 0;
+    for (int64_t i = r0 + lane; i < m; i += 32) {
+      const double t = df_val(col[i].x, col[i].y) * sc;
+      acc = fma(t, t, acc);
+    }
+    return sqrt(warp_sum(acc)) / sc;
+  };
+
+  // ---- the CTA's columns into shared memory; initial norms, first pivot ------
+  for (int s = wid; s < nloc; s += NW) {
+    const float* ph = Bh + (c0 + s) * lda;
+    const float* pl = Bl + (c0 + s) * lda;
+    for (int64_t i = lane; i < m; i += 32) C[s * m + i] = make_float2(ph[i], pl[i]);
+  }
+  double lmax = 0;
+  unsigned long long cw = 0;
+  for (int s = threadIdx.x; s < nloc; s += NT) {
+    s_st[s] = ST_LIVE;
+    const double v = D.vn0[c0 + s];
+    const Df nr = df_split(v);
+    s_vn1[s] = s_vn2[s] = nr;
+    lmax = fmax(lmax, v);
+    const unsigned long long w = xw_pack(nr, c0 + s);
+    cw = w > cw ? w : cw;
+  }
+  lmax = block_max(lmax, s_red);
+  if (threadIdx.x == 0) P.part_d[b] = lmax;
+  warp_word(cw, 0);
+  cta_word();
+  unsigned e = 0;
+  publish(e, 0);
+  if (!collect(e)) return;
+  double maxnrm = 0;
+  for (int bb = threadIdx.x; bb < G; bb += NT) maxnrm = fmax(maxnrm, __ldcg(P.part_d + bb));
+  maxnrm = block_max(maxnrm, s_red);
+  const double ptol = fmax(P.atol * *D.scale, P.rtol * maxnrm);
+
+  int64_t kres = P.kmax, nfac = 0;
+  int64_t j = 0;
+  while (j < P.kmax) {
+    const int64_t jb = min(P.nb, P.kmax - j);
+    int64_t kk = 0, first_small = -1;
+    bool stop_block = false, last_small = false;
+    while (kk < jb && !stop_block) {
+      const int64_t c = j + kk;
+      const int64_t pvt = (int64_t)(XW_IDX - (s_win & XW_IDX));
+      const int owner = s_owner;
+      stamp(c, 0);
+      if (owner == b && threadIdx.x == 0) s_st[pvt - c0] |= ST_DONE;
+      // ---- the pivot column's rows c..m-1 from the winner's stage, and the
+      // per-warp partial sums of squares of rows c+1..m-1
+      {
+        const float2* src = S.stage + ((size_t)(e & 1) * G + owner) * m;
+        Df acc{0.f, 0.f};
+        for (int64_t i = c + threadIdx.x; i < m; i += NT) {
+          const float2 x = __ldcg(src + i);
+          V[i] = x;
+          if (i > c) df_fma_acc(acc, x.x, x.y, x.x, x.y);
+          else s_alpha = Df{x.x, x.y};
+        }
+        acc = quick_two_sum(acc.h, acc.l);
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) acc = df_add(acc, df_shfl_xor(acc, o));
+        if (lane == 0) s_part[wid] = acc;
+      }
+      __syncthreads();
+      stamp(c, 1);
+      const int64_t len = m - c - 1;
+      if (wid == 0) {
+        // xLARFG in double-float (the matrix is scaled to max |B| < 1, so
+        // neither the sum of squares nor beta can overflow, and no entry of
+        // a float pair is small enough for xLARFG's rescaling loop)
+        Df acc = lane < NW ? s_part[lane] : Df{0.f, 0.f};
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) acc = df_add(acc, df_shfl_xor(acc, o));
+        const Df alpha = s_alpha;
+        Df tau{0.f, 0.f}, beta = alpha, scal{1.f, 0.f};
+        if (len > 0 && acc.h > 0.f) {
+          const Df r = df_sqrt(df_add(df_mul(alpha, alpha), acc));
+          beta = alpha.h >= 0.f ? df_neg(r) : r;
+          tau = df_div(df_add(beta, df_neg(alpha)), beta);
+          scal = df_div(Df{1.f, 0.f}, df_add(alpha, df_neg(beta)));
+        }
+        if (lane == 0) {
+          s_taud = df_val(tau.h, tau.l);
+          s_betad = df_val(beta.h, beta.l);
+          s_f = scal;
+          s_tau = tau;
+          s_beta = beta;
+          if (b == 0) {
+            P.tau[c] = s_taud;
+            X.piv[c] = pvt;
+            X.beta[c] = s_betad;
+          }
+        }
+      } else if (len > 0) {
+        // ---- dot products x . a of the warp's live columns, four at a time
+        int s = wid - 1;
+        int q[4];
+        while (quad(s, q)) {
+          const float2* cg[4];
+#pragma unroll
+          for (int g = 0; g < 4; ++g) cg[g] = C + (int64_t)(q[g] >= 0 ? q[g] : q[0]) * m;
+          Df d[4] = {{0.f, 0.f}, {0.f, 0.f}, {0.f, 0.f}, {0.f, 0.f}};
+          for (int64_t i = c + 1 + lane; i < m; i += 32) {
+            const float2 v = V[i];
+#pragma unroll
+            for (int g = 0; g < 4; ++g) {
+              const float2 x = cg[g][i];
+              df_fma_acc(d[g], v.x, v.y, x.x, x.y);
+            }
+          }
+#pragma unroll
+          for (int g = 0; g < 4; ++g) d[g] = quick_two_sum(d[g].h, d[g].l);
+          // transposed butterfly: after the 16- and 8-lane levels, lanes
+          // 8g..8g+7 hold column g's partial sums
+          const bool up = lane & 16;
+          const Df k0 = up ? d[2] : d[0], k1 = up ? d[3] : d[1];
+          const Df e0 = df_add(k0, df_shfl_xor(up ? d[0] : d[2], 16));
+          const Df e1 = df_add(k1, df_shfl_xor(up ? d[1] : d[3], 16));
+          const bool hi = lane & 8;
+          Df t = df_add(hi ? e1 : e0, df_shfl_xor(hi ? e0 : e1, 8));
+#pragma unroll
+          for (int o = 4; o > 0; o >>= 1) t = df_add(t, df_shfl_xor(t, o));
+          const int g = lane >> 3;
+          const int qg = g == 0 ? q[0] : g == 1 ? q[1] : g == 2 ? q[2] : q[3];
+          if ((lane & 7) == 0 && qg >= 0) s_dot[qg] = t;
+        }
+      }
+      __syncthreads();
+      stamp(c, 2);
+      const double tau = s_taud;
+      const Df scal = s_f;
+      // ---- the finished pivot column to global memory (its owner): R's rows
+      // above c, beta, the reflector v = scal x below
+      if (owner == b) {
+        const float2* col = C + (pvt - c0) * m;
+        const Df bt = s_beta;
+        for (int64_t i = threadIdx.x; i < m; i += NT) {
+          float2 y;
+          if (i < c) {
+            y = col[i];
+          } else if (i == c) {
+            y = make_float2(bt.h, bt.l);
+          } else {
+            y = V[i];
+            if (tau != 0) {
+              const Df z = df_mul(Df{y.x, y.y}, scal);
+              y = make_float2(z.h, z.l);
+            }
+          }
+          Bh[pvt * lda + i] = y.x;
+          Bl[pvt * lda + i] = y.y;
+        }
+      }
+      stamp(c, 3);
+      // ---- updates, norm downdates and the warp's candidate ---------------------
+      unsigned long long ww = 0;
+      int wfl = 0;
+      auto sub = [&](int ph) {
+        if (D.stamps && b == 0 && threadIdx.x == 32 && c < P.kmax) D.stamps[c * 16 + ph] = globaltimer_ns();
+      };
+      if (wid > 0) {
+        sub(8);
+        const Df tdf = s_tau;
+        int s = wid - 1;
+        int q[4];
+        while (quad(s, q)) {
+          // lane 8g holds column g's row c and its factors f, f scal
+          const int g = lane >> 3;
+          const int qg = g == 0 ? q[0] : g == 1 ? q[1] : g == 2 ? q[2] : q[3];
+          const bool mine = (lane & 7) == 0 && qg >= 0;
+          float2 x0 = make_float2(0.f, 0.f);
+          Df f{0.f, 0.f}, fs{0.f, 0.f};
+          if (mine) {
+            x0 = C[(int64_t)qg * m + c];
+            if (tau != 0 && len > 0) {
+              f = df_mul(tdf, df_add(Df{x0.x, x0.y}, df_mul(scal, s_dot[qg])));
+              fs = df_mul(f, scal);
+            }
+          }
+          Df fq[4];
+          float2* cg[4];
+#pragma unroll
+          for (int h = 0; h < 4; ++h) {
+            fq[h] = Df{__shfl_sync(0xffffffffu, fs.h, 8 * h), __shfl_sync(0xffffffffu, fs.l, 8 * h)};
+            cg[h] = C + (int64_t)(q[h] >= 0 ? q[h] : q[0]) * m;
+          }
+          sub(9);
+          const bool u0 = fq[0].h != 0.f, u1 = fq[1].h != 0.f, u2 = fq[2].h != 0.f, u3 = fq[3].h != 0.f;
+          if (u0 || u1 || u2 || u3) {
+            for (int64_t i = c + 1 + lane; i < m; i += 32) {
+              const float2 v = V[i];
+#pragma unroll
+              for (int h = 0; h < 4; ++h) {
+                const bool u = h == 0 ? u0 : h == 1 ? u1 : h == 2 ? u2 : u3;
+                if (u) {
+                  const float2 x = cg[h][i];
+                  const Df y = df_axpy_neg(x.x, x.y, fq[h], v.x, v.y);
+                  cg[h][i] = make_float2(y.h, y.l);
+                }
+              }
+            }
+          }
+          sub(10);
+          // lane 8g: column g's new row c, its norm downdate and word
+          int flagged = 0;
+          Df v1{0.f, 0.f};
+          if (mine) {
+            const Df a = df_add(Df{x0.x, x0.y}, df_neg(f));
+            C[(int64_t)qg * m + c] = make_float2(a.h, a.l);
+            v1 = s_vn1[qg];
+            if (c < lastrk - 1 && v1.h != 0.f) {
+              // LAPACK's partial-norm downdate, in double-float
+              Df temp = df_div(a.h < 0.f ? df_neg(a) : a, v1);
+              temp = df_mul(df_add(Df{1.f, 0.f}, temp), df_add(Df{1.f, 0.f}, df_neg(temp)));
+              if (temp.h < 0.f) temp = Df{0.f, 0.f};
+              const Df r = df_div(v1, s_vn2[qg]);
+              const Df temp2 = df_mul(temp, df_mul(r, r));
+              if (temp2.h <= tol3z) {
+                flagged = 1;
+              } else {
+                v1 = df_mul(v1, df_sqrt(temp));
+                s_vn1[qg] = v1;
+              }
+            }
+          }
+          // unreliable downdates: the norm of rows c+1..m-1, recomputed now
+          // (xLAQPS would end the block here and recompute it before the
+          // next pivot; the columns are already up to date, so the result is
+          // the same)
+          unsigned fm = __ballot_sync(0xffffffffu, flagged);
+          sub(11);
+          wfl |= fm != 0;
+          while (fm) {
+            const int L = __ffs(fm) - 1;
+            fm &= fm - 1;
+            const int qf = __shfl_sync(0xffffffffu, qg, L);
+            const double nr = col_nrm2(C + (int64_t)qf * m, c + 1);
+            if (lane == L) {
+              v1 = df_split(nr);
+              s_vn1[qf] = s_vn2[qf] = v1;
+            }
+          }
+          sub(12);
+          if (mine) {
+            const unsigned long long w = xw_pack(v1, c0 + qg);
+            ww = w > ww ? w : ww;
+          }
+        }
+      }
+      warp_word(ww, wfl);
+      sub(13);
+      const bool small = fabs(s_betad) <= ptol;
+      if (small && first_small < 0) first_small = c;
+      last_small = small;
+      cta_word();
+      stamp(c, 4);
+      publish(e + 1, c + 1);
+      stamp(c, 5);
+      ++e;
+      if (!collect(e)) return;
+      stamp(c, 6);
+      stamp(c, 7);
+      stop_block = s_stop != 0;
+      ++kk;
+    }
+    const int64_t jn = j + kk;
+    nfac = jn;
+    // rank test of geqp3_adap_main! (src/pqr.jl:407-415): when R(jn-1, jn-1)
+    // is below ptol, the rank is the first i of this block with |R(i, i)| <= ptol
+    if (last_small) {
+      kres = first_small;
+      break;
+    }
+    j = jn;
+  }
+  // ---- the columns that were not pivots back to global memory ----------------
+  for (int s = wid; s < nloc; s += NW) {
+    if (s_st[s] & ST_DONE) continue;
+    float* ph = Bh + (c0 + s) * lda;
+    float* pl = Bl + (c0 + s) * lda;
+    for (int64_t i = lane; i < m; i += 32) {
+      const float2 y = C[(int64_t)s * m + i];
+      ph[i] = y.x;
+      pl[i] = y.y;
+    }
+  }
+  if (b == 0 && threadIdx.x == 0) {
+    *P.k_out = kres;
+    *X.nfac = nfac;
+  }
+}
+
 // max |B| as the bit pattern of a nonnegative double
 __global__ void df_absmax_kernel(int64_t m, int64_t n, const double* __restrict__ B, int64_t ldb,
                                  unsigned long long* __restrict__ out) {
@@ -1434,6 +1962,91 @@ __global__ void col_norms_kernel(int64_t m, int64_t n, const T* __restrict__ A, 
 
 }  // namespace
 
+// LRA_QR_SMEM=0 keeps the double-float QR's columns in global memory
+// even where they would fit shared memory (both variants stay testable)
+static bool qr_smem_enabled() {
+  static const bool on = [] {
+    const char* e = std::getenv("LRA_QR_SMEM");
+    return !(e && *e == '0');
+  }();
+  return on;
+}
+
+// LRA_TRACE: the mean time per pivot of each phase of the double-float QR
+// (CTA 0's %globaltimer stamps, 16 per pivot)
+static void print_qr_trace(lra_ctx* ctx, const unsigned long long* stamps, int64_t kmax, int64_t m, int64_t n,
+                           const char* kname, bool smem, const unsigned long long* pubt, int G) {
+  std::vector<unsigned long long> h((size_t)16 * kmax), pt;
+  LRA_CUDA(cudaMemcpyAsync(h.data(), stamps, h.size() * 8, cudaMemcpyDeviceToHost, ctx->stream));
+  if (pubt) {
+    pt.resize((size_t)G * kmax);
+    LRA_CUDA(cudaMemcpyAsync(pt.data(), pubt, pt.size() * 8, cudaMemcpyDeviceToHost, ctx->stream));
+  }
+  LRA_CUDA(cudaStreamSynchronize(ctx->stream));
+  if (pubt) {
+    // spread of the CTAs' word times per pivot, and CTA 0's wait after the last
+    double spread = 0, after = 0;
+    int64_t cnt = 0;
+    for (int64_t c = 0; c < kmax; ++c) {
+      const unsigned long long* p = pt.data() + (size_t)c * G;
+      unsigned long long lo = ~0ull, hi = 0;
+      for (int q = 0; q < G; ++q) {
+        lo = std::min(lo, p[q]);
+        hi = std::max(hi, p[q]);
+      }
+      if (!lo || !h[16 * c + 6]) continue;
+      spread += (double)(hi - lo);
+      after += (double)h[16 * c + 6] - (double)hi;
+      ++cnt;
+    }
+    if (cnt)
+      std::fprintf(stderr, "[lra] %s exchange: word spread %.2f us, last word to CTA 0 done %.2f us\n", kname,
+                   spread / cnt / 1e3, after / cnt / 1e3);
+  }
+  static const char* const glob[8] = {"vs-load", "reflector", "scale", "columns", "downdate", "publish", "barrier",
+                                      "write-back+pivot"};
+  static const char* const sm[8] = {"stage-load", "dots+reflector", "owner-write", "updates+downdate",
+                                    "stage+word", "exchange", "-", "rest"};
+  const char* const* lab = smem ? sm : glob;
+  double ph[7] = {0}, cyc = 0, sub[6] = {0};
+  int64_t cnt = 0, nsub = 0, nflag = 0;
+  for (int64_t c = 0; c + 1 < kmax; ++c) {
+    const unsigned long long* t = h.data() + 16 * c;
+    if (!t[0] || !t[7] || !h[16 * (c + 1)]) continue;
+    for (int q = 0; q < 7; ++q) ph[q] += (double)(t[q + 1] - t[q]);
+    cyc += (double)(h[16 * (c + 1)] - t[0]);
+    ++cnt;
+    if (t[8] && t[9] && t[10] && t[11] && t[12] && t[13]) {
+      sub[0] += (double)t[8] - (double)t[3];
+      for (int q = 1; q < 6; ++q) sub[q] += (double)(t[8 + q] - t[7 + q]);
+      if (t[12] - t[11] > 300) ++nflag;
+      ++nsub;
+    }
+  }
+  if (nsub && smem)
+    std::fprintf(stderr,
+                 "[lra] %s warp 1 (us): to start %.2f f+broadcast %.2f update %.2f downdate %.2f recompute %.2f "
+                 "word %.2f; flagged steps %lld\n",
+                 kname, sub[0] / nsub / 1e3, sub[1] / nsub / 1e3, sub[2] / nsub / 1e3, sub[3] / nsub / 1e3,
+                 sub[4] / nsub / 1e3, sub[5] / nsub / 1e3, (long long)nflag);
+  else if (nsub)
+    std::fprintf(stderr,
+                 "[lra] %s warp-0 passes (us): load+dots %.2f reduce+f %.2f update %.2f | load+dots %.2f "
+                 "reduce+f %.2f update %.2f\n",
+                 kname, sub[0] / nsub / 1e3, sub[1] / nsub / 1e3, sub[2] / nsub / 1e3, sub[3] / nsub / 1e3,
+                 sub[4] / nsub / 1e3, sub[5] / nsub / 1e3);
+  if (cnt) {
+    std::fprintf(stderr, "[lra] %s m=%lld n=%lld pivots=%lld us/pivot %.2f:", kname, (long long)m, (long long)n,
+                 (long long)cnt, cyc / cnt / 1e3);
+    double rest = cyc;
+    for (int q = 0; q < 7; ++q) {
+      std::fprintf(stderr, " %s %.2f", lab[q], ph[q] / cnt / 1e3);
+      rest -= ph[q];
+    }
+    std::fprintf(stderr, " %s %.2f\n", lab[7], rest / cnt / 1e3);
+  }
+}
+
 template <typename T>
 int64_t geqp3_adap(lra_ctx* ctx, int64_t m, int64_t n, T* A, int64_t lda, int64_t* jpvt, T* tau,
                    int64_t kmax, int64_t nb, double atol, double rtol, bool pivot) {
@@ -1535,56 +2148,55 @@ int64_t geqp3_adap(lra_ctx* ctx, int64_t m, int64_t n, T* A, int64_t lda, int64_
       QrParams<double> Pd;
       std::memcpy(&Pd, &P, sizeof(Pd));
       Pd.lda = m;
-      raise_smem_limit(ctx, (const void*)geqp3_df_kernel<NT>);
-      // as much L1 as the shared memory leaves: the warps' columns live there
-      LRA_CUDA(cudaFuncSetAttribute(geqp3_df_kernel<NT>, cudaFuncAttributePreferredSharedMemoryCarveout,
-                                    cudaSharedmemCarveoutMaxL1));
-      int per_df = 0;
-      LRA_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_df, geqp3_df_kernel<NT>, NT, smem2));
-      if (per_df < 1) fail(LRA_ECUDA, "geqp3 kernel cannot be resident");
-      void* args[] = {&Pd, &X, &D};
-      LRA_CUDA(cudaLaunchCooperativeKernel((const void*)geqp3_df_kernel<NT>, dim3(grid), dim3(NT), args, smem2,
-                                           ctx->stream));
-      post_launch(ctx, "geqp3_df_kernel");
-      if (D.stamps) {
-        std::vector<unsigned long long> h((size_t)16 * P.kmax);
-        LRA_CUDA(cudaMemcpyAsync(h.data(), D.stamps, h.size() * 8, cudaMemcpyDeviceToHost, ctx->stream));
-        LRA_CUDA(cudaStreamSynchronize(ctx->stream));
-        double ph[7] = {0}, cyc = 0;
-        int64_t cnt = 0;
-        double sub[6] = {0};
-        int64_t nsub = 0;
-        for (int64_t c = 0; c + 1 < P.kmax; ++c) {
-          const unsigned long long* t = h.data() + 16 * c;
-          if (!t[0] || !t[7] || !h[16 * (c + 1)]) continue;
-          for (int q = 0; q < 7; ++q) ph[q] += (double)(t[q + 1] - t[q]);
-          cyc += (double)(h[16 * (c + 1)] - t[0]);
-          ++cnt;
-          if (t[8] && t[9] && t[10] && t[11] && t[12] && t[13]) {
-            sub[0] += (double)(t[8] - t[3]);
-            sub[1] += (double)(t[9] - t[8]);
-            sub[2] += (double)(t[10] - t[9]);
-            sub[3] += (double)(t[11] - t[10]);
-            sub[4] += (double)(t[12] - t[11]);
-            sub[5] += (double)(t[13] - t[12]);
-            ++nsub;
-          }
+      // the columns stay in shared memory when each CTA's share fits there
+      constexpr int NTS = 544;  // warp 0 for the reflector, 16 column warps
+      const int gsm = (int)std::min<int64_t>(std::min(ctx->num_sms, 256),
+                                             std::max<int64_t>(1, (n + NTS / 32 - 2) / (NTS / 32 - 1)));
+      const int64_t ncap = (n + gsm - 1) / gsm;
+      const size_t smem_s = (size_t)m * sizeof(float2) + (size_t)ncap * m * sizeof(float2) + (size_t)ncap * (3 * 8 + 1);
+      bool smq = n < (int64_t)XW_IDX && qr_smem_enabled();
+      if (smq) {
+        raise_smem_limit(ctx, (const void*)geqp3_df_smem_kernel<NTS>);
+        cudaFuncAttributes fa;
+        LRA_CUDA(cudaFuncGetAttributes(&fa, geqp3_df_smem_kernel<NTS>));
+        smq = smem_s <= (size_t)fa.maxDynamicSharedSizeBytes;
+        if (smq) {
+          int per = 0;
+          LRA_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, geqp3_df_smem_kernel<NTS>, NTS, smem_s));
+          smq = per >= 1;
         }
-        if (nsub)
-          std::fprintf(stderr,
-                       "[lra] geqp3_df warp-0 passes (us): load+dots %.2f reduce+f %.2f update %.2f | load+dots %.2f "
-                       "reduce+f %.2f update %.2f\n",
-                       sub[0] / nsub / 1e3, sub[1] / nsub / 1e3, sub[2] / nsub / 1e3, sub[3] / nsub / 1e3,
-                       sub[4] / nsub / 1e3, sub[5] / nsub / 1e3);
-        if (cnt)
-          std::fprintf(stderr,
-                       "[lra] geqp3_df m=%lld n=%lld pivots=%lld us/pivot %.2f: vs-load %.2f reflector %.2f scale %.2f "
-                       "columns %.2f downdate %.2f publish %.2f barrier %.2f write-back+pivot %.2f\n",
-                       (long long)m, (long long)n, (long long)cnt, cyc / cnt / 1e3, ph[0] / cnt / 1e3,
-                       ph[1] / cnt / 1e3, ph[2] / cnt / 1e3, ph[3] / cnt / 1e3, ph[4] / cnt / 1e3, ph[5] / cnt / 1e3,
-                       ph[6] / cnt / 1e3,
-                       (cyc - ph[0] - ph[1] - ph[2] - ph[3] - ph[4] - ph[5] - ph[6]) / cnt / 1e3);
       }
+      const char* kname = smq ? "geqp3_df_smem_kernel" : "geqp3_df_kernel";
+      unsigned long long* pubt = nullptr;
+      if (smq) {
+        Pd.part_d = ctx->arena.alloc_n<double>(gsm);
+        QrSm S;
+        S.pubt = nullptr;
+        if (D.stamps) {
+          S.pubt = ctx->arena.alloc_n<unsigned long long>((size_t)gsm * P.kmax);
+          LRA_CUDA(cudaMemsetAsync(S.pubt, 0, (size_t)gsm * P.kmax * 8, ctx->stream));
+          pubt = S.pubt;
+        }
+        S.xw = ctx->arena.alloc_n<unsigned long long>((size_t)2 * gsm);
+        S.stage = ctx->arena.alloc_n<float2>((size_t)2 * gsm * m);
+        LRA_CUDA(cudaMemsetAsync(S.xw, 0, (size_t)2 * gsm * sizeof(unsigned long long), ctx->stream));
+        void* args[] = {&Pd, &X, &D, &S};
+        LRA_CUDA(cudaLaunchCooperativeKernel((const void*)geqp3_df_smem_kernel<NTS>, dim3(gsm), dim3(NTS), args,
+                                             smem_s, ctx->stream));
+      } else {
+        raise_smem_limit(ctx, (const void*)geqp3_df_kernel<NT>);
+        // as much L1 as the shared memory leaves: the warps' columns live there
+        LRA_CUDA(cudaFuncSetAttribute(geqp3_df_kernel<NT>, cudaFuncAttributePreferredSharedMemoryCarveout,
+                                      cudaSharedmemCarveoutMaxL1));
+        int per_df = 0;
+        LRA_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_df, geqp3_df_kernel<NT>, NT, smem2));
+        if (per_df < 1) fail(LRA_ECUDA, "geqp3 kernel cannot be resident");
+        void* args[] = {&Pd, &X, &D};
+        LRA_CUDA(cudaLaunchCooperativeKernel((const void*)geqp3_df_kernel<NT>, dim3(grid), dim3(NT), args, smem2,
+                                             ctx->stream));
+      }
+      post_launch(ctx, kname);
+      if (D.stamps) print_qr_trace(ctx, D.stamps, P.kmax, m, n, kname, smq, pubt, gsm);
       df_join_kernel<<<gm, 256, 0, ctx->stream>>>(m, n, Bh, Bl, m, scale, reinterpret_cast<double*>(A), lda);
       post_launch(ctx, "df_join_kernel");
     } else {
