@@ -435,7 +435,7 @@ struct QrV2Extra {
 // floating-point norms order like the norms).
 constexpr int QCH = 16;  // rows per lane per register chunk (512 rows)
 constexpr int QG = 4;    // rows per lane issued between uniform range checks
-constexpr unsigned char ST_LIVE = 1, ST_DONE = 2, ST_FLAG = 4;
+constexpr unsigned char ST_LIVE = 1, ST_DONE = 2, ST_FLAG = 4, ST_UPD = 8;
 
 __device__ __forceinline__ long long norm_key(double v) {
   const long long b = __double_as_longlong(v);
@@ -1310,6 +1310,23 @@ struct QrSm {
   unsigned long long* pubt;  // LRA_TRACE: %globaltimer of each CTA's word per pivot, [kmax][G], or null
 };
 
+// the next four live slots s, s + step, ... of a warp (-1: absent); s moves on
+__device__ __forceinline__ int live_quad(const unsigned char* st, int nloc, int step, int& s, int (&q)[4]) {
+  int cnt = 0;
+#pragma unroll
+  for (int g = 0; g < 4; ++g) {
+    while (s < nloc && (st[s] & ST_DONE)) s += step;
+    if (s < nloc) {
+      q[g] = s;
+      ++cnt;
+      s += step;
+    } else {
+      q[g] = -1;
+    }
+  }
+  return cnt;
+}
+
 constexpr unsigned long long XW_IDX = 0xFFFFFFull;  // 24-bit column field, stored as XW_IDX - j
 constexpr unsigned long long XW_LOW = (1ull << 62) - 1;
 
@@ -1326,11 +1343,13 @@ __device__ __forceinline__ unsigned long long xw_pack(Df v, int64_t j) {
 // a_c -= f, a_i -= (f scal) x_i.  A warp takes its columns four at a time:
 // one load of x serves four accumulators, and the four dot products are
 // reduced together (each butterfly level halves the values a lane holds, so
-// the four totals cost about as much as one).  The warp that updates a
-// column also downdates its norm, recomputes it when the downdate is
-// unreliable (LAPACK's tol3z test), and forms its candidate word.
+// the four totals cost about as much as one).  The pivot search needs only
+// row c of each column (the norm downdate), so the rank-1 update of rows
+// c+1..m-1 is deferred: the CTA updates its candidate column (which it
+// stages) and any column whose norm must be recomputed right away, and the
+// other columns while warp 0 waits for the exchange.
 template <int NT>
-__global__ void __launch_bounds__(NT) geqp3_df_smem_kernel(QrParams<double> P, QrV2Extra X, QrDf D, QrSm S) {
+__global__ void __launch_bounds__(NT, 1) geqp3_df_smem_kernel(QrParams<double> P, QrV2Extra X, QrDf D, QrSm S) {
   constexpr int NW = NT / 32;
   constexpr int NCW = NW - 1;  // column warps
   __shared__ Df s_part[NW];
@@ -1353,7 +1372,8 @@ __global__ void __launch_bounds__(NT) geqp3_df_smem_kernel(QrParams<double> P, Q
   Df* s_vn1 = reinterpret_cast<Df*>(C + ncap * m);
   Df* s_vn2 = s_vn1 + ncap;
   Df* s_dot = s_vn2 + ncap;
-  unsigned char* s_st = reinterpret_cast<unsigned char*>(s_dot + ncap);
+  Df* s_fs = s_dot + ncap;  // f scal of each column for the deferred update
+  unsigned char* s_st = reinterpret_cast<unsigned char*>(s_fs + ncap);
   float* __restrict__ Bh = D.Bh;
   float* __restrict__ Bl = D.Bl;
   const float tol3z = (float)sqrt(Real<double>::eps);
@@ -1394,14 +1414,26 @@ __global__ void __launch_bounds__(NT) geqp3_df_smem_kernel(QrParams<double> P, Q
     }
   };
   // stage the CTA's candidate (rows r0..m-1) and publish its word for
-  // exchange e; the word goes out after every thread's staged rows
-  auto publish = [&](unsigned e, int64_t r0) {
+  // exchange e; the candidate's deferred update (upd) is applied on the way.
+  // The word goes out after every thread's staged rows.
+  auto publish = [&](unsigned e, int64_t r0, bool upd) {
     const unsigned long long w = s_win;
     if (w & XW_LOW) {
-      const int64_t jc = (int64_t)(XW_IDX - (w & XW_IDX));
-      const float2* src = C + (jc - c0) * m;
+      const int sc = (int)((int64_t)(XW_IDX - (w & XW_IDX)) - c0);
+      float2* col = C + (int64_t)sc * m;
       float2* dst = S.stage + ((size_t)(e & 1) * G + b) * m;
-      for (int64_t i = r0 + threadIdx.x; i < m; i += NT) dst[i] = src[i];
+      const Df fs = upd ? s_fs[sc] : Df{0.f, 0.f};
+      if (upd && !(s_st[sc] & ST_UPD) && fs.h != 0.f) {
+        for (int64_t i = r0 + threadIdx.x; i < m; i += NT) {
+          const float2 x = col[i], v = V[i];
+          const Df y = df_axpy_neg(x.x, x.y, fs, v.x, v.y);
+          col[i] = dst[i] = make_float2(y.h, y.l);
+        }
+        __syncthreads();
+        if (threadIdx.x == 0) s_st[sc] |= ST_UPD;
+      } else {
+        for (int64_t i = r0 + threadIdx.x; i < m; i += NT) dst[i] = col[i];
+      }
     }
     __syncthreads();
     if (threadIdx.x == 0) {
@@ -1493,26 +1525,7 @@ __global__ void __launch_bounds__(NT) geqp3_df_smem_kernel(QrParams<double> P, Q
     __syncthreads();
     return s_ok != 0;
   };
-  // the next four live slots of this warp from slot s on (-1: absent)
-  auto next_live = [&](int s) {
-    while (s < nloc && (s_st[s] & ST_DONE)) s += NCW;
-    return s;
-  };
-  auto quad = [&](int& s, int* q) {
-    int cnt = 0;
-#pragma unroll
-    for (int g = 0; g < 4; ++g) {
-      s = next_live(s);
-      if (s < nloc) {
-        q[g] = s;
-        ++cnt;
-        s += NCW;
-      } else {
-        q[g] = -1;
-      }
-    }
-    return cnt;
-  };
+  auto quad = [&](int& s, int (&q)[4]) { return live_quad(s_st, nloc, NCW, s, q); };
   // 2-norm of rows r0..m-1 of a shared-memory column, by one warp, in FP64
   auto col_nrm2 = [&](const float2* col, int64_t r0) -> double {
     double mx = 0;
@@ -1550,7 +1563,7 @@ __global__ void __launch_bounds__(NT) geqp3_df_smem_kernel(QrParams<double> P, Q
   warp_word(cw, 0);
   cta_word();
   unsigned e = 0;
-  publish(e, 0);
+  publish(e, 0, false);
   if (!collect(e)) return;
   double maxnrm = 0;
   for (int bb = threadIdx.x; bb < G; bb += NT) maxnrm = fmax(maxnrm, __ldcg(P.part_d + bb));
@@ -1653,28 +1666,6 @@ __global__ void __launch_bounds__(NT) geqp3_df_smem_kernel(QrParams<double> P, Q
       stamp(c, 2);
       const double tau = s_taud;
       const Df scal = s_f;
-      // ---- the finished pivot column to global memory (its owner): R's rows
-      // above c, beta, the reflector v = scal x below
-      if (owner == b) {
-        const float2* col = C + (pvt - c0) * m;
-        const Df bt = s_beta;
-        for (int64_t i = threadIdx.x; i < m; i += NT) {
-          float2 y;
-          if (i < c) {
-            y = col[i];
-          } else if (i == c) {
-            y = make_float2(bt.h, bt.l);
-          } else {
-            y = V[i];
-            if (tau != 0) {
-              const Df z = df_mul(Df{y.x, y.y}, scal);
-              y = make_float2(z.h, z.l);
-            }
-          }
-          Bh[pvt * lda + i] = y.x;
-          Bl[pvt * lda + i] = y.y;
-        }
-      }
       stamp(c, 3);
       // ---- updates, norm downdates and the warp's candidate ---------------------
       unsigned long long ww = 0;
@@ -1701,29 +1692,8 @@ __global__ void __launch_bounds__(NT) geqp3_df_smem_kernel(QrParams<double> P, Q
               fs = df_mul(f, scal);
             }
           }
-          Df fq[4];
-          float2* cg[4];
-#pragma unroll
-          for (int h = 0; h < 4; ++h) {
-            fq[h] = Df{__shfl_sync(0xffffffffu, fs.h, 8 * h), __shfl_sync(0xffffffffu, fs.l, 8 * h)};
-            cg[h] = C + (int64_t)(q[h] >= 0 ? q[h] : q[0]) * m;
-          }
+          if (mine) s_fs[qg] = fs;
           sub(9);
-          const bool u0 = fq[0].h != 0.f, u1 = fq[1].h != 0.f, u2 = fq[2].h != 0.f, u3 = fq[3].h != 0.f;
-          if (u0 || u1 || u2 || u3) {
-            for (int64_t i = c + 1 + lane; i < m; i += 32) {
-              const float2 v = V[i];
-#pragma unroll
-              for (int h = 0; h < 4; ++h) {
-                const bool u = h == 0 ? u0 : h == 1 ? u1 : h == 2 ? u2 : u3;
-                if (u) {
-                  const float2 x = cg[h][i];
-                  const Df y = df_axpy_neg(x.x, x.y, fq[h], v.x, v.y);
-                  cg[h][i] = make_float2(y.h, y.l);
-                }
-              }
-            }
-          }
           sub(10);
           // lane 8g: column g's new row c, its norm downdate and word
           int flagged = 0;
@@ -1747,18 +1717,27 @@ __global__ void __launch_bounds__(NT) geqp3_df_smem_kernel(QrParams<double> P, Q
               }
             }
           }
-          // unreliable downdates: the norm of rows c+1..m-1, recomputed now
-          // (xLAQPS would end the block here and recompute it before the
-          // next pivot; the columns are already up to date, so the result is
-          // the same)
           unsigned fm = __ballot_sync(0xffffffffu, flagged);
           sub(11);
+          // unreliable downdates: the column's update now, and the norm of
+          // its rows c+1..m-1 (xLAQPS would end the block here and recompute
+          // the norm before the next pivot, from the same updated column)
           wfl |= fm != 0;
           while (fm) {
             const int L = __ffs(fm) - 1;
             fm &= fm - 1;
             const int qf = __shfl_sync(0xffffffffu, qg, L);
-            const double nr = col_nrm2(C + (int64_t)qf * m, c + 1);
+            const Df ff{__shfl_sync(0xffffffffu, fs.h, L), __shfl_sync(0xffffffffu, fs.l, L)};
+            float2* col = C + (int64_t)qf * m;
+            if (ff.h != 0.f)
+              for (int64_t i = c + 1 + lane; i < m; i += 32) {
+                const float2 x = col[i], v = V[i];
+                const Df y = df_axpy_neg(x.x, x.y, ff, v.x, v.y);
+                col[i] = make_float2(y.h, y.l);
+              }
+            __syncwarp();
+            if (lane == 0) s_st[qf] |= ST_UPD;
+            const double nr = col_nrm2(col, c + 1);
             if (lane == L) {
               v1 = df_split(nr);
               s_vn1[qf] = s_vn2[qf] = v1;
@@ -1778,9 +1757,67 @@ __global__ void __launch_bounds__(NT) geqp3_df_smem_kernel(QrParams<double> P, Q
       last_small = small;
       cta_word();
       stamp(c, 4);
-      publish(e + 1, c + 1);
+      publish(e + 1, c + 1, true);
       stamp(c, 5);
       ++e;
+      // ---- warps 1..NW-1: the deferred updates, and the finished pivot column
+      // to global memory (its owner); warp 0 meanwhile waits for the exchange
+      if (wid > 0) {
+        const int ct = threadIdx.x - 32;
+        constexpr int NCT = NT - 32;
+      // ---- the finished pivot column to global memory (its owner): R's rows
+      // above c, beta, the reflector v = scal x below
+        if (owner == b) {
+        const float2* col = C + (pvt - c0) * m;
+        const Df bt = s_beta;
+        for (int64_t i = ct; i < m; i += NCT) {
+          float2 y;
+          if (i < c) {
+            y = col[i];
+          } else if (i == c) {
+            y = make_float2(bt.h, bt.l);
+          } else {
+            y = V[i];
+            if (tau != 0) {
+              const Df z = df_mul(Df{y.x, y.y}, scal);
+              y = make_float2(z.h, z.l);
+            }
+          }
+          Bh[pvt * lda + i] = y.x;
+          Bl[pvt * lda + i] = y.y;
+        }
+      }
+        int s = wid - 1;
+        int q[4];
+        while (quad(s, q)) {
+          Df fq[4];
+          float2* cg[4];
+          bool u[4];
+#pragma unroll
+          for (int h = 0; h < 4; ++h) {
+            const int qh = q[h] >= 0 ? q[h] : q[0];
+            cg[h] = C + (int64_t)qh * m;
+            fq[h] = s_fs[qh];
+            u[h] = q[h] >= 0 && fq[h].h != 0.f && !(s_st[qh] & ST_UPD);
+          }
+          if (u[0] || u[1] || u[2] || u[3]) {
+            for (int64_t i = c + 1 + lane; i < m; i += 32) {
+              const float2 v = V[i];
+#pragma unroll
+              for (int h = 0; h < 4; ++h) {
+                if (u[h]) {
+                  const float2 x = cg[h][i];
+                  const Df y = df_axpy_neg(x.x, x.y, fq[h], v.x, v.y);
+                  cg[h][i] = make_float2(y.h, y.l);
+                }
+              }
+            }
+          }
+          __syncwarp();
+          const int qh = lane == 0 ? q[0] : lane == 1 ? q[1] : lane == 2 ? q[2] : lane == 3 ? q[3] : -1;
+          if (qh >= 0) s_st[qh] &= (unsigned char)~ST_UPD;
+        }
+      }
       if (!collect(e)) return;
       stamp(c, 6);
       stamp(c, 7);
@@ -2005,8 +2042,8 @@ static void print_qr_trace(lra_ctx* ctx, const unsigned long long* stamps, int64
   }
   static const char* const glob[8] = {"vs-load", "reflector", "scale", "columns", "downdate", "publish", "barrier",
                                       "write-back+pivot"};
-  static const char* const sm[8] = {"stage-load", "dots+reflector", "owner-write", "updates+downdate",
-                                    "stage+word", "exchange", "-", "rest"};
+  static const char* const sm[8] = {"stage-load", "dots+reflector", "-", "f+downdate+word",
+                                    "stage+word", "deferred-update||exchange", "-", "rest"};
   const char* const* lab = smem ? sm : glob;
   double ph[7] = {0}, cyc = 0, sub[6] = {0};
   int64_t cnt = 0, nsub = 0, nflag = 0;
@@ -2025,7 +2062,7 @@ static void print_qr_trace(lra_ctx* ctx, const unsigned long long* stamps, int64
   }
   if (nsub && smem)
     std::fprintf(stderr,
-                 "[lra] %s warp 1 (us): to start %.2f f+broadcast %.2f update %.2f downdate %.2f recompute %.2f "
+                 "[lra] %s warp 1 (us): to start %.2f f %.2f - %.2f downdate %.2f recompute %.2f "
                  "word %.2f; flagged steps %lld\n",
                  kname, sub[0] / nsub / 1e3, sub[1] / nsub / 1e3, sub[2] / nsub / 1e3, sub[3] / nsub / 1e3,
                  sub[4] / nsub / 1e3, sub[5] / nsub / 1e3, (long long)nflag);
@@ -2153,7 +2190,7 @@ int64_t geqp3_adap(lra_ctx* ctx, int64_t m, int64_t n, T* A, int64_t lda, int64_
       const int gsm = (int)std::min<int64_t>(std::min(ctx->num_sms, 256),
                                              std::max<int64_t>(1, (n + NTS / 32 - 2) / (NTS / 32 - 1)));
       const int64_t ncap = (n + gsm - 1) / gsm;
-      const size_t smem_s = (size_t)m * sizeof(float2) + (size_t)ncap * m * sizeof(float2) + (size_t)ncap * (3 * 8 + 1);
+      const size_t smem_s = (size_t)m * sizeof(float2) + (size_t)ncap * m * sizeof(float2) + (size_t)ncap * (4 * 8 + 1);
       bool smq = n < (int64_t)XW_IDX && qr_smem_enabled();
       if (smq) {
         raise_smem_limit(ctx, (const void*)geqp3_df_smem_kernel<NTS>);
