@@ -438,7 +438,10 @@ void postproc_t(lra_ctx* ctx, const lra_opts& o, Fact<T>& F, bool want_t) {
   F.T_ = ctx->arena.alloc_n<T>((size_t)std::max<int64_t>(k, 1) * std::max<int64_t>(nr, 1));
   if (k > 0 && nr > 0) {
     copy_matrix(ctx, k, nr, F.B + k * F.ld, F.ld, F.T_, k);
-    trsm_upper(ctx, k, nr, F.B, F.ld, F.T_, k);
+    if (k <= kBsMax)
+      trsm_bs(ctx, k, nr, F.B, F.ld, F.T_, k);
+    else
+      trsm_upper(ctx, k, nr, F.B, F.ld, F.T_, k);
   }
   if (maxdet) maxdet_dev<T>(ctx, o, F);
 }
@@ -633,6 +636,198 @@ lra_id* pack_id(lra_ctx* ctx, const Fact<T>& F, int dtype) {
 }
 
 }  // namespace
+
+namespace lra {
+
+// ---- lra_idfact_batched, grouped ----------------------------------------------------
+// Float64 matrices on the mixed path (tensor-core Gaussian sketch, library
+// generator restarted per matrix as for a call on a fresh context): every
+// round sketches the unfinished matrices, factors all their sketches in one
+// grouped launch (geqp3_df_batch), reads the ranks back once and doubles the
+// sketch of those whose rank is not yet revealed (sketchfact_dev's loop);
+// the solves T = R11^{-1} R12 run as one grouped launch.  Each result is
+// what lra_idfact returns for the matrix on a fresh context.
+bool grouped_batch_ok(lra_ctx* ctx, int64_t count, const lra_matdesc* mats, const lra_opts& o, const lra_rand* rand) {
+  if (rand || count <= 0) return false;
+  if (!use_tc(o, LRA_F64) || o.sketch != LRA_SKETCH_RANDN || o.sketch_randn_niter != 0 || o.maxdet_tol >= 0)
+    return false;
+  if (!(o.sketchfact_adap || o.rank < 0)) return false;
+  for (int64_t i = 0; i < count; ++i) {
+    const lra_matdesc& d = mats[i];
+    if (d.m < 1 || d.n < 1 || !d.A || d.lda < d.m) return false;
+    // the largest sketch the doubling can reach: order(nt) with nt up to 2 n
+    int64_t nt = o.nb, order = samp(o, nt);
+    while (nt <= 2 * d.n) {
+      order = samp(o, nt);
+      nt *= 2;
+    }
+    if (!tc_sketch_supported(order, d.m, d.n) || !geqp3_df_batch_fits(ctx, order, d.n)) return false;
+  }
+  return true;
+}
+
+void idfact_batched_grouped(lra_ctx* ctx, int64_t count, const lra_matdesc* mats, const lra_opts& oin,
+                            lra_id** outs) {
+  lra_opts o = oin;
+  o.pqrfact_retval = LRA_RET_T;
+  ctx->gemm_tc = use_tc_gemm(o, LRA_F64);
+  ctx->mixed_rtol = ctx->gemm_tc ? o.rtol : 0.0;
+  const bool adaptive = o.sketchfact_adap || o.rank < 0;
+  size_t free_b = 0, total_b = 0;
+  LRA_CUDA(cudaMemGetInfo(&free_b, &total_b));
+  const double budget = 0.3 * (double)free_b;
+  int64_t c0 = 0;
+  while (c0 < count) {
+    // a chunk whose working set stays inside the budget
+    int64_t c1 = c0;
+    double bytes = 0;
+    while (c1 < count) {
+      const double mn = (double)mats[c1].m * (double)mats[c1].n;
+      const double est = 40.0 * mn + 64.0 * 512.0 * ((double)mats[c1].m + (double)mats[c1].n);
+      if (c1 > c0 && (bytes + est > budget || c1 - c0 >= 1024)) break;
+      bytes += est;
+      ++c1;
+    }
+    const int64_t cn = c1 - c0;
+    const ArenaMark mk = ctx->arena.mark();
+    std::vector<DMat<double>> dA((size_t)cn);
+    std::vector<TcSplit> split((size_t)cn);
+    int* flags = ctx->arena.alloc_n<int>((size_t)cn);
+    LRA_CUDA(cudaMemsetAsync(flags, 0, (size_t)cn * sizeof(int), ctx->stream));
+    for (int64_t i = 0; i < cn; ++i) {
+      const lra_matdesc& d = mats[c0 + i];
+      dA[(size_t)i] = stage_in<double>(ctx, d.A, d.m, d.n, d.lda);
+      if (o.check_finite) all_finite_async(ctx, d.m, d.n, dA[(size_t)i].p, dA[(size_t)i].ld, flags + i);
+      tc_split<double>(ctx, 'n', d.m, d.n, dA[(size_t)i].p, dA[(size_t)i].ld, 6, &split[(size_t)i]);
+    }
+    {
+      std::vector<int> hf((size_t)cn);
+      LRA_CUDA(cudaMemcpyAsync(hf.data(), flags, (size_t)cn * sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+      LRA_CUDA(cudaStreamSynchronize(ctx->stream));
+      for (int64_t i = 0; i < cn; ++i)
+        if (hf[(size_t)i]) fail(LRA_ENONFINITE, "matrix %lld of the batch has NaN or Inf entries", (long long)(c0 + i));
+    }
+    struct St {
+      int64_t nt, order, k = 0;
+      uint64_t ctr = 0;
+      int nsteps = 0;
+      bool done = false;
+      double* B = nullptr;
+      int64_t* jpvt = nullptr;
+      double* tau = nullptr;
+    };
+    std::vector<St> st((size_t)cn);
+    for (auto& s : st) s.nt = adaptive ? o.nb : o.rank;
+    int64_t* kdev = ctx->arena.alloc_n<int64_t>((size_t)cn);
+    int* errs = ctx->arena.alloc_n<int>((size_t)cn);
+    for (int round = 0;; ++round) {
+      if (round > 62) fail(LRA_EINVAL, "adaptive sketch did not terminate");
+      std::vector<int64_t> act;
+      for (int64_t i = 0; i < cn; ++i)
+        if (!st[(size_t)i].done) act.push_back(i);
+      if (act.empty()) break;
+      LRA_CUDA(cudaMemsetAsync(errs, 0, (size_t)cn * sizeof(int), ctx->stream));
+      std::vector<DfBatchItem> items;
+      items.reserve(act.size());
+      for (const int64_t i : act) {
+        St& s = st[(size_t)i];
+        const lra_matdesc& d = mats[c0 + i];
+        s.order = samp(o, s.nt);
+        if (s.order < 1) fail(LRA_EINVAL, "sketch order %lld", (long long)s.order);
+        const int64_t l = std::min(s.order, d.n);
+        const int64_t kmax = (o.rank < 0 || o.rank > l) ? l : o.rank;
+        s.B = ctx->arena.alloc_n<double>((size_t)s.order * d.n);
+        s.jpvt = ctx->arena.alloc_n<int64_t>((size_t)d.n);
+        s.tau = ctx->arena.alloc_n<double>((size_t)std::max<int64_t>(l, 1));
+        const ArenaMark ms = ctx->arena.mark();
+        double* S = ctx->arena.alloc_n<double>((size_t)s.order * d.m);
+        ctx->rng_counter = s.ctr;
+        RandSrc rs(ctx, nullptr, o.seed);
+        rs.gauss(s.order * d.m, S, true);
+        s.ctr = ctx->rng_counter;
+        tc_sketch<double>(ctx, split[(size_t)i], s.order, S, s.B, s.order, errs + i);
+        // S is read by the sketch kernel, which runs before any later use of its memory
+        ctx->arena.release(ms);
+        items.push_back(DfBatchItem{s.order, d.n, s.order, kmax, s.B, s.jpvt, s.tau});
+      }
+      std::vector<int64_t> map(act.begin(), act.end());
+      // the batch writes k of item t to kdev[t]
+      geqp3_df_batch(ctx, (int64_t)items.size(), items.data(), o.nb, o.atol, o.rtol, kdev);
+      std::vector<int64_t> hk(items.size());
+      std::vector<int> he((size_t)cn);
+      LRA_CUDA(cudaMemcpyAsync(hk.data(), kdev, hk.size() * sizeof(int64_t), cudaMemcpyDeviceToHost, ctx->stream));
+      LRA_CUDA(cudaMemcpyAsync(he.data(), errs, (size_t)cn * sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+      LRA_CUDA(cudaStreamSynchronize(ctx->stream));
+      for (size_t t = 0; t < map.size(); ++t) {
+        St& s = st[(size_t)map[t]];
+        if (he[(size_t)map[t]]) fail(LRA_ETIMEDOUT, "tc_sketch: a bounded wait timed out");
+        s.k = hk[t];
+        s.nsteps = round + 1;
+        if (!adaptive || s.k < s.nt)
+          s.done = true;
+        else
+          s.nt *= 2;
+      }
+    }
+    // T = R11^{-1} R12 (the single path's postproc_t), then the results
+    std::vector<double*> Tm((size_t)cn, nullptr);
+    std::vector<BsItem> bs;
+    for (int64_t i = 0; i < cn; ++i) {
+      St& s = st[(size_t)i];
+      const int64_t n = mats[c0 + i].n, k = s.k, nr = n - k;
+      Tm[(size_t)i] = ctx->arena.alloc_n<double>((size_t)std::max<int64_t>(k, 1) * std::max<int64_t>(nr, 1));
+      if (k <= 0 || nr <= 0) continue;
+      if (k <= kBsMax) {
+        bs.push_back(BsItem{k, nr, s.order, s.B, Tm[(size_t)i]});
+      } else {
+        copy_matrix(ctx, k, nr, s.B + k * s.order, s.order, Tm[(size_t)i], k);
+        trsm_upper(ctx, k, nr, s.B, s.order, Tm[(size_t)i], k);
+      }
+    }
+    trsm_bs_batch(ctx, (int64_t)bs.size(), bs.data());
+    for (int64_t i = 0; i < cn; ++i) {
+      const St& s = st[(size_t)i];
+      const int64_t n = mats[c0 + i].n, k = s.k;
+      lra_id* r = static_cast<lra_id*>(hmalloc(sizeof(lra_id)));
+      std::memset(r, 0, sizeof *r);
+      outs[c0 + i] = r;
+      r->dtype = LRA_F64;
+      r->nsteps = s.nsteps;
+      r->k = k;
+      r->n = n;
+      r->sk = static_cast<int64_t*>(hmalloc(sizeof(int64_t) * std::max<int64_t>(k, 1)));
+      r->rd = static_cast<int64_t*>(hmalloc(sizeof(int64_t) * std::max<int64_t>(n - k, 1)));
+      r->T = hmalloc(sizeof(double) * std::max<int64_t>(k * (n - k), 1));
+      to_host(ctx, r->sk, s.jpvt, k);
+      to_host(ctx, r->rd, s.jpvt + k, n - k);
+      if (k > 0 && n > k) to_host(ctx, r->T, Tm[(size_t)i], (size_t)k * (n - k));
+    }
+    LRA_CUDA(cudaStreamSynchronize(ctx->stream));
+    ctx->arena.release(mk);
+    c0 = c1;
+  }
+}
+
+int try_idfact_batched_grouped(lra_ctx* ctx, int dtype, int64_t count, const lra_matdesc* mats,
+                               const lra_opts* opts, const lra_rand* rand, lra_id** outs) {
+  if (!ctx || !opts || dtype != LRA_F64) return -1;
+  if (opts->precision != LRA_PREC_MIXED) return -1;
+  bool ok = false;
+  const int st0 = guarded(ctx, [&] {
+    chkopts(opts);
+    ok = grouped_batch_ok(ctx, count, mats, *opts, rand);
+  });
+  if (st0 != LRA_OK || !ok) return -1;
+  const int st = guarded(ctx, [&] { idfact_batched_grouped(ctx, count, mats, *opts, outs); });
+  if (st != LRA_OK)
+    for (int64_t i = 0; i < count; ++i) {
+      lra_id_free(outs[i]);
+      outs[i] = nullptr;
+    }
+  return st;
+}
+
+}  // namespace lra
 
 extern "C" {
 

@@ -12,6 +12,7 @@
 #include <algorithm>
 #include <cstdio>
 #include <cmath>
+#include <vector>
 
 #include "common.cuh"
 #include "df64.cuh"
@@ -1290,6 +1291,72 @@ template bool potrf_upper<float>(lra_ctx*, int64_t, float*, int64_t);
 template bool potrf_upper<double>(lra_ctx*, int64_t, double*, int64_t);
 template void trsm_right_upper<float>(lra_ctx*, int64_t, int64_t, const float*, int64_t, float*, int64_t);
 template void trsm_right_upper<double>(lra_ctx*, int64_t, int64_t, const double*, int64_t, double*, int64_t);
+// ---- T = R11^{-1} R12 by back substitution, a thread per right-hand side -------
+// The ID's solve (src/id.jl:447, R11 \ R12) for ranks up to kBsMax: row
+// i of x is (x_i - sum_{j > i} R_ij x_j) / R_ii, the sum taken from j = i+1
+// upwards, from the bottom row.  The batched path runs the same per-column
+// loop with a CTA per matrix, so both give the same bits.
+template <typename T>
+__device__ __forceinline__ void bs_column(int k, const T* __restrict__ R, int64_t ldr, T* __restrict__ x) {
+  for (int i = k - 1; i >= 0; --i) {
+    T s = x[i];
+    const T* r = R + i;
+    for (int j = i + 1; j < k; ++j) s = fma(-r[j * ldr], x[j], s);
+    x[i] = s / r[i * ldr];
+  }
+}
+
+template <typename T>
+__global__ void trsm_bs_kernel(int k, int64_t nrhs, const T* __restrict__ R, int64_t ldr, T* X, int64_t ldx) {
+  for (int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; c < nrhs; c += (int64_t)gridDim.x * blockDim.x)
+    bs_column(k, R, ldr, X + c * ldx);
+}
+
+template <typename T>
+void trsm_bs(lra_ctx* ctx, int64_t k, int64_t nrhs, const T* R, int64_t ldr, T* X, int64_t ldx) {
+  if (k <= 0 || nrhs <= 0) return;
+  if (k > kBsMax) fail(LRA_EINVAL, "trsm_bs: k > %d", kBsMax);
+  const unsigned g = (unsigned)std::max<int64_t>(1, std::min<int64_t>((nrhs + 127) / 128, (int64_t)ctx->num_sms * 8));
+  trsm_bs_kernel<T><<<g, 128, 0, ctx->stream>>>((int)k, nrhs, R, ldr, X, ldx);
+  post_launch(ctx, "trsm_bs_kernel");
+}
+
+// one matrix of the batch: T (k x nr, ld k) = R11^{-1} R12, both read from B
+struct BsJob {
+  int64_t k, nr, ldb;
+  const double* B;
+  double* T;
+};
+
+__global__ void __launch_bounds__(256) trsm_bs_group_kernel(const BsJob* __restrict__ jobs) {
+  const BsJob J = jobs[blockIdx.x];
+  for (int64_t c = threadIdx.x; c < J.nr; c += blockDim.x) {
+    double* x = J.T + c * J.k;
+    const double* b = J.B + (J.k + c) * J.ldb;
+    for (int64_t i = 0; i < J.k; ++i) x[i] = b[i];
+    bs_column((int)J.k, J.B, J.ldb, x);
+  }
+}
+
+void trsm_bs_batch(lra_ctx* ctx, int64_t count, const BsItem* items) {
+  if (count <= 0) return;
+  std::vector<BsJob> jobs;
+  jobs.reserve((size_t)count);
+  for (int64_t i = 0; i < count; ++i) {
+    const BsItem& it = items[i];
+    if (it.k > kBsMax) fail(LRA_EINVAL, "trsm_bs_batch: k > %d", kBsMax);
+    if (it.k > 0 && it.nr > 0) jobs.push_back(BsJob{it.k, it.nr, it.ldb, it.B, it.T});
+  }
+  if (jobs.empty()) return;
+  BsJob* d = ctx->arena.alloc_n<BsJob>(jobs.size());
+  LRA_CUDA(cudaMemcpyAsync(d, jobs.data(), jobs.size() * sizeof(BsJob), cudaMemcpyHostToDevice, ctx->stream));
+  trsm_bs_group_kernel<<<(unsigned)jobs.size(), 256, 0, ctx->stream>>>(d);
+  post_launch(ctx, "trsm_bs_group_kernel");
+  LRA_CUDA(cudaStreamSynchronize(ctx->stream));
+}
+
+template void trsm_bs<float>(lra_ctx*, int64_t, int64_t, const float*, int64_t, float*, int64_t);
+template void trsm_bs<double>(lra_ctx*, int64_t, int64_t, const double*, int64_t, double*, int64_t);
 template void trsm_left_diag<float>(lra_ctx*, int, int64_t, const float*, int64_t, float*, int64_t);
 template void trsm_left_diag<double>(lra_ctx*, int, int64_t, const double*, int64_t, double*, int64_t);
 

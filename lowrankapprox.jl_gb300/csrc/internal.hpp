@@ -105,7 +105,8 @@ void tc_split(lra_ctx* ctx, char trans, int64_t M, int64_t N, const T* A, int64_
 // B (order x N, ldb) = S op(A) on tcgen05 tensor cores; S is order x M
 // (ld = order) with entries on the 1/32 lattice.
 template <typename T>
-void tc_sketch(lra_ctx* ctx, const TcSplit& sp, int64_t order, const T* S, T* B, int64_t ldb);
+void tc_sketch(lra_ctx* ctx, const TcSplit& sp, int64_t order, const T* S, T* B, int64_t ldb,
+               int* err_slot = nullptr);
 
 // Raises a kernel's dynamic shared memory limit to the most the device
 // allows beside its static shared memory.  Always the same value per kernel:
@@ -135,6 +136,26 @@ bool tc_gemm_worthwhile(int64_t m, int64_t n, int64_t k);
 void tc_gemm(lra_ctx* ctx, char ta, char tb, int64_t m, int64_t n, int64_t k, double alpha, const double* A,
              int64_t lda, const double* B, int64_t ldb, double beta, double* C, int64_t ldc);
 
+// The mixed path's pivoted QR of many Float64 sketches at once (a CTA per
+// matrix): each B (m x n, ld ldb) is factored in place, its jpvt and tau
+// filled and its rank written to k_dev[i], as geqp3_adap would.
+struct DfBatchItem {
+  int64_t m, n, ldb, kmax;
+  double* B;
+  int64_t* jpvt;
+  double* tau;
+};
+bool geqp3_df_batch_fits(lra_ctx* ctx, int64_t m, int64_t n);
+// lra_idfact_batched's grouped path: whether the batch qualifies, and the run
+bool grouped_batch_ok(lra_ctx* ctx, int64_t count, const lra_matdesc* mats, const lra_opts& o, const lra_rand* rand);
+void idfact_batched_grouped(lra_ctx* ctx, int64_t count, const lra_matdesc* mats, const lra_opts& o,
+                            lra_id** outs);
+// -1 when the batch does not qualify for the grouped path, else its status
+int try_idfact_batched_grouped(lra_ctx* ctx, int dtype, int64_t count, const lra_matdesc* mats,
+                               const lra_opts* opts, const lra_rand* rand, lra_id** outs);
+void geqp3_df_batch(lra_ctx* ctx, int64_t count, const DfBatchItem* items, int64_t nb, double atol, double rtol,
+                    int64_t* k_dev);
+
 // Rank-adaptive column-pivoted Householder QR (geqp3_adap!), in place.
 // pivot == false runs the same Householder QR without pivoting.
 template <typename T>
@@ -151,6 +172,17 @@ int64_t noalloc_max_cols();
 // X (k x nrhs) <- triu(R)^{-1} X, R k x k (ldr).
 template <typename T>
 void trsm_left_diag(lra_ctx* ctx, int jb, int64_t nrhs, const T* R, int64_t ldr, T* X, int64_t ldx);
+// X <- triu(R)^{-1} X (k <= kBsMax) by back substitution, a thread per column
+constexpr int kBsMax = 128;
+template <typename T>
+void trsm_bs(lra_ctx* ctx, int64_t k, int64_t nrhs, const T* R, int64_t ldr, T* X, int64_t ldx);
+// the batch's T = R11^{-1} R12 (R11, R12 from B, ld ldb; T k x nr, ld k)
+struct BsItem {
+  int64_t k, nr, ldb;
+  const double* B;
+  double* T;
+};
+void trsm_bs_batch(lra_ctx* ctx, int64_t count, const BsItem* items);
 template <typename T>
 void trsm_upper(lra_ctx* ctx, int64_t k, int64_t nrhs, const T* R, int64_t ldr, T* X,
                 int64_t ldx);
@@ -262,6 +294,9 @@ void cluster_orth(lra_ctx* ctx, int64_t n, int64_t k, T* Z, int64_t ldz, const i
 // nonfinite check: returns true when every entry is finite
 template <typename T>
 bool all_finite(lra_ctx* ctx, int64_t m, int64_t n, const T* A, int64_t lda);
+template <typename T>
+void all_finite_async(lra_ctx* ctx, int64_t m, int64_t n, const T* A, int64_t lda, int* bad);
+
 // column 2-norms
 template <typename T>
 void col_norms(lra_ctx* ctx, int64_t m, int64_t n, const T* A, int64_t lda, T* out);

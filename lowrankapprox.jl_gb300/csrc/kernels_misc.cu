@@ -304,6 +304,14 @@ void sketch_philox(lra_ctx* ctx, uint64_t seed, uint64_t base, int64_t n, T* out
   post_launch(ctx, "philox_kernel");
 }
 
+// sets *bad (zeroed by the caller) when A has a NaN or Inf entry; no wait
+template <typename T>
+void all_finite_async(lra_ctx* ctx, int64_t m, int64_t n, const T* A, int64_t lda, int* bad) {
+  if (m <= 0 || n <= 0) return;
+  finite_kernel<T><<<grid_for(ctx, m * n, 256, 16), 256, 0, ctx->stream>>>(m, n, A, lda, bad);
+  post_launch(ctx, "finite_kernel");
+}
+
 template <typename T>
 bool all_finite(lra_ctx* ctx, int64_t m, int64_t n, const T* A, int64_t lda) {
   if (m <= 0 || n <= 0) return true;
@@ -361,6 +369,7 @@ void gemv(lra_ctx* ctx, char trans, int64_t m, int64_t n, T alpha, const T* A, i
   template void sketch_from_stream<T>(lra_ctx*, const double*, int64_t, T*, bool);                 \
   template void sketch_philox<T>(lra_ctx*, uint64_t, uint64_t, int64_t, T*);                       \
   template bool all_finite<T>(lra_ctx*, int64_t, int64_t, const T*, int64_t);                      \
+  template void all_finite_async<T>(lra_ctx*, int64_t, int64_t, const T*, int64_t, int*);          \
   template void gemv<T>(lra_ctx*, char, int64_t, int64_t, T, const T*, int64_t, const T*, T, T*);
 INST(float)
 INST(double)

@@ -1348,8 +1348,17 @@ __device__ __forceinline__ unsigned long long xw_pack(Df v, int64_t j) {
 // c+1..m-1 is deferred: the CTA updates its candidate column (which it
 // stages) and any column whose norm must be recomputed right away, and the
 // other columns while warp 0 waits for the exchange.
-template <int NT>
-__global__ void __launch_bounds__(NT, 1) geqp3_df_smem_kernel(QrParams<double> P, QrV2Extra X, QrDf D, QrSm S) {
+//
+// The same step runs with the columns in global memory for a whole matrix
+// per CTA (GCOL): the batched path gives each small matrix one CTA, which
+// needs no exchange at all.  Every column sees the same sequence of
+// operations in both forms (the dot products' lane order and reduction tree,
+// the reflector's partial sums over the same thread-to-row map, the same
+// updates), so a matrix factored alone and in a batch gives the same bits.
+template <int NT, bool GCOL>
+__device__ __forceinline__ void geqp3_df_body(const QrParams<double>& P, const QrV2Extra& X, const QrDf& D,
+                                              const QrSm& S, const int G, const int b, float2* Cg,
+                                              unsigned char* qr_dyn) {
   constexpr int NW = NT / 32;
   constexpr int NCW = NW - 1;  // column warps
   __shared__ Df s_part[NW];
@@ -1360,16 +1369,16 @@ __global__ void __launch_bounds__(NT, 1) geqp3_df_smem_kernel(QrParams<double> P
   __shared__ unsigned long long s_win;
   __shared__ int s_owner, s_stop, s_ok;
   __shared__ double s_taud, s_betad;
-  extern __shared__ unsigned char qr_dyn[];
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-  const int G = gridDim.x, b = blockIdx.x;
   const int64_t m = P.m, n = P.n, lda = P.lda;
   const int64_t c0 = n * b / G, c1 = n * (b + 1) / G;
   const int nloc = (int)(c1 - c0);
   const int64_t ncap = (n + G - 1) / G;
   float2* V = reinterpret_cast<float2*>(qr_dyn);  // rows c..m-1 of the pivot column
-  float2* C = V + m;                              // the CTA's columns, slot s = column c0 + s
-  Df* s_vn1 = reinterpret_cast<Df*>(C + ncap * m);
+  // the CTA's columns, slot s = column c0 + s: shared memory, or (GCOL) a
+  // global m x n workspace
+  float2* C = GCOL ? Cg : V + m;
+  Df* s_vn1 = reinterpret_cast<Df*>(GCOL ? V + m : C + ncap * m);
   Df* s_vn2 = s_vn1 + ncap;
   Df* s_dot = s_vn2 + ncap;
   Df* s_fs = s_dot + ncap;  // f scal of each column for the deferred update
@@ -1421,22 +1430,23 @@ __global__ void __launch_bounds__(NT, 1) geqp3_df_smem_kernel(QrParams<double> P
     if (w & XW_LOW) {
       const int sc = (int)((int64_t)(XW_IDX - (w & XW_IDX)) - c0);
       float2* col = C + (int64_t)sc * m;
-      float2* dst = S.stage + ((size_t)(e & 1) * G + b) * m;
+      float2* dst = GCOL ? nullptr : S.stage + ((size_t)(e & 1) * G + b) * m;
       const Df fs = upd ? s_fs[sc] : Df{0.f, 0.f};
       if (upd && !(s_st[sc] & ST_UPD) && fs.h != 0.f) {
         for (int64_t i = r0 + threadIdx.x; i < m; i += NT) {
           const float2 x = col[i], v = V[i];
           const Df y = df_axpy_neg(x.x, x.y, fs, v.x, v.y);
-          col[i] = dst[i] = make_float2(y.h, y.l);
+          col[i] = make_float2(y.h, y.l);
+          if (!GCOL) dst[i] = make_float2(y.h, y.l);
         }
         __syncthreads();
         if (threadIdx.x == 0) s_st[sc] |= ST_UPD;
-      } else {
+      } else if (!GCOL) {
         for (int64_t i = r0 + threadIdx.x; i < m; i += NT) dst[i] = col[i];
       }
     }
     __syncthreads();
-    if (threadIdx.x == 0) {
+    if (!GCOL && threadIdx.x == 0) {
       const unsigned long long seq = (unsigned long long)(((e >> 1) & 1) ^ 1) << 63;
       const unsigned long long fl = s_stop ? (1ull << 62) : 0ull;
       __threadfence();
@@ -1447,6 +1457,12 @@ __global__ void __launch_bounds__(NT, 1) geqp3_df_smem_kernel(QrParams<double> P
   // wait for all G words of exchange e (bounded), reduce them: the winning
   // word, its CTA and the OR of the stop flags, in shared memory
   auto collect = [&](unsigned e) -> bool {
+    if (GCOL) {
+      // one CTA: its own candidate is the pivot
+      if (threadIdx.x == 0) s_owner = 0;
+      __syncthreads();
+      return true;
+    }
     if (wid == 0) {
       const unsigned long long* xw = S.xw + (size_t)(e & 1) * G;
       const unsigned long long want = ((e >> 1) & 1) ^ 1;
@@ -1541,12 +1557,14 @@ __global__ void __launch_bounds__(NT, 1) geqp3_df_smem_kernel(QrParams<double> P
     return sqrt(warp_sum(acc)) / sc;
   };
 
-  // ---- the CTA's columns into shared memory; initial norms, first pivot ------
-  for (int s = wid; s < nloc; s += NW) {
-    const float* ph = Bh + (c0 + s) * lda;
-    const float* pl = Bl + (c0 + s) * lda;
-    for (int64_t i = lane; i < m; i += 32) C[s * m + i] = make_float2(ph[i], pl[i]);
-  }
+  // ---- the CTA's columns into shared memory (GCOL: the workspace is filled);
+  // initial norms, first pivot
+  if (!GCOL)
+    for (int s = wid; s < nloc; s += NW) {
+      const float* ph = Bh + (c0 + s) * lda;
+      const float* pl = Bl + (c0 + s) * lda;
+      for (int64_t i = lane; i < m; i += 32) C[s * m + i] = make_float2(ph[i], pl[i]);
+    }
   double lmax = 0;
   unsigned long long cw = 0;
   for (int s = threadIdx.x; s < nloc; s += NT) {
@@ -1559,15 +1577,18 @@ __global__ void __launch_bounds__(NT, 1) geqp3_df_smem_kernel(QrParams<double> P
     cw = w > cw ? w : cw;
   }
   lmax = block_max(lmax, s_red);
-  if (threadIdx.x == 0) P.part_d[b] = lmax;
+  if (!GCOL && threadIdx.x == 0) P.part_d[b] = lmax;
   warp_word(cw, 0);
   cta_word();
   unsigned e = 0;
   publish(e, 0, false);
   if (!collect(e)) return;
-  double maxnrm = 0;
-  for (int bb = threadIdx.x; bb < G; bb += NT) maxnrm = fmax(maxnrm, __ldcg(P.part_d + bb));
-  maxnrm = block_max(maxnrm, s_red);
+  double maxnrm = lmax;
+  if (!GCOL) {
+    maxnrm = 0;
+    for (int bb = threadIdx.x; bb < G; bb += NT) maxnrm = fmax(maxnrm, __ldcg(P.part_d + bb));
+    maxnrm = block_max(maxnrm, s_red);
+  }
   const double ptol = fmax(P.atol * *D.scale, P.rtol * maxnrm);
 
   int64_t kres = P.kmax, nfac = 0;
@@ -1585,10 +1606,10 @@ __global__ void __launch_bounds__(NT, 1) geqp3_df_smem_kernel(QrParams<double> P
       // ---- the pivot column's rows c..m-1 from the winner's stage, and the
       // per-warp partial sums of squares of rows c+1..m-1
       {
-        const float2* src = S.stage + ((size_t)(e & 1) * G + owner) * m;
+        const float2* src = GCOL ? C + (pvt - c0) * m : S.stage + ((size_t)(e & 1) * G + owner) * m;
         Df acc{0.f, 0.f};
         for (int64_t i = c + threadIdx.x; i < m; i += NT) {
-          const float2 x = __ldcg(src + i);
+          const float2 x = GCOL ? src[i] : __ldcg(src + i);
           V[i] = x;
           if (i > c) df_fma_acc(acc, x.x, x.y, x.x, x.y);
           else s_alpha = Df{x.x, x.y};
@@ -1765,28 +1786,32 @@ __global__ void __launch_bounds__(NT, 1) geqp3_df_smem_kernel(QrParams<double> P
       if (wid > 0) {
         const int ct = threadIdx.x - 32;
         constexpr int NCT = NT - 32;
-      // ---- the finished pivot column to global memory (its owner): R's rows
-      // above c, beta, the reflector v = scal x below
+        // the finished pivot column (its owner): R's rows above c, beta, the
+        // reflector v = scal x below
         if (owner == b) {
-        const float2* col = C + (pvt - c0) * m;
-        const Df bt = s_beta;
-        for (int64_t i = ct; i < m; i += NCT) {
-          float2 y;
-          if (i < c) {
-            y = col[i];
-          } else if (i == c) {
-            y = make_float2(bt.h, bt.l);
-          } else {
-            y = V[i];
-            if (tau != 0) {
-              const Df z = df_mul(Df{y.x, y.y}, scal);
-              y = make_float2(z.h, z.l);
+          float2* col = C + (pvt - c0) * m;
+          const Df bt = s_beta;
+          for (int64_t i = (GCOL ? c : 0) + ct; i < m; i += NCT) {
+            float2 y;
+            if (i < c) {
+              y = col[i];
+            } else if (i == c) {
+              y = make_float2(bt.h, bt.l);
+            } else {
+              y = V[i];
+              if (tau != 0) {
+                const Df z = df_mul(Df{y.x, y.y}, scal);
+                y = make_float2(z.h, z.l);
+              }
+            }
+            if (GCOL) {
+              col[i] = y;
+            } else {
+              Bh[pvt * lda + i] = y.x;
+              Bl[pvt * lda + i] = y.y;
             }
           }
-          Bh[pvt * lda + i] = y.x;
-          Bl[pvt * lda + i] = y.y;
         }
-      }
         int s = wid - 1;
         int q[4];
         while (quad(s, q)) {
@@ -1835,7 +1860,7 @@ __global__ void __launch_bounds__(NT, 1) geqp3_df_smem_kernel(QrParams<double> P
     j = jn;
   }
   // ---- the columns that were not pivots back to global memory ----------------
-  for (int s = wid; s < nloc; s += NW) {
+  for (int s = wid; s < nloc && !GCOL; s += NW) {
     if (s_st[s] & ST_DONE) continue;
     float* ph = Bh + (c0 + s) * lda;
     float* pl = Bl + (c0 + s) * lda;
@@ -1848,6 +1873,123 @@ __global__ void __launch_bounds__(NT, 1) geqp3_df_smem_kernel(QrParams<double> P
   if (b == 0 && threadIdx.x == 0) {
     *P.k_out = kres;
     *X.nfac = nfac;
+  }
+}
+
+template <int NT>
+__global__ void __launch_bounds__(NT, 1) geqp3_df_smem_kernel(QrParams<double> P, QrV2Extra X, QrDf D, QrSm S) {
+  extern __shared__ unsigned char qr_dyn[];
+  geqp3_df_body<NT, false>(P, X, D, S, gridDim.x, blockIdx.x, nullptr, qr_dyn);
+}
+
+// one matrix of a batch: its parameters and its m x n float2 workspace
+struct QrJob {
+  QrParams<double> P;
+  QrV2Extra X;
+  QrDf D;
+  float2* work;
+};
+
+// persistent grouped pivoted QR: each CTA takes the next matrix (jobs are
+// ordered by decreasing work) and factors it alone
+template <int NT>
+__global__ void __launch_bounds__(NT, 1) geqp3_df_group_kernel(const QrJob* __restrict__ jobs, int njobs, int* next) {
+  extern __shared__ unsigned char qr_dyn[];
+  __shared__ int s_job;
+  const QrSm S{nullptr, nullptr, nullptr};
+  while (true) {
+    __syncthreads();
+    if (threadIdx.x == 0) s_job = atomicAdd(next, 1);
+    __syncthreads();
+    const int j = s_job;
+    if (j >= njobs) return;
+    geqp3_df_body<NT, true>(jobs[j].P, jobs[j].X, jobs[j].D, S, 1, 0, jobs[j].work, qr_dyn);
+  }
+}
+
+// ---- the batch's conversions, a CTA per matrix ---------------------------------
+// prep: max |B| (its power-of-two scale as df_scale_kernel), the scaled
+// float pairs into the workspace and each column's norm as df_split_kernel
+// (the same per-warp arithmetic, so the norms agree bit for bit)
+struct DfPrepJob {
+  int64_t m, n, ldb;
+  const double* B;
+  float2* work;   // m x n
+  double* vn0;    // n
+  double* scale;  // 1
+};
+
+__global__ void __launch_bounds__(512) df_prep_group_kernel(const DfPrepJob* __restrict__ jobs) {
+  __shared__ double red[32];
+  const DfPrepJob J = jobs[blockIdx.x];
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  double mx = 0;
+  for (int64_t j = wid; j < J.n; j += nw)
+    for (int64_t i = lane; i < J.m; i += 32) mx = fmax(mx, fabs(J.B[i + j * J.ldb]));
+  mx = block_max(mx, red);
+  const double sc = mx > 0 ? ldexp(1.0, -(ilogb(mx) + 1)) : 1.0;
+  if (threadIdx.x == 0) *J.scale = sc;
+  for (int64_t j = wid; j < J.n; j += nw) {
+    float2* w = J.work + j * J.m;
+    double cm = 0;
+    for (int64_t i = lane; i < J.m; i += 32) {
+      const double x = J.B[i + j * J.ldb] * sc;
+      const Df d = df_split(x);
+      w[i] = make_float2(d.h, d.l);
+      cm = fmax(cm, fabs(x));
+    }
+    cm = warp_max(cm);
+    double acc = 0;
+    if (cm > 0) {
+      const double s2 = pow2_scale_inv(cm);
+      for (int64_t i = lane; i < J.m; i += 32) {
+        const double t = df_val(w[i].x, w[i].y) * s2;
+        acc = fma(t, t, acc);
+      }
+      acc = sqrt(warp_sum(acc)) / s2;
+    }
+    if (lane == 0) J.vn0[j] = acc;
+  }
+}
+
+// finish: xLAQPS's swaps replayed into the column order, jpvt (1-based), and
+// B = (h + l) / scale in that order (df_join_kernel, then the gather)
+struct DfFinishJob {
+  int64_t m, n, ldb;
+  double* B;
+  const float2* work;
+  const double* scale;
+  const int64_t* piv;
+  const int64_t* nfac;
+  int64_t* jpvt;
+};
+
+__global__ void __launch_bounds__(512) df_finish_group_kernel(const DfFinishJob* __restrict__ jobs) {
+  extern __shared__ int fin_smem[];
+  const DfFinishJob J = jobs[blockIdx.x];
+  int* ca = fin_smem;        // column at position
+  int* ps = fin_smem + J.n;  // position of column
+  for (int64_t i = threadIdx.x; i < J.n; i += blockDim.x) ca[i] = ps[i] = (int)i;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    const int64_t nf = *J.nfac;
+    for (int64_t c = 0; c < nf; ++c) {
+      const int pc = (int)J.piv[c];
+      const int p = ps[pc];
+      const int other = ca[c];
+      ca[p] = other;
+      ps[other] = p;
+      ca[c] = pc;
+      ps[pc] = (int)c;
+    }
+  }
+  __syncthreads();
+  const double inv = 1.0 / *J.scale;
+  for (int64_t j = threadIdx.x; j < J.n; j += blockDim.x) J.jpvt[j] = ca[j] + 1;
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  for (int64_t j = wid; j < J.n; j += nw) {
+    const float2* w = J.work + (int64_t)ca[j] * J.m;
+    for (int64_t i = lane; i < J.m; i += 32) J.B[i + j * J.ldb] = df_val(w[i].x, w[i].y) * inv;
   }
 }
 
@@ -2082,6 +2224,94 @@ static void print_qr_trace(lra_ctx* ctx, const unsigned long long* stamps, int64
     }
     std::fprintf(stderr, " %s %.2f\n", lab[7], rest / cnt / 1e3);
   }
+}
+
+// The mixed path's pivoted QR of many small sketches at once: one grouped
+// launch each for the conversion, the factorization (a CTA per matrix,
+// largest first) and the replay into column order.  Each matrix comes out
+// as geqp3_adap leaves it when its shared-memory kernel runs, bit for bit.
+bool geqp3_df_batch_fits(lra_ctx* ctx, int64_t m, int64_t n) {
+  constexpr int NTG = 544;
+  if (m < 1 || n < 1 || n >= (int64_t)XW_IDX || m > 20480) return false;
+  const size_t smem = (size_t)m * sizeof(float2) + (size_t)n * (4 * 8 + 1);
+  static size_t cap = [&] {
+    int optin = 0;
+    cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, ctx->device);
+    cudaFuncAttributes fa;
+    if (cudaFuncGetAttributes(&fa, geqp3_df_group_kernel<NTG>) != cudaSuccess) {
+      cudaGetLastError();
+      return (size_t)0;
+    }
+    return (size_t)(optin - (int)fa.sharedSizeBytes);
+  }();
+  return smem <= cap && (size_t)2 * n * sizeof(int) <= 200 * 1024;
+}
+
+void geqp3_df_batch(lra_ctx* ctx, int64_t count, const DfBatchItem* items, int64_t nb, double atol, double rtol,
+                    int64_t* k_dev) {
+  constexpr int NTG = 544;
+  if (count <= 0) return;
+  // largest factorizations first, so that the last wave is short
+  std::vector<int64_t> ord((size_t)count);
+  for (int64_t i = 0; i < count; ++i) ord[(size_t)i] = i;
+  std::stable_sort(ord.begin(), ord.end(), [&](int64_t a, int64_t b) {
+    const DfBatchItem &x = items[a], &y = items[b];
+    return x.m * x.n * std::min(x.kmax, x.m) > y.m * y.n * std::min(y.kmax, y.m);
+  });
+  std::vector<DfPrepJob> prep((size_t)count);
+  std::vector<QrJob> qr((size_t)count);
+  std::vector<DfFinishJob> fin((size_t)count);
+  size_t smem_qr = 0, smem_fin = 0;
+  for (int64_t t = 0; t < count; ++t) {
+    const int64_t i = ord[(size_t)t];
+    const DfBatchItem& it = items[i];
+    const int64_t m = it.m, n = it.n;
+    if (!geqp3_df_batch_fits(ctx, m, n)) fail(LRA_EINVAL, "geqp3_df_batch: a sketch does not fit");
+    float2* work = ctx->arena.alloc_n<float2>((size_t)m * n);
+    double* vn0 = ctx->arena.alloc_n<double>(n);
+    double* scale = ctx->arena.alloc_n<double>(1);
+    prep[(size_t)t] = DfPrepJob{m, n, it.ldb, it.B, work, vn0, scale};
+    QrJob& J = qr[(size_t)t];
+    std::memset(&J, 0, sizeof J);
+    J.P.m = m;
+    J.P.n = n;
+    J.P.lda = m;
+    J.P.tau = it.tau;
+    J.P.kmax = std::min<int64_t>(it.kmax, std::min(m, n));
+    J.P.nb = std::max<int64_t>(1, std::min<int64_t>(nb, std::max<int64_t>(J.P.kmax, 1)));
+    J.P.atol = atol;
+    J.P.rtol = rtol;
+    J.P.pivot = 1;
+    J.P.k_out = k_dev + i;
+    J.X.piv = ctx->arena.alloc_n<int64_t>(std::max<int64_t>(J.P.kmax, 1));
+    J.X.nfac = ctx->arena.alloc_n<int64_t>(1);
+    J.X.beta = ctx->arena.alloc_n<double>(std::max<int64_t>(J.P.kmax, 1));
+    J.D.vn0 = vn0;
+    J.D.scale = scale;
+    J.work = work;
+    fin[(size_t)t] = DfFinishJob{m, n, it.ldb, it.B, work, scale, J.X.piv, J.X.nfac, it.jpvt};
+    smem_qr = std::max(smem_qr, (size_t)m * sizeof(float2) + (size_t)n * (4 * 8 + 1));
+    smem_fin = std::max(smem_fin, (size_t)2 * n * sizeof(int));
+  }
+  DfPrepJob* dprep = ctx->arena.alloc_n<DfPrepJob>((size_t)count);
+  QrJob* dqr = ctx->arena.alloc_n<QrJob>((size_t)count);
+  DfFinishJob* dfin = ctx->arena.alloc_n<DfFinishJob>((size_t)count);
+  int* next = ctx->arena.alloc_n<int>(1);
+  LRA_CUDA(cudaMemcpyAsync(dprep, prep.data(), prep.size() * sizeof(DfPrepJob), cudaMemcpyHostToDevice, ctx->stream));
+  LRA_CUDA(cudaMemcpyAsync(dqr, qr.data(), qr.size() * sizeof(QrJob), cudaMemcpyHostToDevice, ctx->stream));
+  LRA_CUDA(cudaMemcpyAsync(dfin, fin.data(), fin.size() * sizeof(DfFinishJob), cudaMemcpyHostToDevice, ctx->stream));
+  LRA_CUDA(cudaMemsetAsync(next, 0, sizeof(int), ctx->stream));
+  df_prep_group_kernel<<<(unsigned)count, 512, 0, ctx->stream>>>(dprep);
+  post_launch(ctx, "df_prep_group_kernel");
+  raise_smem_limit(ctx, (const void*)geqp3_df_group_kernel<NTG>);
+  const int grid = (int)std::min<int64_t>(count, ctx->num_sms);
+  geqp3_df_group_kernel<NTG><<<grid, NTG, smem_qr, ctx->stream>>>(dqr, (int)count, next);
+  post_launch(ctx, "geqp3_df_group_kernel");
+  raise_smem_limit(ctx, (const void*)df_finish_group_kernel);
+  df_finish_group_kernel<<<(unsigned)count, 512, smem_fin, ctx->stream>>>(dfin);
+  post_launch(ctx, "df_finish_group_kernel");
+  // the host copies of the job lists must outlive the asynchronous uploads
+  LRA_CUDA(cudaStreamSynchronize(ctx->stream));
 }
 
 template <typename T>

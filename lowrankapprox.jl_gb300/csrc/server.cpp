@@ -283,6 +283,9 @@ int lra_idfact_batched(lra_ctx* ctx, int dtype, int64_t count, const lra_matdesc
   if (!ctx || !mats || !outs || count < 0 || !opts) return LRA_EINVAL;
   for (int64_t i = 0; i < count; ++i) outs[i] = nullptr;
   if (count == 0) return LRA_OK;
+  // Float64 on the mixed path: grouped launches, a CTA per matrix
+  const int g = lra::try_idfact_batched_grouped(ctx, dtype, count, mats, opts, rand, outs);
+  if (g >= 0) return g;
   size_t free_b = 0, total_b = 0;
   cudaSetDevice(ctx->device);
   if (cudaMemGetInfo(&free_b, &total_b) != cudaSuccess) {

@@ -841,7 +841,7 @@ void tc_split(lra_ctx* ctx, char trans, int64_t M, int64_t N, const T* A, int64_
 }
 
 template <typename T>
-void tc_sketch(lra_ctx* ctx, const TcSplit& sp, int64_t order, const T* S, T* B, int64_t ldb) {
+void tc_sketch(lra_ctx* ctx, const TcSplit& sp, int64_t order, const T* S, T* B, int64_t ldb, int* err_slot) {
   const int64_t K = sp.K, N = sp.N, Kp = sp.Kp;
   const int ns = sp.ns;
   const int64_t Lp = (order + TILE_N - 1) / TILE_N * TILE_N;
@@ -866,8 +866,11 @@ void tc_sketch(lra_ctx* ctx, const TcSplit& sp, int64_t order, const T* S, T* B,
     cuuint32_t box[2] = {KBLK, TILE_N};
     make_map(&tmS, St, 2, dims, strides, box);
   }
-  int* err = ctx->arena.alloc_n<int>(1);
-  LRA_CUDA(cudaMemsetAsync(err, 0, sizeof(int), ctx->stream));
+  int* err = err_slot;
+  if (!err) {
+    err = ctx->arena.alloc_n<int>(1);
+    LRA_CUDA(cudaMemsetAsync(err, 0, sizeof(int), ctx->stream));
+  }
   TcParams P;
   P.K = K;
   P.ncols = N;
@@ -885,6 +888,11 @@ void tc_sketch(lra_ctx* ctx, const TcSplit& sp, int64_t order, const T* S, T* B,
   const int64_t ntiles = ((N + TILE_M - 1) / TILE_M) * (Lp / TILE_N);
   tc_sketch_kernel<<<(unsigned)ntiles, NTHREADS, smem, ctx->stream>>>(tmA, tmS, P);
   post_launch(ctx, "tc_sketch_kernel");
+  // a caller that passes err_slot checks it later (the batch, once per round)
+  if (err_slot) {
+    ctx->arena.release(mk);
+    return;
+  }
   int herr = 0;
   LRA_CUDA(cudaMemcpyAsync(&herr, err, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
   LRA_CUDA(cudaStreamSynchronize(ctx->stream));
@@ -973,7 +981,7 @@ void tc_gemm(lra_ctx* ctx, char ta, char tb, int64_t m, int64_t n, int64_t k, do
 
 template void tc_split<float>(lra_ctx*, char, int64_t, int64_t, const float*, int64_t, int, TcSplit*, bool);
 template void tc_split<double>(lra_ctx*, char, int64_t, int64_t, const double*, int64_t, int, TcSplit*, bool);
-template void tc_sketch<float>(lra_ctx*, const TcSplit&, int64_t, const float*, float*, int64_t);
-template void tc_sketch<double>(lra_ctx*, const TcSplit&, int64_t, const double*, double*, int64_t);
+template void tc_sketch<float>(lra_ctx*, const TcSplit&, int64_t, const float*, float*, int64_t, int*);
+template void tc_sketch<double>(lra_ctx*, const TcSplit&, int64_t, const double*, double*, int64_t, int*);
 
 }  // namespace lra
