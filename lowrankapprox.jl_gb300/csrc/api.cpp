@@ -5,6 +5,7 @@
 // the singular / eigen values that decide the truncation).
 
 #include <algorithm>
+#include <chrono>
 #include <cmath>
 #include <cstdlib>
 #include <cstring>
@@ -666,6 +667,40 @@ bool grouped_batch_ok(lra_ctx* ctx, int64_t count, const lra_matdesc* mats, cons
   return true;
 }
 
+// The per-matrix launches of a batch (staging, byte slices, sketches) are
+// small; they are spread over the context's side streams so that several run
+// at once.  fan_out makes the side streams wait for the work issued so far on
+// the main stream, fan_in makes the main stream wait for the side streams.
+void fan_out(lra_ctx* ctx) {
+  for (int i = 0; i < lra_ctx::kAux; ++i)
+    if (!ctx->aux[i]) LRA_CUDA(cudaStreamCreateWithFlags(&ctx->aux[i], cudaStreamNonBlocking));
+  for (cudaEvent_t& e : ctx->aux_ev)
+    if (!e) LRA_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+  LRA_CUDA(cudaEventRecord(ctx->aux_ev[lra_ctx::kAux], ctx->stream));
+  for (int i = 0; i < lra_ctx::kAux; ++i) LRA_CUDA(cudaStreamWaitEvent(ctx->aux[i], ctx->aux_ev[lra_ctx::kAux], 0));
+}
+
+void fan_in(lra_ctx* ctx) {
+  for (int i = 0; i < lra_ctx::kAux; ++i) {
+    LRA_CUDA(cudaEventRecord(ctx->aux_ev[i], ctx->aux[i]));
+    LRA_CUDA(cudaStreamWaitEvent(ctx->stream, ctx->aux_ev[i], 0));
+  }
+}
+
+// runs fn with ctx->stream switched to side stream i (mod the count)
+template <typename Fn>
+void on_side(lra_ctx* ctx, int64_t i, Fn&& fn) {
+  cudaStream_t main = ctx->stream;
+  ctx->stream = ctx->aux[i % lra_ctx::kAux];
+  try {
+    fn();
+  } catch (...) {
+    ctx->stream = main;
+    throw;
+  }
+  ctx->stream = main;
+}
+
 void idfact_batched_grouped(lra_ctx* ctx, int64_t count, const lra_matdesc* mats, const lra_opts& oin,
                             lra_id** outs) {
   lra_opts o = oin;
@@ -676,6 +711,18 @@ void idfact_batched_grouped(lra_ctx* ctx, int64_t count, const lra_matdesc* mats
   size_t free_b = 0, total_b = 0;
   LRA_CUDA(cudaMemGetInfo(&free_b, &total_b));
   const double budget = 0.3 * (double)free_b;
+  // LRA_TRACE: host-side phase times (each phase waits for the device)
+  const bool tr = trace_on();
+  double tph[6] = {0, 0, 0, 0, 0, 0};
+  auto tnow = [] { return std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now().time_since_epoch()).count(); };
+  double tlast = tnow();
+  auto tmark = [&](int q) {
+    if (!tr) return;
+    LRA_CUDA(cudaStreamSynchronize(ctx->stream));
+    const double t = tnow();
+    tph[q] += t - tlast;
+    tlast = t;
+  };
   int64_t c0 = 0;
   while (c0 < count) {
     // a chunk whose working set stays inside the budget
@@ -694,12 +741,17 @@ void idfact_batched_grouped(lra_ctx* ctx, int64_t count, const lra_matdesc* mats
     std::vector<TcSplit> split((size_t)cn);
     int* flags = ctx->arena.alloc_n<int>((size_t)cn);
     LRA_CUDA(cudaMemsetAsync(flags, 0, (size_t)cn * sizeof(int), ctx->stream));
+    fan_out(ctx);
     for (int64_t i = 0; i < cn; ++i) {
       const lra_matdesc& d = mats[c0 + i];
-      dA[(size_t)i] = stage_in<double>(ctx, d.A, d.m, d.n, d.lda);
-      if (o.check_finite) all_finite_async(ctx, d.m, d.n, dA[(size_t)i].p, dA[(size_t)i].ld, flags + i);
-      tc_split<double>(ctx, 'n', d.m, d.n, dA[(size_t)i].p, dA[(size_t)i].ld, 6, &split[(size_t)i]);
+      on_side(ctx, i, [&] {
+        dA[(size_t)i] = stage_in<double>(ctx, d.A, d.m, d.n, d.lda);
+        if (o.check_finite) all_finite_async(ctx, d.m, d.n, dA[(size_t)i].p, dA[(size_t)i].ld, flags + i);
+        tc_split<double>(ctx, 'n', d.m, d.n, dA[(size_t)i].p, dA[(size_t)i].ld, 6, &split[(size_t)i]);
+      });
     }
+    fan_in(ctx);
+    tmark(0);
     {
       std::vector<int> hf((size_t)cn);
       LRA_CUDA(cudaMemcpyAsync(hf.data(), flags, (size_t)cn * sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
@@ -729,6 +781,7 @@ void idfact_batched_grouped(lra_ctx* ctx, int64_t count, const lra_matdesc* mats
       LRA_CUDA(cudaMemsetAsync(errs, 0, (size_t)cn * sizeof(int), ctx->stream));
       std::vector<DfBatchItem> items;
       items.reserve(act.size());
+      fan_out(ctx);
       for (const int64_t i : act) {
         St& s = st[(size_t)i];
         const lra_matdesc& d = mats[c0 + i];
@@ -739,20 +792,23 @@ void idfact_batched_grouped(lra_ctx* ctx, int64_t count, const lra_matdesc* mats
         s.B = ctx->arena.alloc_n<double>((size_t)s.order * d.n);
         s.jpvt = ctx->arena.alloc_n<int64_t>((size_t)d.n);
         s.tau = ctx->arena.alloc_n<double>((size_t)std::max<int64_t>(l, 1));
-        const ArenaMark ms = ctx->arena.mark();
+        // S stays allocated until the chunk ends: the sketches run on several streams
         double* S = ctx->arena.alloc_n<double>((size_t)s.order * d.m);
         ctx->rng_counter = s.ctr;
-        RandSrc rs(ctx, nullptr, o.seed);
-        rs.gauss(s.order * d.m, S, true);
+        on_side(ctx, i, [&] {
+          RandSrc rs(ctx, nullptr, o.seed);
+          rs.gauss(s.order * d.m, S, true);
+          tc_sketch<double>(ctx, split[(size_t)i], s.order, S, s.B, s.order, errs + i);
+        });
         s.ctr = ctx->rng_counter;
-        tc_sketch<double>(ctx, split[(size_t)i], s.order, S, s.B, s.order, errs + i);
-        // S is read by the sketch kernel, which runs before any later use of its memory
-        ctx->arena.release(ms);
         items.push_back(DfBatchItem{s.order, d.n, s.order, kmax, s.B, s.jpvt, s.tau});
       }
+      fan_in(ctx);
       std::vector<int64_t> map(act.begin(), act.end());
+      tmark(1);
       // the batch writes k of item t to kdev[t]
       geqp3_df_batch(ctx, (int64_t)items.size(), items.data(), o.nb, o.atol, o.rtol, kdev);
+      tmark(2);
       std::vector<int64_t> hk(items.size());
       std::vector<int> he((size_t)cn);
       LRA_CUDA(cudaMemcpyAsync(hk.data(), kdev, hk.size() * sizeof(int64_t), cudaMemcpyDeviceToHost, ctx->stream));
@@ -784,7 +840,9 @@ void idfact_batched_grouped(lra_ctx* ctx, int64_t count, const lra_matdesc* mats
         trsm_upper(ctx, k, nr, s.B, s.order, Tm[(size_t)i], k);
       }
     }
+    tmark(3);
     trsm_bs_batch(ctx, (int64_t)bs.size(), bs.data());
+    tmark(4);
     for (int64_t i = 0; i < cn; ++i) {
       const St& s = st[(size_t)i];
       const int64_t n = mats[c0 + i].n, k = s.k;
@@ -803,9 +861,15 @@ void idfact_batched_grouped(lra_ctx* ctx, int64_t count, const lra_matdesc* mats
       if (k > 0 && n > k) to_host(ctx, r->T, Tm[(size_t)i], (size_t)k * (n - k));
     }
     LRA_CUDA(cudaStreamSynchronize(ctx->stream));
+    tmark(5);
     ctx->arena.release(mk);
     c0 = c1;
   }
+  if (tr)
+    std::fprintf(stderr,
+                 "[lra] idfact_batched grouped, %lld matrices (ms): stage+split %.2f sketches %.2f qr %.2f "
+                 "readback %.2f solve %.2f results %.2f\n",
+                 (long long)count, tph[0], tph[1], tph[2], tph[3], tph[4], tph[5]);
 }
 
 int try_idfact_batched_grouped(lra_ctx* ctx, int dtype, int64_t count, const lra_matdesc* mats,
@@ -877,6 +941,14 @@ void lra_ctx_destroy(lra_ctx* ctx) {
   cudaSetDevice(ctx->device);
   cudaStreamSynchronize(ctx->stream);
   if (ctx->pinned) cudaFreeHost(ctx->pinned);
+  for (int i = 0; i < lra_ctx::kAux; ++i) {
+    if (ctx->aux[i]) {
+      cudaStreamSynchronize(ctx->aux[i]);
+      cudaStreamDestroy(ctx->aux[i]);
+    }
+  }
+  for (cudaEvent_t e : ctx->aux_ev)
+    if (e) cudaEventDestroy(e);
   if (ctx->own_stream) cudaStreamDestroy(ctx->stream);
   delete ctx;
 }

@@ -3,6 +3,9 @@
 #include <cstdlib>
 #include <cstdio>
 #include <cstring>
+#include <mutex>
+#include <set>
+#include <utility>
 
 #include "internal.hpp"
 
@@ -112,6 +115,13 @@ size_t Arena::capacity() const {
 }
 
 void raise_smem_limit(lra_ctx* ctx, const void* kernel) {
+  // the attribute holds a fixed value per kernel and device: set it once
+  static std::mutex mu;
+  static std::set<std::pair<const void*, int>> done;
+  {
+    std::lock_guard<std::mutex> lk(mu);
+    if (done.count({kernel, ctx->device})) return;
+  }
   int optin = 0;
   check_cuda(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, ctx->device),
              "cudaDeviceGetAttribute(MaxSharedMemoryPerBlockOptin)");
@@ -120,6 +130,8 @@ void raise_smem_limit(lra_ctx* ctx, const void* kernel) {
   check_cuda(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                   optin - (int)fa.sharedSizeBytes),
              "cudaFuncSetAttribute(MaxDynamicSharedMemorySize)");
+  std::lock_guard<std::mutex> lk(mu);
+  done.insert({kernel, ctx->device});
 }
 
 bool trace_on() {

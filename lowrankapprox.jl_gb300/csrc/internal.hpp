@@ -77,6 +77,10 @@ struct lra_ctx {
   // pinned host staging (grown on demand)
   void* pinned = nullptr;
   size_t pinned_cap = 0;
+  // side streams of the batched path and their join events (made on first use)
+  static constexpr int kAux = 8;
+  cudaStream_t aux[kAux] = {};
+  cudaEvent_t aux_ev[kAux + 1] = {};
 };
 
 namespace lra {

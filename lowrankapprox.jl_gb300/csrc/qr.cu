@@ -435,6 +435,7 @@ struct QrV2Extra {
 // floating-point norms order like the norms).
 constexpr int QCH = 16;  // rows per lane per register chunk (512 rows)
 constexpr int QG = 4;    // rows per lane issued between uniform range checks
+constexpr int QRPL = 4;  // rows per lane loaded ahead in the double-float QR's column loops
 constexpr unsigned char ST_LIVE = 1, ST_DONE = 2, ST_FLAG = 4, ST_UPD = 8;
 
 __device__ __forceinline__ long long norm_key(double v) {
@@ -1369,6 +1370,7 @@ __device__ __forceinline__ void geqp3_df_body(const QrParams<double>& P, const Q
   __shared__ unsigned long long s_win;
   __shared__ int s_owner, s_stop, s_ok;
   __shared__ double s_taud, s_betad;
+  __shared__ int s_nflag;
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
   const int64_t m = P.m, n = P.n, lda = P.lda;
   const int64_t c0 = n * b / G, c1 = n * (b + 1) / G;
@@ -1382,7 +1384,8 @@ __device__ __forceinline__ void geqp3_df_body(const QrParams<double>& P, const Q
   Df* s_vn2 = s_vn1 + ncap;
   Df* s_dot = s_vn2 + ncap;
   Df* s_fs = s_dot + ncap;  // f scal of each column for the deferred update
-  unsigned char* s_st = reinterpret_cast<unsigned char*>(s_fs + ncap);
+  float2* s_x0 = reinterpret_cast<float2*>(s_fs + ncap);  // row c of each column
+  unsigned char* s_st = reinterpret_cast<unsigned char*>(s_x0 + ncap);
   float* __restrict__ Bh = D.Bh;
   float* __restrict__ Bl = D.Bl;
   const float tol3z = (float)sqrt(Real<double>::eps);
@@ -1602,7 +1605,14 @@ __device__ __forceinline__ void geqp3_df_body(const QrParams<double>& P, const Q
       const int64_t pvt = (int64_t)(XW_IDX - (s_win & XW_IDX));
       const int owner = s_owner;
       stamp(c, 0);
-      if (owner == b && threadIdx.x == 0) s_st[pvt - c0] |= ST_DONE;
+      // the pivot column is done; the previous step's deferred-update marks
+      // are cleared (a thread per slot, so each byte has one writer)
+      for (int s = threadIdx.x; s < nloc; s += NT) {
+        unsigned char st = (unsigned char)(s_st[s] & ~ST_UPD);
+        if (owner == b && s == pvt - c0) st |= ST_DONE;
+        s_st[s] = st;
+      }
+      if (threadIdx.x == 0) s_nflag = 0;
       // ---- the pivot column's rows c..m-1 from the winner's stage, and the
       // per-warp partial sums of squares of rows c+1..m-1
       {
@@ -1657,14 +1667,33 @@ __device__ __forceinline__ void geqp3_df_body(const QrParams<double>& P, const Q
           const float2* cg[4];
 #pragma unroll
           for (int g = 0; g < 4; ++g) cg[g] = C + (int64_t)(q[g] >= 0 ? q[g] : q[0]) * m;
+          // row c of the column, for the update that follows the dots
+          {
+            const int g = lane >> 3;
+            const int qg = g == 0 ? q[0] : g == 1 ? q[1] : g == 2 ? q[2] : q[3];
+            if ((lane & 7) == 0 && qg >= 0) s_x0[qg] = C[(int64_t)qg * m + c];
+          }
+          // QRPL rows per lane are loaded before they are used, so that a
+          // quad has 4 QRPL loads in flight (the global-memory form waits
+          // an L2 round trip per chunk); each lane still adds its rows in
+          // increasing order
           Df d[4] = {{0.f, 0.f}, {0.f, 0.f}, {0.f, 0.f}, {0.f, 0.f}};
-          for (int64_t i = c + 1 + lane; i < m; i += 32) {
-            const float2 v = V[i];
+          for (int64_t b0 = c + 1; b0 < m; b0 += 32 * QRPL) {
+            float2 xv[QRPL], xc[4][QRPL];
 #pragma unroll
-            for (int g = 0; g < 4; ++g) {
-              const float2 x = cg[g][i];
-              df_fma_acc(d[g], v.x, v.y, x.x, x.y);
+            for (int r = 0; r < QRPL; ++r) {
+              const int64_t i = b0 + lane + 32 * r;
+              const bool in = i < m;
+              xv[r] = in ? V[i] : make_float2(0.f, 0.f);
+#pragma unroll
+              for (int g = 0; g < 4; ++g) xc[g][r] = in ? cg[g][i] : make_float2(0.f, 0.f);
             }
+#pragma unroll
+            for (int r = 0; r < QRPL; ++r)
+              if (b0 + lane + 32 * r < m) {
+#pragma unroll
+                for (int g = 0; g < 4; ++g) df_fma_acc(d[g], xv[r].x, xv[r].y, xc[g][r].x, xc[g][r].y);
+              }
           }
 #pragma unroll
           for (int g = 0; g < 4; ++g) d[g] = quick_two_sum(d[g].h, d[g].l);
@@ -1688,89 +1717,84 @@ __device__ __forceinline__ void geqp3_df_body(const QrParams<double>& P, const Q
       const double tau = s_taud;
       const Df scal = s_f;
       stamp(c, 3);
-      // ---- updates, norm downdates and the warp's candidate ---------------------
+      // ---- a thread per column: f, the new row c, the norm downdate and the
+      // candidate word; the columns whose downdate is unreliable are flagged
       unsigned long long ww = 0;
       int wfl = 0;
       auto sub = [&](int ph) {
-        if (D.stamps && b == 0 && threadIdx.x == 32 && c < P.kmax) D.stamps[c * 16 + ph] = globaltimer_ns();
+        if (D.stamps && b == 0 && threadIdx.x == 0 && c < P.kmax) D.stamps[c * 16 + ph] = globaltimer_ns();
       };
-      if (wid > 0) {
-        sub(8);
+      sub(8);
+      {
         const Df tdf = s_tau;
-        int s = wid - 1;
-        int q[4];
-        while (quad(s, q)) {
-          // lane 8g holds column g's row c and its factors f, f scal
-          const int g = lane >> 3;
-          const int qg = g == 0 ? q[0] : g == 1 ? q[1] : g == 2 ? q[2] : q[3];
-          const bool mine = (lane & 7) == 0 && qg >= 0;
-          float2 x0 = make_float2(0.f, 0.f);
+        for (int s = threadIdx.x; s < nloc; s += NT) {
+          const unsigned char st = s_st[s];
+          if (st & ST_DONE) continue;
+          const float2 x0 = len > 0 ? s_x0[s] : C[(int64_t)s * m + c];
           Df f{0.f, 0.f}, fs{0.f, 0.f};
-          if (mine) {
-            x0 = C[(int64_t)qg * m + c];
-            if (tau != 0 && len > 0) {
-              f = df_mul(tdf, df_add(Df{x0.x, x0.y}, df_mul(scal, s_dot[qg])));
-              fs = df_mul(f, scal);
+          if (tau != 0 && len > 0) {
+            f = df_mul(tdf, df_add(Df{x0.x, x0.y}, df_mul(scal, s_dot[s])));
+            fs = df_mul(f, scal);
+          }
+          s_fs[s] = fs;
+          const Df a = df_add(Df{x0.x, x0.y}, df_neg(f));
+          C[(int64_t)s * m + c] = make_float2(a.h, a.l);
+          Df v1 = s_vn1[s];
+          bool flagged = false;
+          if (c < lastrk - 1 && v1.h != 0.f) {
+            // LAPACK's partial-norm downdate, in double-float
+            Df temp = df_div(a.h < 0.f ? df_neg(a) : a, v1);
+            temp = df_mul(df_add(Df{1.f, 0.f}, temp), df_add(Df{1.f, 0.f}, df_neg(temp)));
+            if (temp.h < 0.f) temp = Df{0.f, 0.f};
+            const Df r = df_div(v1, s_vn2[s]);
+            const Df temp2 = df_mul(temp, df_mul(r, r));
+            if (temp2.h <= tol3z) {
+              flagged = true;
+            } else {
+              v1 = df_mul(v1, df_sqrt(temp));
+              s_vn1[s] = v1;
             }
           }
-          if (mine) s_fs[qg] = fs;
-          sub(9);
-          sub(10);
-          // lane 8g: column g's new row c, its norm downdate and word
-          int flagged = 0;
-          Df v1{0.f, 0.f};
-          if (mine) {
-            const Df a = df_add(Df{x0.x, x0.y}, df_neg(f));
-            C[(int64_t)qg * m + c] = make_float2(a.h, a.l);
-            v1 = s_vn1[qg];
-            if (c < lastrk - 1 && v1.h != 0.f) {
-              // LAPACK's partial-norm downdate, in double-float
-              Df temp = df_div(a.h < 0.f ? df_neg(a) : a, v1);
-              temp = df_mul(df_add(Df{1.f, 0.f}, temp), df_add(Df{1.f, 0.f}, df_neg(temp)));
-              if (temp.h < 0.f) temp = Df{0.f, 0.f};
-              const Df r = df_div(v1, s_vn2[qg]);
-              const Df temp2 = df_mul(temp, df_mul(r, r));
-              if (temp2.h <= tol3z) {
-                flagged = 1;
-              } else {
-                v1 = df_mul(v1, df_sqrt(temp));
-                s_vn1[qg] = v1;
-              }
-            }
-          }
-          unsigned fm = __ballot_sync(0xffffffffu, flagged);
-          sub(11);
-          // unreliable downdates: the column's update now, and the norm of
-          // its rows c+1..m-1 (xLAQPS would end the block here and recompute
-          // the norm before the next pivot, from the same updated column)
-          wfl |= fm != 0;
-          while (fm) {
-            const int L = __ffs(fm) - 1;
-            fm &= fm - 1;
-            const int qf = __shfl_sync(0xffffffffu, qg, L);
-            const Df ff{__shfl_sync(0xffffffffu, fs.h, L), __shfl_sync(0xffffffffu, fs.l, L)};
-            float2* col = C + (int64_t)qf * m;
-            if (ff.h != 0.f)
-              for (int64_t i = c + 1 + lane; i < m; i += 32) {
-                const float2 x = col[i], v = V[i];
-                const Df y = df_axpy_neg(x.x, x.y, ff, v.x, v.y);
-                col[i] = make_float2(y.h, y.l);
-              }
-            __syncwarp();
-            if (lane == 0) s_st[qf] |= ST_UPD;
-            const double nr = col_nrm2(col, c + 1);
-            if (lane == L) {
-              v1 = df_split(nr);
-              s_vn1[qf] = s_vn2[qf] = v1;
-            }
-          }
-          sub(12);
-          if (mine) {
-            const unsigned long long w = xw_pack(v1, c0 + qg);
+          if (flagged) {
+            s_st[s] = st | ST_FLAG;
+            atomicAdd(&s_nflag, 1);
+          } else {
+            const unsigned long long w = xw_pack(v1, c0 + s);
             ww = w > ww ? w : ww;
           }
         }
       }
+      __syncthreads();
+      sub(9);
+      // unreliable downdates, a warp per column: its update now and the norm
+      // of its rows c+1..m-1 (xLAQPS would end the block here and recompute
+      // the norm before the next pivot, from the same updated column)
+      if (s_nflag > 0) {
+        wfl = 1;
+        for (int s = wid; s < nloc; s += NW) {
+          if (!(s_st[s] & ST_FLAG)) continue;
+          float2* col = C + (int64_t)s * m;
+          const Df ff = s_fs[s];
+          if (ff.h != 0.f)
+            for (int64_t i = c + 1 + lane; i < m; i += 32) {
+              const float2 x = col[i], v = V[i];
+              const Df y = df_axpy_neg(x.x, x.y, ff, v.x, v.y);
+              col[i] = make_float2(y.h, y.l);
+            }
+          __syncwarp();
+          const double nr = col_nrm2(col, c + 1);
+          if (lane == 0) {
+            const Df v1 = df_split(nr);
+            s_vn1[s] = s_vn2[s] = v1;
+            s_st[s] = (unsigned char)((s_st[s] & ~ST_FLAG) | ST_UPD);
+            const unsigned long long w = xw_pack(v1, c0 + s);
+            ww = w > ww ? w : ww;
+          }
+        }
+      }
+      sub(10);
+      sub(11);
+      sub(12);
       warp_word(ww, wfl);
       sub(13);
       const bool small = fabs(s_betad) <= ptol;
@@ -1812,35 +1836,38 @@ __device__ __forceinline__ void geqp3_df_body(const QrParams<double>& P, const Q
             }
           }
         }
-        int s = wid - 1;
-        int q[4];
-        while (quad(s, q)) {
-          Df fq[4];
-          float2* cg[4];
-          bool u[4];
+        // the rank-1 updates of rows c+1..m-1, QRPL elements per thread at a
+        // time over all (column, row) pairs, loads before stores
+        const int len32 = (int)len;
+        const int E = nloc * len32;
+        for (int e0 = ct; e0 < E; e0 += NCT * QRPL) {
+          float2 xv[QRPL], xc[QRPL];
+          Df fq[QRPL];
+          int64_t at[QRPL];
+          bool u[QRPL];
 #pragma unroll
-          for (int h = 0; h < 4; ++h) {
-            const int qh = q[h] >= 0 ? q[h] : q[0];
-            cg[h] = C + (int64_t)qh * m;
-            fq[h] = s_fs[qh];
-            u[h] = q[h] >= 0 && fq[h].h != 0.f && !(s_st[qh] & ST_UPD);
-          }
-          if (u[0] || u[1] || u[2] || u[3]) {
-            for (int64_t i = c + 1 + lane; i < m; i += 32) {
-              const float2 v = V[i];
-#pragma unroll
-              for (int h = 0; h < 4; ++h) {
-                if (u[h]) {
-                  const float2 x = cg[h][i];
-                  const Df y = df_axpy_neg(x.x, x.y, fq[h], v.x, v.y);
-                  cg[h][i] = make_float2(y.h, y.l);
-                }
+          for (int q = 0; q < QRPL; ++q) {
+            const int e = e0 + q * NCT;
+            u[q] = false;
+            at[q] = 0;
+            if (e < E) {
+              const int sl = e / len32;
+              const int64_t i = c + 1 + (e - sl * len32);
+              fq[q] = s_fs[sl];
+              u[q] = !(s_st[sl] & (ST_DONE | ST_UPD)) && fq[q].h != 0.f;
+              at[q] = (int64_t)sl * m + i;
+              if (u[q]) {
+                xc[q] = C[at[q]];
+                xv[q] = V[i];
               }
             }
           }
-          __syncwarp();
-          const int qh = lane == 0 ? q[0] : lane == 1 ? q[1] : lane == 2 ? q[2] : lane == 3 ? q[3] : -1;
-          if (qh >= 0) s_st[qh] &= (unsigned char)~ST_UPD;
+#pragma unroll
+          for (int q = 0; q < QRPL; ++q)
+            if (u[q]) {
+              const Df y = df_axpy_neg(xc[q].x, xc[q].y, fq[q], xv[q].x, xv[q].y);
+              C[at[q]] = make_float2(y.h, y.l);
+            }
         }
       }
       if (!collect(e)) return;
@@ -1907,29 +1934,40 @@ __global__ void __launch_bounds__(NT, 1) geqp3_df_group_kernel(const QrJob* __re
   }
 }
 
-// ---- the batch's conversions, a CTA per matrix ---------------------------------
+// ---- the batch's conversions ---------------------------------------------------
 // prep: max |B| (its power-of-two scale as df_scale_kernel), the scaled
 // float pairs into the workspace and each column's norm as df_split_kernel
 // (the same per-warp arithmetic, so the norms agree bit for bit)
 struct DfPrepJob {
   int64_t m, n, ldb;
   const double* B;
-  float2* work;   // m x n
-  double* vn0;    // n
-  double* scale;  // 1
+  float2* work;                // m x n
+  double* vn0;                 // n
+  double* scale;               // 1
+  unsigned long long* maxbits;  // 1, zeroed: max |B| as the bits of a double
 };
 
-__global__ void __launch_bounds__(512) df_prep_group_kernel(const DfPrepJob* __restrict__ jobs) {
+// CTAs (matrix, part): max |B| of every part's columns into maxbits
+__global__ void __launch_bounds__(512) df_prep_max_kernel(const DfPrepJob* __restrict__ jobs) {
   __shared__ double red[32];
   const DfPrepJob J = jobs[blockIdx.x];
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
   double mx = 0;
-  for (int64_t j = wid; j < J.n; j += nw)
+  for (int64_t j = (int64_t)blockIdx.y * nw + wid; j < J.n; j += (int64_t)gridDim.y * nw)
     for (int64_t i = lane; i < J.m; i += 32) mx = fmax(mx, fabs(J.B[i + j * J.ldb]));
   mx = block_max(mx, red);
+  if (threadIdx.x == 0 && mx > 0) atomicMax(J.maxbits, (unsigned long long)__double_as_longlong(mx));
+}
+
+// CTAs (matrix, part): the scaled float pairs and each column's norm, a warp
+// per column
+__global__ void __launch_bounds__(512) df_prep_split_kernel(const DfPrepJob* __restrict__ jobs) {
+  const DfPrepJob J = jobs[blockIdx.x];
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  const double mx = __longlong_as_double((long long)*J.maxbits);
   const double sc = mx > 0 ? ldexp(1.0, -(ilogb(mx) + 1)) : 1.0;
-  if (threadIdx.x == 0) *J.scale = sc;
-  for (int64_t j = wid; j < J.n; j += nw) {
+  if (blockIdx.y == 0 && threadIdx.x == 0) *J.scale = sc;
+  for (int64_t j = (int64_t)blockIdx.y * nw + wid; j < J.n; j += (int64_t)gridDim.y * nw) {
     float2* w = J.work + j * J.m;
     double cm = 0;
     for (int64_t i = lane; i < J.m; i += 32) {
@@ -2233,7 +2271,7 @@ static void print_qr_trace(lra_ctx* ctx, const unsigned long long* stamps, int64
 bool geqp3_df_batch_fits(lra_ctx* ctx, int64_t m, int64_t n) {
   constexpr int NTG = 544;
   if (m < 1 || n < 1 || n >= (int64_t)XW_IDX || m > 20480) return false;
-  const size_t smem = (size_t)m * sizeof(float2) + (size_t)n * (4 * 8 + 1);
+  const size_t smem = (size_t)m * sizeof(float2) + (size_t)n * (5 * 8 + 1);
   static size_t cap = [&] {
     int optin = 0;
     cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, ctx->device);
@@ -2262,6 +2300,10 @@ void geqp3_df_batch(lra_ctx* ctx, int64_t count, const DfBatchItem* items, int64
   std::vector<QrJob> qr((size_t)count);
   std::vector<DfFinishJob> fin((size_t)count);
   size_t smem_qr = 0, smem_fin = 0;
+  unsigned long long* maxbits = ctx->arena.alloc_n<unsigned long long>((size_t)count);
+  LRA_CUDA(cudaMemsetAsync(maxbits, 0, (size_t)count * sizeof(unsigned long long), ctx->stream));
+  int64_t nmax = 1;
+  for (int64_t i = 0; i < count; ++i) nmax = std::max(nmax, items[i].n);
   for (int64_t t = 0; t < count; ++t) {
     const int64_t i = ord[(size_t)t];
     const DfBatchItem& it = items[i];
@@ -2270,7 +2312,7 @@ void geqp3_df_batch(lra_ctx* ctx, int64_t count, const DfBatchItem* items, int64
     float2* work = ctx->arena.alloc_n<float2>((size_t)m * n);
     double* vn0 = ctx->arena.alloc_n<double>(n);
     double* scale = ctx->arena.alloc_n<double>(1);
-    prep[(size_t)t] = DfPrepJob{m, n, it.ldb, it.B, work, vn0, scale};
+    prep[(size_t)t] = DfPrepJob{m, n, it.ldb, it.B, work, vn0, scale, maxbits + t};
     QrJob& J = qr[(size_t)t];
     std::memset(&J, 0, sizeof J);
     J.P.m = m;
@@ -2290,8 +2332,16 @@ void geqp3_df_batch(lra_ctx* ctx, int64_t count, const DfBatchItem* items, int64
     J.D.scale = scale;
     J.work = work;
     fin[(size_t)t] = DfFinishJob{m, n, it.ldb, it.B, work, scale, J.X.piv, J.X.nfac, it.jpvt};
-    smem_qr = std::max(smem_qr, (size_t)m * sizeof(float2) + (size_t)n * (4 * 8 + 1));
+    smem_qr = std::max(smem_qr, (size_t)m * sizeof(float2) + (size_t)n * (5 * 8 + 1));
     smem_fin = std::max(smem_fin, (size_t)2 * n * sizeof(int));
+  }
+  // LRA_TRACE: the phase stamps of the largest factorization
+  unsigned long long* stamps = nullptr;
+  if (trace_on()) {
+    const int64_t km = std::max<int64_t>(qr[0].P.kmax, 1);
+    stamps = ctx->arena.alloc_n<unsigned long long>((size_t)16 * km);
+    LRA_CUDA(cudaMemsetAsync(stamps, 0, (size_t)16 * km * 8, ctx->stream));
+    qr[0].D.stamps = stamps;
   }
   DfPrepJob* dprep = ctx->arena.alloc_n<DfPrepJob>((size_t)count);
   QrJob* dqr = ctx->arena.alloc_n<QrJob>((size_t)count);
@@ -2301,15 +2351,44 @@ void geqp3_df_batch(lra_ctx* ctx, int64_t count, const DfBatchItem* items, int64
   LRA_CUDA(cudaMemcpyAsync(dqr, qr.data(), qr.size() * sizeof(QrJob), cudaMemcpyHostToDevice, ctx->stream));
   LRA_CUDA(cudaMemcpyAsync(dfin, fin.data(), fin.size() * sizeof(DfFinishJob), cudaMemcpyHostToDevice, ctx->stream));
   LRA_CUDA(cudaMemsetAsync(next, 0, sizeof(int), ctx->stream));
-  df_prep_group_kernel<<<(unsigned)count, 512, 0, ctx->stream>>>(dprep);
-  post_launch(ctx, "df_prep_group_kernel");
+  cudaEvent_t ev[4];
+  const bool tr = trace_on();
+  if (tr)
+    for (auto& e : ev) LRA_CUDA(cudaEventCreate(&e));
+  if (tr) LRA_CUDA(cudaEventRecord(ev[0], ctx->stream));
+  {
+    const unsigned parts = (unsigned)std::min<int64_t>(16, (nmax + 15) / 16);
+    df_prep_max_kernel<<<dim3((unsigned)count, parts), 512, 0, ctx->stream>>>(dprep);
+    post_launch(ctx, "df_prep_max_kernel");
+    df_prep_split_kernel<<<dim3((unsigned)count, parts), 512, 0, ctx->stream>>>(dprep);
+    post_launch(ctx, "df_prep_split_kernel");
+  }
+  if (tr) LRA_CUDA(cudaEventRecord(ev[1], ctx->stream));
   raise_smem_limit(ctx, (const void*)geqp3_df_group_kernel<NTG>);
   const int grid = (int)std::min<int64_t>(count, ctx->num_sms);
   geqp3_df_group_kernel<NTG><<<grid, NTG, smem_qr, ctx->stream>>>(dqr, (int)count, next);
   post_launch(ctx, "geqp3_df_group_kernel");
+  if (tr) LRA_CUDA(cudaEventRecord(ev[2], ctx->stream));
   raise_smem_limit(ctx, (const void*)df_finish_group_kernel);
   df_finish_group_kernel<<<(unsigned)count, 512, smem_fin, ctx->stream>>>(dfin);
   post_launch(ctx, "df_finish_group_kernel");
+  if (tr) {
+    LRA_CUDA(cudaEventRecord(ev[3], ctx->stream));
+    LRA_CUDA(cudaEventSynchronize(ev[3]));
+    float a = 0, b = 0, c = 0;
+    cudaEventElapsedTime(&a, ev[0], ev[1]);
+    cudaEventElapsedTime(&b, ev[1], ev[2]);
+    cudaEventElapsedTime(&c, ev[2], ev[3]);
+    int64_t piv = 0, mn = 0;
+    for (const DfBatchItem* it = items; it < items + count; ++it) {
+      piv += std::min(it->kmax, std::min(it->m, it->n));
+      mn += it->m * it->n;
+    }
+    std::fprintf(stderr, "[lra] geqp3_df_batch %lld sketches (%.1f MB, <= %lld pivots): prep %.3f ms qr %.3f ms finish %.3f ms\n",
+                 (long long)count, 8e-6 * (double)mn, (long long)piv, a, b, c);
+    print_qr_trace(ctx, stamps, qr[0].P.kmax, qr[0].P.m, qr[0].P.n, "geqp3_df_group_kernel", true, nullptr, 1);
+    for (auto& e : ev) cudaEventDestroy(e);
+  }
   // the host copies of the job lists must outlive the asynchronous uploads
   LRA_CUDA(cudaStreamSynchronize(ctx->stream));
 }
@@ -2420,7 +2499,7 @@ int64_t geqp3_adap(lra_ctx* ctx, int64_t m, int64_t n, T* A, int64_t lda, int64_
       const int gsm = (int)std::min<int64_t>(std::min(ctx->num_sms, 256),
                                              std::max<int64_t>(1, (n + NTS / 32 - 2) / (NTS / 32 - 1)));
       const int64_t ncap = (n + gsm - 1) / gsm;
-      const size_t smem_s = (size_t)m * sizeof(float2) + (size_t)ncap * m * sizeof(float2) + (size_t)ncap * (4 * 8 + 1);
+      const size_t smem_s = (size_t)m * sizeof(float2) + (size_t)ncap * m * sizeof(float2) + (size_t)ncap * (5 * 8 + 1);
       bool smq = n < (int64_t)XW_IDX && qr_smem_enabled();
       if (smq) {
         raise_smem_limit(ctx, (const void*)geqp3_df_smem_kernel<NTS>);

@@ -888,11 +888,11 @@ void tc_sketch(lra_ctx* ctx, const TcSplit& sp, int64_t order, const T* S, T* B,
   const int64_t ntiles = ((N + TILE_M - 1) / TILE_M) * (Lp / TILE_N);
   tc_sketch_kernel<<<(unsigned)ntiles, NTHREADS, smem, ctx->stream>>>(tmA, tmS, P);
   post_launch(ctx, "tc_sketch_kernel");
-  // a caller that passes err_slot checks it later (the batch, once per round)
-  if (err_slot) {
-    ctx->arena.release(mk);
-    return;
-  }
+  // a caller that passes err_slot checks it later (the batch, once per
+  // round) and releases the transposed sketch with its own arena mark: the
+  // batch issues sketches on several streams, so this memory may not be
+  // reused before they have all run
+  if (err_slot) return;
   int herr = 0;
   LRA_CUDA(cudaMemcpyAsync(&herr, err, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
   LRA_CUDA(cudaStreamSynchronize(ctx->stream));
