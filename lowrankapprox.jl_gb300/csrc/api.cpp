@@ -92,6 +92,46 @@ void* hmalloc(size_t bytes) {
   return p;
 }
 
+// A slab holds many result arrays at once (the batched path copies all its
+// results in one transfer); it goes back to the cache when the last array in
+// it has been freed.  Every array must start strictly inside its slab.
+struct Slab {
+  size_t size;
+  int refs;
+  bool pinned;
+};
+std::map<char*, Slab> g_slabs;  // by base address
+
+char* hslab(size_t bytes, int refs) {
+  char* p = nullptr;
+  bool pinned = false;
+  {
+    std::lock_guard<std::mutex> lk(g_pin_mu);
+    auto it = g_pin_free.lower_bound(bytes);
+    if (it != g_pin_free.end() && it->first <= 2 * bytes) {
+      p = static_cast<char*>(it->second);
+      bytes = it->first;
+      g_pin_cached -= it->first;
+      g_pin_free.erase(it);
+      pinned = true;
+    }
+  }
+  if (!p) {
+    void* q = nullptr;
+    if (cudaHostAlloc(&q, bytes, cudaHostAllocPortable) == cudaSuccess && q) {
+      p = static_cast<char*>(q);
+      pinned = true;
+    } else {
+      cudaGetLastError();
+      p = static_cast<char*>(std::malloc(bytes));
+      if (!p) fail(LRA_ENOMEM, "host allocation of %zu bytes", bytes);
+    }
+  }
+  std::lock_guard<std::mutex> lk(g_pin_mu);
+  g_slabs[p] = Slab{bytes, refs, pinned};
+  return p;
+}
+
 void hfree(void* p) {
   if (!p) return;
   {
@@ -107,6 +147,26 @@ void hfree(void* p) {
         cudaFreeHost(p);
       }
       return;
+    }
+    auto sl = g_slabs.upper_bound(static_cast<char*>(p));
+    if (sl != g_slabs.begin()) {
+      --sl;
+      char* base = sl->first;
+      if (static_cast<char*>(p) >= base && static_cast<char*>(p) < base + sl->second.size) {
+        if (--sl->second.refs == 0) {
+          const Slab s = sl->second;
+          g_slabs.erase(sl);
+          if (!s.pinned) {
+            std::free(base);
+          } else if (g_pin_cached + s.size <= kPinCacheCap) {
+            g_pin_free.emplace(s.size, base);
+            g_pin_cached += s.size;
+          } else {
+            cudaFreeHost(base);
+          }
+        }
+        return;
+      }
     }
   }
   std::free(p);
@@ -843,6 +903,21 @@ void idfact_batched_grouped(lra_ctx* ctx, int64_t count, const lra_matdesc* mats
     tmark(3);
     trsm_bs_batch(ctx, (int64_t)bs.size(), bs.data());
     tmark(4);
+    // the results of the chunk packed on the device and copied in one
+    // transfer into a page-locked slab: per matrix jpvt (sk then rd) and T,
+    // with 8 bytes of padding so that every array starts inside the slab
+    std::vector<size_t> off((size_t)cn + 1, 0);
+    std::vector<PackItem> pk((size_t)cn);
+    for (int64_t i = 0; i < cn; ++i) {
+      const int64_t n = mats[c0 + i].n, k = st[(size_t)i].k;
+      pk[(size_t)i] = PackItem{n, k * (n - k), st[(size_t)i].jpvt, Tm[(size_t)i], off[(size_t)i]};
+      off[(size_t)i + 1] = off[(size_t)i] + 8 * (size_t)(n + k * (n - k) + 1);
+    }
+    const size_t total = off[(size_t)cn];
+    char* dout = ctx->arena.alloc_n<char>(total);
+    pack_results(ctx, cn, pk.data(), dout);
+    char* slab = hslab(total, (int)(3 * cn));
+    LRA_CUDA(cudaMemcpyAsync(slab, dout, total, cudaMemcpyDeviceToHost, ctx->stream));
     for (int64_t i = 0; i < cn; ++i) {
       const St& s = st[(size_t)i];
       const int64_t n = mats[c0 + i].n, k = s.k;
@@ -853,12 +928,10 @@ void idfact_batched_grouped(lra_ctx* ctx, int64_t count, const lra_matdesc* mats
       r->nsteps = s.nsteps;
       r->k = k;
       r->n = n;
-      r->sk = static_cast<int64_t*>(hmalloc(sizeof(int64_t) * std::max<int64_t>(k, 1)));
-      r->rd = static_cast<int64_t*>(hmalloc(sizeof(int64_t) * std::max<int64_t>(n - k, 1)));
-      r->T = hmalloc(sizeof(double) * std::max<int64_t>(k * (n - k), 1));
-      to_host(ctx, r->sk, s.jpvt, k);
-      to_host(ctx, r->rd, s.jpvt + k, n - k);
-      if (k > 0 && n > k) to_host(ctx, r->T, Tm[(size_t)i], (size_t)k * (n - k));
+      char* base = slab + off[(size_t)i];
+      r->sk = reinterpret_cast<int64_t*>(base);
+      r->rd = reinterpret_cast<int64_t*>(base) + k;
+      r->T = base + 8 * (size_t)n;
     }
     LRA_CUDA(cudaStreamSynchronize(ctx->stream));
     tmark(5);

@@ -1355,6 +1355,23 @@ void trsm_bs_batch(lra_ctx* ctx, int64_t count, const BsItem* items) {
   LRA_CUDA(cudaStreamSynchronize(ctx->stream));
 }
 
+__global__ void pack_results_kernel(const PackItem* __restrict__ items, char* __restrict__ out) {
+  const PackItem it = items[blockIdx.x];
+  int64_t* p = reinterpret_cast<int64_t*>(out + it.off);
+  for (int64_t i = threadIdx.x; i < it.n; i += blockDim.x) p[i] = it.jpvt[i];
+  double* t = reinterpret_cast<double*>(out + it.off + 8 * (size_t)it.n);
+  for (int64_t i = threadIdx.x; i < it.nt; i += blockDim.x) t[i] = it.T[i];
+}
+
+void pack_results(lra_ctx* ctx, int64_t count, const PackItem* items, char* out) {
+  if (count <= 0) return;
+  PackItem* d = ctx->arena.alloc_n<PackItem>((size_t)count);
+  LRA_CUDA(cudaMemcpyAsync(d, items, (size_t)count * sizeof(PackItem), cudaMemcpyHostToDevice, ctx->stream));
+  pack_results_kernel<<<(unsigned)count, 256, 0, ctx->stream>>>(d, out);
+  post_launch(ctx, "pack_results_kernel");
+  LRA_CUDA(cudaStreamSynchronize(ctx->stream));
+}
+
 template void trsm_bs<float>(lra_ctx*, int64_t, int64_t, const float*, int64_t, float*, int64_t);
 template void trsm_bs<double>(lra_ctx*, int64_t, int64_t, const double*, int64_t, double*, int64_t);
 template void trsm_left_diag<float>(lra_ctx*, int, int64_t, const float*, int64_t, float*, int64_t);

@@ -187,6 +187,15 @@ struct BsItem {
   double* T;
 };
 void trsm_bs_batch(lra_ctx* ctx, int64_t count, const BsItem* items);
+// the batch's results into one device buffer: at byte offset off, n int64
+// (jpvt, 1-based) then nt doubles (T)
+struct PackItem {
+  int64_t n, nt;
+  const int64_t* jpvt;
+  const double* T;
+  size_t off;
+};
+void pack_results(lra_ctx* ctx, int64_t count, const PackItem* items, char* out);
 template <typename T>
 void trsm_upper(lra_ctx* ctx, int64_t k, int64_t nrhs, const T* R, int64_t ldr, T* X,
                 int64_t ldx);

@@ -436,6 +436,8 @@ struct QrV2Extra {
 constexpr int QCH = 16;  // rows per lane per register chunk (512 rows)
 constexpr int QG = 4;    // rows per lane issued between uniform range checks
 constexpr int QRPL = 4;  // rows per lane loaded ahead in the double-float QR's column loops
+constexpr int kQrSeqLen = 96;  // columns this short (below the pivot row) are summed row by row
+constexpr int QSEQB = 8;  // rows loaded ahead by a thread that walks a column
 constexpr unsigned char ST_LIVE = 1, ST_DONE = 2, ST_FLAG = 4, ST_UPD = 8;
 
 __device__ __forceinline__ long long norm_key(double v) {
@@ -1359,7 +1361,7 @@ __device__ __forceinline__ unsigned long long xw_pack(Df v, int64_t j) {
 template <int NT, bool GCOL>
 __device__ __forceinline__ void geqp3_df_body(const QrParams<double>& P, const QrV2Extra& X, const QrDf& D,
                                               const QrSm& S, const int G, const int b, float2* Cg,
-                                              unsigned char* qr_dyn) {
+                                              const int64_t gcs, const int64_t grs, unsigned char* qr_dyn) {
   constexpr int NW = NT / 32;
   constexpr int NCW = NW - 1;  // column warps
   __shared__ Df s_part[NW];
@@ -1370,7 +1372,6 @@ __device__ __forceinline__ void geqp3_df_body(const QrParams<double>& P, const Q
   __shared__ unsigned long long s_win;
   __shared__ int s_owner, s_stop, s_ok;
   __shared__ double s_taud, s_betad;
-  __shared__ int s_nflag;
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
   const int64_t m = P.m, n = P.n, lda = P.lda;
   const int64_t c0 = n * b / G, c1 = n * (b + 1) / G;
@@ -1380,6 +1381,10 @@ __device__ __forceinline__ void geqp3_df_body(const QrParams<double>& P, const Q
   // the CTA's columns, slot s = column c0 + s: shared memory, or (GCOL) a
   // global m x n workspace
   float2* C = GCOL ? Cg : V + m;
+  // element (row i, slot s) at C[s cs + i rs]: column-major in shared
+  // memory; the workspace of GCOL may be row-major (coalesced thread-per-
+  // column access)
+  const int64_t cs = GCOL ? gcs : m, rs = GCOL ? grs : 1;
   Df* s_vn1 = reinterpret_cast<Df*>(GCOL ? V + m : C + ncap * m);
   Df* s_vn2 = s_vn1 + ncap;
   Df* s_dot = s_vn2 + ncap;
@@ -1390,8 +1395,12 @@ __device__ __forceinline__ void geqp3_df_body(const QrParams<double>& P, const Q
   float* __restrict__ Bl = D.Bl;
   const float tol3z = (float)sqrt(Real<double>::eps);
   const int64_t lastrk = m < n ? m : n;
+  // LRA_TRACE: a block barrier before each stamp, so that it marks the end
+  // of the phase for the whole CTA
   auto stamp = [&](int64_t c, int ph) {
-    if (D.stamps && b == 0 && threadIdx.x == 0 && c < P.kmax) D.stamps[c * 16 + ph] = globaltimer_ns();
+    if (!D.stamps) return;
+    __syncthreads();
+    if (b == 0 && threadIdx.x == 0 && c < P.kmax) D.stamps[c * 16 + ph] = globaltimer_ns();
   };
   // the CTA's candidate: max of the warps' words (s_w) and OR of their
   // stop flags (s_fl), into s_win / s_stop
@@ -1432,14 +1441,14 @@ __device__ __forceinline__ void geqp3_df_body(const QrParams<double>& P, const Q
     const unsigned long long w = s_win;
     if (w & XW_LOW) {
       const int sc = (int)((int64_t)(XW_IDX - (w & XW_IDX)) - c0);
-      float2* col = C + (int64_t)sc * m;
+      float2* col = C + (int64_t)sc * cs;
       float2* dst = GCOL ? nullptr : S.stage + ((size_t)(e & 1) * G + b) * m;
       const Df fs = upd ? s_fs[sc] : Df{0.f, 0.f};
       if (upd && !(s_st[sc] & ST_UPD) && fs.h != 0.f) {
         for (int64_t i = r0 + threadIdx.x; i < m; i += NT) {
-          const float2 x = col[i], v = V[i];
+          const float2 x = col[i * rs], v = V[i];
           const Df y = df_axpy_neg(x.x, x.y, fs, v.x, v.y);
-          col[i] = make_float2(y.h, y.l);
+          col[i * rs] = make_float2(y.h, y.l);
           if (!GCOL) dst[i] = make_float2(y.h, y.l);
         }
         __syncthreads();
@@ -1545,20 +1554,6 @@ __device__ __forceinline__ void geqp3_df_body(const QrParams<double>& P, const Q
     return s_ok != 0;
   };
   auto quad = [&](int& s, int (&q)[4]) { return live_quad(s_st, nloc, NCW, s, q); };
-  // 2-norm of rows r0..m-1 of a shared-memory column, by one warp, in FP64
-  auto col_nrm2 = [&](const float2* col, int64_t r0) -> double {
-    double mx = 0;
-    for (int64_t i = r0 + lane; i < m; i += 32) mx = fmax(mx, fabs(df_val(col[i].x, col[i].y)));
-    mx = warp_max(mx);
-    if (mx == 0 || !isfinite(mx)) return mx;
-    const double sc = pow2_scale_inv(mx);
-    double acc = 0;
-    for (int64_t i = r0 + lane; i < m; i += 32) {
-      const double t = df_val(col[i].x, col[i].y) * sc;
-      acc = fma(t, t, acc);
-    }
-    return sqrt(warp_sum(acc)) / sc;
-  };
 
   // ---- the CTA's columns into shared memory (GCOL: the workspace is filled);
   // initial norms, first pivot
@@ -1612,14 +1607,13 @@ __device__ __forceinline__ void geqp3_df_body(const QrParams<double>& P, const Q
         if (owner == b && s == pvt - c0) st |= ST_DONE;
         s_st[s] = st;
       }
-      if (threadIdx.x == 0) s_nflag = 0;
       // ---- the pivot column's rows c..m-1 from the winner's stage, and the
       // per-warp partial sums of squares of rows c+1..m-1
       {
-        const float2* src = GCOL ? C + (pvt - c0) * m : S.stage + ((size_t)(e & 1) * G + owner) * m;
+        const float2* src = GCOL ? C + (pvt - c0) * cs : S.stage + ((size_t)(e & 1) * G + owner) * m;
         Df acc{0.f, 0.f};
         for (int64_t i = c + threadIdx.x; i < m; i += NT) {
-          const float2 x = GCOL ? src[i] : __ldcg(src + i);
+          const float2 x = GCOL ? src[i * rs] : __ldcg(src + i);
           V[i] = x;
           if (i > c) df_fma_acc(acc, x.x, x.y, x.x, x.y);
           else s_alpha = Df{x.x, x.y};
@@ -1659,6 +1653,31 @@ __device__ __forceinline__ void geqp3_df_body(const QrParams<double>& P, const Q
             X.beta[c] = s_betad;
           }
         }
+      } else if (len > 0 && len <= kQrSeqLen) {
+        // ---- short columns: a thread per column, the dot product summed
+        // row by row (a lane-strided sum and its reduction tree cost more
+        // than the products here).  The rule depends on len alone, so both
+        // forms of the kernel sum each column the same way.
+        for (int s = threadIdx.x - 32; s < nloc; s += NT - 32) {
+          if (s_st[s] & ST_DONE) continue;
+          const float2* col = C + (int64_t)s * cs;
+          s_x0[s] = col[c * rs];
+          Df d{0.f, 0.f};
+          // QSEQB rows loaded ahead, then added in row order
+          for (int64_t i0 = c + 1; i0 < m; i0 += QSEQB) {
+            float2 xb[QSEQB];
+#pragma unroll
+            for (int r = 0; r < QSEQB; ++r)
+              if (i0 + r < m) xb[r] = col[(i0 + r) * rs];
+#pragma unroll
+            for (int r = 0; r < QSEQB; ++r)
+              if (i0 + r < m) {
+                const float2 v = V[i0 + r];
+                df_fma_acc(d, v.x, v.y, xb[r].x, xb[r].y);
+              }
+          }
+          s_dot[s] = quick_two_sum(d.h, d.l);
+        }
       } else if (len > 0) {
         // ---- dot products x . a of the warp's live columns, four at a time
         int s = wid - 1;
@@ -1666,12 +1685,12 @@ __device__ __forceinline__ void geqp3_df_body(const QrParams<double>& P, const Q
         while (quad(s, q)) {
           const float2* cg[4];
 #pragma unroll
-          for (int g = 0; g < 4; ++g) cg[g] = C + (int64_t)(q[g] >= 0 ? q[g] : q[0]) * m;
+          for (int g = 0; g < 4; ++g) cg[g] = C + (int64_t)(q[g] >= 0 ? q[g] : q[0]) * cs;
           // row c of the column, for the update that follows the dots
           {
             const int g = lane >> 3;
             const int qg = g == 0 ? q[0] : g == 1 ? q[1] : g == 2 ? q[2] : q[3];
-            if ((lane & 7) == 0 && qg >= 0) s_x0[qg] = C[(int64_t)qg * m + c];
+            if ((lane & 7) == 0 && qg >= 0) s_x0[qg] = C[(int64_t)qg * cs + c * rs];
           }
           // QRPL rows per lane are loaded before they are used, so that a
           // quad has 4 QRPL loads in flight (the global-memory form waits
@@ -1686,7 +1705,7 @@ __device__ __forceinline__ void geqp3_df_body(const QrParams<double>& P, const Q
               const bool in = i < m;
               xv[r] = in ? V[i] : make_float2(0.f, 0.f);
 #pragma unroll
-              for (int g = 0; g < 4; ++g) xc[g][r] = in ? cg[g][i] : make_float2(0.f, 0.f);
+              for (int g = 0; g < 4; ++g) xc[g][r] = in ? cg[g][i * rs] : make_float2(0.f, 0.f);
             }
 #pragma unroll
             for (int r = 0; r < QRPL; ++r)
@@ -1718,7 +1737,7 @@ __device__ __forceinline__ void geqp3_df_body(const QrParams<double>& P, const Q
       const Df scal = s_f;
       stamp(c, 3);
       // ---- a thread per column: f, the new row c, the norm downdate and the
-      // candidate word; the columns whose downdate is unreliable are flagged
+      // candidate word
       unsigned long long ww = 0;
       int wfl = 0;
       auto sub = [&](int ph) {
@@ -1730,7 +1749,7 @@ __device__ __forceinline__ void geqp3_df_body(const QrParams<double>& P, const Q
         for (int s = threadIdx.x; s < nloc; s += NT) {
           const unsigned char st = s_st[s];
           if (st & ST_DONE) continue;
-          const float2 x0 = len > 0 ? s_x0[s] : C[(int64_t)s * m + c];
+          const float2 x0 = len > 0 ? s_x0[s] : C[(int64_t)s * cs + c * rs];
           Df f{0.f, 0.f}, fs{0.f, 0.f};
           if (tau != 0 && len > 0) {
             f = df_mul(tdf, df_add(Df{x0.x, x0.y}, df_mul(scal, s_dot[s])));
@@ -1738,7 +1757,7 @@ __device__ __forceinline__ void geqp3_df_body(const QrParams<double>& P, const Q
           }
           s_fs[s] = fs;
           const Df a = df_add(Df{x0.x, x0.y}, df_neg(f));
-          C[(int64_t)s * m + c] = make_float2(a.h, a.l);
+          C[(int64_t)s * cs + c * rs] = make_float2(a.h, a.l);
           Df v1 = s_vn1[s];
           bool flagged = false;
           if (c < lastrk - 1 && v1.h != 0.f) {
@@ -1756,42 +1775,42 @@ __device__ __forceinline__ void geqp3_df_body(const QrParams<double>& P, const Q
             }
           }
           if (flagged) {
-            s_st[s] = st | ST_FLAG;
-            atomicAdd(&s_nflag, 1);
-          } else {
-            const unsigned long long w = xw_pack(v1, c0 + s);
-            ww = w > ww ? w : ww;
-          }
-        }
-      }
-      __syncthreads();
-      sub(9);
-      // unreliable downdates, a warp per column: its update now and the norm
-      // of its rows c+1..m-1 (xLAQPS would end the block here and recompute
-      // the norm before the next pivot, from the same updated column)
-      if (s_nflag > 0) {
-        wfl = 1;
-        for (int s = wid; s < nloc; s += NW) {
-          if (!(s_st[s] & ST_FLAG)) continue;
-          float2* col = C + (int64_t)s * m;
-          const Df ff = s_fs[s];
-          if (ff.h != 0.f)
-            for (int64_t i = c + 1 + lane; i < m; i += 32) {
-              const float2 x = col[i], v = V[i];
-              const Df y = df_axpy_neg(x.x, x.y, ff, v.x, v.y);
-              col[i] = make_float2(y.h, y.l);
+            // unreliable downdate: the column's update now and the norm of
+            // its rows c+1..m-1 (xLAQPS would end the block here and
+            // recompute the norm before the next pivot, from the same
+            // updated column); this thread alone, row by row, in double-float
+            // at a power-of-two scale that puts the largest entry in [1, 2)
+            float2* col = C + (int64_t)s * cs;
+            if (fs.h != 0.f)
+              for (int64_t i = c + 1; i < m; ++i) {
+                const float2 x = col[i * rs], v = V[i];
+                const Df y = df_axpy_neg(x.x, x.y, fs, v.x, v.y);
+                col[i * rs] = make_float2(y.h, y.l);
+              }
+            float mx = 0.f;
+            for (int64_t i = c + 1; i < m; ++i) mx = fmaxf(mx, fabsf(col[i * rs].x));
+            Df nr{mx, 0.f};
+            if (mx > 0.f && isfinite(mx)) {
+              const int ex = ilogbf(mx);
+              const float sc = ldexpf(1.f, -ex);
+              Df acc{0.f, 0.f};
+              for (int64_t i = c + 1; i < m; ++i) {
+                const float2 x = col[i * rs];
+                df_fma_acc(acc, x.x * sc, x.y * sc, x.x * sc, x.y * sc);
+              }
+              const Df r = df_sqrt(quick_two_sum(acc.h, acc.l));
+              nr = Df{ldexpf(r.h, ex), ldexpf(r.l, ex)};
             }
-          __syncwarp();
-          const double nr = col_nrm2(col, c + 1);
-          if (lane == 0) {
-            const Df v1 = df_split(nr);
+            v1 = nr;
             s_vn1[s] = s_vn2[s] = v1;
-            s_st[s] = (unsigned char)((s_st[s] & ~ST_FLAG) | ST_UPD);
-            const unsigned long long w = xw_pack(v1, c0 + s);
-            ww = w > ww ? w : ww;
+            s_st[s] = st | ST_UPD;
+            wfl = 1;
           }
+          const unsigned long long w = xw_pack(v1, c0 + s);
+          ww = w > ww ? w : ww;
         }
       }
+      sub(9);
       sub(10);
       sub(11);
       sub(12);
@@ -1813,12 +1832,12 @@ __device__ __forceinline__ void geqp3_df_body(const QrParams<double>& P, const Q
         // the finished pivot column (its owner): R's rows above c, beta, the
         // reflector v = scal x below
         if (owner == b) {
-          float2* col = C + (pvt - c0) * m;
+          float2* col = C + (pvt - c0) * cs;
           const Df bt = s_beta;
           for (int64_t i = (GCOL ? c : 0) + ct; i < m; i += NCT) {
             float2 y;
             if (i < c) {
-              y = col[i];
+              y = col[i * rs];
             } else if (i == c) {
               y = make_float2(bt.h, bt.l);
             } else {
@@ -1829,45 +1848,78 @@ __device__ __forceinline__ void geqp3_df_body(const QrParams<double>& P, const Q
               }
             }
             if (GCOL) {
-              col[i] = y;
+              col[i * rs] = y;
             } else {
               Bh[pvt * lda + i] = y.x;
               Bl[pvt * lda + i] = y.y;
             }
           }
         }
-        // the rank-1 updates of rows c+1..m-1, QRPL elements per thread at a
-        // time over all (column, row) pairs, loads before stores
-        const int len32 = (int)len;
-        const int E = nloc * len32;
-        for (int e0 = ct; e0 < E; e0 += NCT * QRPL) {
-          float2 xv[QRPL], xc[QRPL];
-          Df fq[QRPL];
-          int64_t at[QRPL];
-          bool u[QRPL];
+        // the rank-1 updates of rows c+1..m-1.  Shared-memory columns: a warp
+        // per four columns, QRPL rows per lane in registers.  Global columns
+        // (GCOL): a thread per column, whose rows stay in L1 between the
+        // dot products and the update.
+        if (!GCOL) {
+          int s = wid - 1;
+          int q[4];
+          while (quad(s, q)) {
+            Df fq[4];
+            float2* cg[4];
+            bool u[4];
 #pragma unroll
-          for (int q = 0; q < QRPL; ++q) {
-            const int e = e0 + q * NCT;
-            u[q] = false;
-            at[q] = 0;
-            if (e < E) {
-              const int sl = e / len32;
-              const int64_t i = c + 1 + (e - sl * len32);
-              fq[q] = s_fs[sl];
-              u[q] = !(s_st[sl] & (ST_DONE | ST_UPD)) && fq[q].h != 0.f;
-              at[q] = (int64_t)sl * m + i;
-              if (u[q]) {
-                xc[q] = C[at[q]];
-                xv[q] = V[i];
+            for (int h = 0; h < 4; ++h) {
+              const int qh = q[h] >= 0 ? q[h] : q[0];
+              cg[h] = C + (int64_t)qh * cs;
+              fq[h] = s_fs[qh];
+              u[h] = q[h] >= 0 && fq[h].h != 0.f && !(s_st[qh] & ST_UPD);
+            }
+            if (u[0] || u[1] || u[2] || u[3]) {
+              for (int64_t b0 = c + 1; b0 < m; b0 += 32 * QRPL) {
+                float2 xv[QRPL], xc[4][QRPL];
+#pragma unroll
+                for (int r = 0; r < QRPL; ++r) {
+                  const int64_t i = b0 + lane + 32 * r;
+                  const bool in = i < m;
+                  xv[r] = in ? V[i] : make_float2(0.f, 0.f);
+#pragma unroll
+                  for (int h = 0; h < 4; ++h) xc[h][r] = (in && u[h]) ? cg[h][i * rs] : make_float2(0.f, 0.f);
+                }
+#pragma unroll
+                for (int r = 0; r < QRPL; ++r) {
+                  const int64_t i = b0 + lane + 32 * r;
+                  if (i < m) {
+#pragma unroll
+                    for (int h = 0; h < 4; ++h)
+                      if (u[h]) {
+                        const Df y = df_axpy_neg(xc[h][r].x, xc[h][r].y, fq[h], xv[r].x, xv[r].y);
+                        cg[h][i * rs] = make_float2(y.h, y.l);
+                      }
+                  }
+                }
               }
             }
           }
+        }
+        if (GCOL) {
+          for (int sl = ct; sl < nloc; sl += NCT) {
+            if (s_st[sl] & (ST_DONE | ST_UPD)) continue;
+            const Df fs = s_fs[sl];
+            if (fs.h == 0.f) continue;
+            float2* col = C + (int64_t)sl * cs;
+            for (int64_t i0 = c + 1; i0 < m; i0 += QSEQB) {
+              float2 xb[QSEQB];
 #pragma unroll
-          for (int q = 0; q < QRPL; ++q)
-            if (u[q]) {
-              const Df y = df_axpy_neg(xc[q].x, xc[q].y, fq[q], xv[q].x, xv[q].y);
-              C[at[q]] = make_float2(y.h, y.l);
+              for (int r = 0; r < QSEQB; ++r)
+                if (i0 + r < m) xb[r] = col[(i0 + r) * rs];
+#pragma unroll
+              for (int r = 0; r < QSEQB; ++r)
+                if (i0 + r < m) {
+                  const float2 v = V[i0 + r];
+                  const Df y = df_axpy_neg(xb[r].x, xb[r].y, fs, v.x, v.y);
+                  col[(i0 + r) * rs] = make_float2(y.h, y.l);
+                }
             }
+          }
         }
       }
       if (!collect(e)) return;
@@ -1906,7 +1958,7 @@ __device__ __forceinline__ void geqp3_df_body(const QrParams<double>& P, const Q
 template <int NT>
 __global__ void __launch_bounds__(NT, 1) geqp3_df_smem_kernel(QrParams<double> P, QrV2Extra X, QrDf D, QrSm S) {
   extern __shared__ unsigned char qr_dyn[];
-  geqp3_df_body<NT, false>(P, X, D, S, gridDim.x, blockIdx.x, nullptr, qr_dyn);
+  geqp3_df_body<NT, false>(P, X, D, S, gridDim.x, blockIdx.x, nullptr, 0, 0, qr_dyn);
 }
 
 // one matrix of a batch: its parameters and its m x n float2 workspace
@@ -1915,6 +1967,7 @@ struct QrJob {
   QrV2Extra X;
   QrDf D;
   float2* work;
+  int64_t cs, rs;  // element (i, j) of the workspace at work[j cs + i rs]
 };
 
 // persistent grouped pivoted QR: each CTA takes the next matrix (jobs are
@@ -1930,7 +1983,7 @@ __global__ void __launch_bounds__(NT, 1) geqp3_df_group_kernel(const QrJob* __re
     __syncthreads();
     const int j = s_job;
     if (j >= njobs) return;
-    geqp3_df_body<NT, true>(jobs[j].P, jobs[j].X, jobs[j].D, S, 1, 0, jobs[j].work, qr_dyn);
+    geqp3_df_body<NT, true>(jobs[j].P, jobs[j].X, jobs[j].D, S, 1, 0, jobs[j].work, jobs[j].cs, jobs[j].rs, qr_dyn);
   }
 }
 
@@ -1941,7 +1994,8 @@ __global__ void __launch_bounds__(NT, 1) geqp3_df_group_kernel(const QrJob* __re
 struct DfPrepJob {
   int64_t m, n, ldb;
   const double* B;
-  float2* work;                // m x n
+  float2* work;                // m x n, element (i, j) at work[j cs + i rs]
+  int64_t cs, rs;
   double* vn0;                 // n
   double* scale;               // 1
   unsigned long long* maxbits;  // 1, zeroed: max |B| as the bits of a double
@@ -1968,12 +2022,12 @@ __global__ void __launch_bounds__(512) df_prep_split_kernel(const DfPrepJob* __r
   const double sc = mx > 0 ? ldexp(1.0, -(ilogb(mx) + 1)) : 1.0;
   if (blockIdx.y == 0 && threadIdx.x == 0) *J.scale = sc;
   for (int64_t j = (int64_t)blockIdx.y * nw + wid; j < J.n; j += (int64_t)gridDim.y * nw) {
-    float2* w = J.work + j * J.m;
+    float2* w = J.work + j * J.cs;
     double cm = 0;
     for (int64_t i = lane; i < J.m; i += 32) {
       const double x = J.B[i + j * J.ldb] * sc;
       const Df d = df_split(x);
-      w[i] = make_float2(d.h, d.l);
+      w[i * J.rs] = make_float2(d.h, d.l);
       cm = fmax(cm, fabs(x));
     }
     cm = warp_max(cm);
@@ -1981,7 +2035,8 @@ __global__ void __launch_bounds__(512) df_prep_split_kernel(const DfPrepJob* __r
     if (cm > 0) {
       const double s2 = pow2_scale_inv(cm);
       for (int64_t i = lane; i < J.m; i += 32) {
-        const double t = df_val(w[i].x, w[i].y) * s2;
+        const Df d = df_split(J.B[i + j * J.ldb] * sc);
+        const double t = df_val(d.h, d.l) * s2;
         acc = fma(t, t, acc);
       }
       acc = sqrt(warp_sum(acc)) / s2;
@@ -1996,6 +2051,7 @@ struct DfFinishJob {
   int64_t m, n, ldb;
   double* B;
   const float2* work;
+  int64_t cs, rs;
   const double* scale;
   const int64_t* piv;
   const int64_t* nfac;
@@ -2026,8 +2082,8 @@ __global__ void __launch_bounds__(512) df_finish_group_kernel(const DfFinishJob*
   for (int64_t j = threadIdx.x; j < J.n; j += blockDim.x) J.jpvt[j] = ca[j] + 1;
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
   for (int64_t j = wid; j < J.n; j += nw) {
-    const float2* w = J.work + (int64_t)ca[j] * J.m;
-    for (int64_t i = lane; i < J.m; i += 32) J.B[i + j * J.ldb] = df_val(w[i].x, w[i].y) * inv;
+    const float2* w = J.work + (int64_t)ca[j] * J.cs;
+    for (int64_t i = lane; i < J.m; i += 32) J.B[i + j * J.ldb] = df_val(w[i * J.rs].x, w[i * J.rs].y) * inv;
   }
 }
 
@@ -2269,7 +2325,7 @@ static void print_qr_trace(lra_ctx* ctx, const unsigned long long* stamps, int64
 // largest first) and the replay into column order.  Each matrix comes out
 // as geqp3_adap leaves it when its shared-memory kernel runs, bit for bit.
 bool geqp3_df_batch_fits(lra_ctx* ctx, int64_t m, int64_t n) {
-  constexpr int NTG = 544;
+  constexpr int NTG = 512;
   if (m < 1 || n < 1 || n >= (int64_t)XW_IDX || m > 20480) return false;
   const size_t smem = (size_t)m * sizeof(float2) + (size_t)n * (5 * 8 + 1);
   static size_t cap = [&] {
@@ -2287,7 +2343,7 @@ bool geqp3_df_batch_fits(lra_ctx* ctx, int64_t m, int64_t n) {
 
 void geqp3_df_batch(lra_ctx* ctx, int64_t count, const DfBatchItem* items, int64_t nb, double atol, double rtol,
                     int64_t* k_dev) {
-  constexpr int NTG = 544;
+  constexpr int NTG = 512;
   if (count <= 0) return;
   // largest factorizations first, so that the last wave is short
   std::vector<int64_t> ord((size_t)count);
@@ -2312,7 +2368,11 @@ void geqp3_df_batch(lra_ctx* ctx, int64_t count, const DfBatchItem* items, int64
     float2* work = ctx->arena.alloc_n<float2>((size_t)m * n);
     double* vn0 = ctx->arena.alloc_n<double>(n);
     double* scale = ctx->arena.alloc_n<double>(1);
-    prep[(size_t)t] = DfPrepJob{m, n, it.ldb, it.B, work, vn0, scale, maxbits + t};
+    // row-major when every step sums its columns row by row (a thread per
+    // column reads a row of the workspace coalesced), else column-major
+    const bool rowmaj = m - 1 <= kQrSeqLen;
+    const int64_t cs = rowmaj ? 1 : m, rs = rowmaj ? n : 1;
+    prep[(size_t)t] = DfPrepJob{m, n, it.ldb, it.B, work, cs, rs, vn0, scale, maxbits + t};
     QrJob& J = qr[(size_t)t];
     std::memset(&J, 0, sizeof J);
     J.P.m = m;
@@ -2331,7 +2391,9 @@ void geqp3_df_batch(lra_ctx* ctx, int64_t count, const DfBatchItem* items, int64
     J.D.vn0 = vn0;
     J.D.scale = scale;
     J.work = work;
-    fin[(size_t)t] = DfFinishJob{m, n, it.ldb, it.B, work, scale, J.X.piv, J.X.nfac, it.jpvt};
+    J.cs = cs;
+    J.rs = rs;
+    fin[(size_t)t] = DfFinishJob{m, n, it.ldb, it.B, work, cs, rs, scale, J.X.piv, J.X.nfac, it.jpvt};
     smem_qr = std::max(smem_qr, (size_t)m * sizeof(float2) + (size_t)n * (5 * 8 + 1));
     smem_fin = std::max(smem_fin, (size_t)2 * n * sizeof(int));
   }
@@ -2495,7 +2557,7 @@ int64_t geqp3_adap(lra_ctx* ctx, int64_t m, int64_t n, T* A, int64_t lda, int64_
       std::memcpy(&Pd, &P, sizeof(Pd));
       Pd.lda = m;
       // the columns stay in shared memory when each CTA's share fits there
-      constexpr int NTS = 544;  // warp 0 for the reflector, 16 column warps
+      constexpr int NTS = 512;  // warp 0 for the reflector, 15 column warps
       const int gsm = (int)std::min<int64_t>(std::min(ctx->num_sms, 256),
                                              std::max<int64_t>(1, (n + NTS / 32 - 2) / (NTS / 32 - 1)));
       const int64_t ncap = (n + gsm - 1) / gsm;
