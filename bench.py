@@ -50,6 +50,7 @@ def parse():
                     help="kernel matrices in the batched measurement (0: skip); the FP64 path runs on the first "
                          "--batch-native of them")
     ap.add_argument("--batch-native", type=int, default=256)
+    ap.add_argument("--no-tall", action="store_true", help="skip the tall Float32 idfact measurement")
     return ap.parse_args()
 
 
@@ -169,6 +170,62 @@ def measure_serving(lra, work, precision: str, slots: int = 8):
         srv.close()
     return {"requests": len(work), "slots": slots, "arrival_rate_per_s": rate, "matrices_s": len(work) / wall,
             "p50_ms": st["p50_ms"], "p99_ms": st["p99_ms"], "burst_matrices_s": burst}
+
+
+def tall_f32_matrix(m: int = 65536, n: int = 4096, seed: int = 6):
+    """The tall Float32 config: A = U diag(s) V' with U, V Haar (QR of seeded
+    Gaussians, on the GPU) and s_i = exp(-(i-1)/60)."""
+    import torch
+    g = torch.Generator(device="cuda").manual_seed(seed)
+    U = torch.linalg.qr(torch.randn(m, n, generator=g, device="cuda", dtype=torch.float32)).Q
+    V = torch.linalg.qr(torch.randn(n, n, generator=g, device="cuda", dtype=torch.float32)).Q
+    sv = torch.exp(-torch.arange(n, dtype=torch.float32, device="cuda") / 60.0)
+    A = ((U * sv[None, :]) @ V.T).t().contiguous().t()
+    del U, V
+    return A
+
+
+def measure_tall(lra, ctx, A, peaks, reps: int = 3):
+    """idfact of the tall Float32 matrix at rtol 1e-6 with the SRFT and the
+    Gaussian sketch: per call time, the sketch stage's achieved rate (the SRFT
+    reads A once per adaptive step: GB/s against HBM; the Gaussian sketch as
+    three BF16 digit planes on the tensor cores: TFLOP/s against BF16), rank
+    and error."""
+    import torch
+    m, n = A.shape
+    out = {"workload": f"idfact {m}x{n} F32 U diag(s) V', s_i=exp(-(i-1)/60), rtol 1e-6"}
+    nrm = lra.snorm(A, ctx=ctx)
+    for sk in ("srft", "randn"):
+        o = lra.LRAOptions(np.float32, rtol=1e-6, sketch=sk, precision="mixed", seed=5)
+        V = lra.idfact(A, o, ctx=ctx)
+        torch.cuda.synchronize()
+        sketch_ms, t = 0.0, 0.0
+        for _ in range(reps):
+            t0 = time.perf_counter()
+            V = lra.idfact(A, o, ctx=ctx)
+            torch.cuda.synchronize()
+            t += time.perf_counter() - t0
+            sketch_ms += ctx.stage_ms()["sketch"]
+        t /= reps
+        sketch_ms /= reps
+        a, b = o.sketchfact_srft_samp if sk == "srft" else o.sketchfact_randn_samp
+        orders = [a * (o.nb << j) + b for j in range(V.nsteps)]
+        r = {"ms_per_call": 1e3 * t, "matrices_s": 1.0 / t, "rank": V.k, "steps": V.nsteps, "orders": orders,
+             "sketch_ms": sketch_ms,
+             "rel_spectral_err": lra.snormdiff(A, V, ctx=ctx) / nrm}
+        if sk == "srft":
+            gbs = len(orders) * m * n * 4 / (sketch_ms * 1e-3) / 1e9
+            hbm = peaks.get("hbm_gbs") or 6800.0
+            r["sketch_roofline"] = {"bound": "hbm", "achieved": gbs, "peak": hbm, "unit": "GB/s", "frac": gbs / hbm,
+                                    "bytes": "A read once per step"}
+        else:
+            fl = sum(2.0 * 3 * l * m * n for l in orders)
+            tf = fl / (sketch_ms * 1e-3) / 1e12
+            bf = peaks.get("bf16_tflops") or 1900.0
+            r["sketch_roofline"] = {"bound": "tensor", "achieved": tf, "peak": bf, "unit": "TFLOP/s", "frac": tf / bf,
+                                    "flops": "3 BF16 digit planes x 2 l m n per step"}
+        out[sk] = r
+    return out
 
 
 def measure_batched(lra, mats, precision: str, ctx):
@@ -456,6 +513,15 @@ def main():
         except Exception as e:  # pragma: no cover
             batched = {"failed": str(e)}
 
+    tall = None
+    if rank == 0 and not args.no_tall:
+        try:
+            At = tall_f32_matrix()
+            tall = measure_tall(lra, ctx, At, peaks)
+            del At
+        except Exception as e:  # pragma: no cover
+            tall = {"failed": str(e)}
+
     if rank == 0:
         per_ms = sorted(1e3 * p for p in per)
         line = {
@@ -470,7 +536,7 @@ def main():
             "rank": k, "rel_spectral_err": err / nrm,
             "e2e": {"value": e2e_val, "unit": "matrices/s", "h2d_bytes_per_step": h2d,
                     "d2h_bytes_per_step": d2h},
-            "fp64_path": fp64, "serving": serving, "batched": batched,
+            "fp64_path": fp64, "serving": serving, "batched": batched, "tall_f32": tall,
             "roofline": roof, "roofline_sketch": roof_sketch, "cpu_baseline": cpu, "clocks": clk, "gpu_launches": launches,
         }
         print(json.dumps(line), flush=True)

@@ -67,8 +67,10 @@ __global__ void __launch_bounds__(SRFT_NT) srft_fft_kernel(int64_t M, int64_t N,
     for (int q = 0; q < MAX_PAIRS_PER_THREAD; ++q) zr[q] = zi[q] = T(0);
     for (int64_t kk0 = 0; kk0 < m2; kk0 += 2 * kcp) {
       // load: Z[bitrev(jj)][p] = X[jj, kk0 + 2p] + i X[jj, kk0 + 2p + 1]
-      for (int64_t t = threadIdx.x; t < l * 2 * kcp; t += SRFT_NT) {
-        const int64_t jj = t / (2 * kcp), r = t % (2 * kcp);
+      // (32-bit index arithmetic: l kcp < 2^31)
+      const int k2 = 2 * kcp;
+      for (int t = threadIdx.x; t < (int)l * k2; t += SRFT_NT) {
+        const int jj = t / k2, r = t - jj * k2;
         const int64_t kk = kk0 + r;
         T v = T(0);
         if (kk < m2) {
@@ -86,10 +88,10 @@ __global__ void __launch_bounds__(SRFT_NT) srft_fft_kernel(int64_t M, int64_t N,
       for (int s = 1; s <= lbits; ++s) {
         const int64_t half = (int64_t)1 << (s - 1);
         const int64_t stride = l >> s;  // twiddle index step
-        for (int64_t t = threadIdx.x; t < (l / 2) * kcp; t += SRFT_NT) {
-          const int64_t bf = t / kcp, p = t % kcp;
-          const int64_t grp = bf / half, pos = bf % half;
-          const int64_t i0 = grp * 2 * half + pos, i1 = i0 + half;
+        for (int t = threadIdx.x; t < (int)(l / 2) * kcp; t += SRFT_NT) {
+          const int bf = t / kcp, p = t - bf * kcp;
+          const int grp = bf >> (s - 1), pos = bf & (int)(half - 1);
+          const int i0 = grp * 2 * (int)half + pos, i1 = i0 + (int)half;
           const Cx<T> w = tw_l[pos * stride];
           Cx<T>* a = Z + i0 * kcp + p;
           Cx<T>* b = Z + i1 * kcp + p;
@@ -108,7 +110,9 @@ __global__ void __launch_bounds__(SRFT_NT) srft_fft_kernel(int64_t M, int64_t N,
         const int64_t pr = threadIdx.x + (int64_t)q * SRFT_NT;
         if (pr < npairs) {
           const int64_t f = idx[2 * pr] - 1;
-          const int64_t C = f % l, Cm = (l - C) % l;
+          const int64_t C = f & (l - 1), Cm = (l - C) & (l - 1);
+          // the phase index f kk mod M, stepped by f per kk (exact, no division)
+          int64_t ph = (f * kk0) % M;
           for (int p = 0; p < kcp; ++p) {
             const int64_t kka = kk0 + 2 * p;
             if (kka >= m2) break;
@@ -116,14 +120,18 @@ __global__ void __launch_bounds__(SRFT_NT) srft_fft_kernel(int64_t M, int64_t N,
             const Cx<T> z1 = Z[C * kcp + p], z2 = Z[Cm * kcp + p];
             const T yar = T(0.5) * (z1.re + z2.re), yai = T(0.5) * (z1.im - z2.im);  // sequence a
             const T ybr = T(0.5) * (z1.im + z2.im), ybi = T(0.5) * (z2.re - z1.re);  // sequence b
-            const Cx<T> wa = tw_M[(f * kka) % M];
+            const Cx<T> wa = tw_M[ph];
             zr[q] += yar * wa.re - yai * wa.im;
             zi[q] += yar * wa.im + yai * wa.re;
+            ph += f;
+            if (ph >= M) ph -= M;
             if (kka + 1 < m2) {
-              const Cx<T> wb = tw_M[(f * (kka + 1)) % M];
+              const Cx<T> wb = tw_M[ph];
               zr[q] += ybr * wb.re - ybi * wb.im;
               zi[q] += ybr * wb.im + ybi * wb.re;
             }
+            ph += f;
+            if (ph >= M) ph -= M;
           }
         }
       }
