@@ -820,7 +820,8 @@ __global__ void symcheck_kernel(int64_t n, const T* __restrict__ A, int64_t lda,
 }  // namespace
 
 template <typename T>
-void jacobi_svd(lra_ctx* ctx, int64_t n, T* X, int64_t ldx, T* V, int64_t ldv, T* S, bool quadratic_stop) {
+void jacobi_svd(lra_ctx* ctx, int64_t n, T* X, int64_t ldx, T* V, int64_t ldv, T* S, bool quadratic_stop,
+                double stop) {
   // Float64: a CTA of 128 threads per pair; Float32: block Jacobi with the
   // block pair in shared memory when it fits, else a warp per pair
   constexpr bool pair_cta = sizeof(T) == 8;
@@ -862,7 +863,7 @@ void jacobi_svd(lra_ctx* ctx, int64_t n, T* X, int64_t ldx, T* V, int64_t ldv, T
   // A sweep whose cosines were all below sqrt(tol)/10 leaves them near
   // tol^2/100 times a modest gap factor (quadratic convergence), so the
   // sweep that would only confirm it is skipped.
-  P.stop = quadratic_stop ? std::sqrt(P.tol) * 0.1 : P.tol;
+  P.stop = stop > 0 ? stop : (quadratic_stop ? std::sqrt(P.tol) * 0.1 : P.tol);
   P.max_sweeps = 40;
   P.part = ctx->arena.alloc_n<double>(grid);
   P.bar = reinterpret_cast<GridBar*>(ctx->arena.alloc(sizeof(GridBar)));
@@ -954,8 +955,8 @@ bool is_symmetric(lra_ctx* ctx, int64_t n, const T* A, int64_t lda) {
   return h == 0;
 }
 
-template void jacobi_svd<float>(lra_ctx*, int64_t, float*, int64_t, float*, int64_t, float*, bool);
-template void jacobi_svd<double>(lra_ctx*, int64_t, double*, int64_t, double*, int64_t, double*, bool);
+template void jacobi_svd<float>(lra_ctx*, int64_t, float*, int64_t, float*, int64_t, float*, bool, double);
+template void jacobi_svd<double>(lra_ctx*, int64_t, double*, int64_t, double*, int64_t, double*, bool, double);
 template bool is_symmetric<float>(lra_ctx*, int64_t, const float*, int64_t);
 template bool is_symmetric<double>(lra_ctx*, int64_t, const double*, int64_t);
 

@@ -213,7 +213,9 @@ void orgqr(lra_ctx* ctx, int64_t m, int64_t k, T* V, int64_t ldv, const T* tau);
 // One-sided Jacobi SVD of X (n x n, square, in place): on exit X = U * S,
 // V (n x n) accumulates the right rotations, S gets the column norms.
 template <typename T>
-void jacobi_svd(lra_ctx* ctx, int64_t n, T* X, int64_t ldx, T* V, int64_t ldv, T* S, bool quadratic_stop = false);
+// stop > 0 ends the sweeps once a sweep's largest cosine is below it
+void jacobi_svd(lra_ctx* ctx, int64_t n, T* X, int64_t ldx, T* V, int64_t ldv, T* S, bool quadratic_stop = false,
+                double stop = 0);
 
 // G = R^T R in place (upper R, lower part zeroed), blocked; false when G is
 // not numerically positive definite

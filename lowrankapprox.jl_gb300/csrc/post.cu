@@ -20,6 +20,7 @@
 
 #include <algorithm>
 #include <cmath>
+#include <cstdio>
 #include <cstring>
 #include <numeric>
 #include <vector>
@@ -163,7 +164,118 @@ __global__ void absmax_bits_kernel(int64_t m, int64_t n, const T* __restrict__ a
   if ((threadIdx.x & 31) == 0 && mx > 0) atomicMax(out, (unsigned long long)__double_as_longlong(mx));
 }
 
+// X^ = X with every column scaled to unit norm (zero columns stay zero)
+__global__ void unit_cols_kernel(int64_t n, const double* __restrict__ X, int64_t ldx, const double* __restrict__ s,
+                                 double* __restrict__ Xh) {
+  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < n * n; t += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t i = t % n, j = t / n;
+    Xh[t] = s[j] > 0 ? X[i + j * ldx] / s[j] : 0.0;
+  }
+}
+
+// T antisymmetric from the Gram matrix of the unit columns: for p < q the
+// tangent of the one-sided Jacobi angle of the pair, zeta = (s_q^2 - s_p^2) /
+// (2 s_p s_q c_pq), t = sign(zeta) / (|zeta| + sqrt(1 + zeta^2)); T_pq = t,
+// T_qp = -t.  The largest |c_pq| goes to maxc (bits of a double).
+__global__ void gram_tangent_kernel(int64_t n, const double* __restrict__ Gh, const double* __restrict__ s,
+                                    double* __restrict__ T, unsigned long long* __restrict__ maxc) {
+  double mc = 0;
+  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < n * n; t += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t r = t % n, col = t / n;
+    if (r == col) {
+      T[t] = 0;
+      continue;
+    }
+    const int64_t p = r < col ? r : col, q = r < col ? col : r;
+    const double c = Gh[p + q * n];
+    mc = fmax(mc, fabs(c));
+    double tg = 0;
+    if (c != 0 && s[p] > 0 && s[q] > 0) {
+      const double zeta = (s[q] * s[q] - s[p] * s[p]) / (2.0 * s[p] * s[q] * c);
+      tg = copysign(1.0, zeta) / (fabs(zeta) + sqrt(1.0 + zeta * zeta));
+    }
+    T[t] = r < col ? tg : -tg;
+  }
+  mc = warp_max(mc);
+  if ((threadIdx.x & 31) == 0 && mc > 0) atomicMax(maxc, (unsigned long long)__double_as_longlong(mc));
+}
+
+// W = I + T + T2 / 2 (exp(T) to second order) and DW = diag(s) W
+__global__ void gram_rotation_kernel(int64_t n, const double* __restrict__ T, const double* __restrict__ T2,
+                                     const double* __restrict__ s, double* __restrict__ W, double* __restrict__ DW) {
+  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < n * n; t += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t i = t % n, j = t / n;
+    const double w = (i == j ? 1.0 : 0.0) + T[t] + 0.5 * T2[t];
+    W[t] = w;
+    DW[t] = s[i] * w;
+  }
+}
+
 }  // namespace
+
+// ---- Gram-matrix polish of a nearly orthogonal X ----------------------------------
+// After the FP32 sweeps and X <- X W, the columns of X are orthogonal to
+// about 1e-6 relative to their norms.  One-sided Jacobi would finish with a
+// sweep or two of pairwise rotations; here every pair's rotation comes from
+// the Gram matrix of the unit columns, G^ = X^' X^ (one GEMM: each entry is a
+// cosine, accurate to ~2^-45 absolutely on the tensor cores), and all the
+// rotations are applied at once, W = exp(T) to second order with T the
+// antisymmetric matrix of the pairs' angle tangents.  The cosines square
+// every iteration (1e-6 -> ~1e-11 -> rounding).  X <- X^ (diag(s) W) keeps
+// each column's error relative to its own norm, which the plain product X W
+// would not for a graded X.  Returns false when the largest cosine is still
+// above tol after a few iterations (clusters of equal singular values, where
+// simultaneous rotations interfere); the caller then finishes with pairwise
+// sweeps from the X and Wacc reached so far.  Wacc (n x n, ld n) is multiplied
+// by each W; S gets the column norms of the final X.
+constexpr double kGramStart = 3e-2;  // largest cosine the FP32 sweeps leave for the Gram polish
+
+bool gram_polish(lra_ctx* ctx, int64_t n, double* X, int64_t ldx, double* Wacc, double* S, double tol,
+                 int max_iter) {
+  const ArenaMark mk = ctx->arena.mark();
+  const size_t nn = (size_t)n * n;
+  double* Xh = ctx->arena.alloc_n<double>(nn);
+  double* Gh = ctx->arena.alloc_n<double>(nn);
+  double* Tm = ctx->arena.alloc_n<double>(nn);
+  double* T2 = ctx->arena.alloc_n<double>(nn);
+  double* W = ctx->arena.alloc_n<double>(nn);
+  double* DW = ctx->arena.alloc_n<double>(nn);
+  double* tmp = ctx->arena.alloc_n<double>(nn);
+  unsigned long long* maxc = ctx->arena.alloc_n<unsigned long long>(1);
+  const unsigned g = (unsigned)std::max<int64_t>(1, std::min<int64_t>(((int64_t)nn + 255) / 256, ctx->num_sms * 8));
+  bool ok = false;
+  for (int it = 0; it <= max_iter; ++it) {
+    col_norms<double>(ctx, n, n, X, ldx, S);
+    unit_cols_kernel<<<g, 256, 0, ctx->stream>>>(n, X, ldx, S, Xh);
+    post_launch(ctx, "unit_cols_kernel");
+    gemm<double>(ctx, 't', 'n', n, n, n, 1.0, Xh, n, Xh, n, 0.0, Gh, n);
+    LRA_CUDA(cudaMemsetAsync(maxc, 0, sizeof(unsigned long long), ctx->stream));
+    gram_tangent_kernel<<<g, 256, 0, ctx->stream>>>(n, Gh, S, Tm, maxc);
+    post_launch(ctx, "gram_tangent_kernel");
+    unsigned long long hb = 0;
+    LRA_CUDA(cudaMemcpyAsync(&hb, maxc, sizeof(hb), cudaMemcpyDeviceToHost, ctx->stream));
+    LRA_CUDA(cudaStreamSynchronize(ctx->stream));
+    double mc;
+    std::memcpy(&mc, &hb, sizeof(mc));
+    if (trace_on()) std::fprintf(stderr, "[lra] gram polish n=%lld iteration %d: max cosine %.3e\n", (long long)n, it, mc);
+    if (!std::isfinite(mc)) break;
+    if (mc <= tol) {
+      ok = true;
+      break;
+    }
+    if (it == max_iter) break;
+    gemm<double>(ctx, 'n', 'n', n, n, n, 1.0, Tm, n, Tm, n, 0.0, T2, n);
+    gram_rotation_kernel<<<g, 256, 0, ctx->stream>>>(n, Tm, T2, S, W, DW);
+    post_launch(ctx, "gram_rotation_kernel");
+    gemm<double>(ctx, 'n', 'n', n, n, n, 1.0, Xh, n, DW, n, 0.0, tmp, n);
+    copy_matrix(ctx, n, n, tmp, n, X, ldx);
+    gemm<double>(ctx, 'n', 'n', n, n, n, 1.0, Wacc, n, W, n, 0.0, tmp, n);
+    copy_matrix(ctx, n, n, tmp, n, Wacc, n);
+  }
+  LRA_CUDA(cudaStreamSynchronize(ctx->stream));
+  ctx->arena.release(mk);
+  return ok;
+}
 
 template <typename T>
 void jacobi_svd_fast(lra_ctx* ctx, int64_t n, T* X, int64_t ldx, T* V, int64_t ldv, T* S) {
@@ -210,7 +322,9 @@ void jacobi_svd_fast(lra_ctx* ctx, int64_t n, T* X, int64_t ldx, T* V, int64_t l
   float* V32 = ctx->arena.alloc_n<float>((size_t)n * n);
   float* S32 = ctx->arena.alloc_n<float>(n);
   cast<T, float>(ctx, n, n, X, ldx, X32, n, scale);
-  jacobi_svd<float>(ctx, n, X32, n, V32, n, S32, true);
+  // the Gram polish converges quadratically from cosines of a few 1e-3 (the
+  // FP32 sweeps stop there); the pairwise FP64 sweeps want them near 1e-6
+  jacobi_svd<float>(ctx, n, X32, n, V32, n, S32, true, df_polish ? kGramStart : 0.0);
   // 2. the rotation in FP64, re-orthonormalized by two Newton-Schulz steps
   //    W <- W (3 I - W'W) / 2: with |I - W'W| near 1e-6 from the FP32
   //    sweeps the error squares each step, to rounding level after two
@@ -228,11 +342,27 @@ void jacobi_svd_fast(lra_ctx* ctx, int64_t n, T* X, int64_t ldx, T* V, int64_t l
   T* Y = ctx->arena.alloc_n<T>((size_t)n * n);
   gemm<T>(ctx, 'n', 'n', n, n, n, T(1), X, ldx, W, n, T(0), Y, n);
   copy_matrix(ctx, n, n, Y, n, X, ldx);
-  // Y <- V2
+  // Y <- V2: the Gram polish on the mixed path, pairwise double-float sweeps
+  // after it when it did not converge, FP64 sweeps otherwise
   bool done = false;
   if constexpr (sizeof(T) == 8)
-    if (df_polish) done = jacobi_svd_df(ctx, n, reinterpret_cast<double*>(X), ldx, reinterpret_cast<double*>(Y), n,
-                                        reinterpret_cast<double*>(S));
+    if (df_polish) {
+      double* Xd = reinterpret_cast<double*>(X);
+      double* Yd = reinterpret_cast<double*>(Y);
+      const double tol =
+          std::max((double)Real<double>::eps * 2.0 * std::sqrt((double)n), 8.0 * std::ldexp(1.0, -46) * std::sqrt((double)n));
+      set_identity(ctx, n, n, Yd, n);
+      done = gram_polish(ctx, n, Xd, ldx, Yd, reinterpret_cast<double*>(S), tol, 5);
+      if (!done) {
+        double* Y2 = reinterpret_cast<double*>(W2);
+        done = jacobi_svd_df(ctx, n, Xd, ldx, Y2, n, reinterpret_cast<double*>(S));
+        if (!done) jacobi_svd<double>(ctx, n, Xd, ldx, Y2, n, reinterpret_cast<double*>(S), true);
+        double* Gd = reinterpret_cast<double*>(G);
+        gemm<double>(ctx, 'n', 'n', n, n, n, 1.0, Yd, n, Y2, n, 0.0, Gd, n);
+        copy_matrix(ctx, n, n, Gd, n, Yd, n);
+        done = true;
+      }
+    }
   if (!done) jacobi_svd<T>(ctx, n, X, ldx, Y, n, S, true);
   gemm<T>(ctx, 'n', 'n', n, n, n, T(1), W, n, Y, n, T(0), V, ldv);
   LRA_CUDA(cudaStreamSynchronize(ctx->stream));
