@@ -176,10 +176,16 @@ __global__ void unit_cols_kernel(int64_t n, const double* __restrict__ X, int64_
 // T antisymmetric from the Gram matrix of the unit columns: for p < q the
 // tangent of the one-sided Jacobi angle of the pair, zeta = (s_q^2 - s_p^2) /
 // (2 s_p s_q c_pq), t = sign(zeta) / (|zeta| + sqrt(1 + zeta^2)); T_pq = t,
-// T_qp = -t.  The largest |c_pq| goes to maxc (bits of a double).
+// T_qp = -t.  Angles with |t| > kGramMaxTan (nearly equal norms: a cluster,
+// where simultaneous rotations interfere, or a pair the FP32 sweeps left far
+// from orthogonal) are left out.  maxc[0] gets the largest |c_pq|, maxc[1]
+// the largest over the pairs that rotate, maxc[2] the largest |t| (bits of
+// doubles).
+constexpr double kGramMaxTan = 0.01;
+
 __global__ void gram_tangent_kernel(int64_t n, const double* __restrict__ Gh, const double* __restrict__ s,
                                     double* __restrict__ T, unsigned long long* __restrict__ maxc) {
-  double mc = 0;
+  double mc = 0, ma = 0, mt = 0;
   for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < n * n; t += (int64_t)gridDim.x * blockDim.x) {
     const int64_t r = t % n, col = t / n;
     if (r == col) {
@@ -193,19 +199,44 @@ __global__ void gram_tangent_kernel(int64_t n, const double* __restrict__ Gh, co
     if (c != 0 && s[p] > 0 && s[q] > 0) {
       const double zeta = (s[q] * s[q] - s[p] * s[p]) / (2.0 * s[p] * s[q] * c);
       tg = copysign(1.0, zeta) / (fabs(zeta) + sqrt(1.0 + zeta * zeta));
+      if (!(fabs(tg) <= kGramMaxTan)) {
+        tg = 0;
+      } else {
+        ma = fmax(ma, fabs(c));
+        mt = fmax(mt, fabs(tg));
+      }
     }
     T[t] = r < col ? tg : -tg;
   }
   mc = warp_max(mc);
-  if ((threadIdx.x & 31) == 0 && mc > 0) atomicMax(maxc, (unsigned long long)__double_as_longlong(mc));
+  ma = warp_max(ma);
+  mt = warp_max(mt);
+  if ((threadIdx.x & 31) == 0) {
+    if (mc > 0) atomicMax(maxc, (unsigned long long)__double_as_longlong(mc));
+    if (ma > 0) atomicMax(maxc + 1, (unsigned long long)__double_as_longlong(ma));
+    if (mt > 0) atomicMax(maxc + 2, (unsigned long long)__double_as_longlong(mt));
+  }
 }
 
-// W = I + T + T2 / 2 (exp(T) to second order) and DW = diag(s) W
+// W = I + T + T2 / 2, exp(T) to second order: W'W = I + T^4 / 4 for
+// antisymmetric T (the third-order terms cancel)
 __global__ void gram_rotation_kernel(int64_t n, const double* __restrict__ T, const double* __restrict__ T2,
-                                     const double* __restrict__ s, double* __restrict__ W, double* __restrict__ DW) {
+                                     double* __restrict__ W) {
   for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < n * n; t += (int64_t)gridDim.x * blockDim.x) {
     const int64_t i = t % n, j = t / n;
-    const double w = (i == j ? 1.0 : 0.0) + T[t] + 0.5 * T2[t];
+    W[t] = (i == j ? 1.0 : 0.0) + T[t] + 0.5 * T2[t];
+  }
+}
+
+// W <- W - W T^4 / 8 (one Newton-Schulz step, W (3 I - W'W) / 2, written for
+// W'W = I + T^4 / 4: the defect falls to O(T^8) while every product involved
+// is small, so no entry of W loses its own relative accuracy), and DW =
+// diag(s) W
+__global__ void gram_finish_kernel(int64_t n, const double* __restrict__ WT4, const double* __restrict__ s,
+                                   double* __restrict__ W, double* __restrict__ DW) {
+  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < n * n; t += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t i = t % n;
+    const double w = WT4 ? W[t] - 0.125 * WT4[t] : W[t];
     W[t] = w;
     DW[t] = s[i] * w;
   }
@@ -226,8 +257,10 @@ __global__ void gram_rotation_kernel(int64_t n, const double* __restrict__ T, co
 // would not for a graded X.  Returns false when the largest cosine is still
 // above tol after a few iterations (clusters of equal singular values, where
 // simultaneous rotations interfere); the caller then finishes with pairwise
-// sweeps from the X and Wacc reached so far.  Wacc (n x n, ld n) is multiplied
-// by each W; S gets the column norms of the final X.
+// sweeps from the X and Wacc reached so far (pairs of nearly equal norms are
+// left to them; an iteration that raised the largest cosine is undone).
+// Wacc (n x n, ld n) is multiplied by each W; S gets the column norms of the
+// final X.
 constexpr double kGramStart = 3e-2;  // largest cosine the FP32 sweeps leave for the Gram polish
 
 bool gram_polish(lra_ctx* ctx, int64_t n, double* X, int64_t ldx, double* Wacc, double* S, double tol,
@@ -241,32 +274,60 @@ bool gram_polish(lra_ctx* ctx, int64_t n, double* X, int64_t ldx, double* Wacc, 
   double* W = ctx->arena.alloc_n<double>(nn);
   double* DW = ctx->arena.alloc_n<double>(nn);
   double* tmp = ctx->arena.alloc_n<double>(nn);
-  unsigned long long* maxc = ctx->arena.alloc_n<unsigned long long>(1);
+  double* Xs = ctx->arena.alloc_n<double>(nn);  // X and Wacc before the last update
+  double* Ws = ctx->arena.alloc_n<double>(nn);
+  unsigned long long* maxc = ctx->arena.alloc_n<unsigned long long>(3);
   const unsigned g = (unsigned)std::max<int64_t>(1, std::min<int64_t>(((int64_t)nn + 255) / 256, ctx->num_sms * 8));
   bool ok = false;
+  double prev = INFINITY;
   for (int it = 0; it <= max_iter; ++it) {
     col_norms<double>(ctx, n, n, X, ldx, S);
     unit_cols_kernel<<<g, 256, 0, ctx->stream>>>(n, X, ldx, S, Xh);
     post_launch(ctx, "unit_cols_kernel");
     gemm<double>(ctx, 't', 'n', n, n, n, 1.0, Xh, n, Xh, n, 0.0, Gh, n);
-    LRA_CUDA(cudaMemsetAsync(maxc, 0, sizeof(unsigned long long), ctx->stream));
+    LRA_CUDA(cudaMemsetAsync(maxc, 0, 3 * sizeof(unsigned long long), ctx->stream));
     gram_tangent_kernel<<<g, 256, 0, ctx->stream>>>(n, Gh, S, Tm, maxc);
     post_launch(ctx, "gram_tangent_kernel");
-    unsigned long long hb = 0;
-    LRA_CUDA(cudaMemcpyAsync(&hb, maxc, sizeof(hb), cudaMemcpyDeviceToHost, ctx->stream));
+    unsigned long long hb[3] = {0, 0, 0};
+    LRA_CUDA(cudaMemcpyAsync(hb, maxc, sizeof(hb), cudaMemcpyDeviceToHost, ctx->stream));
     LRA_CUDA(cudaStreamSynchronize(ctx->stream));
-    double mc;
-    std::memcpy(&mc, &hb, sizeof(mc));
-    if (trace_on()) std::fprintf(stderr, "[lra] gram polish n=%lld iteration %d: max cosine %.3e\n", (long long)n, it, mc);
-    if (!std::isfinite(mc)) break;
+    double mc, ma, mt;
+    std::memcpy(&mc, &hb[0], sizeof(mc));
+    std::memcpy(&ma, &hb[1], sizeof(ma));
+    std::memcpy(&mt, &hb[2], sizeof(mt));
+    if (trace_on())
+      std::fprintf(stderr, "[lra] gram polish n=%lld iteration %d: max cosine %.3e (rotating pairs %.3e)\n",
+                   (long long)n, it, mc, ma);
+    if (!std::isfinite(mc) || mc > prev) {
+      // the last update did not help: back to the state before it
+      if (it > 0) {
+        copy_matrix(ctx, n, n, Xs, n, X, ldx);
+        copy_matrix(ctx, n, n, Ws, n, Wacc, n);
+        col_norms<double>(ctx, n, n, X, ldx, S);
+      }
+      break;
+    }
     if (mc <= tol) {
       ok = true;
       break;
     }
-    if (it == max_iter) break;
+    // only pairs of nearly equal norms are left: the pairwise sweeps finish
+    if (ma <= tol || it == max_iter) break;
+    prev = mc;
+    copy_matrix(ctx, n, n, X, ldx, Xs, n);
+    copy_matrix(ctx, n, n, Wacc, n, Ws, n);
     gemm<double>(ctx, 'n', 'n', n, n, n, 1.0, Tm, n, Tm, n, 0.0, T2, n);
-    gram_rotation_kernel<<<g, 256, 0, ctx->stream>>>(n, Tm, T2, S, W, DW);
+    gram_rotation_kernel<<<g, 256, 0, ctx->stream>>>(n, Tm, T2, W);
     post_launch(ctx, "gram_rotation_kernel");
+    // the orthogonality defect T^4 / 4 matters from |t| ~ 1e-4 on
+    const double* WT4 = nullptr;
+    if (mt * mt * mt * mt > 4e-16) {
+      gemm<double>(ctx, 'n', 'n', n, n, n, 1.0, T2, n, T2, n, 0.0, Tm, n);  // T^4 (T is not needed again)
+      gemm<double>(ctx, 'n', 'n', n, n, n, 1.0, W, n, Tm, n, 0.0, Gh, n);   // W T^4
+      WT4 = Gh;
+    }
+    gram_finish_kernel<<<g, 256, 0, ctx->stream>>>(n, WT4, S, W, DW);
+    post_launch(ctx, "gram_finish_kernel");
     gemm<double>(ctx, 'n', 'n', n, n, n, 1.0, Xh, n, DW, n, 0.0, tmp, n);
     copy_matrix(ctx, n, n, tmp, n, X, ldx);
     gemm<double>(ctx, 'n', 'n', n, n, n, 1.0, Wacc, n, W, n, 0.0, tmp, n);

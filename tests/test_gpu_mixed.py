@@ -94,6 +94,8 @@ def test_psvd_mixed_vs_native(lra):
     assert em < 1e-9
     k = min(Fm.k, Fn.k)
     assert np.allclose(Fm.S[:k], Fn.S[:k], rtol=1e-8, atol=1e-12 * Fn.S[0])
+    assert np.abs(Fm.U.T @ Fm.U - np.eye(Fm.k)).max() < 1e-11
+    assert np.abs(Fm.Vt @ Fm.Vt.T - np.eye(Fm.k)).max() < 1e-10
 
 
 def test_mixed_device_input(lra):
@@ -120,3 +122,29 @@ def test_srft_fft_path(lra, oracle, dt, M, order):
     R = oracle.srft_exact(A.astype(np.float64), d, idx, order)
     tol = 1e-10 if dt == np.float64 else 2e-5
     assert np.abs(B - R).max() <= tol * np.abs(R).max()
+
+
+def test_psvd_mixed_clustered(lra):
+    """Clusters of equal singular values: the Gram polish's simultaneous
+    rotations interfere inside a cluster; the result must still match the
+    FP64 path (the pairwise sweeps take over when the polish stalls)."""
+    rng = np.random.default_rng(12)
+    m, n = 1024, 768
+    U, _ = np.linalg.qr(rng.standard_normal((m, n)))
+    V, _ = np.linalg.qr(rng.standard_normal((n, n)))
+    s = np.concatenate([np.ones(40), 0.5 * np.ones(40), 0.25 * 10.0 ** (-np.arange(n - 80) / 20.0)])
+    A = np.asfortranarray((U * s) @ V.T)
+    g = lattice(13, 6_000_000)
+    Fm = lra.psvdfact(A, lra.LRAOptions(rtol=1e-10, precision="mixed"), rand=lra.RandStream(gauss=g))
+    Fn = lra.psvdfact(A, lra.LRAOptions(rtol=1e-10, precision="native"), rand=lra.RandStream(gauss=g))
+    assert abs(Fm.k - Fn.k) <= 1
+    nrm = np.linalg.norm(A, 2)
+    em = np.linalg.norm(A - Fm.matrix(), 2) / nrm
+    en = np.linalg.norm(A - Fn.matrix(), 2) / nrm
+    assert em <= 2 * en + 1e-14 and em < 1e-9
+    # orthonormal factors to well below rtol (the mixed path's products
+    # carry tensor-core rounding of ~2^-45 per GEMM)
+    k = Fm.k
+    assert np.abs(Fm.U.T @ Fm.U - np.eye(k)).max() < 1e-11
+    assert np.abs(Fm.Vt @ Fm.Vt.T - np.eye(k)).max() < 1e-10
+    assert np.allclose(Fm.S[:80], s[:80], rtol=1e-12)
