@@ -279,6 +279,32 @@ def _host(ptr, shape, dtype, order="F") -> np.ndarray:
     return np.array(np.frombuffer(buf, dtype=dtype, count=count).reshape(shape, order=order), copy=True)
 
 
+class _Result:
+    """Keeps a library result struct alive while numpy arrays view its memory
+    (no host copy of the factors); the matching lra_*_free runs when the last
+    view is gone."""
+
+    def __init__(self, free, ptr):
+        self._free, self._ptr = free, ptr
+
+    def __del__(self):
+        try:
+            self._free(self._ptr)
+        except Exception:  # pragma: no cover - interpreter shutdown
+            pass
+
+
+def _view(ptr, shape, dtype, owner, order="F") -> np.ndarray:
+    """A numpy array on library result memory, kept alive by owner."""
+    count = int(np.prod(shape)) if len(shape) else 1
+    if count == 0 or not ptr:
+        return np.zeros(shape, dtype=dtype, order=order)
+    ct = C.c_double if dtype == np.float64 else (C.c_float if dtype == np.float32 else C.c_int64)
+    buf = (ct * count).from_address(int(ptr) if not isinstance(ptr, int) else ptr)
+    buf._owner = owner
+    return np.frombuffer(buf, dtype=dtype, count=count).reshape(shape, order=order)
+
+
 def _iptr(p) -> int:
     return C.cast(p, C.c_void_p).value or 0
 
@@ -415,14 +441,12 @@ def idfact(*args, **kwargs) -> IDPackedV:
                         _rand(rand), C.byref(out))
     _raise(st, ctx)
     r = out.contents
-    try:
-        k, n = r.k, r.n
-        sk = _host(_iptr(r.sk), (k,), np.int64)
-        rd = _host(_iptr(r.rd), (n - k,), np.int64)
-        T = _host(r.T, (k, n - k), M.np_dtype)
-        return IDPackedV(sk, rd, T, r.nsteps)
-    finally:
-        lib.lra_id_free(out)
+    own = _Result(lib.lra_id_free, out)
+    k, n = r.k, r.n
+    sk = _view(_iptr(r.sk), (k,), np.int64, own)
+    rd = _view(_iptr(r.rd), (n - k,), np.int64, own)
+    T = _view(r.T, (k, n - k), M.np_dtype, own)
+    return IDPackedV(sk, rd, T, r.nsteps)
 
 
 def idfact_batched(mats, opts: LRAOptions | None = None, rands=None, ctx: "Context | None" = None):
@@ -448,12 +472,10 @@ def idfact_batched(mats, opts: LRAOptions | None = None, rands=None, ctx: "Conte
     res = []
     for M, p in zip(Ms, outs):
         r = p.contents
-        try:
-            k, n = r.k, r.n
-            res.append(IDPackedV(_host(_iptr(r.sk), (k,), np.int64), _host(_iptr(r.rd), (n - k,), np.int64),
-                                 _host(r.T, (k, n - k), M.np_dtype), r.nsteps))
-        finally:
-            lib.lra_id_free(p)
+        own = _Result(lib.lra_id_free, p)
+        k, n = r.k, r.n
+        res.append(IDPackedV(_view(_iptr(r.sk), (k,), np.int64, own), _view(_iptr(r.rd), (n - k,), np.int64, own),
+                             _view(r.T, (k, n - k), M.np_dtype, own), r.nsteps))
     return res
 
 
@@ -565,16 +587,14 @@ def _psvd(A, opts, kwargs, vals_only):
                           1 if vals_only else 0, C.byref(out))
     _raise(st, ctx)
     r = out.contents
-    try:
-        k = r.k
-        S = _host(r.S, (k,), M.np_dtype)
-        if vals_only:
-            return S
-        U = _host(r.U, (M.m, k), M.np_dtype)
-        Vt = _host(r.Vt, (k, M.n), M.np_dtype)
-        return PartialSVD(U, S, Vt)
-    finally:
-        lib.lra_psvd_free(out)
+    own = _Result(lib.lra_psvd_free, out)
+    k = r.k
+    S = _view(r.S, (k,), M.np_dtype, own)
+    if vals_only:
+        return S
+    U = _view(r.U, (M.m, k), M.np_dtype, own)
+    Vt = _view(r.Vt, (k, M.n), M.np_dtype, own)
+    return PartialSVD(U, S, Vt)
 
 
 class Server:
