@@ -644,24 +644,20 @@ class Server:
         if st != _ffi.LRA_OK:
             raise LRAError(st, "lra_server_poll: unknown ticket")
         M, rand, req, kind = self._keep.pop(ticket)
-        try:
-            if res.status != _ffi.LRA_OK:
-                raise LRAError(res.status, f"{kind} in the server: {res.error.decode(errors='replace')}")
-            if kind == "idfact":
-                r = res.id.contents
-                k, n = r.k, r.n
-                out = IDPackedV(_host(_iptr(r.sk), (k,), np.int64), _host(_iptr(r.rd), (n - k,), np.int64),
-                                _host(r.T, (k, n - k), M.np_dtype), r.nsteps)
-            else:
-                r = res.psvd.contents
-                k = r.k
-                out = PartialSVD(_host(r.U, (M.m, k), M.np_dtype), _host(r.S, (k,), M.np_dtype),
-                                 _host(r.Vt, (k, M.n), M.np_dtype))
-        finally:
-            if res.id:
-                lib.lra_id_free(res.id)
-            if res.psvd:
-                lib.lra_psvd_free(res.psvd)
+        own_id = _Result(lib.lra_id_free, res.id) if res.id else None
+        own_sv = _Result(lib.lra_psvd_free, res.psvd) if res.psvd else None
+        if res.status != _ffi.LRA_OK:
+            raise LRAError(res.status, f"{kind} in the server: {res.error.decode(errors='replace')}")
+        if kind == "idfact":
+            r = res.id.contents
+            k, n = r.k, r.n
+            out = IDPackedV(_view(_iptr(r.sk), (k,), np.int64, own_id), _view(_iptr(r.rd), (n - k,), np.int64, own_id),
+                            _view(r.T, (k, n - k), M.np_dtype, own_id), r.nsteps)
+        else:
+            r = res.psvd.contents
+            k = r.k
+            out = PartialSVD(_view(r.U, (M.m, k), M.np_dtype, own_sv), _view(r.S, (k,), M.np_dtype, own_sv),
+                             _view(r.Vt, (k, M.n), M.np_dtype, own_sv))
         out.queue_ms, out.run_ms, out.total_ms, out.slot = res.queue_ms, res.run_ms, res.total_ms, res.slot
         return out
 
