@@ -456,8 +456,13 @@ def main():
     qr_ms = st["qr"] / nl
     pivots = sum(min(l, kq + 32) if i == nl - 1 else l for i, (l, kq) in enumerate(zip(orders, ks)))
     qr_gbs = qr_bytes / (qr_ms * 1e-3) / 1e9
+    # DRAM traffic of one launch from the committed ncu capture of the 520-row
+    # launch (profiles/geqp3_df_smem_kernel_sketch520x8192.md: 34.25 MB read +
+    # 0.16 MB written, the sketch read once), scaled to the average launch by
+    # its sketch size
+    qr_traffic = (34.25e6 + 0.16e6) * (sum(orders) / nl) / 520.0
     roof = {"kernel": "geqp3_df_smem_kernel (pivoted QR of the sketch)", "bound": "hbm", "achieved": qr_gbs,
-            "peak": hbm, "unit": "GB/s", "frac": qr_gbs / hbm, "traffic": None,
+            "peak": hbm, "unit": "GB/s", "frac": qr_gbs / hbm, "traffic": qr_traffic,
             "peak_source": f"{src} hbm_gbs, burst",
             "bytes_per_launch": qr_bytes, "ms_per_launch": qr_ms,
             "note": f"latency-bound: {1e3 * st['qr'] / pivots:.1f} us per pivot over {pivots} pivots, "
