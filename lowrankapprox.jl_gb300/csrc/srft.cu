@@ -43,6 +43,16 @@ __global__ void cis_table_kernel(int64_t n, Cx<T>* tab) {
 
 __device__ __forceinline__ unsigned bitrev(unsigned x, int bits) { return __brev(x) >> (32 - bits); }
 
+// exp(-2 pi i t / M): Float32 evaluates it in registers (the table is read
+// at random and its loads, not the arithmetic, bound the sampled sums);
+// Float64 keeps the table (FP64 sin/cos would cost more than the loads)
+__device__ __forceinline__ Cx<float> twiddle(const Cx<float>* tab, int64_t t, int64_t M) {
+  float s, c;
+  sincospif(2.0f * ((float)t / (float)M), &s, &c);
+  return Cx<float>{c, -s};
+}
+__device__ __forceinline__ Cx<double> twiddle(const Cx<double>* tab, int64_t t, int64_t) { return tab[t]; }
+
 constexpr int SRFT_NT = 256;
 constexpr int MAX_PAIRS_PER_THREAD = 8;  // sampled frequencies per thread
 
@@ -120,13 +130,13 @@ __global__ void __launch_bounds__(SRFT_NT) srft_fft_kernel(int64_t M, int64_t N,
             const Cx<T> z1 = Z[C * kcp + p], z2 = Z[Cm * kcp + p];
             const T yar = T(0.5) * (z1.re + z2.re), yai = T(0.5) * (z1.im - z2.im);  // sequence a
             const T ybr = T(0.5) * (z1.im + z2.im), ybi = T(0.5) * (z2.re - z1.re);  // sequence b
-            const Cx<T> wa = tw_M[ph];
+            const Cx<T> wa = twiddle(tw_M, ph, M);
             zr[q] += yar * wa.re - yai * wa.im;
             zi[q] += yar * wa.im + yai * wa.re;
             ph += f;
             if (ph >= M) ph -= M;
             if (kka + 1 < m2) {
-              const Cx<T> wb = tw_M[ph];
+              const Cx<T> wb = twiddle(tw_M, ph, M);
               zr[q] += ybr * wb.re - ybi * wb.im;
               zi[q] += ybr * wb.im + ybi * wb.re;
             }
@@ -165,7 +175,9 @@ bool srft_sketch_fft(lra_ctx* ctx, char trans, int64_t M, int64_t N, const T* A,
   while (((int64_t)1 << lbits) < l) ++lbits;
   const int64_t m2 = M / l;
   const size_t per = (size_t)l * sizeof(Cx<T>);
-  int64_t kcp = std::min<int64_t>(16, (int64_t)((160 * 1024) / per));
+  // at most 48 KB of shared memory per CTA, so that several CTAs (and their
+  // loads) share an SM
+  int64_t kcp = std::min<int64_t>(16, (int64_t)((48 * 1024) / per));
   kcp = std::min<int64_t>(kcp, (m2 + 1) / 2);
   if (kcp < 1) return false;
   const ArenaMark mk = ctx->arena.mark();
