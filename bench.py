@@ -51,6 +51,8 @@ def parse():
                          "--batch-native of them")
     ap.add_argument("--batch-native", type=int, default=256)
     ap.add_argument("--no-tall", action="store_true", help="skip the tall Float32 idfact measurement")
+    ap.add_argument("--srft-sweep", action="store_true",
+                    help="only the SRFT sketch sweep on a Gaussian 65536x4096 Float32 matrix (one JSON line)")
     return ap.parse_args()
 
 
@@ -228,6 +230,37 @@ def measure_tall(lra, ctx, A, peaks, reps: int = 3):
     return out
 
 
+def load_peaks() -> dict:
+    try:
+        return json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
+    except Exception:
+        return {}
+
+
+def measure_srft_sweep(lra, ctx, A, peaks, reps: int = 3):
+    """The SRFT sketch alone at the tall config's orders (40, 72, ..., 1032)
+    on a device-resident Float32 matrix, the sketch written to device memory:
+    per call ms (signs, frequencies, twiddle tables and srft_dif_kernel)
+    and GB/s of A read once against HBM."""
+    import torch
+    m, n = A.shape
+    o = lra.LRAOptions(np.float32, sketch="srft", seed=5)
+    hbm = peaks.get("hbm_gbs") or 6800.0
+    out = {"workload": f"SRFT sketch of a {m}x{n} F32 matrix, device in and out"}
+    for order in [8 + (32 << j) for j in range(6)]:
+        B = torch.empty((n, order), dtype=torch.float32, device=A.device).t()
+        lra.sketch(A, order, o, ctx=ctx, out=B)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for _ in range(reps):
+            lra.sketch(A, order, o, ctx=ctx, out=B)
+        torch.cuda.synchronize()
+        t = (time.perf_counter() - t0) / reps
+        gbs = m * n * 4 / t / 1e9
+        out[str(order)] = {"ms": 1e3 * t, "gbs": gbs, "frac_hbm": gbs / hbm}
+    return out
+
+
 def measure_batched(lra, mats, precision: str, ctx):
     """lra_idfact_batched over the kernel matrices (rtol 1e-10)."""
     import torch
@@ -350,6 +383,10 @@ def main():
     import lowrankapprox as lra
 
     ctx = lra.Context(local)
+    if args.srft_sweep:
+        G = torch.randn((4096, 65536), dtype=torch.float32, device="cuda").t()
+        print(json.dumps({"srft_sweep": measure_srft_sweep(lra, ctx, G, load_peaks())}), flush=True)
+        return
     n = args.n
     A = make_matrix(n)
     torch.cuda.synchronize()
@@ -438,12 +475,7 @@ def main():
     # sketch read and written once per launch) sits far below the HBM
     # roofline; the tensor-core sketch, which streams the input, is reported
     # beside it.
-    import json as _json
-    peaks = {}
-    try:
-        peaks = _json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
-    except Exception:
-        pass
+    peaks = load_peaks()
     orders, ks = sketch_orders(k)
     k_id = k  # ID rank ~ psvd rank before truncation
     flops = psvd_flops(n, n, k_id, k, orders, ks)
@@ -523,6 +555,7 @@ def main():
         try:
             At = tall_f32_matrix()
             tall = measure_tall(lra, ctx, At, peaks)
+            tall["srft_sweep"] = measure_srft_sweep(lra, ctx, At, peaks)
             del At
         except Exception as e:  # pragma: no cover
             tall = {"failed": str(e)}

@@ -168,21 +168,66 @@ __global__ void philox_kernel(uint64_t seed, uint64_t base, int64_t n, T* __rest
   }
 }
 
+// an all-ones exponent field (Inf / NaN), tested on the bits
+__device__ __forceinline__ int nonfinite(double v) {
+  return ((unsigned long long)__double_as_longlong(v) >> 52 & 0x7FF) == 0x7FF;
+}
+__device__ __forceinline__ int nonfinite(float v) { return (__float_as_uint(v) >> 23 & 0xFF) == 0xFF; }
+
+// grid (x: row runs, y: columns); each thread keeps four loads in flight
 template <typename T>
 __global__ void finite_kernel(int64_t m, int64_t n, const T* __restrict__ A, int64_t lda, int* bad) {
-  const int64_t total = m * n;
   int local = 0;
-  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < total;
-       t += (int64_t)gridDim.x * blockDim.x) {
-    const int64_t i = t % m, j = t / m;
-    // an all-ones exponent field (Inf / NaN), tested on the bits
-    if constexpr (sizeof(T) == 8) {
-      if ((((unsigned long long)__double_as_longlong((double)A[i + j * lda]) >> 52) & 0x7FF) == 0x7FF) local = 1;
-    } else {
-      if (((__float_as_uint((float)A[i + j * lda]) >> 23) & 0xFF) == 0xFF) local = 1;
+  const int64_t rstep = (int64_t)gridDim.x * blockDim.x * 4;
+  for (int64_t j = blockIdx.y; j < n; j += gridDim.y) {
+    const T* a = A + j * lda;
+    for (int64_t i0 = (int64_t)blockIdx.x * blockDim.x * 4 + threadIdx.x; i0 < m; i0 += rstep) {
+      T v[4];
+#pragma unroll
+      for (int u = 0; u < 4; ++u) {
+        const int64_t i = i0 + (int64_t)u * blockDim.x;
+        v[u] = i < m ? __ldcs(a + i) : T(0);
+      }
+#pragma unroll
+      for (int u = 0; u < 4; ++u) local |= nonfinite(v[u]);
     }
   }
   if (__syncthreads_or(local) && threadIdx.x == 0) atomicExch(bad, 1);
+}
+
+// the same test on 16-byte words of columns whose length and leading
+// dimension are multiples of 16 bytes (Float32: 4 values per word, Float64 2)
+template <bool F64>
+__global__ void finite_vec_kernel(int64_t mv, int64_t n, const uint4* __restrict__ A, int64_t ldv, int* bad) {
+  int local = 0;
+  const int64_t rstep = (int64_t)gridDim.x * blockDim.x * 4;
+  for (int64_t j = blockIdx.y; j < n; j += gridDim.y) {
+    const uint4* a = A + j * ldv;
+    for (int64_t i0 = (int64_t)blockIdx.x * blockDim.x * 4 + threadIdx.x; i0 < mv; i0 += rstep) {
+      uint4 v[4];
+#pragma unroll
+      for (int u = 0; u < 4; ++u) {
+        const int64_t i = i0 + (int64_t)u * blockDim.x;
+        v[u] = i < mv ? __ldcs(a + i) : make_uint4(0, 0, 0, 0);
+      }
+#pragma unroll
+      for (int u = 0; u < 4; ++u) {
+        if constexpr (F64) {
+          local |= ((v[u].y >> 20 & 0x7FF) == 0x7FF) | ((v[u].w >> 20 & 0x7FF) == 0x7FF);
+        } else {
+          local |= ((v[u].x >> 23 & 0xFF) == 0xFF) | ((v[u].y >> 23 & 0xFF) == 0xFF) |
+                   ((v[u].z >> 23 & 0xFF) == 0xFF) | ((v[u].w >> 23 & 0xFF) == 0xFF);
+        }
+      }
+    }
+  }
+  if (__syncthreads_or(local) && threadIdx.x == 0) atomicExch(bad, 1);
+}
+
+static dim3 finite_grid(lra_ctx* ctx, int64_t m, int64_t n) {
+  const int64_t gx = std::max<int64_t>(1, std::min<int64_t>((m + 1023) / 1024, 64));
+  const int64_t gy = std::max<int64_t>(1, std::min<int64_t>({(int64_t)ctx->num_sms * 8 / gx + 1, n, 65535}));
+  return dim3((unsigned)gx, (unsigned)gy);
 }
 
 // y = alpha A^T x + beta y: one warp per column
@@ -306,10 +351,22 @@ void sketch_philox(lra_ctx* ctx, uint64_t seed, uint64_t base, int64_t n, T* out
 
 // sets *bad (zeroed by the caller) when A has a NaN or Inf entry; no wait
 template <typename T>
+static void launch_finite(lra_ctx* ctx, int64_t m, int64_t n, const T* A, int64_t lda, int* bad) {
+  constexpr int per = 16 / sizeof(T);
+  if (reinterpret_cast<uintptr_t>(A) % 16 == 0 && m % per == 0 && lda % per == 0) {
+    finite_vec_kernel<sizeof(T) == 8><<<finite_grid(ctx, m / per, n), 256, 0, ctx->stream>>>(
+        m / per, n, reinterpret_cast<const uint4*>(A), lda / per, bad);
+    post_launch(ctx, "finite_vec_kernel");
+    return;
+  }
+  finite_kernel<T><<<finite_grid(ctx, m, n), 256, 0, ctx->stream>>>(m, n, A, lda, bad);
+  post_launch(ctx, "finite_kernel");
+}
+
+template <typename T>
 void all_finite_async(lra_ctx* ctx, int64_t m, int64_t n, const T* A, int64_t lda, int* bad) {
   if (m <= 0 || n <= 0) return;
-  finite_kernel<T><<<grid_for(ctx, m * n, 256, 16), 256, 0, ctx->stream>>>(m, n, A, lda, bad);
-  post_launch(ctx, "finite_kernel");
+  launch_finite(ctx, m, n, A, lda, bad);
 }
 
 template <typename T>
@@ -318,8 +375,7 @@ bool all_finite(lra_ctx* ctx, int64_t m, int64_t n, const T* A, int64_t lda) {
   const ArenaMark mark = ctx->arena.mark();
   int* bad = ctx->arena.alloc_n<int>(1);
   LRA_CUDA(cudaMemsetAsync(bad, 0, sizeof(int), ctx->stream));
-  finite_kernel<T><<<grid_for(ctx, m * n, 256, 16), 256, 0, ctx->stream>>>(m, n, A, lda, bad);
-  post_launch(ctx, "finite_kernel");
+  launch_finite(ctx, m, n, A, lda, bad);
   int h = 0;
   LRA_CUDA(cudaMemcpyAsync(&h, bad, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
   LRA_CUDA(cudaStreamSynchronize(ctx->stream));

@@ -533,8 +533,11 @@ def sketchfact(*args, **kwargs):
     return _pqr_out(lib, out, M.np_dtype, True)
 
 
-def sketch(*args, **kwargs) -> np.ndarray:
-    """sketch([side, trans,] A, order[, opts]) (src/sketch.jl:35-50)."""
+def sketch(*args, **kwargs):
+    """sketch([side, trans,] A, order[, opts]) (src/sketch.jl:35-50).  With
+    out= a column-major CUDA tensor of the sketch's shape and element type,
+    the sketch is written there (device to device) and out is returned;
+    otherwise a new host array."""
     args = list(args)
     side, trans = "left", "n"
     if len(args) >= 2 and isinstance(args[0], str) and isinstance(args[1], str):
@@ -544,16 +547,24 @@ def sketch(*args, **kwargs) -> np.ndarray:
     opts = args.pop(0) if args else None
     ctx = kwargs.pop("ctx", None) or default_context()
     rand = kwargs.pop("rand", None)
+    out = kwargs.pop("out", None)
     M = _mat(A)
     opts = (opts or LRAOptions(M.np_dtype)).copy(**kwargs)
     Mop = M.m if trans == "n" else M.n
     Nop = M.n if trans == "n" else M.m
     shape = (order, Nop) if side == "left" else (Mop, order)
-    B = np.zeros(shape, dtype=M.np_dtype, order="F")
+    if out is not None:
+        O = _mat(out)
+        if O.keep is not out or (O.m, O.n) != shape or O.dtype != M.dtype:
+            raise ArgumentError(_ffi.LRA_EINVAL, "out must be a column-major CUDA tensor of the sketch's shape and type")
+        B, ptr, ld = out, O.ptr, O.ld
+    else:
+        B = np.zeros(shape, dtype=M.np_dtype, order="F")
+        ptr, ld = B.ctypes.data, max(shape[0], 1)
     lib = _ffi.load()
     co = opts.to_c()
     st = lib.lra_sketch(ctx.handle, M.dtype, side[0].encode(), trans.encode(), M.m, M.n, C.c_void_p(M.ptr),
-                        M.ld, order, C.byref(co), _rand(rand), C.c_void_p(B.ctypes.data), max(shape[0], 1))
+                        M.ld, order, C.byref(co), _rand(rand), C.c_void_p(ptr), ld)
     _raise(st, ctx)
     return B
 

@@ -108,12 +108,18 @@ def test_mixed_device_input(lra):
 
 
 @pytest.mark.parametrize("dt", [np.float32, np.float64])
-@pytest.mark.parametrize("M,order", [(4096, 72), (2048, 520), (1536, 136)])
+@pytest.mark.parametrize(
+    "M,order",
+    [(4096, 72), (2048, 520), (1536, 136), (65536, 40), (65536, 264), (65536, 1032), (32768, 520),
+     # outside the FFT kernel's range: odd m2 = 3, and l' = 2048
+     (1536, 520), (4096, 2100)])
 def test_srft_fft_path(lra, oracle, dt, M, order):
-    """SRFT through l'-point FFTs (l' a power of two: 64, 512, 128) against
-    the full-length FFT of the same signs and frequencies."""
+    """SRFT through l'-point FFTs (l' a power of two) against the full-length
+    FFT of the same signs and frequencies; the tall shapes run whole chunks
+    of the decimation-in-frequency kernel, the short ones partial chunks and
+    the fallback."""
     rng = np.random.default_rng(M + order)
-    A = np.asfortranarray(rng.standard_normal((M, 300)).astype(dt))
+    A = np.asfortranarray(rng.standard_normal((M, 300 if M <= 4096 else 48)).astype(dt))
     g = rng.standard_normal(M + 10)
     q = rng.integers(1, 2**62, order + 10, dtype=np.int64)
     B = lra.sketch("left", "n", A, order, lra.LRAOptions(dt, sketch="srft"), rand=lra.RandStream(gauss=g, ints=q))
