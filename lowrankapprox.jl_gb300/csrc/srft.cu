@@ -278,6 +278,20 @@ __host__ __device__ constexpr size_t sk_align16(size_t b) { return (b + 15) & ~(
 // log2 of the block length before pass q of the decimation-in-frequency FFT
 constexpr int sk_block_bits(int lb, int q) { return lb - sk_ns_bits(lb, q); }
 
+// per-pass twiddle tables: pass q (all but the last) keeps
+// w^(n1 k2) = exp(-2 pi i n1 k2 / 2^NB) at [(k2 - 1) 2^NPB + n1], so that the
+// lanes of a warp (consecutive n1) read consecutive entries
+constexpr int sk_tw_len(int lb, int q) {
+  return ((1 << sk_bits(lb, q)) - 1) << (sk_block_bits(lb, q) - sk_bits(lb, q));
+}
+constexpr int sk_tw_off(int lb, int q) {
+  int o = 0;
+  for (int i = 0; i < q; ++i)
+    if (i + 1 < sk_passes(lb)) o += sk_tw_len(lb, i);
+  return o;
+}
+constexpr int sk_tw_size(int lb) { return sk_tw_off(lb, sk_passes(lb)); }
+
 // position in Z of frequency k after all passes (digits of k in the pass
 // radices, reversed)
 template <int LB>
@@ -294,12 +308,13 @@ __device__ __forceinline__ int sk_pos(int k) {
 // one group of pass q, in place: v[k2] = w^(n1 k2) sum over n2 of
 // v[n2] exp(-2 pi i n2 k2 / R), w = exp(-2 pi i / 2^NB)
 template <typename T, int LB, int Q, int R>
-__device__ __forceinline__ void sk_butterfly(Cx<T> (&v)[R], int n1, const Cx<T>* tab) {
+__device__ __forceinline__ void sk_butterfly(Cx<T> (&v)[R], int n1, const Cx<T>* tw) {
   constexpr int NB = sk_block_bits(LB, Q), NPB = NB - sk_bits(LB, Q);
   dft_reg<R>(v);
   if constexpr (NPB > 0) {
+    const Cx<T>* tq = tw + sk_tw_off(LB, Q) + n1;
 #pragma unroll
-    for (int k2 = 1; k2 < R; ++k2) v[k2] = cmul(v[k2], tab[(n1 * k2) << (LB - NB)]);
+    for (int k2 = 1; k2 < R; ++k2) v[k2] = cmul(v[k2], tq[(k2 - 1) << NPB]);
   }
 }
 
@@ -408,10 +423,15 @@ struct SkPair {
   int f, cc, dph16;  // cc = pos(C) | pos(l - C mod l) << 16
 };
 
+// CTAs per SM the register budget aims at: three (80 registers) for l up to
+// 128, two (128 registers, no spills) for the three-pass transforms and the
+// radix-16 pairs, where spilled values cost more than the third CTA gains
+constexpr int sk_min_ctas(int lb) { return lb >= 8 ? 2 : 3; }
+
 // grid: columns of op(A) (column-major M x N); a CTA takes the chunks of its
 // columns in turn, loading the next chunk while it sums the current one
 template <typename T, int LB>
-__global__ void __launch_bounds__(SK_NT, 3) srft_dif_kernel(int M, int64_t N, const T* __restrict__ A, int64_t lda,
+__global__ void __launch_bounds__(SK_NT, sk_min_ctas(LB)) srft_dif_kernel(int M, int64_t N, const T* __restrict__ A, int64_t lda,
                                                             const unsigned* __restrict__ dbits,
                                                             const int64_t* __restrict__ idx, int order, int pcb,
                                                             int nsl, const Cx<T>* __restrict__ tw_l,
@@ -431,8 +451,15 @@ __global__ void __launch_bounds__(SK_NT, 3) srft_dif_kernel(int M, int64_t N, co
   SkPair<T>* pairs = reinterpret_cast<SkPair<T>*>(sk_smem + sk_align16((size_t)items * (2 * sizeof(Cx<T>) + 4)));
   Cx<T>* tab = reinterpret_cast<Cx<T>*>(reinterpret_cast<unsigned char*>(pairs) +
                                         sk_align16((size_t)npairs * sizeof(SkPair<T>)));
-  Cx<T>* Z = tab + L;  // [l][PC + 1], rows in digit-reversed frequency order after the passes
-  for (int t = threadIdx.x; t < L; t += SK_NT) tab[t] = tw_l[t];
+  Cx<T>* Z = tab + sk_tw_size(LB);  // [l][PC + 1], rows in digit-reversed frequency order after the passes
+#pragma unroll
+  for (int q = 0; q + 1 < sk_passes(LB); ++q) {
+    const int npb = sk_block_bits(LB, q) - sk_bits(LB, q), len = sk_tw_len(LB, q);
+    for (int e = threadIdx.x; e < len; e += SK_NT) {
+      const int k2 = (e >> npb) + 1, n1 = e & ((1 << npb) - 1);
+      tab[sk_tw_off(LB, q) + e] = tw_l[(n1 * k2) << (LB - sk_block_bits(LB, q))];
+    }
+  }
   for (int pr = threadIdx.x; pr < npairs; pr += SK_NT) {
     const int f = (int)(idx[2 * pr] - 1);
     const int C = f & (L - 1);
@@ -587,7 +614,7 @@ bool srft_sketch_fft(lra_ctx* ctx, char trans, int64_t M, int64_t N, const T* A,
     while ((2 << nsl) <= (1 << pcb) && (2 << nsl) <= 32 && ((int64_t)2 << nsl) * npairs <= SK_NT) ++nsl;
     const size_t items = (size_t)npairs << nsl;
     const size_t smem = sk_align16(items * (2 * sizeof(Cx<T>) + 4)) + sk_align16((size_t)npairs * sizeof(SkPair<T>)) +
-                        (size_t)l * sizeof(Cx<T>) * (size_t)(2 + (1 << pcb));
+                        ((size_t)sk_tw_size(lbits) + (size_t)l * (size_t)(1 + (1 << pcb))) * sizeof(Cx<T>);
     unsigned* dbits = ctx->arena.alloc_n<unsigned>((size_t)(M + 31) / 32);
     sign_bits_kernel<T><<<g1, 256, 0, ctx->stream>>>(M, d, dbits);
     post_launch(ctx, "sign_bits_kernel");
