@@ -346,7 +346,10 @@ __global__ void __launch_bounds__(NT) jacobi_pair_kernel(JacParams<T> P) {
 // memory and rotates every pair among them there (2 JB - 1 local rounds of
 // JB pairs, a warp per pair) before writing them back.  A sweep then costs
 // about n / JB grid barriers instead of n, and the local rotations also
-// reach the pairs inside each block.
+// reach the pairs inside each block.  The local rotations are applied to X
+// one by one and gathered into a 2 JB x 2 JB orthogonal matrix, which is
+// applied to the block's columns of V once, a thread per row, after the
+// local rounds.
 constexpr int JB = 8;
 constexpr int JB_RPL = 16;  // rows per lane in registers (columns up to 512 long)
 
@@ -359,6 +362,7 @@ template <int JBT>
 __global__ void __launch_bounds__(JBT * 32) jacobi_block_kernel(JacParams<float> P) {
   extern __shared__ float jb_smem[];
   __shared__ double red[32];
+  __shared__ float Ql[2 * JBT][2 * JBT];  // column k of the block's local rotation at Ql[k][.]
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
   const int64_t n = P.n;
   float* Xs = jb_smem;                       // [2 JBT][n]
@@ -393,6 +397,8 @@ __global__ void __launch_bounds__(JBT * 32) jacobi_block_kernel(JacParams<float>
             }
           }
         }
+        for (int e = threadIdx.x; e < 4 * JBT * JBT; e += JBT * 32)
+          Ql[e / (2 * JBT)][e % (2 * JBT)] = e / (2 * JBT) == e % (2 * JBT) ? 1.0f : 0.0f;
         asm volatile("cp.async.wait_all;" ::: "memory");
         __syncthreads();
         unsigned vmask = 0;  // local columns that exist
@@ -446,21 +452,10 @@ __global__ void __launch_bounds__(JBT * 32) jacobi_block_kernel(JacParams<float>
                       xq[i] = sn * u[tt] + c * w[tt];
                     }
                   }
-                  float* vp = Vs + p * ni;
-                  float* vq = Vs + q * ni;
-#pragma unroll
-                  for (int tt = 0; tt < JB_RPL; ++tt) {
-                    const int i = lane + 32 * tt;
-                    u[tt] = i < ni ? vp[i] : 0.0f;
-                    w[tt] = i < ni ? vq[i] : 0.0f;
-                  }
-#pragma unroll
-                  for (int tt = 0; tt < JB_RPL; ++tt) {
-                    const int i = lane + 32 * tt;
-                    if (i < ni) {
-                      vp[i] = c * u[tt] - sn * w[tt];
-                      vq[i] = sn * u[tt] + c * w[tt];
-                    }
+                  if (lane < 2 * JBT) {
+                    const float qu = Ql[p][lane], qw = Ql[q][lane];
+                    Ql[p][lane] = c * qu - sn * qw;
+                    Ql[q][lane] = sn * qu + c * qw;
                   }
                 }
               }
@@ -482,15 +477,15 @@ __global__ void __launch_bounds__(JBT * 32) jacobi_block_kernel(JacParams<float>
                   const float t = copysignf(1.0f, zeta) / (fabsf(zeta) + sqrtf(1.0f + zeta * zeta));
                   const float c = rsqrtf(1.0f + t * t);
                   const float sn = c * t;
-                  float* vp = Vs + p * ni;
-                  float* vq = Vs + q * ni;
                   for (int i = lane; i < ni; i += 32) {
                     const float u = xp[i], w = xq[i];
                     xp[i] = c * u - sn * w;
                     xq[i] = sn * u + c * w;
-                    const float vu = vp[i], vw = vq[i];
-                    vp[i] = c * vu - sn * vw;
-                    vq[i] = sn * vu + c * vw;
+                  }
+                  if (lane < 2 * JBT) {
+                    const float qu = Ql[p][lane], qw = Ql[q][lane];
+                    Ql[p][lane] = c * qu - sn * qw;
+                    Ql[q][lane] = sn * qu + c * qw;
                   }
                 }
               }
@@ -498,6 +493,21 @@ __global__ void __launch_bounds__(JBT * 32) jacobi_block_kernel(JacParams<float>
           }
           __syncthreads();
         }
+        // the block's columns of V times the gathered rotation, a thread per row
+        for (int i = threadIdx.x; i < ni; i += JBT * 32) {
+          float acc[2 * JBT];
+#pragma unroll
+          for (int k = 0; k < 2 * JBT; ++k) acc[k] = 0.0f;
+#pragma unroll 1
+          for (int j = 0; j < 2 * JBT; ++j) {  // (not unrolled: Ql would be hoisted into registers)
+            const float v = Vs[j * ni + i];
+#pragma unroll
+            for (int k = 0; k < 2 * JBT; ++k) acc[k] = fmaf(v, Ql[k][j], acc[k]);
+          }
+#pragma unroll
+          for (int k = 0; k < 2 * JBT; ++k) Vs[k * ni + i] = acc[k];
+        }
+        __syncthreads();
         for (int k = 0; k < 2 * JBT; ++k) {
           const int64_t j = gcol(k);
           if (j < 0) continue;
