@@ -181,6 +181,20 @@ constexpr int sk_chunk() {
   return 32768 / (2 * (int)sizeof(T));
 }
 constexpr int sk_passes(int lb) { return (lb + 3) / 4; }
+
+// a kernel configuration: NT threads, and either a run-time chunk width PC
+// (PCF = 0: rows padded to PC + 1 elements) or the compile-time width PCF
+// >= 16 with unpadded rows whose elements are permuted by p ^ (row & 15)
+// (a row then spans all 32 banks, so every pass reads and writes whole rows
+// without conflicts, and the random rows of the sampled sums still spread
+// over the banks)
+template <typename T, int LB, int NTT, int PCF>
+struct SkCfg {
+  static constexpr int NT = NTT;
+  static constexpr int CHUNK = PCF ? (PCF << LB) : sk_chunk<T>();
+  static constexpr int PCFB = PCF >= 256 ? 8 : PCF >= 128 ? 7 : PCF >= 64 ? 6 : PCF >= 32 ? 5 : PCF >= 16 ? 4 : 0;
+  static constexpr int SWM = PCF >= 16 ? 15 : 0;
+};
 // log2 of the radix of pass q (radices 2..16, as even as the passes allow)
 constexpr int sk_bits(int lb, int q) { return lb / sk_passes(lb) + (q < lb % sk_passes(lb) ? 1 : 0); }
 // log2 of the sub-transform length before pass q
@@ -332,10 +346,10 @@ __device__ __forceinline__ double flip1(double x, unsigned w) {
 
 // the inputs of pass 0 for one chunk, held in registers from their loads
 // (issued while the previous chunk's sums run) to their use
-template <typename T, int LB>
+template <typename T, int LB, class CF>
 struct SkIn {
   static constexpr int R = 1 << sk_bits(LB, 0);
-  static constexpr int NG = (sk_chunk<T>() / R + SK_NT - 1) / SK_NT;
+  static constexpr int NG = (CF::CHUNK / R + CF::NT - 1) / CF::NT;
   Cx<T> x[NG][R];
   unsigned w[NG][R];
 };
@@ -343,14 +357,14 @@ struct SkIn {
 // loads of pass 0: z[jj][p] = d x at (jj, kk0 + 2p) + i d x at (jj, kk0 + 2p + 1)
 // for the rows jj = n1 + n2 l / R of each group; the signs d = +-1 come as
 // bits (bit i of dbits set where d[i] = -1)
-template <typename T, int LB>
-__device__ __forceinline__ void sk_load(SkIn<T, LB>& in, const T* __restrict__ x, const unsigned* __restrict__ dbits,
-                                        int m2, int kk0, int pcb) {
-  constexpr int R = SkIn<T, LB>::R, NG = SkIn<T, LB>::NG, NP = (1 << LB) / R;
+template <typename T, int LB, class CF>
+__device__ __forceinline__ void sk_load(SkIn<T, LB, CF>& in, const T* __restrict__ x,
+                                        const unsigned* __restrict__ dbits, int m2, int kk0, int pcb) {
+  constexpr int R = SkIn<T, LB, CF>::R, NG = SkIn<T, LB, CF>::NG, NP = (1 << LB) / R;
   const int groups = NP << pcb;
 #pragma unroll
   for (int k = 0; k < NG; ++k) {
-    const int g = threadIdx.x + k * SK_NT;
+    const int g = threadIdx.x + k * CF::NT;
     if (g < groups) {
       const int n1 = g >> pcb, p = g & ((1 << pcb) - 1);
 #pragma unroll
@@ -364,22 +378,23 @@ __device__ __forceinline__ void sk_load(SkIn<T, LB>& in, const T* __restrict__ x
 }
 
 // pass 0: signs applied, transformed, written to Z
-template <typename T, int LB>
-__device__ __forceinline__ void sk_first(const SkIn<T, LB>& in, Cx<T>* Z, const Cx<T>* tab, int pcb, int pcp) {
-  constexpr int R = SkIn<T, LB>::R, NG = SkIn<T, LB>::NG, NP = (1 << LB) / R;
+template <typename T, int LB, class CF>
+__device__ __forceinline__ void sk_first(const SkIn<T, LB, CF>& in, Cx<T>* Z, const Cx<T>* tab, int pcb, int pcp) {
+  constexpr int R = SkIn<T, LB, CF>::R, NG = SkIn<T, LB, CF>::NG, NP = (1 << LB) / R;
   const int groups = NP << pcb;
   __syncthreads();  // the previous chunk's sums have read Z
 #pragma unroll
   for (int k = 0; k < NG; ++k) {
-    const int g = threadIdx.x + k * SK_NT;
+    const int g = threadIdx.x + k * CF::NT;
     if (g < groups) {
-      const int n1 = g >> pcb, p = g & ((1 << pcb) - 1);
+      const int n1 = g >> pcb, p = (g & ((1 << pcb) - 1)) ^ (n1 & CF::SWM);
       Cx<T> v[R];
 #pragma unroll
       for (int r = 0; r < R; ++r) v[r] = Cx<T>{flip0(in.x[k][r].re, in.w[k][r]), flip1(in.x[k][r].im, in.w[k][r])};
       sk_butterfly<T, LB, 0, R>(v, n1, tab);
+      // rows n1 + r NP with n1 < NP: the row's swizzle splits into n1's and r NP's
 #pragma unroll
-      for (int r = 0; r < R; ++r) Z[(n1 + r * NP) * pcp + p] = v[r];
+      for (int r = 0; r < R; ++r) Z[(n1 + r * NP) * pcp + (p ^ ((r * NP) & CF::SWM))] = v[r];
     }
   }
   __syncthreads();
@@ -387,29 +402,31 @@ __device__ __forceinline__ void sk_first(const SkIn<T, LB>& in, Cx<T>* Z, const 
 
 // passes Q >= 1, each in place in shared memory (a thread reads and writes
 // the same R rows of its groups), one barrier per pass
-template <typename T, int LB, int Q>
+template <typename T, int LB, class CF, int Q>
 __device__ __forceinline__ void sk_rest(Cx<T>* Z, const Cx<T>* tab, int pcb, int pcp) {
   if constexpr (Q < sk_passes(LB)) {
     constexpr int RB = sk_bits(LB, Q), R = 1 << RB, NB = sk_block_bits(LB, Q), NPB = NB - RB;
-    constexpr int NG = (sk_chunk<T>() / R + SK_NT - 1) / SK_NT;
+    constexpr int NG = (CF::CHUNK / R + CF::NT - 1) / CF::NT;
     const int groups = ((1 << LB) / R) << pcb;
 #pragma unroll
     for (int k = 0; k < NG; ++k) {
-      const int g = threadIdx.x + k * SK_NT;
+      const int g = threadIdx.x + k * CF::NT;
       if (g < groups) {
-        const int gi = g >> pcb, p = g & ((1 << pcb) - 1);
+        const int gi = g >> pcb;
         const int n1 = gi & ((1 << NPB) - 1);
-        Cx<T>* z = Z + (((gi >> NPB) << NB) + n1) * pcp + p;
+        const int base = ((gi >> NPB) << NB) + n1;  // rows base + (r << NPB), disjoint bits
+        const int p = (g & ((1 << pcb) - 1)) ^ (base & CF::SWM);
+        Cx<T>* z = Z + base * pcp;
         Cx<T> v[R];
 #pragma unroll
-        for (int r = 0; r < R; ++r) v[r] = z[(r << NPB) * pcp];
+        for (int r = 0; r < R; ++r) v[r] = z[(r << NPB) * pcp + (p ^ ((r << NPB) & CF::SWM))];
         sk_butterfly<T, LB, Q, R>(v, n1, tab);
 #pragma unroll
-        for (int r = 0; r < R; ++r) z[(r << NPB) * pcp] = v[r];
+        for (int r = 0; r < R; ++r) z[(r << NPB) * pcp + (p ^ ((r << NPB) & CF::SWM))] = v[r];
       }
     }
     __syncthreads();
-    sk_rest<T, LB, Q + 1>(Z, tab, pcb, pcp);
+    sk_rest<T, LB, CF, Q + 1>(Z, tab, pcb, pcp);
   }
 }
 
@@ -426,12 +443,12 @@ struct SkPair {
 // CTAs per SM the register budget aims at: three (80 registers) for l up to
 // 128, two (128 registers, no spills) for the three-pass transforms and the
 // radix-16 pairs, where spilled values cost more than the third CTA gains
-constexpr int sk_min_ctas(int lb) { return lb >= 8 ? 2 : 3; }
+constexpr int sk_min_ctas(int lb, int nt) { return nt > 256 ? 1 : lb >= 8 ? 2 : 3; }
 
 // grid: columns of op(A) (column-major M x N); a CTA takes the chunks of its
 // columns in turn, loading the next chunk while it sums the current one
-template <typename T, int LB>
-__global__ void __launch_bounds__(SK_NT, sk_min_ctas(LB)) srft_dif_kernel(int M, int64_t N, const T* __restrict__ A, int64_t lda,
+template <typename T, int LB, class CF>
+__global__ void __launch_bounds__(CF::NT, sk_min_ctas(LB, CF::NT)) srft_dif_kernel(int M, int64_t N, const T* __restrict__ A, int64_t lda,
                                                             const unsigned* __restrict__ dbits,
                                                             const int64_t* __restrict__ idx, int order, int pcb,
                                                             int nsl, const Cx<T>* __restrict__ tw_l,
@@ -439,7 +456,8 @@ __global__ void __launch_bounds__(SK_NT, sk_min_ctas(LB)) srft_dif_kernel(int M,
                                                             int64_t ldb) {
   extern __shared__ __align__(16) unsigned char sk_smem[];
   constexpr int L = 1 << LB;
-  const int PC = 1 << pcb, pcp = PC + 1, NS = 1 << nsl;
+  if (CF::PCFB) pcb = CF::PCFB;
+  const int PC = 1 << pcb, pcp = CF::SWM ? PC : PC + 1, NS = 1 << nsl;
   const int npairs = (order + 1) / 2, items = npairs << nsl;
   const int m2 = M >> LB, per_chunk = PC >> nsl, nchunks = m2 / (2 * PC);
   const int run = per_chunk < SK_RUN ? per_chunk : SK_RUN;
@@ -455,12 +473,12 @@ __global__ void __launch_bounds__(SK_NT, sk_min_ctas(LB)) srft_dif_kernel(int M,
 #pragma unroll
   for (int q = 0; q + 1 < sk_passes(LB); ++q) {
     const int npb = sk_block_bits(LB, q) - sk_bits(LB, q), len = sk_tw_len(LB, q);
-    for (int e = threadIdx.x; e < len; e += SK_NT) {
+    for (int e = threadIdx.x; e < len; e += CF::NT) {
       const int k2 = (e >> npb) + 1, n1 = e & ((1 << npb) - 1);
       tab[sk_tw_off(LB, q) + e] = tw_l[(n1 * k2) << (LB - sk_block_bits(LB, q))];
     }
   }
-  for (int pr = threadIdx.x; pr < npairs; pr += SK_NT) {
+  for (int pr = threadIdx.x; pr < npairs; pr += CF::NT) {
     const int f = (int)(idx[2 * pr] - 1);
     const int C = f & (L - 1);
     const Cx<T> w = twiddle(tw_M, f, M);
@@ -478,34 +496,36 @@ __global__ void __launch_bounds__(SK_NT, sk_min_ctas(LB)) srft_dif_kernel(int M,
   // exact integer phase f kk mod M; the item's own thread is the only one
   // to touch its state
   auto start_column = [&]() {
-    for (int it = threadIdx.x; it < items; it += SK_NT) {
+    for (int it = threadIdx.x; it < items; it += CF::NT) {
       st_acc[it] = Cx<T>{T(0), T(0)};
       st_ph[it] = (int)(((int64_t)pairs[it >> nsl].f * (2 * (it & (NS - 1)))) % M);
     }
   };
   int64_t col = blockIdx.x;
   int ch = 0;
-  SkIn<T, LB> in;
+  SkIn<T, LB, CF> in;
   if (col < N) {
     start_column();
-    sk_load<T, LB>(in, A + col * lda, dbits, m2, 0, pcb);
+    sk_load<T, LB, CF>(in, A + col * lda, dbits, m2, 0, pcb);
   }
   while (col < N) {
-    sk_first<T, LB>(in, Z, tab, pcb, pcp);
-    sk_rest<T, LB, 1>(Z, tab, pcb, pcp);
+    sk_first<T, LB, CF>(in, Z, tab, pcb, pcp);
+    sk_rest<T, LB, CF, 1>(Z, tab, pcb, pcp);
     int64_t ncol = col;
     int nch = ch + 1;
     if (nch == nchunks) {
       ncol = col + gridDim.x;
       nch = 0;
     }
-    if (ncol < N) sk_load<T, LB>(in, A + ncol * lda, dbits, m2, nch * 2 * PC, pcb);
+    if (ncol < N) sk_load<T, LB, CF>(in, A + ncol * lda, dbits, m2, nch * 2 * PC, pcb);
     const int t0 = ch * per_chunk;  // steps taken so far in this column
-    for (int it = threadIdx.x; it < items; it += SK_NT) {
+    for (int it = threadIdx.x; it < items; it += CF::NT) {
       const SkPair<T> P = pairs[it >> nsl];
       const int s = it & (NS - 1);
-      const Cx<T>* z1p = Z + (P.cc & 0xffff) * pcp + s;
-      const Cx<T>* z2p = Z + (P.cc >> 16) * pcp + s;
+      const int row1 = P.cc & 0xffff, row2 = P.cc >> 16;
+      const int sw1 = row1 & CF::SWM, sw2 = row2 & CF::SWM;
+      const Cx<T>* z1p = Z + row1 * pcp;
+      const Cx<T>* z2p = Z + row2 * pcp;
       Cx<T> a = st_acc[it], c = st_cur[it];
       int h = st_ph[it];
       for (int i0 = 0; i0 < per_chunk; i0 += run) {
@@ -516,7 +536,8 @@ __global__ void __launch_bounds__(SK_NT, sk_min_ctas(LB)) srft_dif_kernel(int M,
         }
 #pragma unroll 4
         for (int i = 0; i < run; ++i) {
-          const Cx<T> z1 = z1p[(i0 + i) << nsl], z2 = z2p[(i0 + i) << nsl];
+          const int pp = s + ((i0 + i) << nsl);
+          const Cx<T> z1 = z1p[pp ^ sw1], z2 = z2p[pp ^ sw2];
           // t = (z1 + conj z2) + v (z1 - conj z2) = 2 (Y_a + Y_b w^f)
           const T sr = z1.re + z2.re, si = z1.im - z2.im, dr = z1.re - z2.re, di = z1.im + z2.im;
           const T tr = sr + P.v.re * dr - P.v.im * di, ti = si + P.v.re * di + P.v.im * dr;
@@ -531,7 +552,7 @@ __global__ void __launch_bounds__(SK_NT, sk_min_ctas(LB)) srft_dif_kernel(int M,
     }
     if (ch + 1 == nchunks) {
       // combine the NS splits of each pair (consecutive lanes) and store
-      for (int it0 = 0; it0 < items; it0 += SK_NT) {
+      for (int it0 = 0; it0 < items; it0 += CF::NT) {
         const int it = it0 + threadIdx.x;
         Cx<T> a = it < items ? st_acc[it] : Cx<T>{T(0), T(0)};
         for (int o = NS >> 1; o > 0; o >>= 1) {
@@ -551,17 +572,17 @@ __global__ void __launch_bounds__(SK_NT, sk_min_ctas(LB)) srft_dif_kernel(int M,
   }
 }
 
-template <typename T, int LB>
+template <typename T, int LB, class CF>
 void launch_dif(lra_ctx* ctx, int M, int64_t N, const T* A, int64_t lda, const unsigned* d,
-                     const int64_t* idx, int order, int pcb, int nsl, const Cx<T>* tw_l, const Cx<T>* tw_M, T* B,
-                     int64_t ldb, size_t smem) {
-  auto* kern = srft_dif_kernel<T, LB>;
+                const int64_t* idx, int order, int pcb, int nsl, const Cx<T>* tw_l, const Cx<T>* tw_M, T* B,
+                int64_t ldb, size_t smem) {
+  auto* kern = srft_dif_kernel<T, LB, CF>;
   raise_smem_limit(ctx, (const void*)kern);
   int per_sm = 0;
-  LRA_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, SK_NT, smem));
+  LRA_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, CF::NT, smem));
   if (per_sm < 1) per_sm = 1;
   const unsigned grid = (unsigned)std::min<int64_t>(N, (int64_t)ctx->num_sms * per_sm);
-  kern<<<grid, SK_NT, smem, ctx->stream>>>(M, N, A, lda, d, idx, order, pcb, nsl, tw_l, tw_M, B, ldb);
+  kern<<<grid, CF::NT, smem, ctx->stream>>>(M, N, A, lda, d, idx, order, pcb, nsl, tw_l, tw_M, B, ldb);
   post_launch(ctx, "srft_dif_kernel");
 }
 
@@ -605,28 +626,55 @@ bool srft_sketch_fft(lra_ctx* ctx, char trans, int64_t M, int64_t N, const T* A,
                         npairs <= (int64_t)SK_PAIRS_MAX && ldx % 2 == 0 &&
                         reinterpret_cast<uintptr_t>(X) % pair_align == 0;
   if (dif) {
-    // chunk width PC: a power of two dividing m2 / 2, at most the kernel's
-    const int64_t pc_max = std::max<int64_t>(1, (int64_t)sk_chunk<T>() >> lbits);
+    // Float32 with l' = 128 .. 512 and m2 / 2 a multiple of PC = 8192 / l':
+    // 512 threads and swizzled rows PC wide (chunks of 8192 complex values;
+    // measured 2%, 4% and 19% faster than the padded form at 128, 256 and
+    // 512, and 3% slower at 64); otherwise 256 threads and padded rows of a
+    // chunk width PC, a power of two dividing m2 / 2, at most the kernel's
+    const int wide_pcb = 13 - lbits;
+    const bool wide = sizeof(T) == 4 && lbits >= 7 && lbits <= 9 && (m2 / 2) % (1 << wide_pcb) == 0;
+    const int nt = wide ? 512 : SK_NT;
     int pcb = 0;
-    while (((int64_t)2 << pcb) <= pc_max && (m2 / 2) % ((int64_t)2 << pcb) == 0) ++pcb;
+    if (wide) {
+      pcb = wide_pcb;
+    } else {
+      const int64_t pc_max = std::max<int64_t>(1, (int64_t)sk_chunk<T>() >> lbits);
+      while (((int64_t)2 << pcb) <= pc_max && (m2 / 2) % ((int64_t)2 << pcb) == 0) ++pcb;
+    }
     // splits of each pair's sum: as many as idle threads allow, within a warp
     int nsl = 0;
-    while ((2 << nsl) <= (1 << pcb) && (2 << nsl) <= 32 && ((int64_t)2 << nsl) * npairs <= SK_NT) ++nsl;
+    while ((2 << nsl) <= (1 << pcb) && (2 << nsl) <= 32 && ((int64_t)2 << nsl) * npairs <= nt) ++nsl;
     const size_t items = (size_t)npairs << nsl;
     const size_t smem = sk_align16(items * (2 * sizeof(Cx<T>) + 4)) + sk_align16((size_t)npairs * sizeof(SkPair<T>)) +
-                        ((size_t)sk_tw_size(lbits) + (size_t)l * (size_t)(1 + (1 << pcb))) * sizeof(Cx<T>);
+                        ((size_t)sk_tw_size(lbits) + (size_t)l * (size_t)((wide ? 0 : 1) + (1 << pcb))) * sizeof(Cx<T>);
     unsigned* dbits = ctx->arena.alloc_n<unsigned>((size_t)(M + 31) / 32);
     sign_bits_kernel<T><<<g1, 256, 0, ctx->stream>>>(M, d, dbits);
     post_launch(ctx, "sign_bits_kernel");
     const int Mi = (int)M, oi = (int)order;
-    switch (lbits) {
-#define SK_CASE(LB)                                                                                      \
-  case LB:                                                                                               \
-    launch_dif<T, LB>(ctx, Mi, N, X, ldx, dbits, idx, oi, pcb, nsl, tw_l, tw_M, B, ldb, smem);   \
+    if constexpr (sizeof(T) == 4) {
+      if (wide) {
+        switch (lbits) {
+#define SK_WIDE(LB)                                                                                             \
+  case LB:                                                                                                      \
+    launch_dif<T, LB, SkCfg<T, LB, 512, (1 << (13 - LB))>>(ctx, Mi, N, X, ldx, dbits, idx, oi, pcb, nsl, tw_l, \
+                                                           tw_M, B, ldb, smem);                               \
     break;
-      SK_CASE(1) SK_CASE(2) SK_CASE(3) SK_CASE(4) SK_CASE(5)
-      SK_CASE(6) SK_CASE(7) SK_CASE(8) SK_CASE(9) SK_CASE(10)
+          SK_WIDE(7) SK_WIDE(8) SK_WIDE(9)
+#undef SK_WIDE
+        }
+      }
+    }
+    if (!wide) {
+      switch (lbits) {
+#define SK_CASE(LB)                                                                                          \
+  case LB:                                                                                                   \
+    launch_dif<T, LB, SkCfg<T, LB, SK_NT, 0>>(ctx, Mi, N, X, ldx, dbits, idx, oi, pcb, nsl, tw_l, tw_M, B, ldb, \
+                                             smem);                                                          \
+    break;
+        SK_CASE(1) SK_CASE(2) SK_CASE(3) SK_CASE(4) SK_CASE(5)
+        SK_CASE(6) SK_CASE(7) SK_CASE(8) SK_CASE(9) SK_CASE(10)
 #undef SK_CASE
+      }
     }
   } else {
     const size_t per = (size_t)l * sizeof(Cx<T>);

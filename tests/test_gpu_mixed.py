@@ -110,7 +110,8 @@ def test_mixed_device_input(lra):
 @pytest.mark.parametrize("dt", [np.float32, np.float64])
 @pytest.mark.parametrize(
     "M,order",
-    [(4096, 72), (2048, 520), (1536, 136), (65536, 40), (65536, 264), (65536, 1032), (32768, 520),
+    [(4096, 72), (2048, 520), (1536, 136), (65536, 40), (65536, 72), (65536, 136), (65536, 264), (65536, 1032),
+     (32768, 520), (8192, 264),
      # outside the FFT kernel's range: odd m2 = 3, and l' = 2048
      (1536, 520), (4096, 2100)])
 def test_srft_fft_path(lra, oracle, dt, M, order):
