@@ -184,16 +184,16 @@ constexpr int sk_passes(int lb) { return (lb + 3) / 4; }
 
 // a kernel configuration: NT threads, and either a run-time chunk width PC
 // (PCF = 0: rows padded to PC + 1 elements) or the compile-time width PCF
-// >= 16 with unpadded rows whose elements are permuted by p ^ (row & 15)
-// (a row then spans all 32 banks, so every pass reads and writes whole rows
-// without conflicts, and the random rows of the sampled sums still spread
-// over the banks)
+// >= 8 with unpadded rows whose elements are permuted by p ^ (row & 15)
+// (p ^ (row & 7) for PCF = 8): a row of 16 or more then spans all 32 banks,
+// so every pass reads and writes whole rows without conflicts, and the
+// random rows of the sampled sums still spread over the banks
 template <typename T, int LB, int NTT, int PCF>
 struct SkCfg {
   static constexpr int NT = NTT;
   static constexpr int CHUNK = PCF ? (PCF << LB) : sk_chunk<T>();
-  static constexpr int PCFB = PCF >= 256 ? 8 : PCF >= 128 ? 7 : PCF >= 64 ? 6 : PCF >= 32 ? 5 : PCF >= 16 ? 4 : 0;
-  static constexpr int SWM = PCF >= 16 ? 15 : 0;
+  static constexpr int PCFB = PCF >= 256 ? 8 : PCF >= 128 ? 7 : PCF >= 64 ? 6 : PCF >= 32 ? 5 : PCF >= 16 ? 4 : PCF >= 8 ? 3 : 0;
+  static constexpr int SWM = PCF >= 16 ? 15 : PCF >= 8 ? 7 : 0;
 };
 // log2 of the radix of pass q (radices 2..16, as even as the passes allow)
 constexpr int sk_bits(int lb, int q) { return lb / sk_passes(lb) + (q < lb % sk_passes(lb) ? 1 : 0); }
@@ -626,13 +626,14 @@ bool srft_sketch_fft(lra_ctx* ctx, char trans, int64_t M, int64_t N, const T* A,
                         npairs <= (int64_t)SK_PAIRS_MAX && ldx % 2 == 0 &&
                         reinterpret_cast<uintptr_t>(X) % pair_align == 0;
   if (dif) {
-    // Float32 with l' = 128 .. 512 and m2 / 2 a multiple of PC = 8192 / l':
+    // Float32 with l' = 128 .. 1024 and m2 / 2 a multiple of PC = 8192 / l':
     // 512 threads and swizzled rows PC wide (chunks of 8192 complex values;
-    // measured 2%, 4% and 19% faster than the padded form at 128, 256 and
-    // 512, and 3% slower at 64); otherwise 256 threads and padded rows of a
-    // chunk width PC, a power of two dividing m2 / 2, at most the kernel's
+    // measured 2%, 4%, 19% and 17% faster than the padded form at 128, 256,
+    // 512 and 1024, and 3% slower at 64); otherwise 256 threads and padded
+    // rows of a chunk width PC, a power of two dividing m2 / 2, at most the
+    // kernel's
     const int wide_pcb = 13 - lbits;
-    const bool wide = sizeof(T) == 4 && lbits >= 7 && lbits <= 9 && (m2 / 2) % (1 << wide_pcb) == 0;
+    const bool wide = sizeof(T) == 4 && lbits >= 7 && lbits <= 10 && (m2 / 2) % (1 << wide_pcb) == 0;
     const int nt = wide ? 512 : SK_NT;
     int pcb = 0;
     if (wide) {
@@ -659,7 +660,7 @@ bool srft_sketch_fft(lra_ctx* ctx, char trans, int64_t M, int64_t N, const T* A,
     launch_dif<T, LB, SkCfg<T, LB, 512, (1 << (13 - LB))>>(ctx, Mi, N, X, ldx, dbits, idx, oi, pcb, nsl, tw_l, \
                                                            tw_M, B, ldb, smem);                               \
     break;
-          SK_WIDE(7) SK_WIDE(8) SK_WIDE(9)
+          SK_WIDE(7) SK_WIDE(8) SK_WIDE(9) SK_WIDE(10)
 #undef SK_WIDE
         }
       }
