@@ -201,19 +201,22 @@ def measure_tall(lra, ctx, A, peaks, reps: int = 3):
         o = lra.LRAOptions(np.float32, rtol=1e-6, sketch=sk, precision="mixed", seed=5)
         V = lra.idfact(A, o, ctx=ctx)
         torch.cuda.synchronize()
-        sketch_ms, t = 0.0, 0.0
+        stages = {"sketch": 0.0, "qr": 0.0, "solve": 0.0, "post": 0.0}
+        t = 0.0
         for _ in range(reps):
             t0 = time.perf_counter()
             V = lra.idfact(A, o, ctx=ctx)
             torch.cuda.synchronize()
             t += time.perf_counter() - t0
-            sketch_ms += ctx.stage_ms()["sketch"]
+            for kk, v in ctx.stage_ms().items():
+                stages[kk] = stages.get(kk, 0.0) + v
         t /= reps
-        sketch_ms /= reps
+        stages = {kk: v / reps for kk, v in stages.items()}
+        sketch_ms = stages["sketch"]
         a, b = o.sketchfact_srft_samp if sk == "srft" else o.sketchfact_randn_samp
         orders = [a * (o.nb << j) + b for j in range(V.nsteps)]
         r = {"ms_per_call": 1e3 * t, "matrices_s": 1.0 / t, "rank": V.k, "steps": V.nsteps, "orders": orders,
-             "sketch_ms": sketch_ms,
+             "sketch_ms": sketch_ms, "stage_ms": stages,
              "rel_spectral_err": lra.snormdiff(A, V, ctx=ctx) / nrm}
         if sk == "srft":
             gbs = len(orders) * m * n * 4 / (sketch_ms * 1e-3) / 1e9

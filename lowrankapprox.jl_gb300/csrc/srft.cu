@@ -622,9 +622,11 @@ bool srft_sketch_fft(lra_ctx* ctx, char trans, int64_t M, int64_t N, const T* A,
     post_launch(ctx, "cis_table_kernel");
   }
   const int64_t pair_align = 2 * (int64_t)sizeof(T);
-  const bool dif = lbits <= 10 && m2 % 2 == 0 && M < ((int64_t)1 << 31) &&
-                        npairs <= (int64_t)SK_PAIRS_MAX && ldx % 2 == 0 &&
-                        reinterpret_cast<uintptr_t>(X) % pair_align == 0;
+  bool dif = lbits <= 10 && m2 % 2 == 0 && M < ((int64_t)1 << 31) && npairs <= (int64_t)SK_PAIRS_MAX &&
+             ldx % 2 == 0 && reinterpret_cast<uintptr_t>(X) % pair_align == 0;
+  bool wide = false;
+  int pcb = 0, nsl = 0;
+  size_t smem = 0;
   if (dif) {
     // Float32 with l' = 128 .. 1024 and m2 / 2 a multiple of PC = 8192 / l':
     // 512 threads and swizzled rows PC wide (chunks of 8192 complex values;
@@ -633,9 +635,8 @@ bool srft_sketch_fft(lra_ctx* ctx, char trans, int64_t M, int64_t N, const T* A,
     // rows of a chunk width PC, a power of two dividing m2 / 2, at most the
     // kernel's
     const int wide_pcb = 13 - lbits;
-    const bool wide = sizeof(T) == 4 && lbits >= 7 && lbits <= 10 && (m2 / 2) % (1 << wide_pcb) == 0;
+    wide = sizeof(T) == 4 && lbits >= 7 && lbits <= 10 && (m2 / 2) % (1 << wide_pcb) == 0;
     const int nt = wide ? 512 : SK_NT;
-    int pcb = 0;
     if (wide) {
       pcb = wide_pcb;
     } else {
@@ -643,11 +644,15 @@ bool srft_sketch_fft(lra_ctx* ctx, char trans, int64_t M, int64_t N, const T* A,
       while (((int64_t)2 << pcb) <= pc_max && (m2 / 2) % ((int64_t)2 << pcb) == 0) ++pcb;
     }
     // splits of each pair's sum: as many as idle threads allow, within a warp
-    int nsl = 0;
     while ((2 << nsl) <= (1 << pcb) && (2 << nsl) <= 32 && ((int64_t)2 << nsl) * npairs <= nt) ++nsl;
     const size_t items = (size_t)npairs << nsl;
-    const size_t smem = sk_align16(items * (2 * sizeof(Cx<T>) + 4)) + sk_align16((size_t)npairs * sizeof(SkPair<T>)) +
-                        ((size_t)sk_tw_size(lbits) + (size_t)l * (size_t)((wide ? 0 : 1) + (1 << pcb))) * sizeof(Cx<T>);
+    smem = sk_align16(items * (2 * sizeof(Cx<T>) + 4)) + sk_align16((size_t)npairs * sizeof(SkPair<T>)) +
+           ((size_t)sk_tw_size(lbits) + (size_t)l * (size_t)((wide ? 0 : 1) + (1 << pcb))) * sizeof(Cx<T>);
+    int optin = 0;
+    LRA_CUDA(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, ctx->device));
+    dif = smem + 1024 <= (size_t)optin;  // (the kernel's static shared memory is a few bytes)
+  }
+  if (dif) {
     unsigned* dbits = ctx->arena.alloc_n<unsigned>((size_t)(M + 31) / 32);
     sign_bits_kernel<T><<<g1, 256, 0, ctx->stream>>>(M, d, dbits);
     post_launch(ctx, "sign_bits_kernel");
