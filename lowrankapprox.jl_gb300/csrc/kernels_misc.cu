@@ -224,9 +224,12 @@ __global__ void finite_vec_kernel(int64_t mv, int64_t n, const uint4* __restrict
   if (__syncthreads_or(local) && threadIdx.x == 0) atomicExch(bad, 1);
 }
 
+// (x: runs of 1024 rows, at most 64; y: columns, so that a block sees at
+// least 4096 elements and the grid about eight blocks per SM)
 static dim3 finite_grid(lra_ctx* ctx, int64_t m, int64_t n) {
   const int64_t gx = std::max<int64_t>(1, std::min<int64_t>((m + 1023) / 1024, 64));
-  const int64_t gy = std::max<int64_t>(1, std::min<int64_t>({(int64_t)ctx->num_sms * 8 / gx + 1, n, 65535}));
+  const int64_t by_size = (m * n + gx * 4096 - 1) / (gx * 4096);
+  const int64_t gy = std::max<int64_t>(1, std::min<int64_t>({(int64_t)ctx->num_sms * 8 / gx + 1, by_size, n, 65535}));
   return dim3((unsigned)gx, (unsigned)gy);
 }
 
