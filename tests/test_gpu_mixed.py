@@ -131,6 +131,24 @@ def test_srft_fft_path(lra, oracle, dt, M, order):
     assert np.abs(B - R).max() <= tol * np.abs(R).max()
 
 
+def test_sketch_into_device_tensor(lra):
+    """sketch(..., out=B) with B a column-major CUDA tensor: the same values
+    as the host result; a tensor of the wrong shape is refused."""
+    import torch
+    rng = np.random.default_rng(5)
+    A = np.asfortranarray(rng.standard_normal((4096, 64)).astype(np.float32))
+    g = rng.standard_normal(5000)
+    q = rng.integers(1, 2**62, 600, dtype=np.int64)
+    o = lra.LRAOptions(np.float32, sketch="srft")
+    H = lra.sketch("left", "n", A, 264, o, rand=lra.RandStream(gauss=g, ints=q))
+    B = torch.empty((64, 264), dtype=torch.float32, device="cuda").t()
+    R = lra.sketch("left", "n", A, 264, o, rand=lra.RandStream(gauss=g, ints=q), out=B)
+    assert R is B
+    assert np.array_equal(B.cpu().numpy(), H)
+    with pytest.raises(lra.LRAError):
+        lra.sketch("left", "n", A, 264, o, out=torch.empty((64, 263), dtype=torch.float32, device="cuda").t())
+
+
 def test_psvd_mixed_clustered(lra):
     """Clusters of equal singular values: the Gram polish's simultaneous
     rotations interfere inside a cluster; the result must still match the
