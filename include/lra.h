@@ -211,10 +211,23 @@ int lra_sketch(lra_ctx* ctx, int dtype, char side, char trans, int64_t m,
 
 /* sketchfact(side, trans, A) (src/sketch.jl:52-63, 223-240): adaptive
    sketch + partial pivoted QR; returns PartialQRFactors with the options'
-   pqrfact_retval (Q is the Q of the sketch, as in the reference).          */
+   pqrfact_retval (Q is the Q of the sketch, as in the reference).  side
+   'l': the QR of S op(A) (order x N', pivots over the columns of op(A));
+   side 'r': the QR of op(A) S (M' x order, pivots over the sketch's
+   columns; its Q is prange's basis of the range of op(A)).                 */
 int lra_sketchfact(lra_ctx* ctx, int dtype, char side, char trans, int64_t m,
                    int64_t n, const void* A, int64_t lda, const lra_opts* opts,
                    const lra_rand* rand, lra_pqr** out);
+
+/* prange(trans, A, opts) (src/prange.jl:14-61): an orthonormal basis of the
+   range of op(A) for trans 'n' / 'c' (the Q of sketchfact(:right, ...); of
+   pqrfact with sketch :none; of the skeleton columns for :sub), or of the
+   ranges of A and A' together for trans 'b' (A square).  The result holds
+   Q only (m' x k, retval LRA_RET_Q), n = k and p the identity.  maxdet_tol
+   >= 0 gives LRA_ENOTSUP.                                                   */
+int lra_prange(lra_ctx* ctx, int dtype, char trans, int64_t m, int64_t n,
+               const void* A, int64_t lda, const lra_opts* opts,
+               const lra_rand* rand, lra_pqr** out);
 
 /* geqp3_adap! (src/pqr.jl:348-418) on a DEVICE matrix, in place: B (m x n,
    ldb) becomes R (upper) + Householder vectors (below), jpvt (n, int64,

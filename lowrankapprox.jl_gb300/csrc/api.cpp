@@ -490,6 +490,51 @@ Fact<T> sketchfact_dev(lra_ctx* ctx, const lra_opts& o, char trans, int64_t M, i
   return F;
 }
 
+// sketchfact(:right, trans, A) (src/sketch.jl:223-240 and twins): the same
+// adaptive loop on the right sketch op(A) S (M x order), made as the
+// transpose of the left sketch of op(A)' exactly as lra_sketch makes it;
+// the pivots run over the sketch's order columns
+template <typename T>
+Fact<T> sketchfact_right_dev(lra_ctx* ctx, const lra_opts& o, char trans, int64_t M, int64_t N, const T* A,
+                             int64_t lda, RandSrc& rs, int dtype) {
+  const bool adaptive = o.sketchfact_adap || o.rank < 0;
+  int64_t nt = adaptive ? o.nb : o.rank;
+  const char tt = trans == 'n' ? 'c' : 'n';
+  Fact<T> F;
+  F.order = M;
+  F.ld = std::max<int64_t>(M, 1);
+  const ArenaMark base = ctx->arena.mark();
+  for (int step = 0;; ++step) {
+    if (step > 62) fail(LRA_EINVAL, "adaptive sketch did not terminate");
+    const int64_t order = samp(o, nt);
+    if (order < 0) fail(LRA_EINVAL, "sketch order %lld", (long long)order);
+    const int64_t l = std::min(order, M);
+    const int64_t kmax = (o.rank < 0 || o.rank > l) ? l : o.rank;
+    F.N = order;
+    F.B = ctx->arena.alloc_n<T>((size_t)F.ld * std::max<int64_t>(order, 1));
+    F.jpvt = ctx->arena.alloc_n<int64_t>(std::max<int64_t>(order, 1));
+    F.tau = ctx->arena.alloc_n<T>(std::max<int64_t>(l, 1));
+    {
+      Stage st(ctx, 0);
+      const ArenaMark mk = ctx->arena.mark();
+      T* Bt = ctx->arena.alloc_n<T>((size_t)std::max<int64_t>(order, 1) * std::max<int64_t>(M, 1));
+      make_sketch<T>(ctx, o, tt, N, M, A, lda, order, rs, Bt, dtype, nullptr, true);
+      if (order > 0 && M > 0) transpose(ctx, order, M, Bt, order, F.B, F.ld);
+      LRA_CUDA(cudaStreamSynchronize(ctx->stream));
+      ctx->arena.release(mk);
+    }
+    {
+      Stage st(ctx, 1);
+      F.k = geqp3_adap<T>(ctx, M, order, F.B, F.ld, F.jpvt, F.tau, kmax, o.nb, o.atol, o.rtol, true);
+    }
+    F.nsteps = step + 1;
+    if (!adaptive || F.k < nt) break;
+    nt *= 2;
+    ctx->arena.release(base);
+  }
+  return F;
+}
+
 template <typename T>
 void postproc_t(lra_ctx* ctx, const lra_opts& o, Fact<T>& F, bool want_t) {
   const bool maxdet = F.k > 0 && F.k < F.N && o.maxdet_tol >= 0;
@@ -1226,7 +1271,8 @@ int lra_sketchfact(lra_ctx* ctx, int dtype, char side, char trans, int64_t m, in
     check_dims(m, n);
     if (!out) fail(LRA_EINVAL, "out is NULL");
     const char t = chktrans(trans);
-    if (side != 'l' && side != 'L') fail(LRA_ENOTSUP, "sketchfact: only side = :left is built");
+    if (side != 'l' && side != 'L' && side != 'r' && side != 'R') fail(LRA_EINVAL, "side");
+    const bool left = side == 'l' || side == 'L';
     lra_opts o = *opts;
     if (o.sketch == LRA_SKETCH_NONE) o.sketch = LRA_SKETCH_RANDN;
     dispatch(dtype, [&](auto z) {
@@ -1234,8 +1280,11 @@ int lra_sketchfact(lra_ctx* ctx, int dtype, char side, char trans, int64_t m, in
       DMat<T> dA = stage_in<T>(ctx, A, m, n, lda);
       check_input(ctx, o, m, n, dA);
       RandSrc rs(ctx, rand, o.seed);
-      const int64_t M = t == 'n' ? m : n, N = t == 'n' ? n : m;
-      Fact<T> F = sketchfact_dev<T>(ctx, o, t, M, N, dA.p, dA.ld, rs, dtype);
+      const int64_t Mo = t == 'n' ? m : n, No = t == 'n' ? n : m;
+      // left: the pivoted QR of S op(A) (columns of op(A)); right: of op(A) S
+      Fact<T> F = left ? sketchfact_dev<T>(ctx, o, t, Mo, No, dA.p, dA.ld, rs, dtype)
+                       : sketchfact_right_dev<T>(ctx, o, t, Mo, No, dA.p, dA.ld, rs, dtype);
+      const int64_t N = F.N;
       const bool rq = o.pqrfact_retval & LRA_RET_Q, rr = o.pqrfact_retval & LRA_RET_R,
                  rt = o.pqrfact_retval & LRA_RET_T;
       postproc_t<T>(ctx, o, F, rt);
@@ -1269,6 +1318,103 @@ int lra_sketchfact(lra_ctx* ctx, int dtype, char side, char trans, int64_t m, in
                                      cudaMemcpyDeviceToHost, ctx->stream));
         r->retval |= LRA_RET_Q;
       }
+      LRA_CUDA(cudaStreamSynchronize(ctx->stream));
+      *out = r;
+    });
+  });
+}
+
+int lra_prange(lra_ctx* ctx, int dtype, char trans, int64_t m, int64_t n, const void* A, int64_t lda,
+               const lra_opts* opts, const lra_rand* rand, lra_pqr** out) {
+  if (out) *out = nullptr;
+  return guarded(ctx, [&] {
+    chkopts(opts);
+    ctx->gemm_tc = use_tc_gemm(*opts, dtype);
+    ctx->mixed_rtol = ctx->gemm_tc ? opts->rtol : 0.0;
+    check_dims(m, n);
+    if (!out) fail(LRA_EINVAL, "out is NULL");
+    char t = (trans == 'b' || trans == 'B') ? 'b' : chktrans(trans);  // prange_chktrans, src/prange.jl:79-80
+    const lra_opts& o = *opts;
+    if (o.maxdet_tol >= 0) fail(LRA_ENOTSUP, "prange with maxdet_tol >= 0 is not built");
+    dispatch(dtype, [&](auto z) {
+      using T = decltype(z);
+      DMat<T> dA = stage_in<T>(ctx, A, m, n, lda);
+      check_input(ctx, o, m, n, dA);
+      RandSrc rs(ctx, rand, o.seed);
+      if (t == 'b') {
+        if (m != n) fail(LRA_EDIM, "prange(:b): the matrix must be square");
+        if (is_symmetric(ctx, n, dA.p, dA.ld)) t = 'n';  // src/prange.jl:24
+      }
+      // one side's factorization (src/prange.jl:26-31, 47-52): the pivoted QR
+      // of op(A) itself (sketch :none) or of the right sketch op(A) S; Q
+      // (M x k, ld M) replaces the reflectors, and R11 is kept on request
+      auto side_q = [&](char tr, int64_t& k, T** R11) -> T* {
+        const int64_t M = tr == 'n' ? m : n, N = tr == 'n' ? n : m;
+        Fact<T> F;
+        if (o.sketch == LRA_SKETCH_NONE) {
+          T* B = dense_op(ctx, tr, m, n, dA);
+          F = pqr_backend_dev<T>(ctx, o, B, M, N, M);
+        } else {
+          F = sketchfact_right_dev<T>(ctx, o, tr, M, N, dA.p, dA.ld, rs, dtype);
+        }
+        k = F.k;
+        const int64_t kk = std::max<int64_t>(k, 1);
+        if (R11) {
+          *R11 = ctx->arena.alloc_n<T>((size_t)kk * kk);
+          copy_matrix(ctx, k, k, F.B, F.ld, *R11, kk);
+          zero_lower(ctx, k, k, *R11, kk);
+        }
+        orgqr(ctx, M, k, F.B, F.ld, F.tau);
+        return F.B;
+      };
+      const int64_t M = t == 'c' ? n : m;
+      int64_t k = 0;
+      T* Q = nullptr;
+      if (t == 'b') {
+        // src/prange.jl:32-45: the row and column bases scaled by their
+        // R11, side by side, and the Q of their pivoted QR
+        int64_t kr = 0, kc = 0;
+        T *Rr = nullptr, *Rc = nullptr;
+        T* Qr = side_q('c', kr, &Rr);
+        T* Qc = side_q('n', kc, &Rc);
+        const int64_t kb = kr + kc;
+        T* Bc = ctx->arena.alloc_n<T>((size_t)std::max<int64_t>(M, 1) * std::max<int64_t>(kb, 1));
+        if (kr > 0) gemm<T>(ctx, 'n', 'n', M, kr, kr, T(1), Qr, M, Rr, kr, T(0), Bc, M);
+        if (kc > 0) gemm<T>(ctx, 'n', 'n', M, kc, kc, T(1), Qc, M, Rc, kc, T(0), Bc + kr * M, M);
+        Fact<T> F = pqr_backend_dev<T>(ctx, o, Bc, M, kb, M);
+        k = F.k;
+        orgqr(ctx, M, k, F.B, F.ld, F.tau);
+        Q = F.B;
+      } else if (o.sketch == LRA_SKETCH_SUB) {
+        // prange_sub (src/prange.jl:63-77): the skeleton columns of op(A)
+        // from the left sketch, made orthonormal (orthcols!, src/util.jl)
+        const int64_t N = t == 'n' ? n : m;
+        Fact<T> F = sketchfact_dev<T>(ctx, o, t, M, N, dA.p, dA.ld, rs, dtype);
+        const int64_t kc = F.k, kq = std::min(M, kc);
+        Q = getcols<T>(ctx, t, m, n, dA, F.jpvt, kc);
+        int64_t* jp = ctx->arena.alloc_n<int64_t>(std::max<int64_t>(kc, 1));
+        T* tau = ctx->arena.alloc_n<T>(std::max<int64_t>(kq, 1));
+        if (kq > 0) {
+          geqp3_adap<T>(ctx, M, kc, Q, std::max<int64_t>(M, 1), jp, tau, kq, 32, -1.0, 0.0, false);
+          orgqr(ctx, M, kq, Q, std::max<int64_t>(M, 1), tau);
+        }
+        k = kq;
+      } else {
+        Q = side_q(t, k, nullptr);
+      }
+      lra_pqr* r = static_cast<lra_pqr*>(hmalloc(sizeof(lra_pqr)));
+      std::memset(r, 0, sizeof *r);
+      r->dtype = dtype;
+      r->m = M;
+      r->n = k;
+      r->k = k;
+      r->p = static_cast<int64_t*>(hmalloc(sizeof(int64_t) * std::max<int64_t>(k, 1)));
+      for (int64_t i = 0; i < k; ++i) r->p[i] = i + 1;
+      r->Q = hmalloc(sizeof(T) * std::max<int64_t>(M * k, 1));
+      if (k > 0 && M > 0)
+        LRA_CUDA(cudaMemcpy2DAsync(r->Q, M * sizeof(T), Q, M * sizeof(T), M * sizeof(T), k, cudaMemcpyDeviceToHost,
+                                   ctx->stream));
+      r->retval = LRA_RET_Q;
       LRA_CUDA(cudaStreamSynchronize(ctx->stream));
       *out = r;
     });

@@ -142,6 +142,26 @@ function pqrfact(trans::Symbol, A::StridedMatrix{T}, opts::Union{LRAOptions,Noth
 end
 pqrfact(A::StridedMatrix, args...; kw...) = pqrfact(:n, A, args...; kw...)
 
+"prange(trans, A[, opts]) -- src/prange.jl:14-61 on the GPU: an orthonormal basis of the range (:n, :c, :b)."
+function prange(trans::Symbol, A::StridedMatrix{T}, opts::Union{LRAOptions,Nothing}=nothing;
+                precision::Symbol=:native, kw...) where T<:Union{Float32,Float64}
+  trans in (:n, :c, :b) || throw(ArgumentError("trans"))
+  o = opts_of(T, opts, kw); c = ctx(); out = Ref{Ptr{lra_pqr}}(C_NULL)
+  co = Ref(c_opts(o; precision))
+  st = ccall((:lra_prange, liblra), Cint,
+             (Ptr{Cvoid}, Cint, Cchar, Int64, Int64, Ptr{T}, Int64, Ref{lra_opts}, Ptr{lra_rand}, Ref{Ptr{lra_pqr}}),
+             c.h, dtype(T), trans == :n ? 'n' : (trans == :c ? 'c' : 'b'), size(A,1), size(A,2), A, stride(A,2), co,
+             C_NULL, out)
+  check(st, c)
+  r = unsafe_load(out[])
+  try
+    takem(r.Q, T, r.m, r.k)
+  finally
+    ccall((:lra_pqr_free, liblra), Cvoid, (Ptr{lra_pqr},), out[])
+  end
+end
+prange(A::StridedMatrix, args...; kw...) = prange(:n, A, args...; kw...)
+
 function _psvd(A::StridedMatrix{T}, opts, vals::Bool; precision::Symbol=:native, kw...) where T
   o = opts_of(T, opts, kw); c = ctx(); out = Ref{Ptr{lra_psvd}}(C_NULL)
   co = Ref(c_opts(o; precision))

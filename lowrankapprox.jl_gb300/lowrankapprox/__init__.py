@@ -24,7 +24,7 @@ from ._ffi import LRA_F32, LRA_F64
 __all__ = [
     "LRAOptions", "RandStream", "Context", "IDPackedV", "PartialQRFactors", "PartialQR", "PartialSVD",
     "PartialHermitianEigen", "CURPackedU", "idfact", "id", "pqrfact", "pqr", "psvdfact", "psvdvals",
-    "psvd", "pheigfact", "pheigvals", "pheig", "curfact", "cur", "sketch", "sketchfact", "snorm",
+    "psvd", "pheigfact", "pheigvals", "pheig", "curfact", "cur", "sketch", "sketchfact", "prange", "snorm",
     "snormdiff", "geqp3_adap", "matrixlib", "LRAError", "ArgumentError", "DimensionMismatch",
     "lattice_gauss", "default_context", "Server", "idfact_batched",
 ]
@@ -531,6 +531,31 @@ def sketchfact(*args, **kwargs):
                             C.c_void_p(M.ptr), M.ld, C.byref(co), _rand(rand), C.byref(out))
     _raise(st, ctx)
     return _pqr_out(lib, out, M.np_dtype, True)
+
+
+def prange(*args, **kwargs) -> np.ndarray:
+    """prange([trans,] A[, opts]) (src/prange.jl:14-61): an orthonormal basis
+    (m' x k) of the range of op(A); trans "b" takes the ranges of A and A'
+    together (A square)."""
+    args = list(args)
+    trans = "n"
+    if args and isinstance(args[0], str):
+        trans = args.pop(0)
+    if trans not in ("n", "c", "t", "b"):
+        raise ArgumentError(_ffi.LRA_EINVAL, "trans")  # prange_chktrans, src/prange.jl:79-80
+    A = args.pop(0)
+    opts = args.pop(0) if args else None
+    ctx = kwargs.pop("ctx", None) or default_context()
+    rand = kwargs.pop("rand", None)
+    M = _mat(A)
+    opts = (opts or LRAOptions(M.np_dtype)).copy(**kwargs)
+    lib = _ffi.load()
+    out = C.POINTER(_ffi.lra_pqr)()
+    co = opts.to_c()
+    st = lib.lra_prange(ctx.handle, M.dtype, trans.encode(), M.m, M.n, C.c_void_p(M.ptr), M.ld, C.byref(co),
+                        _rand(rand), C.byref(out))
+    _raise(st, ctx)
+    return _pqr_out(lib, out, M.np_dtype, False).Q
 
 
 def sketch(*args, **kwargs):

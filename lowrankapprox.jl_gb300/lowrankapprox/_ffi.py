@@ -119,6 +119,7 @@ SIGNATURES = [
                           _P(lra_rand), _vp, _i64]),
     ("lra_sketchfact", _i32, [_vp, _i32, _ch, _ch, _i64, _i64, _vp, _i64, _P(lra_opts),
                               _P(lra_rand), _P(_P(lra_pqr))]),
+    ("lra_prange", _i32, [_vp, _i32, _ch, _i64, _i64, _vp, _i64, _P(lra_opts), _P(lra_rand), _P(_P(lra_pqr))]),
     ("lra_geqp3_adap", _i32, [_vp, _i32, _i64, _i64, _vp, _i64, _vp, _vp, _P(lra_opts), _P(_i64)]),
     ("lra_geqp3_adap_noalloc", _i32, [_vp, _i32, _i64, _i64, _vp, _i64, _vp, _vp, _P(lra_opts), _P(_i64)]),
     ("lra_idfact", _i32, [_vp, _i32, _ch, _i64, _i64, _vp, _i64, _P(lra_opts), _P(lra_rand),

@@ -599,6 +599,37 @@ def sketchfact(side, trans, A, opts: Opts, rs: RandStream, backend="oracle", fas
 # factorizations
 # --------------------------------------------------------------------------
 
+def prange(trans, A, opts: Opts, rs: RandStream, backend="oracle") -> np.ndarray:
+    """prange (src/prange.jl:14-77): an orthonormal basis of the range of
+    op(A), or of A and A' together for trans "b"."""
+    opts = opts.for_dtype(A.dtype)
+    if trans == "b":
+        m, n = A.shape
+        if m != n:
+            raise ValueError("prange(:b) needs a square matrix")
+        if _ishermitian(A):
+            return prange("n", A, opts, rs, backend)
+        oq = replace(opts, pqrfact_retval="qr")
+        if opts.sketch == "none":
+            Fr = pqrfact("c", A, oq, rs, backend)
+            Fc = pqrfact("n", A, oq, rs, backend)
+        else:
+            Fr = sketchfact("right", "c", A, oq, rs, backend)
+            Fc = sketchfact("right", "n", A, oq, rs, backend)
+        kr, kc = Fr["k"], Fc["k"]
+        B = np.concatenate([Fr["Q"] @ np.triu(Fr["R"][:kr, :kr]), Fc["Q"] @ np.triu(Fc["R"][:kc, :kc])], axis=1)
+        return pqrfact_backend(np.asfortranarray(B.astype(A.dtype)), replace(opts, pqrfact_retval="q"), backend)["Q"]
+    oq = replace(opts, pqrfact_retval="q")
+    if opts.sketch == "none":
+        return pqrfact(trans, A, oq, rs, backend)["Q"]
+    if opts.sketch == "sub":
+        F = sketchfact("left", trans, A, opts, rs, backend)
+        k = F["k"]
+        B = np.asfortranarray(_op(A, trans)[:, np.asarray(F["p"][:k]) - 1])
+        return orthcols(B)[:, :min(B.shape)]
+    return sketchfact("right", trans, A, oq, rs, backend)["Q"]
+
+
 def _getcols(trans, A, cols):
     """getcols (src/util.jl:25-29), cols 1-based."""
     c = np.asarray(cols, np.int64) - 1

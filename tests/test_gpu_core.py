@@ -99,6 +99,57 @@ def test_idfact_parity(lra, oracle, sketch, dt, trans):
 
 
 @pytest.mark.parametrize("sketch", ["randn", "sub", "srft", "sprn"])
+@pytest.mark.parametrize("side", ["left", "right"])
+@pytest.mark.parametrize("trans", ["n", "c"])
+def test_sketchfact_parity(lra, oracle, sketch, side, trans):
+    """sketchfact on both sides (src/sketch.jl:52-63): rank, pivots up to the
+    noise floor, and the factors of the sketch (Q orthonormal, Q R = B P)."""
+    A = real_fourier(128, 64)
+    rtol = 5 * np.finfo(np.float64).eps
+    ors, grs = both_rs(oracle, lra, 17)
+    ref = oracle.sketchfact(side, trans, A, oracle.Opts(rtol=rtol, sketch=sketch, pqrfact_retval="qr"), ors)
+    F = lra.sketchfact(side, trans, A, lra.LRAOptions(np.float64, rtol=rtol, sketch=sketch, pqrfact_retval="qr"),
+                       rand=grs)
+    assert abs(F.k - ref["k"]) <= 1
+    k = F.k
+    Aop = A if trans == "n" else A.T
+    assert F.Q.shape[1] == k and (side == "left" or F.Q.shape[0] == Aop.shape[0])
+    assert np.abs(F.Q.T @ F.Q - np.eye(k)).max() < 1e-12
+    if F.k == ref["k"]:
+        head = max(0, k - 2)
+        assert np.array_equal(np.asarray(F.p)[:head], np.asarray(ref["p"])[:head])
+    if side == "right":
+        # the basis spans op(A)'s range up to the tolerance
+        E = Aop - F.Q @ (F.Q.T @ Aop)
+        assert np.linalg.norm(E) <= 100 * rtol * np.linalg.norm(Aop) * max(1, k)
+
+
+@pytest.mark.parametrize("sketch", SKETCHES)
+@pytest.mark.parametrize("dt", [np.float32, np.float64])
+@pytest.mark.parametrize("trans", ["n", "c", "b"])
+def test_prange_parity(lra, oracle, sketch, dt, trans):
+    """prange (src/prange.jl:14-77) against the oracle on the same streams:
+    the reference test's criteria (test/prange.jl:20-29), an orthonormal
+    basis, and the oracle's rank within one."""
+    A = real_fourier(128, 128, 6).astype(dt)
+    rtol = 5 * np.finfo(dt).eps
+    ors, grs = both_rs(oracle, lra, 23)
+    Qr = oracle.prange(trans, A, oracle.Opts(rtol=rtol, sketch=sketch), ors)
+    Q = lra.prange(trans, A, lra.LRAOptions(dt, rtol=rtol, sketch=sketch), rand=grs)
+    nrm = np.linalg.norm(A)
+    Q64 = Q.astype(np.float64)
+    if trans == "n":
+        err = np.linalg.norm(A - Q64 @ (Q64.T @ A))
+    elif trans == "c":
+        err = np.linalg.norm(A - (A @ Q64) @ Q64.T)
+    else:
+        err = np.linalg.norm(A - Q64 @ (Q64.T @ A @ Q64) @ Q64.T)
+    assert err < 100 * rtol * nrm
+    assert np.abs(Q64.T @ Q64 - np.eye(Q.shape[1])).max() < 100 * rtol * max(1, Q.shape[1])
+    assert abs(Q.shape[1] - Qr.shape[1]) <= 1
+
+
+@pytest.mark.parametrize("sketch", ["randn", "sub", "srft", "sprn"])
 @pytest.mark.parametrize("dt", [np.float32, np.float64])
 def test_sketch_values(lra, oracle, sketch, dt):
     rng = np.random.default_rng(4)

@@ -164,6 +164,22 @@ def test_reference_criteria_psvd_pheig_cur(oracle, sketch):
     assert len(U["rows"]) == len(U["cols"]) > 0
 
 
+@pytest.mark.parametrize("sketch", SKETCHES)
+@pytest.mark.parametrize("dt", [np.float32, np.float64])
+def test_reference_criteria_prange(oracle, sketch, dt):
+    # test/prange.jl:20-29 (maxdet off here: the build's prange refuses it)
+    A = real_fourier(128, 128, 6).astype(dt)
+    rtol = 5 * np.finfo(dt).eps
+    opts = oracle.Opts(rtol=rtol, sketch=sketch)
+    nrm = np.linalg.norm(A)
+    Q = oracle.prange("n", A, opts, rs_for(oracle, sketch, 128, 7))
+    assert np.linalg.norm(A - Q @ (Q.T @ A)) < 100 * rtol * nrm
+    Q = oracle.prange("c", A, opts, rs_for(oracle, sketch, 128, 8))
+    assert np.linalg.norm(A - (A @ Q) @ Q.T) < 100 * rtol * nrm
+    Q = oracle.prange("b", A, opts, rs_for(oracle, sketch, 128, 9))
+    assert np.linalg.norm(A - Q @ (Q.T @ A @ Q) @ Q.T) < 100 * rtol * nrm
+
+
 def test_snorm_criteria(oracle):
     rng = np.random.default_rng(7)
     A = rng.random((20, 10))
