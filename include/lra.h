@@ -293,6 +293,17 @@ int lra_curfact(lra_ctx* ctx, int dtype, int64_t m, int64_t n, const void* A,
                 int64_t lda, const lra_opts* opts, const lra_rand* rand,
                 lra_cur** out);
 
+/* the middle factor of CUR(A, U) (src/cur.jl:85-93, 100-115): the
+   pseudo-inverse of A[rows, cols] (k x k, rows and cols 1-based host arrays
+   of k entries each) as a PartialSVD (V, 1 ./ S, U'), with W = A[rows, cols]
+   = U diag(S) V' computed on the device.  C = A[:, cols] and R = A[rows, :]
+   are plain gathers the caller makes (the reference indexes A for them).
+   For HermitianCURPackedU / SymmetricCURPackedU pass cols as rows too; the
+   factor is the same pseudo-inverse, held as a PartialSVD.                  */
+int lra_cur_middle(lra_ctx* ctx, int dtype, int64_t m, int64_t n,
+                   const void* A, int64_t lda, int64_t k, const int64_t* rows,
+                   const int64_t* cols, lra_psvd** out);
+
 /* ---- spectral norms (src/snorm.jl) ------------------------------------------ */
 
 /* snorm(A) (src/snorm.jl:14-45) */

