@@ -224,6 +224,27 @@ function curfact(A::StridedMatrix{T}, opts::Union{LRAOptions,Nothing}=nothing; p
   end
 end
 
+"""CUR(A, U) -- src/cur.jl:85-115: C = A[:, cols], R = A[rows, :] and the
+pseudo-inverse of A[rows, cols] computed on the GPU (lra_cur_middle).  The
+reference's own CUR / HermitianCUR types are built from the three parts."""
+function CUR(A::StridedMatrix{T}, U::Union{CURPackedU,HermitianCURPackedU}) where T<:Union{Float32,Float64}
+  rows = Int64.(U[:rows]); cols = Int64.(U[:cols])
+  length(rows) == length(cols) || throw(DimensionMismatch("rows and cols differ in length"))
+  c = ctx(); out = Ref{Ptr{lra_psvd}}(C_NULL); k = length(cols)
+  st = ccall((:lra_cur_middle, liblra), Cint,
+             (Ptr{Cvoid}, Cint, Int64, Int64, Ptr{T}, Int64, Int64, Ptr{Int64}, Ptr{Int64}, Ref{Ptr{lra_psvd}}),
+             c.h, dtype(T), size(A,1), size(A,2), A, stride(A,2), k, rows, cols, out)
+  check(st, c)
+  p = unsafe_load(out[])
+  try
+    W = PartialSVD(takem(p.U, T, p.m, p.k), take(Ptr{T}(p.S), p.k), takem(p.Vt, T, p.k, p.n))
+    U isa HermitianCURPackedU ? LowRankApprox.HermitianCUR(cols, A[:, cols], W) :
+                                LowRankApprox.CUR(rows, cols, A[:, cols], W, A[rows, :])
+  finally
+    ccall((:lra_psvd_free, liblra), Cvoid, (Ptr{lra_psvd},), out[])
+  end
+end
+
 "snorm(A[, opts]) -- src/snorm.jl:14-45 on the GPU."
 function snorm(A::StridedMatrix{T}, opts::Union{LRAOptions,Nothing}=nothing; kw...) where T<:Union{Float32,Float64}
   o = opts_of(T, opts, kw); c = ctx(); s = Ref{Float64}(0)
