@@ -799,12 +799,12 @@ def CUR(A, U: CURPackedU, ctx: "Context | None" = None) -> CURFactor:
     """CUR(A, U::CURPackedU) (src/cur.jl:85-115): C = A[:, cols],
     R = A[rows, :] (A[cols, :] for the Hermitian and symmetric forms) and the
     middle factor computed on the device."""
-    ctx = ctx or default_context()
-    M = _mat(A)
     rows = np.ascontiguousarray(np.asarray(U.cols if U.kind else U.rows, np.int64))
     cols = np.ascontiguousarray(np.asarray(U.cols, np.int64))
     if len(rows) != len(cols):
         raise DimensionMismatch(_ffi.LRA_EDIM, "rows and cols differ in length")
+    ctx = ctx or default_context()
+    M = _mat(A)
     k = len(cols)
     lib = _ffi.load()
     out = C.POINTER(_ffi.lra_psvd)()

@@ -98,3 +98,14 @@ def test_python_options_mirror():
     assert o2.rtol == 1e-3 and o.rtol != 1e-3
     with pytest.raises(ValueError):
         L.LRAOptions(bogus=1)
+
+
+def test_python_argument_checks_before_the_device():
+    # prange_chktrans (src/prange.jl:79-80) and CUR's row / column count are
+    # checked on the host, before any context or device work
+    import lowrankapprox as L
+    A = np.zeros((4, 4))
+    with pytest.raises(L.ArgumentError):
+        L.prange("x", A)
+    with pytest.raises(L.DimensionMismatch):
+        L.CUR(A, L.CURPackedU(np.array([1, 2]), np.array([1])))
