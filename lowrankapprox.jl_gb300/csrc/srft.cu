@@ -13,9 +13,12 @@
 // into chunks of PC complex columns (two real columns kk = 2p, 2p + 1 packed
 // into one complex sequence, so one l-point FFT serves both).  The l-point
 // FFTs are mixed-radix decimation in frequency (radix 2..16 in registers,
-// one to three passes), in place in shared memory (rows padded by one
-// element), so each pass needs one barrier and a thread keeps one group of
-// R values at a time; the first pass takes its inputs straight from HBM
+// one to three passes), in place in shared memory, so each pass needs one
+// barrier and a thread keeps one group of R values at a time.  Two forms:
+// 256 threads with rows padded by one element (any chunk width), and, for
+// Float32 with l = 128 .. 1024, 512 threads with 8192-value chunks whose
+// unpadded rows are swizzled so that the passes are free of bank conflicts
+// (SkCfg below).  The first pass takes its inputs straight from HBM
 // with coalesced 8- or 16-byte loads (lanes along p) and the signs d = +-1
 // as bits.  The output rows are in digit-reversed order, which the sampled
 // sums read through a per-frequency index.  The sums unpack the two real
