@@ -197,6 +197,23 @@ def test_reference_criteria_cur_build(oracle, sketch):
         assert np.linalg.norm(A - F["C"] @ ((V * s) @ Ut) @ F["R"]) < 1000 * rtol * np.linalg.norm(A)
 
 
+@pytest.mark.parametrize("sketch", SKETCHES)
+@pytest.mark.parametrize("dt", [np.float32, np.float64])
+def test_reference_criteria_pqr(oracle, sketch, dt):
+    # test/pqr.jl:8-30, with its options (maxdet_tol = 0, one power iteration)
+    A = real_fourier(128, 64, 12).astype(dt)
+    rtol = 5 * np.finfo(dt).eps
+    opts = oracle.Opts(rtol=rtol, sketch=sketch, maxdet_tol=0.0, sketch_randn_niter=1)
+    nrm = np.linalg.norm(A)
+    for i, trans in enumerate(("n", "c")):
+        F = oracle.pqrfact(trans, A, opts, rs_for(oracle, sketch, 128, 13 + i))
+        Aop = A if trans == "n" else A.T
+        P = np.empty_like(F["p"])
+        P[F["p"] - 1] = np.arange(len(F["p"]))
+        E = F["Q"].astype(np.float64) @ F["R"].astype(np.float64)[:, P]
+        assert np.linalg.norm(Aop - E) < 100 * rtol * nrm
+
+
 def test_snorm_criteria(oracle):
     rng = np.random.default_rng(7)
     A = rng.random((20, 10))
