@@ -143,17 +143,23 @@ def rs_for(oracle, sketch, M, seed):
 def test_reference_criteria_id(oracle, sketch, dt):
     A = real_fourier(128, 64).astype(dt)
     rtol = 5 * np.finfo(dt).eps
-    opts = oracle.Opts(rtol=rtol, sketch=sketch)
-    V = oracle.idfact("n", A, opts, rs_for(oracle, sketch, 128, 1))
-    E = oracle.id_matrix("n", A, V)
-    assert np.linalg.norm(A - E) < 100 * rtol * np.linalg.norm(A)     # test/id.jl:31
+    # the defaults, and the reference test's options (test/id.jl:8: maxdet_tol
+    # = 0, one power iteration)
+    for extra in ({}, {"maxdet_tol": 0.0, "sketch_randn_niter": 1}):
+        opts = oracle.Opts(rtol=rtol, sketch=sketch, **extra)
+        V = oracle.idfact("n", A, opts, rs_for(oracle, sketch, 128, 1))
+        E = oracle.id_matrix("n", A, V)
+        assert np.linalg.norm(A - E) < 100 * rtol * np.linalg.norm(A)     # test/id.jl:31
 
 
 @pytest.mark.parametrize("sketch", SKETCHES)
-def test_reference_criteria_psvd_pheig_cur(oracle, sketch):
+@pytest.mark.parametrize("ref_opts", [False, True])
+def test_reference_criteria_psvd_pheig_cur(oracle, sketch, ref_opts):
     A = real_fourier(128, 64)
     rtol = 5 * np.finfo(np.float64).eps
-    opts = oracle.Opts(rtol=rtol, sketch=sketch)
+    # ref_opts: the reference tests' options (test/psvd.jl:10, test/pheig.jl:8)
+    extra = {"maxdet_tol": 0.0, "sketch_randn_niter": 1} if ref_opts else {}
+    opts = oracle.Opts(rtol=rtol, sketch=sketch, **extra)
     F = oracle.psvdfact(A, opts, rs_for(oracle, sketch, 128, 2))
     assert np.linalg.norm(A - (F["U"] * F["S"]) @ F["Vt"]) < 100 * rtol * np.linalg.norm(A)
     H = real_fourier(128, 128, 4)
