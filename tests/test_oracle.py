@@ -220,6 +220,19 @@ def test_reference_criteria_pqr(oracle, sketch, dt):
         assert np.linalg.norm(Aop - E) < 100 * rtol * nrm
 
 
+@pytest.mark.parametrize("sketch", ["randn", "sub", "srft", "sprn"])
+@pytest.mark.parametrize("dt", [np.float32, np.float64])
+def test_reference_sketch_shapes(oracle, sketch, dt):
+    # test/sketch.jl:9-31: shapes of the four sides / transposes, niter = 1
+    A = np.asfortranarray(np.random.default_rng(14).random((20, 10)).astype(dt))
+    opts = oracle.Opts(sketch=sketch, sketch_randn_niter=1)
+    rs = rs_for(oracle, sketch, 20, 15)
+    assert oracle.sketch("left", "n", A, 5, opts, rs).shape == (5, 10)
+    assert oracle.sketch("left", "c", A, 5, opts, rs).shape == (5, 20)
+    assert oracle.sketch("right", "n", A, 5, opts, rs).shape == (20, 5)
+    assert oracle.sketch("right", "c", A, 5, opts, rs).shape == (10, 5)
+
+
 def test_snorm_criteria(oracle):
     rng = np.random.default_rng(7)
     A = rng.random((20, 10))
