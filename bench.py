@@ -56,16 +56,17 @@ def parse():
     return ap.parse_args()
 
 
-def make_matrix(n: int, rank_cols: int = 1024):
-    """A = U diag(s) V' built on the GPU from seeded numpy Gaussians."""
+def make_matrix(n: int, rank_cols: int = 1024, device: str = "cuda"):
+    """A = U diag(s) V' built on the device (the GPU unless told otherwise)
+    from seeded numpy Gaussians."""
     import torch
     r = min(n, rank_cols)
     facs = []
     for seed in (1, 2):
         Q, R = np.linalg.qr(np.random.default_rng(seed).standard_normal((n, r)))
-        facs.append(torch.from_numpy(Q * np.sign(np.diag(R))[None, :]).cuda())
+        facs.append(torch.from_numpy(Q * np.sign(np.diag(R))[None, :]).to(device))
     U, V = facs
-    s = torch.pow(10.0, -torch.arange(r, dtype=torch.float64, device="cuda") / 40.0)
+    s = torch.pow(10.0, -torch.arange(r, dtype=torch.float64, device=device) / 40.0)
     A = (U * s[None, :]) @ V.T
     del U, V, facs
     # column-major storage
@@ -346,7 +347,8 @@ def run_reference(args):
     threads = os.cpu_count() or 1
     os.environ.setdefault("OPENBLAS_NUM_THREADS", str(threads))
     import torch
-    A = make_matrix(args.n).cpu().numpy()
+    # the same matrix as the GPU arm's; built on the host when no GPU is there
+    A = make_matrix(args.n, device="cuda" if torch.cuda.is_available() else "cpu").cpu().numpy()
     A = np.asfortranarray(A)
     times = []
     k = 0
