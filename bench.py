@@ -47,9 +47,9 @@ def parse():
     ap.add_argument("--serve-requests", type=int, default=64,
                     help="requests per precision in the serving measurement (0: skip)")
     ap.add_argument("--batch", type=int, default=2048,
-                    help="kernel matrices in the batched measurement (0: skip); the FP64 path runs on the first "
-                         "--batch-native of them")
-    ap.add_argument("--batch-native", type=int, default=256)
+                    help="kernel matrices in the batched measurement (0: skip)")
+    ap.add_argument("--batch-native", type=int, default=0,
+                    help="run the FP64 path on the first N of them only (0: the whole batch)")
     ap.add_argument("--no-tall", action="store_true", help="skip the tall Float32 idfact measurement")
     ap.add_argument("--srft-sweep", action="store_true",
                     help="only the SRFT sketch sweep on a Gaussian 65536x4096 Float32 matrix (one JSON line)")
@@ -328,16 +328,56 @@ class Clocks:
                 "samples": len(sm)}
 
 
-def cpu_reference_step(A_host, rtol, seed, threads):
+def lattice_stream(seed, n):
+    """N(0,1) draws on the 1/32 lattice (the values the mixed path multiplies
+    exactly), shared by the oracle and the GPU."""
+    rng = np.random.default_rng(seed)
+    return np.clip(np.rint(rng.standard_normal(n) * 32), -127, 127) / 32.0
+
+
+def cpu_reference_step(A_host, rtol, seed, threads, keep=False):
     """The oracle's psvdfact on the host cores (numpy/OpenBLAS + C xLAQPS)."""
     from oracle import oracle as O
-    rng = np.random.default_rng(seed)
     m, n = A_host.shape
-    g = np.clip(np.rint(rng.standard_normal(2200 * m) * 32), -127, 127) / 32.0
+    g = lattice_stream(seed, 2200 * m)
     backend = "lapack" if O.lapack_available() else "c"
     t0 = time.perf_counter()
     F = O.psvdfact(A_host, O.Opts(rtol=rtol), O.RandStream(gauss=g), backend=backend)
-    return time.perf_counter() - t0, F["k"], backend
+    dt = time.perf_counter() - t0
+    if keep:
+        return dt, F["k"], backend, F, g
+    return dt, F["k"], backend
+
+
+def rel_err_psvd(A, U, S, Vt, x0, iters=32):
+    """||A - U diag(S) Vt||_2 / ||A||_2 by power iteration (float64 torch on
+    A's device), the same start vector for every result compared."""
+    import torch
+    dev = A.device
+    Ut, St, Vtt = (torch.as_tensor(np.asarray(X, np.float64), device=dev) for X in (U, S, Vt))
+
+    def snorm(apply, applyc):
+        x = torch.as_tensor(x0, dtype=torch.float64, device=dev)
+        s = 0.0
+        for _ in range(iters):
+            x = applyc(apply(x / torch.linalg.vector_norm(x)))
+            s = float(torch.linalg.vector_norm(x)) ** 0.5
+        return s
+    e = snorm(lambda x: A @ x - Ut @ (St * (Vtt @ x)), lambda y: A.T @ y - Vtt.T @ (St * (Ut.T @ y)))
+    return e / snorm(lambda x: A @ x, lambda y: A.T @ y)
+
+
+def replica_rate(elapsed: float, steps: int, world: int) -> tuple[float, float]:
+    """Whole-job rate of `world` replicas that each ran `steps` steps: the
+    slowest rank's time (a MAX all-reduce over the process group when
+    world > 1) and world * steps / that time."""
+    if world > 1:
+        import torch
+        import torch.distributed as dist
+        t = torch.tensor([elapsed], dtype=torch.float64)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        elapsed = float(t[0])
+    return elapsed, world * steps / elapsed
 
 
 def run_reference(args):
@@ -427,11 +467,7 @@ def main():
     barrier()
     clk = clocks.stop()
     launches = ctx.launches - l0
-    if world > 1:
-        t = torch.tensor([elapsed], dtype=torch.float64)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        elapsed = float(t[0])
-    value = world * args.steps / elapsed
+    elapsed, value = replica_rate(elapsed, args.steps, world)
 
     # ---- end to end from pinned host memory ------------------------------------
     Ah = torch.empty((n, n), dtype=torch.float64, pin_memory=True)
@@ -493,17 +529,18 @@ def main():
     qr_ms = st["qr"] / nl
     pivots = sum(min(l, kq + 32) if i == nl - 1 else l for i, (l, kq) in enumerate(zip(orders, ks)))
     qr_gbs = qr_bytes / (qr_ms * 1e-3) / 1e9
-    # DRAM traffic of one launch from the committed ncu capture of the 520-row
-    # launch (profiles/geqp3_df_smem_kernel_sketch520x8192.md: 34.25 MB read +
-    # 0.16 MB written, the sketch read once), scaled to the average launch by
-    # its sketch size
+    # DRAM traffic per launch: one ncu capture of the 520-row launch of this
+    # workload read 34.25 MB and wrote 0.16 MB (the sketch read once); the
+    # figure is scaled to the average launch by its sketch size, not
+    # measured in this run
     qr_traffic = (34.25e6 + 0.16e6) * (sum(orders) / nl) / 520.0
     roof = {"kernel": "geqp3_df_smem_kernel (pivoted QR of the sketch)", "bound": "hbm", "achieved": qr_gbs,
             "peak": hbm, "unit": "GB/s", "frac": qr_gbs / hbm, "traffic": qr_traffic,
+            "traffic_source": "scaled by sketch size from one ncu capture of the 520-row launch (34.4 MB)",
             "peak_source": f"{src} hbm_gbs, burst",
             "bytes_per_launch": qr_bytes, "ms_per_launch": qr_ms,
             "note": f"latency-bound: {1e3 * st['qr'] / pivots:.1f} us per pivot over {pivots} pivots, "
-                    "one exchange between the CTAs each; traffic from ncu is in profiles/"}
+                    "one exchange between the CTAs each"}
     # the sketch: six BF16 digit planes of A against the lattice Gaussian
     sk_flops = sum(2.0 * 6 * (-(-l // 96) * 96) * n * n for l in orders) / nl
     sk_ms = st["sketch"] / nl
@@ -516,17 +553,34 @@ def main():
     roof["stage_ms"] = st
 
     # ---- CPU baseline (oracle on the host cores, one bounded sample) -------------------
-    cpu = None
+    cpu, parity = None, None
     if rank == 0 and not args.no_cpu_baseline:
         try:
             Ac = np.asfortranarray(A.cpu().numpy())
-            dt, kc, backend = cpu_reference_step(Ac, args.rtol, 5, os.cpu_count())
+            dt, kc, backend, Fo, gs = cpu_reference_step(Ac, args.rtol, 5, os.cpu_count(), keep=True)
             cpu = {"value": 1.0 / dt, "unit": "matrices/s", "cores": os.cpu_count(), "kind": "port",
                    "sample": f"one full {n}^2 psvdfact (oracle: numpy/OpenBLAS BLAS-3 + xLAQPS {backend}), "
                              f"rank {kc}"}
+            # parity on the same sketch: the GPU path fed the oracle's stream
+            Fs = lra.psvdfact(A, opts, rand=lra.RandStream(gauss=gs), ctx=ctx)
+            Vs = lra.idfact(A, opts, rand=lra.RandStream(gauss=gs), ctx=ctx)
+            sk_ref = np.asarray(Fo["sk"])
+            kk = min(len(sk_ref), Vs.k)
+            agree = int(np.argmax(np.asarray(Vs.sk[:kk]) != sk_ref[:kk])) if not np.array_equal(
+                Vs.sk[:kk], sk_ref[:kk]) else kk
+            x0 = np.random.default_rng(7).standard_normal(n)
+            e_gpu = rel_err_psvd(A, Fs.U, Fs.S, Fs.Vt, x0)
+            e_ref = rel_err_psvd(A, Fo["U"], Fo["S"], Fo["Vt"], x0)
+            parity = {"stream": "lattice N(0,1) seed 5, injected into both", "rank": Fs.k, "oracle_rank": Fo["k"],
+                      "id_rank": Vs.k, "oracle_id_rank": Fo["id_k"], "skeleton_prefix_equal": agree,
+                      "rel_spectral_err": e_gpu, "oracle_rel_spectral_err": e_ref, "err_ratio": e_gpu / e_ref,
+                      "max_rel_sv_diff": float(np.abs(np.asarray(Fs.S[:min(Fs.k, Fo["k"])]) -
+                                                      np.asarray(Fo["S"][:min(Fs.k, Fo["k"])])).max() /
+                                               Fo["S"][0])}
         except Exception as e:  # pragma: no cover
-            cpu = {"value": None, "unit": "matrices/s", "cores": os.cpu_count(), "kind": "port",
-                   "sample": f"failed: {e}"}
+            cpu = cpu or {"value": None, "unit": "matrices/s", "cores": os.cpu_count(), "kind": "port",
+                          "sample": f"failed: {e}"}
+            parity = {"failed": str(e)}
 
     # ---- serving loop and batched idfact (bounded samples of those configs) ------------
     serving, batched = None, None
@@ -544,12 +598,12 @@ def main():
     if rank == 0 and args.batch > 0:
         try:
             mats = kernel_matrices(args.batch)
-            nn = max(1, min(args.batch_native, len(mats)))
+            nn = len(mats) if args.batch_native <= 0 else max(1, min(args.batch_native, len(mats)))
             batched = {"mixed": measure_batched(lra, mats, "mixed", ctx),
                        "native": measure_batched(lra, mats[:nn], "native", ctx),
                        "sample": f"{args.batch} kernel matrices 1/(1+|x-y|^2), m, n ~ U{{128..2048}}, F64, "
-                                 f"rtol 1e-10, lra_idfact_batched; the FP64 path on the first {nn} (a "
-                                 "per-matrix path: its rate does not depend on the batch size)"}
+                                 f"rtol 1e-10, lra_idfact_batched; the FP64 path on "
+                                 + ("the same batch" if nn == len(mats) else f"the first {nn}")}
             batched["mixed_vs_native"] = batched["mixed"]["matrices_s"] / batched["native"]["matrices_s"]
             del mats
         except Exception as e:  # pragma: no cover
@@ -580,7 +634,8 @@ def main():
             "e2e": {"value": e2e_val, "unit": "matrices/s", "h2d_bytes_per_step": h2d,
                     "d2h_bytes_per_step": d2h},
             "fp64_path": fp64, "serving": serving, "batched": batched, "tall_f32": tall,
-            "roofline": roof, "roofline_sketch": roof_sketch, "cpu_baseline": cpu, "clocks": clk, "gpu_launches": launches,
+            "roofline": roof, "roofline_sketch": roof_sketch, "cpu_baseline": cpu, "oracle_parity": parity,
+            "clocks": clk, "gpu_launches": launches,
         }
         print(json.dumps(line), flush=True)
     if world > 1:

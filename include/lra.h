@@ -48,7 +48,10 @@ typedef enum lra_status {
   LRA_EBUSY = 10       /* server queue full / over HBM budget             */
 } lra_status;
 
-typedef enum lra_dtype { LRA_F32 = 0, LRA_F64 = 1 } lra_dtype;
+/* element types: Float32, Float64, ComplexF32, ComplexF64 (complex arrays
+   hold (re, im) pairs, Julia's Complex{T} layout; complex types run on the
+   native path whatever opts->precision says) */
+typedef enum lra_dtype { LRA_F32 = 0, LRA_F64 = 1, LRA_C32 = 2, LRA_C64 = 3 } lra_dtype;
 
 /* src/LowRankApprox.jl:138 -- the valid sketch symbols */
 typedef enum lra_sketch_kind {
@@ -194,6 +197,33 @@ int64_t lra_ctx_launches(const lra_ctx* ctx);
 /* device time of the last call's stages, ms: sketch, qr, solve, post */
 int lra_ctx_stage_ms(const lra_ctx* ctx, double out[4]);
 
+/* The shapes this engine's autotuner picks (the tcgen05 sketch tile N per
+   element type and sketch order, the pivoted QR's row count for a thread
+   per column, the SRFT kernel form per l'), read when a context is created
+   from the table LRA_TUNING names or the one beside liblra.so
+   (tuning_gb300.txt, written by lowrankapprox/autotune.py).  set overrides
+   one entry of this context (keys "tc_tile_n" with index dtype * 16 +
+   ceil(log2 order), "qr_seq_len", "srft_wide" with index log2 l');
+   get writes the table in force and its source as text and returns the
+   length it needs (with the terminating zero).  No counterpart in the
+   reference, whose BLAS picks its own blocking.                           */
+int lra_ctx_set_tuning(lra_ctx* ctx, const char* key, int64_t index, int64_t value);
+int lra_ctx_get_tuning(const lra_ctx* ctx, char* buf, int64_t len);
+
+/* Limit of every bounded device-side wait (grid barriers, the pivoted QR's
+   exchange between CTAs, the tensor-core sketch's mbarriers), in ns; 0
+   restores the default of 4 s.  A wait that runs out makes its call return
+   LRA_ETIMEDOUT and leaves the context usable.  The setting belongs to the
+   device: it applies to every context on ctx's device.  Failure detection
+   of this engine, no counterpart in the reference.                         */
+int lra_ctx_set_wait_limit(lra_ctx* ctx, int64_t ns);
+/* Self-test of the bounded waits: a two-CTA cooperative kernel meets at a
+   grid barrier whose arrival count starts at the grid size, so no arrival
+   completes it; both CTAs wait out the limit above and return.  Returns
+   LRA_ETIMEDOUT when that happened as designed; any other status means the
+   bounded-wait machinery misbehaved.                                       */
+int lra_ctx_probe_wait(lra_ctx* ctx);
+
 /* LRAOptions(T) defaults (src/LowRankApprox.jl:96-119) */
 int lra_opts_init(lra_opts* opts, int dtype);
 /* chkopts! (src/LowRankApprox.jl:133-141) */
@@ -239,20 +269,33 @@ int lra_geqp3_adap(lra_ctx* ctx, int dtype, int64_t m, int64_t n, void* B,
                    int64_t* k);
 
 /* The same pivoted QR as lra_geqp3_adap, for callers that cannot allocate
-   device memory while they factor: code inside a CUDA stream capture, a
-   serving loop that reserved all of its memory up front, or a host whose
-   device allocator is owned by another framework.  It has no counterpart in
-   the reference.  Its scratch (partial norms, pivot candidates, counters,
-   grid barrier) is one fixed 1 MiB device array inside liblra, so the matrix
-   may have at most 32768 columns (larger n returns LRA_EINVAL); B, jpvt and
-   tau are caller-owned device buffers as above.  The first call on a device
-   resolves the array's device address (cudaGetSymbolAddress) and should
-   come before any stream capture.  All calls on a device share the array:
-   calls that overlap on the GPU race and must be serialized by the caller.
-   No cudaMalloc / cudaFree or allocating library routine is called.        */
+   device memory while they factor: a serving loop that reserved all of its
+   memory up front, or a host whose device allocator is owned by another
+   framework.  It has no counterpart in the reference.  Its scratch (partial
+   norms, pivot candidates, counters, grid barrier) is one fixed 1 MiB device
+   array inside liblra, so the matrix may have at most 32768 columns (larger
+   n returns LRA_EINVAL); B, jpvt and tau are caller-owned device buffers as
+   above.  The first call on a device resolves the array's device address
+   (cudaGetSymbolAddress) and caches it by device ordinal, so only the
+   device's primary context is supported.  Each call synchronizes the
+   context's stream and reads k back.  All calls on a device share the
+   array: calls that overlap on the GPU race and must be serialized by the
+   caller.  A rank of 0 (opts->rank == 0) returns k = 0 and the identity in
+   jpvt.  No cudaMalloc / cudaFree or allocating library routine is called. */
 int lra_geqp3_adap_noalloc(lra_ctx* ctx, int dtype, int64_t m, int64_t n, void* B,
                            int64_t ldb, int64_t* jpvt, void* tau,
                            const lra_opts* opts, int64_t* k);
+
+/* n draws of the in-library generator, the one a call with rand == NULL
+   uses in place of the reference's randn (src/util.jl:4-11,
+   src/sketch.jl:92): Philox-4x32-10 keyed by `seed`, counters from
+   `counter` on (each counter gives two values), Box-Muller, rounded to the
+   1/32 lattice; written to out (host or device, float64).  On a fresh
+   context a call draws its Gaussian sketches in adaptive-step order: step t
+   takes order_t * M values at counter c_t, with c_0 = 0 and c_(t+1) = c_t +
+   (order_t * M + 1) / 2.  Lets a caller reproduce the sketch a call used.  */
+int lra_rand_gauss(lra_ctx* ctx, uint64_t seed, uint64_t counter, int64_t n,
+                   double* out);
 
 /* C = alpha op(A) op(B) + beta C in Float64 (column-major device arrays;
    trans 'n' or 't'), computed the way the factorizations compute their
@@ -323,6 +366,55 @@ int lra_snormdiff_psvd(lra_ctx* ctx, int dtype, int64_t m, int64_t n,
                        const void* A, int64_t lda, const lra_psvd* F,
                        const lra_opts* opts, const lra_rand* rand,
                        double* out);
+
+/* ---- matrix-free operators (LinearOperator / HermitianLinearOperator,
+   src/linop.jl:9-40) -----------------------------------------------------------
+   An operator A (m x n) known only through the caller's product: matmat
+   writes Y = op(A) X for trans 'n' (op(A) = A: X is n x ncols, Y m x ncols)
+   or 'c' (op(A) = A': X is m x ncols, Y n x ncols), column-major DEVICE
+   arrays of the operator's element type with leading dimensions ldx, ldy.
+   It is called from the host thread of the library call, with X ready in
+   the order of `stream` (a cudaStream_t), and must either enqueue its work
+   on that stream or finish it before it returns; it returns 0, or nonzero
+   to make the call fail with LRA_ECUDA.  hermitian != 0 marks a
+   HermitianLinearOperator (m == n, A' = A): matmat is then called with 'n'
+   only.  As in the reference (chkopts!, src/LowRankApprox.jl:142-148), a
+   factorization of an operator uses the Gaussian sketch whatever
+   opts->sketch says; it runs in native precision (the products are the
+   caller's) and without the finite check.  A[:, cols] and A[rows, :] are
+   formed as products with unit columns (src/linop.jl:56-77).              */
+typedef int (*lra_matmat_fn)(void* user, char trans, int64_t ncols, const void* X, int64_t ldx, void* Y,
+                             int64_t ldy, void* stream);
+
+typedef struct lra_linop {
+  int64_t m, n;
+  int32_t dtype;       /* LRA_F32 / LRA_F64 */
+  int32_t hermitian;
+  lra_matmat_fn matmat;
+  void* user;
+} lra_linop;
+
+/* sketchfact / idfact / pqrfact / prange / psvdfact (psvdvals) / pheigfact
+   (pheigvals) / curfact / snorm of an operator: the entry points above with
+   A given as a lra_linop (src/sketch.jl:52-66, src/id.jl:434-450,
+   src/pqr.jl:290-307, src/prange.jl:14-61, src/psvd.jl:238-290,
+   src/pheig.jl:276-311, src/cur.jl:532-564, src/snorm.jl:14-45)         */
+int lra_sketchfact_linop(lra_ctx* ctx, char side, char trans, const lra_linop* A, const lra_opts* opts,
+                         const lra_rand* rand, lra_pqr** out);
+int lra_idfact_linop(lra_ctx* ctx, char trans, const lra_linop* A, const lra_opts* opts,
+                     const lra_rand* rand, lra_id** out);
+int lra_pqrfact_linop(lra_ctx* ctx, char trans, const lra_linop* A, const lra_opts* opts,
+                      const lra_rand* rand, lra_pqr** out);
+int lra_prange_linop(lra_ctx* ctx, char trans, const lra_linop* A, const lra_opts* opts,
+                     const lra_rand* rand, lra_pqr** out);
+int lra_psvdfact_linop(lra_ctx* ctx, const lra_linop* A, const lra_opts* opts, const lra_rand* rand,
+                       int vals_only, lra_psvd** out);
+int lra_pheigfact_linop(lra_ctx* ctx, const lra_linop* A, const lra_opts* opts, const lra_rand* rand,
+                        int vals_only, lra_pheig** out);
+int lra_curfact_linop(lra_ctx* ctx, const lra_linop* A, const lra_opts* opts, const lra_rand* rand,
+                      lra_cur** out);
+int lra_snorm_linop(lra_ctx* ctx, const lra_linop* A, const lra_opts* opts, const lra_rand* rand,
+                    double* out);
 
 /* ---- batches of independent matrices ---------------------------------------- */
 

@@ -41,6 +41,7 @@ struct DMat {
 
 template <typename T>
 DMat<T> stage_in(lra_ctx* ctx, const void* A, int64_t m, int64_t n, int64_t lda) {
+  if (ctx->linop) return DMat<T>{nullptr, std::max<int64_t>(m, 1)};  // matrix-free: no entries to stage
   if (m == 0 || n == 0) return DMat<T>{static_cast<const T*>(A), std::max<int64_t>(lda, 1)};
   if (!A) fail(LRA_EINVAL, "null matrix pointer");
   if (lda < std::max<int64_t>(1, m)) fail(LRA_EDIM, "lda (%lld) < m (%lld)", (long long)lda, (long long)m);
@@ -327,6 +328,59 @@ int slices_for(const lra_opts& o, int dtype) {
   return s;
 }
 
+// ---- matrix-free operators ---------------------------------------------------------
+// a dense sub-matrix taken from an operator is factored as a matrix: the
+// operator is set aside while this scope lives
+struct DenseScope {
+  lra_ctx* ctx;
+  const lra_linop* saved;
+  explicit DenseScope(lra_ctx* c) : ctx(c), saved(c->linop) { c->linop = nullptr; }
+  ~DenseScope() { ctx->linop = saved; }
+};
+
+// Y = op(L) X through the caller's product (trans 'n': L, 'c': L'; a
+// HermitianLinearOperator is its own adjoint), in stream order
+template <typename T>
+void linop_apply(lra_ctx* ctx, char trans, int64_t ncols, const T* X, int64_t ldx, T* Y, int64_t ldy) {
+  const lra_linop* L = ctx->linop;
+  if (ncols <= 0) return;
+  const char tr = (L->hermitian || trans == 'n') ? 'n' : 'c';
+  const int64_t rows = tr == 'n' ? L->m : L->n;
+  if (rows <= 0) return;
+  if (L->matmat(L->user, tr, ncols, X, ldx, Y, ldy, (void*)ctx->stream) != 0)
+    fail(LRA_ECUDA, "the operator's matmat callback returned an error");
+  LRA_CUDA(cudaGetLastError());
+}
+
+// C (rows x N, ldc) = X (rows x K, ldx) op(L), op(L) K x N: (op(L)' X')'
+template <typename T>
+void linop_rmul(lra_ctx* ctx, char trans, int64_t rows, int64_t K, int64_t N, const T* X, int64_t ldx, T* C,
+                int64_t ldc) {
+  if (rows <= 0 || N <= 0) return;
+  const ArenaMark mk = ctx->arena.mark();
+  T* Xt = ctx->arena.alloc_n<T>((size_t)std::max<int64_t>(K, 1) * rows);
+  T* Ct = ctx->arena.alloc_n<T>((size_t)N * rows);
+  transpose(ctx, rows, K, X, ldx, Xt, std::max<int64_t>(K, 1));
+  linop_apply<T>(ctx, trans == 'n' ? 'c' : 'n', rows, Xt, std::max<int64_t>(K, 1), Ct, N);
+  transpose(ctx, N, rows, Ct, N, C, ldc);
+  LRA_CUDA(cudaStreamSynchronize(ctx->stream));
+  ctx->arena.release(mk);
+}
+
+// E (N x k): the unit columns e_idx[i] (idx 1-based, device)
+template <typename T>
+T* unit_cols(lra_ctx* ctx, int64_t N, const int64_t* idx, int64_t k) {
+  const int64_t kk = std::max<int64_t>(k, 1);
+  T* I = ctx->arena.alloc_n<T>((size_t)kk * kk);
+  T* Et = ctx->arena.alloc_n<T>((size_t)kk * std::max<int64_t>(N, 1));
+  T* E = ctx->arena.alloc_n<T>((size_t)std::max<int64_t>(N, 1) * kk);
+  set_identity(ctx, k, k, I, kk);
+  set_zero(ctx, Et, kk * N);
+  scatter_cols(ctx, k, k, I, kk, idx, Et, kk);
+  transpose(ctx, k, N, Et, kk, E, std::max<int64_t>(N, 1));
+  return E;
+}
+
 // ---- sketches ----------------------------------------------------------------------
 template <typename T>
 void orthrows(lra_ctx* ctx, int64_t rows, int64_t cols, T* B) {
@@ -377,7 +431,12 @@ void make_sketch(lra_ctx* ctx, const lra_opts& o, char trans, int64_t M, int64_t
       } else {
         rs.gauss(order * M, S, o.precision == LRA_PREC_MIXED);
       }
-      if (tc) {
+      // the products with op(A): a GEMM, or the operator's own product for
+      // a matrix-free input (sketch_randn_* with A a LinOp, src/linop.jl)
+      const bool lin = ctx->linop != nullptr;
+      if (lin) {
+        linop_rmul<T>(ctx, trans, order, M, N, S, order, B, order);
+      } else if (tc) {
         TcSplit local;
         if (!split) split = &local;
         if (split->ns == 0) tc_split<T>(ctx, trans, M, N, A, lda, dtype == LRA_F64 ? 6 : 3, split);
@@ -391,12 +450,18 @@ void make_sketch(lra_ctx* ctx, const lra_opts& o, char trans, int64_t M, int64_t
         for (int64_t it = 0; it < o.sketch_randn_niter; ++it) {
           orthrows(ctx, order, N, B);
           // Bq = Bp op(A)^T (order x M)
-          gemm<T>(ctx, 'n', trans == 'c' ? 'n' : 't', order, M, N, T(1), B, order, A, lda, T(0), Bq, order);
+          if (lin)
+            linop_rmul<T>(ctx, trans == 'n' ? 'c' : 'n', order, N, M, B, order, Bq, order);
+          else
+            gemm<T>(ctx, 'n', trans == 'c' ? 'n' : 't', order, M, N, T(1), B, order, A, lda, T(0), Bq, order);
           if (herm) {
             copy_matrix(ctx, order, M, Bq, order, B, order);
           } else {
             orthrows(ctx, order, M, Bq);
-            gemm<T>(ctx, 'n', tA, order, N, M, T(1), Bq, order, A, lda, T(0), B, order);
+            if (lin)
+              linop_rmul<T>(ctx, trans, order, M, N, Bq, order, B, order);
+            else
+              gemm<T>(ctx, 'n', tA, order, N, M, T(1), Bq, order, A, lda, T(0), B, order);
           }
         }
       }
@@ -444,6 +509,10 @@ struct Fact {
   T* T_ = nullptr;  // k x (N - k), ld = k
   int64_t swaps = 0;  // maxdet swaps: when > 0, R11 no longer matches sk
   bool embed = true;  // B = S op(A) with S a subspace embedding (randn/srft)
+  // after maxdet swaps with an R factor requested: the Householder QR of the
+  // updated R1 (k x k, ld k; R above, reflectors below) and its tau
+  T* r1 = nullptr;
+  T* r1tau = nullptr;
 };
 
 template <typename T>
@@ -621,8 +690,13 @@ bool skeleton_qr(lra_ctx* ctx, const Fact<T>& F, int64_t M, T* Ask, T* RA, int d
 // getcols(trans, A, idx): M x k device matrix
 template <typename T>
 T* getcols(lra_ctx* ctx, char trans, int64_t m, int64_t n, const DMat<T>& A, const int64_t* idx, int64_t k) {
-  const int64_t M = trans == 'n' ? m : n;
+  const int64_t M = trans == 'n' ? m : n, N = trans == 'n' ? n : m;
   T* C = ctx->arena.alloc_n<T>((size_t)std::max<int64_t>(M, 1) * std::max<int64_t>(k, 1));
+  if (ctx->linop) {
+    // A[:, cols] of an operator is op(A) times unit columns (src/linop.jl:56-63)
+    if (k > 0 && M > 0) linop_apply<T>(ctx, trans, k, unit_cols<T>(ctx, N, idx, k), std::max<int64_t>(N, 1), C, M);
+    return C;
+  }
   if (trans == 'n') {
     gather_cols(ctx, m, k, A.p, A.ld, idx, C, M);
   } else {
@@ -640,25 +714,68 @@ T* getcols(lra_ctx* ctx, char trans, int64_t m, int64_t n, const DMat<T>& A, con
 // above `bound` and `update` is set, swap p and apply maxdet_update!
 // (src/pqr.jl:479-501, T part).  Returns whether max |T| > bound.
 template <typename T>
-bool maxdet_step(lra_ctx* ctx, int64_t k, int64_t nr, T* Tm, int64_t* jpvt, double bound, bool update);
+bool maxdet_step(lra_ctx* ctx, int64_t k, int64_t nr, T* Tm, int64_t* jpvt, double bound, bool update, T* R1,
+                 int64_t ldr);
 
 namespace {
 
-// strong rank-revealing swaps on T and p (the ID path: no R factor)
+// strong rank-revealing swaps (maxdet_swapcols!, src/pqr.jl:445-476): T and
+// p always; with an R factor requested, R1 = triu(R[:, 1:k]) follows each
+// swap (maxdet_update!, src/pqr.jl:494-499) and, after the last one, is
+// re-factored by an unpivoted Householder QR (qrfact!(R1), :467), whose
+// reflectors then rotate Q (gemqrt!, :468) and whose R replaces R11
+// (:469-474).  Without an R factor R1 stays triangular, its QR is the
+// identity and Q is left as it is.
 template <typename T>
 void maxdet_dev(lra_ctx* ctx, const lra_opts& o, Fact<T>& F) {
-  if (o.pqrfact_retval & (LRA_RET_R | LRA_RET_Q))
-    fail(LRA_ENOTSUP, "maxdet_tol >= 0 together with a Q or R factor is not supported");
-  const int64_t k = F.k, nr = F.N - k;
+  const int64_t k = F.k, nr = F.N - k, kk = std::max<int64_t>(k, 1);
+  const bool retr = o.pqrfact_retval & LRA_RET_R;
+  T* R1 = nullptr;
+  if (retr && k > 0) {
+    R1 = ctx->arena.alloc_n<T>((size_t)kk * kk);
+    copy_matrix(ctx, k, k, F.B, F.ld, R1, kk);
+    zero_lower(ctx, k, k, R1, kk);
+  }
   const int64_t cap = 64 * (k + nr) + 1000;  // the determinant grows every swap
   int64_t niter = 0;
   while (niter < cap) {
     const bool upd = niter != o.maxdet_niter;
-    if (!maxdet_step<T>(ctx, k, nr, F.T_, F.jpvt, 1.0 + o.maxdet_tol, upd)) break;
+    if (!maxdet_step<T>(ctx, k, nr, F.T_, F.jpvt, 1.0 + o.maxdet_tol, upd, R1, kk)) break;
     if (!upd) break;
     ++niter;
   }
   F.swaps = niter;
+  if (niter > 0 && R1) {
+    T* tau1 = ctx->arena.alloc_n<T>(kk);
+    int64_t* jp = ctx->arena.alloc_n<int64_t>(kk);
+    geqp3_adap<T>(ctx, k, k, R1, kk, jp, tau1, k, 32, -1.0, 0.0, false);
+    F.r1 = R1;
+    F.r1tau = tau1;
+  }
+}
+
+// R11 of the returned R: the re-factored R1 after maxdet swaps, else the
+// pivoted QR's own (k x k upper triangle into R11, ld k)
+template <typename T>
+void result_r11(lra_ctx* ctx, const Fact<T>& F, T* R11) {
+  const int64_t k = F.k, kk = std::max<int64_t>(k, 1);
+  if (F.r1)
+    copy_matrix(ctx, k, k, F.r1, kk, R11, kk);
+  else
+    copy_matrix(ctx, k, k, F.B, F.ld, R11, kk);
+  zero_lower(ctx, k, k, R11, kk);
+}
+
+// Q (M x k, ld ldq) <- Q Qf, Qf the reflectors of the re-factored R1
+// (LAPACK.gemqrt!('R', 'N', ...), src/pqr.jl:468), as (Qf^T Q^T)^T
+template <typename T>
+void maxdet_rotate_q(lra_ctx* ctx, const Fact<T>& F, int64_t M, T* Q, int64_t ldq) {
+  const int64_t k = F.k;
+  if (!F.r1 || k <= 0 || M <= 0) return;
+  T* Qt = ctx->arena.alloc_n<T>((size_t)k * M);
+  transpose(ctx, M, k, Q, ldq, Qt, k);
+  apply_q(ctx, 't', k, k, F.r1, k, F.r1tau, Qt, k, M);
+  transpose(ctx, k, M, Qt, k, Q, ldq);
 }
 
 }  // namespace
@@ -716,6 +833,7 @@ void dispatch(int dtype, Fn&& fn) {
 
 template <typename T>
 void check_input(lra_ctx* ctx, const lra_opts& o, int64_t m, int64_t n, const DMat<T>& A) {
+  if (ctx->linop) return;  // the operator's entries are not available
   if (o.check_finite && !all_finite(ctx, m, n, A.p, A.ld)) fail(LRA_ENONFINITE, "input has NaN or Inf entries");
 }
 
@@ -1011,6 +1129,954 @@ int try_idfact_batched_grouped(lra_ctx* ctx, int dtype, int64_t count, const lra
 
 }  // namespace lra
 
+
+namespace lra {
+namespace {
+int64_t psvdrank(const std::vector<double>& s, const lra_opts& o);
+std::pair<int64_t, int64_t> pheigrank(const std::vector<double>& w, const lra_opts& o);
+}  // namespace
+}  // namespace lra
+
+// ======================================================================================
+// complex element types (ComplexF32 / ComplexF64): the same drivers on the
+// complex kernels of cplx.cu, native precision.  The reference's A' is a
+// conjugate transpose throughout; Gaussian draws are crandn's pairs
+// (src/util.jl:4-11): entry t of a complex draw is (g[2t], g[2t + 1]).
+// ======================================================================================
+namespace lra {
+namespace {
+
+bool is_cplx(int dtype) { return dtype == LRA_C32 || dtype == LRA_C64; }
+
+template <class Fn>
+void dispatch_c(int dtype, Fn&& fn) {
+  if (dtype == LRA_C32)
+    fn(float{});
+  else
+    fn(double{});
+}
+
+template <typename R>
+using CX = cx<R>;
+
+// complex Gaussian draws (n entries) into out
+template <typename R>
+void cgauss(RandSrc& rs, int64_t n, CX<R>* out) {
+  rs.gauss<R>(2 * n, reinterpret_cast<R*>(out), false);
+}
+
+// raw Gaussian doubles on the device (the injected stream, or the library's)
+template <typename R>
+const double* gauss_raw_dev(lra_ctx* ctx, RandSrc& rs, int64_t n) {
+  if (rs.injected_gauss()) return rs.take_gauss_raw(n);
+  double* d = ctx->arena.alloc_n<double>(std::max<int64_t>(n, 1));
+  rs.gauss<double>(n, d, false);
+  return d;
+}
+
+template <typename R>
+void check_input_c(lra_ctx* ctx, const lra_opts& o, int64_t m, int64_t n, const DMat<CX<R>>& A) {
+  if (ctx->linop) return;
+  if (o.check_finite &&
+      !all_finite(ctx, 2 * m, n, reinterpret_cast<const R*>(A.p), 2 * A.ld))
+    fail(LRA_ENONFINITE, "input has NaN or Inf entries");
+}
+
+// orthcols!(thin = false): Q of the QR in the first min(m, n) columns, zeros after
+template <typename R>
+void orthcols_c(lra_ctx* ctx, int64_t m, int64_t n, CX<R>* B) {
+  const ArenaMark mk = ctx->arena.mark();
+  const int64_t kq = std::min(m, n);
+  int64_t* jp = ctx->arena.alloc_n<int64_t>(std::max<int64_t>(n, 1));
+  CX<R>* tau = ctx->arena.alloc_n<CX<R>>(std::max<int64_t>(kq, 1));
+  cgeqp3<R>(ctx, m, n, B, std::max<int64_t>(m, 1), jp, tau, kq, 32, -1.0, 0.0, false);
+  corgqr<R>(ctx, m, kq, B, std::max<int64_t>(m, 1), tau);
+  if (n > kq) set_zero<CX<R>>(ctx, B + kq * m, m * (n - kq));
+  LRA_CUDA(cudaStreamSynchronize(ctx->stream));
+  ctx->arena.release(mk);
+}
+
+// orthrows!(thin = false): rows of the LQ's Q (the QR of B^H), zeros after
+template <typename R>
+void orthrows_c(lra_ctx* ctx, int64_t m, int64_t n, CX<R>* B) {
+  const ArenaMark mk = ctx->arena.mark();
+  CX<R>* W = ctx->arena.alloc_n<CX<R>>((size_t)std::max<int64_t>(n, 1) * std::max<int64_t>(m, 1));
+  cadjoint<R>(ctx, m, n, B, std::max<int64_t>(m, 1), W, std::max<int64_t>(n, 1));
+  orthcols_c<R>(ctx, n, m, W);
+  cadjoint<R>(ctx, n, m, W, std::max<int64_t>(n, 1), B, std::max<int64_t>(m, 1));
+  LRA_CUDA(cudaStreamSynchronize(ctx->stream));
+  ctx->arena.release(mk);
+}
+
+// the operand accessors of the gather-type sketches: the left sketch of
+// op(A) reads op(A) itself, the right sketch reads op(A)^T (its output is
+// written transposed)
+inline char c_mode(char trans, bool right) {
+  // 'n': A(t, col) as stored; 'c': conj(A(col, t)); 't': A(col, t); 'j': conj(A(t, col))
+  if (!right) return trans == 'n' ? 'n' : 'c';
+  return trans == 'n' ? 't' : 'j';
+}
+
+// sketch(side, trans, A, order) for complex A (src/sketch.jl:35-46, 87-690):
+// left: B (order x N) = S op(A); right: B (M x order) = op(A) S, op(A) M x N
+template <typename R>
+void make_sketch_c(lra_ctx* ctx, const lra_opts& o, char trans, int64_t M, int64_t N, const CX<R>* A, int64_t lda,
+                   int64_t order, RandSrc& rs, CX<R>* B, bool right) {
+  const ArenaMark mk = ctx->arena.mark();
+  const CX<R> one(1), zero(0);
+  const char op = trans == 'n' ? 'n' : 'c', opH = trans == 'n' ? 'c' : 'n';
+  const int64_t ldb = right ? std::max<int64_t>(M, 1) : std::max<int64_t>(order, 1);
+  switch (o.sketch) {
+    case LRA_SKETCH_RANDN: {
+      const bool herm = (M == N) && [&] {
+        return ctx->linop ? ctx->linop->hermitian != 0 : cis_hermitian<R>(ctx, M, A, lda);
+      }();
+      if (!right) {
+        CX<R>* S = ctx->arena.alloc_n<CX<R>>((size_t)std::max<int64_t>(order * M, 1));
+        cgauss<R>(rs, order * M, S);
+        cgemm<R>(ctx, 'n', op, order, N, M, one, S, ldb, A, lda, zero, B, ldb);
+        CX<R>* Bq = ctx->arena.alloc_n<CX<R>>((size_t)std::max<int64_t>(order * M, 1));
+        for (int64_t it = 0; it < o.sketch_randn_niter; ++it) {
+          orthrows_c<R>(ctx, order, N, B);
+          cgemm<R>(ctx, 'n', opH, order, M, N, one, B, ldb, A, lda, zero, Bq, ldb);
+          if (herm) {
+            copy_matrix<CX<R>>(ctx, order, M, Bq, ldb, B, ldb);
+          } else {
+            orthrows_c<R>(ctx, order, M, Bq);
+            cgemm<R>(ctx, 'n', op, order, N, M, one, Bq, ldb, A, lda, zero, B, ldb);
+          }
+        }
+      } else {
+        CX<R>* S = ctx->arena.alloc_n<CX<R>>((size_t)std::max<int64_t>(N * order, 1));
+        cgauss<R>(rs, N * order, S);
+        cgemm<R>(ctx, op, 'n', M, order, N, one, A, lda, S, std::max<int64_t>(N, 1), zero, B, ldb);
+        CX<R>* Bq = ctx->arena.alloc_n<CX<R>>((size_t)std::max<int64_t>(N * order, 1));
+        const int64_t ldq = std::max<int64_t>(N, 1);
+        for (int64_t it = 0; it < o.sketch_randn_niter; ++it) {
+          orthcols_c<R>(ctx, M, order, B);
+          cgemm<R>(ctx, opH, 'n', N, order, M, one, A, lda, B, ldb, zero, Bq, ldq);
+          if (herm) {
+            copy_matrix<CX<R>>(ctx, N, order, Bq, ldq, B, ldb);
+          } else {
+            orthcols_c<R>(ctx, N, order, Bq);
+            cgemm<R>(ctx, op, 'n', M, order, N, one, A, lda, Bq, ldq, zero, B, ldb);
+          }
+        }
+      }
+      break;
+    }
+    case LRA_SKETCH_SRFT: {
+      // the transform runs over the sketched dimension K: M (left) or N (right)
+      const int64_t K = right ? N : M, C = right ? M : N;
+      if (K >= ((int64_t)1 << 31)) fail(LRA_ENOTSUP, "complex SRFT of more than 2^31 rows");
+      CX<R>* d = ctx->arena.alloc_n<CX<R>>(std::max<int64_t>(K, 1));
+      cphases<R>(ctx, gauss_raw_dev<R>(ctx, rs, 2 * K), K, d);
+      int64_t* idx = ctx->arena.alloc_n<int64_t>(std::max<int64_t>(order, 1));
+      rs.ints(order, K, idx, false);
+      CX<R>* Bl = right ? ctx->arena.alloc_n<CX<R>>((size_t)std::max<int64_t>(order * C, 1)) : B;
+      csrft_direct<R>(ctx, c_mode(trans, right), K, C, A, lda, d, idx, order, Bl, std::max<int64_t>(order, 1));
+      if (right) transpose<CX<R>>(ctx, order, C, Bl, std::max<int64_t>(order, 1), B, ldb);
+      break;
+    }
+    case LRA_SKETCH_SUB: {
+      const int64_t K = right ? N : M, C = right ? M : N;
+      int64_t* rows = ctx->arena.alloc_n<int64_t>(std::max<int64_t>(order, 1));
+      rs.ints(order, K, rows, false);
+      CX<R>* Bl = right ? ctx->arena.alloc_n<CX<R>>((size_t)std::max<int64_t>(order * C, 1)) : B;
+      csub<R>(ctx, c_mode(trans, right), C, A, lda, rows, order, Bl, std::max<int64_t>(order, 1));
+      if (right) transpose<CX<R>>(ctx, order, C, Bl, std::max<int64_t>(order, 1), B, ldb);
+      break;
+    }
+    case LRA_SKETCH_SPRN: {
+      const int64_t K = right ? N : M, C = right ? M : N;
+      int64_t* perm = ctx->arena.alloc_n<int64_t>(std::max<int64_t>(K, 1));
+      rs.ints(K, K, perm, true);
+      CX<R>* g = ctx->arena.alloc_n<CX<R>>(std::max<int64_t>(K, 1));
+      cgauss<R>(rs, K, g);
+      std::vector<int64_t> start(order + 1, 0);
+      for (int64_t i = 1; i <= order; ++i) start[i] = start[i - 1] + (K - i) / order + 1;
+      int64_t* dst = ctx->arena.alloc_n<int64_t>(order + 1);
+      LRA_CUDA(cudaMemcpyAsync(dst, start.data(), (order + 1) * sizeof(int64_t), cudaMemcpyHostToDevice,
+                               ctx->stream));
+      CX<R>* Bl = right ? ctx->arena.alloc_n<CX<R>>((size_t)std::max<int64_t>(order * C, 1)) : B;
+      csprn<R>(ctx, c_mode(trans, right), K, C, A, lda, perm, g, dst, order, Bl, std::max<int64_t>(order, 1));
+      if (right) transpose<CX<R>>(ctx, order, C, Bl, std::max<int64_t>(order, 1), B, ldb);
+      break;
+    }
+    default:
+      fail(LRA_EINVAL, "sketch");
+  }
+  LRA_CUDA(cudaStreamSynchronize(ctx->stream));
+  ctx->arena.release(mk);
+}
+
+template <typename R>
+struct CFact {
+  CX<R>* B = nullptr;  // rows x N, R in the upper triangle
+  int64_t ld = 0, order = 0, N = 0;
+  int64_t* jpvt = nullptr;
+  CX<R>* tau = nullptr;
+  int64_t k = 0;
+  int nsteps = 0;
+  CX<R>* T_ = nullptr;
+  int64_t swaps = 0;
+  CX<R>* r1 = nullptr;
+  CX<R>* r1tau = nullptr;
+};
+
+// geqp3_adap! of a dense rows x N device matrix B (ld), in place
+template <typename R>
+CFact<R> cpqr_backend(lra_ctx* ctx, const lra_opts& o, CX<R>* B, int64_t rows, int64_t N, int64_t ld) {
+  CFact<R> F;
+  F.B = B;
+  F.ld = ld;
+  F.order = rows;
+  F.N = N;
+  const int64_t l = std::min(rows, N);
+  const int64_t kmax = (o.rank < 0 || o.rank > l) ? l : o.rank;
+  F.jpvt = ctx->arena.alloc_n<int64_t>(std::max<int64_t>(N, 1));
+  F.tau = ctx->arena.alloc_n<CX<R>>(std::max<int64_t>(l, 1));
+  Stage st(ctx, 1);
+  F.k = cgeqp3<R>(ctx, rows, N, B, ld, F.jpvt, F.tau, kmax, o.nb, o.atol, o.rtol, true);
+  return F;
+}
+
+// sketchfact (src/sketch.jl:223-240 and twins): the adaptive doubling loop
+template <typename R>
+CFact<R> sketchfact_c(lra_ctx* ctx, const lra_opts& o, char trans, bool right, int64_t M, int64_t N,
+                      const CX<R>* A, int64_t lda, RandSrc& rs) {
+  const bool adaptive = o.sketchfact_adap || o.rank < 0;
+  int64_t nt = adaptive ? o.nb : o.rank;
+  CFact<R> F;
+  const ArenaMark base = ctx->arena.mark();
+  for (int step = 0;; ++step) {
+    if (step > 62) fail(LRA_EINVAL, "adaptive sketch did not terminate");
+    const int64_t order = samp(o, nt);
+    if (order < 0) fail(LRA_EINVAL, "sketch order %lld", (long long)order);
+    const int64_t rows = right ? M : order, cols = right ? order : N;
+    CX<R>* B = ctx->arena.alloc_n<CX<R>>((size_t)std::max<int64_t>(rows, 1) * std::max<int64_t>(cols, 1));
+    {
+      Stage st(ctx, 0);
+      make_sketch_c<R>(ctx, o, trans, M, N, A, lda, order, rs, B, right);
+    }
+    lra_opts oq = o;
+    F = cpqr_backend<R>(ctx, oq, B, rows, cols, std::max<int64_t>(rows, 1));
+    F.nsteps = step + 1;
+    if (!adaptive || F.k < nt) break;
+    nt *= 2;
+    ctx->arena.release(base);
+  }
+  return F;
+}
+
+// T = R11 \ R12 and maxdet (src/pqr.jl:420-501), as postproc_t does
+template <typename R>
+void cpostproc(lra_ctx* ctx, const lra_opts& o, CFact<R>& F, bool want_t) {
+  const bool maxdet = F.k > 0 && F.k < F.N && o.maxdet_tol >= 0;
+  if (!(want_t || maxdet)) return;
+  Stage st(ctx, 2);
+  const int64_t k = F.k, nr = F.N - k, kk = std::max<int64_t>(k, 1);
+  F.T_ = ctx->arena.alloc_n<CX<R>>((size_t)kk * std::max<int64_t>(nr, 1));
+  if (k > 0 && nr > 0) {
+    copy_matrix<CX<R>>(ctx, k, nr, F.B + k * F.ld, F.ld, F.T_, k);
+    ctrsm_upper<R>(ctx, k, nr, F.B, F.ld, F.T_, k);
+  }
+  if (!maxdet) return;
+  const bool retr = o.pqrfact_retval & LRA_RET_R;
+  CX<R>* R1 = nullptr;
+  if (retr) {
+    R1 = ctx->arena.alloc_n<CX<R>>((size_t)kk * kk);
+    copy_matrix<CX<R>>(ctx, k, k, F.B, F.ld, R1, kk);
+    zero_lower<CX<R>>(ctx, k, k, R1, kk);
+  }
+  const int64_t cap = 64 * (k + nr) + 1000;
+  int64_t niter = 0;
+  while (niter < cap) {
+    const bool upd = niter != o.maxdet_niter;
+    if (!cmaxdet_step<R>(ctx, k, nr, F.T_, F.jpvt, 1.0 + o.maxdet_tol, upd, R1, kk)) break;
+    if (!upd) break;
+    ++niter;
+  }
+  F.swaps = niter;
+  if (niter > 0 && R1) {
+    CX<R>* t1 = ctx->arena.alloc_n<CX<R>>(kk);
+    int64_t* jp = ctx->arena.alloc_n<int64_t>(kk);
+    cgeqp3<R>(ctx, k, k, R1, kk, jp, t1, k, 32, -1.0, 0.0, false);
+    F.r1 = R1;
+    F.r1tau = t1;
+  }
+}
+
+template <typename R>
+void cresult_r11(lra_ctx* ctx, const CFact<R>& F, CX<R>* R11) {
+  const int64_t k = F.k, kk = std::max<int64_t>(k, 1);
+  if (F.r1)
+    copy_matrix<CX<R>>(ctx, k, k, F.r1, kk, R11, kk);
+  else
+    copy_matrix<CX<R>>(ctx, k, k, F.B, F.ld, R11, kk);
+  zero_lower<CX<R>>(ctx, k, k, R11, kk);
+}
+
+// Q <- Q Qf after maxdet re-factored R1 (gemqrt!('R', 'N'), src/pqr.jl:468)
+template <typename R>
+void cmaxdet_rotate_q(lra_ctx* ctx, const CFact<R>& F, int64_t M, CX<R>* Q, int64_t ldq) {
+  const int64_t k = F.k;
+  if (!F.r1 || k <= 0 || M <= 0) return;
+  CX<R>* Qh = ctx->arena.alloc_n<CX<R>>((size_t)k * M);
+  cadjoint<R>(ctx, M, k, Q, ldq, Qh, k);                       // Q^H (k x M)
+  capply_q<R>(ctx, 'c', k, k, F.r1, k, F.r1tau, Qh, k, M);      // Qf^H Q^H
+  cadjoint<R>(ctx, k, M, Qh, k, Q, ldq);
+}
+
+// op(A) as a dense device copy (M x N, ld M)
+template <typename R>
+CX<R>* cdense_op(lra_ctx* ctx, char trans, int64_t m, int64_t n, const DMat<CX<R>>& A) {
+  const int64_t M = trans == 'n' ? m : n, N = trans == 'n' ? n : m;
+  CX<R>* B = ctx->arena.alloc_n<CX<R>>((size_t)std::max<int64_t>(M, 1) * std::max<int64_t>(N, 1));
+  if (trans == 'n')
+    copy_matrix<CX<R>>(ctx, m, n, A.p, A.ld, B, std::max<int64_t>(M, 1));
+  else
+    cadjoint<R>(ctx, m, n, A.p, A.ld, B, std::max<int64_t>(M, 1));
+  return B;
+}
+
+// getcols(trans, A, idx) (src/util.jl:25-29): M x k
+template <typename R>
+CX<R>* cgetcols(lra_ctx* ctx, char trans, int64_t m, int64_t n, const DMat<CX<R>>& A, const int64_t* idx,
+                int64_t k) {
+  const int64_t M = trans == 'n' ? m : n;
+  CX<R>* C = ctx->arena.alloc_n<CX<R>>((size_t)std::max<int64_t>(M, 1) * std::max<int64_t>(k, 1));
+  if (trans == 'n') {
+    gather_cols<CX<R>>(ctx, m, k, A.p, A.ld, idx, C, std::max<int64_t>(M, 1));
+  } else {
+    CX<R>* Rw = ctx->arena.alloc_n<CX<R>>((size_t)std::max<int64_t>(k, 1) * std::max<int64_t>(n, 1));
+    gather_rows<CX<R>>(ctx, k, n, A.p, A.ld, idx, Rw, std::max<int64_t>(k, 1));
+    cadjoint<R>(ctx, k, n, Rw, std::max<int64_t>(k, 1), C, std::max<int64_t>(M, 1));
+  }
+  return C;
+}
+
+template <typename R>
+CFact<R> cid_core(lra_ctx* ctx, const lra_opts& o, char trans, int64_t m, int64_t n, const DMat<CX<R>>& A,
+                  RandSrc& rs, bool want_t) {
+  const int64_t M = trans == 'n' ? m : n, N = trans == 'n' ? n : m;
+  CFact<R> F;
+  if (o.sketch == LRA_SKETCH_NONE) {
+    CX<R>* B = cdense_op<R>(ctx, trans, m, n, A);
+    F = cpqr_backend<R>(ctx, o, B, M, N, std::max<int64_t>(M, 1));
+  } else {
+    F = sketchfact_c<R>(ctx, o, trans, false, M, N, A.p, A.ld, rs);
+  }
+  cpostproc<R>(ctx, o, F, want_t);
+  return F;
+}
+
+template <typename R>
+lra_id* cpack_id(lra_ctx* ctx, const CFact<R>& F, int dtype) {
+  lra_id* r = static_cast<lra_id*>(hmalloc(sizeof(lra_id)));
+  std::memset(r, 0, sizeof *r);
+  r->dtype = dtype;
+  r->nsteps = F.nsteps;
+  r->k = F.k;
+  r->n = F.N;
+  r->sk = static_cast<int64_t*>(hmalloc(sizeof(int64_t) * std::max<int64_t>(F.k, 1)));
+  r->rd = static_cast<int64_t*>(hmalloc(sizeof(int64_t) * std::max<int64_t>(F.N - F.k, 1)));
+  r->T = hmalloc(sizeof(CX<R>) * std::max<int64_t>(F.k * (F.N - F.k), 1));
+  to_host(ctx, r->sk, F.jpvt, F.k);
+  to_host(ctx, r->rd, F.jpvt + F.k, F.N - F.k);
+  if (F.k > 0 && F.N > F.k) to_host(ctx, r->T, F.T_, (size_t)F.k * (F.N - F.k));
+  LRA_CUDA(cudaStreamSynchronize(ctx->stream));
+  return r;
+}
+
+// the pivoted QR's Q (rows x k) of F and its R = [R11 | R11 T] (k x N)
+template <typename R>
+void cfact_qr(lra_ctx* ctx, CFact<R>& F, bool rq, bool rr, lra_pqr* r) {
+  const int64_t k = F.k, N = F.N, rows = F.order, kk = std::max<int64_t>(k, 1);
+  if (rr) {
+    CX<R>* Rm = ctx->arena.alloc_n<CX<R>>((size_t)kk * std::max<int64_t>(N, 1));
+    cresult_r11<R>(ctx, F, Rm);
+    if (N > k && k > 0) {
+      if (F.T_)
+        cgemm<R>(ctx, 'n', 'n', k, N - k, k, CX<R>(1), Rm, kk, F.T_, kk, CX<R>(0), Rm + k * kk, kk);
+      else {
+        copy_matrix<CX<R>>(ctx, k, N - k, F.B + k * F.ld, F.ld, Rm + k * kk, kk);
+      }
+    }
+    r->R = hmalloc(sizeof(CX<R>) * std::max<int64_t>(k * N, 1));
+    to_host(ctx, r->R, Rm, (size_t)k * N);
+    r->retval |= LRA_RET_R;
+  }
+  if (rq) {
+    corgqr<R>(ctx, rows, k, F.B, F.ld, F.tau);
+    cmaxdet_rotate_q<R>(ctx, F, rows, F.B, F.ld);
+    r->Q = hmalloc(sizeof(CX<R>) * std::max<int64_t>(rows * k, 1));
+    if (k > 0 && rows > 0)
+      LRA_CUDA(cudaMemcpy2DAsync(r->Q, rows * sizeof(CX<R>), F.B, F.ld * sizeof(CX<R>), rows * sizeof(CX<R>), k,
+                                 cudaMemcpyDeviceToHost, ctx->stream));
+    r->retval |= LRA_RET_Q;
+  }
+}
+
+template <typename R>
+lra_pqr* new_pqr(int dtype, int64_t m, int64_t n, int64_t k) {
+  lra_pqr* r = static_cast<lra_pqr*>(hmalloc(sizeof(lra_pqr)));
+  std::memset(r, 0, sizeof *r);
+  r->dtype = dtype;
+  r->m = m;
+  r->n = n;
+  r->k = k;
+  r->p = static_cast<int64_t*>(hmalloc(sizeof(int64_t) * std::max<int64_t>(n, 1)));
+  return r;
+}
+
+// sketchfact(side, trans, A) for complex A
+template <typename R>
+lra_pqr* csketchfact(lra_ctx* ctx, const lra_opts& o0, char side, char t, int64_t m, int64_t n,
+                     const DMat<CX<R>>& A, RandSrc& rs, int dtype) {
+  lra_opts o = o0;
+  if (o.sketch == LRA_SKETCH_NONE) o.sketch = LRA_SKETCH_RANDN;
+  const bool right = side == 'r' || side == 'R';
+  const int64_t M = t == 'n' ? m : n, N = t == 'n' ? n : m;
+  CFact<R> F = sketchfact_c<R>(ctx, o, t, right, M, N, A.p, A.ld, rs);
+  const bool rq = o.pqrfact_retval & LRA_RET_Q, rr = o.pqrfact_retval & LRA_RET_R, rt = o.pqrfact_retval & LRA_RET_T;
+  cpostproc<R>(ctx, o, F, rt);
+  lra_pqr* r = new_pqr<R>(dtype, F.order, F.N, F.k);
+  try {
+    to_host(ctx, r->p, F.jpvt, F.N);
+    if (rt) {
+      r->T = hmalloc(sizeof(CX<R>) * std::max<int64_t>(F.k * (F.N - F.k), 1));
+      if (F.k > 0 && F.N > F.k) to_host(ctx, r->T, F.T_, (size_t)F.k * (F.N - F.k));
+      r->retval |= LRA_RET_T;
+    }
+    if (rr && !F.T_ && F.k > 0 && F.k < F.N) {
+      // R = triu(B[1:k, :]) without maxdet (src/pqr.jl:428)
+      CX<R>* Rm = ctx->arena.alloc_n<CX<R>>((size_t)F.k * F.N);
+      copy_matrix<CX<R>>(ctx, F.k, F.N, F.B, F.ld, Rm, F.k);
+      zero_lower<CX<R>>(ctx, F.k, F.N, Rm, F.k);
+      r->R = hmalloc(sizeof(CX<R>) * (size_t)F.k * F.N);
+      to_host(ctx, r->R, Rm, (size_t)F.k * F.N);
+      r->retval |= LRA_RET_R;
+      cfact_qr<R>(ctx, F, rq, false, r);
+    } else {
+      cfact_qr<R>(ctx, F, rq, rr, r);
+    }
+    LRA_CUDA(cudaStreamSynchronize(ctx->stream));
+  } catch (...) {
+    lra_pqr_free(r);
+    throw;
+  }
+  return r;
+}
+
+// pqrfact(trans, A) (src/pqr.jl:290-307)
+template <typename R>
+lra_pqr* cpqrfact(lra_ctx* ctx, const lra_opts& o, char t, int64_t m, int64_t n, const DMat<CX<R>>& A,
+                  RandSrc& rs, int dtype) {
+  const int64_t M = t == 'n' ? m : n, N = t == 'n' ? n : m;
+  const bool rq = o.pqrfact_retval & LRA_RET_Q, rr = o.pqrfact_retval & LRA_RET_R, rt = o.pqrfact_retval & LRA_RET_T;
+  lra_pqr* r = new_pqr<R>(dtype, M, N, 0);
+  try {
+    if (o.sketch == LRA_SKETCH_NONE) {
+      CX<R>* B = cdense_op<R>(ctx, t, m, n, A);
+      CFact<R> F = cpqr_backend<R>(ctx, o, B, M, N, std::max<int64_t>(M, 1));
+      cpostproc<R>(ctx, o, F, rt || rr);
+      r->k = F.k;
+      to_host(ctx, r->p, F.jpvt, N);
+      cfact_qr<R>(ctx, F, rq, rr, r);
+      if (rt) {
+        r->T = hmalloc(sizeof(CX<R>) * std::max<int64_t>(F.k * (N - F.k), 1));
+        if (F.k > 0 && N > F.k) to_host(ctx, r->T, F.T_, (size_t)F.k * (N - F.k));
+        r->retval |= LRA_RET_T;
+      }
+    } else {
+      lra_opts oi = o;
+      oi.pqrfact_retval = LRA_RET_T;
+      CFact<R> F = cid_core<R>(ctx, oi, t, m, n, A, rs, true);
+      const int64_t k = F.k, kk = std::max<int64_t>(k, 1);
+      r->k = k;
+      to_host(ctx, r->p, F.jpvt, N);
+      // Q, R11 = qr(A[:, sk]); R = [R11 | R11 T] (pqrr, src/pqr.jl:330-340)
+      CX<R>* Ask = cgetcols<R>(ctx, t, m, n, A, F.jpvt, k);
+      int64_t* jp = ctx->arena.alloc_n<int64_t>(kk);
+      CX<R>* tau = ctx->arena.alloc_n<CX<R>>(kk);
+      cgeqp3<R>(ctx, M, k, Ask, std::max<int64_t>(M, 1), jp, tau, k, 32, -1.0, 0.0, false);
+      CFact<R> Q;
+      Q.B = Ask;
+      Q.ld = std::max<int64_t>(M, 1);
+      Q.order = M;
+      Q.N = N;
+      Q.k = k;
+      Q.tau = tau;
+      if (rr) {
+        CX<R>* Rm = ctx->arena.alloc_n<CX<R>>((size_t)kk * std::max<int64_t>(N, 1));
+        copy_matrix<CX<R>>(ctx, k, k, Ask, Q.ld, Rm, kk);
+        zero_lower<CX<R>>(ctx, k, k, Rm, kk);
+        if (N > k && k > 0)
+          cgemm<R>(ctx, 'n', 'n', k, N - k, k, CX<R>(1), Rm, kk, F.T_, kk, CX<R>(0), Rm + k * kk, kk);
+        r->R = hmalloc(sizeof(CX<R>) * std::max<int64_t>(k * N, 1));
+        to_host(ctx, r->R, Rm, (size_t)k * N);
+        r->retval |= LRA_RET_R;
+      }
+      if (rq) cfact_qr<R>(ctx, Q, true, false, r);
+      if (rt) {
+        r->T = hmalloc(sizeof(CX<R>) * std::max<int64_t>(k * (N - k), 1));
+        if (k > 0 && N > k) to_host(ctx, r->T, F.T_, (size_t)k * (N - k));
+        r->retval |= LRA_RET_T;
+      }
+    }
+    LRA_CUDA(cudaStreamSynchronize(ctx->stream));
+  } catch (...) {
+    lra_pqr_free(r);
+    throw;
+  }
+  return r;
+}
+
+// SVD of a k x k device matrix X (ld ldx, destroyed): U (k x k, ld k), S
+// descending (host), V (k x k, ld k) with X = U diag(S) V^H
+template <typename R>
+std::vector<R> csmall_svd(lra_ctx* ctx, int64_t k, CX<R>* X, int64_t ldx, CX<R>* U, CX<R>* V) {
+  const int64_t kk = std::max<int64_t>(k, 1);
+  std::vector<R> hS(k);
+  if (k <= 0) return hS;
+  CX<R>* Xw = ctx->arena.alloc_n<CX<R>>((size_t)kk * kk);
+  copy_matrix<CX<R>>(ctx, k, k, X, ldx, Xw, kk);
+  CX<R>* Vw = ctx->arena.alloc_n<CX<R>>((size_t)kk * kk);
+  R* S = ctx->arena.alloc_n<R>(kk);
+  cjacobi_svd<R>(ctx, k, Xw, kk, Vw, kk, S);
+  to_host(ctx, hS.data(), S, k);
+  LRA_CUDA(cudaStreamSynchronize(ctx->stream));
+  std::vector<int64_t> ord(k);
+  std::iota(ord.begin(), ord.end(), 0);
+  std::stable_sort(ord.begin(), ord.end(), [&](int64_t a, int64_t b) { return hS[a] > hS[b]; });
+  std::vector<int64_t> cols(k);
+  std::vector<R> sorted(k);
+  for (int64_t i = 0; i < k; ++i) {
+    cols[i] = ord[i] + 1;
+    sorted[i] = hS[ord[i]];
+  }
+  int64_t* dc = ctx->arena.alloc_n<int64_t>(kk);
+  LRA_CUDA(cudaMemcpyAsync(dc, cols.data(), k * sizeof(int64_t), cudaMemcpyHostToDevice, ctx->stream));
+  gather_cols<CX<R>>(ctx, k, k, Xw, kk, dc, U, kk);
+  gather_cols<CX<R>>(ctx, k, k, Vw, kk, dc, V, kk);
+  LRA_CUDA(cudaStreamSynchronize(ctx->stream));
+  return sorted;
+}
+
+// psvdfact / psvdvals (src/psvd.jl:238-290)
+template <typename R>
+lra_psvd* cpsvd(lra_ctx* ctx, const lra_opts& o, int64_t m, int64_t n, const DMat<CX<R>>& A, RandSrc& rs,
+                int dtype, bool vals_only) {
+  const bool tall = m >= n;
+  const char t = tall ? 'n' : 'c';
+  const int64_t M = tall ? m : n, N = tall ? n : m;  // op(A) is M x N
+  lra_opts oi = o;
+  oi.pqrfact_retval = LRA_RET_T;
+  CFact<R> F = cid_core<R>(ctx, oi, t, m, n, A, rs, true);
+  const int64_t k = F.k, kk = std::max<int64_t>(k, 1), ldq = std::max<int64_t>(M, 1), ldn = std::max<int64_t>(N, 1);
+  Stage st(ctx, 3);
+  // Q, R = qr(op(A)[:, sk])
+  CX<R>* Q = cgetcols<R>(ctx, t, m, n, A, F.jpvt, k);
+  int64_t* jp = ctx->arena.alloc_n<int64_t>(kk);
+  CX<R>* tau = ctx->arena.alloc_n<CX<R>>(kk);
+  cgeqp3<R>(ctx, M, k, Q, ldq, jp, tau, k, 32, -1.0, 0.0, false);
+  CX<R>* Rm = ctx->arena.alloc_n<CX<R>>((size_t)kk * kk);
+  copy_matrix<CX<R>>(ctx, k, k, Q, ldq, Rm, kk);
+  zero_lower<CX<R>>(ctx, k, k, Rm, kk);
+  corgqr<R>(ctx, M, k, Q, ldq, tau);
+  // Wh = (R Vhat)^H (N x k): rows sk <- R^H, rows rd <- T^H R^H
+  CX<R>* Wh = ctx->arena.alloc_n<CX<R>>((size_t)ldn * kk);
+  {
+    CX<R>* Rh = ctx->arena.alloc_n<CX<R>>((size_t)kk * kk);
+    cadjoint<R>(ctx, k, k, Rm, kk, Rh, kk);
+    CX<R>* Wp = ctx->arena.alloc_n<CX<R>>((size_t)ldn * kk);  // [R^H; T^H R^H] in pivoted row order
+    copy_matrix<CX<R>>(ctx, k, k, Rh, kk, Wp, ldn);
+    if (N > k && k > 0)
+      cgemm<R>(ctx, 'c', 'n', N - k, k, k, CX<R>(1), F.T_, kk, Rh, kk, CX<R>(0), Wp + k, ldn);
+    set_zero<CX<R>>(ctx, Wh, ldn * kk);
+    CX<R>* Wpt = ctx->arena.alloc_n<CX<R>>((size_t)kk * ldn);
+    transpose<CX<R>>(ctx, N, k, Wp, ldn, Wpt, kk);
+    CX<R>* Wt = ctx->arena.alloc_n<CX<R>>((size_t)kk * ldn);
+    scatter_cols<CX<R>>(ctx, k, N, Wpt, kk, F.jpvt, Wt, kk);
+    transpose<CX<R>>(ctx, k, N, Wt, kk, Wh, ldn);
+  }
+  // Wh = Q2 R2; R2^H = Ux S Vx^H; W = R Vhat = Ux S (Q2 Vx)^H
+  int64_t* jp2 = ctx->arena.alloc_n<int64_t>(kk);
+  CX<R>* tau2 = ctx->arena.alloc_n<CX<R>>(kk);
+  cgeqp3<R>(ctx, N, k, Wh, ldn, jp2, tau2, k, 32, -1.0, 0.0, false);
+  CX<R>* R2 = ctx->arena.alloc_n<CX<R>>((size_t)kk * kk);
+  copy_matrix<CX<R>>(ctx, k, k, Wh, ldn, R2, kk);
+  zero_lower<CX<R>>(ctx, k, k, R2, kk);
+  CX<R>* X = ctx->arena.alloc_n<CX<R>>((size_t)kk * kk);
+  cadjoint<R>(ctx, k, k, R2, kk, X, kk);
+  CX<R>* Ux = ctx->arena.alloc_n<CX<R>>((size_t)kk * kk);
+  CX<R>* Vx = ctx->arena.alloc_n<CX<R>>((size_t)kk * kk);
+  std::vector<R> hS = csmall_svd<R>(ctx, k, X, kk, Ux, Vx);
+  std::vector<double> sd(hS.begin(), hS.end());
+  const int64_t kr = psvdrank(sd, o), lkr = std::max<int64_t>(kr, 1);
+  lra_psvd* r = static_cast<lra_psvd*>(hmalloc(sizeof(lra_psvd)));
+  std::memset(r, 0, sizeof *r);
+  r->dtype = dtype;
+  r->m = m;
+  r->n = n;
+  r->k = kr;
+  r->S = hmalloc(sizeof(R) * lkr);
+  std::memcpy(r->S, hS.data(), sizeof(R) * kr);
+  if (vals_only) return r;
+  // Vfull = Q2 Vx (N x k): the reflectors of Wh applied to [Vx; 0]
+  CX<R>* Vf = ctx->arena.alloc_n<CX<R>>((size_t)ldn * lkr);
+  set_zero<CX<R>>(ctx, Vf, ldn * lkr);
+  copy_matrix<CX<R>>(ctx, k, kr, Vx, kk, Vf, ldn);
+  capply_q<R>(ctx, 'n', N, k, Wh, ldn, tau2, Vf, ldn, kr);
+  // op(A) = (Q Ux) S Vf^H
+  CX<R>* Uf = ctx->arena.alloc_n<CX<R>>((size_t)ldq * lkr);
+  cgemm<R>(ctx, 'n', 'n', M, kr, k, CX<R>(1), Q, ldq, Ux, kk, CX<R>(0), Uf, ldq);
+  // A = Uf S Vf^H (m >= n), or A = op(A)^H = Vf S Uf^H (m < n)
+  CX<R>* Uo = tall ? Uf : Vf;
+  CX<R>* Vo = tall ? Vf : Uf;
+  const int64_t ldu = tall ? ldq : ldn, ldv = tall ? ldn : ldq;
+  CX<R>* Vt = ctx->arena.alloc_n<CX<R>>((size_t)lkr * std::max<int64_t>(n, 1));
+  cadjoint<R>(ctx, n, kr, Vo, ldv, Vt, lkr);
+  r->U = hmalloc(sizeof(CX<R>) * std::max<int64_t>(m * kr, 1));
+  r->Vt = hmalloc(sizeof(CX<R>) * std::max<int64_t>(kr * n, 1));
+  if (m > 0 && kr > 0)
+    LRA_CUDA(cudaMemcpy2DAsync(r->U, m * sizeof(CX<R>), Uo, ldu * sizeof(CX<R>), m * sizeof(CX<R>), kr,
+                               cudaMemcpyDeviceToHost, ctx->stream));
+  to_host(ctx, r->Vt, Vt, (size_t)kr * n);
+  LRA_CUDA(cudaStreamSynchronize(ctx->stream));
+  return r;
+}
+
+// pheigfact / pheigvals (src/pheig.jl:276-311)
+template <typename R>
+lra_pheig* cpheig(lra_ctx* ctx, const lra_opts& o, int64_t n, const DMat<CX<R>>& A, RandSrc& rs, int dtype,
+                  bool vals_only) {
+  lra_opts oi = o;
+  oi.pqrfact_retval = LRA_RET_T;
+  CFact<R> F = cid_core<R>(ctx, oi, 'n', n, n, A, rs, true);
+  const int64_t k = F.k, kk = std::max<int64_t>(k, 1), ldn = std::max<int64_t>(n, 1);
+  Stage st(ctx, 3);
+  // Q, R = qr(Vhat^H): Vhat^H (n x k) has rows sk = I, rows rd = T^H
+  CX<R>* Vh = ctx->arena.alloc_n<CX<R>>((size_t)ldn * kk);
+  {
+    CX<R>* P = ctx->arena.alloc_n<CX<R>>((size_t)kk * ldn);  // Vhat (k x n) in pivoted order
+    set_identity<CX<R>>(ctx, k, k, P, kk);
+    if (n > k && k > 0) copy_matrix<CX<R>>(ctx, k, n - k, F.T_, kk, P + k * kk, kk);
+    CX<R>* Vm = ctx->arena.alloc_n<CX<R>>((size_t)kk * ldn);
+    scatter_cols<CX<R>>(ctx, k, n, P, kk, F.jpvt, Vm, kk);
+    cadjoint<R>(ctx, k, n, Vm, kk, Vh, ldn);
+  }
+  int64_t* jp = ctx->arena.alloc_n<int64_t>(kk);
+  CX<R>* tau = ctx->arena.alloc_n<CX<R>>(kk);
+  cgeqp3<R>(ctx, n, k, Vh, ldn, jp, tau, k, 32, -1.0, 0.0, false);
+  CX<R>* Rm = ctx->arena.alloc_n<CX<R>>((size_t)kk * kk);
+  copy_matrix<CX<R>>(ctx, k, k, Vh, ldn, Rm, kk);
+  zero_lower<CX<R>>(ctx, k, k, Rm, kk);
+  // B = R (A[sk, sk] R^H)
+  CX<R>* Ass = ctx->arena.alloc_n<CX<R>>((size_t)kk * kk);
+  {
+    CX<R>* Ac = cgetcols<R>(ctx, 'n', n, n, A, F.jpvt, k);
+    gather_rows<CX<R>>(ctx, k, k, Ac, ldn, F.jpvt, Ass, kk);
+  }
+  CX<R>* Cm = ctx->arena.alloc_n<CX<R>>((size_t)kk * kk);
+  cgemm<R>(ctx, 'n', 'c', k, k, k, CX<R>(1), Ass, kk, Rm, kk, CX<R>(0), Cm, kk);
+  CX<R>* B = ctx->arena.alloc_n<CX<R>>((size_t)kk * kk);
+  cgemm<R>(ctx, 'n', 'n', k, k, k, CX<R>(1), Rm, kk, Cm, kk, CX<R>(0), B, kk);
+  chermitianize<R>(ctx, k, B, kk);
+  // eigen! through the Jacobi SVD of the positive shift B + s I
+  R* cn = ctx->arena.alloc_n<R>(kk);
+  ccol_norms<R>(ctx, k, k, B, kk, cn);
+  std::vector<R> hcn(k);
+  to_host(ctx, hcn.data(), cn, k);
+  LRA_CUDA(cudaStreamSynchronize(ctx->stream));
+  double fro = 0;
+  for (R v : hcn) fro += (double)v * (double)v;
+  const R shift = (R)(std::sqrt(fro) * 1.0001 + (fro == 0 ? 1.0 : 0.0));
+  cadd_diag<R>(ctx, k, B, kk, shift);
+  CX<R>* U = ctx->arena.alloc_n<CX<R>>((size_t)kk * kk);
+  CX<R>* Z = ctx->arena.alloc_n<CX<R>>((size_t)kk * kk);
+  std::vector<R> hS = csmall_svd<R>(ctx, k, B, kk, U, Z);
+  std::vector<double> w(k);
+  for (int64_t i = 0; i < k; ++i) w[i] = (double)hS[i] - (double)shift;
+  std::vector<int64_t> ord(k);
+  std::iota(ord.begin(), ord.end(), 0);
+  std::stable_sort(ord.begin(), ord.end(), [&](int64_t a, int64_t b) { return w[a] < w[b]; });
+  std::vector<double> ws(k);
+  for (int64_t i = 0; i < k; ++i) ws[i] = w[ord[i]];
+  auto kp = pheigrank(ws, o);
+  std::vector<int64_t> sel;
+  if (kp.first + kp.second < k) {
+    for (int64_t i = 0; i < kp.first; ++i) sel.push_back(i);
+    for (int64_t i = k - kp.second; i < k; ++i) sel.push_back(i);
+  } else {
+    for (int64_t i = 0; i < k; ++i) sel.push_back(i);
+  }
+  const int64_t ke = (int64_t)sel.size();
+  lra_pheig* r = static_cast<lra_pheig*>(hmalloc(sizeof(lra_pheig)));
+  std::memset(r, 0, sizeof *r);
+  r->dtype = dtype;
+  r->n = n;
+  r->k = ke;
+  r->values = hmalloc(sizeof(R) * std::max<int64_t>(ke, 1));
+  std::vector<double> vals(ke);
+  for (int64_t i = 0; i < ke; ++i) {
+    vals[i] = ws[sel[i]];
+    static_cast<R*>(r->values)[i] = (R)vals[i];
+  }
+  if (!vals_only && ke > 0) {
+    std::vector<int64_t> cols1(ke);
+    for (int64_t i = 0; i < ke; ++i) cols1[i] = ord[sel[i]] + 1;
+    int64_t* dcols = ctx->arena.alloc_n<int64_t>(ke);
+    LRA_CUDA(cudaMemcpyAsync(dcols, cols1.data(), ke * sizeof(int64_t), cudaMemcpyHostToDevice, ctx->stream));
+    CX<R>* Zs = ctx->arena.alloc_n<CX<R>>((size_t)ldn * ke);
+    set_zero<CX<R>>(ctx, Zs, ldn * ke);
+    gather_cols<CX<R>>(ctx, k, ke, Z, kk, dcols, Zs, ldn);
+    std::vector<int64_t> cl;
+    int64_t a = 0;
+    while (a < ke) {
+      const double va = vals[a];
+      int64_t b = a + 1;
+      while (b < ke) {
+        if (2 * std::fabs((va - vals[b]) / (va + vals[b])) > o.pheig_orthtol) break;
+        ++b;
+      }
+      --b;
+      if (b > a) {
+        cl.push_back(a);
+        cl.push_back(b + 1);
+      }
+      a = b + 1;
+    }
+    if (!cl.empty()) {
+      int64_t* dcl = ctx->arena.alloc_n<int64_t>(cl.size());
+      LRA_CUDA(cudaMemcpyAsync(dcl, cl.data(), cl.size() * sizeof(int64_t), cudaMemcpyHostToDevice, ctx->stream));
+      ccluster_orth<R>(ctx, k, ke, Zs, ldn, dcl, (int64_t)cl.size() / 2);
+    }
+    capply_q<R>(ctx, 'n', n, k, Vh, ldn, tau, Zs, ldn, ke);
+    r->vectors = hmalloc(sizeof(CX<R>) * (size_t)n * ke);
+    to_host(ctx, r->vectors, Zs, (size_t)n * ke);
+    LRA_CUDA(cudaStreamSynchronize(ctx->stream));
+  }
+  return r;
+}
+
+// curfact (src/cur.jl:532-606)
+template <typename R>
+lra_cur* ccurfact(lra_ctx* ctx, const lra_opts& o0, int64_t m, int64_t n, const DMat<CX<R>>& A, RandSrc& rs) {
+  lra_opts o = o0;
+  o.pqrfact_retval = 0;
+  auto sel = [&](char t, int64_t mm, int64_t nn, const DMat<CX<R>>& X) {
+    CFact<R> F = cid_core<R>(ctx, o, t, mm, nn, X, rs, false);
+    std::vector<int64_t> idx(F.k);
+    to_host(ctx, idx.data(), F.jpvt, F.k);
+    LRA_CUDA(cudaStreamSynchronize(ctx->stream));
+    return idx;
+  };
+  lra_cur* r = static_cast<lra_cur*>(hmalloc(sizeof(lra_cur)));
+  std::memset(r, 0, sizeof *r);
+  std::vector<int64_t> rows, cols;
+  if (m == n && cis_hermitian<R>(ctx, n, A.p, A.ld)) {
+    cols = sel('n', m, n, A);
+    rows = cols;
+    r->kind = 1;
+  } else if (m >= n) {
+    rows = sel('c', m, n, A);
+    const int64_t kr = (int64_t)rows.size();
+    int64_t* drows = ctx->arena.alloc_n<int64_t>(std::max<int64_t>(kr, 1));
+    LRA_CUDA(cudaMemcpyAsync(drows, rows.data(), kr * sizeof(int64_t), cudaMemcpyHostToDevice, ctx->stream));
+    CX<R>* Ar = ctx->arena.alloc_n<CX<R>>((size_t)std::max<int64_t>(kr, 1) * std::max<int64_t>(n, 1));
+    gather_rows<CX<R>>(ctx, kr, n, A.p, A.ld, drows, Ar, std::max<int64_t>(kr, 1));
+    cols = sel('n', kr, n, DMat<CX<R>>{Ar, std::max<int64_t>(kr, 1)});
+  } else {
+    cols = sel('n', m, n, A);
+    const int64_t kc = (int64_t)cols.size();
+    int64_t* dcols = ctx->arena.alloc_n<int64_t>(std::max<int64_t>(kc, 1));
+    LRA_CUDA(cudaMemcpyAsync(dcols, cols.data(), kc * sizeof(int64_t), cudaMemcpyHostToDevice, ctx->stream));
+    CX<R>* Ac = ctx->arena.alloc_n<CX<R>>((size_t)std::max<int64_t>(m, 1) * std::max<int64_t>(kc, 1));
+    gather_cols<CX<R>>(ctx, m, kc, A.p, A.ld, dcols, Ac, std::max<int64_t>(m, 1));
+    rows = sel('c', m, kc, DMat<CX<R>>{Ac, std::max<int64_t>(m, 1)});
+  }
+  if (r->kind == 0) {
+    const size_t k = std::min(rows.size(), cols.size());
+    rows.resize(k);
+    cols.resize(k);
+  }
+  r->kr = (int64_t)rows.size();
+  r->kc = (int64_t)cols.size();
+  r->rows = static_cast<int64_t*>(hmalloc(sizeof(int64_t) * std::max<size_t>(rows.size(), 1)));
+  r->cols = static_cast<int64_t*>(hmalloc(sizeof(int64_t) * std::max<size_t>(cols.size(), 1)));
+  std::memcpy(r->rows, rows.data(), rows.size() * sizeof(int64_t));
+  std::memcpy(r->cols, cols.data(), cols.size() * sizeof(int64_t));
+  return r;
+}
+
+// prange (src/prange.jl:14-77)
+template <typename R>
+lra_pqr* cprange(lra_ctx* ctx, const lra_opts& o, char t, int64_t m, int64_t n, const DMat<CX<R>>& A, RandSrc& rs,
+                 int dtype) {
+  if (t == 'b') {
+    if (m != n) fail(LRA_EDIM, "prange(:b): the matrix must be square");
+    if (cis_hermitian<R>(ctx, n, A.p, A.ld)) t = 'n';
+  }
+  auto side_q = [&](char tr, int64_t& k, CX<R>** R11) -> CX<R>* {
+    const int64_t M = tr == 'n' ? m : n, N = tr == 'n' ? n : m;
+    CFact<R> F;
+    if (o.sketch == LRA_SKETCH_NONE) {
+      CX<R>* B = cdense_op<R>(ctx, tr, m, n, A);
+      F = cpqr_backend<R>(ctx, o, B, M, N, std::max<int64_t>(M, 1));
+    } else {
+      F = sketchfact_c<R>(ctx, o, tr, true, M, N, A.p, A.ld, rs);
+    }
+    if (R11 && o.maxdet_tol >= 0) {
+      lra_opts oq = o;
+      oq.pqrfact_retval = LRA_RET_Q | LRA_RET_R;
+      cpostproc<R>(ctx, oq, F, false);
+    }
+    k = F.k;
+    const int64_t kk = std::max<int64_t>(k, 1);
+    if (R11) {
+      *R11 = ctx->arena.alloc_n<CX<R>>((size_t)kk * kk);
+      cresult_r11<R>(ctx, F, *R11);
+    }
+    corgqr<R>(ctx, M, k, F.B, F.ld, F.tau);
+    cmaxdet_rotate_q<R>(ctx, F, M, F.B, F.ld);
+    return F.B;
+  };
+  const int64_t M = t == 'c' ? n : m;
+  int64_t k = 0;
+  CX<R>* Q = nullptr;
+  if (t == 'b') {
+    int64_t kr = 0, kc = 0;
+    CX<R>*Rr = nullptr, *Rc = nullptr;
+    CX<R>* Qr = side_q('c', kr, &Rr);
+    CX<R>* Qc = side_q('n', kc, &Rc);
+    const int64_t kb = kr + kc;
+    CX<R>* Bc = ctx->arena.alloc_n<CX<R>>((size_t)std::max<int64_t>(M, 1) * std::max<int64_t>(kb, 1));
+    if (kr > 0) cgemm<R>(ctx, 'n', 'n', M, kr, kr, CX<R>(1), Qr, M, Rr, kr, CX<R>(0), Bc, M);
+    if (kc > 0) cgemm<R>(ctx, 'n', 'n', M, kc, kc, CX<R>(1), Qc, M, Rc, kc, CX<R>(0), Bc + kr * M, M);
+    CFact<R> F = cpqr_backend<R>(ctx, o, Bc, M, kb, std::max<int64_t>(M, 1));
+    k = F.k;
+    corgqr<R>(ctx, M, k, F.B, F.ld, F.tau);
+    Q = F.B;
+  } else if (o.sketch == LRA_SKETCH_SUB) {
+    const int64_t N = t == 'n' ? n : m;
+    CFact<R> F = sketchfact_c<R>(ctx, o, t, false, M, N, A.p, A.ld, rs);
+    if (o.maxdet_tol >= 0) {
+      lra_opts oq = o;
+      oq.pqrfact_retval = LRA_RET_Q;
+      cpostproc<R>(ctx, oq, F, false);
+    }
+    const int64_t kc = F.k, kq = std::min(M, kc);
+    Q = cgetcols<R>(ctx, t, m, n, A, F.jpvt, kc);
+    if (kq > 0) orthcols_c<R>(ctx, M, kc, Q);
+    k = kq;
+  } else {
+    Q = side_q(t, k, nullptr);
+  }
+  lra_pqr* r = new_pqr<R>(dtype, M, k, k);
+  for (int64_t i = 0; i < k; ++i) r->p[i] = i + 1;
+  r->Q = hmalloc(sizeof(CX<R>) * std::max<int64_t>(M * k, 1));
+  if (k > 0 && M > 0) to_host(ctx, r->Q, Q, (size_t)M * k);
+  r->retval = LRA_RET_Q;
+  LRA_CUDA(cudaStreamSynchronize(ctx->stream));
+  return r;
+}
+
+// snorm / snormdiff power iteration (src/snorm.jl:14-53), complex vectors
+template <typename R, class FwdFn, class AdjFn>
+double csnorm_loop(lra_ctx* ctx, const lra_opts& o, int64_t m, int64_t n, bool herm, RandSrc& rs, FwdFn fwd,
+                   AdjFn adj) {
+  CX<R>* xn = ctx->arena.alloc_n<CX<R>>(std::max<int64_t>(n, 1));
+  CX<R>* xm = ctx->arena.alloc_n<CX<R>>(std::max<int64_t>(m, 1));
+  R* nrm = ctx->arena.alloc_n<R>(1);
+  cgauss<R>(rs, n, xn);
+  auto norm = [&](const CX<R>* x, int64_t len) {
+    ccol_norms<R>(ctx, len, 1, x, std::max<int64_t>(len, 1), nrm);
+    R h = 0;
+    to_host(ctx, &h, nrm, 1);
+    LRA_CUDA(cudaStreamSynchronize(ctx->stream));
+    return (double)h;
+  };
+  double xnrm = norm(xn, n);
+  double s = 1, t = 0;
+  int64_t niter = 0;
+  while (s > 0 && std::fabs(s - t) > std::max(o.atol, t * o.rtol)) {
+    if (niter == o.snorm_niter) break;
+    ++niter;
+    scale_vec<R>(ctx, 2 * n, reinterpret_cast<R*>(xn), (R)(1.0 / xnrm));
+    if (herm) {
+      fwd(xn, xm);
+      copy_matrix<CX<R>>(ctx, n, 1, xm, std::max<int64_t>(n, 1), xn, std::max<int64_t>(n, 1));
+    } else {
+      fwd(xn, xm);
+      adj(xm, xn);
+    }
+    xnrm = norm(xn, n);
+    t = s;
+    s = herm ? xnrm : std::sqrt(xnrm);
+  }
+  return s;
+}
+
+
+template <typename R>
+double csnormdiff_dense(lra_ctx* ctx, const lra_opts& o, int64_t m, int64_t n, const CX<R>* A, int64_t lda,
+                        const CX<R>* B, int64_t ldb, bool herm, RandSrc& rs) {
+  const CX<R> one(1), mone(-1), zero(0);
+  const int64_t lm = std::max<int64_t>(m, 1), ln = std::max<int64_t>(n, 1);
+  return csnorm_loop<R>(
+      ctx, o, m, n, herm, rs,
+      [&](const CX<R>* x, CX<R>* y) {
+        cgemm<R>(ctx, 'n', 'n', m, 1, n, one, A, lda, x, ln, zero, y, lm);
+        cgemm<R>(ctx, 'n', 'n', m, 1, n, mone, B, ldb, x, ln, one, y, lm);
+      },
+      [&](const CX<R>* y, CX<R>* x) {
+        cgemm<R>(ctx, 'c', 'n', n, 1, m, one, A, lda, y, lm, zero, x, ln);
+        cgemm<R>(ctx, 'c', 'n', n, 1, m, mone, B, ldb, y, lm, one, x, ln);
+      });
+}
+
+// the middle factor of CUR(A, U) (src/cur.jl:85-115): the pseudo-inverse of
+// W = A[rows, cols] = Uw diag(S) Vw^H as the PartialSVD (Vw, 1 ./ S, Uw^H)
+template <typename R>
+lra_psvd* ccur_middle(lra_ctx* ctx, int64_t m, int64_t n, const void* A, int64_t lda, int64_t k,
+                      const int64_t* rows, const int64_t* cols, int dtype) {
+  const int64_t kk = std::max<int64_t>(k, 1);
+  DMat<CX<R>> dA = stage_in<CX<R>>(ctx, A, m, n, lda);
+  CX<R>* W = ctx->arena.alloc_n<CX<R>>((size_t)kk * kk);
+  if (k > 0) {
+    int64_t* dr = ctx->arena.alloc_n<int64_t>(kk);
+    int64_t* dc = ctx->arena.alloc_n<int64_t>(kk);
+    LRA_CUDA(cudaMemcpyAsync(dr, rows, k * sizeof(int64_t), cudaMemcpyHostToDevice, ctx->stream));
+    LRA_CUDA(cudaMemcpyAsync(dc, cols, k * sizeof(int64_t), cudaMemcpyHostToDevice, ctx->stream));
+    CX<R>* Ac = ctx->arena.alloc_n<CX<R>>((size_t)std::max<int64_t>(m, 1) * kk);
+    gather_cols<CX<R>>(ctx, m, k, dA.p, dA.ld, dc, Ac, std::max<int64_t>(m, 1));
+    gather_rows<CX<R>>(ctx, k, k, Ac, std::max<int64_t>(m, 1), dr, W, kk);
+  }
+  CX<R>* Uw = ctx->arena.alloc_n<CX<R>>((size_t)kk * kk);
+  CX<R>* Vw = ctx->arena.alloc_n<CX<R>>((size_t)kk * kk);
+  std::vector<R> hS = csmall_svd<R>(ctx, k, W, kk, Uw, Vw);
+  lra_psvd* r = static_cast<lra_psvd*>(hmalloc(sizeof(lra_psvd)));
+  std::memset(r, 0, sizeof *r);
+  r->dtype = dtype;
+  r->m = k;
+  r->n = k;
+  r->k = k;
+  r->S = hmalloc(sizeof(R) * kk);
+  for (int64_t i = 0; i < k; ++i) static_cast<R*>(r->S)[i] = hS[i] > R(0) ? R(1) / hS[i] : R(0);
+  CX<R>* Uh = ctx->arena.alloc_n<CX<R>>((size_t)kk * kk);
+  cadjoint<R>(ctx, k, k, Uw, kk, Uh, kk);
+  r->U = hmalloc(sizeof(CX<R>) * (size_t)kk * kk);
+  r->Vt = hmalloc(sizeof(CX<R>) * (size_t)kk * kk);
+  to_host(ctx, r->U, Vw, (size_t)k * k);
+  to_host(ctx, r->Vt, Uh, (size_t)k * k);
+  LRA_CUDA(cudaStreamSynchronize(ctx->stream));
+  return r;
+}
+}  // namespace
+}  // namespace lra
+
 extern "C" {
 
 const char* lra_status_string(int s) {
@@ -1050,8 +2116,26 @@ int lra_ctx_create(int device, lra_ctx** out) {
     return LRA_ECUDA;
   }
   c->own_stream = true;
+  load_tuning(&c->tuning, &c->tuning_source);
   *out = c;
   return LRA_OK;
+}
+
+int lra_ctx_set_tuning(lra_ctx* ctx, const char* key, int64_t index, int64_t value) {
+  if (!ctx) return LRA_EINVAL;
+  if (!key || !set_tuning(&ctx->tuning, key, index, value)) {
+    ctx->last_error = "unknown tuning key or value out of range";
+    return LRA_EINVAL;
+  }
+  return LRA_OK;
+}
+
+int lra_ctx_get_tuning(const lra_ctx* ctx, char* buf, int64_t len) {
+  if (!ctx) return LRA_EINVAL;
+  const std::string s = "# source: " + ctx->tuning_source + "\n" + tuning_text(ctx->tuning);
+  if (!buf || len <= 0) return (int)s.size() + 1;
+  std::snprintf(buf, (size_t)len, "%s", s.c_str());
+  return (int)s.size() + 1;
 }
 
 void lra_ctx_destroy(lra_ctx* ctx) {
@@ -1090,11 +2174,42 @@ int lra_ctx_stage_ms(const lra_ctx* ctx, double out[4]) {
   return LRA_OK;
 }
 
+int lra_ctx_set_wait_limit(lra_ctx* ctx, int64_t ns) {
+  if (!ctx) return LRA_EINVAL;
+  if (ns < 0) {
+    ctx->last_error = "wait limit < 0";
+    return LRA_EINVAL;
+  }
+  if (cudaSetDevice(ctx->device) != cudaSuccess || cudaStreamSynchronize(ctx->stream) != cudaSuccess ||
+      set_wait_limit_qr((uint64_t)ns) != cudaSuccess || set_wait_limit_dense((uint64_t)ns) != cudaSuccess ||
+      set_wait_limit_tc((uint64_t)ns) != cudaSuccess) {
+    ctx->last_error = cudaGetErrorString(cudaGetLastError());
+    return LRA_ECUDA;
+  }
+  ctx->last_error.clear();
+  return LRA_OK;
+}
+
+int lra_ctx_probe_wait(lra_ctx* ctx) {
+  int returned = 0, err = 0;
+  const int st = guarded(ctx, [&] { err = probe_grid_wait(ctx, &returned); });
+  if (st != LRA_OK) return st;
+  if (err == 4 && returned == 2) {
+    ctx->last_error = "probe: the grid barrier's bounded wait ran out and both CTAs returned";
+    return LRA_ETIMEDOUT;
+  }
+  char msg[128];
+  std::snprintf(msg, sizeof msg, "probe: unexpected barrier state (err %d, %d CTAs returned)", err, returned);
+  ctx->last_error = msg;
+  return LRA_ECUDA;
+}
+
 int lra_opts_init(lra_opts* o, int dtype) {
   if (!o) return LRA_EINVAL;
-  if (dtype != LRA_F32 && dtype != LRA_F64) return LRA_EINVAL;
+  if (dtype != LRA_F32 && dtype != LRA_F64 && dtype != LRA_C32 && dtype != LRA_C64) return LRA_EINVAL;
   std::memset(o, 0, sizeof *o);
-  const double eps = dtype == LRA_F64 ? 2.220446049250313e-16 : 1.1920928955078125e-07;
+  // eps(real(T)) (src/LowRankApprox.jl:96-119)
+  const double eps = (dtype == LRA_F64 || dtype == LRA_C64) ? 2.220446049250313e-16 : 1.1920928955078125e-07;
   o->atol = 0;
   o->maxdet_niter = -1;
   o->maxdet_tol = -1;
@@ -1139,6 +2254,25 @@ int lra_sketch(lra_ctx* ctx, int dtype, char side, char trans, int64_t m, int64_
     if (side != 'l' && side != 'r' && side != 'L' && side != 'R') fail(LRA_EINVAL, "side");
     lra_opts o = *opts;
     if (o.sketch == LRA_SKETCH_NONE) o.sketch = LRA_SKETCH_RANDN;  // src/sketch.jl:68-74
+    if (is_cplx(dtype)) {
+      dispatch_c(dtype, [&](auto z) {
+        using R = decltype(z);
+        DMat<CX<R>> dA = stage_in<CX<R>>(ctx, A, m, n, lda);
+        check_input_c<R>(ctx, o, m, n, dA);
+        RandSrc rs(ctx, rand, o.seed);
+        const bool left = side == 'l' || side == 'L';
+        const int64_t M = t == 'n' ? m : n, N = t == 'n' ? n : m;
+        const int64_t rows = left ? order : M, cols = left ? N : order;
+        if (ldb < std::max<int64_t>(rows, 1)) fail(LRA_EDIM, "ldb");
+        CX<R>* Bd = ctx->arena.alloc_n<CX<R>>((size_t)std::max<int64_t>(rows, 1) * std::max<int64_t>(cols, 1));
+        make_sketch_c<R>(ctx, o, t, M, N, dA.p, dA.ld, order, rs, Bd, !left);
+        if (rows > 0 && cols > 0)
+          LRA_CUDA(cudaMemcpy2DAsync(B, ldb * sizeof(CX<R>), Bd, std::max<int64_t>(rows, 1) * sizeof(CX<R>),
+                                     rows * sizeof(CX<R>), cols,
+                                     is_dev(B) ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost, ctx->stream));
+      });
+      return;
+    }
     dispatch(dtype, [&](auto z) {
       using T = decltype(z);
       DMat<T> dA = stage_in<T>(ctx, A, m, n, lda);
@@ -1173,6 +2307,16 @@ int lra_geqp3_adap(lra_ctx* ctx, int dtype, int64_t m, int64_t n, void* B, int64
     if (m > 0 && n > 0 && (!is_dev(B) || !is_dev(jpvt) || !is_dev(tau)))
       fail(LRA_EINVAL, "lra_geqp3_adap works on device buffers");
     if (ldb < std::max<int64_t>(1, m)) fail(LRA_EDIM, "ldb");
+    if (is_cplx(dtype)) {
+      dispatch_c(dtype, [&](auto z) {
+        using R = decltype(z);
+        const int64_t l = std::min(m, n);
+        const int64_t kmax = (opts->rank < 0 || opts->rank > l) ? l : opts->rank;
+        *k = cgeqp3<R>(ctx, m, n, static_cast<CX<R>*>(B), ldb, jpvt, static_cast<CX<R>*>(tau), kmax, opts->nb,
+                       opts->atol, opts->rtol, true);
+      });
+      return;
+    }
     dispatch(dtype, [&](auto z) {
       using T = decltype(z);
       const int64_t l = std::min(m, n);
@@ -1214,7 +2358,25 @@ int lra_geqp3_adap_noalloc(lra_ctx* ctx, int dtype, int64_t m, int64_t n, void* 
     cudaStreamSynchronize(ctx->stream);
     cudaGetLastError();
     return e.status;
+  } catch (const std::bad_alloc&) {
+    ctx->last_error = "host allocation failed";
+    return LRA_ENOMEM;
+  } catch (...) {
+    ctx->last_error = "unexpected exception";
+    return LRA_ECUDA;
   }
+}
+
+int lra_rand_gauss(lra_ctx* ctx, uint64_t seed, uint64_t counter, int64_t n, double* out) {
+  return guarded(ctx, [&] {
+    if (n < 0) fail(LRA_EINVAL, "n < 0");
+    if (n == 0) return;
+    if (!out) fail(LRA_EINVAL, "out is NULL");
+    double* d = is_dev(out) ? out : ctx->arena.alloc_n<double>(n);
+    sketch_philox<double>(ctx, seed, counter, n, d);
+    if (d != out)
+      LRA_CUDA(cudaMemcpyAsync(out, d, (size_t)n * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
+  });
 }
 
 int lra_dgemm(lra_ctx* ctx, int precision, char transa, char transb, int64_t m, int64_t n, int64_t k,
@@ -1250,6 +2412,17 @@ int lra_idfact(lra_ctx* ctx, int dtype, char trans, int64_t m, int64_t n, const 
     const char t = chktrans(trans);
     lra_opts o = *opts;
     o.pqrfact_retval = LRA_RET_T;  // src/id.jl:437
+    if (is_cplx(dtype)) {
+      dispatch_c(dtype, [&](auto z) {
+        using R = decltype(z);
+        DMat<CX<R>> dA = stage_in<CX<R>>(ctx, A, m, n, lda);
+        check_input_c<R>(ctx, o, m, n, dA);
+        RandSrc rs(ctx, rand, o.seed);
+        CFact<R> F = cid_core<R>(ctx, o, t, m, n, dA, rs, true);
+        *out = cpack_id<R>(ctx, F, dtype);
+      });
+      return;
+    }
     dispatch(dtype, [&](auto z) {
       using T = decltype(z);
       DMat<T> dA = stage_in<T>(ctx, A, m, n, lda);
@@ -1275,6 +2448,16 @@ int lra_sketchfact(lra_ctx* ctx, int dtype, char side, char trans, int64_t m, in
     const bool left = side == 'l' || side == 'L';
     lra_opts o = *opts;
     if (o.sketch == LRA_SKETCH_NONE) o.sketch = LRA_SKETCH_RANDN;
+    if (is_cplx(dtype)) {
+      dispatch_c(dtype, [&](auto z) {
+        using R = decltype(z);
+        DMat<CX<R>> dA = stage_in<CX<R>>(ctx, A, m, n, lda);
+        check_input_c<R>(ctx, o, m, n, dA);
+        RandSrc rs(ctx, rand, o.seed);
+        *out = csketchfact<R>(ctx, o, side, t, m, n, dA, rs, dtype);
+      });
+      return;
+    }
     dispatch(dtype, [&](auto z) {
       using T = decltype(z);
       DMat<T> dA = stage_in<T>(ctx, A, m, n, lda);
@@ -1299,8 +2482,14 @@ int lra_sketchfact(lra_ctx* ctx, int dtype, char side, char trans, int64_t m, in
       const int64_t k = F.k;
       if (rr) {
         T* R = ctx->arena.alloc_n<T>((size_t)std::max<int64_t>(k * N, 1));
-        copy_matrix(ctx, k, N, F.B, F.ld, R, std::max<int64_t>(k, 1));
-        zero_lower(ctx, k, N, R, std::max<int64_t>(k, 1));
+        if (F.r1) {
+          // after maxdet swaps: R = [R1 | R1 T] with R1 re-factored (src/pqr.jl:469-474)
+          result_r11<T>(ctx, F, R);
+          if (N > k) gemm<T>(ctx, 'n', 'n', k, N - k, k, T(1), R, k, F.T_, k, T(0), R + k * k, k);
+        } else {
+          copy_matrix(ctx, k, N, F.B, F.ld, R, std::max<int64_t>(k, 1));
+          zero_lower(ctx, k, N, R, std::max<int64_t>(k, 1));
+        }
         r->R = hmalloc(sizeof(T) * std::max<int64_t>(k * N, 1));
         to_host(ctx, r->R, R, (size_t)k * N);
         r->retval |= LRA_RET_R;
@@ -1312,6 +2501,7 @@ int lra_sketchfact(lra_ctx* ctx, int dtype, char side, char trans, int64_t m, in
       }
       if (rq) {
         orgqr(ctx, F.order, k, F.B, F.ld, F.tau);
+        maxdet_rotate_q<T>(ctx, F, F.order, F.B, F.ld);
         r->Q = hmalloc(sizeof(T) * std::max<int64_t>(F.order * k, 1));
         if (k > 0)
           LRA_CUDA(cudaMemcpy2DAsync(r->Q, F.order * sizeof(T), F.B, F.ld * sizeof(T), F.order * sizeof(T), k,
@@ -1335,7 +2525,16 @@ int lra_prange(lra_ctx* ctx, int dtype, char trans, int64_t m, int64_t n, const 
     if (!out) fail(LRA_EINVAL, "out is NULL");
     char t = (trans == 'b' || trans == 'B') ? 'b' : chktrans(trans);  // prange_chktrans, src/prange.jl:79-80
     const lra_opts& o = *opts;
-    if (o.maxdet_tol >= 0) fail(LRA_ENOTSUP, "prange with maxdet_tol >= 0 is not built");
+    if (is_cplx(dtype)) {
+      dispatch_c(dtype, [&](auto z) {
+        using R = decltype(z);
+        DMat<CX<R>> dA = stage_in<CX<R>>(ctx, A, m, n, lda);
+        check_input_c<R>(ctx, o, m, n, dA);
+        RandSrc rs(ctx, rand, o.seed);
+        *out = cprange<R>(ctx, o, t, m, n, dA, rs, dtype);
+      });
+      return;
+    }
     dispatch(dtype, [&](auto z) {
       using T = decltype(z);
       DMat<T> dA = stage_in<T>(ctx, A, m, n, lda);
@@ -1347,7 +2546,11 @@ int lra_prange(lra_ctx* ctx, int dtype, char trans, int64_t m, int64_t n, const 
       }
       // one side's factorization (src/prange.jl:26-31, 47-52): the pivoted QR
       // of op(A) itself (sketch :none) or of the right sketch op(A) S; Q
-      // (M x k, ld M) replaces the reflectors, and R11 is kept on request
+      // (M x k, ld M) replaces the reflectors, and R11 is kept on request.
+      // With maxdet_tol >= 0 the :b form asks for "qr" (src/prange.jl:25), so
+      // the swaps re-factor R1 and rotate Q; with Q alone (:n, :c) they
+      // leave Q as it is (maxdet_swapcols!, src/pqr.jl:467-468) and are
+      // skipped.
       auto side_q = [&](char tr, int64_t& k, T** R11) -> T* {
         const int64_t M = tr == 'n' ? m : n, N = tr == 'n' ? n : m;
         Fact<T> F;
@@ -1357,14 +2560,19 @@ int lra_prange(lra_ctx* ctx, int dtype, char trans, int64_t m, int64_t n, const 
         } else {
           F = sketchfact_right_dev<T>(ctx, o, tr, M, N, dA.p, dA.ld, rs, dtype);
         }
+        if (R11 && o.maxdet_tol >= 0) {
+          lra_opts oq = o;
+          oq.pqrfact_retval = LRA_RET_Q | LRA_RET_R;
+          postproc_t<T>(ctx, oq, F, false);
+        }
         k = F.k;
         const int64_t kk = std::max<int64_t>(k, 1);
         if (R11) {
           *R11 = ctx->arena.alloc_n<T>((size_t)kk * kk);
-          copy_matrix(ctx, k, k, F.B, F.ld, *R11, kk);
-          zero_lower(ctx, k, k, *R11, kk);
+          result_r11<T>(ctx, F, *R11);
         }
         orgqr(ctx, M, k, F.B, F.ld, F.tau);
+        maxdet_rotate_q<T>(ctx, F, M, F.B, F.ld);
         return F.B;
       };
       const int64_t M = t == 'c' ? n : m;
@@ -1390,6 +2598,12 @@ int lra_prange(lra_ctx* ctx, int dtype, char trans, int64_t m, int64_t n, const 
         // from the left sketch, made orthonormal (orthcols!, src/util.jl)
         const int64_t N = t == 'n' ? n : m;
         Fact<T> F = sketchfact_dev<T>(ctx, o, t, M, N, dA.p, dA.ld, rs, dtype);
+        if (o.maxdet_tol >= 0) {
+          // the swaps move the skeleton columns prange_sub takes
+          lra_opts oq = o;
+          oq.pqrfact_retval = LRA_RET_Q;
+          postproc_t<T>(ctx, oq, F, false);
+        }
         const int64_t kc = F.k, kq = std::min(M, kc);
         Q = getcols<T>(ctx, t, m, n, dA, F.jpvt, kc);
         int64_t* jp = ctx->arena.alloc_n<int64_t>(std::max<int64_t>(kc, 1));
@@ -1432,6 +2646,16 @@ int lra_pqrfact(lra_ctx* ctx, int dtype, char trans, int64_t m, int64_t n, const
     if (!out) fail(LRA_EINVAL, "out is NULL");
     const char t = chktrans(trans);
     const lra_opts& o = *opts;
+    if (is_cplx(dtype)) {
+      dispatch_c(dtype, [&](auto z) {
+        using R = decltype(z);
+        DMat<CX<R>> dA = stage_in<CX<R>>(ctx, A, m, n, lda);
+        check_input_c<R>(ctx, o, m, n, dA);
+        RandSrc rs(ctx, rand, o.seed);
+        *out = cpqrfact<R>(ctx, o, t, m, n, dA, rs, dtype);
+      });
+      return;
+    }
     dispatch(dtype, [&](auto z) {
       using T = decltype(z);
       DMat<T> dA = stage_in<T>(ctx, A, m, n, lda);
@@ -1458,9 +2682,10 @@ int lra_pqrfact(lra_ctx* ctx, int dtype, char trans, int64_t m, int64_t n, const
           postproc_t<T>(ctx, oo, F, rt || rr);
           const int64_t k = F.k;
           R11 = ctx->arena.alloc_n<T>((size_t)std::max<int64_t>(k * k, 1));
-          copy_matrix(ctx, k, k, F.B, F.ld, R11, std::max<int64_t>(k, 1));
+          result_r11<T>(ctx, F, R11);
           if (rq) {
             orgqr(ctx, M, k, F.B, F.ld, F.tau);
+            maxdet_rotate_q<T>(ctx, F, M, F.B, F.ld);
             Qd = F.B;
           }
         } else {
@@ -1744,6 +2969,16 @@ int lra_psvdfact(lra_ctx* ctx, int dtype, int64_t m, int64_t n, const void* A, i
     ctx->mixed_rtol = ctx->gemm_tc ? opts->rtol : 0.0;
     check_dims(m, n);
     if (!out) fail(LRA_EINVAL, "out is NULL");
+    if (is_cplx(dtype)) {
+      dispatch_c(dtype, [&](auto z) {
+        using R = decltype(z);
+        DMat<CX<R>> dA = stage_in<CX<R>>(ctx, A, m, n, lda);
+        check_input_c<R>(ctx, *opts, m, n, dA);
+        RandSrc rs(ctx, rand, opts->seed);
+        *out = cpsvd<R>(ctx, *opts, m, n, dA, rs, dtype, vals_only != 0);
+      });
+      return;
+    }
     dispatch(dtype, [&](auto z) {
       using T = decltype(z);
       DMat<T> dA = stage_in<T>(ctx, A, m, n, lda);
@@ -1784,6 +3019,18 @@ int lra_pheigfact(lra_ctx* ctx, int dtype, int64_t n, const void* A, int64_t lda
     check_dims(n, n);
     if (!out) fail(LRA_EINVAL, "out is NULL");
     const lra_opts& o = *opts;
+    if (is_cplx(dtype)) {
+      dispatch_c(dtype, [&](auto z) {
+        using R = decltype(z);
+        DMat<CX<R>> dA = stage_in<CX<R>>(ctx, A, n, n, lda);
+        check_input_c<R>(ctx, o, n, n, dA);
+        const bool herm = ctx->linop ? ctx->linop->hermitian != 0 : cis_hermitian<R>(ctx, n, dA.p, dA.ld);
+        if (!herm) fail(LRA_ENOTHERM, "matrix must be Hermitian");
+        RandSrc rs(ctx, rand, o.seed);
+        *out = cpheig<R>(ctx, o, n, dA, rs, dtype, vals_only != 0);
+      });
+      return;
+    }
     dispatch(dtype, [&](auto z) {
       using T = decltype(z);
       DMat<T> dA = stage_in<T>(ctx, A, n, n, lda);
@@ -1819,10 +3066,16 @@ int lra_pheigfact(lra_ctx* ctx, int dtype, int64_t n, const void* A, int64_t lda
         zero_lower(ctx, k, k, R, ldk);
       }
       // B = R (A[sk, sk] R')
-      T* Ar = ctx->arena.alloc_n<T>((size_t)ldk * ldn);
-      gather_rows(ctx, k, n, dA.p, dA.ld, F.jpvt, Ar, ldk);
       T* Ass = ctx->arena.alloc_n<T>((size_t)ldk * ldk);
-      gather_cols(ctx, k, k, Ar, ldk, F.jpvt, Ass, ldk);
+      if (ctx->linop) {
+        // an operator's A[sk, sk]: rows sk of A[:, sk] (src/linop.jl:73-77)
+        T* Ac = getcols<T>(ctx, 'n', n, n, dA, F.jpvt, k);
+        gather_rows(ctx, k, k, Ac, ldn, F.jpvt, Ass, ldk);
+      } else {
+        T* Ar = ctx->arena.alloc_n<T>((size_t)ldk * ldn);
+        gather_rows(ctx, k, n, dA.p, dA.ld, F.jpvt, Ar, ldk);
+        gather_cols(ctx, k, k, Ar, ldk, F.jpvt, Ass, ldk);
+      }
       T* C = ctx->arena.alloc_n<T>((size_t)ldk * ldk);
       gemm<T>(ctx, 'n', 't', k, k, k, T(1), Ass, ldk, R, ldk, T(0), C, ldk);
       T* B = ctx->arena.alloc_n<T>((size_t)ldk * ldk);
@@ -1933,9 +3186,16 @@ int lra_cur_middle(lra_ctx* ctx, int dtype, int64_t m, int64_t n, const void* A,
     check_dims(m, n);
     if (!out || (k > 0 && (!rows || !cols))) fail(LRA_EINVAL, "NULL argument");
     if (k < 0 || k > std::min(m, n)) fail(LRA_EDIM, "k");
-    if (dtype != LRA_F32 && dtype != LRA_F64) fail(LRA_EINVAL, "dtype");
+    if (dtype != LRA_F32 && dtype != LRA_F64 && !is_cplx(dtype)) fail(LRA_EINVAL, "dtype");
     for (int64_t i = 0; i < k; ++i)
       if (rows[i] < 1 || rows[i] > m || cols[i] < 1 || cols[i] > n) fail(LRA_EINVAL, "row or column index");
+    if (is_cplx(dtype)) {
+      dispatch_c(dtype, [&](auto z) {
+        using R = decltype(z);
+        *out = ccur_middle<R>(ctx, m, n, A, lda, k, rows, cols, dtype);
+      });
+      return;
+    }
     dispatch(dtype, [&](auto z) {
       using T = decltype(z);
       const int64_t kk = std::max<int64_t>(k, 1);
@@ -1996,6 +3256,16 @@ int lra_curfact(lra_ctx* ctx, int dtype, int64_t m, int64_t n, const void* A, in
     if (!out) fail(LRA_EINVAL, "out is NULL");
     lra_opts o = *opts;
     o.pqrfact_retval = 0;  // src/cur.jl:534
+    if (is_cplx(dtype)) {
+      dispatch_c(dtype, [&](auto z) {
+        using R = decltype(z);
+        DMat<CX<R>> dA = stage_in<CX<R>>(ctx, A, m, n, lda);
+        check_input_c<R>(ctx, o, m, n, dA);
+        RandSrc rs(ctx, rand, o.seed);
+        *out = ccurfact<R>(ctx, o, m, n, dA, rs);
+      });
+      return;
+    }
     dispatch(dtype, [&](auto z) {
       using T = decltype(z);
       DMat<T> dA = stage_in<T>(ctx, A, m, n, lda);
@@ -2021,15 +3291,28 @@ int lra_curfact(lra_ctx* ctx, int dtype, int64_t m, int64_t n, const void* A, in
         int64_t* drows = ctx->arena.alloc_n<int64_t>(std::max<int64_t>(kr, 1));
         LRA_CUDA(cudaMemcpyAsync(drows, rows.data(), kr * sizeof(int64_t), cudaMemcpyHostToDevice, ctx->stream));
         T* Ar = ctx->arena.alloc_n<T>((size_t)std::max<int64_t>(kr, 1) * std::max<int64_t>(n, 1));
-        gather_rows(ctx, kr, n, dA.p, dA.ld, drows, Ar, std::max<int64_t>(kr, 1));
+        if (ctx->linop) {
+          // an operator's A[rows, :] is (A' E)' (src/linop.jl:64-71), a dense matrix
+          T* Art = getcols<T>(ctx, 'c', m, n, dA, drows, kr);
+          transpose(ctx, n, kr, Art, std::max<int64_t>(n, 1), Ar, std::max<int64_t>(kr, 1));
+        } else {
+          gather_rows(ctx, kr, n, dA.p, dA.ld, drows, Ar, std::max<int64_t>(kr, 1));
+        }
+        DenseScope dense(ctx);
         cols = sel('n', kr, n, DMat<T>{Ar, std::max<int64_t>(kr, 1)});
       } else {
         cols = sel('n', m, n, dA);
         const int64_t kc = (int64_t)cols.size();
         int64_t* dcols = ctx->arena.alloc_n<int64_t>(std::max<int64_t>(kc, 1));
         LRA_CUDA(cudaMemcpyAsync(dcols, cols.data(), kc * sizeof(int64_t), cudaMemcpyHostToDevice, ctx->stream));
-        T* Ac = ctx->arena.alloc_n<T>((size_t)std::max<int64_t>(m, 1) * std::max<int64_t>(kc, 1));
-        gather_cols(ctx, m, kc, dA.p, dA.ld, dcols, Ac, std::max<int64_t>(m, 1));
+        T* Ac;
+        if (ctx->linop) {
+          Ac = getcols<T>(ctx, 'n', m, n, dA, dcols, kc);
+        } else {
+          Ac = ctx->arena.alloc_n<T>((size_t)std::max<int64_t>(m, 1) * std::max<int64_t>(kc, 1));
+          gather_cols(ctx, m, kc, dA.p, dA.ld, dcols, Ac, std::max<int64_t>(m, 1));
+        }
+        DenseScope dense(ctx);
         rows = sel('c', m, kc, DMat<T>{Ac, std::max<int64_t>(m, 1)});
       }
       if (r->kind == 0) {
@@ -2097,6 +3380,58 @@ double snorm_loop(lra_ctx* ctx, const lra_opts& o, int64_t m, int64_t n, bool he
 }  // namespace
 }  // namespace lra
 
+// ---- matrix-free operators (LinearOperator, src/linop.jl:9-40) ----------------------
+namespace lra {
+namespace {
+
+// runs an entry point with ctx->linop = L and the options a matrix-free
+// input takes: the Gaussian sketch whatever opts->sketch says (chkopts!,
+// src/LowRankApprox.jl:142-148), in native precision (the products are the
+// operator's), and no finite check (its entries are never formed)
+template <class Fn>
+int with_linop(lra_ctx* ctx, const lra_linop* L, const lra_opts* opts, Fn&& call) {
+  if (!ctx) return LRA_EINVAL;
+  const char* bad = nullptr;
+  int st = LRA_EINVAL;
+  if (!L) {
+    bad = "operator is NULL";
+  } else if (!L->matmat) {
+    bad = "operator has no matmat";
+  } else if (L->m < 0 || L->n < 0) {
+    bad = "negative dimension";
+    st = LRA_EDIM;
+  } else if (L->dtype != LRA_F32 && L->dtype != LRA_F64) {
+    bad = "dtype";
+  } else if (L->hermitian && L->m != L->n) {
+    bad = "a Hermitian operator must be square";
+    st = LRA_EDIM;
+  } else if (!opts) {
+    bad = "opts is NULL";
+  }
+  if (bad) {
+    ctx->last_error = bad;
+    return st;
+  }
+  lra_opts o = *opts;
+  o.sketch = LRA_SKETCH_RANDN;
+  o.precision = LRA_PREC_NATIVE;
+  o.check_finite = 0;
+  ctx->linop = L;
+  int r = LRA_ECUDA;
+  try {
+    r = call(&o);
+  } catch (...) {
+    ctx->last_error = "unexpected exception";
+  }
+  ctx->linop = nullptr;
+  return r;
+}
+
+inline int64_t lin_ld(const lra_linop* L) { return std::max<int64_t>(L->m, 1); }
+
+}  // namespace
+}  // namespace lra
+
 extern "C" {
 
 int lra_snorm(lra_ctx* ctx, int dtype, int64_t m, int64_t n, const void* A, int64_t lda, int hermitian,
@@ -2105,16 +3440,42 @@ int lra_snorm(lra_ctx* ctx, int dtype, int64_t m, int64_t n, const void* A, int6
     chkopts(opts);
     check_dims(m, n);
     if (!out) fail(LRA_EINVAL, "out is NULL");
+    if (is_cplx(dtype)) {
+      dispatch_c(dtype, [&](auto z) {
+        using R = decltype(z);
+        DMat<CX<R>> dA = stage_in<CX<R>>(ctx, A, m, n, lda);
+        check_input_c<R>(ctx, *opts, m, n, dA);
+        const bool herm = hermitian < 0 ? (m == n && cis_hermitian<R>(ctx, n, dA.p, dA.ld)) : hermitian != 0;
+        RandSrc rs(ctx, rand, opts->seed);
+        const CX<R> one(1), zero(0);
+        *out = csnorm_loop<R>(
+            ctx, *opts, m, n, herm, rs,
+            [&](const CX<R>* x, CX<R>* y) { cgemm<R>(ctx, 'n', 'n', m, 1, n, one, dA.p, dA.ld, x, std::max<int64_t>(n, 1), zero, y, std::max<int64_t>(m, 1)); },
+            [&](const CX<R>* y, CX<R>* x) { cgemm<R>(ctx, 'c', 'n', n, 1, m, one, dA.p, dA.ld, y, std::max<int64_t>(m, 1), zero, x, std::max<int64_t>(n, 1)); });
+      });
+      return;
+    }
     dispatch(dtype, [&](auto z) {
       using T = decltype(z);
       DMat<T> dA = stage_in<T>(ctx, A, m, n, lda);
       check_input(ctx, *opts, m, n, dA);
       const bool herm = hermitian < 0 ? (m == n && is_symmetric(ctx, n, dA.p, dA.ld)) : hermitian != 0;
       RandSrc rs(ctx, rand, opts->seed);
+      const bool lin = ctx->linop != nullptr;
       *out = snorm_loop<T>(
           ctx, *opts, m, n, herm, rs,
-          [&](const T* x, T* y) { gemv<T>(ctx, 'n', m, n, T(1), dA.p, dA.ld, x, T(0), y); },
-          [&](const T* y, T* x) { gemv<T>(ctx, 't', m, n, T(1), dA.p, dA.ld, y, T(0), x); });
+          [&](const T* x, T* y) {
+            if (lin)
+              linop_apply<T>(ctx, 'n', 1, x, std::max<int64_t>(n, 1), y, std::max<int64_t>(m, 1));
+            else
+              gemv<T>(ctx, 'n', m, n, T(1), dA.p, dA.ld, x, T(0), y);
+          },
+          [&](const T* y, T* x) {
+            if (lin)
+              linop_apply<T>(ctx, 'c', 1, y, std::max<int64_t>(m, 1), x, std::max<int64_t>(n, 1));
+            else
+              gemv<T>(ctx, 't', m, n, T(1), dA.p, dA.ld, y, T(0), x);
+          });
     });
   });
 }
@@ -2125,6 +3486,17 @@ int lra_snormdiff(lra_ctx* ctx, int dtype, int64_t m, int64_t n, const void* A, 
     chkopts(opts);
     check_dims(m, n);
     if (!out) fail(LRA_EINVAL, "out is NULL");
+    if (is_cplx(dtype)) {
+      dispatch_c(dtype, [&](auto z) {
+        using R = decltype(z);
+        DMat<CX<R>> dA = stage_in<CX<R>>(ctx, A, m, n, lda);
+        DMat<CX<R>> dB = stage_in<CX<R>>(ctx, B, m, n, ldb);
+        const bool herm = m == n && cis_hermitian<R>(ctx, n, dA.p, dA.ld) && cis_hermitian<R>(ctx, n, dB.p, dB.ld);
+        RandSrc rs(ctx, rand, opts->seed);
+        *out = csnormdiff_dense<R>(ctx, *opts, m, n, dA.p, dA.ld, dB.p, dB.ld, herm, rs);
+      });
+      return;
+    }
     dispatch(dtype, [&](auto z) {
       using T = decltype(z);
       DMat<T> dA = stage_in<T>(ctx, A, m, n, lda);
@@ -2152,6 +3524,36 @@ int lra_snormdiff_id(lra_ctx* ctx, int dtype, char trans, int64_t m, int64_t n, 
     check_dims(m, n);
     if (!out || !F) fail(LRA_EINVAL, "NULL argument");
     const char t = chktrans(trans);
+    if (is_cplx(dtype)) {
+      dispatch_c(dtype, [&](auto z) {
+        using R = decltype(z);
+        if (F->dtype != dtype) fail(LRA_EINVAL, "dtype of F");
+        DMat<CX<R>> dA = stage_in<CX<R>>(ctx, A, m, n, lda);
+        const int64_t M = t == 'n' ? m : n, N = t == 'n' ? n : m;
+        if (F->n != N) fail(LRA_EDIM, "ID size");
+        const int64_t k = F->k, ldm = std::max<int64_t>(M, 1);
+        CX<R>* Aop = cdense_op<R>(ctx, t, m, n, dA);
+        int64_t* p = ctx->arena.alloc_n<int64_t>(std::max<int64_t>(N, 1));
+        LRA_CUDA(cudaMemcpyAsync(p, F->sk, k * sizeof(int64_t), cudaMemcpyHostToDevice, ctx->stream));
+        LRA_CUDA(cudaMemcpyAsync(p + k, F->rd, (N - k) * sizeof(int64_t), cudaMemcpyHostToDevice, ctx->stream));
+        CX<R>* Td = ctx->arena.alloc_n<CX<R>>((size_t)std::max<int64_t>(k * (N - k), 1));
+        if (k > 0 && N > k)
+          LRA_CUDA(cudaMemcpyAsync(Td, F->T, (size_t)k * (N - k) * sizeof(CX<R>), cudaMemcpyHostToDevice, ctx->stream));
+        CX<R>* Cm = ctx->arena.alloc_n<CX<R>>((size_t)ldm * std::max<int64_t>(k, 1));
+        gather_cols<CX<R>>(ctx, M, k, Aop, ldm, p, Cm, ldm);
+        CX<R>* Fp = ctx->arena.alloc_n<CX<R>>((size_t)ldm * std::max<int64_t>(N, 1));
+        CX<R>* Fd = ctx->arena.alloc_n<CX<R>>((size_t)ldm * std::max<int64_t>(N, 1));
+        copy_matrix<CX<R>>(ctx, M, k, Cm, ldm, Fp, ldm);
+        if (k > 0 && N > k)
+          cgemm<R>(ctx, 'n', 'n', M, N - k, k, CX<R>(1), Cm, ldm, Td, k, CX<R>(0), Fp + k * ldm, ldm);
+        else if (N > k)
+          set_zero<CX<R>>(ctx, Fp + k * ldm, ldm * (N - k));
+        scatter_cols<CX<R>>(ctx, M, N, Fp, ldm, p, Fd, ldm);
+        RandSrc rs(ctx, rand, opts->seed);
+        *out = csnormdiff_dense<R>(ctx, *opts, M, N, Aop, ldm, Fd, ldm, false, rs);
+      });
+      return;
+    }
     dispatch(dtype, [&](auto z) {
       using T = decltype(z);
       if (F->dtype != dtype) fail(LRA_EINVAL, "dtype of F");
@@ -2197,6 +3599,35 @@ int lra_snormdiff_psvd(lra_ctx* ctx, int dtype, int64_t m, int64_t n, const void
     chkopts(opts);
     check_dims(m, n);
     if (!out || !F || !F->U || !F->Vt) fail(LRA_EINVAL, "NULL argument");
+    if (is_cplx(dtype)) {
+      dispatch_c(dtype, [&](auto z) {
+        using R = decltype(z);
+        if (F->dtype != dtype) fail(LRA_EINVAL, "dtype of F");
+        if (F->m != m || F->n != n) fail(LRA_EDIM, "PSVD size");
+        DMat<CX<R>> dA = stage_in<CX<R>>(ctx, A, m, n, lda);
+        const int64_t k = F->k, kk = std::max<int64_t>(k, 1), ldm = std::max<int64_t>(m, 1);
+        CX<R>* U = ctx->arena.alloc_n<CX<R>>((size_t)ldm * kk);
+        CX<R>* Vt = ctx->arena.alloc_n<CX<R>>((size_t)kk * std::max<int64_t>(n, 1));
+        LRA_CUDA(cudaMemcpyAsync(U, F->U, (size_t)m * k * sizeof(CX<R>), cudaMemcpyHostToDevice, ctx->stream));
+        LRA_CUDA(cudaMemcpyAsync(Vt, F->Vt, (size_t)k * n * sizeof(CX<R>), cudaMemcpyHostToDevice, ctx->stream));
+        // US = U diag(S) on the host values of S, then the dense F = US Vt
+        std::vector<CX<R>> hU((size_t)m * k);
+        std::memcpy(hU.data(), F->U, hU.size() * sizeof(CX<R>));
+        const R* hs = static_cast<const R*>(F->S);
+        for (int64_t j = 0; j < k; ++j)
+          for (int64_t i = 0; i < m; ++i) hU[i + j * m] = hs[j] * hU[i + j * m];
+        LRA_CUDA(cudaMemcpyAsync(U, hU.data(), hU.size() * sizeof(CX<R>), cudaMemcpyHostToDevice, ctx->stream));
+        CX<R>* Fd = ctx->arena.alloc_n<CX<R>>((size_t)ldm * std::max<int64_t>(n, 1));
+        if (k > 0)
+          cgemm<R>(ctx, 'n', 'n', m, n, k, CX<R>(1), U, ldm, Vt, kk, CX<R>(0), Fd, ldm);
+        else
+          set_zero<CX<R>>(ctx, Fd, ldm * n);
+        LRA_CUDA(cudaStreamSynchronize(ctx->stream));
+        RandSrc rs(ctx, rand, opts->seed);
+        *out = csnormdiff_dense<R>(ctx, *opts, m, n, dA.p, dA.ld, Fd, ldm, false, rs);
+      });
+      return;
+    }
     dispatch(dtype, [&](auto z) {
       using T = decltype(z);
       if (F->dtype != dtype) fail(LRA_EINVAL, "dtype of F");
@@ -2232,6 +3663,66 @@ int lra_snormdiff_psvd(lra_ctx* ctx, int dtype, int64_t m, int64_t n, const void
             gemv<T>(ctx, 't', k, n, T(-1), Vt, kk, w, T(1), x);
           });
     });
+  });
+}
+
+
+int lra_sketchfact_linop(lra_ctx* ctx, char side, char trans, const lra_linop* L, const lra_opts* opts,
+                         const lra_rand* rand, lra_pqr** out) {
+  return with_linop(ctx, L, opts, [&](const lra_opts* o) {
+    return lra_sketchfact(ctx, L->dtype, side, trans, L->m, L->n, L, lin_ld(L), o, rand, out);
+  });
+}
+
+int lra_idfact_linop(lra_ctx* ctx, char trans, const lra_linop* L, const lra_opts* opts, const lra_rand* rand,
+                     lra_id** out) {
+  return with_linop(ctx, L, opts, [&](const lra_opts* o) {
+    return lra_idfact(ctx, L->dtype, trans, L->m, L->n, L, lin_ld(L), o, rand, out);
+  });
+}
+
+int lra_pqrfact_linop(lra_ctx* ctx, char trans, const lra_linop* L, const lra_opts* opts, const lra_rand* rand,
+                      lra_pqr** out) {
+  return with_linop(ctx, L, opts, [&](const lra_opts* o) {
+    return lra_pqrfact(ctx, L->dtype, trans, L->m, L->n, L, lin_ld(L), o, rand, out);
+  });
+}
+
+int lra_prange_linop(lra_ctx* ctx, char trans, const lra_linop* L, const lra_opts* opts, const lra_rand* rand,
+                     lra_pqr** out) {
+  return with_linop(ctx, L, opts, [&](const lra_opts* o) {
+    return lra_prange(ctx, L->dtype, trans, L->m, L->n, L, lin_ld(L), o, rand, out);
+  });
+}
+
+int lra_psvdfact_linop(lra_ctx* ctx, const lra_linop* L, const lra_opts* opts, const lra_rand* rand,
+                       int vals_only, lra_psvd** out) {
+  return with_linop(ctx, L, opts, [&](const lra_opts* o) {
+    return lra_psvdfact(ctx, L->dtype, L->m, L->n, L, lin_ld(L), o, rand, vals_only, out);
+  });
+}
+
+int lra_pheigfact_linop(lra_ctx* ctx, const lra_linop* L, const lra_opts* opts, const lra_rand* rand,
+                        int vals_only, lra_pheig** out) {
+  return with_linop(ctx, L, opts, [&](const lra_opts* o) {
+    if (L->m != L->n) {
+      ctx->last_error = "pheigfact needs a square operator";
+      return (int)LRA_EDIM;
+    }
+    return lra_pheigfact(ctx, L->dtype, L->n, L, lin_ld(L), o, rand, vals_only, out);
+  });
+}
+
+int lra_curfact_linop(lra_ctx* ctx, const lra_linop* L, const lra_opts* opts, const lra_rand* rand,
+                      lra_cur** out) {
+  return with_linop(ctx, L, opts, [&](const lra_opts* o) {
+    return lra_curfact(ctx, L->dtype, L->m, L->n, L, lin_ld(L), o, rand, out);
+  });
+}
+
+int lra_snorm_linop(lra_ctx* ctx, const lra_linop* L, const lra_opts* opts, const lra_rand* rand, double* out) {
+  return with_linop(ctx, L, opts, [&](const lra_opts* o) {
+    return lra_snorm(ctx, L->dtype, L->m, L->n, L, lin_ld(L), -1, o, rand, out);
   });
 }
 

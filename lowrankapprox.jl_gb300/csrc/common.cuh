@@ -11,9 +11,25 @@ namespace lra {
 
 constexpr int kWarp = 32;
 
-// Limit of every device-side wait (ns of %globaltimer).  A wait that runs
-// out sets an error status and returns; nothing traps or spins forever.
+// Default limit of every device-side wait (ns of %globaltimer).  A wait
+// that runs out sets an error status and returns; nothing traps or spins
+// forever.
 constexpr uint64_t kWaitLimitNs = 4000000000ull;
+
+// The limit in force, one copy per translation unit (no relocatable device
+// code): lra_ctx_set_wait_limit writes every copy on the context's device.
+// A wait reads it once when it starts.
+static __device__ unsigned long long g_wait_limit_ns = kWaitLimitNs;
+
+__device__ __forceinline__ uint64_t wait_limit_ns() {
+  return *((volatile const unsigned long long*)&g_wait_limit_ns);
+}
+
+// host side: this translation unit's copy (synchronous)
+static inline cudaError_t set_unit_wait_limit(uint64_t ns) {
+  const unsigned long long v = ns ? ns : kWaitLimitNs;
+  return cudaMemcpyToSymbol(g_wait_limit_ns, &v, sizeof v);
+}
 
 __device__ __forceinline__ uint64_t globaltimer_ns() {
   uint64_t t;
@@ -133,10 +149,10 @@ __device__ __forceinline__ bool grid_sync(GridBar* gb) {
       __threadfence();
       atomicAdd(&gb->gen, 1u);
     } else {
-      const uint64_t t0 = globaltimer_ns();
+      const uint64_t t0 = globaltimer_ns(), lim = wait_limit_ns();
       while (*vgen == g) {
         if (*verr != 0) break;
-        if (globaltimer_ns() - t0 > kWaitLimitNs) {
+        if (globaltimer_ns() - t0 > lim) {
           atomicCAS(&gb->err, 0, 4);
           break;
         }

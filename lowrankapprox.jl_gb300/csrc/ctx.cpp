@@ -1,8 +1,12 @@
 // Context runtime of liblra: errors, device workspace arena, launch hooks.
 
+#include <dlfcn.h>
+
 #include <cstdlib>
 #include <cstdio>
 #include <cstring>
+#include <fstream>
+#include <sstream>
 #include <mutex>
 #include <set>
 #include <utility>
@@ -140,6 +144,91 @@ bool trace_on() {
     return e && *e && *e != '0';
   }();
   return on;
+}
+
+// ---- tuning table -------------------------------------------------------------------
+//
+// Text, one entry per line ("#" starts a comment):
+//   tc_tile_n <f32|f64> <log2 order> <32|64|96>
+//   qr_seq_len <rows>
+//   srft_wide <log2 l'> <0|1>
+// lowrankapprox/autotune.py writes it from its sweeps; unknown keys and
+// out-of-range values are ignored, so an old table never breaks a newer
+// library.
+
+static void tuning_defaults(lra_tuning* t) {
+  for (auto& row : t->tc_tile_n)
+    for (int& v : row) v = 96;
+  t->qr_seq_len = 96;
+  for (int lb = 0; lb <= 10; ++lb) t->srft_wide[lb] = (lb >= 7 && lb <= 10) ? 1 : 0;
+}
+
+bool set_tuning(lra_tuning* t, const char* key, int64_t index, int64_t value) {
+  if (!std::strcmp(key, "tc_tile_n")) {
+    if (index < 0 || index >= 32 || (value != 32 && value != 64 && value != 96)) return false;
+    t->tc_tile_n[index / 16][index % 16] = (int)value;
+    return true;
+  }
+  if (!std::strcmp(key, "qr_seq_len")) {
+    if (value < 0 || value > 4096) return false;
+    t->qr_seq_len = (int)value;
+    return true;
+  }
+  if (!std::strcmp(key, "srft_wide")) {
+    if (index < 0 || index > 10 || (value != 0 && value != 1)) return false;
+    t->srft_wide[index] = (int)value;
+    return true;
+  }
+  return false;
+}
+
+static std::string library_dir() {
+  Dl_info info;
+  if (dladdr(reinterpret_cast<void*>(&tuning_defaults), &info) && info.dli_fname) {
+    std::string p = info.dli_fname;
+    const size_t slash = p.rfind('/');
+    if (slash != std::string::npos) return p.substr(0, slash);
+  }
+  return ".";
+}
+
+void load_tuning(lra_tuning* t, std::string* source) {
+  tuning_defaults(t);
+  *source = "defaults";
+  const char* env = std::getenv("LRA_TUNING");
+  const std::string path = env && *env ? std::string(env) : library_dir() + "/tuning_gb300.txt";
+  std::ifstream f(path);
+  if (!f) return;
+  std::string line;
+  int used = 0;
+  while (std::getline(f, line)) {
+    const size_t hash = line.find('#');
+    if (hash != std::string::npos) line.resize(hash);
+    std::istringstream in(line);
+    std::string key;
+    if (!(in >> key)) continue;
+    if (key == "tc_tile_n") {
+      std::string dt;
+      int64_t lb = -1, v = 0;
+      if (in >> dt >> lb >> v) used += set_tuning(t, "tc_tile_n", (dt == "f64" ? 16 : 0) + lb, v);
+    } else if (key == "qr_seq_len") {
+      int64_t v = 0;
+      if (in >> v) used += set_tuning(t, "qr_seq_len", 0, v);
+    } else if (key == "srft_wide") {
+      int64_t lb = -1, v = 0;
+      if (in >> lb >> v) used += set_tuning(t, "srft_wide", lb, v);
+    }
+  }
+  *source = path + " (" + std::to_string(used) + " entries)";
+}
+
+std::string tuning_text(const lra_tuning& t) {
+  std::ostringstream o;
+  for (int d = 0; d < 2; ++d)
+    for (int lb = 0; lb < 16; ++lb) o << "tc_tile_n " << (d ? "f64 " : "f32 ") << lb << ' ' << t.tc_tile_n[d][lb] << '\n';
+  o << "qr_seq_len " << t.qr_seq_len << '\n';
+  for (int lb = 0; lb <= 10; ++lb) o << "srft_wide " << lb << ' ' << t.srft_wide[lb] << '\n';
+  return o.str();
 }
 
 }  // namespace lra

@@ -952,6 +952,7 @@ bool jacobi_svd_df(lra_ctx* ctx, int64_t n, double* X, int64_t ldx, double* V, i
 
 template <typename T>
 bool is_symmetric(lra_ctx* ctx, int64_t n, const T* A, int64_t lda) {
+  if (ctx->linop) return ctx->linop->hermitian != 0;  // a HermitianLinearOperator is, by its type
   const ArenaMark mk = ctx->arena.mark();
   int* bad = ctx->arena.alloc_n<int>(1);
   LRA_CUDA(cudaMemsetAsync(bad, 0, sizeof(int), ctx->stream));
@@ -1387,5 +1388,7 @@ template void trsm_bs<float>(lra_ctx*, int64_t, int64_t, const float*, int64_t, 
 template void trsm_bs<double>(lra_ctx*, int64_t, int64_t, const double*, int64_t, double*, int64_t);
 template void trsm_left_diag<float>(lra_ctx*, int, int64_t, const float*, int64_t, float*, int64_t);
 template void trsm_left_diag<double>(lra_ctx*, int, int64_t, const double*, int64_t, double*, int64_t);
+
+cudaError_t set_wait_limit_dense(uint64_t ns) { return set_unit_wait_limit(ns); }
 
 }  // namespace lra

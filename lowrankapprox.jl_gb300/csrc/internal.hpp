@@ -9,6 +9,7 @@
 #include <vector>
 
 #include "../../include/lra.h"
+#include "cplx.cuh"
 
 namespace lra {
 
@@ -59,6 +60,21 @@ class Arena {
 
 }  // namespace lra
 
+// Shapes the autotuner (lowrankapprox/autotune.py) picks, read from its
+// table when a context is created (ctx.cpp: load_tuning); the defaults are
+// the shapes the sweeps before it had chosen.
+struct lra_tuning {
+  // tcgen05 sketch tile N (32, 64 or 96 sketch rows per CTA) by element
+  // type (0 Float32, 1 Float64) and ceil(log2(sketch order)), 0..15
+  int tc_tile_n[2][16];
+  // rows below which the double-float pivoted QR sums a column with one
+  // thread (a warp per four columns above)
+  int qr_seq_len;
+  // Float32 SRFT: 1 selects the 512-thread swizzled form for log2(l') when
+  // it applies (7..10), 0 the 256-thread padded form
+  int srft_wide[11];
+};
+
 struct lra_ctx {
   int device = 0;
   int num_sms = 0;
@@ -81,6 +97,10 @@ struct lra_ctx {
   static constexpr int kAux = 8;
   cudaStream_t aux[kAux] = {};
   cudaEvent_t aux_ev[kAux + 1] = {};
+  // the operator of a matrix-free call (lra_*_linop) while it runs, else null
+  const lra_linop* linop = nullptr;
+  lra_tuning tuning{};
+  std::string tuning_source;  // the table file read, or "defaults"
 };
 
 namespace lra {
@@ -341,5 +361,71 @@ void gemv(lra_ctx* ctx, char trans, int64_t m, int64_t n, T alpha, const T* A, i
 // kernel-launch accounting (every launcher calls this once per launch)
 inline void count_launch(lra_ctx* ctx, int n = 1) { ctx->launches += n; }
 void post_launch(lra_ctx* ctx, const char* name);
+
+// the bounded-wait limit of each translation unit that waits (ns; 0: the
+// default), and the grid-barrier self-test: returns the barrier's error
+// word (4 when its wait ran out) and the number of CTAs that returned
+cudaError_t set_wait_limit_qr(uint64_t ns);
+cudaError_t set_wait_limit_dense(uint64_t ns);
+cudaError_t set_wait_limit_tc(uint64_t ns);
+int probe_grid_wait(lra_ctx* ctx, int* returned);
+
+// the tuning table: defaults, then the file named by LRA_TUNING or the
+// table beside liblra.so (tuning_gb300.txt); the source is recorded
+void load_tuning(lra_tuning* t, std::string* source);
+// one entry by name ("tc_tile_n", "qr_seq_len", "srft_wide"), the index
+// addressing the table (dtype * 16 + log2 order; log2 l'); false if unknown
+bool set_tuning(lra_tuning* t, const char* key, int64_t index, int64_t value);
+std::string tuning_text(const lra_tuning& t);
+
+// ---- complex element types (cplx.cu) -------------------------------------------------
+// C = alpha op(A) op(B) + beta C, op 'n', 't' or 'c' (conjugate transpose)
+template <typename R>
+void cgemm(lra_ctx* ctx, char ta, char tb, int64_t m, int64_t n, int64_t k, cx<R> alpha, const cx<R>* A,
+           int64_t lda, const cx<R>* B, int64_t ldb, cx<R> beta, cx<R>* C, int64_t ldc);
+// dst (n x m) = src^H; A <- conj(A)
+template <typename R>
+void cadjoint(lra_ctx* ctx, int64_t m, int64_t n, const cx<R>* src, int64_t lds, cx<R>* dst, int64_t ldd);
+template <typename R>
+void cconj(lra_ctx* ctx, int64_t m, int64_t n, cx<R>* A, int64_t lda);
+template <typename R>
+void ccol_norms(lra_ctx* ctx, int64_t m, int64_t n, const cx<R>* A, int64_t lda, R* out);
+// geqp3_adap! with ZLAQPS / CLAQPS rules (pivot) or a plain Householder QR
+template <typename R>
+int64_t cgeqp3(lra_ctx* ctx, int64_t m, int64_t n, cx<R>* A, int64_t lda, int64_t* jpvt, cx<R>* tau, int64_t kmax,
+               int64_t nb, double atol, double rtol, bool pivot);
+// X <- Q X ('n') or Q^H X ('c'), Q = H_1 ... H_k of the QR's reflectors
+template <typename R>
+void capply_q(lra_ctx* ctx, char trans, int64_t m, int64_t k, const cx<R>* V, int64_t ldv, const cx<R>* tau,
+              cx<R>* X, int64_t ldx, int64_t nc);
+template <typename R>
+void corgqr(lra_ctx* ctx, int64_t m, int64_t k, cx<R>* V, int64_t ldv, const cx<R>* tau);
+template <typename R>
+void ctrsm_upper(lra_ctx* ctx, int64_t k, int64_t nrhs, const cx<R>* R_, int64_t ldr, cx<R>* X, int64_t ldx);
+// one-sided Jacobi: X (k x k) <- U, V, S (unsorted) with X = U diag(S) V^H
+template <typename R>
+void cjacobi_svd(lra_ctx* ctx, int64_t k, cx<R>* X, int64_t ldx, cx<R>* V, int64_t ldv, R* S);
+template <typename R>
+bool cis_hermitian(lra_ctx* ctx, int64_t n, const cx<R>* A, int64_t lda);
+template <typename R>
+void chermitianize(lra_ctx* ctx, int64_t n, cx<R>* B, int64_t ldb);
+template <typename R>
+void cadd_diag(lra_ctx* ctx, int64_t n, cx<R>* A, int64_t lda, R s);
+template <typename R>
+void cphases(lra_ctx* ctx, const double* g, int64_t n, cx<R>* d);
+template <typename R>
+void csrft_direct(lra_ctx* ctx, char trans, int64_t M, int64_t N, const cx<R>* A, int64_t lda, const cx<R>* d,
+                  const int64_t* idx, int64_t order, cx<R>* B, int64_t ldb);
+template <typename R>
+void csprn(lra_ctx* ctx, char trans, int64_t M, int64_t N, const cx<R>* A, int64_t lda, const int64_t* perm,
+           const cx<R>* g, const int64_t* start, int64_t order, cx<R>* B, int64_t ldb);
+template <typename R>
+void csub(lra_ctx* ctx, char trans, int64_t N, const cx<R>* A, int64_t lda, const int64_t* rows, int64_t order,
+          cx<R>* B, int64_t ldb);
+template <typename R>
+bool cmaxdet_step(lra_ctx* ctx, int64_t k, int64_t nr, cx<R>* T, int64_t* jpvt, double bound, bool update, cx<R>* R1,
+                  int64_t ldr);
+template <typename R>
+void ccluster_orth(lra_ctx* ctx, int64_t n, int64_t k, cx<R>* Z, int64_t ldz, const int64_t* cl, int64_t ncl);
 
 }  // namespace lra

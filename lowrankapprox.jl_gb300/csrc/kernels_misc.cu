@@ -434,6 +434,23 @@ INST(float)
 INST(double)
 #undef INST
 
+// the data movement of complex matrices (the complex drivers)
+#define INSTX(T)                                                                                   \
+  template void copy_matrix<T>(lra_ctx*, int64_t, int64_t, const T*, int64_t, T*, int64_t);        \
+  template void transpose<T>(lra_ctx*, int64_t, int64_t, const T*, int64_t, T*, int64_t);          \
+  template void gather_cols<T>(lra_ctx*, int64_t, int64_t, const T*, int64_t, const int64_t*, T*,  \
+                               int64_t);                                                           \
+  template void gather_rows<T>(lra_ctx*, int64_t, int64_t, const T*, int64_t, const int64_t*, T*,  \
+                               int64_t);                                                           \
+  template void scatter_cols<T>(lra_ctx*, int64_t, int64_t, const T*, int64_t, const int64_t*, T*, \
+                                int64_t);                                                          \
+  template void set_zero<T>(lra_ctx*, T*, int64_t);                                                \
+  template void set_identity<T>(lra_ctx*, int64_t, int64_t, T*, int64_t);                          \
+  template void zero_lower<T>(lra_ctx*, int64_t, int64_t, T*, int64_t);
+INSTX(cx<float>)
+INSTX(cx<double>)
+#undef INSTX
+
 }  // namespace lra
 
 namespace lra {

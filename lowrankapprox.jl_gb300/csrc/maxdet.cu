@@ -1,6 +1,7 @@
 // Determinant-maximizing column swaps of the ID (strong rank-revealing QR,
 // Gu & Eisenstat 1996): maxdet_swapcols! / maxdet_update!
-// (src/pqr.jl:445-501), the T / permutation part, on the device.
+// (src/pqr.jl:445-501) on the device: T and the permutation, and R1 when
+// an R factor is returned.
 
 #include <algorithm>
 
@@ -93,10 +94,31 @@ __global__ void maxdet_ger_kernel(int64_t k, int64_t nr, T* Tm, const int64_t* p
   }
 }
 
+// maxdet_update!'s R part (src/pqr.jl:494-499): y = R1 w1 with w1 = T(:, j)
+// - e_i as it was before the T update; a thread per row of R1 (k x k)
+template <typename T>
+__global__ void maxdet_r1_gemv_kernel(int64_t k, const T* __restrict__ R1, int64_t ldr, const T* __restrict__ w1,
+                                      T* __restrict__ y) {
+  for (int64_t l = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; l < k; l += (int64_t)gridDim.x * blockDim.x) {
+    T acc = T(0);
+    for (int64_t c = 0; c < k; ++c) acc += R1[l + c * ldr] * w1[c];
+    y[l] = acc;
+  }
+}
+
+// R1(:, i) += y, after every row of y was formed from the old column i
+template <typename T>
+__global__ void maxdet_r1_add_kernel(int64_t k, T* R1, int64_t ldr, const int64_t* pidx, const T* y) {
+  const int64_t i = *pidx % k;
+  for (int64_t l = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; l < k; l += (int64_t)gridDim.x * blockDim.x)
+    R1[l + i * ldr] += y[l];
+}
+
 }  // namespace
 
 template <typename T>
-bool maxdet_step(lra_ctx* ctx, int64_t k, int64_t nr, T* Tm, int64_t* jpvt, double bound, bool update) {
+bool maxdet_step(lra_ctx* ctx, int64_t k, int64_t nr, T* Tm, int64_t* jpvt, double bound, bool update, T* R1,
+                 int64_t ldr) {
   const int64_t total = k * nr;
   if (total <= 0) return false;
   const ArenaMark mk = ctx->arena.mark();
@@ -116,6 +138,14 @@ bool maxdet_step(lra_ctx* ctx, int64_t k, int64_t nr, T* Tm, int64_t* jpvt, doub
     T* w2 = ctx->arena.alloc_n<T>(nr);
     maxdet_prep_kernel<T><<<1, 256, 0, ctx->stream>>>(k, nr, Tm, jpvt, pi + nb, w1, w2);
     post_launch(ctx, "maxdet_prep_kernel");
+    if (R1) {
+      T* y = ctx->arena.alloc_n<T>(k);
+      const unsigned gk = (unsigned)std::max<int64_t>(1, std::min<int64_t>((k + 127) / 128, (int64_t)ctx->num_sms * 4));
+      maxdet_r1_gemv_kernel<T><<<gk, 128, 0, ctx->stream>>>(k, R1, ldr, w1, y);
+      post_launch(ctx, "maxdet_r1_gemv_kernel");
+      maxdet_r1_add_kernel<T><<<gk, 128, 0, ctx->stream>>>(k, R1, ldr, pi + nb, y);
+      post_launch(ctx, "maxdet_r1_add_kernel");
+    }
     const unsigned g = (unsigned)std::max<int64_t>(1, std::min<int64_t>((total + 255) / 256, (int64_t)ctx->num_sms * 8));
     maxdet_ger_kernel<T><<<g, 256, 0, ctx->stream>>>(k, nr, Tm, pi + nb, w1, w2);
     post_launch(ctx, "maxdet_ger_kernel");
@@ -125,7 +155,7 @@ bool maxdet_step(lra_ctx* ctx, int64_t k, int64_t nr, T* Tm, int64_t* jpvt, doub
   return big;
 }
 
-template bool maxdet_step<float>(lra_ctx*, int64_t, int64_t, float*, int64_t*, double, bool);
-template bool maxdet_step<double>(lra_ctx*, int64_t, int64_t, double*, int64_t*, double, bool);
+template bool maxdet_step<float>(lra_ctx*, int64_t, int64_t, float*, int64_t*, double, bool, float*, int64_t);
+template bool maxdet_step<double>(lra_ctx*, int64_t, int64_t, double*, int64_t*, double, bool, double*, int64_t);
 
 }  // namespace lra

@@ -53,6 +53,9 @@ struct QrParams {
   int pivot;
   int64_t* k_out;
   int64_t vcap;  // reflector rows that fit the dynamic shared memory
+  // double-float QR: columns with at most this many rows below the pivot
+  // row are summed by one thread each (the tuning table's qr_seq_len)
+  int seq_len = 96;
 };
 
 constexpr int CH = 16;  // rows per lane held in registers per column chunk
@@ -436,7 +439,7 @@ struct QrV2Extra {
 constexpr int QCH = 16;  // rows per lane per register chunk (512 rows)
 constexpr int QG = 4;    // rows per lane issued between uniform range checks
 constexpr int QRPL = 4;  // rows per lane loaded ahead in the double-float QR's column loops
-constexpr int kQrSeqLen = 96;  // columns this short (below the pivot row) are summed row by row
+
 constexpr int QSEQB = 8;  // rows loaded ahead by a thread that walks a column
 constexpr unsigned char ST_LIVE = 1, ST_DONE = 2, ST_FLAG = 4, ST_UPD = 8;
 
@@ -1492,7 +1495,7 @@ __device__ __forceinline__ void geqp3_df_body(const QrParams<double>& P, const Q
       }
       bool ok = true;
       if (__any_sync(0xffffffffu, pending != 0)) {
-        const uint64_t t0 = globaltimer_ns();
+        const uint64_t t0 = globaltimer_ns(), lim = wait_limit_ns();
         for (unsigned it = 1;; ++it) {
 #pragma unroll
           for (int q = 0; q < PB; ++q)
@@ -1507,7 +1510,7 @@ __device__ __forceinline__ void geqp3_df_body(const QrParams<double>& P, const Q
           int bad = 0;
           if (lane == 0) {
             bad = *((volatile int*)&P.bar->err) != 0;
-            if (!bad && globaltimer_ns() - t0 > kWaitLimitNs) {
+            if (!bad && globaltimer_ns() - t0 > lim) {
               atomicCAS(&P.bar->err, 0, 4);
               bad = 1;
             }
@@ -1653,7 +1656,7 @@ __device__ __forceinline__ void geqp3_df_body(const QrParams<double>& P, const Q
             X.beta[c] = s_betad;
           }
         }
-      } else if (len > 0 && len <= kQrSeqLen) {
+      } else if (len > 0 && len <= P.seq_len) {
         // ---- short columns: a thread per column, the dot product summed
         // row by row (a lane-strided sum and its reduction tree cost more
         // than the products here).  The rule depends on len alone, so both
@@ -2197,6 +2200,11 @@ __global__ void jpvt_kernel(int64_t n, const int64_t* col_at, int64_t* jpvt) {
     jpvt[t] = col_at[t] + 1;
 }
 
+__global__ void jpvt_identity_kernel(int64_t n, int64_t* jpvt) {
+  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < n; t += (int64_t)gridDim.x * blockDim.x)
+    jpvt[t] = t + 1;
+}
+
 // ---- Householder application, one warp per column of X ----------------------
 template <typename T>
 __global__ void apply_q_kernel(int trans, int64_t m, int64_t k, const T* __restrict__ V, int64_t ldv,
@@ -2370,7 +2378,7 @@ void geqp3_df_batch(lra_ctx* ctx, int64_t count, const DfBatchItem* items, int64
     double* scale = ctx->arena.alloc_n<double>(1);
     // row-major when every step sums its columns row by row (a thread per
     // column reads a row of the workspace coalesced), else column-major
-    const bool rowmaj = m - 1 <= kQrSeqLen;
+    const bool rowmaj = m - 1 <= ctx->tuning.qr_seq_len;
     const int64_t cs = rowmaj ? 1 : m, rs = rowmaj ? n : 1;
     prep[(size_t)t] = DfPrepJob{m, n, it.ldb, it.B, work, cs, rs, vn0, scale, maxbits + t};
     QrJob& J = qr[(size_t)t];
@@ -2384,6 +2392,7 @@ void geqp3_df_batch(lra_ctx* ctx, int64_t count, const DfBatchItem* items, int64
     J.P.atol = atol;
     J.P.rtol = rtol;
     J.P.pivot = 1;
+    J.P.seq_len = ctx->tuning.qr_seq_len;
     J.P.k_out = k_dev + i;
     J.X.piv = ctx->arena.alloc_n<int64_t>(std::max<int64_t>(J.P.kmax, 1));
     J.X.nfac = ctx->arena.alloc_n<int64_t>(1);
@@ -2495,6 +2504,7 @@ int64_t geqp3_adap(lra_ctx* ctx, int64_t m, int64_t n, T* A, int64_t lda, int64_
   P.pivot = pivot ? 1 : 0;
   P.k_out = ctx->arena.alloc_n<int64_t>(1);
   P.vcap = vcap;
+  P.seq_len = ctx->tuning.qr_seq_len;
   LRA_CUDA(cudaMemsetAsync(small, 0, 8 * sizeof(int), ctx->stream));
   LRA_CUDA(cudaMemsetAsync(P.bar, 0, sizeof(GridBar), ctx->stream));
   if (P.kmax <= 0) {
@@ -2698,13 +2708,52 @@ void col_norms(lra_ctx* ctx, int64_t m, int64_t n, const T* A, int64_t lda, T* o
   post_launch(ctx, "col_norms_kernel");
 }
 
+// ---- bounded waits: the limit in force, and a self-test ----------------------------
+
+cudaError_t set_wait_limit_qr(uint64_t ns) { return set_unit_wait_limit(ns); }
+
+namespace {
+
+// Two CTAs meet at a grid barrier whose arrival count starts at the grid
+// size, so that no arrival completes it: both wait until the limit runs
+// out, the barrier records the time-out and every CTA returns.
+__global__ void probe_wait_kernel(GridBar* gb, int* returned) {
+  if (!grid_sync(gb)) {
+    if (threadIdx.x == 0) atomicAdd(returned, 1);
+    return;
+  }
+  if (threadIdx.x == 0) atomicAdd(returned, 1000);  // the barrier completed: not expected
+}
+
+}  // namespace
+
+int probe_grid_wait(lra_ctx* ctx, int* returned) {
+  const ArenaMark mark = ctx->arena.mark();
+  GridBar* gb = reinterpret_cast<GridBar*>(ctx->arena.alloc(sizeof(GridBar)));
+  int* ret = ctx->arena.alloc_n<int>(1);
+  static const GridBar init{2u, 0u, 0, 0};
+  LRA_CUDA(cudaMemcpyAsync(gb, &init, sizeof init, cudaMemcpyHostToDevice, ctx->stream));
+  LRA_CUDA(cudaMemsetAsync(ret, 0, sizeof(int), ctx->stream));
+  void* args[] = {&gb, &ret};
+  LRA_CUDA(cudaLaunchCooperativeKernel((const void*)probe_wait_kernel, dim3(2), dim3(32), args, 0, ctx->stream));
+  post_launch(ctx, "probe_wait_kernel");
+  GridBar hb;
+  int hr = 0;
+  LRA_CUDA(cudaMemcpyAsync(&hb, gb, sizeof hb, cudaMemcpyDeviceToHost, ctx->stream));
+  LRA_CUDA(cudaMemcpyAsync(&hr, ret, sizeof hr, cudaMemcpyDeviceToHost, ctx->stream));
+  LRA_CUDA(cudaStreamSynchronize(ctx->stream));
+  ctx->arena.release(mark);
+  *returned = hr;
+  return hb.err;
+}
+
 // ---- pivoted QR without any device allocation --------------------------------------
 //
-// Some callers cannot allocate device memory while they factor: code that
-// runs between the begin and end of a CUDA stream capture, a serving loop
-// that has reserved all of its device memory up front, or a host framework
-// that owns the device allocator (a Julia or Python memory pool) and does
-// not let a library call cudaMalloc behind its back.  For them the pivoted
+// Some callers cannot allocate device memory while they factor: a serving
+// loop that has reserved all of its device memory up front and must not
+// grow, or a host framework that owns the device allocator (a Julia or
+// Python memory pool) and does not let a library call cudaMalloc behind its
+// back.  For them the pivoted
 // QR's scratch -- the partial column norms, the per-CTA pivot candidates,
 // the block-stop counters and the grid barrier -- lives in one fixed device
 // array of this file, sized for at most kNoAllocMaxCols columns.  Every GPU
@@ -2712,10 +2761,13 @@ void col_norms(lra_ctx* ctx, int64_t m, int64_t n, const T* A, int64_t lda, T* o
 //
 // The array's host-side name is not a device address; its address is taken
 // once per device with cudaGetSymbolAddress, with that device current, on
-// the first call that runs on the device.  That first call should therefore
-// happen before any stream capture begins.  All calls on a device share the
-// array: calls that overlap on the GPU (different streams, threads or
-// contexts) race on it and must be serialized by the caller.
+// the first call that runs on the device, and cached by device ordinal.  So
+// the entry point supports the device's primary context (the runtime API's
+// context) only: a caller that makes another driver-API context current on
+// the same device would be handed the primary context's address.  All calls
+// on a device share the array: calls that overlap on the GPU (different
+// streams, threads or contexts) race on it and must be serialized by the
+// caller.  Each call synchronizes its stream and reads the rank back.
 
 constexpr int64_t kNoAllocMaxCols = 32768;
 constexpr int kNoAllocMaxGrid = 1024;
@@ -2798,7 +2850,14 @@ int64_t geqp3_adap_noalloc(lra_ctx* ctx, int64_t m, int64_t n, T* A, int64_t lda
   // the barrier, which must start at zero (the kernel initializes the rest)
   LRA_CUDA(cudaMemsetAsync(small, 0, 8 * sizeof(int), ctx->stream));
   LRA_CUDA(cudaMemsetAsync(P.bar, 0, sizeof(GridBar), ctx->stream));
-  if (P.kmax <= 0) fail(LRA_EINVAL, "lra_geqp3_adap_noalloc: nothing to factor (rank 0 or empty)");
+  if (P.kmax <= 0) {
+    // nothing to factor (rank 0): the identity permutation, as lra_geqp3_adap
+    const unsigned gi = (unsigned)std::max<int64_t>(1, std::min<int64_t>((n + 255) / 256, ctx->num_sms * 4));
+    jpvt_identity_kernel<<<gi, 256, 0, ctx->stream>>>(n, jpvt);
+    post_launch(ctx, "jpvt_identity_kernel");
+    LRA_CUDA(cudaStreamSynchronize(ctx->stream));
+    return 0;
+  }
   void* args[] = {&P};
   LRA_CUDA(cudaLaunchCooperativeKernel((const void*)geqp3_kernel<T, NT>, dim3(grid), dim3(NT), args,
                                        dyn_smem, ctx->stream));

@@ -167,6 +167,7 @@ int lra_server_create(int device, int slots, int64_t hbm_budget_bytes, lra_serve
 int lra_server_submit(lra_server* s, const lra_request* req, uint64_t* ticket) {
   if (!s || !req || !ticket) return LRA_EINVAL;
   if (req->kind != LRA_REQ_IDFACT && req->kind != LRA_REQ_PSVDFACT) return LRA_EINVAL;
+  if (req->dtype == LRA_C32 || req->dtype == LRA_C64) return LRA_ENOTSUP;  // complex types: single calls
   if (req->dtype != LRA_F32 && req->dtype != LRA_F64) return LRA_EINVAL;
   if (req->m < 0 || req->n < 0 || !req->A) return LRA_EDIM;
   Req* q = new (std::nothrow) Req();

@@ -638,7 +638,8 @@ bool srft_sketch_fft(lra_ctx* ctx, char trans, int64_t M, int64_t N, const T* A,
     // rows of a chunk width PC, a power of two dividing m2 / 2, at most the
     // kernel's
     const int wide_pcb = 13 - lbits;
-    wide = sizeof(T) == 4 && lbits >= 7 && lbits <= 10 && (m2 / 2) % (1 << wide_pcb) == 0;
+    wide = sizeof(T) == 4 && lbits >= 7 && lbits <= 10 && (m2 / 2) % (1 << wide_pcb) == 0 &&
+           ctx->tuning.srft_wide[lbits] != 0;
     const int nt = wide ? 512 : SK_NT;
     if (wide) {
       pcb = wide_pcb;

@@ -44,16 +44,22 @@ namespace lra {
 namespace {
 
 constexpr int TILE_M = 128;   // columns of op(A) per CTA
-constexpr int TILE_N = 96;    // sketch rows per CTA
+// sketch rows per CTA (the MMA N): 32, 64 or 96, picked per element type and
+// sketch order by the tuning table; five accumulators of TN columns fit TMEM
 constexpr int KBLK = 64;      // K per stage (128 bytes of BF16: one SW128 row)
 constexpr int CHUNK_KB = 8;   // K-blocks per exact chunk (512)
 constexpr int NSTAGE = 2;
 constexpr int TILE_BYTES = TILE_M * KBLK * 2;  // 16 KB (one slice tile)
-constexpr int S_BYTES = TILE_N * KBLK * 2;     // 12 KB (a 1024 multiple)
 constexpr int NTHREADS = 320;
 constexpr int MAX_SLICES = 6;
 constexpr int MAX_EXACT = 4;
-constexpr int COLS = TILE_N / 2;               // sketch rows per drain thread
+template <int TN>
+struct TcTile {
+  static constexpr int S_BYTES = TN * KBLK * 2;  // 4, 8 or 12 KB (1024 multiples)
+  static constexpr int COLS = TN / 2;            // sketch rows per drain thread
+  static constexpr uint32_t TMEM_COLS = 5 * TN <= 256 ? 256u : 512u;
+  static_assert(S_BYTES % 1024 == 0 && COLS % 16 == 0 && TN % 16 == 0, "tile N");
+};
 constexpr int kNonFinite = 1 << 20;            // exponent of a column holding NaN / Inf
 
 struct TcParams {
@@ -100,10 +106,10 @@ __device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
 // bounded wait; returns false (and records the error) on time-out
 __device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, int* err) {
   if (mbar_try_wait(bar, parity)) return true;
-  const uint64_t t0 = globaltimer_ns();
+  const uint64_t t0 = globaltimer_ns(), lim = wait_limit_ns();
   while (!mbar_try_wait(bar, parity)) {
     if (*((volatile int*)err) != 0) return false;
-    if (globaltimer_ns() - t0 > kWaitLimitNs) {
+    if (globaltimer_ns() - t0 > lim) {
       atomicCAS(err, 0, 4);
       return false;
     }
@@ -191,9 +197,13 @@ __device__ __forceinline__ void tc_fence_after() {
 }
 
 // ---- the sketch kernel ----------------------------------------------------------
+template <int TILE_N>
 __global__ void __launch_bounds__(NTHREADS, 1)
     tc_sketch_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmS,
                      TcParams P) {
+  constexpr int S_BYTES = TcTile<TILE_N>::S_BYTES;
+  constexpr int COLS = TcTile<TILE_N>::COLS;
+  constexpr uint32_t TMEM_COLS = TcTile<TILE_N>::TMEM_COLS;
   extern __shared__ __align__(1024) unsigned char smem_raw[];
   // 1024-align the tile area
   unsigned char* base = reinterpret_cast<unsigned char*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
@@ -228,7 +238,8 @@ __global__ void __launch_bounds__(NTHREADS, 1)
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
   if (warp == 1) {
-    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], 512;" ::"r"(smem_u32(tmem_slot))
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(tmem_slot)),
+                 "r"(TMEM_COLS)
                  : "memory");
     asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
   }
@@ -361,7 +372,7 @@ __global__ void __launch_bounds__(NTHREADS, 1)
   __syncthreads();
   if (warp == 1) {
     tc_fence_after();
-    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, 512;" ::"r"(tmem) : "memory");
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(TMEM_COLS) : "memory");
   }
 }
 
@@ -840,10 +851,19 @@ void tc_split(lra_ctx* ctx, char trans, int64_t M, int64_t N, const T* A, int64_
   }
 }
 
+// the tile N of the tuning table for this element type and sketch order
+static int tuned_tile_n(const lra_ctx* ctx, bool f64, int64_t order) {
+  int lb = 0;
+  while (lb < 15 && ((int64_t)1 << lb) < order) ++lb;
+  const int v = ctx->tuning.tc_tile_n[f64 ? 1 : 0][lb];
+  return (v == 32 || v == 64) ? v : 96;
+}
+
 template <typename T>
 void tc_sketch(lra_ctx* ctx, const TcSplit& sp, int64_t order, const T* S, T* B, int64_t ldb, int* err_slot) {
   const int64_t K = sp.K, N = sp.N, Kp = sp.Kp;
   const int ns = sp.ns;
+  const int TILE_N = tuned_tile_n(ctx, sizeof(T) == 8, order);
   const int64_t Lp = (order + TILE_N - 1) / TILE_N * TILE_N;
   const ArenaMark mk = ctx->arena.mark();
   __nv_bfloat16* St = ctx->arena.alloc_n<__nv_bfloat16>((size_t)Kp * Lp);
@@ -863,7 +883,7 @@ void tc_sketch(lra_ctx* ctx, const TcSplit& sp, int64_t order, const T* S, T* B,
   {
     cuuint64_t dims[2] = {(cuuint64_t)Kp, (cuuint64_t)Lp};
     cuuint64_t strides[1] = {(cuuint64_t)Kp * 2};
-    cuuint32_t box[2] = {KBLK, TILE_N};
+    cuuint32_t box[2] = {KBLK, (cuuint32_t)TILE_N};
     make_map(&tmS, St, 2, dims, strides, box);
   }
   int* err = err_slot;
@@ -883,10 +903,18 @@ void tc_sketch(lra_ctx* ctx, const TcSplit& sp, int64_t order, const T* S, T* B,
   P.ldb = ldb;
   P.out_double = sizeof(T) == 8 ? 1 : 0;
   P.err = err;
-  const size_t smem = 1024 + (size_t)NSTAGE * (S_BYTES + ns * TILE_BYTES) + 256;
-  raise_smem_limit(ctx, (const void*)tc_sketch_kernel);
+  const size_t smem = 1024 + (size_t)NSTAGE * ((size_t)TILE_N * KBLK * 2 + ns * TILE_BYTES) + 256;
   const int64_t ntiles = ((N + TILE_M - 1) / TILE_M) * (Lp / TILE_N);
-  tc_sketch_kernel<<<(unsigned)ntiles, NTHREADS, smem, ctx->stream>>>(tmA, tmS, P);
+  auto launch = [&](auto kern) {
+    raise_smem_limit(ctx, (const void*)kern);
+    kern<<<(unsigned)ntiles, NTHREADS, smem, ctx->stream>>>(tmA, tmS, P);
+  };
+  if (TILE_N == 32)
+    launch(tc_sketch_kernel<32>);
+  else if (TILE_N == 64)
+    launch(tc_sketch_kernel<64>);
+  else
+    launch(tc_sketch_kernel<96>);
   post_launch(ctx, "tc_sketch_kernel");
   // a caller that passes err_slot checks it later (the batch, once per
   // round) and releases the transposed sketch with its own arena mark: the
@@ -983,5 +1011,7 @@ template void tc_split<float>(lra_ctx*, char, int64_t, int64_t, const float*, in
 template void tc_split<double>(lra_ctx*, char, int64_t, int64_t, const double*, int64_t, int, TcSplit*, bool);
 template void tc_sketch<float>(lra_ctx*, const TcSplit&, int64_t, const float*, float*, int64_t, int*);
 template void tc_sketch<double>(lra_ctx*, const TcSplit&, int64_t, const double*, double*, int64_t, int*);
+
+cudaError_t set_wait_limit_tc(uint64_t ns) { return set_unit_wait_limit(ns); }
 
 }  // namespace lra

@@ -19,14 +19,22 @@ from dataclasses import dataclass
 import numpy as np
 
 from . import _ffi
-from ._ffi import LRA_F32, LRA_F64
+from ._ffi import LRA_C32, LRA_C64, LRA_F32, LRA_F64
+
+_NP_OF = {LRA_F32: np.float32, LRA_F64: np.float64, LRA_C32: np.complex64, LRA_C64: np.complex128}
+_DT_OF = {np.dtype(v): k for k, v in _NP_OF.items()}
+
+
+def _real_of(np_dtype):
+    """The real type of an element type (Float32 for ComplexF32, ...)."""
+    return np.float32 if np.dtype(np_dtype) in (np.float32, np.complex64) else np.float64
 
 __all__ = [
     "LRAOptions", "RandStream", "Context", "IDPackedV", "PartialQRFactors", "PartialQR", "PartialSVD",
     "PartialHermitianEigen", "CURPackedU", "CURFactor", "CUR", "idfact", "id", "pqrfact", "pqr", "psvdfact", "psvdvals",
     "psvd", "pheigfact", "pheigvals", "pheig", "curfact", "cur", "sketch", "sketchfact", "prange", "snorm",
     "snormdiff", "geqp3_adap", "matrixlib", "LRAError", "ArgumentError", "DimensionMismatch",
-    "lattice_gauss", "default_context", "Server", "idfact_batched",
+    "LinearOperator", "LinOp", "HermLinOp", "lattice_gauss", "library_gauss", "library_sketch_stream", "default_context", "Server", "idfact_batched",
 ]
 
 
@@ -150,6 +158,28 @@ def lattice_gauss(rng_or_seed, n: int) -> np.ndarray:
     return np.clip(np.rint(rng.standard_normal(n) * 32.0), -127, 127) / 32.0
 
 
+def library_gauss(seed: int, n: int, counter: int = 0, ctx=None) -> np.ndarray:
+    """The in-library generator's draws (lra_rand_gauss): n lattice
+    Gaussians of the Philox stream of `seed` from `counter` on -- what a call
+    with no injected stream multiplies as its Gaussian sketch."""
+    ctx = ctx or default_context()
+    out = np.empty(int(n), np.float64)
+    _raise(_ffi.load().lra_rand_gauss(ctx.handle, int(seed) & 0xFFFFFFFFFFFFFFFF, int(counter), int(n),
+                                      out.ctypes.data), ctx)
+    return out
+
+
+def library_sketch_stream(seed: int, M: int, orders, ctx=None) -> np.ndarray:
+    """The Gaussian draws of a fresh-context call's adaptive steps, in order
+    (step t: orders[t] * M values at counter c_t, c_(t+1) = c_t +
+    (orders[t] * M + 1) // 2), as one injectable stream."""
+    parts, c = [], 0
+    for l in orders:
+        parts.append(library_gauss(seed, l * M, c, ctx))
+        c += (l * M + 1) // 2
+    return np.concatenate(parts) if parts else np.zeros(0)
+
+
 class RandStream:
     """Injected random numbers (lra_rand): a float64 Gaussian stream and an
     int64 index stream, host numpy arrays or CUDA tensors."""
@@ -216,6 +246,27 @@ class Context:
     def set_stream(self, stream_ptr: int):
         _raise(_ffi.load().lra_ctx_set_stream(self.handle, C.c_void_p(stream_ptr)), self)
 
+    def tuning(self) -> str:
+        """The autotuned shapes in force and the table they came from."""
+        lib = _ffi.load()
+        n = lib.lra_ctx_get_tuning(self.handle, None, 0)
+        buf = C.create_string_buffer(max(int(n), 1))
+        lib.lra_ctx_get_tuning(self.handle, buf, len(buf))
+        return buf.value.decode()
+
+    def set_tuning(self, key: str, index: int, value: int):
+        """Override one tuning entry of this context (lra_ctx_set_tuning)."""
+        _raise(_ffi.load().lra_ctx_set_tuning(self.handle, key.encode(), int(index), int(value)), self)
+
+    def set_wait_limit(self, ns: int):
+        """Limit of the device-side bounded waits on this device (0: 4 s)."""
+        _raise(_ffi.load().lra_ctx_set_wait_limit(self.handle, int(ns)), self)
+
+    def probe_wait(self) -> int:
+        """The bounded-wait self-test (lra_ctx_probe_wait); returns its
+        status, LRA_ETIMEDOUT when the barrier gave up as designed."""
+        return int(_ffi.load().lra_ctx_probe_wait(self.handle))
+
 
 _DEFAULT = None
 
@@ -231,6 +282,125 @@ def _is_torch(a) -> bool:
     return type(a).__module__.startswith("torch")
 
 
+class _DevArray:
+    """A column-major device array (rows x cols, leading dimension ld) seen
+    through the CUDA array interface, for a zero-copy torch view."""
+
+    def __init__(self, ptr, rows, cols, ld, np_dtype):
+        isz = np.dtype(np_dtype).itemsize
+        self.__cuda_array_interface__ = {"shape": (rows, cols), "typestr": np.dtype(np_dtype).str,
+                                         "data": (int(ptr), False), "strides": (isz, max(ld, 1) * isz),
+                                         "version": 2}
+
+
+class LinearOperator:
+    """LinearOperator / HermitianLinearOperator (src/linop.jl:9-40): an m x n
+    operator known only through its products.  ``mul(X)`` returns A X and
+    ``mulc(Y)`` returns A' Y for CUDA tensors (X: n x k, Y: m x k); a
+    Hermitian operator needs ``mul`` only.  The factorizations take it in
+    place of a matrix (the lra_*_linop entry points): the library calls back
+    into ``mul`` / ``mulc`` on its own stream, which is torch's current
+    stream while they run.  Scalar multiples, sums, products and adjoints
+    build new operators, as the reference's operator algebra does
+    (src/linop.jl:96-153)."""
+
+    def __init__(self, m: int, n: int, mul, mulc=None, T=np.float64, hermitian: bool = False):
+        if hermitian and m != n:
+            raise DimensionMismatch(_ffi.LRA_EDIM, "a Hermitian operator must be square")
+        if mulc is None and not hermitian:
+            raise ArgumentError(_ffi.LRA_EINVAL, "mulc is required unless the operator is Hermitian")
+        self.m, self.n, self.hermitian = int(m), int(n), bool(hermitian)
+        self.mul, self.mulc = mul, (mul if hermitian else mulc)
+        self.np_dtype = np.dtype(T).type
+        if self.np_dtype not in (np.float32, np.float64):
+            raise ArgumentError(_ffi.LRA_EINVAL, "Float32 or Float64 operator expected")
+        self._cb = _ffi.MATMAT(self._matmat)
+        self.c = _ffi.lra_linop(self.m, self.n, LRA_F64 if self.np_dtype == np.float64 else LRA_F32,
+                                1 if hermitian else 0, self._cb, None)
+
+    @classmethod
+    def from_matrix(cls, A, hermitian=None):
+        """LinOp(A) (src/linop.jl:24-31) of a CUDA tensor: Hermitian when A
+        equals A' unless told otherwise."""
+        import torch
+        if hermitian is None:
+            hermitian = A.shape[0] == A.shape[1] and bool(torch.equal(A, A.T))
+        T = np.float64 if A.dtype == torch.float64 else np.float32
+        return cls(A.shape[0], A.shape[1], lambda X: A @ X, None if hermitian else (lambda Y: A.T @ Y), T,
+                   hermitian)
+
+    @property
+    def shape(self):
+        return (self.m, self.n)
+
+    @property
+    def H(self) -> "LinearOperator":
+        """adjoint(A) (src/linop.jl:42-43)."""
+        if self.hermitian:
+            return self
+        return LinearOperator(self.n, self.m, self.mulc, self.mul, self.np_dtype)
+
+    def __matmul__(self, X):
+        if isinstance(X, LinearOperator):
+            if self.n != X.m:
+                raise DimensionMismatch(_ffi.LRA_EDIM, "operator sizes")
+            a, b = self, X
+            return LinearOperator(a.m, b.n, lambda Z: a.mul(b.mul(Z)), lambda Z: b.mulc(a.mulc(Z)), a.np_dtype)
+        return self.mul(X)
+
+    def __mul__(self, c):
+        if isinstance(c, LinearOperator):
+            return self @ c
+        c = float(c)
+        return LinearOperator(self.m, self.n, lambda X: c * self.mul(X), lambda Y: c * self.mulc(Y),
+                              self.np_dtype, self.hermitian)
+
+    __rmul__ = __mul__
+
+    def __truediv__(self, c):
+        return self * (1.0 / float(c))
+
+    def __add__(self, o: "LinearOperator"):
+        if (self.m, self.n) != (o.m, o.n):
+            raise DimensionMismatch(_ffi.LRA_EDIM, "operator sizes")
+        return LinearOperator(self.m, self.n, lambda X: self.mul(X) + o.mul(X),
+                              lambda Y: self.mulc(Y) + o.mulc(Y), self.np_dtype, self.hermitian and o.hermitian)
+
+    def __neg__(self):
+        return self * -1.0
+
+    def __sub__(self, o):
+        return self + (-o)
+
+    def matrix(self):
+        """Matrix(A) = A * I (src/linop.jl:54)."""
+        import torch
+        dt = torch.float64 if self.np_dtype == np.float64 else torch.float32
+        return self.mul(torch.eye(self.n, dtype=dt, device="cuda"))
+
+    def _matmat(self, user, trans, ncols, X, ldx, Y, ldy, stream):
+        try:
+            import torch
+            tr = trans.decode() if isinstance(trans, bytes) else str(trans)
+            rin, rout = (self.n, self.m) if tr == "n" else (self.m, self.n)
+            Xt = torch.as_tensor(_DevArray(X, rin, ncols, ldx, self.np_dtype), device="cuda")
+            Yt = torch.as_tensor(_DevArray(Y, rout, ncols, ldy, self.np_dtype), device="cuda")
+            with torch.cuda.stream(torch.cuda.ExternalStream(int(stream or 0))):
+                Yt.copy_(self.mul(Xt) if tr == "n" else self.mulc(Xt))
+            return 0
+        except Exception as e:  # reported as LRA_ECUDA by the library
+            self.last_error = e
+            return 1
+
+
+def _lcall(lib, name, ctx, M, pre=(), post=()):
+    """lra_<name>(ctx, dtype, *pre, m, n, A, lda, *post) for a matrix, or
+    lra_<name>_linop(ctx, *pre, &op, *post) for a LinearOperator."""
+    if M.lin is not None:
+        return getattr(lib, name + "_linop")(ctx.handle, *pre, C.byref(M.lin.c), *post)
+    return getattr(lib, name)(ctx.handle, M.dtype, *pre, M.m, M.n, C.c_void_p(M.ptr), M.ld, *post)
+
+
 @dataclass
 class _Mat:
     ptr: int
@@ -240,33 +410,38 @@ class _Mat:
     dtype: int
     np_dtype: type
     keep: object
+    lin: object = None
 
 
 def _mat(A) -> _Mat:
+    if isinstance(A, LinearOperator):
+        return _Mat(0, A.m, A.n, max(A.m, 1), A.c.dtype, A.np_dtype, A, A)
     if _is_torch(A):
         import torch
         if A.dim() != 2:
             raise DimensionMismatch(_ffi.LRA_EDIM, "matrix expected")
-        if A.dtype not in (torch.float32, torch.float64):
-            raise ArgumentError(_ffi.LRA_EINVAL, "Float32 or Float64 matrix expected")
+        tmap = {torch.float32: LRA_F32, torch.float64: LRA_F64, torch.complex64: LRA_C32,
+                torch.complex128: LRA_C64}
+        if A.dtype not in tmap:
+            raise ArgumentError(_ffi.LRA_EINVAL, "Float32, Float64, ComplexF32 or ComplexF64 matrix expected")
         if not A.is_cuda:
             return _mat(A.numpy())
+        # the library works on its own stream: what torch queued to make A
+        # must be done before the library reads it
+        torch.cuda.current_stream(A.device).synchronize()
         m, n = A.shape
         if not (A.stride(0) == 1 and A.stride(1) >= max(1, m)):
             A = A.t().contiguous().t()
-        dt = LRA_F64 if A.dtype == torch.float64 else LRA_F32
-        return _Mat(A.data_ptr(), m, n, max(A.stride(1), 1), dt,
-                    np.float64 if dt == LRA_F64 else np.float32, A)
+        dt = tmap[A.dtype]
+        return _Mat(A.data_ptr(), m, n, max(A.stride(1), 1), dt, _NP_OF[dt], A)
     A = np.asarray(A)
     if A.ndim != 2:
         raise DimensionMismatch(_ffi.LRA_EDIM, "matrix expected")
-    if A.dtype not in (np.float32, np.float64):
-        if np.iscomplexobj(A):
-            raise ArgumentError(_ffi.LRA_ENOTSUP, "complex element types are not built")
-        A = A.astype(np.float64)
+    if A.dtype not in _DT_OF:
+        A = A.astype(np.complex128 if np.iscomplexobj(A) else np.float64)
     A = np.asfortranarray(A)
     m, n = A.shape
-    dt = LRA_F64 if A.dtype == np.float64 else LRA_F32
+    dt = _DT_OF[A.dtype]
     return _Mat(A.ctypes.data, m, n, max(m, 1), dt, A.dtype.type, A)
 
 
@@ -274,8 +449,7 @@ def _host(ptr, shape, dtype, order="F") -> np.ndarray:
     count = int(np.prod(shape)) if len(shape) else 1
     if count == 0 or not ptr:
         return np.zeros(shape, dtype=dtype, order=order)
-    ct = C.c_double if dtype == np.float64 else (C.c_float if dtype == np.float32 else C.c_int64)
-    buf = (ct * count).from_address(int(ptr) if not isinstance(ptr, int) else ptr)
+    buf = (C.c_byte * (count * np.dtype(dtype).itemsize)).from_address(int(ptr) if not isinstance(ptr, int) else ptr)
     return np.array(np.frombuffer(buf, dtype=dtype, count=count).reshape(shape, order=order), copy=True)
 
 
@@ -299,8 +473,7 @@ def _view(ptr, shape, dtype, owner, order="F") -> np.ndarray:
     count = int(np.prod(shape)) if len(shape) else 1
     if count == 0 or not ptr:
         return np.zeros(shape, dtype=dtype, order=order)
-    ct = C.c_double if dtype == np.float64 else (C.c_float if dtype == np.float32 else C.c_int64)
-    buf = (ct * count).from_address(int(ptr) if not isinstance(ptr, int) else ptr)
+    buf = (C.c_byte * (count * np.dtype(dtype).itemsize)).from_address(int(ptr) if not isinstance(ptr, int) else ptr)
     buf._owner = owner
     return np.frombuffer(buf, dtype=dtype, count=count).reshape(shape, order=order)
 
@@ -393,7 +566,7 @@ class PartialSVD:
         return len(self.S)
 
     def __getitem__(self, d):
-        return {"U": self.U, "S": self.S, "Vt": self.Vt, "V": None if self.Vt is None else self.Vt.T,
+        return {"U": self.U, "S": self.S, "Vt": self.Vt, "V": None if self.Vt is None else self.Vt.conj().T,
                 "k": self.k}[d]
 
     def matrix(self) -> np.ndarray:
@@ -414,7 +587,7 @@ class PartialHermitianEigen:
         return {"values": self.values, "vectors": self.vectors, "k": self.k}[d]
 
     def matrix(self) -> np.ndarray:
-        return (self.vectors * self.values) @ self.vectors.T
+        return (self.vectors * self.values) @ self.vectors.conj().T
 
 
 class CURPackedU:
@@ -437,8 +610,7 @@ def idfact(*args, **kwargs) -> IDPackedV:
     lib = _ffi.load()
     out = C.POINTER(_ffi.lra_id)()
     co = opts.to_c()
-    st = lib.lra_idfact(ctx.handle, M.dtype, trans.encode(), M.m, M.n, C.c_void_p(M.ptr), M.ld, C.byref(co),
-                        _rand(rand), C.byref(out))
+    st = _lcall(lib, "lra_idfact", ctx, M, (trans.encode(),), (C.byref(co), _rand(rand), C.byref(out)))
     _raise(st, ctx)
     r = out.contents
     own = _Result(lib.lra_id_free, out)
@@ -505,8 +677,7 @@ def pqrfact(*args, **kwargs):
     lib = _ffi.load()
     out = C.POINTER(_ffi.lra_pqr)()
     co = opts.to_c()
-    st = lib.lra_pqrfact(ctx.handle, M.dtype, trans.encode(), M.m, M.n, C.c_void_p(M.ptr), M.ld,
-                         C.byref(co), _rand(rand), C.byref(out))
+    st = _lcall(lib, "lra_pqrfact", ctx, M, (trans.encode(),), (C.byref(co), _rand(rand), C.byref(out)))
     _raise(st, ctx)
     return _pqr_out(lib, out, M.np_dtype, True)
 
@@ -527,8 +698,8 @@ def sketchfact(*args, **kwargs):
     lib = _ffi.load()
     out = C.POINTER(_ffi.lra_pqr)()
     co = opts.to_c()
-    st = lib.lra_sketchfact(ctx.handle, M.dtype, side[0].encode(), trans.encode(), M.m, M.n,
-                            C.c_void_p(M.ptr), M.ld, C.byref(co), _rand(rand), C.byref(out))
+    st = _lcall(lib, "lra_sketchfact", ctx, M, (side[0].encode(), trans.encode()),
+                (C.byref(co), _rand(rand), C.byref(out)))
     _raise(st, ctx)
     return _pqr_out(lib, out, M.np_dtype, True)
 
@@ -552,8 +723,7 @@ def prange(*args, **kwargs) -> np.ndarray:
     lib = _ffi.load()
     out = C.POINTER(_ffi.lra_pqr)()
     co = opts.to_c()
-    st = lib.lra_prange(ctx.handle, M.dtype, trans.encode(), M.m, M.n, C.c_void_p(M.ptr), M.ld, C.byref(co),
-                        _rand(rand), C.byref(out))
+    st = _lcall(lib, "lra_prange", ctx, M, (trans.encode(),), (C.byref(co), _rand(rand), C.byref(out)))
     _raise(st, ctx)
     return _pqr_out(lib, out, M.np_dtype, False).Q
 
@@ -619,13 +789,12 @@ def _psvd(A, opts, kwargs, vals_only):
     lib = _ffi.load()
     out = C.POINTER(_ffi.lra_psvd)()
     co = opts.to_c()
-    st = lib.lra_psvdfact(ctx.handle, M.dtype, M.m, M.n, C.c_void_p(M.ptr), M.ld, C.byref(co), _rand(rand),
-                          1 if vals_only else 0, C.byref(out))
+    st = _lcall(lib, "lra_psvdfact", ctx, M, (), (C.byref(co), _rand(rand), 1 if vals_only else 0, C.byref(out)))
     _raise(st, ctx)
     r = out.contents
     own = _Result(lib.lra_psvd_free, out)
     k = r.k
-    S = _view(r.S, (k,), M.np_dtype, own)
+    S = _view(r.S, (k,), _real_of(M.np_dtype), own)
     if vals_only:
         return S
     U = _view(r.U, (M.m, k), M.np_dtype, own)
@@ -737,13 +906,17 @@ def _pheig(A, opts, kwargs, vals_only):
     lib = _ffi.load()
     out = C.POINTER(_ffi.lra_pheig)()
     co = opts.to_c()
-    st = lib.lra_pheigfact(ctx.handle, M.dtype, M.n, C.c_void_p(M.ptr), M.ld, C.byref(co), _rand(rand),
-                           1 if vals_only else 0, C.byref(out))
+    if M.lin is not None:
+        st = lib.lra_pheigfact_linop(ctx.handle, C.byref(M.lin.c), C.byref(co), _rand(rand), 1 if vals_only else 0,
+                                     C.byref(out))
+    else:
+        st = lib.lra_pheigfact(ctx.handle, M.dtype, M.n, C.c_void_p(M.ptr), M.ld, C.byref(co), _rand(rand),
+                               1 if vals_only else 0, C.byref(out))
     _raise(st, ctx)
     r = out.contents
     try:
         k = r.k
-        w = _host(r.values, (k,), M.np_dtype)
+        w = _host(r.values, (k,), _real_of(M.np_dtype))
         if vals_only:
             return w
         return PartialHermitianEigen(w, _host(r.vectors, (M.n, k), M.np_dtype))
@@ -772,8 +945,7 @@ def curfact(A, opts: LRAOptions | None = None, **kwargs) -> CURPackedU:
     lib = _ffi.load()
     out = C.POINTER(_ffi.lra_cur)()
     co = opts.to_c()
-    st = lib.lra_curfact(ctx.handle, M.dtype, M.m, M.n, C.c_void_p(M.ptr), M.ld, C.byref(co), _rand(rand),
-                         C.byref(out))
+    st = _lcall(lib, "lra_curfact", ctx, M, (), (C.byref(co), _rand(rand), C.byref(out)))
     _raise(st, ctx)
     r = out.contents
     try:
@@ -814,7 +986,7 @@ def CUR(A, U: CURPackedU, ctx: "Context | None" = None) -> CURFactor:
     _raise(st, ctx)
     own = _Result(lib.lra_psvd_free, out)
     r = out.contents
-    W = PartialSVD(_view(r.U, (k, k), M.np_dtype, own), _view(r.S, (k,), M.np_dtype, own),
+    W = PartialSVD(_view(r.U, (k, k), M.np_dtype, own), _view(r.S, (k,), _real_of(M.np_dtype), own),
                    _view(r.Vt, (k, k), M.np_dtype, own))
     if _is_torch(A):
         import torch
@@ -868,8 +1040,11 @@ def snorm(A, opts: LRAOptions | None = None, hermitian=None, **kwargs) -> float:
     out = C.c_double()
     co = opts.to_c()
     herm = -1 if hermitian is None else (1 if hermitian else 0)
-    st = _ffi.load().lra_snorm(ctx.handle, M.dtype, M.m, M.n, C.c_void_p(M.ptr), M.ld, herm, C.byref(co),
-                               _rand(rand), C.byref(out))
+    if M.lin is not None:
+        st = _ffi.load().lra_snorm_linop(ctx.handle, C.byref(M.lin.c), C.byref(co), _rand(rand), C.byref(out))
+    else:
+        st = _ffi.load().lra_snorm(ctx.handle, M.dtype, M.m, M.n, C.c_void_p(M.ptr), M.ld, herm, C.byref(co),
+                                   _rand(rand), C.byref(out))
     _raise(st, ctx)
     return out.value
 
@@ -890,7 +1065,7 @@ def snormdiff(A, B, opts: LRAOptions | None = None, trans: str = "n", **kwargs) 
         st = lib.lra_snormdiff_id(ctx.handle, M.dtype, trans.encode(), M.m, M.n, C.c_void_p(M.ptr), M.ld,
                                   C.byref(cid), C.byref(co), _rand(rand), C.byref(out))
     elif isinstance(B, PartialSVD):
-        keep = [np.asfortranarray(B.U.astype(M.np_dtype)), np.ascontiguousarray(B.S.astype(M.np_dtype)),
+        keep = [np.asfortranarray(B.U.astype(M.np_dtype)), np.ascontiguousarray(B.S.astype(_real_of(M.np_dtype))),
                 np.asfortranarray(B.Vt.astype(M.np_dtype))]
         cps = _ffi.lra_psvd(M.dtype, 0, M.m, M.n, B.k, keep[0].ctypes.data, keep[1].ctypes.data,
                             keep[2].ctypes.data)
@@ -928,3 +1103,11 @@ def matrixlib(name: str, *args, dtype=np.float64) -> np.ndarray:
             x, y = np.asarray(args[0]), np.asarray(args[1])
         return np.asfortranarray(np.exp(-2j * np.pi * np.outer(x, y)))
     raise ArgumentError(_ffi.LRA_EINVAL, "name")
+
+
+LinOp = LinearOperator
+
+
+def HermLinOp(n: int, mul, T=np.float64) -> LinearOperator:
+    """HermitianLinearOperator (src/linop.jl:17-21, 33-39)."""
+    return LinearOperator(n, n, mul, None, T, True)

@@ -14,7 +14,7 @@ LIB_PATH = os.path.join(HERE, "liblra.so")
 
 LRA_OK, LRA_EINVAL, LRA_EDIM, LRA_ENOMEM, LRA_ETIMEDOUT, LRA_ENONFINITE, LRA_ECUDA, LRA_ERAND, \
     LRA_ENOTSUP, LRA_ENOTHERM, LRA_EBUSY = range(11)
-LRA_F32, LRA_F64 = 0, 1
+LRA_F32, LRA_F64, LRA_C32, LRA_C64 = 0, 1, 2, 3
 SKETCH = {"none": 0, "randn": 1, "sprn": 2, "srft": 3, "sub": 4}
 RET_Q, RET_R, RET_T = 1, 2, 4
 PREC = {"native": 0, "mixed": 1}
@@ -102,6 +102,16 @@ class lra_server_stats(C.Structure):
                 ("hbm_budget", C.c_int64), ("hbm_in_use", C.c_int64)]
 
 
+# the operator's product callback (lra_matmat_fn) and lra_linop
+MATMAT = C.CFUNCTYPE(C.c_int, C.c_void_p, C.c_char, C.c_int64, C.c_void_p, C.c_int64, C.c_void_p, C.c_int64,
+                     C.c_void_p)
+
+
+class lra_linop(C.Structure):
+    _fields_ = [("m", C.c_int64), ("n", C.c_int64), ("dtype", C.c_int32), ("hermitian", C.c_int32),
+                ("matmat", MATMAT), ("user", C.c_void_p)]
+
+
 # every exported entry point: (name, restype, argtypes)
 _vp, _i64, _i32, _d, _ch = C.c_void_p, C.c_int64, C.c_int, C.c_double, C.c_char
 _P = C.POINTER
@@ -113,6 +123,10 @@ SIGNATURES = [
     ("lra_status_string", C.c_char_p, [_i32]),
     ("lra_ctx_launches", _i64, [_vp]),
     ("lra_ctx_stage_ms", _i32, [_vp, _P(_d)]),
+    ("lra_ctx_set_tuning", _i32, [_vp, C.c_char_p, _i64, _i64]),
+    ("lra_ctx_get_tuning", _i32, [_vp, C.c_char_p, _i64]),
+    ("lra_ctx_set_wait_limit", _i32, [_vp, _i64]),
+    ("lra_ctx_probe_wait", _i32, [_vp]),
     ("lra_opts_init", _i32, [_P(lra_opts), _i32]),
     ("lra_chkopts", _i32, [_P(lra_opts)]),
     ("lra_sketch", _i32, [_vp, _i32, _ch, _ch, _i64, _i64, _vp, _i64, _i64, _P(lra_opts),
@@ -133,6 +147,7 @@ SIGNATURES = [
     ("lra_curfact", _i32, [_vp, _i32, _i64, _i64, _vp, _i64, _P(lra_opts), _P(lra_rand),
                            _P(_P(lra_cur))]),
     ("lra_cur_middle", _i32, [_vp, _i32, _i64, _i64, _vp, _i64, _i64, _P(_i64), _P(_i64), _P(_P(lra_psvd))]),
+    ("lra_rand_gauss", _i32, [_vp, C.c_uint64, C.c_uint64, _i64, _vp]),
     ("lra_dgemm", _i32, [_vp, _i32, C.c_char, C.c_char, _i64, _i64, _i64, _d, _vp, _i64, _vp, _i64, _d,
                          _vp, _i64]),
     ("lra_snorm", _i32, [_vp, _i32, _i64, _i64, _vp, _i64, _i32, _P(lra_opts), _P(lra_rand),
@@ -143,6 +158,14 @@ SIGNATURES = [
                                 _P(lra_rand), _P(_d)]),
     ("lra_snormdiff_psvd", _i32, [_vp, _i32, _i64, _i64, _vp, _i64, _P(lra_psvd), _P(lra_opts),
                                   _P(lra_rand), _P(_d)]),
+    ("lra_sketchfact_linop", _i32, [_vp, _ch, _ch, _P(lra_linop), _P(lra_opts), _P(lra_rand), _P(_P(lra_pqr))]),
+    ("lra_idfact_linop", _i32, [_vp, _ch, _P(lra_linop), _P(lra_opts), _P(lra_rand), _P(_P(lra_id))]),
+    ("lra_pqrfact_linop", _i32, [_vp, _ch, _P(lra_linop), _P(lra_opts), _P(lra_rand), _P(_P(lra_pqr))]),
+    ("lra_prange_linop", _i32, [_vp, _ch, _P(lra_linop), _P(lra_opts), _P(lra_rand), _P(_P(lra_pqr))]),
+    ("lra_psvdfact_linop", _i32, [_vp, _P(lra_linop), _P(lra_opts), _P(lra_rand), _i32, _P(_P(lra_psvd))]),
+    ("lra_pheigfact_linop", _i32, [_vp, _P(lra_linop), _P(lra_opts), _P(lra_rand), _i32, _P(_P(lra_pheig))]),
+    ("lra_curfact_linop", _i32, [_vp, _P(lra_linop), _P(lra_opts), _P(lra_rand), _P(_P(lra_cur))]),
+    ("lra_snorm_linop", _i32, [_vp, _P(lra_linop), _P(lra_opts), _P(lra_rand), _P(_d)]),
     ("lra_idfact_batched", _i32, [_vp, _i32, _i64, _P(lra_matdesc), _P(lra_opts), _P(lra_rand),
                                   _P(_P(lra_id))]),
     ("lra_server_create", _i32, [_i32, _i32, _i64, _P(_vp)]),

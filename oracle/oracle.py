@@ -96,7 +96,7 @@ def _lapack():
         for c in cands:
             try:
                 lib = ctypes.CDLL(c)
-                for s in ("d", "s"):
+                for s in ("d", "s", "z", "c"):
                     f = getattr(lib, f"scipy_{s}laqps_64_")
                     f.argtypes = [_p] * 14
                     f.restype = None
@@ -112,7 +112,26 @@ def _ptr(a: np.ndarray) -> int:
 
 
 def _sfx(dtype) -> str:
-    return "d" if np.dtype(dtype) == np.float64 else "s"
+    return {np.dtype(np.float64): "d", np.dtype(np.float32): "s", np.dtype(np.complex128): "z",
+            np.dtype(np.complex64): "c"}[np.dtype(dtype)]
+
+
+def _H(X):
+    """X' in the reference: the conjugate transpose."""
+    return X.conj().T if np.iscomplexobj(X) else X.T
+
+
+def _real(dtype):
+    return np.float32 if np.dtype(dtype) in (np.float32, np.complex64) else np.float64
+
+
+def crandn(rs: "RandStream", n: int, dtype) -> np.ndarray:
+    """crandn(T, n) (src/util.jl:4-11) from the stream: real types take n
+    values, complex types n pairs (re, im) of the reinterpreted real draw."""
+    if np.iscomplexobj(np.zeros(0, dtype)):
+        g = rs.take_gauss(2 * n)
+        return (g[0::2] + 1j * g[1::2]).astype(dtype)
+    return rs.take_gauss(n).astype(dtype)
 
 
 # --------------------------------------------------------------------------
@@ -190,8 +209,8 @@ def laqps(m, n, offset, nb, a, lda, jpvt, tau, vn1, vn2, auxv, f, ldf, *, backen
     pa = _ptr(a) + a_off * lda * isz
     pj = _ptr(jpvt) + a_off * 8
     pt = _ptr(tau) + a_off * isz
-    p1 = _ptr(vn1) + v_off * isz
-    p2 = _ptr(vn2) + v_off * isz
+    p1 = _ptr(vn1) + v_off * vn1.dtype.itemsize
+    p2 = _ptr(vn2) + v_off * vn2.dtype.itemsize
     if backend == "oracle":
         getattr(_lib(), f"ora_{_sfx(dt)}laqps")(m, n, offset, nb, _ptr(kb), pa, lda, pj, pt, p1,
                                                  p2, _ptr(auxv), _ptr(f), ldf)
@@ -227,6 +246,8 @@ def geqp3_adap(B: np.ndarray, opts: Opts, backend: str = "oracle"):
     tau = np.zeros(max(k, 1), B.dtype)
     if k <= 0:
         return jpvt, tau[:0], 0
+    if np.iscomplexobj(B) and backend != "lapack":
+        return _geqp3_complex(B, opts, k, jpvt, tau)
     if backend == "c":
         kout = np.zeros(1, np.int64)
         getattr(_lib(), f"ora_{_sfx(B.dtype)}geqp3_adap")(
@@ -234,9 +255,9 @@ def geqp3_adap(B: np.ndarray, opts: Opts, backend: str = "oracle"):
             int(opts.rank), int(opts.nb), _ptr(kout))
         return jpvt, tau[:k], int(kout[0])
     nb = min(opts.nb, k)
-    vn1 = np.empty(n, B.dtype)
+    vn1 = np.empty(n, _real(B.dtype))
     for j in range(n):
-        vn1[j] = _nrm2(B[:, j])
+        vn1[j] = _nrm2(B[:, j]) if not np.iscomplexobj(B) else np.linalg.norm(B[:, j])
     vn2 = vn1.copy()
     maxnrm = float(vn1.max()) if n else 0.0
     ptol = max(opts.atol, opts.rtol * maxnrm)
@@ -256,6 +277,71 @@ def geqp3_adap(B: np.ndarray, opts: Opts, backend: str = "oracle"):
     return jpvt, tau[:k], k
 
 
+def _geqp3_complex(B, opts: Opts, kmax: int, jpvt, tau):
+    """geqp3_adap! for complex types (src/pqr.jl:348-418) with the rules of
+    ZLAQPS / CLAQPS (src/lapack.jl:117-139) column by column: IxAMAX pivots
+    on the partial norms, the complex xLARFG reflector (beta real), H^H
+    applied to the trailing columns, the tol3z downdate whose unreliable
+    columns are recomputed and end the block, and the block-end rank test.
+    Checked against the real LAPACK routine in the oracle's tests."""
+    m, n = B.shape
+    rdt = _real(B.dtype)
+    eps = float(np.finfo(rdt).eps) / 2
+    tol3z = np.sqrt(eps)
+    vn1 = np.array([np.linalg.norm(B[:, j]) for j in range(n)], np.float64)
+    vn2 = vn1.copy()
+    ptol = max(opts.atol, opts.rtol * (vn1.max() if n else 0.0))
+    lastrk = min(m, n)
+    nb = max(1, min(opts.nb, kmax))
+    c = 0
+    while c < kmax:
+        jb = min(nb, kmax - c)
+        kk, first_small, last_small, flag = 0, -1, False, False
+        while kk < jb and not flag:
+            pvt = c + int(np.argmax(vn1[c:]))
+            if pvt != c:
+                B[:, [c, pvt]] = B[:, [pvt, c]]
+                jpvt[c], jpvt[pvt] = jpvt[pvt], jpvt[c]
+                vn1[pvt], vn2[pvt] = vn1[c], vn2[c]
+            alpha = complex(B[c, c])
+            x = B[c + 1:, c].astype(np.complex128)
+            xnorm = float(np.linalg.norm(x))
+            if xnorm == 0 and alpha.imag == 0:
+                t, beta, scal = 0j, alpha.real, 1.0 + 0j
+            else:
+                r = float(np.sqrt(alpha.real ** 2 + alpha.imag ** 2 + xnorm ** 2))
+                beta = -np.copysign(r, alpha.real)
+                t = complex((beta - alpha.real) / beta, -alpha.imag / beta)
+                scal = 1.0 / (alpha - beta)
+            tau[c] = t
+            v = np.concatenate([[1.0 + 0j], x * scal])
+            if t != 0 and c + 1 < n:
+                W = v.conj() @ B[c:, c + 1:].astype(np.complex128)
+                B[c:, c + 1:] = (B[c:, c + 1:] - np.conj(t) * np.outer(v, W)).astype(B.dtype)
+            B[c, c] = beta
+            B[c + 1:, c] = (x * scal).astype(B.dtype)
+            if c < lastrk - 1:
+                for j in range(c + 1, n):
+                    if vn1[j] != 0:
+                        temp = abs(complex(B[c, j])) / vn1[j]
+                        temp = max(0.0, (1 + temp) * (1 - temp))
+                        temp2 = temp * (vn1[j] / vn2[j]) ** 2
+                        if temp2 <= tol3z:
+                            vn1[j] = vn2[j] = np.linalg.norm(B[c + 1:, j])
+                            flag = True
+                        else:
+                            vn1[j] *= np.sqrt(temp)
+            small = abs(beta) <= ptol
+            if small and first_small < 0:
+                first_small = c
+            last_small = small
+            c += 1
+            kk += 1
+        if last_small:
+            return jpvt, tau[:kmax], first_small
+    return jpvt, tau[:kmax], kmax
+
+
 def _nrm2(x: np.ndarray):
     """xNRM2 of the C restatement."""
     x = np.ascontiguousarray(x)
@@ -266,6 +352,11 @@ def maxdet_t(R: np.ndarray) -> np.ndarray:
     """T = R11 \\ R12 (src/pqr.jl:438-442), back substitution like xTRSM."""
     k, n = R.shape
     R = np.asfortranarray(R)
+    if np.iscomplexobj(R):
+        import scipy.linalg
+        if k == 0 or n == k:
+            return np.zeros((k, n - k), R.dtype, order="F")
+        return np.asfortranarray(scipy.linalg.solve_triangular(np.triu(R[:, :k]), R[:, k:]).astype(R.dtype))
     T = np.zeros((k, n - k), R.dtype, order="F")
     if k > 0 and n > k:
         getattr(_lib(), f"ora_{_sfx(R.dtype)}maxdet_t")(k, n, _ptr(R), max(1, k), _ptr(T), max(1, k))
@@ -343,7 +434,7 @@ def _orgqr(V: np.ndarray, tau: np.ndarray) -> np.ndarray:
         v = np.zeros(m, V.dtype)
         v[i] = 1
         v[i + 1:] = V[i + 1:, i]
-        w = v[i:] @ Q[i:, :]
+        w = v[i:].conj() @ Q[i:, :]
         Q[i:, :] -= tau[i] * np.outer(v[i:], w)
     return Q
 
@@ -358,16 +449,16 @@ def pqrfact_backend(B: np.ndarray, opts: Opts, backend: str = "oracle") -> dict:
 # --------------------------------------------------------------------------
 
 def _op(A, trans):
-    return A if trans == "n" else A.T
+    return A if trans == "n" else _H(A)
 
 
 def orthrows(B):
     """orthrows!(thin=false) (src/util.jl:87-97): LQ, keep Q's rows."""
     m, n = B.shape
     k = min(m, n)
-    q, _ = np.linalg.qr(B.T)
+    q, _ = np.linalg.qr(_H(B))
     out = np.zeros_like(B)
-    out[:k, :] = q[:, :k].T
+    out[:k, :] = _H(q[:, :k])
     return out
 
 
@@ -381,7 +472,7 @@ def orthcols(B):
 
 
 def _ishermitian(A) -> bool:
-    return A.shape[0] == A.shape[1] and np.array_equal(A, A.T)
+    return A.shape[0] == A.shape[1] and np.array_equal(A, _H(A))
 
 
 def sketch_randn(side, trans, A, order, opts: Opts, rs: RandStream):
@@ -391,11 +482,11 @@ def sketch_randn(side, trans, A, order, opts: Opts, rs: RandStream):
     opA = _op(A, trans)
     if side == "left":
         M = opA.shape[0]
-        S = rs.take_gauss(order * M).reshape((order, M), order="F").astype(dt)
+        S = crandn(rs, order * M, dt).reshape((order, M), order="F")
         Bp = S @ opA
         for _ in range(opts.sketch_randn_niter):
             Bp = orthrows(Bp)
-            Bq = Bp @ opA.T
+            Bq = Bp @ _H(opA)
             if isherm:
                 Bp = Bq
             else:
@@ -403,11 +494,11 @@ def sketch_randn(side, trans, A, order, opts: Opts, rs: RandStream):
                 Bp = Bq @ opA
         return np.asfortranarray(Bp.astype(dt))
     N = opA.shape[1]
-    S = rs.take_gauss(N * order).reshape((N, order), order="F").astype(dt)
+    S = crandn(rs, N * order, dt).reshape((N, order), order="F")
     Bp = opA @ S
     for _ in range(opts.sketch_randn_niter):
         Bp = orthcols(Bp)
-        Bq = opA.T @ Bp
+        Bq = _H(opA) @ Bp
         if isherm:
             Bp = Bq
         else:
@@ -508,16 +599,62 @@ def srft_exact(Xin: np.ndarray, d: np.ndarray, idx: np.ndarray, k: int) -> np.nd
     return out.astype(Xin.dtype)
 
 
+def srft_sampled_dft(Xin: np.ndarray, d: np.ndarray, idx: np.ndarray, k: int, chunk: int = 8192) -> np.ndarray:
+    """srft_exact's output computed from the sampled DFT rows only: for the
+    frequencies f = idx[i] - 1 it forms exp(-2 pi i f j / M) with the phase
+    reduced exactly as (f * j) mod M, and multiplies by d * x (float64 GEMMs
+    over row chunks).  Same values as the full FFT up to rounding, at a cost
+    of 2 k M c flops, which keeps tall sketches (65536 rows) tractable."""
+    M, c = Xin.shape
+    pos = list(range(0, k, 2))
+    freqs = np.array([int(idx[i]) - 1 for i in pos], np.int64)
+    npos = len(pos)
+    acc = np.zeros((2 * npos, c))           # rows: Re of each frequency, then Im
+    for j0 in range(0, M, chunk):
+        j = np.arange(j0, min(M, j0 + chunk), dtype=np.int64)
+        ang = (2 * np.pi / M) * ((freqs[:, None] * j[None, :]) % M).astype(np.float64)
+        E = np.concatenate([np.cos(ang), -np.sin(ang)])
+        X = d[j0:j0 + len(j), None] * Xin[j0:j0 + len(j), :].astype(np.float64)
+        acc += E @ X
+    out = np.zeros((k, c))
+    for r, i in enumerate(pos):
+        out[i] = acc[r]
+        if i + 1 < k:
+            out[i + 1] = acc[npos + r]
+    return out.astype(Xin.dtype)
+
+
+def srft_sampled_dft_complex(Xin: np.ndarray, d: np.ndarray, idx: np.ndarray, k: int, chunk: int = 8192):
+    """The complex SRFT (srft_apply! for complex types, src/sketch.jl:452-472):
+    y_i = sum_t d_t x_t exp(-2 pi i f_i t / M), f_i = idx_i - 1, one
+    complex value per index, the phase reduced exactly as (f t) mod M."""
+    M, c = Xin.shape
+    f = np.asarray(idx, np.int64) - 1
+    out = np.zeros((k, c), np.complex128)
+    for j0 in range(0, M, chunk):
+        j = np.arange(j0, min(M, j0 + chunk), dtype=np.int64)
+        E = np.exp(-2j * np.pi * (((f[:, None] * j[None, :]) % M).astype(np.float64) / M))
+        out += E @ (d[j0:j0 + len(j), None] * Xin[j0:j0 + len(j), :].astype(np.complex128))
+    return out.astype(Xin.dtype)
+
+
 def sketch_srft(side, trans, A, order, rs: RandStream, fast: bool = False):
     """SRFT mul! (src/sketch.jl:474-522), real types, left side."""
     opA = _op(A, trans)
     if side != "left":
         return sketch_srft("left", "n", opA.T, order, rs, fast).T.copy(order="F")
     M = opA.shape[0]
+    if np.iscomplexobj(opA):
+        # random phases crandn / |crandn| (src/sketch.jl:345-351); the
+        # sample is the DFT of d .* x at the frequencies idx (:452-472)
+        z = crandn(rs, M, np.complex128)
+        d = z / np.abs(z)
+        idx = (rs.take_ints(order) - 1) % M + 1
+        return np.asfortranarray(srft_sampled_dft_complex(opA, d, idx, order))
     d = np.where(rs.take_gauss(M) > 0, 1.0, -1.0)
     idx = (rs.take_ints(order) - 1) % M + 1
     if fast:
-        return np.asfortranarray(srft_exact(opA, d, idx, order))
+        return np.asfortranarray(srft_sampled_dft(opA, d, idx, order))
     return np.asfortranarray(_srft_apply_columns(opA, d, idx, order))
 
 
@@ -528,7 +665,7 @@ def sketch_sprn(side, trans, A, order, rs: RandStream):
         return sketch_sprn("left", "n", opA.T, order, rs).T.copy(order="F")
     M, N = opA.shape
     r = np.argsort(rs.take_ints(M), kind="stable")      # randperm(m) from M keys
-    g = rs.take_gauss(M).astype(A.dtype)
+    g = crandn(rs, M, A.dtype)
     C = np.zeros((order, N), A.dtype, order="F")
     idx = 0
     for i in range(1, order + 1):
@@ -579,10 +716,11 @@ def sketchfact(side, trans, A, opts: Opts, rs: RandStream, backend="oracle", fas
         while True:
             order = _samp(opts, n)
             B = sketch(side, trans, A, order, opts, rs, fast_srft)
+            B0 = B.copy(order="F") if trace is not None else None
             p, tau, k = geqp3_adap(B, opts_, backend)
             steps += 1
             if trace is not None:
-                trace.append({"order": order, "k": k})
+                trace.append({"order": order, "k": k, "B": B0})
             if k < n:
                 F = pqrback_postproc(B, p, tau, k, opts)
                 F["nsteps"] = steps
@@ -590,6 +728,8 @@ def sketchfact(side, trans, A, opts: Opts, rs: RandStream, backend="oracle", fas
             n *= 2
     order = _samp(opts, opts.rank)
     B = sketch(side, trans, A, order, opts, rs, fast_srft)
+    if trace is not None:
+        trace.append({"order": order, "B": B.copy(order="F")})
     F = pqrfact_backend(B, opts, backend)
     F["nsteps"] = 1
     return F
@@ -633,7 +773,7 @@ def prange(trans, A, opts: Opts, rs: RandStream, backend="oracle") -> np.ndarray
 def _getcols(trans, A, cols):
     """getcols (src/util.jl:25-29), cols 1-based."""
     c = np.asarray(cols, np.int64) - 1
-    return np.asfortranarray(A[:, c] if trans == "n" else A[c, :].T)
+    return np.asfortranarray(A[:, c] if trans == "n" else _H(A[c, :]))
 
 
 def idfact(trans, A, opts: Opts, rs: RandStream, backend="oracle", fast_srft=False,
@@ -641,7 +781,10 @@ def idfact(trans, A, opts: Opts, rs: RandStream, backend="oracle", fast_srft=Fal
     """idfact (src/id.jl:434-447): returns sk, rd (1-based), T, k."""
     opts = replace(opts.for_dtype(A.dtype), pqrfact_retval="t")
     if opts.sketch == "none":
-        F = pqrfact_backend(np.asfortranarray(_op(A, trans).copy()), opts, backend)
+        B = np.asfortranarray(_op(A, trans).copy())
+        if trace is not None:
+            trace.append({"order": None, "B": B.copy(order="F")})
+        F = pqrfact_backend(B, opts, backend)
         F["nsteps"] = 0
     else:
         F = sketchfact("left", trans, A, opts, rs, backend, fast_srft, trace)
@@ -662,12 +805,15 @@ def id_matrix(trans, A, V) -> np.ndarray:
     return out
 
 
-def pqrfact(trans, A, opts: Opts, rs: RandStream, backend="oracle") -> dict:
+def pqrfact(trans, A, opts: Opts, rs: RandStream, backend="oracle", trace=None) -> dict:
     """pqrfact (src/pqr.jl:290-307)."""
     opts = opts.for_dtype(A.dtype)
     if opts.sketch == "none":
-        return pqrfact_backend(np.asfortranarray(_op(A, trans).copy()), opts, backend)
-    V = idfact(trans, A, opts, rs, backend)
+        B = np.asfortranarray(_op(A, trans).copy())
+        if trace is not None:
+            trace.append({"order": None, "B": B.copy(order="F")})
+        return pqrfact_backend(B, opts, backend)
+    V = idfact(trans, A, opts, rs, backend, trace=trace)
     Aq = _getcols(trans, A, V["sk"])
     q, r = np.linalg.qr(Aq)
     out = {"p": np.concatenate([V["sk"], V["rd"]]), "k": V["k"], "T": None, "Q": None, "R": None}
@@ -702,12 +848,12 @@ def _v_matrix(V, n, dtype):
     return out
 
 
-def psvdfact(A, opts: Opts, rs: RandStream, backend="oracle", vals_only=False) -> dict:
+def psvdfact(A, opts: Opts, rs: RandStream, backend="oracle", vals_only=False, trace=None) -> dict:
     """psvdfact / psvdvals (src/psvd.jl:238-290)."""
     opts = opts.for_dtype(A.dtype)
     m, n = A.shape
     if m >= n:
-        V = idfact("n", A, opts, rs, backend)
+        V = idfact("n", A, opts, rs, backend, trace=trace)
         q, r = np.linalg.qr(_getcols("n", A, V["sk"]))
         W = r @ _v_matrix(V, n, A.dtype)
         if vals_only:
@@ -715,9 +861,9 @@ def psvdfact(A, opts: Opts, rs: RandStream, backend="oracle", vals_only=False) -
         else:
             u, s, vt = np.linalg.svd(W, full_matrices=False)
     else:
-        V = idfact("c", A, opts, rs, backend)
+        V = idfact("c", A, opts, rs, backend, trace=trace)
         q, r = np.linalg.qr(_getcols("c", A, V["sk"]))
-        W = _v_matrix(V, m, A.dtype).T @ r.T
+        W = _H(_v_matrix(V, m, A.dtype)) @ _H(r)
         if vals_only:
             s = np.linalg.svd(W, compute_uv=False)
         else:
@@ -730,8 +876,8 @@ def psvdfact(A, opts: Opts, rs: RandStream, backend="oracle", vals_only=False) -
         Vt = vt[:k, :]
     else:
         U = u[:, :k]
-        Vt = vt[:k, :] @ q.T
-    return {"U": U, "S": s[:k], "Vt": Vt, "k": k, "id_k": V["k"]}
+        Vt = vt[:k, :] @ _H(q)
+    return {"U": U, "S": s[:k], "Vt": Vt, "k": k, "id_k": V["k"], "sk": V["sk"], "rd": V["rd"]}
 
 
 def _pheigrank1(w, opts: Opts, wmax):
@@ -777,18 +923,19 @@ def pheigorth(values, vectors, opts: Opts):
         a = b + 1
 
 
-def pheigfact(A, opts: Opts, rs: RandStream, backend="oracle", vals_only=False) -> dict:
+def pheigfact(A, opts: Opts, rs: RandStream, backend="oracle", vals_only=False, trace=None) -> dict:
     """pheigfact / pheigvals (src/pheig.jl:276-311)."""
     opts = opts.for_dtype(A.dtype)
     if not _ishermitian(A):
         raise ValueError("matrix must be Hermitian")
     n = A.shape[0]
-    V = idfact("n", A, opts, rs, backend)
-    q, r = np.linalg.qr(_v_matrix(V, n, A.dtype).T)
+    V = idfact("n", A, opts, rs, backend, trace=trace)
+    q, r = np.linalg.qr(_H(_v_matrix(V, n, A.dtype)))
     sk = V["sk"] - 1
-    B = r @ (A[np.ix_(sk, sk)] @ r.T)
-    B = np.triu(B) + np.triu(B, 1).T
-    Bh = 0.5 * (B + B.T)
+    B = r @ (A[np.ix_(sk, sk)] @ _H(r))
+    # hermitianize!(B) (src/util.jl:31-45): the averaged upper triangle
+    U = 0.5 * (B + _H(B))
+    Bh = np.triu(U) + _H(np.triu(U, 1))
     if vals_only:
         w = np.linalg.eigvalsh(Bh)
     else:
@@ -801,7 +948,7 @@ def pheigfact(A, opts: Opts, rs: RandStream, backend="oracle", vals_only=False) 
         return {"values": w, "k": len(w)}
     Z = Z[:, idx].copy()
     pheigorth(w, Z, opts)
-    return {"values": w, "vectors": q @ Z, "k": len(w)}
+    return {"values": w, "vectors": q @ Z, "k": len(w), "id_k": V["k"], "sk": V["sk"], "rd": V["rd"]}
 
 
 def curfact(A, opts: Opts, rs: RandStream, backend="oracle") -> dict:
@@ -835,8 +982,8 @@ def cur_build(A, U: dict) -> dict:
     cols = np.asarray(U["cols"], np.int64)
     C = np.asfortranarray(A[:, cols - 1])
     R = np.asfortranarray(A[rows - 1, :])
-    Uw, s, Vt = np.linalg.svd(C[rows - 1, :].astype(np.float64))
-    return {"rows": rows, "cols": cols, "C": C, "R": R, "U": (Vt.T, 1.0 / s, Uw.T)}
+    Uw, s, Vt = np.linalg.svd(C[rows - 1, :].astype(np.complex128 if np.iscomplexobj(C) else np.float64))
+    return {"rows": rows, "cols": cols, "C": C, "R": R, "U": (_H(Vt), 1.0 / s, _H(Uw))}
 
 
 def _curfact_none(A, opts, backend):
@@ -847,14 +994,14 @@ def _curfact_none(A, opts, backend):
         return {"kind": 1, "rows": cols.copy(), "cols": cols.copy()}
     m, n = A.shape
     if m >= n:
-        F = pqrfact_backend(np.asfortranarray(A.T.copy()), opts, backend)
+        F = pqrfact_backend(np.asfortranarray(_H(A).copy()), opts, backend)
         rows = F["p"][:F["k"]]
         F = pqrfact_backend(np.asfortranarray(A[rows - 1, :]), opts, backend)
         cols = F["p"][:F["k"]]
     else:
         F = pqrfact_backend(np.asfortranarray(A.copy()), opts, backend)
         cols = F["p"][:F["k"]]
-        F = pqrfact_backend(np.asfortranarray(A[:, cols - 1].T), opts, backend)
+        F = pqrfact_backend(np.asfortranarray(_H(A[:, cols - 1])), opts, backend)
         rows = F["p"][:F["k"]]
     k = min(len(rows), len(cols))
     return {"kind": 0, "rows": rows[:k].copy(), "cols": cols[:k].copy()}
@@ -883,14 +1030,14 @@ def snorm(apply, applyc, n: int, dtype, opts: Opts, rs: RandStream, hermitian=Fa
 
 def snorm_dense(A, opts: Opts, rs: RandStream) -> float:
     herm = _ishermitian(A)
-    return snorm(lambda x: A @ x, lambda y: A.T @ y, A.shape[1], A.dtype.type, opts, rs, herm)
+    return snorm(lambda x: A @ x, lambda y: _H(A) @ y, A.shape[1], A.dtype.type, opts, rs, herm)
 
 
 def snormdiff_dense(A, B, opts: Opts, rs: RandStream) -> float:
     """snormdiff(A, B) = snorm(LinOp(A) - LinOp(B)) (src/snorm.jl:50-53);
     the difference is Hermitian only if both are (src/linop.jl:163-169)."""
     herm = _ishermitian(A) and _ishermitian(B)
-    return snorm(lambda x: A @ x - B @ x, lambda y: A.T @ y - B.T @ y, A.shape[1],
+    return snorm(lambda x: A @ x - B @ x, lambda y: _H(A) @ y - _H(B) @ y, A.shape[1],
                  A.dtype.type, opts, rs, herm)
 
 

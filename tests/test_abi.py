@@ -109,3 +109,27 @@ def test_python_argument_checks_before_the_device():
         L.prange("x", A)
     with pytest.raises(L.DimensionMismatch):
         L.CUR(A, L.CURPackedU(np.array([1, 2]), np.array([1])))
+
+
+def test_tuning_table_syntax():
+    """The committed tuning table (written by lowrankapprox/autotune.py)
+    holds only keys and values the library accepts."""
+    path = os.path.join(ROOT, "lowrankapprox.jl_gb300", "lowrankapprox", "tuning_gb300.txt")
+    if not os.path.exists(path):
+        pytest.skip("no tuning table committed")
+    seen = set()
+    for line in open(path):
+        line = line.split("#", 1)[0].split()
+        if not line:
+            continue
+        key = line[0]
+        seen.add(key)
+        if key == "tc_tile_n":
+            assert line[1] in ("f32", "f64") and 0 <= int(line[2]) < 16 and int(line[3]) in (32, 64, 96)
+        elif key == "qr_seq_len":
+            assert 0 <= int(line[1]) <= 4096
+        elif key == "srft_wide":
+            assert 0 <= int(line[1]) <= 10 and int(line[2]) in (0, 1)
+        else:
+            raise AssertionError(f"unknown key {key}")
+    assert {"tc_tile_n", "qr_seq_len", "srft_wide"} <= seen

@@ -21,14 +21,24 @@ def assert_pqr_parity(p, R, p_ref, R_ref, k, tol, name=""):
         assert np.abs(R[:, k:][:, o] - R_ref[:, k:][:, o_ref]).max() <= tol * scale, name
 
 
+def _wide(B):
+    """B in double precision (complex128 for complex types)."""
+    return np.asarray(B, np.complex128 if np.iscomplexobj(B) else np.float64)
+
+
 def residual_norms(B, piv, cols):
-    """Norms of columns `cols` of B after projecting out B[:, piv] (float64)."""
-    B = np.asarray(B, np.float64)
+    """Norms of columns `cols` of B after projecting out B[:, piv] (double
+    precision)."""
+    B = _wide(B)
     X = B[:, np.asarray(cols) - 1]
     if len(piv):
         Q, _ = np.linalg.qr(B[:, np.asarray(piv) - 1])
-        X = X - Q @ (Q.T @ X)
+        X = X - Q @ (Q.conj().T @ X)
     return np.linalg.norm(X, axis=0)
+
+
+def _single(dt):
+    return np.dtype(dt) in (np.float32, np.complex64)
 
 
 def check_pivots(B, p, p_ref, k, dt, name=""):
@@ -36,9 +46,9 @@ def check_pivots(B, p, p_ref, k, dt, name=""):
     are a near-tie: there, the exact residual norms of both candidates agree
     to the precision's tie tolerance, and the sequences may differ after.
     Returns the number of leading pivots that agree."""
-    tie = 5e-4 if np.dtype(dt) == np.float32 else 1e-9
+    tie = 5e-4 if _single(dt) else 1e-9
     eps = float(np.finfo(dt).eps)
-    floor = 1e3 * eps * float(np.linalg.norm(np.asarray(B, np.float64), axis=0).max())
+    floor = 1e3 * eps * float(np.linalg.norm(_wide(B), axis=0).max())
     for i in range(k):
         if p[i] == p_ref[i]:
             continue
@@ -47,6 +57,40 @@ def check_pivots(B, p, p_ref, k, dt, name=""):
         assert abs(r[0] - r[1]) <= tie * r.max() + floor, (name, i, r)
         return i
     return k
+
+
+def tie_tolerances(B, dt):
+    tie = 5e-4 if _single(dt) else 1e-9
+    eps = float(np.finfo(dt).eps)
+    return tie, 1e3 * eps * float(np.linalg.norm(_wide(B), axis=0).max())
+
+
+def check_rank(B, k, k_ref, p, p_ref, rtol, dt, atol=0.0, nb=32, name=""):
+    """Ranks equal, or different only where geqp3_adap!'s stop test
+    (|R_ii| <= ptol, src/pqr.jl:404-413) sits on a near-tie: among the
+    pivots of the blocks around the two ranks, some exact residual norm
+    equals ptol = max(atol, rtol * max column norm) to within the
+    precision's tie tolerance (or lies at the rounding floor)."""
+    if k == k_ref:
+        return
+    assert abs(k - k_ref) <= nb, (name, k, k_ref)
+    tie, floor = tie_tolerances(B, dt)
+    ptol = max(atol, rtol * float(np.linalg.norm(_wide(B), axis=0).max()))
+    big = np.asarray(p if k > k_ref else p_ref)
+    lo, hi = max(0, min(k, k_ref) - nb), min(len(big), max(k, k_ref) + 1)
+    r = [residual_norms(B, big[:i], [big[i]])[0] for i in range(lo, hi)]
+    assert any(abs(ri - ptol) <= tie * ptol + floor for ri in r), (name, k, k_ref, ptol, min(r), max(r))
+
+
+def reconstruction_gap(A, sk, rd, T, rd_ref, T_ref):
+    """||A[:, sk] (T - T_ref)||_F / ||A||_F with the columns of the two
+    interpolation matrices aligned by their redundant column (the order of
+    rd comes from pivots below the rank tolerance): how far apart the two
+    put the reconstructed columns (same skeleton)."""
+    C = np.asarray(A)[:, np.asarray(sk) - 1].astype(np.complex128 if np.iscomplexobj(A) else np.float64)
+    o, o_ref = np.argsort(np.asarray(rd)), np.argsort(np.asarray(rd_ref))
+    D = np.asarray(T)[:, o].astype(C.dtype) - np.asarray(T_ref)[:, o_ref].astype(C.dtype)
+    return np.linalg.norm(C @ D) / np.linalg.norm(A)
 
 
 def qr_cases(golden):
@@ -246,3 +290,33 @@ def test_maxdet_bounds_T(oracle):
     opts = oracle.Opts(rtol=1e-10, maxdet_tol=0.0)
     V = oracle.idfact("n", A, opts, rs_for(oracle, "randn", 128, 9))
     assert np.abs(V["T"]).max() <= 1 + 1e-12
+
+
+def test_srft_sampled_dft_matches_fft(oracle):
+    """The sampled-DFT form the large-sketch checks use gives the full
+    FFT's values (odd and even orders, a non-power-of-two length)."""
+    rng = np.random.default_rng(4)
+    for M in (96, 1000):
+        X = rng.standard_normal((M, 7))
+        d = np.where(rng.standard_normal(M) > 0, 1.0, -1.0)
+        for k in (7, 40):
+            idx = rng.integers(1, M + 1, k)
+            a = oracle.srft_sampled_dft(X, d, idx, k, chunk=64)
+            b = oracle.srft_exact(X, d, idx, k)
+            assert np.allclose(a, b, rtol=1e-10, atol=1e-10 * np.abs(b).max())
+
+
+def test_check_rank_accepts_only_threshold_ties():
+    """check_rank: a rank off by one passes only when a pivot residual sits
+    on the stop threshold; a genuine gap fails."""
+    rng = np.random.default_rng(9)
+    Q, _ = np.linalg.qr(rng.standard_normal((60, 40)))
+    s = 10.0 ** (-np.arange(40) / 4.0)
+    B = (Q * s) @ np.linalg.qr(rng.standard_normal((40, 40)))[0]
+    p = np.arange(1, 41)
+    # the exact residual of pivot 10 after pivots 1..10 (0-based position 10)
+    r10 = residual_norms(B, p[:10], [p[10]])[0]
+    rtol = r10 / np.linalg.norm(B, axis=0).max()
+    check_rank(B, 10, 11, p, p, rtol, np.float64)            # on the threshold: a tie
+    with pytest.raises(AssertionError):
+        check_rank(B, 10, 11, p, p, 1e3 * rtol, np.float64)  # far from it
