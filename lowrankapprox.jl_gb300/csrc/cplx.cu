@@ -570,8 +570,16 @@ __global__ void cphase_kernel(int64_t n, const double* __restrict__ g, C<R>* d) 
 // the SRFT of complex types samples the DFT of d .* x at the frequencies
 // idx (srft_apply!, src/sketch.jl:452-472); the phase is reduced exactly
 // as (f t) mod M
+// the operand accessor of the gather-type sketches: element (t, col) is
+// A(col, t) when mode & 1 (transposed) else A(t, col), conjugated when mode & 2
 template <typename R>
-__global__ void csrft_direct_kernel(int trans, int64_t M, int64_t N, const C<R>* __restrict__ A, int64_t lda,
+__device__ __forceinline__ C<R> opel(int mode, const C<R>* A, int64_t lda, int64_t t, int64_t col) {
+  const C<R> a = (mode & 1) ? A[col + t * lda] : A[t + col * lda];
+  return (mode & 2) ? conj(a) : a;
+}
+
+template <typename R>
+__global__ void csrft_direct_kernel(int mode, int64_t M, int64_t N, const C<R>* __restrict__ A, int64_t lda,
                                     const C<R>* __restrict__ d, const int64_t* __restrict__ idx, int64_t order,
                                     C<R>* B, int64_t ldb) {
   for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < order * N;
@@ -580,7 +588,7 @@ __global__ void csrft_direct_kernel(int trans, int64_t M, int64_t N, const C<R>*
     const int64_t f = idx[i] - 1;
     C<R> acc(0);
     for (int64_t s = 0; s < M; ++s) {
-      const C<R> a = trans ? conj(A[col + s * lda]) : A[s + col * lda];
+      const C<R> a = opel(mode, A, lda, s, col);
       const int64_t r = (f * s) % M;  // f, s < M < 2^31
       R sn, cs;
       if constexpr (sizeof(R) == 8)
@@ -596,7 +604,7 @@ __global__ void csrft_direct_kernel(int trans, int64_t M, int64_t N, const C<R>*
 // B(i, :) = sum over the rows r of group i of g_r op(A)(perm_r, :)
 // (SparseRandomGaussian, src/sketch.jl:571-653), groups of fld(M - i, l) + 1
 template <typename R>
-__global__ void csprn_kernel(int trans, int64_t M, int64_t N, const C<R>* __restrict__ A, int64_t lda,
+__global__ void csprn_kernel(int mode, int64_t M, int64_t N, const C<R>* __restrict__ A, int64_t lda,
                              const int64_t* __restrict__ perm, const C<R>* __restrict__ g,
                              const int64_t* __restrict__ start, int64_t order, C<R>* B, int64_t ldb) {
   for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < order * N;
@@ -604,8 +612,7 @@ __global__ void csprn_kernel(int trans, int64_t M, int64_t N, const C<R>* __rest
     const int64_t i = t % order, col = t / order;
     C<R> acc(0);
     for (int64_t l = start[i]; l < start[i + 1]; ++l) {
-      const int64_t r = perm[l] - 1;
-      const C<R> a = trans ? conj(A[col + r * lda]) : A[r + col * lda];
+      const C<R> a = opel(mode, A, lda, perm[l] - 1, col);
       acc += g[l] * a;
     }
     B[i + col * ldb] = acc;
@@ -614,13 +621,12 @@ __global__ void csprn_kernel(int trans, int64_t M, int64_t N, const C<R>* __rest
 
 // B(i, :) = op(A)(rows_i, :) (RandomSubset, src/sketch.jl:248-293)
 template <typename R>
-__global__ void csub_kernel(int trans, int64_t N, const C<R>* __restrict__ A, int64_t lda,
+__global__ void csub_kernel(int mode, int64_t N, const C<R>* __restrict__ A, int64_t lda,
                             const int64_t* __restrict__ rows, int64_t order, C<R>* B, int64_t ldb) {
   for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < order * N;
        t += (int64_t)gridDim.x * blockDim.x) {
     const int64_t i = t % order, col = t / order;
-    const int64_t r = rows[i] - 1;
-    B[i + col * ldb] = trans ? conj(A[col + r * lda]) : A[r + col * lda];
+    B[i + col * ldb] = opel(mode, A, lda, rows[i] - 1, col);
   }
 }
 
@@ -735,6 +741,10 @@ __global__ void ccluster_orth_kernel(int64_t n, C<R>* Z, int64_t ldz, const int6
 }  // namespace
 
 // ---- launchers ----------------------------------------------------------------------
+
+// the accessor mode of a sketch operand: 'n' A(t, col); 'c' conj(A(col, t));
+// 't' A(col, t); 'j' conj(A(t, col))
+inline int cmode(char m) { return m == 'n' ? 0 : m == 'c' ? 3 : m == 't' ? 1 : 2; }
 
 template <typename R>
 void cgemm(lra_ctx* ctx, char ta, char tb, int64_t m, int64_t n, int64_t k, cx<R> alpha, const cx<R>* A,
@@ -906,7 +916,7 @@ template <typename R>
 void csrft_direct(lra_ctx* ctx, char trans, int64_t M, int64_t N, const cx<R>* A, int64_t lda, const cx<R>* d,
                   const int64_t* idx, int64_t order, cx<R>* B, int64_t ldb) {
   if (order <= 0 || N <= 0) return;
-  csrft_direct_kernel<R><<<grid_for_c(ctx, order * N, 128), 128, 0, ctx->stream>>>(trans == 'n' ? 0 : 1, M, N, A,
+  csrft_direct_kernel<R><<<grid_for_c(ctx, order * N, 128), 128, 0, ctx->stream>>>(cmode(trans), M, N, A,
                                                                                  lda, d, idx, order, B, ldb);
   post_launch(ctx, "csrft_direct_kernel");
 }
@@ -915,7 +925,7 @@ template <typename R>
 void csprn(lra_ctx* ctx, char trans, int64_t M, int64_t N, const cx<R>* A, int64_t lda, const int64_t* perm,
            const cx<R>* g, const int64_t* start, int64_t order, cx<R>* B, int64_t ldb) {
   if (order <= 0 || N <= 0) return;
-  csprn_kernel<R><<<grid_for_c(ctx, order * N, 128), 128, 0, ctx->stream>>>(trans == 'n' ? 0 : 1, M, N, A, lda, perm,
+  csprn_kernel<R><<<grid_for_c(ctx, order * N, 128), 128, 0, ctx->stream>>>(cmode(trans), M, N, A, lda, perm,
                                                                           g, start, order, B, ldb);
   post_launch(ctx, "csprn_kernel");
 }
@@ -924,7 +934,7 @@ template <typename R>
 void csub(lra_ctx* ctx, char trans, int64_t N, const cx<R>* A, int64_t lda, const int64_t* rows, int64_t order,
           cx<R>* B, int64_t ldb) {
   if (order <= 0 || N <= 0) return;
-  csub_kernel<R><<<grid_for_c(ctx, order * N, 256), 256, 0, ctx->stream>>>(trans == 'n' ? 0 : 1, N, A, lda, rows,
+  csub_kernel<R><<<grid_for_c(ctx, order * N, 256), 256, 0, ctx->stream>>>(cmode(trans), N, A, lda, rows,
                                                                           order, B, ldb);
   post_launch(ctx, "csub_kernel");
 }

@@ -1312,7 +1312,7 @@ __global__ void __launch_bounds__(NT) geqp3_df_kernel(QrParams<double> P, QrV2Ex
 // index, as with xLAQPS's idamax.
 struct QrSm {
   unsigned long long* xw;    // [2][G] exchange words, zeroed before the launch
-  float2* stage;             // [2][G][m] staged candidate columns
+  void* stage;               // [2][G][m] staged candidate columns (elements of the arithmetic)
   unsigned long long* pubt;  // LRA_TRACE: %globaltimer of each CTA's word per pivot, [kmax][G], or null
 };
 
@@ -1336,12 +1336,85 @@ __device__ __forceinline__ int live_quad(const unsigned char* st, int nloc, int 
 constexpr unsigned long long XW_IDX = 0xFFFFFFull;  // 24-bit column field, stored as XW_IDX - j
 constexpr unsigned long long XW_LOW = (1ull << 62) - 1;
 
-__device__ __forceinline__ unsigned long long xw_pack(Df v, int64_t j) {
+// The arithmetic of the shared-memory pivoted QR.  Float64 sketches are
+// held as double-float pairs (the mixed path's sketch has 2^-48
+// resolution); Float32 sketches as plain FP32, the precision of xLAQPS for
+// Float32.  Both give the step the same operations in the same order.
+struct QrArithDf {
+  using T = double;
+  using E = float2;  // a stored element
+  using V = Df;      // a working value
+  __device__ static V zero() { return Df{0.f, 0.f}; }
+  __device__ static V one() { return Df{1.f, 0.f}; }
+  __device__ static E ezero() { return make_float2(0.f, 0.f); }
+  __device__ static V ld(E e) { return Df{e.x, e.y}; }
+  __device__ static E st(V v) { return make_float2(v.h, v.l); }
+  __device__ static float hi(V v) { return v.h; }
+  __device__ static float ehi(E e) { return e.x; }
+  __device__ static void fma_acc(V& a, E v, E x) { df_fma_acc(a, v.x, v.y, x.x, x.y); }
+  __device__ static V norm(V a) { return quick_two_sum(a.h, a.l); }
+  __device__ static V add(V a, V b) { return df_add(a, b); }
+  __device__ static V mul(V a, V b) { return df_mul(a, b); }
+  __device__ static V div(V a, V b) { return df_div(a, b); }
+  __device__ static V sqrt_(V a) { return df_sqrt(a); }
+  __device__ static V neg(V a) { return df_neg(a); }
+  __device__ static V shfl_xor(V a, int o) { return df_shfl_xor(a, o); }
+  __device__ static E axpy_neg(E x, V f, E v) {
+    const Df y = df_axpy_neg(x.x, x.y, f, v.x, v.y);
+    return make_float2(y.h, y.l);
+  }
+  __device__ static double val(V v) { return df_val(v.h, v.l); }
+  __device__ static V split(double x) { return df_split(x); }
+  __device__ static E escale(E e, float sc) { return make_float2(e.x * sc, e.y * sc); }
+  __device__ static V from_float(float f) { return Df{f, 0.f}; }
+  __device__ static V ldexp_(V v, int ex) { return Df{ldexpf(v.h, ex), ldexpf(v.l, ex)}; }
+  __device__ static E from_planes(const float* h, const float* l, int64_t i) { return make_float2(h[i], l[i]); }
+  __device__ static void to_planes(E y, float* h, float* l, int64_t i) {
+    h[i] = y.x;
+    l[i] = y.y;
+  }
   // 38 bits of the key (df_key < 2^63 for h > 0); zero, negative zero and
   // NaN norms rank lowest
-  const unsigned long long k = v.h > 0.f ? (unsigned long long)df_key(v) >> 25 : 0ull;
-  return (k << 24) | (XW_IDX - (unsigned long long)j);
+  __device__ static unsigned long long key38(V v) { return v.h > 0.f ? (unsigned long long)df_key(v) >> 25 : 0ull; }
+};
+
+struct QrArithF32 {
+  using T = float;
+  using E = float;
+  using V = float;
+  __device__ static V zero() { return 0.f; }
+  __device__ static V one() { return 1.f; }
+  __device__ static E ezero() { return 0.f; }
+  __device__ static V ld(E e) { return e; }
+  __device__ static E st(V v) { return v; }
+  __device__ static float hi(V v) { return v; }
+  __device__ static float ehi(E e) { return e; }
+  __device__ static void fma_acc(V& a, E v, E x) { a = fmaf(v, x, a); }
+  __device__ static V norm(V a) { return a; }
+  __device__ static V add(V a, V b) { return a + b; }
+  __device__ static V mul(V a, V b) { return a * b; }
+  __device__ static V div(V a, V b) { return a / b; }
+  __device__ static V sqrt_(V a) { return a > 0.f ? sqrtf(a) : 0.f; }
+  __device__ static V neg(V a) { return -a; }
+  __device__ static V shfl_xor(V a, int o) { return __shfl_xor_sync(0xffffffffu, a, o); }
+  __device__ static E axpy_neg(E x, V f, E v) { return fmaf(-f, v, x); }
+  __device__ static double val(V v) { return (double)v; }
+  __device__ static V split(double x) { return (float)x; }
+  __device__ static E escale(E e, float sc) { return e * sc; }
+  __device__ static V from_float(float f) { return f; }
+  __device__ static V ldexp_(V v, int ex) { return ldexpf(v, ex); }
+  __device__ static E from_planes(const float* h, const float*, int64_t i) { return h[i]; }
+  __device__ static void to_planes(E y, float* h, float*, int64_t i) { h[i] = y; }
+  // the 31 bits of a positive float, at the place of the double-float
+  // key's 38 bits
+  __device__ static unsigned long long key38(V v) { return v > 0.f ? (unsigned long long)__float_as_uint(v) << 6 : 0ull; }
+};
+
+template <class A>
+__device__ __forceinline__ unsigned long long xw_pack(typename A::V v, int64_t j) {
+  return (A::key38(v) << 24) | (XW_IDX - (unsigned long long)j);
 }
+
 
 // Warp 0 computes the reflector's scalars while warps 1..NW-1 take the dot
 // products of their columns with the (unscaled) reflector tail x; with
@@ -1361,16 +1434,18 @@ __device__ __forceinline__ unsigned long long xw_pack(Df v, int64_t j) {
 // operations in both forms (the dot products' lane order and reduction tree,
 // the reflector's partial sums over the same thread-to-row map, the same
 // updates), so a matrix factored alone and in a batch gives the same bits.
-template <int NT, bool GCOL>
-__device__ __forceinline__ void geqp3_df_body(const QrParams<double>& P, const QrV2Extra& X, const QrDf& D,
-                                              const QrSm& S, const int G, const int b, float2* Cg,
+template <class A, int NT, bool GCOL>
+__device__ __forceinline__ void geqp3_df_body(const QrParams<typename A::T>& P, const QrV2Extra& X, const QrDf& D,
+                                              const QrSm& S, const int G, const int b, typename A::E* Cg,
                                               const int64_t gcs, const int64_t grs, unsigned char* qr_dyn) {
+  using E = typename A::E;
+  using V = typename A::V;
   constexpr int NW = NT / 32;
   constexpr int NCW = NW - 1;  // column warps
-  __shared__ Df s_part[NW];
+  __shared__ V s_part[NW];
   __shared__ unsigned long long s_w[NW];
   __shared__ int s_fl[NW];
-  __shared__ Df s_alpha, s_f, s_tau, s_beta;
+  __shared__ V s_alpha, s_f, s_tau, s_beta;
   __shared__ double s_red[32];
   __shared__ unsigned long long s_win;
   __shared__ int s_owner, s_stop, s_ok;
@@ -1380,23 +1455,23 @@ __device__ __forceinline__ void geqp3_df_body(const QrParams<double>& P, const Q
   const int64_t c0 = n * b / G, c1 = n * (b + 1) / G;
   const int nloc = (int)(c1 - c0);
   const int64_t ncap = (n + G - 1) / G;
-  float2* V = reinterpret_cast<float2*>(qr_dyn);  // rows c..m-1 of the pivot column
+  E* Vc = reinterpret_cast<E*>(qr_dyn);  // rows c..m-1 of the pivot column
   // the CTA's columns, slot s = column c0 + s: shared memory, or (GCOL) a
   // global m x n workspace
-  float2* C = GCOL ? Cg : V + m;
+  E* C = GCOL ? Cg : Vc + m;
   // element (row i, slot s) at C[s cs + i rs]: column-major in shared
   // memory; the workspace of GCOL may be row-major (coalesced thread-per-
   // column access)
   const int64_t cs = GCOL ? gcs : m, rs = GCOL ? grs : 1;
-  Df* s_vn1 = reinterpret_cast<Df*>(GCOL ? V + m : C + ncap * m);
-  Df* s_vn2 = s_vn1 + ncap;
-  Df* s_dot = s_vn2 + ncap;
-  Df* s_fs = s_dot + ncap;  // f scal of each column for the deferred update
-  float2* s_x0 = reinterpret_cast<float2*>(s_fs + ncap);  // row c of each column
+  V* s_vn1 = reinterpret_cast<V*>(GCOL ? Vc + m : C + ncap * m);
+  V* s_vn2 = s_vn1 + ncap;
+  V* s_dot = s_vn2 + ncap;
+  V* s_fs = s_dot + ncap;  // f scal of each column for the deferred update
+  E* s_x0 = reinterpret_cast<E*>(s_fs + ncap);  // row c of each column
   unsigned char* s_st = reinterpret_cast<unsigned char*>(s_x0 + ncap);
   float* __restrict__ Bh = D.Bh;
   float* __restrict__ Bl = D.Bl;
-  const float tol3z = (float)sqrt(Real<double>::eps);
+  const float tol3z = (float)sqrt((double)Real<typename A::T>::eps);
   const int64_t lastrk = m < n ? m : n;
   // LRA_TRACE: a block barrier before each stamp, so that it marks the end
   // of the phase for the whole CTA
@@ -1444,15 +1519,14 @@ __device__ __forceinline__ void geqp3_df_body(const QrParams<double>& P, const Q
     const unsigned long long w = s_win;
     if (w & XW_LOW) {
       const int sc = (int)((int64_t)(XW_IDX - (w & XW_IDX)) - c0);
-      float2* col = C + (int64_t)sc * cs;
-      float2* dst = GCOL ? nullptr : S.stage + ((size_t)(e & 1) * G + b) * m;
-      const Df fs = upd ? s_fs[sc] : Df{0.f, 0.f};
-      if (upd && !(s_st[sc] & ST_UPD) && fs.h != 0.f) {
+      E* col = C + (int64_t)sc * cs;
+      E* dst = GCOL ? nullptr : static_cast<E*>(S.stage) + ((size_t)(e & 1) * G + b) * m;
+      const V fs = upd ? s_fs[sc] : A::zero();
+      if (upd && !(s_st[sc] & ST_UPD) && A::hi(fs) != 0.f) {
         for (int64_t i = r0 + threadIdx.x; i < m; i += NT) {
-          const float2 x = col[i * rs], v = V[i];
-          const Df y = df_axpy_neg(x.x, x.y, fs, v.x, v.y);
-          col[i * rs] = make_float2(y.h, y.l);
-          if (!GCOL) dst[i] = make_float2(y.h, y.l);
+          const E y = A::axpy_neg(col[i * rs], fs, Vc[i]);
+          col[i * rs] = y;
+          if (!GCOL) dst[i] = y;
         }
         __syncthreads();
         if (threadIdx.x == 0) s_st[sc] |= ST_UPD;
@@ -1563,18 +1637,18 @@ __device__ __forceinline__ void geqp3_df_body(const QrParams<double>& P, const Q
   if (!GCOL)
     for (int s = wid; s < nloc; s += NW) {
       const float* ph = Bh + (c0 + s) * lda;
-      const float* pl = Bl + (c0 + s) * lda;
-      for (int64_t i = lane; i < m; i += 32) C[s * m + i] = make_float2(ph[i], pl[i]);
+      const float* pl = Bl ? Bl + (c0 + s) * lda : nullptr;
+      for (int64_t i = lane; i < m; i += 32) C[s * m + i] = A::from_planes(ph, pl, i);
     }
   double lmax = 0;
   unsigned long long cw = 0;
   for (int s = threadIdx.x; s < nloc; s += NT) {
     s_st[s] = ST_LIVE;
     const double v = D.vn0[c0 + s];
-    const Df nr = df_split(v);
+    const V nr = A::split(v);
     s_vn1[s] = s_vn2[s] = nr;
     lmax = fmax(lmax, v);
-    const unsigned long long w = xw_pack(nr, c0 + s);
+    const unsigned long long w = xw_pack<A>(nr, c0 + s);
     cw = w > cw ? w : cw;
   }
   lmax = block_max(lmax, s_red);
@@ -1613,17 +1687,17 @@ __device__ __forceinline__ void geqp3_df_body(const QrParams<double>& P, const Q
       // ---- the pivot column's rows c..m-1 from the winner's stage, and the
       // per-warp partial sums of squares of rows c+1..m-1
       {
-        const float2* src = GCOL ? C + (pvt - c0) * cs : S.stage + ((size_t)(e & 1) * G + owner) * m;
-        Df acc{0.f, 0.f};
+        const E* src = GCOL ? C + (pvt - c0) * cs : static_cast<const E*>(S.stage) + ((size_t)(e & 1) * G + owner) * m;
+        V acc = A::zero();
         for (int64_t i = c + threadIdx.x; i < m; i += NT) {
-          const float2 x = GCOL ? src[i * rs] : __ldcg(src + i);
-          V[i] = x;
-          if (i > c) df_fma_acc(acc, x.x, x.y, x.x, x.y);
-          else s_alpha = Df{x.x, x.y};
+          const E x = GCOL ? src[i * rs] : __ldcg(src + i);
+          Vc[i] = x;
+          if (i > c) A::fma_acc(acc, x, x);
+          else s_alpha = A::ld(x);
         }
-        acc = quick_two_sum(acc.h, acc.l);
+        acc = A::norm(acc);
 #pragma unroll
-        for (int o = 16; o > 0; o >>= 1) acc = df_add(acc, df_shfl_xor(acc, o));
+        for (int o = 16; o > 0; o >>= 1) acc = A::add(acc, A::shfl_xor(acc, o));
         if (lane == 0) s_part[wid] = acc;
       }
       __syncthreads();
@@ -1633,25 +1707,25 @@ __device__ __forceinline__ void geqp3_df_body(const QrParams<double>& P, const Q
         // xLARFG in double-float (the matrix is scaled to max |B| < 1, so
         // neither the sum of squares nor beta can overflow, and no entry of
         // a float pair is small enough for xLARFG's rescaling loop)
-        Df acc = lane < NW ? s_part[lane] : Df{0.f, 0.f};
+        V acc = lane < NW ? s_part[lane] : A::zero();
 #pragma unroll
-        for (int o = 16; o > 0; o >>= 1) acc = df_add(acc, df_shfl_xor(acc, o));
-        const Df alpha = s_alpha;
-        Df tau{0.f, 0.f}, beta = alpha, scal{1.f, 0.f};
-        if (len > 0 && acc.h > 0.f) {
-          const Df r = df_sqrt(df_add(df_mul(alpha, alpha), acc));
-          beta = alpha.h >= 0.f ? df_neg(r) : r;
-          tau = df_div(df_add(beta, df_neg(alpha)), beta);
-          scal = df_div(Df{1.f, 0.f}, df_add(alpha, df_neg(beta)));
+        for (int o = 16; o > 0; o >>= 1) acc = A::add(acc, A::shfl_xor(acc, o));
+        const V alpha = s_alpha;
+        V tau = A::zero(), beta = alpha, scal = A::one();
+        if (len > 0 && A::hi(acc) > 0.f) {
+          const V r = A::sqrt_(A::add(A::mul(alpha, alpha), acc));
+          beta = A::hi(alpha) >= 0.f ? A::neg(r) : r;
+          tau = A::div(A::add(beta, A::neg(alpha)), beta);
+          scal = A::div(A::one(), A::add(alpha, A::neg(beta)));
         }
         if (lane == 0) {
-          s_taud = df_val(tau.h, tau.l);
-          s_betad = df_val(beta.h, beta.l);
+          s_taud = A::val(tau);
+          s_betad = A::val(beta);
           s_f = scal;
           s_tau = tau;
           s_beta = beta;
           if (b == 0) {
-            P.tau[c] = s_taud;
+            P.tau[c] = (typename A::T)s_taud;
             X.piv[c] = pvt;
             X.beta[c] = s_betad;
           }
@@ -1663,30 +1737,27 @@ __device__ __forceinline__ void geqp3_df_body(const QrParams<double>& P, const Q
         // forms of the kernel sum each column the same way.
         for (int s = threadIdx.x - 32; s < nloc; s += NT - 32) {
           if (s_st[s] & ST_DONE) continue;
-          const float2* col = C + (int64_t)s * cs;
+          const E* col = C + (int64_t)s * cs;
           s_x0[s] = col[c * rs];
-          Df d{0.f, 0.f};
+          V d = A::zero();
           // QSEQB rows loaded ahead, then added in row order
           for (int64_t i0 = c + 1; i0 < m; i0 += QSEQB) {
-            float2 xb[QSEQB];
+            E xb[QSEQB];
 #pragma unroll
             for (int r = 0; r < QSEQB; ++r)
               if (i0 + r < m) xb[r] = col[(i0 + r) * rs];
 #pragma unroll
             for (int r = 0; r < QSEQB; ++r)
-              if (i0 + r < m) {
-                const float2 v = V[i0 + r];
-                df_fma_acc(d, v.x, v.y, xb[r].x, xb[r].y);
-              }
+              if (i0 + r < m) A::fma_acc(d, Vc[i0 + r], xb[r]);
           }
-          s_dot[s] = quick_two_sum(d.h, d.l);
+          s_dot[s] = A::norm(d);
         }
       } else if (len > 0) {
         // ---- dot products x . a of the warp's live columns, four at a time
         int s = wid - 1;
         int q[4];
         while (quad(s, q)) {
-          const float2* cg[4];
+          const E* cg[4];
 #pragma unroll
           for (int g = 0; g < 4; ++g) cg[g] = C + (int64_t)(q[g] >= 0 ? q[g] : q[0]) * cs;
           // row c of the column, for the update that follows the dots
@@ -1699,36 +1770,36 @@ __device__ __forceinline__ void geqp3_df_body(const QrParams<double>& P, const Q
           // quad has 4 QRPL loads in flight (the global-memory form waits
           // an L2 round trip per chunk); each lane still adds its rows in
           // increasing order
-          Df d[4] = {{0.f, 0.f}, {0.f, 0.f}, {0.f, 0.f}, {0.f, 0.f}};
+          V d[4] = {A::zero(), A::zero(), A::zero(), A::zero()};
           for (int64_t b0 = c + 1; b0 < m; b0 += 32 * QRPL) {
-            float2 xv[QRPL], xc[4][QRPL];
+            E xv[QRPL], xc[4][QRPL];
 #pragma unroll
             for (int r = 0; r < QRPL; ++r) {
               const int64_t i = b0 + lane + 32 * r;
               const bool in = i < m;
-              xv[r] = in ? V[i] : make_float2(0.f, 0.f);
+              xv[r] = in ? Vc[i] : A::ezero();
 #pragma unroll
-              for (int g = 0; g < 4; ++g) xc[g][r] = in ? cg[g][i * rs] : make_float2(0.f, 0.f);
+              for (int g = 0; g < 4; ++g) xc[g][r] = in ? cg[g][i * rs] : A::ezero();
             }
 #pragma unroll
             for (int r = 0; r < QRPL; ++r)
               if (b0 + lane + 32 * r < m) {
 #pragma unroll
-                for (int g = 0; g < 4; ++g) df_fma_acc(d[g], xv[r].x, xv[r].y, xc[g][r].x, xc[g][r].y);
+                for (int g = 0; g < 4; ++g) A::fma_acc(d[g], xv[r], xc[g][r]);
               }
           }
 #pragma unroll
-          for (int g = 0; g < 4; ++g) d[g] = quick_two_sum(d[g].h, d[g].l);
+          for (int g = 0; g < 4; ++g) d[g] = A::norm(d[g]);
           // transposed butterfly: after the 16- and 8-lane levels, lanes
           // 8g..8g+7 hold column g's partial sums
           const bool up = lane & 16;
-          const Df k0 = up ? d[2] : d[0], k1 = up ? d[3] : d[1];
-          const Df e0 = df_add(k0, df_shfl_xor(up ? d[0] : d[2], 16));
-          const Df e1 = df_add(k1, df_shfl_xor(up ? d[1] : d[3], 16));
+          const V k0 = up ? d[2] : d[0], k1 = up ? d[3] : d[1];
+          const V e0 = A::add(k0, A::shfl_xor(up ? d[0] : d[2], 16));
+          const V e1 = A::add(k1, A::shfl_xor(up ? d[1] : d[3], 16));
           const bool hi = lane & 8;
-          Df t = df_add(hi ? e1 : e0, df_shfl_xor(hi ? e0 : e1, 8));
+          V t = A::add(hi ? e1 : e0, A::shfl_xor(hi ? e0 : e1, 8));
 #pragma unroll
-          for (int o = 4; o > 0; o >>= 1) t = df_add(t, df_shfl_xor(t, o));
+          for (int o = 4; o > 0; o >>= 1) t = A::add(t, A::shfl_xor(t, o));
           const int g = lane >> 3;
           const int qg = g == 0 ? q[0] : g == 1 ? q[1] : g == 2 ? q[2] : q[3];
           if ((lane & 7) == 0 && qg >= 0) s_dot[qg] = t;
@@ -1737,7 +1808,7 @@ __device__ __forceinline__ void geqp3_df_body(const QrParams<double>& P, const Q
       __syncthreads();
       stamp(c, 2);
       const double tau = s_taud;
-      const Df scal = s_f;
+      const V scal = s_f;
       stamp(c, 3);
       // ---- a thread per column: f, the new row c, the norm downdate and the
       // candidate word
@@ -1748,32 +1819,32 @@ __device__ __forceinline__ void geqp3_df_body(const QrParams<double>& P, const Q
       };
       sub(8);
       {
-        const Df tdf = s_tau;
+        const V tdf = s_tau;
         for (int s = threadIdx.x; s < nloc; s += NT) {
           const unsigned char st = s_st[s];
           if (st & ST_DONE) continue;
-          const float2 x0 = len > 0 ? s_x0[s] : C[(int64_t)s * cs + c * rs];
-          Df f{0.f, 0.f}, fs{0.f, 0.f};
+          const E x0 = len > 0 ? s_x0[s] : C[(int64_t)s * cs + c * rs];
+          V f = A::zero(), fs = A::zero();
           if (tau != 0 && len > 0) {
-            f = df_mul(tdf, df_add(Df{x0.x, x0.y}, df_mul(scal, s_dot[s])));
-            fs = df_mul(f, scal);
+            f = A::mul(tdf, A::add(A::ld(x0), A::mul(scal, s_dot[s])));
+            fs = A::mul(f, scal);
           }
           s_fs[s] = fs;
-          const Df a = df_add(Df{x0.x, x0.y}, df_neg(f));
-          C[(int64_t)s * cs + c * rs] = make_float2(a.h, a.l);
-          Df v1 = s_vn1[s];
+          const V a = A::add(A::ld(x0), A::neg(f));
+          C[(int64_t)s * cs + c * rs] = A::st(a);
+          V v1 = s_vn1[s];
           bool flagged = false;
-          if (c < lastrk - 1 && v1.h != 0.f) {
-            // LAPACK's partial-norm downdate, in double-float
-            Df temp = df_div(a.h < 0.f ? df_neg(a) : a, v1);
-            temp = df_mul(df_add(Df{1.f, 0.f}, temp), df_add(Df{1.f, 0.f}, df_neg(temp)));
-            if (temp.h < 0.f) temp = Df{0.f, 0.f};
-            const Df r = df_div(v1, s_vn2[s]);
-            const Df temp2 = df_mul(temp, df_mul(r, r));
-            if (temp2.h <= tol3z) {
+          if (c < lastrk - 1 && A::hi(v1) != 0.f) {
+            // LAPACK's partial-norm downdate
+            V temp = A::div(A::hi(a) < 0.f ? A::neg(a) : a, v1);
+            temp = A::mul(A::add(A::one(), temp), A::add(A::one(), A::neg(temp)));
+            if (A::hi(temp) < 0.f) temp = A::zero();
+            const V r = A::div(v1, s_vn2[s]);
+            const V temp2 = A::mul(temp, A::mul(r, r));
+            if (A::hi(temp2) <= tol3z) {
               flagged = true;
             } else {
-              v1 = df_mul(v1, df_sqrt(temp));
+              v1 = A::mul(v1, A::sqrt_(temp));
               s_vn1[s] = v1;
             }
           }
@@ -1783,33 +1854,29 @@ __device__ __forceinline__ void geqp3_df_body(const QrParams<double>& P, const Q
             // recompute the norm before the next pivot, from the same
             // updated column); this thread alone, row by row, in double-float
             // at a power-of-two scale that puts the largest entry in [1, 2)
-            float2* col = C + (int64_t)s * cs;
-            if (fs.h != 0.f)
-              for (int64_t i = c + 1; i < m; ++i) {
-                const float2 x = col[i * rs], v = V[i];
-                const Df y = df_axpy_neg(x.x, x.y, fs, v.x, v.y);
-                col[i * rs] = make_float2(y.h, y.l);
-              }
+            E* col = C + (int64_t)s * cs;
+            if (A::hi(fs) != 0.f)
+              for (int64_t i = c + 1; i < m; ++i) col[i * rs] = A::axpy_neg(col[i * rs], fs, Vc[i]);
             float mx = 0.f;
-            for (int64_t i = c + 1; i < m; ++i) mx = fmaxf(mx, fabsf(col[i * rs].x));
-            Df nr{mx, 0.f};
+            for (int64_t i = c + 1; i < m; ++i) mx = fmaxf(mx, fabsf(A::ehi(col[i * rs])));
+            V nr = A::from_float(mx);
             if (mx > 0.f && isfinite(mx)) {
               const int ex = ilogbf(mx);
               const float sc = ldexpf(1.f, -ex);
-              Df acc{0.f, 0.f};
+              V acc = A::zero();
               for (int64_t i = c + 1; i < m; ++i) {
-                const float2 x = col[i * rs];
-                df_fma_acc(acc, x.x * sc, x.y * sc, x.x * sc, x.y * sc);
+                const E x = A::escale(col[i * rs], sc);
+                A::fma_acc(acc, x, x);
               }
-              const Df r = df_sqrt(quick_two_sum(acc.h, acc.l));
-              nr = Df{ldexpf(r.h, ex), ldexpf(r.l, ex)};
+              const V r = A::sqrt_(A::norm(acc));
+              nr = A::ldexp_(r, ex);
             }
             v1 = nr;
             s_vn1[s] = s_vn2[s] = v1;
             s_st[s] = st | ST_UPD;
             wfl = 1;
           }
-          const unsigned long long w = xw_pack(v1, c0 + s);
+          const unsigned long long w = xw_pack<A>(v1, c0 + s);
           ww = w > ww ? w : ww;
         }
       }
@@ -1835,26 +1902,22 @@ __device__ __forceinline__ void geqp3_df_body(const QrParams<double>& P, const Q
         // the finished pivot column (its owner): R's rows above c, beta, the
         // reflector v = scal x below
         if (owner == b) {
-          float2* col = C + (pvt - c0) * cs;
-          const Df bt = s_beta;
+          E* col = C + (pvt - c0) * cs;
+          const V bt = s_beta;
           for (int64_t i = (GCOL ? c : 0) + ct; i < m; i += NCT) {
-            float2 y;
+            E y;
             if (i < c) {
               y = col[i * rs];
             } else if (i == c) {
-              y = make_float2(bt.h, bt.l);
+              y = A::st(bt);
             } else {
-              y = V[i];
-              if (tau != 0) {
-                const Df z = df_mul(Df{y.x, y.y}, scal);
-                y = make_float2(z.h, z.l);
-              }
+              y = Vc[i];
+              if (tau != 0) y = A::st(A::mul(A::ld(y), scal));
             }
             if (GCOL) {
               col[i * rs] = y;
             } else {
-              Bh[pvt * lda + i] = y.x;
-              Bl[pvt * lda + i] = y.y;
+              A::to_planes(y, Bh + pvt * lda, Bl ? Bl + pvt * lda : nullptr, i);
             }
           }
         }
@@ -1866,26 +1929,26 @@ __device__ __forceinline__ void geqp3_df_body(const QrParams<double>& P, const Q
           int s = wid - 1;
           int q[4];
           while (quad(s, q)) {
-            Df fq[4];
-            float2* cg[4];
+            V fq[4];
+            E* cg[4];
             bool u[4];
 #pragma unroll
             for (int h = 0; h < 4; ++h) {
               const int qh = q[h] >= 0 ? q[h] : q[0];
               cg[h] = C + (int64_t)qh * cs;
               fq[h] = s_fs[qh];
-              u[h] = q[h] >= 0 && fq[h].h != 0.f && !(s_st[qh] & ST_UPD);
+              u[h] = q[h] >= 0 && A::hi(fq[h]) != 0.f && !(s_st[qh] & ST_UPD);
             }
             if (u[0] || u[1] || u[2] || u[3]) {
               for (int64_t b0 = c + 1; b0 < m; b0 += 32 * QRPL) {
-                float2 xv[QRPL], xc[4][QRPL];
+                E xv[QRPL], xc[4][QRPL];
 #pragma unroll
                 for (int r = 0; r < QRPL; ++r) {
                   const int64_t i = b0 + lane + 32 * r;
                   const bool in = i < m;
-                  xv[r] = in ? V[i] : make_float2(0.f, 0.f);
+                  xv[r] = in ? Vc[i] : A::ezero();
 #pragma unroll
-                  for (int h = 0; h < 4; ++h) xc[h][r] = (in && u[h]) ? cg[h][i * rs] : make_float2(0.f, 0.f);
+                  for (int h = 0; h < 4; ++h) xc[h][r] = (in && u[h]) ? cg[h][i * rs] : A::ezero();
                 }
 #pragma unroll
                 for (int r = 0; r < QRPL; ++r) {
@@ -1893,10 +1956,7 @@ __device__ __forceinline__ void geqp3_df_body(const QrParams<double>& P, const Q
                   if (i < m) {
 #pragma unroll
                     for (int h = 0; h < 4; ++h)
-                      if (u[h]) {
-                        const Df y = df_axpy_neg(xc[h][r].x, xc[h][r].y, fq[h], xv[r].x, xv[r].y);
-                        cg[h][i * rs] = make_float2(y.h, y.l);
-                      }
+                      if (u[h]) cg[h][i * rs] = A::axpy_neg(xc[h][r], fq[h], xv[r]);
                   }
                 }
               }
@@ -1906,21 +1966,17 @@ __device__ __forceinline__ void geqp3_df_body(const QrParams<double>& P, const Q
         if (GCOL) {
           for (int sl = ct; sl < nloc; sl += NCT) {
             if (s_st[sl] & (ST_DONE | ST_UPD)) continue;
-            const Df fs = s_fs[sl];
-            if (fs.h == 0.f) continue;
-            float2* col = C + (int64_t)sl * cs;
+            const V fs = s_fs[sl];
+            if (A::hi(fs) == 0.f) continue;
+            E* col = C + (int64_t)sl * cs;
             for (int64_t i0 = c + 1; i0 < m; i0 += QSEQB) {
-              float2 xb[QSEQB];
+              E xb[QSEQB];
 #pragma unroll
               for (int r = 0; r < QSEQB; ++r)
                 if (i0 + r < m) xb[r] = col[(i0 + r) * rs];
 #pragma unroll
               for (int r = 0; r < QSEQB; ++r)
-                if (i0 + r < m) {
-                  const float2 v = V[i0 + r];
-                  const Df y = df_axpy_neg(xb[r].x, xb[r].y, fs, v.x, v.y);
-                  col[(i0 + r) * rs] = make_float2(y.h, y.l);
-                }
+                if (i0 + r < m) col[(i0 + r) * rs] = A::axpy_neg(xb[r], fs, Vc[i0 + r]);
             }
           }
         }
@@ -1945,12 +2001,8 @@ __device__ __forceinline__ void geqp3_df_body(const QrParams<double>& P, const Q
   for (int s = wid; s < nloc && !GCOL; s += NW) {
     if (s_st[s] & ST_DONE) continue;
     float* ph = Bh + (c0 + s) * lda;
-    float* pl = Bl + (c0 + s) * lda;
-    for (int64_t i = lane; i < m; i += 32) {
-      const float2 y = C[(int64_t)s * m + i];
-      ph[i] = y.x;
-      pl[i] = y.y;
-    }
+    float* pl = Bl ? Bl + (c0 + s) * lda : nullptr;
+    for (int64_t i = lane; i < m; i += 32) A::to_planes(C[(int64_t)s * m + i], ph, pl, i);
   }
   if (b == 0 && threadIdx.x == 0) {
     *P.k_out = kres;
@@ -1958,10 +2010,11 @@ __device__ __forceinline__ void geqp3_df_body(const QrParams<double>& P, const Q
   }
 }
 
-template <int NT>
-__global__ void __launch_bounds__(NT, 1) geqp3_df_smem_kernel(QrParams<double> P, QrV2Extra X, QrDf D, QrSm S) {
+template <class A, int NT>
+__global__ void __launch_bounds__(NT, 1) geqp3_df_smem_kernel(QrParams<typename A::T> P, QrV2Extra X, QrDf D,
+                                                              QrSm S) {
   extern __shared__ unsigned char qr_dyn[];
-  geqp3_df_body<NT, false>(P, X, D, S, gridDim.x, blockIdx.x, nullptr, 0, 0, qr_dyn);
+  geqp3_df_body<A, NT, false>(P, X, D, S, gridDim.x, blockIdx.x, nullptr, 0, 0, qr_dyn);
 }
 
 // one matrix of a batch: its parameters and its m x n float2 workspace
@@ -1986,7 +2039,8 @@ __global__ void __launch_bounds__(NT, 1) geqp3_df_group_kernel(const QrJob* __re
     __syncthreads();
     const int j = s_job;
     if (j >= njobs) return;
-    geqp3_df_body<NT, true>(jobs[j].P, jobs[j].X, jobs[j].D, S, 1, 0, jobs[j].work, jobs[j].cs, jobs[j].rs, qr_dyn);
+    geqp3_df_body<QrArithDf, NT, true>(jobs[j].P, jobs[j].X, jobs[j].D, S, 1, 0, jobs[j].work, jobs[j].cs,
+                                       jobs[j].rs, qr_dyn);
   }
 }
 
@@ -2137,13 +2191,79 @@ __global__ void df_split_kernel(int64_t m, int64_t n, const double* __restrict__
   }
 }
 
-// B = (h + l) / scale
+// the step at which each column became a pivot (n when it did not):
+// step_of[piv[c]] = c for c < nfac
+__global__ void qr_step_of_kernel(int64_t n, const int64_t* __restrict__ piv, const int64_t* __restrict__ nfac_p,
+                                  int64_t* __restrict__ step_of) {
+  const int64_t nfac = *nfac_p;
+  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < n; t += (int64_t)gridDim.x * blockDim.x)
+    step_of[t] = n;
+  __syncthreads();
+  if (blockIdx.x == 0)
+    for (int64_t c = threadIdx.x; c < nfac; c += blockDim.x) step_of[piv[c]] = c;
+}
+
+// B = (h + l) / scale, except the Householder vectors below the diagonal of
+// the pivot columns (rows below the step of column j), which carry no scale
 __global__ void df_join_kernel(int64_t m, int64_t n, const float* __restrict__ Bh, const float* __restrict__ Bl,
-                               int64_t ldh, const double* __restrict__ scale, double* __restrict__ B, int64_t ldb) {
+                               int64_t ldh, const double* __restrict__ scale, double* __restrict__ B, int64_t ldb,
+                               const int64_t* __restrict__ step_of) {
   const double inv = 1.0 / *scale;
   for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < m * n; t += (int64_t)gridDim.x * blockDim.x) {
     const int64_t i = t % m, j = t / m;
-    B[i + j * ldb] = df_val(Bh[i + j * ldh], Bl[i + j * ldh]) * inv;
+    const double v = df_val(Bh[i + j * ldh], Bl[i + j * ldh]);
+    B[i + j * ldb] = i > step_of[j] ? v : v * inv;
+  }
+}
+
+// the Float32 sketch's conversions for the shared-memory QR: max |B| (as
+// the bits of a double, for df_scale_kernel), B * scale (exact: a power of
+// two) with each column's norm, and back
+__global__ void f32_absmax_kernel(int64_t m, int64_t n, const float* __restrict__ B, int64_t ldb,
+                                  unsigned long long* __restrict__ out) {
+  double mx = 0;
+  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < m * n; t += (int64_t)gridDim.x * blockDim.x)
+    mx = fmax(mx, (double)fabsf(B[t % m + (t / m) * ldb]));
+  mx = warp_max(mx);
+  if ((threadIdx.x & 31) == 0 && mx > 0) atomicMax(out, (unsigned long long)__double_as_longlong(mx));
+}
+
+__global__ void f32_split_kernel(int64_t m, int64_t n, const float* __restrict__ B, int64_t ldb,
+                                 const double* __restrict__ scale, float* __restrict__ Bs, int64_t lds,
+                                 double* __restrict__ vn0) {
+  const int lane = threadIdx.x & 31;
+  const int64_t w0 = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
+  const int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
+  const float sc = (float)*scale;
+  for (int64_t j = w0; j < n; j += nw) {
+    double mx = 0;
+    for (int64_t i = lane; i < m; i += 32) {
+      const float x = B[i + j * ldb] * sc;
+      Bs[i + j * lds] = x;
+      mx = fmax(mx, (double)fabsf(x));
+    }
+    mx = warp_max(mx);
+    double acc = 0;
+    if (mx > 0) {
+      const double s = pow2_scale_inv(mx);
+      for (int64_t i = lane; i < m; i += 32) {
+        const double t = (double)Bs[i + j * lds] * s;
+        acc = fma(t, t, acc);
+      }
+      acc = sqrt(warp_sum(acc)) / s;
+    }
+    if (lane == 0) vn0[j] = acc;
+  }
+}
+
+__global__ void f32_join_kernel(int64_t m, int64_t n, const float* __restrict__ Bs, int64_t lds,
+                                const double* __restrict__ scale, float* __restrict__ B, int64_t ldb,
+                                const int64_t* __restrict__ step_of) {
+  const float inv = (float)(1.0 / *scale);
+  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < m * n; t += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t i = t % m, j = t / m;
+    const float v = Bs[i + j * lds];
+    B[i + j * ldb] = i > step_of[j] ? v : v * inv;
   }
 }
 
@@ -2542,7 +2662,72 @@ int64_t geqp3_adap(lra_ctx* ctx, int64_t m, int64_t n, T* A, int64_t lda, int64_
     post_launch(ctx, "iota_kernel");
     // the mixed-precision path factors Float64 sketches in double-float
     const bool dfq = sizeof(T) == 8 && ctx->gemm_tc && pivot;
-    if (dfq) {
+    // Float32 sketches stay in shared memory in FP32 when each CTA's share
+    // of the columns fits (the same kernel, QrArithF32)
+    constexpr int NTF = 512;
+    const int gsf = (int)std::min<int64_t>(std::min(ctx->num_sms, 256),
+                                           std::max<int64_t>(1, (n + NTF / 32 - 2) / (NTF / 32 - 1)));
+    const int64_t ncf = (n + gsf - 1) / gsf;
+    const size_t smem_f = (size_t)m * 4 + (size_t)ncf * m * 4 + (size_t)ncf * (4 * 4 + 4 + 1);
+    bool f32q = false;
+    if constexpr (sizeof(T) == 4) {
+      if (pivot && !dfq && n < (int64_t)XW_IDX && qr_smem_enabled()) {
+        raise_smem_limit(ctx, (const void*)geqp3_df_smem_kernel<QrArithF32, NTF>);
+        cudaFuncAttributes fa;
+        LRA_CUDA(cudaFuncGetAttributes(&fa, geqp3_df_smem_kernel<QrArithF32, NTF>));
+        f32q = smem_f <= (size_t)fa.maxDynamicSharedSizeBytes;
+        if (f32q) {
+          int per = 0;
+          LRA_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, geqp3_df_smem_kernel<QrArithF32, NTF>, NTF,
+                                                                 smem_f));
+          f32q = per >= 1;
+        }
+      }
+    }
+    if (f32q) {
+      if constexpr (sizeof(T) == 4) {
+        float* Bs = ctx->arena.alloc_n<float>((size_t)m * n);
+        double* vn0 = ctx->arena.alloc_n<double>(n);
+        double* scale = ctx->arena.alloc_n<double>(1);
+        unsigned long long* mx = ctx->arena.alloc_n<unsigned long long>(1);
+        LRA_CUDA(cudaMemsetAsync(mx, 0, sizeof(unsigned long long), ctx->stream));
+        const unsigned gm = (unsigned)std::max<int64_t>(1, std::min<int64_t>((m * n + 255) / 256, ctx->num_sms * 8));
+        f32_absmax_kernel<<<gm, 256, 0, ctx->stream>>>(m, n, A, lda, mx);
+        post_launch(ctx, "f32_absmax_kernel");
+        df_scale_kernel<<<1, 1, 0, ctx->stream>>>(mx, scale);
+        post_launch(ctx, "df_scale_kernel");
+        const unsigned gs = (unsigned)std::max<int64_t>(1, std::min<int64_t>((n + 7) / 8, ctx->num_sms * 8));
+        f32_split_kernel<<<gs, 256, 0, ctx->stream>>>(m, n, A, lda, scale, Bs, m, vn0);
+        post_launch(ctx, "f32_split_kernel");
+        QrDf D{Bs, nullptr, vn0, scale, nullptr};
+        if (trace_on()) {
+          D.stamps = ctx->arena.alloc_n<unsigned long long>((size_t)16 * std::max<int64_t>(P.kmax, 1));
+          LRA_CUDA(cudaMemsetAsync(D.stamps, 0, (size_t)16 * std::max<int64_t>(P.kmax, 1) * 8, ctx->stream));
+        }
+        QrParams<float> Pf = P;
+        Pf.lda = m;
+        Pf.part_d = ctx->arena.alloc_n<double>(gsf);
+        QrSm S;
+        S.pubt = nullptr;
+        if (D.stamps) {
+          S.pubt = ctx->arena.alloc_n<unsigned long long>((size_t)gsf * P.kmax);
+          LRA_CUDA(cudaMemsetAsync(S.pubt, 0, (size_t)gsf * P.kmax * 8, ctx->stream));
+        }
+        S.xw = ctx->arena.alloc_n<unsigned long long>((size_t)2 * gsf);
+        S.stage = ctx->arena.alloc_n<float>((size_t)2 * gsf * m);
+        LRA_CUDA(cudaMemsetAsync(S.xw, 0, (size_t)2 * gsf * sizeof(unsigned long long), ctx->stream));
+        void* args[] = {&Pf, &X, &D, &S};
+        LRA_CUDA(cudaLaunchCooperativeKernel((const void*)geqp3_df_smem_kernel<QrArithF32, NTF>, dim3(gsf), dim3(NTF),
+                                             args, smem_f, ctx->stream));
+        post_launch(ctx, "geqp3_f32_smem_kernel");
+        if (D.stamps) print_qr_trace(ctx, D.stamps, P.kmax, m, n, "geqp3_f32_smem_kernel", true, S.pubt, gsf);
+        int64_t* step_of = ctx->arena.alloc_n<int64_t>(n);
+        qr_step_of_kernel<<<1, 1024, 0, ctx->stream>>>(n, X.piv, X.nfac, step_of);
+        post_launch(ctx, "qr_step_of_kernel");
+        f32_join_kernel<<<gm, 256, 0, ctx->stream>>>(m, n, Bs, m, scale, A, lda, step_of);
+        post_launch(ctx, "f32_join_kernel");
+      }
+    } else if (dfq) {
       float* Bh = ctx->arena.alloc_n<float>((size_t)m * n);
       float* Bl = ctx->arena.alloc_n<float>((size_t)m * n);
       double* vn0 = ctx->arena.alloc_n<double>(n);
@@ -2574,13 +2759,13 @@ int64_t geqp3_adap(lra_ctx* ctx, int64_t m, int64_t n, T* A, int64_t lda, int64_
       const size_t smem_s = (size_t)m * sizeof(float2) + (size_t)ncap * m * sizeof(float2) + (size_t)ncap * (5 * 8 + 1);
       bool smq = n < (int64_t)XW_IDX && qr_smem_enabled();
       if (smq) {
-        raise_smem_limit(ctx, (const void*)geqp3_df_smem_kernel<NTS>);
+        raise_smem_limit(ctx, (const void*)geqp3_df_smem_kernel<QrArithDf, NTS>);
         cudaFuncAttributes fa;
-        LRA_CUDA(cudaFuncGetAttributes(&fa, geqp3_df_smem_kernel<NTS>));
+        LRA_CUDA(cudaFuncGetAttributes(&fa, geqp3_df_smem_kernel<QrArithDf, NTS>));
         smq = smem_s <= (size_t)fa.maxDynamicSharedSizeBytes;
         if (smq) {
           int per = 0;
-          LRA_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, geqp3_df_smem_kernel<NTS>, NTS, smem_s));
+          LRA_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, geqp3_df_smem_kernel<QrArithDf, NTS>, NTS, smem_s));
           smq = per >= 1;
         }
       }
@@ -2599,7 +2784,7 @@ int64_t geqp3_adap(lra_ctx* ctx, int64_t m, int64_t n, T* A, int64_t lda, int64_
         S.stage = ctx->arena.alloc_n<float2>((size_t)2 * gsm * m);
         LRA_CUDA(cudaMemsetAsync(S.xw, 0, (size_t)2 * gsm * sizeof(unsigned long long), ctx->stream));
         void* args[] = {&Pd, &X, &D, &S};
-        LRA_CUDA(cudaLaunchCooperativeKernel((const void*)geqp3_df_smem_kernel<NTS>, dim3(gsm), dim3(NTS), args,
+        LRA_CUDA(cudaLaunchCooperativeKernel((const void*)geqp3_df_smem_kernel<QrArithDf, NTS>, dim3(gsm), dim3(NTS), args,
                                              smem_s, ctx->stream));
       } else {
         raise_smem_limit(ctx, (const void*)geqp3_df_kernel<NT>);
@@ -2615,7 +2800,11 @@ int64_t geqp3_adap(lra_ctx* ctx, int64_t m, int64_t n, T* A, int64_t lda, int64_
       }
       post_launch(ctx, kname);
       if (D.stamps) print_qr_trace(ctx, D.stamps, P.kmax, m, n, kname, smq, pubt, gsm);
-      df_join_kernel<<<gm, 256, 0, ctx->stream>>>(m, n, Bh, Bl, m, scale, reinterpret_cast<double*>(A), lda);
+      int64_t* step_of = ctx->arena.alloc_n<int64_t>(n);
+      qr_step_of_kernel<<<1, 1024, 0, ctx->stream>>>(n, X.piv, X.nfac, step_of);
+      post_launch(ctx, "qr_step_of_kernel");
+      df_join_kernel<<<gm, 256, 0, ctx->stream>>>(m, n, Bh, Bl, m, scale, reinterpret_cast<double*>(A), lda,
+                                                  step_of);
       post_launch(ctx, "df_join_kernel");
     } else {
       void* args[] = {&P, &X};

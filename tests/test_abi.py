@@ -133,3 +133,35 @@ def test_tuning_table_syntax():
         else:
             raise AssertionError(f"unknown key {key}")
     assert {"tc_tile_n", "qr_seq_len", "srft_wide"} <= seen
+
+
+def test_julia_shim_binds_exported_symbols(lib):
+    """The Julia binding (julia/LowRankApproxGPU.jl) ccalls only entry points
+    that the header declares and the library exports, and its mirrors of the
+    header's structs list the same fields in the same order."""
+    jl = open(os.path.join(ROOT, "lowrankapprox.jl_gb300", "julia", "LowRankApproxGPU.jl")).read()
+    called = set(re.findall(r"\(:(lra_\w+), liblra\)", jl))
+    called |= {f"lra_{n}_linop" for n in re.findall(r"\(:(pqrfact|prange), true\)", jl)}
+    assert len(called) >= 30
+    declared = set(header_symbols())
+    assert called <= declared, sorted(called - declared)
+    # field widths in order: the layout ccall sees
+    csize = {"double": 8, "int64_t": 8, "uint64_t": 8, "int32_t": 4, "lra_matmat_fn": 8}
+    hdr = re.sub(r"/\*.*?\*/", "", open(os.path.join(ROOT, "include", "lra.h")).read(), flags=re.S)
+    for name in ("lra_opts", "lra_rand", "lra_id", "lra_pqr", "lra_psvd", "lra_pheig", "lra_cur", "lra_linop"):
+        body = re.search(r"typedef struct %s \{(.*?)\} %s;" % (name, name), hdr, re.S).group(1)
+        cw = []
+        for decl in filter(str.strip, body.split(";")):
+            typ, names = re.match(r"\s*(?:const\s+)?(\w+)\s*(.*)", decl).groups()
+            for f in names.split(","):
+                arr = re.search(r"\[(\d+)\]", f)
+                w = 8 if "*" in f else csize[typ]
+                cw.append(w * (int(arr.group(1)) if arr else 1))
+        m = re.search(r"struct %s\b(.*?)\bend\b" % name, jl, re.S)
+        jw = []
+        for t in re.findall(r"\w+::([\w{},]+)", m.group(1)):
+            tup = re.match(r"NTuple\{(\d+),(\w+)\}", t)
+            base = tup.group(2) if tup else t
+            w = 8 if base.startswith("Ptr") else {"Float64": 8, "Int64": 8, "UInt64": 8, "Int32": 4}[base]
+            jw.append(w * (int(tup.group(1)) if tup else 1))
+        assert jw == cw, (name, jw, cw)

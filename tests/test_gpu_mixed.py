@@ -173,3 +173,49 @@ def test_psvd_mixed_clustered(lra):
     assert np.abs(Fm.U.T @ Fm.U - np.eye(k)).max() < 1e-11
     assert np.abs(Fm.Vt @ Fm.Vt.T - np.eye(k)).max() < 1e-10
     assert np.allclose(Fm.S[:80], s[:80], rtol=1e-12)
+
+
+def test_mixed_q_factors(lra):
+    """A Q built from the pivoted QR's reflectors on the mixed path (the
+    double-float shared-memory kernel): pqrfact with sketch :none, the
+    right sketchfact's Q and prange give orthonormal bases that reproduce
+    A (the reflectors below the diagonal carry no scale)."""
+    A = decaying(700, 500, 20.0, 9) * 37.0          # a scale far from 1
+    rtol = 1e-10
+    o = lra.LRAOptions(rtol=rtol, precision="mixed")
+    F = lra.pqrfact(A, o.copy(sketch="none"))
+    Q = np.asarray(F.Q)
+    assert np.abs(Q.T @ Q - np.eye(F.k)).max() < 1e-12
+    assert relerr(A, F.matrix()) < 100 * rtol
+    g = lattice(14, 4_000_000)
+    S = lra.sketchfact("right", "n", A, o.copy(pqrfact_retval="qr"), rand=lra.RandStream(gauss=g))
+    Qs = np.asarray(S.Q)
+    assert np.abs(Qs.T @ Qs - np.eye(S.k)).max() < 1e-12
+    assert np.linalg.norm(A - Qs @ (Qs.T @ A)) <= 100 * rtol * np.linalg.norm(A)
+    P = np.asarray(lra.prange("n", A, o, rand=lra.RandStream(gauss=g)))
+    assert np.abs(P.T @ P - np.eye(P.shape[1])).max() < 1e-12
+    assert np.linalg.norm(A - P @ (P.T @ A)) <= 100 * rtol * np.linalg.norm(A)
+
+
+@pytest.mark.parametrize("shape", [(72, 900), (264, 4096), (1032, 4096), (40, 300)])
+def test_f32_shared_memory_qr_vs_oracle(lra, oracle, shape):
+    """Float32 sketches factored in shared memory (the one-word exchange
+    kernel in FP32) against the real LAPACK SLAQPS: rank, pivots up to a
+    demonstrated near-tie, R and tau."""
+    import torch
+    from test_oracle import assert_pqr_parity, check_rank
+    m, n = shape
+    rng = np.random.default_rng(m + n)
+    B = (rng.standard_normal((m, n)) @ np.diag(np.exp(-np.arange(n) / (n / 12.0))) * 3.0).astype(np.float32)
+    B = np.asfortranarray(B)
+    rtol = 1e-5
+    W = B.copy(order="F")
+    be = "lapack" if oracle.lapack_available() else "c"
+    p_ref, t_ref, k_ref = oracle.geqp3_adap(W, oracle.Opts(rtol=rtol).for_dtype(np.float32), backend=be)
+    Bd = torch.from_numpy(B).cuda().t().contiguous().t()
+    jpvt, tau, k = lra.geqp3_adap(Bd, lra.LRAOptions(np.float32, rtol=rtol))
+    p = jpvt.cpu().numpy()
+    check_rank(B, k, k_ref, p, p_ref, rtol, np.float32)
+    same = check_pivots(B, p, p_ref, min(k, k_ref), np.float32)
+    if same == k == k_ref:
+        assert_pqr_parity(p, np.triu(Bd.cpu().numpy()[:k]), p_ref, np.triu(W[:k]), k, 5e-5)
