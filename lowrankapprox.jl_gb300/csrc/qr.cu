@@ -1849,32 +1849,12 @@ __device__ __forceinline__ void geqp3_df_body(const QrParams<typename A::T>& P, 
             }
           }
           if (flagged) {
-            // unreliable downdate: the column's update now and the norm of
-            // its rows c+1..m-1 (xLAQPS would end the block here and
-            // recompute the norm before the next pivot, from the same
-            // updated column); this thread alone, row by row, in double-float
-            // at a power-of-two scale that puts the largest entry in [1, 2)
-            E* col = C + (int64_t)s * cs;
-            if (A::hi(fs) != 0.f)
-              for (int64_t i = c + 1; i < m; ++i) col[i * rs] = A::axpy_neg(col[i * rs], fs, Vc[i]);
-            float mx = 0.f;
-            for (int64_t i = c + 1; i < m; ++i) mx = fmaxf(mx, fabsf(A::ehi(col[i * rs])));
-            V nr = A::from_float(mx);
-            if (mx > 0.f && isfinite(mx)) {
-              const int ex = ilogbf(mx);
-              const float sc = ldexpf(1.f, -ex);
-              V acc = A::zero();
-              for (int64_t i = c + 1; i < m; ++i) {
-                const E x = A::escale(col[i * rs], sc);
-                A::fma_acc(acc, x, x);
-              }
-              const V r = A::sqrt_(A::norm(acc));
-              nr = A::ldexp_(r, ex);
-            }
-            v1 = nr;
-            s_vn1[s] = s_vn2[s] = v1;
-            s_st[s] = st | ST_UPD;
+            // unreliable downdate: xLAQPS would end the block here and
+            // recompute the norm before the next pivot, from the updated
+            // column; a warp does that below
+            s_st[s] = st | ST_FLAG;
             wfl = 1;
+            continue;
           }
           const unsigned long long w = xw_pack<A>(v1, c0 + s);
           ww = w > ww ? w : ww;
@@ -1882,7 +1862,54 @@ __device__ __forceinline__ void geqp3_df_body(const QrParams<typename A::T>& P, 
       }
       sub(9);
       sub(10);
-      sub(11);
+      // ---- the flagged columns, a warp each: the deferred update of rows
+      // c+1..m-1 now, then their norm in double-float at a power-of-two
+      // scale that puts the largest entry in [1, 2) (lane-strided partial
+      // sums and a butterfly, the same tree in both forms of the kernel)
+      if (__syncthreads_or(wfl)) {
+        sub(11);
+        for (int s = wid; s < nloc; s += NW) {
+          if (!(s_st[s] & ST_FLAG)) continue;
+          E* col = C + (int64_t)s * cs;
+          const V fs = s_fs[s];
+          const bool upd = A::hi(fs) != 0.f;
+          float mx = 0.f;
+          for (int64_t i = c + 1 + lane; i < m; i += 32) {
+            E y = col[i * rs];
+            if (upd) {
+              y = A::axpy_neg(y, fs, Vc[i]);
+              col[i * rs] = y;
+            }
+            mx = fmaxf(mx, fabsf(A::ehi(y)));
+          }
+#pragma unroll
+          for (int o = 16; o > 0; o >>= 1) mx = fmaxf(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+          V nr = A::from_float(mx);
+          if (mx > 0.f && isfinite(mx)) {
+            const int ex = ilogbf(mx);
+            const float sc = ldexpf(1.f, -ex);
+            V acc = A::zero();
+            for (int64_t i = c + 1 + lane; i < m; i += 32) {
+              const E x = A::escale(col[i * rs], sc);
+              A::fma_acc(acc, x, x);
+            }
+            acc = A::norm(acc);
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) acc = A::add(acc, A::shfl_xor(acc, o));
+            nr = A::ldexp_(A::sqrt_(acc), ex);
+          }
+          __syncwarp();
+          if (lane == 0) {
+            s_vn1[s] = s_vn2[s] = nr;
+            s_st[s] = (unsigned char)((s_st[s] & ~ST_FLAG) | ST_UPD);
+          }
+          const unsigned long long w = xw_pack<A>(nr, c0 + s);
+          ww = w > ww ? w : ww;
+        }
+        wfl = 1;
+      } else {
+        sub(11);
+      }
       sub(12);
       warp_word(ww, wfl);
       sub(13);
