@@ -194,6 +194,10 @@ const char* lra_last_error(const lra_ctx* ctx);
 const char* lra_status_string(int status);
 /* number of kernels this context has launched (instrumentation) */
 int64_t lra_ctx_launches(const lra_ctx* ctx);
+/* number of launches of the kernel called `name` (the names the launch
+   list of a profiler shows, e.g. "geqp3_df_smem_kernel"), cumulative over
+   the context's life (instrumentation; no counterpart in the reference) */
+int64_t lra_ctx_kernel_launches(const lra_ctx* ctx, const char* name);
 /* device time of the last call's stages, ms: sketch, qr, solve, post */
 int lra_ctx_stage_ms(const lra_ctx* ctx, double out[4]);
 

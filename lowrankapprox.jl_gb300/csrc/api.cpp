@@ -10,6 +10,7 @@
 #include <cstdlib>
 #include <cstring>
 #include <new>
+#include <limits>
 #include <numeric>
 #include <vector>
 #include <unordered_map>
@@ -210,6 +211,19 @@ struct RandSrc {
   }
   bool injected_gauss() const { return r && r->gauss; }
   bool injected_ints() const { return r && r->ints; }
+
+  // the position in both streams (a step drawn ahead and not used is
+  // rewound, so that later draws see the positions of the step-by-step loop)
+  struct Pos {
+    int64_t g, q;
+    uint64_t counter;
+  };
+  Pos pos() const { return Pos{g, q, ctx->rng_counter}; }
+  void seek(const Pos& p) {
+    g = p.g;
+    q = p.q;
+    ctx->rng_counter = p.counter;
+  }
 
   const double* take_gauss_raw(int64_t n) {
     if (g + n > r->gauss_len)
@@ -518,6 +532,142 @@ struct Fact {
 template <typename T>
 void maxdet_dev(lra_ctx* ctx, const lra_opts& o, Fact<T>& F);
 
+// The rank a step whose rank reached its threshold points to: where the
+// line through log |R_ii| over the middle half of its pivots crosses the
+// rank test's threshold (rtol |R_11|, or atol).  The last pivots of a short
+// sketch fall faster than the matrix's spectrum, so they are left out.  A step whose factorization
+// stopped below kmax revealed the rank itself.  -1 when the diagonal gives
+// no estimate; a large value when it does not decay.  Used only to decide
+// how many steps to factor together.
+template <typename T>
+int64_t predict_rank(lra_ctx* ctx, const Fact<T>& F, int64_t kmax, const lra_opts& o) {
+  const int64_t k = F.k;
+  if (k <= 1) return -1;
+  if (k < kmax) return k;
+  std::vector<T> d((size_t)k);
+  LRA_CUDA(cudaMemcpy2DAsync(d.data(), sizeof(T), F.B, (size_t)(F.ld + 1) * sizeof(T), sizeof(T), (size_t)k,
+                             cudaMemcpyDeviceToHost, ctx->stream));
+  LRA_CUDA(cudaStreamSynchronize(ctx->stream));
+  const double d0 = std::fabs((double)d[0]);
+  const double ptol = std::max(o.atol, o.rtol * d0);
+  const int64_t i1 = k / 4, i2 = std::max<int64_t>(i1 + 1, (3 * k) / 4);
+  const double a = std::fabs((double)d[(size_t)i1]), b = std::fabs((double)d[(size_t)i2]);
+  if (!(ptol > 0) || !(a > 0) || !(b > 0) || !std::isfinite(a) || !std::isfinite(b)) return -1;
+  if (b <= ptol) return k;
+  const double slope = (std::log(b) - std::log(a)) / (double)(i2 - i1);
+  if (!(slope < -1e-12)) return std::numeric_limits<int64_t>::max() / 4;
+  const double r = (double)i2 + (std::log(ptol) - std::log(b)) / slope;
+  return r > 1e15 ? std::numeric_limits<int64_t>::max() / 4 : std::max<int64_t>(k, (int64_t)r);
+}
+
+// Steps step, step + 1, ... of sketchfact_dev's loop (thresholds nt, 2 nt,
+// ...) up to the first whose threshold exceeds 1.3 times the predicted rank,
+// as many as one shared-memory launch holds, sketched in order and factored
+// together.  Returns the number of steps taken when one of them revealed
+// its rank (F is then that step's factorization and the random streams stand
+// where that step left them), minus that number when none did (the streams
+// stand after the last), and 0 when fewer than two steps fit one launch
+// (nothing done).
+template <typename T>
+int sketchfact_steps(lra_ctx* ctx, const lra_opts& o, char trans, int64_t M, int64_t N, const T* A, int64_t lda,
+                     RandSrc& rs, int dtype, TcSplit* split, int step, int64_t nt, int64_t rank_hint,
+                     const ArenaMark& base, Fact<T>& F) {
+  const int64_t limit = rank_hint > (int64_t)1 << 40 ? (int64_t)1 << 40 : rank_hint + (rank_hint * 3) / 10;
+  std::vector<int64_t> orders, nts, ms;
+  int64_t t = nt;
+  for (int i = 0; i < ctx->tuning.qr_steps && i < 8; ++i) {
+    const int64_t order = samp(o, t);
+    if (order <= 0) break;
+    orders.push_back(order);
+    nts.push_back(t);
+    ms.push_back(order);
+    // the step that should reveal the rank (its threshold above the
+    // prediction), or the one whose sketch covers every column, is the last
+    if (t > limit || std::min(order, N) >= N) break;
+    if (t > ((int64_t)1 << 40)) break;
+    t *= 2;
+  }
+  int cnt = geqp3_steps_fit<T>(ctx, (int)orders.size(), ms.data(), N);
+  if (cnt < 2) return 0;
+  std::vector<QrStep<T>> st;
+  std::vector<RandSrc::Pos> after;
+  {
+    Stage sg(ctx, 0);
+    for (int i = 0; i < cnt; ++i) {
+      const int64_t order = orders[(size_t)i];
+      const int64_t l = std::min(order, N);
+      const int64_t kmax = (o.rank < 0 || o.rank > l) ? l : o.rank;
+      QrStep<T> q;
+      q.m = order;
+      q.n = N;
+      q.lda = std::max<int64_t>(order, 1);
+      q.A = ctx->arena.alloc_n<T>((size_t)q.lda * N);
+      q.jpvt = ctx->arena.alloc_n<int64_t>(N);
+      q.tau = ctx->arena.alloc_n<T>(std::max<int64_t>(l, 1));
+      q.kmax = kmax;
+      q.nt = nts[(size_t)i];
+      const RandSrc::Pos before = rs.pos();
+      try {
+        make_sketch<T>(ctx, o, trans, M, N, A, lda, order, rs, q.A, dtype, split);
+      } catch (const Error& e) {
+        // an injected stream too short for a step drawn ahead: the launch
+        // ends before it (the step-by-step loop meets the same error only if
+        // it gets there)
+        if (e.status != LRA_ERAND || i == 0) throw;
+        rs.seek(before);
+        cnt = i;
+        break;
+      }
+      st.push_back(q);
+      after.push_back(rs.pos());
+    }
+  }
+  if (cnt < 2) {
+    // not enough left to share a launch: back to one step at a time
+    rs.seek(after.empty() ? rs.pos() : after[0]);
+    if (!after.empty()) {
+      // the one sketch drawn is the step's own; factor it here
+      const QrStep<T>& q = st[0];
+      int64_t k = 0;
+      {
+        Stage sq(ctx, 1);
+        k = geqp3_adap<T>(ctx, q.m, q.n, q.A, q.lda, q.jpvt, q.tau, q.kmax, o.nb, o.atol, o.rtol, true);
+      }
+      F.order = q.m;
+      F.ld = q.lda;
+      F.B = q.A;
+      F.jpvt = q.jpvt;
+      F.tau = q.tau;
+      F.k = k;
+      F.nsteps = step + 1;
+      if (k < q.nt) return 1;
+      ctx->arena.release(base);
+      return -1;
+    }
+    return 0;
+  }
+  std::vector<int64_t> ks((size_t)cnt);
+  int c;
+  {
+    Stage sq(ctx, 1);
+    c = geqp3_adap_steps<T>(ctx, cnt, st.data(), o.nb, o.atol, o.rtol, ks.data());
+  }
+  if (c < 0) {
+    ctx->arena.release(base);
+    return -cnt;
+  }
+  const QrStep<T>& q = st[(size_t)c];
+  F.order = q.m;
+  F.ld = q.lda;
+  F.B = q.A;
+  F.jpvt = q.jpvt;
+  F.tau = q.tau;
+  F.k = ks[(size_t)c];
+  F.nsteps = step + c + 1;
+  rs.seek(after[(size_t)c]);
+  return c + 1;
+}
+
 template <typename T>
 Fact<T> sketchfact_dev(lra_ctx* ctx, const lra_opts& o, char trans, int64_t M, int64_t N, const T* A,
                        int64_t lda, RandSrc& rs, int dtype) {
@@ -532,8 +682,29 @@ Fact<T> sketchfact_dev(lra_ctx* ctx, const lra_opts& o, char trans, int64_t M, i
     tc_split<T>(ctx, trans, M, N, A, lda, dtype == LRA_F64 ? 6 : 3, &split);
   }
   const ArenaMark base = ctx->arena.mark();
+  // Steps factored together: once a step's rank has reached its threshold,
+  // the decay of its R diagonal predicts the rank, and the steps up to the
+  // one that should reveal it are sketched and factored by one launch of the
+  // shared-memory pivoted QR (each on CTAs of its own; a step that reveals
+  // its rank stops the later ones).  The first step whose rank comes out
+  // below its threshold is the result, the same as one step at a time; the
+  // prediction only decides how many steps share a launch.
+  const bool ahead = adaptive && !ctx->linop && ctx->tuning.qr_steps > 1 && N > 0 && M > 0;
+  int64_t rank_hint = -1;
   for (int step = 0;; ++step) {
     if (step > 62) fail(LRA_EINVAL, "adaptive sketch did not terminate");
+    if (ahead && rank_hint >= 0) {
+      const int done = sketchfact_steps<T>(ctx, o, trans, M, N, A, lda, rs, dtype, split.ns ? &split : nullptr,
+                                           step, nt, rank_hint, base, F);
+      if (done > 0) break;
+      if (done < 0) {
+        // every step of the launch reached its threshold
+        step += -done - 1;
+        for (int i = 0; i < -done; ++i) nt *= 2;
+        rank_hint = -1;
+        continue;
+      }
+    }
     const int64_t order = samp(o, nt);
     if (order < 0) fail(LRA_EINVAL, "sketch order %lld", (long long)order);
     const int64_t l = std::min(order, N);
@@ -553,6 +724,7 @@ Fact<T> sketchfact_dev(lra_ctx* ctx, const lra_opts& o, char trans, int64_t M, i
     }
     F.nsteps = step + 1;
     if (!adaptive || F.k < nt) break;
+    if (ahead) rank_hint = predict_rank<T>(ctx, F, kmax, o);
     nt *= 2;
     ctx->arena.release(base);
   }
@@ -2167,6 +2339,12 @@ int lra_ctx_set_stream(lra_ctx* ctx, void* stream) {
 const char* lra_last_error(const lra_ctx* ctx) { return ctx ? ctx->last_error.c_str() : "no context"; }
 
 int64_t lra_ctx_launches(const lra_ctx* ctx) { return ctx ? ctx->launches : 0; }
+
+int64_t lra_ctx_kernel_launches(const lra_ctx* ctx, const char* name) {
+  if (!ctx || !name) return 0;
+  const auto it = ctx->launches_by_name.find(name);
+  return it == ctx->launches_by_name.end() ? 0 : it->second;
+}
 
 int lra_ctx_stage_ms(const lra_ctx* ctx, double out[4]) {
   if (!ctx || !out) return LRA_EINVAL;

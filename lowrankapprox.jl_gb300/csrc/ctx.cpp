@@ -35,6 +35,7 @@ void check_cuda(cudaError_t e, const char* what) {
 
 void post_launch(lra_ctx* ctx, const char* name) {
   count_launch(ctx);
+  ++ctx->launches_by_name[name];
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) fail(LRA_ECUDA, "launch of %s: %s", name, cudaGetErrorString(e));
 }
@@ -152,6 +153,7 @@ bool trace_on() {
 //   tc_tile_n <f32|f64> <log2 order> <32|64|96>
 //   qr_seq_len <rows>
 //   srft_wide <log2 l'> <0|1>
+//   qr_steps <1..8>
 // lowrankapprox/autotune.py writes it from its sweeps; unknown keys and
 // out-of-range values are ignored, so an old table never breaks a newer
 // library.
@@ -161,6 +163,7 @@ static void tuning_defaults(lra_tuning* t) {
     for (int& v : row) v = 96;
   t->qr_seq_len = 96;
   for (int lb = 0; lb <= 10; ++lb) t->srft_wide[lb] = (lb >= 7 && lb <= 10) ? 1 : 0;
+  t->qr_steps = 8;
 }
 
 bool set_tuning(lra_tuning* t, const char* key, int64_t index, int64_t value) {
@@ -177,6 +180,11 @@ bool set_tuning(lra_tuning* t, const char* key, int64_t index, int64_t value) {
   if (!std::strcmp(key, "srft_wide")) {
     if (index < 0 || index > 10 || (value != 0 && value != 1)) return false;
     t->srft_wide[index] = (int)value;
+    return true;
+  }
+  if (!std::strcmp(key, "qr_steps")) {
+    if (value < 1 || value > 8) return false;
+    t->qr_steps = (int)value;
     return true;
   }
   return false;
@@ -217,6 +225,9 @@ void load_tuning(lra_tuning* t, std::string* source) {
     } else if (key == "srft_wide") {
       int64_t lb = -1, v = 0;
       if (in >> lb >> v) used += set_tuning(t, "srft_wide", lb, v);
+    } else if (key == "qr_steps") {
+      int64_t v = 0;
+      if (in >> v) used += set_tuning(t, "qr_steps", 0, v);
     }
   }
   *source = path + " (" + std::to_string(used) + " entries)";
@@ -228,6 +239,7 @@ std::string tuning_text(const lra_tuning& t) {
     for (int lb = 0; lb < 16; ++lb) o << "tc_tile_n " << (d ? "f64 " : "f32 ") << lb << ' ' << t.tc_tile_n[d][lb] << '\n';
   o << "qr_seq_len " << t.qr_seq_len << '\n';
   for (int lb = 0; lb <= 10; ++lb) o << "srft_wide " << lb << ' ' << t.srft_wide[lb] << '\n';
+  o << "qr_steps " << t.qr_steps << '\n';
   return o.str();
 }
 

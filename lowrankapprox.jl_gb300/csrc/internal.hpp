@@ -6,6 +6,7 @@
 
 #include <cstdarg>
 #include <string>
+#include <unordered_map>
 #include <vector>
 
 #include "../../include/lra.h"
@@ -73,6 +74,9 @@ struct lra_tuning {
   // Float32 SRFT: 1 selects the 512-thread swizzled form for log2(l') when
   // it applies (7..10), 0 the 256-thread padded form
   int srft_wide[11];
+  // adaptive sketch steps the shared-memory pivoted QR may factor in one
+  // launch (1: one step at a time)
+  int qr_steps;
 };
 
 struct lra_ctx {
@@ -83,6 +87,7 @@ struct lra_ctx {
   lra::Arena arena;
   std::string last_error;
   int64_t launches = 0;
+  std::unordered_map<std::string, int64_t> launches_by_name;
   double stage_ms[4] = {0, 0, 0, 0};
   cudaEvent_t ev[5] = {nullptr, nullptr, nullptr, nullptr, nullptr};
   uint64_t rng_counter = 0;  // advances per call of the in-library generator
@@ -182,6 +187,30 @@ void geqp3_df_batch(lra_ctx* ctx, int64_t count, const DfBatchItem* items, int64
 
 // Rank-adaptive column-pivoted Householder QR (geqp3_adap!), in place.
 // pivot == false runs the same Householder QR without pivoting.
+// Several adaptive steps' sketches factored by one launch of the
+// shared-memory pivoted QR, each on CTAs of its own.  A step whose rank
+// comes out below its threshold (k < nt) stops the steps after it at their
+// next pivot; the factors (A, jpvt, tau) are written for the first such step
+// only.  k[i] is step i's rank (-1 for a step that a lower one stopped).
+// Returns the index of that first step, or -1 when every step's rank reached
+// its threshold (no factors written).
+template <typename T>
+struct QrStep {
+  int64_t m, n;
+  T* A;
+  int64_t lda;
+  int64_t* jpvt;
+  T* tau;
+  int64_t kmax, nt;
+};
+// how many of the leading steps (m[i] x n sketches, i < count) one launch can
+// hold together: 0 when the shared-memory kernel does not apply
+template <typename T>
+int geqp3_steps_fit(lra_ctx* ctx, int count, const int64_t* m, int64_t n);
+template <typename T>
+int geqp3_adap_steps(lra_ctx* ctx, int count, const QrStep<T>* steps, int64_t nb, double atol, double rtol,
+                     int64_t* k);
+
 template <typename T>
 int64_t geqp3_adap(lra_ctx* ctx, int64_t m, int64_t n, T* A, int64_t lda, int64_t* jpvt,
                    T* tau, int64_t kmax, int64_t nb, double atol, double rtol, bool pivot);

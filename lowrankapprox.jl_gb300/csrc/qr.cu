@@ -1314,6 +1314,13 @@ struct QrSm {
   unsigned long long* xw;    // [2][G] exchange words, zeroed before the launch
   void* stage;               // [2][G][m] staged candidate columns (elements of the arithmetic)
   unsigned long long* pubt;  // LRA_TRACE: %globaltimer of each CTA's word per pivot, [kmax][G], or null
+  // several adaptive steps factored by one launch: the lowest index of a
+  // step whose rank came out below its threshold (k < nt), shared by the
+  // launch's steps, or null; a step whose index is higher stops at its next
+  // exchange
+  int* success = nullptr;
+  int job = 0;
+  int64_t nt = 0;
 };
 
 // the next four live slots s, s + step, ... of a warp (-1: absent); s moves on
@@ -1335,6 +1342,10 @@ __device__ __forceinline__ int live_quad(const unsigned char* st, int nloc, int 
 
 constexpr unsigned long long XW_IDX = 0xFFFFFFull;  // 24-bit column field, stored as XW_IDX - j
 constexpr unsigned long long XW_LOW = (1ull << 62) - 1;
+// the word of a CTA that stops a cancelled step: above every candidate's
+// (a finite norm's key stays below 2^38 - 1), so every CTA of the step sees
+// it at the same exchange
+constexpr unsigned long long XW_CANCEL = XW_LOW;
 
 // The arithmetic of the shared-memory pivoted QR.  Float64 sketches are
 // held as double-float pairs (the mixed path's sketch has 2^-48
@@ -1448,7 +1459,7 @@ __device__ __forceinline__ void geqp3_df_body(const QrParams<typename A::T>& P, 
   __shared__ V s_alpha, s_f, s_tau, s_beta;
   __shared__ double s_red[32];
   __shared__ unsigned long long s_win;
-  __shared__ int s_owner, s_stop, s_ok;
+  __shared__ int s_owner, s_stop, s_ok, s_cancel;
   __shared__ double s_taud, s_betad;
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
   const int64_t m = P.m, n = P.n, lda = P.lda;
@@ -1516,8 +1527,9 @@ __device__ __forceinline__ void geqp3_df_body(const QrParams<typename A::T>& P, 
   // exchange e; the candidate's deferred update (upd) is applied on the way.
   // The word goes out after every thread's staged rows.
   auto publish = [&](unsigned e, int64_t r0, bool upd) {
-    const unsigned long long w = s_win;
-    if (w & XW_LOW) {
+    const bool cancel = !GCOL && s_cancel;
+    const unsigned long long w = cancel ? XW_CANCEL : s_win;
+    if (!cancel && (w & XW_LOW)) {
       const int sc = (int)((int64_t)(XW_IDX - (w & XW_IDX)) - c0);
       E* col = C + (int64_t)sc * cs;
       E* dst = GCOL ? nullptr : static_cast<E*>(S.stage) + ((size_t)(e & 1) * G + b) * m;
@@ -1555,6 +1567,10 @@ __device__ __forceinline__ void geqp3_df_body(const QrParams<typename A::T>& P, 
     if (wid == 0) {
       const unsigned long long* xw = S.xw + (size_t)(e & 1) * G;
       const unsigned long long want = ((e >> 1) & 1) ^ 1;
+      // a lower step of the launch revealed its rank: this step stops at
+      // the next exchange (the load overlaps the polls below)
+      int canc = 0;
+      if (S.success && lane == 0) canc = *((volatile int*)S.success) < S.job;
       constexpr int PB = 8;  // G <= 256
       unsigned long long w[PB];
       unsigned pending = 0;
@@ -1624,7 +1640,8 @@ __device__ __forceinline__ void geqp3_df_body(const QrParams<typename A::T>& P, 
         s_win = best;
         s_owner = own;
         s_stop = fl;
-        s_ok = ok ? 1 : 0;
+        s_ok = ok && best != XW_CANCEL ? 1 : 0;
+        s_cancel = canc;
       }
     }
     __syncthreads();
@@ -1632,6 +1649,7 @@ __device__ __forceinline__ void geqp3_df_body(const QrParams<typename A::T>& P, 
   };
   auto quad = [&](int& s, int (&q)[4]) { return live_quad(s_st, nloc, NCW, s, q); };
 
+  if (threadIdx.x == 0) s_cancel = 0;
   // ---- the CTA's columns into shared memory (GCOL: the workspace is filled);
   // initial norms, first pivot
   if (!GCOL)
@@ -2034,14 +2052,44 @@ __device__ __forceinline__ void geqp3_df_body(const QrParams<typename A::T>& P, 
   if (b == 0 && threadIdx.x == 0) {
     *P.k_out = kres;
     *X.nfac = nfac;
+    if (S.success && kres < S.nt) atomicMin(S.success, S.job);
   }
 }
 
+// one sketch of a shared-memory launch: its parameters and its CTAs
+// [off, off + G) of the grid
+template <class A>
+struct SmJob {
+  QrParams<typename A::T> P;
+  QrV2Extra X;
+  QrDf D;
+  QrSm S;
+  int G, off;
+};
+constexpr int kSmJobs = 8;  // sketches per launch
+template <class A>
+struct SmJobs {
+  SmJob<A> j[kSmJobs];
+  int n;
+};
+
+// the sketches of a launch (one, or several adaptive steps at once), each
+// factored by its own CTAs with its own exchange
 template <class A, int NT>
-__global__ void __launch_bounds__(NT, 1) geqp3_df_smem_kernel(QrParams<typename A::T> P, QrV2Extra X, QrDf D,
-                                                              QrSm S) {
+__global__ void __launch_bounds__(NT, 1) geqp3_df_smem_kernel(const SmJobs<A> J) {
   extern __shared__ unsigned char qr_dyn[];
-  geqp3_df_body<A, NT, false>(P, X, D, S, gridDim.x, blockIdx.x, nullptr, 0, 0, qr_dyn);
+  // the CTA's sketch, copied from the parameters to shared memory once
+  __shared__ __align__(16) unsigned char s_jb[sizeof(SmJob<A>)];
+  int q = 0;
+  while (q + 1 < J.n && (int)blockIdx.x >= J.j[q + 1].off) ++q;
+  {
+    const unsigned* src = reinterpret_cast<const unsigned*>(&J.j[q]);
+    unsigned* dst = reinterpret_cast<unsigned*>(s_jb);
+    for (int i = threadIdx.x; i < (int)(sizeof(SmJob<A>) / 4); i += NT) dst[i] = src[i];
+  }
+  __syncthreads();
+  const SmJob<A>& job = *reinterpret_cast<const SmJob<A>*>(s_jb);
+  geqp3_df_body<A, NT, false>(job.P, job.X, job.D, job.S, job.G, (int)blockIdx.x - job.off, nullptr, 0, 0, qr_dyn);
 }
 
 // one matrix of a batch: its parameters and its m x n float2 workspace
@@ -2611,6 +2659,303 @@ void geqp3_df_batch(lra_ctx* ctx, int64_t count, const DfBatchItem* items, int64
   LRA_CUDA(cudaStreamSynchronize(ctx->stream));
 }
 
+// ---- the shared-memory pivoted QR in phases ---------------------------------------
+// prepare (buffers; the sketch converted to the kernel's arithmetic, its
+// column norms), launch (one sketch, or several adaptive steps' sketches on
+// CTAs of their own), finish (the factors joined back, xLAQPS's swaps
+// replayed, the columns permuted), so that a launch can hold several steps.
+
+template <typename T>
+using SmA = typename std::conditional<sizeof(T) == 8, QrArithDf, QrArithF32>::type;
+constexpr int kSmNT = 512;  // warp 0 for the reflector, 15 column warps
+
+// dynamic shared memory of a CTA holding ncap columns of m rows: the pivot
+// column, the columns, four values, a stored element and a state byte per
+// column
+template <class A>
+size_t sm_smem(int64_t m, int64_t ncap) {
+  using E = typename A::E;
+  using V = typename A::V;
+  return (size_t)(m + ncap * m) * sizeof(E) + (size_t)ncap * (4 * sizeof(V) + sizeof(E) + 1);
+}
+
+template <class A>
+size_t sm_capacity(lra_ctx* ctx) {
+  raise_smem_limit(ctx, (const void*)geqp3_df_smem_kernel<A, kSmNT>);
+  cudaFuncAttributes fa;
+  LRA_CUDA(cudaFuncGetAttributes(&fa, geqp3_df_smem_kernel<A, kSmNT>));
+  return (size_t)fa.maxDynamicSharedSizeBytes;
+}
+
+template <class A>
+bool sm_resident(lra_ctx* ctx, size_t smem) {
+  int per = 0;
+  LRA_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, geqp3_df_smem_kernel<A, kSmNT>, kSmNT, smem));
+  return per >= 1;
+}
+
+// a sketch factored alone: every SM, at least one column per column warp
+static int sm_natural_ctas(lra_ctx* ctx, int64_t n) {
+  return (int)std::min<int64_t>(std::min(ctx->num_sms, 256),
+                                std::max<int64_t>(1, (n + kSmNT / 32 - 2) / (kSmNT / 32 - 1)));
+}
+
+// the fewest CTAs whose shared memory holds an m x n sketch (0: not one column)
+template <class A>
+int sm_min_ctas(size_t cap, int64_t m, int64_t n) {
+  using E = typename A::E;
+  using V = typename A::V;
+  const size_t fixed = (size_t)m * sizeof(E);
+  const size_t per = (size_t)m * sizeof(E) + 4 * sizeof(V) + sizeof(E) + 1;
+  if (cap < fixed + per) return 0;
+  const int64_t ncap = (int64_t)((cap - fixed) / per);
+  return (int)((n + ncap - 1) / ncap);
+}
+
+template <typename T>
+struct SmQr {
+  int64_t m = 0, n = 0, lda = 0;
+  T* A = nullptr;
+  int64_t* jpvt = nullptr;
+  int G = 0;
+  size_t smem = 0;
+  SmJob<SmA<T>> job;
+  int64_t* col_at = nullptr;
+  int64_t* pos = nullptr;
+  double* scale = nullptr;
+  unsigned gm = 1;
+};
+
+template <typename T>
+void sm_prepare(lra_ctx* ctx, SmQr<T>& q, int64_t m, int64_t n, T* A, int64_t lda, int64_t* jpvt, T* tau,
+                int64_t kmax, int64_t nb, double atol, double rtol, int G) {
+  using Ar = SmA<T>;
+  using E = typename Ar::E;
+  q.m = m;
+  q.n = n;
+  q.A = A;
+  q.lda = lda;
+  q.jpvt = jpvt;
+  q.G = G;
+  q.smem = sm_smem<Ar>(m, (n + G - 1) / G);
+  QrParams<T>& P = q.job.P;
+  P = QrParams<T>{};
+  P.m = m;
+  P.n = n;
+  P.lda = m;  // the converted sketch's leading dimension
+  P.A = A;
+  P.jpvt = jpvt;
+  P.tau = tau;
+  P.part_d = ctx->arena.alloc_n<double>(G);
+  P.bar = reinterpret_cast<GridBar*>(ctx->arena.alloc(sizeof(GridBar)));
+  P.kmax = std::min<int64_t>(kmax, std::min(m, n));
+  P.nb = std::max<int64_t>(1, std::min<int64_t>(nb, std::max<int64_t>(P.kmax, 1)));
+  P.atol = atol;
+  P.rtol = rtol;
+  P.pivot = 1;
+  P.k_out = ctx->arena.alloc_n<int64_t>(1);
+  P.seq_len = ctx->tuning.qr_seq_len;
+  LRA_CUDA(cudaMemsetAsync(P.bar, 0, sizeof(GridBar), ctx->stream));
+  LRA_CUDA(cudaMemsetAsync(P.k_out, 0, sizeof(int64_t), ctx->stream));
+  QrV2Extra& X = q.job.X;
+  X.piv = ctx->arena.alloc_n<int64_t>(std::max<int64_t>(P.kmax, 1));
+  X.nfac = ctx->arena.alloc_n<int64_t>(1);
+  X.part_k = ctx->arena.alloc_n<long long>(G);
+  X.beta = ctx->arena.alloc_n<double>(std::max<int64_t>(P.kmax, 1));
+  LRA_CUDA(cudaMemsetAsync(X.nfac, 0, sizeof(int64_t), ctx->stream));
+  q.col_at = ctx->arena.alloc_n<int64_t>(n);
+  q.pos = ctx->arena.alloc_n<int64_t>(n);
+  const unsigned gi = (unsigned)std::max<int64_t>(1, std::min<int64_t>((n + 255) / 256, ctx->num_sms * 4));
+  iota_kernel<<<gi, 256, 0, ctx->stream>>>(n, q.col_at, q.pos);
+  post_launch(ctx, "iota_kernel");
+  // the sketch at a power-of-two scale in the kernel's arithmetic
+  double* vn0 = ctx->arena.alloc_n<double>(n);
+  q.scale = ctx->arena.alloc_n<double>(1);
+  unsigned long long* mx = ctx->arena.alloc_n<unsigned long long>(1);
+  LRA_CUDA(cudaMemsetAsync(mx, 0, sizeof(unsigned long long), ctx->stream));
+  q.gm = (unsigned)std::max<int64_t>(1, std::min<int64_t>((m * n + 255) / 256, ctx->num_sms * 8));
+  const unsigned gs = (unsigned)std::max<int64_t>(1, std::min<int64_t>((n + 7) / 8, ctx->num_sms * 8));
+  QrDf& D = q.job.D;
+  D = QrDf{nullptr, nullptr, vn0, q.scale, nullptr};
+  if constexpr (sizeof(T) == 8) {
+    const double* Bd = reinterpret_cast<const double*>(A);
+    df_absmax_kernel<<<q.gm, 256, 0, ctx->stream>>>(m, n, Bd, lda, mx);
+    post_launch(ctx, "df_absmax_kernel");
+    df_scale_kernel<<<1, 1, 0, ctx->stream>>>(mx, q.scale);
+    post_launch(ctx, "df_scale_kernel");
+    D.Bh = ctx->arena.alloc_n<float>((size_t)m * n);
+    D.Bl = ctx->arena.alloc_n<float>((size_t)m * n);
+    df_split_kernel<<<gs, 256, 0, ctx->stream>>>(m, n, Bd, lda, q.scale, D.Bh, D.Bl, m, vn0);
+    post_launch(ctx, "df_split_kernel");
+  } else {
+    const float* Bf = reinterpret_cast<const float*>(A);
+    f32_absmax_kernel<<<q.gm, 256, 0, ctx->stream>>>(m, n, Bf, lda, mx);
+    post_launch(ctx, "f32_absmax_kernel");
+    df_scale_kernel<<<1, 1, 0, ctx->stream>>>(mx, q.scale);
+    post_launch(ctx, "df_scale_kernel");
+    D.Bh = ctx->arena.alloc_n<float>((size_t)m * n);
+    f32_split_kernel<<<gs, 256, 0, ctx->stream>>>(m, n, Bf, lda, q.scale, D.Bh, m, vn0);
+    post_launch(ctx, "f32_split_kernel");
+  }
+  QrSm& S = q.job.S;
+  S = QrSm{nullptr, nullptr, nullptr};
+  if (trace_on()) {
+    const int64_t km = std::max<int64_t>(P.kmax, 1);
+    D.stamps = ctx->arena.alloc_n<unsigned long long>((size_t)16 * km);
+    LRA_CUDA(cudaMemsetAsync(D.stamps, 0, (size_t)16 * km * 8, ctx->stream));
+    S.pubt = ctx->arena.alloc_n<unsigned long long>((size_t)G * km);
+    LRA_CUDA(cudaMemsetAsync(S.pubt, 0, (size_t)G * km * 8, ctx->stream));
+  }
+  S.xw = ctx->arena.alloc_n<unsigned long long>((size_t)2 * G);
+  S.stage = ctx->arena.alloc_n<E>((size_t)2 * G * m);
+  LRA_CUDA(cudaMemsetAsync(S.xw, 0, (size_t)2 * G * sizeof(unsigned long long), ctx->stream));
+  q.job.G = G;
+  q.job.off = 0;
+}
+
+// one cooperative launch for nq prepared sketches (CTAs laid out in order)
+template <typename T>
+void sm_launch(lra_ctx* ctx, SmQr<T>* const* qs, int nq) {
+  using Ar = SmA<T>;
+  SmJobs<Ar> J;
+  J.n = nq;
+  int off = 0;
+  size_t smem = 0;
+  for (int i = 0; i < nq; ++i) {
+    J.j[i] = qs[i]->job;
+    J.j[i].G = qs[i]->G;
+    J.j[i].off = off;
+    off += qs[i]->G;
+    smem = std::max(smem, qs[i]->smem);
+  }
+  void* args[] = {&J};
+  LRA_CUDA(cudaLaunchCooperativeKernel((const void*)geqp3_df_smem_kernel<Ar, kSmNT>, dim3(off), dim3(kSmNT), args,
+                                       smem, ctx->stream));
+  post_launch(ctx, sizeof(T) == 8 ? "geqp3_df_smem_kernel" : "geqp3_f32_smem_kernel");
+}
+
+// the factors back into the sketch: R and the reflectors, xLAQPS's column
+// swaps replayed into jpvt, the columns in pivot order
+template <typename T>
+void sm_finish(lra_ctx* ctx, SmQr<T>& q) {
+  const int64_t m = q.m, n = q.n;
+  const QrV2Extra& X = q.job.X;
+  const QrDf& D = q.job.D;
+  if (D.stamps)
+    print_qr_trace(ctx, D.stamps, q.job.P.kmax, m, n, sizeof(T) == 8 ? "geqp3_df_smem_kernel" : "geqp3_f32_smem_kernel",
+                   true, q.job.S.pubt, q.G);
+  int64_t* step_of = ctx->arena.alloc_n<int64_t>(n);
+  qr_step_of_kernel<<<1, 1024, 0, ctx->stream>>>(n, X.piv, X.nfac, step_of);
+  post_launch(ctx, "qr_step_of_kernel");
+  if constexpr (sizeof(T) == 8) {
+    df_join_kernel<<<q.gm, 256, 0, ctx->stream>>>(m, n, D.Bh, D.Bl, m, q.scale, reinterpret_cast<double*>(q.A), q.lda,
+                                                  step_of);
+    post_launch(ctx, "df_join_kernel");
+  } else {
+    f32_join_kernel<<<q.gm, 256, 0, ctx->stream>>>(m, n, D.Bh, m, q.scale, reinterpret_cast<float*>(q.A), q.lda,
+                                                   step_of);
+    post_launch(ctx, "f32_join_kernel");
+  }
+  if (n <= 24576) {
+    const size_t rs = (size_t)2 * n * sizeof(int);
+    raise_smem_limit(ctx, (const void*)geqp3_replay_smem_kernel);
+    geqp3_replay_smem_kernel<<<1, 1024, rs, ctx->stream>>>(n, X.piv, X.nfac, q.col_at);
+    post_launch(ctx, "geqp3_replay_smem_kernel");
+  } else {
+    geqp3_replay_kernel<<<1, 32, 0, ctx->stream>>>(n, X.piv, X.nfac, q.col_at, q.pos);
+    post_launch(ctx, "geqp3_replay_kernel");
+  }
+  const unsigned gi = (unsigned)std::max<int64_t>(1, std::min<int64_t>((n + 255) / 256, ctx->num_sms * 4));
+  jpvt_kernel<<<gi, 256, 0, ctx->stream>>>(n, q.col_at, q.jpvt);
+  post_launch(ctx, "jpvt_kernel");
+  T* tmp = ctx->arena.alloc_n<T>((size_t)m * n);
+  gather_cols(ctx, m, n, q.A, q.lda, q.jpvt, tmp, m);
+  copy_matrix(ctx, m, n, tmp, m, q.A, q.lda);
+}
+
+// the shared-memory kernel applies to an m x n sketch of this type (the
+// mixed path's double-float for Float64, FP32 for Float32)
+template <typename T>
+static bool sm_applies(lra_ctx* ctx, int64_t m, int64_t n) {
+  if (!qr_smem_enabled() || n >= (int64_t)XW_IDX || m <= 0 || n <= 0) return false;
+  if (sizeof(T) == 8 && !ctx->gemm_tc) return false;
+  // the rows a CTA stages per column (the single-step form's reflector bound)
+  const int64_t vcap = std::min<int64_t>(m, (int64_t)(160 * 1024 / sizeof(T)));
+  return m - 1 <= vcap;
+}
+
+template <typename T>
+int geqp3_steps_fit(lra_ctx* ctx, int count, const int64_t* m, int64_t n) {
+  using Ar = SmA<T>;
+  const size_t cap = sm_capacity<Ar>(ctx);
+  int total = 0, fit = 0;
+  for (int i = 0; i < count && i < kSmJobs; ++i) {
+    if (!sm_applies<T>(ctx, m[i], n)) break;
+    const int g = sm_min_ctas<Ar>(cap, m[i], n);
+    if (g <= 0 || g > sm_natural_ctas(ctx, n) || total + g > ctx->num_sms) break;
+    total += g;
+    fit = i + 1;
+  }
+  return fit;
+}
+
+template <typename T>
+int geqp3_adap_steps(lra_ctx* ctx, int count, const QrStep<T>* st, int64_t nb, double atol, double rtol,
+                     int64_t* k) {
+  using Ar = SmA<T>;
+  if (count < 1 || count > kSmJobs) fail(LRA_EINVAL, "geqp3_adap_steps: %d steps", count);
+  std::vector<int64_t> ms(count);
+  for (int i = 0; i < count; ++i) {
+    ms[i] = st[i].m;
+    if (st[i].n != st[0].n) fail(LRA_EINVAL, "geqp3_adap_steps: the steps' column counts differ");
+  }
+  if (geqp3_steps_fit<T>(ctx, count, ms.data(), st[0].n) < count) fail(LRA_EINVAL, "geqp3_adap_steps: no fit");
+  const ArenaMark mark = ctx->arena.mark();
+  const size_t cap = sm_capacity<Ar>(ctx);
+  // each step on the fewest CTAs that hold it; the rest to the last (the
+  // largest, with the most pivots)
+  std::vector<int> G(count);
+  int used = 0;
+  for (int i = 0; i < count; ++i) used += G[i] = sm_min_ctas<Ar>(cap, st[i].m, st[i].n);
+  G[count - 1] = std::min(sm_natural_ctas(ctx, st[count - 1].n), G[count - 1] + (ctx->num_sms - used));
+  int* success = ctx->arena.alloc_n<int>(1);
+  LRA_CUDA(cudaMemsetAsync(success, 0x7f, sizeof(int), ctx->stream));
+  std::vector<SmQr<T>> q(count);
+  std::vector<SmQr<T>*> qp(count);
+  size_t smem = 0;
+  for (int i = 0; i < count; ++i) {
+    sm_prepare<T>(ctx, q[i], st[i].m, st[i].n, st[i].A, st[i].lda, st[i].jpvt, st[i].tau, st[i].kmax, nb, atol,
+                  rtol, G[i]);
+    q[i].job.S.success = success;
+    q[i].job.S.job = i;
+    q[i].job.S.nt = st[i].nt;
+    qp[i] = &q[i];
+    smem = std::max(smem, q[i].smem);
+  }
+  if (smem > cap || !sm_resident<Ar>(ctx, smem)) fail(LRA_ECUDA, "geqp3_adap_steps: the launch cannot be resident");
+  sm_launch<T>(ctx, qp.data(), count);
+  std::vector<int64_t> kk(count);
+  std::vector<GridBar> hb(count);
+  int win = 0x7f7f7f7f;
+  for (int i = 0; i < count; ++i) {
+    LRA_CUDA(cudaMemcpyAsync(&kk[i], q[i].job.P.k_out, sizeof(int64_t), cudaMemcpyDeviceToHost, ctx->stream));
+    LRA_CUDA(cudaMemcpyAsync(&hb[i], q[i].job.P.bar, sizeof(GridBar), cudaMemcpyDeviceToHost, ctx->stream));
+  }
+  LRA_CUDA(cudaMemcpyAsync(&win, success, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+  LRA_CUDA(cudaStreamSynchronize(ctx->stream));
+  for (int i = 0; i < count; ++i)
+    if (hb[i].err != 0) {
+      ctx->arena.release(mark);
+      fail(LRA_ETIMEDOUT, "geqp3: a wait between CTAs timed out");
+    }
+  const int c = win >= 0 && win < count ? win : -1;
+  for (int i = 0; i < count; ++i) k[i] = (c >= 0 && i > c) ? -1 : kk[i];
+  if (c >= 0) sm_finish<T>(ctx, q[c]);
+  LRA_CUDA(cudaStreamSynchronize(ctx->stream));
+  ctx->arena.release(mark);
+  return c;
+}
+
 template <typename T>
 int64_t geqp3_adap(lra_ctx* ctx, int64_t m, int64_t n, T* A, int64_t lda, int64_t* jpvt, T* tau,
                    int64_t kmax, int64_t nb, double atol, double rtol, bool pivot) {
@@ -2670,6 +3015,28 @@ int64_t geqp3_adap(lra_ctx* ctx, int64_t m, int64_t n, T* A, int64_t lda, int64_
   const int64_t nslot = (n + nwarps - 1) / nwarps * (NT / 32);
   const size_t smem2 = dyn_smem + (size_t)nslot * (3 * sizeof(T) + 1);
   const bool v2 = (m - 1) <= vcap && smem2 <= 200 * 1024;
+  if (v2 && pivot && sm_applies<T>(ctx, m, n)) {
+    // the shared-memory kernels (Float32 in FP32, the mixed path's Float64 in
+    // double-float) when each CTA's share of the columns fits there
+    using Ar = SmA<T>;
+    const int G = sm_natural_ctas(ctx, n);
+    const size_t need = sm_smem<Ar>(m, (n + G - 1) / G);
+    if (need <= sm_capacity<Ar>(ctx) && sm_resident<Ar>(ctx, need)) {
+      SmQr<T> q;
+      sm_prepare<T>(ctx, q, m, n, A, lda, jpvt, tau, P.kmax, nb, atol, rtol, G);
+      SmQr<T>* qp = &q;
+      sm_launch<T>(ctx, &qp, 1);
+      sm_finish<T>(ctx, q);
+      int64_t k = 0;
+      GridBar hb;
+      LRA_CUDA(cudaMemcpyAsync(&k, q.job.P.k_out, sizeof(int64_t), cudaMemcpyDeviceToHost, ctx->stream));
+      LRA_CUDA(cudaMemcpyAsync(&hb, q.job.P.bar, sizeof(GridBar), cudaMemcpyDeviceToHost, ctx->stream));
+      LRA_CUDA(cudaStreamSynchronize(ctx->stream));
+      ctx->arena.release(mark);
+      if (hb.err != 0) fail(LRA_ETIMEDOUT, "geqp3: a wait between CTAs timed out");
+      return k;
+    }
+  }
   if (v2) {
     raise_smem_limit(ctx, (const void*)geqp3_v2_kernel<T, NT>);
     LRA_CUDA(cudaFuncSetAttribute(geqp3_v2_kernel<T, NT>, cudaFuncAttributePreferredSharedMemoryCarveout,
@@ -2689,72 +3056,7 @@ int64_t geqp3_adap(lra_ctx* ctx, int64_t m, int64_t n, T* A, int64_t lda, int64_
     post_launch(ctx, "iota_kernel");
     // the mixed-precision path factors Float64 sketches in double-float
     const bool dfq = sizeof(T) == 8 && ctx->gemm_tc && pivot;
-    // Float32 sketches stay in shared memory in FP32 when each CTA's share
-    // of the columns fits (the same kernel, QrArithF32)
-    constexpr int NTF = 512;
-    const int gsf = (int)std::min<int64_t>(std::min(ctx->num_sms, 256),
-                                           std::max<int64_t>(1, (n + NTF / 32 - 2) / (NTF / 32 - 1)));
-    const int64_t ncf = (n + gsf - 1) / gsf;
-    const size_t smem_f = (size_t)m * 4 + (size_t)ncf * m * 4 + (size_t)ncf * (4 * 4 + 4 + 1);
-    bool f32q = false;
-    if constexpr (sizeof(T) == 4) {
-      if (pivot && !dfq && n < (int64_t)XW_IDX && qr_smem_enabled()) {
-        raise_smem_limit(ctx, (const void*)geqp3_df_smem_kernel<QrArithF32, NTF>);
-        cudaFuncAttributes fa;
-        LRA_CUDA(cudaFuncGetAttributes(&fa, geqp3_df_smem_kernel<QrArithF32, NTF>));
-        f32q = smem_f <= (size_t)fa.maxDynamicSharedSizeBytes;
-        if (f32q) {
-          int per = 0;
-          LRA_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, geqp3_df_smem_kernel<QrArithF32, NTF>, NTF,
-                                                                 smem_f));
-          f32q = per >= 1;
-        }
-      }
-    }
-    if (f32q) {
-      if constexpr (sizeof(T) == 4) {
-        float* Bs = ctx->arena.alloc_n<float>((size_t)m * n);
-        double* vn0 = ctx->arena.alloc_n<double>(n);
-        double* scale = ctx->arena.alloc_n<double>(1);
-        unsigned long long* mx = ctx->arena.alloc_n<unsigned long long>(1);
-        LRA_CUDA(cudaMemsetAsync(mx, 0, sizeof(unsigned long long), ctx->stream));
-        const unsigned gm = (unsigned)std::max<int64_t>(1, std::min<int64_t>((m * n + 255) / 256, ctx->num_sms * 8));
-        f32_absmax_kernel<<<gm, 256, 0, ctx->stream>>>(m, n, A, lda, mx);
-        post_launch(ctx, "f32_absmax_kernel");
-        df_scale_kernel<<<1, 1, 0, ctx->stream>>>(mx, scale);
-        post_launch(ctx, "df_scale_kernel");
-        const unsigned gs = (unsigned)std::max<int64_t>(1, std::min<int64_t>((n + 7) / 8, ctx->num_sms * 8));
-        f32_split_kernel<<<gs, 256, 0, ctx->stream>>>(m, n, A, lda, scale, Bs, m, vn0);
-        post_launch(ctx, "f32_split_kernel");
-        QrDf D{Bs, nullptr, vn0, scale, nullptr};
-        if (trace_on()) {
-          D.stamps = ctx->arena.alloc_n<unsigned long long>((size_t)16 * std::max<int64_t>(P.kmax, 1));
-          LRA_CUDA(cudaMemsetAsync(D.stamps, 0, (size_t)16 * std::max<int64_t>(P.kmax, 1) * 8, ctx->stream));
-        }
-        QrParams<float> Pf = P;
-        Pf.lda = m;
-        Pf.part_d = ctx->arena.alloc_n<double>(gsf);
-        QrSm S;
-        S.pubt = nullptr;
-        if (D.stamps) {
-          S.pubt = ctx->arena.alloc_n<unsigned long long>((size_t)gsf * P.kmax);
-          LRA_CUDA(cudaMemsetAsync(S.pubt, 0, (size_t)gsf * P.kmax * 8, ctx->stream));
-        }
-        S.xw = ctx->arena.alloc_n<unsigned long long>((size_t)2 * gsf);
-        S.stage = ctx->arena.alloc_n<float>((size_t)2 * gsf * m);
-        LRA_CUDA(cudaMemsetAsync(S.xw, 0, (size_t)2 * gsf * sizeof(unsigned long long), ctx->stream));
-        void* args[] = {&Pf, &X, &D, &S};
-        LRA_CUDA(cudaLaunchCooperativeKernel((const void*)geqp3_df_smem_kernel<QrArithF32, NTF>, dim3(gsf), dim3(NTF),
-                                             args, smem_f, ctx->stream));
-        post_launch(ctx, "geqp3_f32_smem_kernel");
-        if (D.stamps) print_qr_trace(ctx, D.stamps, P.kmax, m, n, "geqp3_f32_smem_kernel", true, S.pubt, gsf);
-        int64_t* step_of = ctx->arena.alloc_n<int64_t>(n);
-        qr_step_of_kernel<<<1, 1024, 0, ctx->stream>>>(n, X.piv, X.nfac, step_of);
-        post_launch(ctx, "qr_step_of_kernel");
-        f32_join_kernel<<<gm, 256, 0, ctx->stream>>>(m, n, Bs, m, scale, A, lda, step_of);
-        post_launch(ctx, "f32_join_kernel");
-      }
-    } else if (dfq) {
+    if (dfq) {
       float* Bh = ctx->arena.alloc_n<float>((size_t)m * n);
       float* Bl = ctx->arena.alloc_n<float>((size_t)m * n);
       double* vn0 = ctx->arena.alloc_n<double>(n);
@@ -2778,42 +3080,10 @@ int64_t geqp3_adap(lra_ctx* ctx, int64_t m, int64_t n, T* A, int64_t lda, int64_
       QrParams<double> Pd;
       std::memcpy(&Pd, &P, sizeof(Pd));
       Pd.lda = m;
-      // the columns stay in shared memory when each CTA's share fits there
-      constexpr int NTS = 512;  // warp 0 for the reflector, 15 column warps
-      const int gsm = (int)std::min<int64_t>(std::min(ctx->num_sms, 256),
-                                             std::max<int64_t>(1, (n + NTS / 32 - 2) / (NTS / 32 - 1)));
-      const int64_t ncap = (n + gsm - 1) / gsm;
-      const size_t smem_s = (size_t)m * sizeof(float2) + (size_t)ncap * m * sizeof(float2) + (size_t)ncap * (5 * 8 + 1);
-      bool smq = n < (int64_t)XW_IDX && qr_smem_enabled();
-      if (smq) {
-        raise_smem_limit(ctx, (const void*)geqp3_df_smem_kernel<QrArithDf, NTS>);
-        cudaFuncAttributes fa;
-        LRA_CUDA(cudaFuncGetAttributes(&fa, geqp3_df_smem_kernel<QrArithDf, NTS>));
-        smq = smem_s <= (size_t)fa.maxDynamicSharedSizeBytes;
-        if (smq) {
-          int per = 0;
-          LRA_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, geqp3_df_smem_kernel<QrArithDf, NTS>, NTS, smem_s));
-          smq = per >= 1;
-        }
-      }
-      const char* kname = smq ? "geqp3_df_smem_kernel" : "geqp3_df_kernel";
-      unsigned long long* pubt = nullptr;
-      if (smq) {
-        Pd.part_d = ctx->arena.alloc_n<double>(gsm);
-        QrSm S;
-        S.pubt = nullptr;
-        if (D.stamps) {
-          S.pubt = ctx->arena.alloc_n<unsigned long long>((size_t)gsm * P.kmax);
-          LRA_CUDA(cudaMemsetAsync(S.pubt, 0, (size_t)gsm * P.kmax * 8, ctx->stream));
-          pubt = S.pubt;
-        }
-        S.xw = ctx->arena.alloc_n<unsigned long long>((size_t)2 * gsm);
-        S.stage = ctx->arena.alloc_n<float2>((size_t)2 * gsm * m);
-        LRA_CUDA(cudaMemsetAsync(S.xw, 0, (size_t)2 * gsm * sizeof(unsigned long long), ctx->stream));
-        void* args[] = {&Pd, &X, &D, &S};
-        LRA_CUDA(cudaLaunchCooperativeKernel((const void*)geqp3_df_smem_kernel<QrArithDf, NTS>, dim3(gsm), dim3(NTS), args,
-                                             smem_s, ctx->stream));
-      } else {
+      // the columns stay in global memory (a CTA's share does not fit shared
+      // memory)
+      const char* kname = "geqp3_df_kernel";
+      {
         raise_smem_limit(ctx, (const void*)geqp3_df_kernel<NT>);
         // as much L1 as the shared memory leaves: the warps' columns live there
         LRA_CUDA(cudaFuncSetAttribute(geqp3_df_kernel<NT>, cudaFuncAttributePreferredSharedMemoryCarveout,
@@ -2826,7 +3096,7 @@ int64_t geqp3_adap(lra_ctx* ctx, int64_t m, int64_t n, T* A, int64_t lda, int64_
                                              ctx->stream));
       }
       post_launch(ctx, kname);
-      if (D.stamps) print_qr_trace(ctx, D.stamps, P.kmax, m, n, kname, smq, pubt, gsm);
+      if (D.stamps) print_qr_trace(ctx, D.stamps, P.kmax, m, n, kname, false, nullptr, 1);
       int64_t* step_of = ctx->arena.alloc_n<int64_t>(n);
       qr_step_of_kernel<<<1, 1024, 0, ctx->stream>>>(n, X.piv, X.nfac, step_of);
       post_launch(ctx, "qr_step_of_kernel");
@@ -3099,7 +3369,9 @@ template int64_t geqp3_adap_noalloc<double>(lra_ctx*, int64_t, int64_t, double*,
   template void apply_q<T>(lra_ctx*, char, int64_t, int64_t, const T*, int64_t, const T*, T*,    \
                            int64_t, int64_t);                                                    \
   template void orgqr<T>(lra_ctx*, int64_t, int64_t, T*, int64_t, const T*);                      \
-  template void col_norms<T>(lra_ctx*, int64_t, int64_t, const T*, int64_t, T*);
+  template void col_norms<T>(lra_ctx*, int64_t, int64_t, const T*, int64_t, T*);                  \
+  template int geqp3_steps_fit<T>(lra_ctx*, int, const int64_t*, int64_t);                        \
+  template int geqp3_adap_steps<T>(lra_ctx*, int, const QrStep<T>*, int64_t, double, double, int64_t*);
 INST(float)
 INST(double)
 #undef INST

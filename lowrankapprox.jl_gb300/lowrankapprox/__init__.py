@@ -238,6 +238,11 @@ class Context:
     def launches(self) -> int:
         return int(_ffi.load().lra_ctx_launches(self.handle))
 
+    def kernel_launches(self, name: str) -> int:
+        """Launches of the kernel called `name` on this context so far
+        (lra_ctx_kernel_launches)."""
+        return int(_ffi.load().lra_ctx_kernel_launches(self.handle, name.encode()))
+
     def stage_ms(self):
         out = (C.c_double * 4)()
         _ffi.load().lra_ctx_stage_ms(self.handle, out)

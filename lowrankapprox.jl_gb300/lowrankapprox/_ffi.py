@@ -122,6 +122,7 @@ SIGNATURES = [
     ("lra_last_error", C.c_char_p, [_vp]),
     ("lra_status_string", C.c_char_p, [_i32]),
     ("lra_ctx_launches", _i64, [_vp]),
+    ("lra_ctx_kernel_launches", _i64, [_vp, C.c_char_p]),
     ("lra_ctx_stage_ms", _i32, [_vp, _P(_d)]),
     ("lra_ctx_set_tuning", _i32, [_vp, C.c_char_p, _i64, _i64]),
     ("lra_ctx_get_tuning", _i32, [_vp, C.c_char_p, _i64]),
