@@ -53,6 +53,8 @@ def parse():
     ap.add_argument("--no-tall", action="store_true", help="skip the tall Float32 idfact measurement")
     ap.add_argument("--srft-sweep", action="store_true",
                     help="only the SRFT sketch sweep on a Gaussian 65536x4096 Float32 matrix (one JSON line)")
+    ap.add_argument("--tall-only", action="store_true",
+                    help="only the tall Float32 idfact measurement (one JSON line)")
     return ap.parse_args()
 
 
@@ -90,6 +92,25 @@ def psvd_flops(m, n, k_id, k, orders, ks):
 
 
 QR_KERNELS = ("geqp3_df_smem_kernel", "geqp3_f32_smem_kernel", "geqp3_df_kernel", "geqp3_v2_kernel")
+
+
+def tuning_record(ctx) -> dict:
+    """The shape table the library runs with (lra_ctx_get_tuning): its
+    source and every entry, for the bench line."""
+    t = {"source": None, "tc_tile_n": {"f32": [0] * 16, "f64": [0] * 16}, "srft_wide": [0] * 11}
+    for line in ctx.tuning().splitlines():
+        w = line.split()
+        if not w:
+            continue
+        if w[0] == "#" and len(w) > 2 and w[1] == "source:":
+            t["source"] = " ".join(w[2:]).split("/")[-1]
+        elif w[0] == "tc_tile_n" and len(w) == 4:
+            t["tc_tile_n"][w[1]][int(w[2])] = int(w[3])
+        elif w[0] == "srft_wide" and len(w) == 3:
+            t["srft_wide"][int(w[1])] = int(w[2])
+        elif len(w) == 2 and w[0] in ("qr_seq_len", "qr_steps"):
+            t[w[0]] = int(w[1])
+    return t
 
 
 def sketch_orders(k, nb=32):
@@ -207,6 +228,7 @@ def measure_tall(lra, ctx, A, peaks, reps: int = 3):
         torch.cuda.synchronize()
         stages = {"sketch": 0.0, "qr": 0.0, "solve": 0.0, "post": 0.0}
         t = 0.0
+        q0 = sum(ctx.kernel_launches(kn) for kn in QR_KERNELS)
         for _ in range(reps):
             t0 = time.perf_counter()
             V = lra.idfact(A, o, ctx=ctx)
@@ -219,8 +241,9 @@ def measure_tall(lra, ctx, A, peaks, reps: int = 3):
         sketch_ms = stages["sketch"]
         a, b = o.sketchfact_srft_samp if sk == "srft" else o.sketchfact_randn_samp
         orders = [a * (o.nb << j) + b for j in range(V.nsteps)]
+        qr_launches = (sum(ctx.kernel_launches(kn) for kn in QR_KERNELS) - q0) / reps
         r = {"ms_per_call": 1e3 * t, "matrices_s": 1.0 / t, "rank": V.k, "steps": V.nsteps, "orders": orders,
-             "sketch_ms": sketch_ms, "stage_ms": stages,
+             "sketch_ms": sketch_ms, "stage_ms": stages, "qr_launches_per_call": qr_launches,
              "rel_spectral_err": lra.snormdiff(A, V, ctx=ctx) / nrm}
         if sk == "srft":
             gbs = len(orders) * m * n * 4 / (sketch_ms * 1e-3) / 1e9
@@ -435,6 +458,11 @@ def main():
         G = torch.randn((4096, 65536), dtype=torch.float32, device="cuda").t()
         print(json.dumps({"srft_sweep": measure_srft_sweep(lra, ctx, G, load_peaks())}), flush=True)
         return
+    if args.tall_only:
+        At = tall_f32_matrix()
+        print(json.dumps({"tall_f32": measure_tall(lra, ctx, At, load_peaks(), reps=max(1, args.steps))}),
+              flush=True)
+        return
     n = args.n
     A = make_matrix(n)
     torch.cuda.synchronize()
@@ -644,6 +672,7 @@ def main():
                     "d2h_bytes_per_step": d2h},
             "fp64_path": fp64, "serving": serving, "batched": batched, "tall_f32": tall,
             "roofline": roof, "roofline_sketch": roof_sketch, "cpu_baseline": cpu, "oracle_parity": parity,
+            "tuning": tuning_record(ctx),
             "clocks": clk, "gpu_launches": launches,
         }
         print(json.dumps(line), flush=True)
