@@ -124,16 +124,17 @@ def sketch_orders(k, nb=32):
         nt *= 2
 
 
-def serving_workload(count: int, seed: int = 5):
-    """Requests shaped like the serving config, scaled to a bounded sample:
-    70 % idfact / 30 % psvdfact, m and n log-uniform in [256, 4096], F32 / F64
-    half and half, s_i = 10^(-(i-1)/r) with r ~ U[20, 200], rtol 1e-6 (F32)
-    and 1e-10 (F64).  A = (G1 diag(s)) G2' from Gaussian G1, G2 on the GPU."""
+def serving_workload(count: int, seed: int = 5, hi: int = 16384):
+    """Requests shaped like the serving config, a bounded sample of it:
+    70 % idfact / 30 % psvdfact, m and n log-uniform in [256, hi] (16384 in
+    the config), F32 / F64 half and half, s_i = 10^(-(i-1)/r) with
+    r ~ U[20, 200], rtol 1e-6 (F32) and 1e-10 (F64).  A = (G1 diag(s)) G2'
+    from Gaussian G1, G2 on the GPU."""
     import torch
     rng = np.random.default_rng(seed)
     out = []
     for i in range(count):
-        m, n = (int(round(np.exp(rng.uniform(np.log(256), np.log(4096))))) for _ in range(2))
+        m, n = (int(round(np.exp(rng.uniform(np.log(256), np.log(hi))))) for _ in range(2))
         dt = torch.float64 if rng.random() < 0.5 else torch.float32
         kind = "idfact" if rng.random() < 0.7 else "psvdfact"
         r = rng.uniform(20, 200)

@@ -561,7 +561,9 @@ int64_t predict_rank(lra_ctx* ctx, const Fact<T>& F, int64_t kmax, const lra_opt
 }
 
 // Steps step, step + 1, ... of sketchfact_dev's loop (thresholds nt, 2 nt,
-// ...) up to the first whose threshold exceeds 1.3 times the predicted rank,
+// ...) up to the first whose threshold exceeds twice the predicted rank (a
+// step that reveals the rank stops the ones after it, so a wide margin
+// costs their sketches only),
 // as many as one shared-memory launch holds, sketched in order and factored
 // together.  Returns the number of steps taken when one of them revealed
 // its rank (F is then that step's factorization and the random streams stand
@@ -572,7 +574,7 @@ template <typename T>
 int sketchfact_steps(lra_ctx* ctx, const lra_opts& o, char trans, int64_t M, int64_t N, const T* A, int64_t lda,
                      RandSrc& rs, int dtype, TcSplit* split, int step, int64_t nt, int64_t rank_hint,
                      const ArenaMark& base, Fact<T>& F) {
-  const int64_t limit = rank_hint > (int64_t)1 << 40 ? (int64_t)1 << 40 : rank_hint + (rank_hint * 3) / 10;
+  const int64_t limit = rank_hint > (int64_t)1 << 40 ? (int64_t)1 << 40 : 2 * rank_hint + 64;
   std::vector<int64_t> orders, nts, ms;
   int64_t t = nt;
   for (int i = 0; i < ctx->tuning.qr_steps && i < 8; ++i) {
@@ -698,10 +700,11 @@ Fact<T> sketchfact_dev(lra_ctx* ctx, const lra_opts& o, char trans, int64_t M, i
                                            step, nt, rank_hint, base, F);
       if (done > 0) break;
       if (done < 0) {
-        // every step of the launch reached its threshold
+        // every step of the launch reached its threshold: the rank is at
+        // least the last one's, and the next launch takes the steps after
         step += -done - 1;
         for (int i = 0; i < -done; ++i) nt *= 2;
-        rank_hint = -1;
+        rank_hint = nt;
         continue;
       }
     }

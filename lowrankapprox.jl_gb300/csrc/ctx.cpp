@@ -154,6 +154,8 @@ bool trace_on() {
 //   qr_seq_len <rows>
 //   srft_wide <log2 l'> <0|1>
 //   qr_steps <1..8>
+//   qr_sms <SMs a pivoted-QR launch may take; 0: all>
+//   tc_split <most K parts of the tensor-core sketch; 0: as many as fill the SMs>
 // lowrankapprox/autotune.py writes it from its sweeps; unknown keys and
 // out-of-range values are ignored, so an old table never breaks a newer
 // library.
@@ -164,6 +166,8 @@ static void tuning_defaults(lra_tuning* t) {
   t->qr_seq_len = 96;
   for (int lb = 0; lb <= 10; ++lb) t->srft_wide[lb] = (lb >= 7 && lb <= 10) ? 1 : 0;
   t->qr_steps = 8;
+  t->qr_sms = 0;
+  t->tc_split = 0;
 }
 
 bool set_tuning(lra_tuning* t, const char* key, int64_t index, int64_t value) {
@@ -185,6 +189,16 @@ bool set_tuning(lra_tuning* t, const char* key, int64_t index, int64_t value) {
   if (!std::strcmp(key, "qr_steps")) {
     if (value < 1 || value > 8) return false;
     t->qr_steps = (int)value;
+    return true;
+  }
+  if (!std::strcmp(key, "qr_sms")) {
+    if (value < 0 || value > 4096) return false;
+    t->qr_sms = (int)value;
+    return true;
+  }
+  if (!std::strcmp(key, "tc_split")) {
+    if (value < 0 || value > 4096) return false;
+    t->tc_split = (int)value;
     return true;
   }
   return false;
@@ -225,9 +239,9 @@ void load_tuning(lra_tuning* t, std::string* source) {
     } else if (key == "srft_wide") {
       int64_t lb = -1, v = 0;
       if (in >> lb >> v) used += set_tuning(t, "srft_wide", lb, v);
-    } else if (key == "qr_steps") {
+    } else if (key == "qr_steps" || key == "qr_sms" || key == "tc_split") {
       int64_t v = 0;
-      if (in >> v) used += set_tuning(t, "qr_steps", 0, v);
+      if (in >> v) used += set_tuning(t, key.c_str(), 0, v);
     }
   }
   *source = path + " (" + std::to_string(used) + " entries)";
@@ -240,6 +254,8 @@ std::string tuning_text(const lra_tuning& t) {
   o << "qr_seq_len " << t.qr_seq_len << '\n';
   for (int lb = 0; lb <= 10; ++lb) o << "srft_wide " << lb << ' ' << t.srft_wide[lb] << '\n';
   o << "qr_steps " << t.qr_steps << '\n';
+  o << "qr_sms " << t.qr_sms << '\n';
+  o << "tc_split " << t.tc_split << '\n';
   return o.str();
 }
 

@@ -77,6 +77,12 @@ struct lra_tuning {
   // adaptive sketch steps the shared-memory pivoted QR may factor in one
   // launch (1: one step at a time)
   int qr_steps;
+  // SMs a pivoted-QR launch may take (0: all); more when the sketch needs
+  // them to fit shared memory.  The serving loop shares the device this way
+  int qr_sms;
+  // most parts the tensor-core sketch splits K into when its tiles are too
+  // few for the SMs (0: as many as fill them, 1: no split)
+  int tc_split;
 };
 
 struct lra_ctx {

@@ -2694,9 +2694,17 @@ bool sm_resident(lra_ctx* ctx, size_t smem) {
   return per >= 1;
 }
 
-// a sketch factored alone: every SM, at least one column per column warp
+// the SMs a pivoted-QR launch of this context may take (the tuning's
+// qr_sms cap, else all)
+static int qr_sm_cap(const lra_ctx* ctx) {
+  const int c = ctx->tuning.qr_sms;
+  return c > 0 ? std::min(c, ctx->num_sms) : ctx->num_sms;
+}
+
+// a sketch factored alone: every SM it may take, at least one column per
+// column warp
 static int sm_natural_ctas(lra_ctx* ctx, int64_t n) {
-  return (int)std::min<int64_t>(std::min(ctx->num_sms, 256),
+  return (int)std::min<int64_t>(std::min(qr_sm_cap(ctx), 256),
                                 std::max<int64_t>(1, (n + kSmNT / 32 - 2) / (kSmNT / 32 - 1)));
 }
 
@@ -2892,7 +2900,7 @@ int geqp3_steps_fit(lra_ctx* ctx, int count, const int64_t* m, int64_t n) {
   for (int i = 0; i < count && i < kSmJobs; ++i) {
     if (!sm_applies<T>(ctx, m[i], n)) break;
     const int g = sm_min_ctas<Ar>(cap, m[i], n);
-    if (g <= 0 || g > sm_natural_ctas(ctx, n) || total + g > ctx->num_sms) break;
+    if (g <= 0 || g > sm_natural_ctas(ctx, n) || total + g > qr_sm_cap(ctx)) break;
     total += g;
     fit = i + 1;
   }
@@ -2917,7 +2925,7 @@ int geqp3_adap_steps(lra_ctx* ctx, int count, const QrStep<T>* st, int64_t nb, d
   std::vector<int> G(count);
   int used = 0;
   for (int i = 0; i < count; ++i) used += G[i] = sm_min_ctas<Ar>(cap, st[i].m, st[i].n);
-  G[count - 1] = std::min(sm_natural_ctas(ctx, st[count - 1].n), G[count - 1] + (ctx->num_sms - used));
+  G[count - 1] = std::min(sm_natural_ctas(ctx, st[count - 1].n), G[count - 1] + (qr_sm_cap(ctx) - used));
   int* success = ctx->arena.alloc_n<int>(1);
   LRA_CUDA(cudaMemsetAsync(success, 0x7f, sizeof(int), ctx->stream));
   std::vector<SmQr<T>> q(count);
@@ -2970,7 +2978,7 @@ int64_t geqp3_adap(lra_ctx* ctx, int64_t m, int64_t n, T* A, int64_t lda, int64_
   LRA_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, geqp3_kernel<T, NT>, NT, dyn_smem));
   if (per_sm < 1) fail(LRA_ECUDA, "geqp3 kernel cannot be resident");
   const int64_t want = (n + (NT / 32) - 1) / (NT / 32);
-  int grid = (int)std::min<int64_t>((int64_t)ctx->num_sms * std::min(per_sm, 1), want);
+  int grid = (int)std::min<int64_t>((int64_t)qr_sm_cap(ctx) * std::min(per_sm, 1), want);
   grid = std::max(grid, 1);
 
   QrParams<T> P;
@@ -3019,7 +3027,10 @@ int64_t geqp3_adap(lra_ctx* ctx, int64_t m, int64_t n, T* A, int64_t lda, int64_
     // the shared-memory kernels (Float32 in FP32, the mixed path's Float64 in
     // double-float) when each CTA's share of the columns fits there
     using Ar = SmA<T>;
-    const int G = sm_natural_ctas(ctx, n);
+    // the CTAs it may take, or the fewest that hold the sketch when those
+    // are more
+    const int G = std::min(std::max(sm_natural_ctas(ctx, n), sm_min_ctas<Ar>(sm_capacity<Ar>(ctx), m, n)),
+                           std::min(ctx->num_sms, 256));
     const size_t need = sm_smem<Ar>(m, (n + G - 1) / G);
     if (need <= sm_capacity<Ar>(ctx) && sm_resident<Ar>(ctx, need)) {
       SmQr<T> q;

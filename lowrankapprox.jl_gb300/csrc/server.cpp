@@ -97,9 +97,14 @@ struct lra_server {
       queue.pop_front();
       in_use += q->est;
       ++running;
+      // the pivoted QR's launches take this request's share of the SMs, so
+      // that the requests in flight factor side by side (a column's
+      // arithmetic does not depend on the CTA count: the same bits)
+      const int share = std::max(16, ctx->num_sms / (int)std::max<int64_t>(running, 1));
       q->slot = slot;
       q->t_start = Clock::now();
       lk.unlock();
+      ctx->tuning.qr_sms = share;
       ctx->rng_counter = 0;  // each request starts its own stream of draws
       const lra_request& r = q->r;
       int st;

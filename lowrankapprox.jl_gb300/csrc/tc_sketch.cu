@@ -48,7 +48,7 @@ constexpr int TILE_M = 128;   // columns of op(A) per CTA
 // sketch order by the tuning table; five accumulators of TN columns fit TMEM
 constexpr int KBLK = 64;      // K per stage (128 bytes of BF16: one SW128 row)
 constexpr int CHUNK_KB = 8;   // K-blocks per exact chunk (512)
-constexpr int NSTAGE = 2;
+constexpr int MAX_NSTAGE = 4;  // ring stages, as many as shared memory holds (at least 2)
 constexpr int TILE_BYTES = TILE_M * KBLK * 2;  // 16 KB (one slice tile)
 constexpr int NTHREADS = 320;
 constexpr int MAX_SLICES = 6;
@@ -73,6 +73,13 @@ struct TcParams {
   int64_t ldb;
   int out_double;
   int* err;
+  // split over K: blockIdx.y takes kc_per 512-long chunks, and the CTAs add
+  // their exact partial sums X into W (Lp x ncols int64, zeroed) instead of
+  // writing B; null for one split
+  int kc_per;
+  long long* W;
+  int64_t ldw;
+  int nstage;  // TMA ring stages (2..MAX_NSTAGE)
 };
 
 // ---- PTX helpers -------------------------------------------------------------
@@ -210,6 +217,7 @@ __global__ void __launch_bounds__(NTHREADS, 1)
   const int ns = P.ns;
   const int stage_bytes = S_BYTES + ns * TILE_BYTES;
   unsigned char* stages = base;
+  const int NSTAGE = P.nstage;
   uint64_t* full = reinterpret_cast<uint64_t*>(base + NSTAGE * stage_bytes);
   uint64_t* empty = full + NSTAGE;
   uint64_t* acc_ready = empty + NSTAGE;
@@ -220,7 +228,11 @@ __global__ void __launch_bounds__(NTHREADS, 1)
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int64_t ntl = (P.L + TILE_N - 1) / TILE_N;
   const int64_t n_tile = blockIdx.x / ntl, l_tile = blockIdx.x % ntl;
-  const int nkb = (int)((P.K + KBLK - 1) / KBLK);
+  // this CTA's K blocks [kb0, kb0 + nkb): whole 512-long chunks, so that
+  // every chunk is rounded as without the split
+  const int nkb_all = (int)((P.K + KBLK - 1) / KBLK);
+  const int kb0 = (int)blockIdx.y * P.kc_per * CHUNK_KB;
+  const int nkb = min(nkb_all - kb0, P.kc_per * CHUNK_KB);
   const int nchunks = (nkb + CHUNK_KB - 1) / CHUNK_KB;
   const int n_exact = ns < MAX_EXACT ? ns : MAX_EXACT;
   const bool has_tail = ns > MAX_EXACT;
@@ -259,9 +271,9 @@ __global__ void __launch_bounds__(NTHREADS, 1)
         ++issued;
         unsigned char* st = stages + s * stage_bytes;
         mbar_expect_tx(full + s, (uint32_t)stage_bytes);
-        tma_load_2d(st, &tmS, kb * KBLK, (int)(l_tile * TILE_N), full + s);
+        tma_load_2d(st, &tmS, (kb0 + kb) * KBLK, (int)(l_tile * TILE_N), full + s);
         for (int q = 0; q < ns; ++q)
-          tma_load_3d(st + S_BYTES + q * TILE_BYTES, &tmA, kb * KBLK, (int)(n_tile * TILE_M), q, full + s);
+          tma_load_3d(st + S_BYTES + q * TILE_BYTES, &tmA, (kb0 + kb) * KBLK, (int)(n_tile * TILE_M), q, full + s);
       }
       // no copy may still be landing in shared memory when the CTA exits
       int dummy = 0;
@@ -353,7 +365,16 @@ __global__ void __launch_bounds__(NTHREADS, 1)
     const int e = (ok && j < P.ncols) ? P.colexp[j] : 0;
     const int sc = e - 5 - 8 * n_exact - t;  // B = 2^(e - 5 - 8E - t) X
     const int64_t r0 = l_tile * TILE_N + half * COLS;
-    if (ok && j < P.ncols) {
+    if (ok && j < P.ncols && P.W) {
+      // a part of K: the exact partial sums, added as integers (any order
+      // gives the same total)
+#pragma unroll
+      for (int c = 0; c < COLS; ++c) {
+        const int64_t row = r0 + c;
+        if (row < P.L)
+          atomicAdd(reinterpret_cast<unsigned long long*>(P.W + row + j * P.ldw), (unsigned long long)X[c]);
+      }
+    } else if (ok && j < P.ncols) {
 #pragma unroll
       for (int c = 0; c < COLS; ++c) {
         const int64_t row = r0 + c;
@@ -373,6 +394,24 @@ __global__ void __launch_bounds__(NTHREADS, 1)
   if (warp == 1) {
     tc_fence_after();
     asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(TMEM_COLS) : "memory");
+  }
+}
+
+// the split-K sketch's sums W (exact int64) scaled into B, as the unsplit
+// kernel's epilogue does
+__global__ void tc_sketch_finish_kernel(int64_t L, int64_t ncols, const long long* __restrict__ W, int64_t ldw,
+                                        const int* __restrict__ colexp, int n_exact, int t, void* B, int64_t ldb,
+                                        int out_double) {
+  const int64_t total = L * ncols;
+  for (int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; q < total; q += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t row = q % L, j = q / L;
+    const int e = colexp[j];
+    const double v = e >= kNonFinite ? __longlong_as_double(0x7FF8000000000000ll)
+                                     : ldexp((double)W[row + j * ldw], e - 5 - 8 * n_exact - t);
+    if (out_double)
+      static_cast<double*>(B)[row + j * ldb] = v;
+    else
+      static_cast<float*>(B)[row + j * ldb] = (float)v;
   }
 }
 
@@ -903,11 +942,32 @@ void tc_sketch(lra_ctx* ctx, const TcSplit& sp, int64_t order, const T* S, T* B,
   P.ldb = ldb;
   P.out_double = sizeof(T) == 8 ? 1 : 0;
   P.err = err;
-  const size_t smem = 1024 + (size_t)NSTAGE * ((size_t)TILE_N * KBLK * 2 + ns * TILE_BYTES) + 256;
+  // as many ring stages as the shared memory holds
+  const size_t stage_bytes = (size_t)TILE_N * KBLK * 2 + (size_t)ns * TILE_BYTES;
+  int smem_optin = 0;
+  LRA_CUDA(cudaDeviceGetAttribute(&smem_optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, ctx->device));
+  P.nstage = (int)std::max<size_t>(2, std::min<size_t>(MAX_NSTAGE, ((size_t)smem_optin - 1024 - 256) / stage_bytes));
+  const size_t smem = 1024 + (size_t)P.nstage * stage_bytes + 256;
   const int64_t ntiles = ((N + TILE_M - 1) / TILE_M) * (Lp / TILE_N);
+  // too few tiles for two CTAs per SM: split K over more CTAs (whole
+  // chunks each, at least two), their exact sums added as integers
+  const int nkb = (int)((K + KBLK - 1) / KBLK);
+  const int nchunks = (nkb + CHUNK_KB - 1) / CHUNK_KB;
+  int nsplit = 1;
+  if (ntiles < 2 * (int64_t)ctx->num_sms && nchunks >= 4)
+    nsplit = (int)std::min<int64_t>((2 * (int64_t)ctx->num_sms + ntiles - 1) / ntiles, nchunks / 2);
+  if (ctx->tuning.tc_split > 0) nsplit = std::min(nsplit, ctx->tuning.tc_split);
+  P.kc_per = (nchunks + nsplit - 1) / nsplit;
+  nsplit = (nchunks + P.kc_per - 1) / P.kc_per;
+  P.W = nullptr;
+  P.ldw = Lp;
+  if (nsplit > 1) {
+    P.W = ctx->arena.alloc_n<long long>((size_t)Lp * N);
+    LRA_CUDA(cudaMemsetAsync(P.W, 0, (size_t)Lp * N * sizeof(long long), ctx->stream));
+  }
   auto launch = [&](auto kern) {
     raise_smem_limit(ctx, (const void*)kern);
-    kern<<<(unsigned)ntiles, NTHREADS, smem, ctx->stream>>>(tmA, tmS, P);
+    kern<<<dim3((unsigned)ntiles, (unsigned)nsplit), NTHREADS, smem, ctx->stream>>>(tmA, tmS, P);
   };
   if (TILE_N == 32)
     launch(tc_sketch_kernel<32>);
@@ -916,6 +976,14 @@ void tc_sketch(lra_ctx* ctx, const TcSplit& sp, int64_t order, const T* S, T* B,
   else
     launch(tc_sketch_kernel<96>);
   post_launch(ctx, "tc_sketch_kernel");
+  if (nsplit > 1) {
+    const int n_exact = ns < MAX_EXACT ? ns : MAX_EXACT;
+    const int t = ns > MAX_EXACT ? P.tshift : 0;
+    const unsigned g = (unsigned)std::max<int64_t>(1, std::min<int64_t>((order * N + 255) / 256, ctx->num_sms * 8));
+    tc_sketch_finish_kernel<<<g, 256, 0, ctx->stream>>>(order, N, P.W, Lp, sp.colexp, n_exact, t, B, ldb,
+                                                         P.out_double);
+    post_launch(ctx, "tc_sketch_finish_kernel");
+  }
   // a caller that passes err_slot checks it later (the batch, once per
   // round) and releases the transposed sketch with its own arena mark: the
   // batch issues sketches on several streams, so this memory may not be

@@ -61,3 +61,27 @@ def test_qr_seq_len_changes_only_rounding(lra):
         # T = R11 \ R12 carries cond(R11) ~ 1 / rtol: compare what it reconstructs
         assert reconstruction_gap(A, V.sk, V.rd, V.T, res[0].rd, res[0].T) <= 1e-12
     ctx.close()
+
+
+@pytest.mark.parametrize("dt", [np.float32, np.float64])
+@pytest.mark.parametrize("shape", [(3000, 700, 40), (20000, 300, 136), (9000, 1200, 264)])
+def test_k_split_gives_the_same_bits(lra, dt, shape):
+    """The tensor-core sketch split over K (a few column tiles, many rows):
+    whole 512-long chunks per part and the parts' exact integer sums added,
+    so the split gives the bits of the unsplit kernel."""
+    m, n, order = shape
+    rng = np.random.default_rng(m + n)
+    A = np.asfortranarray(rng.standard_normal((m, n)).astype(dt))
+    A[:, 5] *= 1e-30                       # a column far below the others
+    g = lra.lattice_gauss(17, order * m + 8)
+    o = lra.LRAOptions(dt, precision="mixed", rtol=1e-10 if dt == np.float64 else 1e-6)
+    outs = []
+    for split in (1, 0, 2):
+        ctx = lra.Context(0)
+        ctx.set_tuning("tc_split", 0, split)
+        outs.append(lra.sketch("left", "n", A, order, o, rand=lra.RandStream(gauss=g), ctx=ctx))
+        ctx.close()
+    assert np.array_equal(outs[0], outs[1]) and np.array_equal(outs[0], outs[2])
+    R = g[:order * m].reshape((order, m), order="F") @ A.astype(np.float64)
+    scale = np.abs(R).max(axis=0) + 1e-300
+    assert (np.abs(outs[0] - R) / scale).max() <= (1e-12 if dt == np.float64 else 1e-5)
