@@ -44,7 +44,7 @@ def parse():
     ap.add_argument("--rtol", type=float, default=1e-10)
     ap.add_argument("--no-fp64-leg", action="store_true")
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--serve-requests", type=int, default=64,
+    ap.add_argument("--serve-requests", type=int, default=200,
                     help="requests per precision in the serving measurement (0: skip)")
     ap.add_argument("--batch", type=int, default=2048,
                     help="kernel matrices in the batched measurement (0: skip)")
@@ -129,7 +129,8 @@ def serving_workload(count: int, seed: int = 5, hi: int = 16384):
     70 % idfact / 30 % psvdfact, m and n log-uniform in [256, hi] (16384 in
     the config), F32 / F64 half and half, s_i = 10^(-(i-1)/r) with
     r ~ U[20, 200], rtol 1e-6 (F32) and 1e-10 (F64).  A = (G1 diag(s)) G2'
-    from Gaussian G1, G2 on the GPU."""
+    from Gaussian G1, G2 on the GPU, over the first min(m, n, 16 r + 64)
+    singular values (the rest lie below 1e-16 of the first)."""
     import torch
     rng = np.random.default_rng(seed)
     out = []
@@ -138,7 +139,8 @@ def serving_workload(count: int, seed: int = 5, hi: int = 16384):
         dt = torch.float64 if rng.random() < 0.5 else torch.float32
         kind = "idfact" if rng.random() < 0.7 else "psvdfact"
         r = rng.uniform(20, 200)
-        k = min(m, n)
+        # singular values past 16 r are below 1e-16 of the first: left out
+        k = min(m, n, int(16 * r) + 64)
         g = torch.Generator(device="cuda").manual_seed(int(rng.integers(1 << 31)))
         G1 = torch.randn(m, k, generator=g, device="cuda", dtype=torch.float64) / np.sqrt(m)
         G2 = torch.randn(n, k, generator=g, device="cuda", dtype=torch.float64) / np.sqrt(n)
@@ -627,9 +629,11 @@ def main():
             work = serving_workload(args.serve_requests)
             serving = {"mixed": measure_serving(lra, work, "mixed"),
                        "native": measure_serving(lra, work, "native"),
-                       "sample": f"{args.serve_requests} requests: 70% idfact / 30% psvdfact, m, n log-uniform "
-                                 "[256, 4096], F32/F64 half each, rtol 1e-6 / 1e-10, Poisson arrivals at 80% "
+                       "sample": f"{args.serve_requests} requests of the serving config's distribution: 70% "
+                                 "idfact / 30% psvdfact, m, n log-uniform [256, 16384], F32/F64 half each, "
+                                 "s_i = 10^(-i/r), r ~ U[20, 200], rtol 1e-6 / 1e-10, Poisson arrivals at 80% "
                                  "of the burst rate, 8 slots, 150 GB budget"}
+            serving["mixed_vs_native"] = serving["mixed"]["matrices_s"] / serving["native"]["matrices_s"]
             del work
         except Exception as e:  # pragma: no cover
             serving = {"failed": str(e)}

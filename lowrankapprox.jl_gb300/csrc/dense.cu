@@ -840,13 +840,16 @@ void jacobi_svd(lra_ctx* ctx, int64_t n, T* X, int64_t ldx, T* V, int64_t ldv, T
   set_identity(ctx, n, n, V, ldv);
   const ArenaMark mk = ctx->arena.mark();
   // FP32: 8-column blocks (16-column blocks halve the grid barriers but
-  // measured slower: the local sweeps become issue-bound on half the SMs)
-  const int jbt = 8;
+  // measured slower: the local sweeps become issue-bound on half the SMs);
+  // 4-column blocks for the longer columns whose 8-column block pair does
+  // not fit shared memory (up to about 3500 rows); a warp per pair beyond
+  const size_t blk_cap = 220 * 1024;
+  const int jbt = (size_t)4 * 8 * n * sizeof(float) <= blk_cap ? 8 : 4;
   const size_t blk_smem = (size_t)4 * jbt * n * sizeof(float);
-  const bool block = !pair_cta && n >= 4 * jbt && blk_smem <= 200 * 1024;
+  const bool block = !pair_cta && n >= 4 * jbt && blk_smem <= blk_cap;
   const void* kern = pair_cta ? (const void*)jacobi_pair_kernel<T, NT>
-                              : (block ? (jbt == 16 ? (const void*)jacobi_block_kernel<16>
-                                                    : (const void*)jacobi_block_kernel<8>)
+                              : (block ? (jbt == 8 ? (const void*)jacobi_block_kernel<8>
+                                                   : (const void*)jacobi_block_kernel<4>)
                                        : (const void*)jacobi_kernel<T, NT>);
   const int nt = block ? jbt * 32 : NT;
   const size_t smem = block ? blk_smem : 0;

@@ -242,6 +242,68 @@ __global__ void gram_finish_kernel(int64_t n, const double* __restrict__ WT4, co
   }
 }
 
+// the pairs whose cosine is above tol (p < q): appended to pairs[] (at most
+// cap; count may go past it)
+__global__ void gram_bad_pairs_kernel(int64_t n, const double* __restrict__ Gh, double tol, int2* __restrict__ pairs,
+                                      int* __restrict__ count, int cap) {
+  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < n * n; t += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t p = t % n, q = t / n;
+    if (p >= q || !(fabs(Gh[p + q * n]) > tol)) continue;
+    const int i = atomicAdd(count, 1);
+    if (i < cap) pairs[i] = make_int2((int)p, (int)q);
+  }
+}
+
+// one exact one-sided Jacobi rotation per CTA, on disjoint column pairs of X
+// (and the same rotation on Wacc): the FP64 dots of the pair, the angle as
+// the FP32 sweeps take it, the two columns rotated
+__global__ void __launch_bounds__(256) pair_rotate_kernel(int64_t n, double* __restrict__ X, int64_t ldx,
+                                                          double* __restrict__ Wacc, const int2* __restrict__ pairs) {
+  __shared__ double red[3][8];
+  const int2 pq = pairs[blockIdx.x];
+  double* xp = X + (int64_t)pq.x * ldx;
+  double* xq = X + (int64_t)pq.y * ldx;
+  double a = 0, b = 0, g = 0;
+  for (int64_t i = threadIdx.x; i < n; i += blockDim.x) {
+    const double u = xp[i], w = xq[i];
+    a = fma(u, u, a);
+    b = fma(w, w, b);
+    g = fma(u, w, g);
+  }
+  a = warp_sum(a);
+  b = warp_sum(b);
+  g = warp_sum(g);
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  if (lane == 0) {
+    red[0][wid] = a;
+    red[1][wid] = b;
+    red[2][wid] = g;
+  }
+  __syncthreads();
+  a = b = g = 0;
+  for (int w = 0; w < (int)(blockDim.x >> 5); ++w) {
+    a += red[0][w];
+    b += red[1][w];
+    g += red[2][w];
+  }
+  if (g == 0 || !(a > 0) || !(b > 0)) return;
+  const double zeta = (b - a) / (2.0 * g);
+  const double t = copysign(1.0, zeta) / (fabs(zeta) + sqrt(1.0 + zeta * zeta));
+  const double c = 1.0 / sqrt(1.0 + t * t), sn = c * t;
+  for (int64_t i = threadIdx.x; i < n; i += blockDim.x) {
+    const double u = xp[i], w = xq[i];
+    xp[i] = c * u - sn * w;
+    xq[i] = sn * u + c * w;
+  }
+  double* vp = Wacc + (int64_t)pq.x * n;
+  double* vq = Wacc + (int64_t)pq.y * n;
+  for (int64_t i = threadIdx.x; i < n; i += blockDim.x) {
+    const double u = vp[i], w = vq[i];
+    vp[i] = c * u - sn * w;
+    vq[i] = sn * u + c * w;
+  }
+}
+
 }  // namespace
 
 // ---- Gram-matrix polish of a nearly orthogonal X ----------------------------------
@@ -263,6 +325,65 @@ __global__ void gram_finish_kernel(int64_t n, const double* __restrict__ WT4, co
 // final X.
 constexpr double kGramStart = 3e-2;  // largest cosine the FP32 sweeps leave for the Gram polish
 
+// The pairs the simultaneous rotations leave out (nearly equal norms), when
+// they are few: exact rotations of those pairs, in rounds of disjoint pairs
+// taken largest cosine first.  False (nothing done) when there are none or
+// too many; the pairwise sweeps over all pairs then finish instead.
+static bool rotate_bad_pairs(lra_ctx* ctx, int64_t n, double* X, int64_t ldx, double* Wacc, const double* Gh,
+                             double tol) {
+  const int cap = (int)std::min<int64_t>(32 * n, 1 << 22);
+  const ArenaMark mk = ctx->arena.mark();
+  int2* dp = ctx->arena.alloc_n<int2>((size_t)cap);
+  int* cnt = ctx->arena.alloc_n<int>(1);
+  LRA_CUDA(cudaMemsetAsync(cnt, 0, sizeof(int), ctx->stream));
+  const unsigned g = (unsigned)std::max<int64_t>(1, std::min<int64_t>((n * n + 255) / 256, ctx->num_sms * 8));
+  gram_bad_pairs_kernel<<<g, 256, 0, ctx->stream>>>(n, Gh, tol, dp, cnt, cap);
+  post_launch(ctx, "gram_bad_pairs_kernel");
+  int hc = 0;
+  LRA_CUDA(cudaMemcpyAsync(&hc, cnt, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+  LRA_CUDA(cudaStreamSynchronize(ctx->stream));
+  if (trace_on()) std::fprintf(stderr, "[lra] gram polish n=%lld: %d pairs above %.2e\n", (long long)n, hc, tol);
+  if (hc <= 0 || hc > cap) {
+    ctx->arena.release(mk);
+    return false;
+  }
+  std::vector<int2> hp((size_t)hc);
+  std::vector<double> hcos((size_t)hc);
+  LRA_CUDA(cudaMemcpyAsync(hp.data(), dp, (size_t)hc * sizeof(int2), cudaMemcpyDeviceToHost, ctx->stream));
+  LRA_CUDA(cudaStreamSynchronize(ctx->stream));
+  // the cosines, for the order (host copies of the few Gram entries involved)
+  for (int i = 0; i < hc; ++i)
+    LRA_CUDA(cudaMemcpyAsync(&hcos[(size_t)i], Gh + hp[(size_t)i].x + (int64_t)hp[(size_t)i].y * n, sizeof(double),
+                             cudaMemcpyDeviceToHost, ctx->stream));
+  LRA_CUDA(cudaStreamSynchronize(ctx->stream));
+  std::vector<int> ord((size_t)hc);
+  std::iota(ord.begin(), ord.end(), 0);
+  std::stable_sort(ord.begin(), ord.end(), [&](int a, int b) { return std::fabs(hcos[(size_t)a]) > std::fabs(hcos[(size_t)b]); });
+  std::vector<char> used((size_t)n);
+  std::vector<char> done((size_t)hc, 0);
+  int left = hc;
+  for (int round = 0; left > 0 && round < 1024; ++round) {
+    std::fill(used.begin(), used.end(), 0);
+    std::vector<int2> sel;
+    for (int i : ord) {
+      if (done[(size_t)i]) continue;
+      const int2 pq = hp[(size_t)i];
+      if (used[(size_t)pq.x] || used[(size_t)pq.y]) continue;
+      used[(size_t)pq.x] = used[(size_t)pq.y] = 1;
+      done[(size_t)i] = 1;
+      --left;
+      sel.push_back(pq);
+    }
+    LRA_CUDA(cudaMemcpyAsync(dp, sel.data(), sel.size() * sizeof(int2), cudaMemcpyHostToDevice, ctx->stream));
+    pair_rotate_kernel<<<(unsigned)sel.size(), 256, 0, ctx->stream>>>(n, X, ldx, Wacc, dp);
+    post_launch(ctx, "pair_rotate_kernel");
+    // sel is reused next round: the copy must have been read
+    LRA_CUDA(cudaStreamSynchronize(ctx->stream));
+  }
+  ctx->arena.release(mk);
+  return true;
+}
+
 bool gram_polish(lra_ctx* ctx, int64_t n, double* X, int64_t ldx, double* Wacc, double* S, double tol,
                  int max_iter) {
   const ArenaMark mk = ctx->arena.mark();
@@ -280,6 +401,7 @@ bool gram_polish(lra_ctx* ctx, int64_t n, double* X, int64_t ldx, double* Wacc, 
   const unsigned g = (unsigned)std::max<int64_t>(1, std::min<int64_t>(((int64_t)nn + 255) / 256, ctx->num_sms * 8));
   bool ok = false;
   double prev = INFINITY;
+  int cleanups = 0;
   for (int it = 0; it <= max_iter; ++it) {
     col_norms<double>(ctx, n, n, X, ldx, S);
     unit_cols_kernel<<<g, 256, 0, ctx->stream>>>(n, X, ldx, S, Xh);
@@ -311,8 +433,22 @@ bool gram_polish(lra_ctx* ctx, int64_t n, double* X, int64_t ldx, double* Wacc, 
       ok = true;
       break;
     }
-    // only pairs of nearly equal norms are left: the pairwise sweeps finish
-    if (ma <= tol || it == max_iter) break;
+    // only pairs of nearly equal norms are left: exact rotations of those
+    // pairs when they are few (then the check again), else the pairwise
+    // sweeps finish
+    if (ma <= tol) {
+      if (cleanups < 3 && it < max_iter) {
+        prev = mc;
+        copy_matrix(ctx, n, n, X, ldx, Xs, n);
+        copy_matrix(ctx, n, n, Wacc, n, Ws, n);
+        if (rotate_bad_pairs(ctx, n, X, ldx, Wacc, Gh, tol)) {
+          ++cleanups;
+          continue;
+        }
+      }
+      break;
+    }
+    if (it == max_iter) break;
     prev = mc;
     copy_matrix(ctx, n, n, X, ldx, Xs, n);
     copy_matrix(ctx, n, n, Wacc, n, Ws, n);
@@ -385,7 +521,10 @@ void jacobi_svd_fast(lra_ctx* ctx, int64_t n, T* X, int64_t ldx, T* V, int64_t l
   cast<T, float>(ctx, n, n, X, ldx, X32, n, scale);
   // the Gram polish converges quadratically from cosines of a few 1e-3 (the
   // FP32 sweeps stop there); the pairwise FP64 sweeps want them near 1e-6
-  jacobi_svd<float>(ctx, n, X32, n, V32, n, S32, true, df_polish ? kGramStart : 0.0);
+  // (neighbouring singular values of a smooth spectrum of n are ~1/n apart
+  // relative to each other, and the simultaneous rotations converge only
+  // from cosines below that gap: the start level falls with n)
+  jacobi_svd<float>(ctx, n, X32, n, V32, n, S32, true, df_polish ? std::min(kGramStart, 12.0 / (double)n) : 0.0);
   // 2. the rotation in FP64, re-orthonormalized by two Newton-Schulz steps
   //    W <- W (3 I - W'W) / 2: with |I - W'W| near 1e-6 from the FP32
   //    sweeps the error squares each step, to rounding level after two
@@ -413,7 +552,7 @@ void jacobi_svd_fast(lra_ctx* ctx, int64_t n, T* X, int64_t ldx, T* V, int64_t l
       const double tol =
           std::max((double)Real<double>::eps * 2.0 * std::sqrt((double)n), 8.0 * std::ldexp(1.0, -46) * std::sqrt((double)n));
       set_identity(ctx, n, n, Yd, n);
-      done = gram_polish(ctx, n, Xd, ldx, Yd, reinterpret_cast<double*>(S), tol, 5);
+      done = gram_polish(ctx, n, Xd, ldx, Yd, reinterpret_cast<double*>(S), tol, n > 1024 ? 8 : 5);
       if (!done) {
         double* Y2 = reinterpret_cast<double*>(W2);
         done = jacobi_svd_df(ctx, n, Xd, ldx, Y2, n, reinterpret_cast<double*>(S));

@@ -1311,7 +1311,12 @@ __global__ void __launch_bounds__(NT) geqp3_df_kernel(QrParams<double> P, QrV2Ex
 // below the error of the downdated norms); ties go to the smaller column
 // index, as with xLAQPS's idamax.
 struct QrSm {
-  unsigned long long* xw;    // [2][G] exchange words, zeroed before the launch
+  // the exchange, zeroed before the launch: exchange e's largest word in
+  // amax[(e % 4) * 16] and OR of stop flags in astop[(e % 4) * 32] (a 128-byte
+  // line each), and one arrival counter (G per exchange)
+  unsigned long long* amax;
+  unsigned* astop;
+  unsigned* arrive;
   void* stage;               // [2][G][m] staged candidate columns (elements of the arithmetic)
   unsigned long long* pubt;  // LRA_TRACE: %globaltimer of each CTA's word per pivot, [kmax][G], or null
   // several adaptive steps factored by one launch: the lowest index of a
@@ -1548,15 +1553,18 @@ __device__ __forceinline__ void geqp3_df_body(const QrParams<typename A::T>& P, 
     }
     __syncthreads();
     if (!GCOL && threadIdx.x == 0) {
-      const unsigned long long seq = (unsigned long long)(((e >> 1) & 1) ^ 1) << 63;
-      const unsigned long long fl = s_stop ? (1ull << 62) : 0ull;
+      // the word into the exchange's maximum (and the stop flag into its
+      // OR), then the arrival, released after the staged rows
       __threadfence();
       if (S.pubt && r0 >= 1 && r0 - 1 < P.kmax) S.pubt[(r0 - 1) * G + b] = globaltimer_ns();
-      *((volatile unsigned long long*)(S.xw + (size_t)(e & 1) * G + b)) = seq | fl | (w & XW_LOW);
+      const unsigned slot = e & 3;
+      if (w & XW_LOW) atomicMax(S.amax + slot * 16, w & XW_LOW);
+      if (!cancel && s_stop) atomicOr(S.astop + slot * 32, 1u);
+      asm volatile("red.release.gpu.global.add.u32 [%0], 1;" ::"l"(S.arrive) : "memory");
     }
   };
-  // wait for all G words of exchange e (bounded), reduce them: the winning
-  // word, its CTA and the OR of the stop flags, in shared memory
+  // wait for all G arrivals of exchange e (bounded): the winning word, its
+  // CTA and the OR of the stop flags, in shared memory
   auto collect = [&](unsigned e) -> bool {
     if (GCOL) {
       // one CTA: its own candidate is the pivot
@@ -1564,85 +1572,60 @@ __device__ __forceinline__ void geqp3_df_body(const QrParams<typename A::T>& P, 
       __syncthreads();
       return true;
     }
-    if (wid == 0) {
-      const unsigned long long* xw = S.xw + (size_t)(e & 1) * G;
-      const unsigned long long want = ((e >> 1) & 1) ^ 1;
+    if (threadIdx.x == 0) {
       // a lower step of the launch revealed its rank: this step stops at
-      // the next exchange (the load overlaps the polls below)
-      int canc = 0;
-      if (S.success && lane == 0) canc = *((volatile int*)S.success) < S.job;
-      constexpr int PB = 8;  // G <= 256
-      unsigned long long w[PB];
-      unsigned pending = 0;
-#pragma unroll
-      for (int q = 0; q < PB; ++q) {
-        const int bb = lane + 32 * q;
-        w[q] = 0;
-        if (bb < G) {
-          w[q] = *((const volatile unsigned long long*)(xw + bb));
-          if ((w[q] >> 63) != want) pending |= 1u << q;
-        }
-      }
+      // the next exchange
+      const int canc = S.success ? (*((volatile int*)S.success) < S.job ? 1 : 0) : 0;
+      // every CTA's arrival at exchange e (the counter grows by G per
+      // exchange), bounded
+      const unsigned target = (unsigned)G * (e + 1u);
       bool ok = true;
-      if (__any_sync(0xffffffffu, pending != 0)) {
+      unsigned v;
+      asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(S.arrive) : "memory");
+      if ((int)(v - target) < 0) {
         const uint64_t t0 = globaltimer_ns(), lim = wait_limit_ns();
         for (unsigned it = 1;; ++it) {
-#pragma unroll
-          for (int q = 0; q < PB; ++q)
-            if (pending & (1u << q)) {
-              w[q] = *((const volatile unsigned long long*)(xw + lane + 32 * q));
-              if ((w[q] >> 63) == want) pending &= ~(1u << q);
-            }
-          if (!__any_sync(0xffffffffu, pending != 0)) break;
-          // the error word and the clock every 16th round: a poll round is
-          // one L2 round trip, and a dependent second load would double it
+          asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(S.arrive) : "memory");
+          if ((int)(v - target) >= 0) break;
+          // the error word and the clock every 16th poll
           if (it & 15) continue;
-          int bad = 0;
-          if (lane == 0) {
-            bad = *((volatile int*)&P.bar->err) != 0;
-            if (!bad && globaltimer_ns() - t0 > lim) {
-              atomicCAS(&P.bar->err, 0, 4);
-              bad = 1;
-            }
+          if (*((volatile int*)&P.bar->err) != 0) {
+            ok = false;
+            break;
           }
-          if (__shfl_sync(0xffffffffu, bad, 0)) {
+          if (globaltimer_ns() - t0 > lim) {
+            atomicCAS(&P.bar->err, 0, 4);
             ok = false;
             break;
           }
         }
       }
-      __threadfence();
-      unsigned long long best = 0;
-      int own = 0, fl = 0;
-#pragma unroll
-      for (int q = 0; q < PB; ++q) {
-        const int bb = lane + 32 * q;
-        if (bb < G) {
-          const unsigned long long lw = w[q] & XW_LOW;
-          fl |= (int)((w[q] >> 62) & 1);
-          if (lw > best) {
-            best = lw;
-            own = bb;
-          }
-        }
+      const unsigned slot = e & 3;
+      unsigned long long best;
+      unsigned fl;
+      asm volatile("ld.relaxed.gpu.global.u64 %0, [%1];" : "=l"(best) : "l"(S.amax + slot * 16) : "memory");
+      asm volatile("ld.relaxed.gpu.global.u32 %0, [%1];" : "=r"(fl) : "l"(S.astop + slot * 32) : "memory");
+      // every CTA has read exchange e - 1 (each read it before arriving at
+      // e): its slot is cleared for exchange e + 3, before this CTA's next
+      // arrival releases the clearing
+      if (b == 0 && ok) {
+        const unsigned prev = (e + 3) & 3;
+        asm volatile("st.relaxed.gpu.global.u64 [%0], %1;" ::"l"(S.amax + prev * 16), "l"(0ull) : "memory");
+        asm volatile("st.relaxed.gpu.global.u32 [%0], %1;" ::"l"(S.astop + prev * 32), "r"(0u) : "memory");
       }
-#pragma unroll
-      for (int o = 16; o > 0; o >>= 1) {
-        const unsigned long long b2 = __shfl_xor_sync(0xffffffffu, best, o);
-        const int o2 = __shfl_xor_sync(0xffffffffu, own, o);
-        if (b2 > best || (b2 == best && o2 < own)) {
-          best = b2;
-          own = o2;
-        }
-        fl |= __shfl_xor_sync(0xffffffffu, fl, o);
+      // the winner's CTA: the one whose columns [n b / G, n (b + 1) / G)
+      // hold the winning column
+      const int64_t jw = (int64_t)(XW_IDX - (best & XW_IDX));
+      int own = 0;
+      if ((best & XW_LOW) != 0 && best != XW_CANCEL) {
+        own = (int)(((jw + 1) * (int64_t)G - 1) / n);
+        own = own < 0 ? 0 : (own >= G ? G - 1 : own);
       }
-      if (lane == 0) {
-        s_win = best;
-        s_owner = own;
-        s_stop = fl;
-        s_ok = ok && best != XW_CANCEL ? 1 : 0;
-        s_cancel = canc;
-      }
+      s_win = best;
+      s_owner = own;
+      s_stop = fl ? 1 : 0;
+      s_ok = ok && best != XW_CANCEL ? 1 : 0;
+      s_cancel = canc;
     }
     __syncthreads();
     return s_ok != 0;
@@ -2814,9 +2797,14 @@ void sm_prepare(lra_ctx* ctx, SmQr<T>& q, int64_t m, int64_t n, T* A, int64_t ld
     S.pubt = ctx->arena.alloc_n<unsigned long long>((size_t)G * km);
     LRA_CUDA(cudaMemsetAsync(S.pubt, 0, (size_t)G * km * 8, ctx->stream));
   }
-  S.xw = ctx->arena.alloc_n<unsigned long long>((size_t)2 * G);
+  // the exchange: 4 max words and 4 stop words a 128-byte line apart, and
+  // the arrival counter on a line of its own
+  unsigned char* xb = static_cast<unsigned char*>(ctx->arena.alloc(1152));
+  S.amax = reinterpret_cast<unsigned long long*>(xb);
+  S.astop = reinterpret_cast<unsigned*>(xb + 512);
+  S.arrive = reinterpret_cast<unsigned*>(xb + 1024);
   S.stage = ctx->arena.alloc_n<E>((size_t)2 * G * m);
-  LRA_CUDA(cudaMemsetAsync(S.xw, 0, (size_t)2 * G * sizeof(unsigned long long), ctx->stream));
+  LRA_CUDA(cudaMemsetAsync(xb, 0, 1152, ctx->stream));
   q.job.G = G;
   q.job.off = 0;
 }

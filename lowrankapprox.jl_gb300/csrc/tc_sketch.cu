@@ -942,11 +942,15 @@ void tc_sketch(lra_ctx* ctx, const TcSplit& sp, int64_t order, const T* S, T* B,
   P.ldb = ldb;
   P.out_double = sizeof(T) == 8 ? 1 : 0;
   P.err = err;
-  // as many ring stages as the shared memory holds
+  // two ring stages when two CTAs fit an SM (their loads interleave), else
+  // as many stages as the one CTA's shared memory holds
   const size_t stage_bytes = (size_t)TILE_N * KBLK * 2 + (size_t)ns * TILE_BYTES;
-  int smem_optin = 0;
+  int smem_optin = 0, smem_sm = 0;
   LRA_CUDA(cudaDeviceGetAttribute(&smem_optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, ctx->device));
-  P.nstage = (int)std::max<size_t>(2, std::min<size_t>(MAX_NSTAGE, ((size_t)smem_optin - 1024 - 256) / stage_bytes));
+  LRA_CUDA(cudaDeviceGetAttribute(&smem_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, ctx->device));
+  const bool two_ctas = 2 * (2 * stage_bytes + 1024 + 256 + 1024) <= (size_t)smem_sm;
+  P.nstage = two_ctas ? 2
+                      : (int)std::max<size_t>(2, std::min<size_t>(MAX_NSTAGE, ((size_t)smem_optin - 1024 - 256) / stage_bytes));
   const size_t smem = 1024 + (size_t)P.nstage * stage_bytes + 256;
   const int64_t ntiles = ((N + TILE_M - 1) / TILE_M) * (Lp / TILE_N);
   // too few tiles for two CTAs per SM: split K over more CTAs (whole

@@ -219,3 +219,21 @@ def test_f32_shared_memory_qr_vs_oracle(lra, oracle, shape):
     same = check_pivots(B, p, p_ref, min(k, k_ref), np.float32)
     if same == k == k_ref:
         assert_pqr_parity(p, np.triu(Bd.cpu().numpy()[:k]), p_ref, np.triu(W[:k]), k, 5e-5)
+
+
+def test_psvd_large_rank(lra):
+    """psvdfact at a rank where the mixed path preconditions its k x k Jacobi
+    SVD with a pivoted QR (k >= 1024) and polishes near-equal pairs with
+    exact rotations: the reference test's criterion (test/psvd.jl:29), the
+    singular values against numpy's to the rank threshold, orthonormal U
+    and V."""
+    A = decaying(2600, 1500, 110.0, 12)
+    rtol = 1e-10
+    F = lra.psvdfact(A, lra.LRAOptions(rtol=rtol, precision="mixed", seed=3))
+    assert F.k >= 1024
+    E = (np.asarray(F.U) * F.S) @ np.asarray(F.Vt)
+    assert np.linalg.norm(A - E) < 100 * rtol * np.linalg.norm(A)
+    s = np.linalg.svd(A, compute_uv=False)
+    assert np.abs(F.S - s[:F.k]).max() <= 10 * rtol * s[0]
+    for Q in (np.asarray(F.U), np.asarray(F.Vt).T):
+        assert np.abs(Q.T @ Q - np.eye(F.k)).max() < 1e-8
