@@ -401,9 +401,9 @@ __global__ void __launch_bounds__(JBT * 32) jacobi_block_kernel(JacParams<float>
           Ql[e / (2 * JBT)][e % (2 * JBT)] = e / (2 * JBT) == e % (2 * JBT) ? 1.0f : 0.0f;
         asm volatile("cp.async.wait_all;" ::: "memory");
         __syncthreads();
-        unsigned vmask = 0;  // local columns that exist
+        unsigned long long vmask = 0;  // local columns that exist
 #pragma unroll
-        for (int k = 0; k < 2 * JBT; ++k) vmask |= (gcol(k) >= 0 ? 1u : 0u) << k;
+        for (int k = 0; k < 2 * JBT; ++k) vmask |= (gcol(k) >= 0 ? 1ull : 0ull) << k;
         const int ni = (int)n;
         for (int lr = 0; lr < 2 * JBT - 1; ++lr) {
           // round-robin pair of this warp among the 2 JBT local columns
@@ -414,7 +414,7 @@ __global__ void __launch_bounds__(JBT * 32) jacobi_block_kernel(JacParams<float>
             p = q;
             q = t;
           }
-          if (((vmask >> p) & 1u) && ((vmask >> q) & 1u)) {
+          if (((vmask >> p) & 1ull) && ((vmask >> q) & 1ull)) {
             float* xp = Xs + p * ni;
             float* xq = Xs + q * ni;
             float a = 0, b = 0, g = 0;
@@ -452,10 +452,10 @@ __global__ void __launch_bounds__(JBT * 32) jacobi_block_kernel(JacParams<float>
                       xq[i] = sn * u[tt] + c * w[tt];
                     }
                   }
-                  if (lane < 2 * JBT) {
-                    const float qu = Ql[p][lane], qw = Ql[q][lane];
-                    Ql[p][lane] = c * qu - sn * qw;
-                    Ql[q][lane] = sn * qu + c * qw;
+                  for (int l = lane; l < 2 * JBT; l += 32) {
+                    const float qu = Ql[p][l], qw = Ql[q][l];
+                    Ql[p][l] = c * qu - sn * qw;
+                    Ql[q][l] = sn * qu + c * qw;
                   }
                 }
               }
@@ -482,10 +482,10 @@ __global__ void __launch_bounds__(JBT * 32) jacobi_block_kernel(JacParams<float>
                     xp[i] = c * u - sn * w;
                     xq[i] = sn * u + c * w;
                   }
-                  if (lane < 2 * JBT) {
-                    const float qu = Ql[p][lane], qw = Ql[q][lane];
-                    Ql[p][lane] = c * qu - sn * qw;
-                    Ql[q][lane] = sn * qu + c * qw;
+                  for (int l = lane; l < 2 * JBT; l += 32) {
+                    const float qu = Ql[p][l], qw = Ql[q][l];
+                    Ql[p][l] = c * qu - sn * qw;
+                    Ql[q][l] = sn * qu + c * qw;
                   }
                 }
               }
@@ -843,14 +843,20 @@ void jacobi_svd(lra_ctx* ctx, int64_t n, T* X, int64_t ldx, T* V, int64_t ldv, T
   // measured slower: the local sweeps become issue-bound on half the SMs);
   // 4-column blocks for the longer columns whose 8-column block pair does
   // not fit shared memory (up to about 3500 rows); a warp per pair beyond
-  const size_t blk_cap = 220 * 1024;
-  const int jbt = (size_t)4 * 8 * n * sizeof(float) <= blk_cap ? 8 : 4;
+  const size_t blk_cap = 210 * 1024;
+  int jbt = (size_t)4 * 8 * n * sizeof(float) <= blk_cap ? 8 : 4;
+  // the tuning table may ask for another block size (when it fits)
+  const int want = ctx->tuning.jacobi_jb;
+  if ((want == 4 || want == 8 || want == 16 || want == 32) && (size_t)4 * want * n * sizeof(float) <= blk_cap)
+    jbt = want;
   const size_t blk_smem = (size_t)4 * jbt * n * sizeof(float);
   const bool block = !pair_cta && n >= 4 * jbt && blk_smem <= blk_cap;
   const void* kern = pair_cta ? (const void*)jacobi_pair_kernel<T, NT>
-                              : (block ? (jbt == 8 ? (const void*)jacobi_block_kernel<8>
-                                                   : (const void*)jacobi_block_kernel<4>)
-                                       : (const void*)jacobi_kernel<T, NT>);
+                     : !block ? (const void*)jacobi_kernel<T, NT>
+                     : jbt == 32 ? (const void*)jacobi_block_kernel<32>
+                     : jbt == 16 ? (const void*)jacobi_block_kernel<16>
+                     : jbt == 8 ? (const void*)jacobi_block_kernel<8>
+                                : (const void*)jacobi_block_kernel<4>;
   const int nt = block ? jbt * 32 : NT;
   const size_t smem = block ? blk_smem : 0;
   if (block) raise_smem_limit(ctx, (const void*)kern);

@@ -83,6 +83,11 @@ struct lra_tuning {
   // most parts the tensor-core sketch splits K into when its tiles are too
   // few for the SMs (0: as many as fill them, 1: no split)
   int tc_split;
+  // columns per block of the FP32 block Jacobi (4, 8, 16, 32; 0: by size)
+  int jacobi_jb;
+  // largest cosine, in units of 1e-4, at which the FP32 sweeps hand the
+  // core SVD to the Gram polish (0: min(3e-2, 12 / n))
+  int gram_start;
 };
 
 struct lra_ctx {

@@ -524,7 +524,8 @@ void jacobi_svd_fast(lra_ctx* ctx, int64_t n, T* X, int64_t ldx, T* V, int64_t l
   // (neighbouring singular values of a smooth spectrum of n are ~1/n apart
   // relative to each other, and the simultaneous rotations converge only
   // from cosines below that gap: the start level falls with n)
-  jacobi_svd<float>(ctx, n, X32, n, V32, n, S32, true, df_polish ? std::min(kGramStart, 12.0 / (double)n) : 0.0);
+  const double start = ctx->tuning.gram_start > 0 ? 1e-4 * ctx->tuning.gram_start : std::min(kGramStart, 12.0 / (double)n);
+  jacobi_svd<float>(ctx, n, X32, n, V32, n, S32, true, df_polish ? start : 0.0);
   // 2. the rotation in FP64, re-orthonormalized by two Newton-Schulz steps
   //    W <- W (3 I - W'W) / 2: with |I - W'W| near 1e-6 from the FP32
   //    sweeps the error squares each step, to rounding level after two

@@ -85,3 +85,24 @@ def test_k_split_gives_the_same_bits(lra, dt, shape):
     R = g[:order * m].reshape((order, m), order="F") @ A.astype(np.float64)
     scale = np.abs(R).max(axis=0) + 1e-300
     assert (np.abs(outs[0] - R) / scale).max() <= (1e-12 if dt == np.float64 else 1e-5)
+
+
+@pytest.mark.parametrize("jb", [4, 8, 16, 32])
+def test_jacobi_block_sizes(lra, jb):
+    """The FP32 block Jacobi of psvdfact's core SVD with every block size
+    (the block pair in shared memory; 32-column blocks gather their
+    rotations into a 64 x 64 matrix): the same rank and singular values to
+    the rank threshold, and the reference test's criterion (test/psvd.jl:29)."""
+    from test_gpu_mixed import decaying
+    A = decaying(1500, 1100, 30.0, 21)
+    rtol = 1e-10
+    ctx = lra.Context(0)
+    ctx.set_tuning("jacobi_jb", 0, jb)
+    F = lra.psvdfact(A, lra.LRAOptions(rtol=rtol, precision="mixed", seed=2), ctx=ctx)
+    ctx.close()
+    E = (np.asarray(F.U) * F.S) @ np.asarray(F.Vt)
+    assert np.linalg.norm(A - E) < 100 * rtol * np.linalg.norm(A)
+    s = np.linalg.svd(A, compute_uv=False)
+    assert np.abs(F.S - s[:F.k]).max() <= 10 * rtol * s[0]
+    for Q in (np.asarray(F.U), np.asarray(F.Vt).T):
+        assert np.abs(Q.T @ Q - np.eye(F.k)).max() < 1e-10
