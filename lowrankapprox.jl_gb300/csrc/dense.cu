@@ -36,6 +36,9 @@ struct JacParams {
   double* part;
   GridBar* bar;
   int* sweeps_out;
+  // block Jacobi: V stays in global memory (only X's block pair in shared
+  // memory), so that longer columns fit 8-column blocks
+  int vglobal = 0;
 };
 
 constexpr int JCH = 16;  // rows per lane per register chunk (512 rows)
@@ -366,7 +369,8 @@ __global__ void __launch_bounds__(JBT * 32) jacobi_block_kernel(JacParams<float>
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
   const int64_t n = P.n;
   float* Xs = jb_smem;                       // [2 JBT][n]
-  float* Vs = jb_smem + (size_t)2 * JBT * n;  // [2 JBT][n]
+  float* Vs = jb_smem + (size_t)2 * JBT * n;  // [2 JBT][n], unless V stays in global memory
+  const bool vg = P.vglobal != 0;
   const int64_t nblk = (n + JBT - 1) / JBT;
   const int64_t nbb = nblk + (nblk & 1);
   const float tol = (float)P.tol;
@@ -390,10 +394,10 @@ __global__ void __launch_bounds__(JBT * 32) jacobi_block_kernel(JacParams<float>
           for (int64_t i = threadIdx.x; i < n; i += JBT * 32) {
             if (j >= 0) {
               cp_async4(Xs + k * n + i, P.X + i + j * P.ldx);
-              cp_async4(Vs + k * n + i, P.V + i + j * P.ldv);
+              if (!vg) cp_async4(Vs + k * n + i, P.V + i + j * P.ldv);
             } else {
               Xs[k * n + i] = 0.0f;
-              Vs[k * n + i] = 0.0f;
+              if (!vg) Vs[k * n + i] = 0.0f;
             }
           }
         }
@@ -493,19 +497,35 @@ __global__ void __launch_bounds__(JBT * 32) jacobi_block_kernel(JacParams<float>
           }
           __syncthreads();
         }
-        // the block's columns of V times the gathered rotation, a thread per row
+        // the block's columns of V times the gathered rotation, a thread per
+        // row (rows of V read and written in place, coalesced, when V stays
+        // in global memory)
         for (int i = threadIdx.x; i < ni; i += JBT * 32) {
           float acc[2 * JBT];
 #pragma unroll
           for (int k = 0; k < 2 * JBT; ++k) acc[k] = 0.0f;
 #pragma unroll 1
           for (int j = 0; j < 2 * JBT; ++j) {  // (not unrolled: Ql would be hoisted into registers)
-            const float v = Vs[j * ni + i];
+            float v;
+            if (vg) {
+              const int64_t gj = gcol(j);
+              v = gj >= 0 ? P.V[i + gj * P.ldv] : 0.0f;
+            } else {
+              v = Vs[j * ni + i];
+            }
 #pragma unroll
             for (int k = 0; k < 2 * JBT; ++k) acc[k] = fmaf(v, Ql[k][j], acc[k]);
           }
+          if (vg) {
 #pragma unroll
-          for (int k = 0; k < 2 * JBT; ++k) Vs[k * ni + i] = acc[k];
+            for (int k = 0; k < 2 * JBT; ++k) {
+              const int64_t gk = gcol(k);
+              if (gk >= 0) P.V[i + gk * P.ldv] = acc[k];
+            }
+          } else {
+#pragma unroll
+            for (int k = 0; k < 2 * JBT; ++k) Vs[k * ni + i] = acc[k];
+          }
         }
         __syncthreads();
         for (int k = 0; k < 2 * JBT; ++k) {
@@ -513,7 +533,7 @@ __global__ void __launch_bounds__(JBT * 32) jacobi_block_kernel(JacParams<float>
           if (j < 0) continue;
           for (int64_t i = threadIdx.x; i < n; i += JBT * 32) {
             P.X[i + j * P.ldx] = Xs[k * n + i];
-            P.V[i + j * P.ldv] = Vs[k * n + i];
+            if (!vg) P.V[i + j * P.ldv] = Vs[k * n + i];
           }
         }
         __syncthreads();
@@ -844,12 +864,18 @@ void jacobi_svd(lra_ctx* ctx, int64_t n, T* X, int64_t ldx, T* V, int64_t ldv, T
   // 4-column blocks for the longer columns whose 8-column block pair does
   // not fit shared memory (up to about 3500 rows); a warp per pair beyond
   const size_t blk_cap = 210 * 1024;
-  int jbt = (size_t)4 * 8 * n * sizeof(float) <= blk_cap ? 8 : 4;
+  // 8-column blocks with the block pair of X and V in shared memory; for
+  // longer columns V stays in global memory (read and written once per block
+  // pair), up to about 3400 rows; beyond, a warp per pair
+  int jbt = 8;
+  bool vglobal = (size_t)4 * jbt * n * sizeof(float) > blk_cap;
   // the tuning table may ask for another block size (when it fits)
   const int want = ctx->tuning.jacobi_jb;
-  if ((want == 4 || want == 8 || want == 16 || want == 32) && (size_t)4 * want * n * sizeof(float) <= blk_cap)
+  if ((want == 4 || want == 8 || want == 16 || want == 32) && (size_t)2 * want * n * sizeof(float) <= blk_cap) {
     jbt = want;
-  const size_t blk_smem = (size_t)4 * jbt * n * sizeof(float);
+    vglobal = (size_t)4 * jbt * n * sizeof(float) > blk_cap;
+  }
+  const size_t blk_smem = (size_t)(vglobal ? 2 : 4) * jbt * n * sizeof(float);
   const bool block = !pair_cta && n >= 4 * jbt && blk_smem <= blk_cap;
   const void* kern = pair_cta ? (const void*)jacobi_pair_kernel<T, NT>
                      : !block ? (const void*)jacobi_kernel<T, NT>
@@ -878,6 +904,7 @@ void jacobi_svd(lra_ctx* ctx, int64_t n, T* X, int64_t ldx, T* V, int64_t ldv, T
   P.V = V;
   P.ldv = ldv;
   P.S = S;
+  P.vglobal = block && vglobal ? 1 : 0;
   P.tol = (double)Real<T>::eps * 2.0 * std::sqrt((double)n);
   // A sweep whose cosines were all below sqrt(tol)/10 leaves them near
   // tol^2/100 times a modest gap factor (quadratic convergence), so the

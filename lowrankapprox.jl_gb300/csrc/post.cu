@@ -402,6 +402,7 @@ bool gram_polish(lra_ctx* ctx, int64_t n, double* X, int64_t ldx, double* Wacc, 
   bool ok = false;
   double prev = INFINITY;
   int cleanups = 0;
+  bool last_cleanup = false;
   for (int it = 0; it <= max_iter; ++it) {
     col_norms<double>(ctx, n, n, X, ldx, S);
     unit_cols_kernel<<<g, 256, 0, ctx->stream>>>(n, X, ldx, S, Xh);
@@ -420,7 +421,9 @@ bool gram_polish(lra_ctx* ctx, int64_t n, double* X, int64_t ldx, double* Wacc, 
     if (trace_on())
       std::fprintf(stderr, "[lra] gram polish n=%lld iteration %d: max cosine %.3e (rotating pairs %.3e)\n",
                    (long long)n, it, mc, ma);
-    if (!std::isfinite(mc) || mc > prev) {
+    // progress: a simultaneous update is judged by the pairs it rotates
+    // (pairs it leaves out keep their cosine), an exact cleanup by all pairs
+    if (!std::isfinite(mc) || (last_cleanup ? mc > prev : ma > prev)) {
       // the last update did not help: back to the state before it
       if (it > 0) {
         copy_matrix(ctx, n, n, Xs, n, X, ldx);
@@ -443,13 +446,15 @@ bool gram_polish(lra_ctx* ctx, int64_t n, double* X, int64_t ldx, double* Wacc, 
         copy_matrix(ctx, n, n, Wacc, n, Ws, n);
         if (rotate_bad_pairs(ctx, n, X, ldx, Wacc, Gh, tol)) {
           ++cleanups;
+          last_cleanup = true;
           continue;
         }
       }
       break;
     }
     if (it == max_iter) break;
-    prev = mc;
+    prev = ma;
+    last_cleanup = false;
     copy_matrix(ctx, n, n, X, ldx, Xs, n);
     copy_matrix(ctx, n, n, Wacc, n, Ws, n);
     gemm<double>(ctx, 'n', 'n', n, n, n, 1.0, Tm, n, Tm, n, 0.0, T2, n);

@@ -221,16 +221,18 @@ def test_f32_shared_memory_qr_vs_oracle(lra, oracle, shape):
         assert_pqr_parity(p, np.triu(Bd.cpu().numpy()[:k]), p_ref, np.triu(W[:k]), k, 5e-5)
 
 
-def test_psvd_large_rank(lra):
-    """psvdfact at a rank where the mixed path preconditions its k x k Jacobi
-    SVD with a pivoted QR (k >= 1024) and polishes near-equal pairs with
-    exact rotations: the reference test's criterion (test/psvd.jl:29), the
-    singular values against numpy's to the rank threshold, orthonormal U
-    and V."""
-    A = decaying(2600, 1500, 110.0, 12)
+@pytest.mark.parametrize("shape", [(2600, 1500, 110.0, 1024), (3000, 2200, 180.0, 1700)])
+def test_psvd_large_rank(lra, shape):
+    """psvdfact at ranks where the core SVD's FP32 block Jacobi keeps V in
+    shared memory (k ~ 1100) and in global memory (k ~ 1800), and the Gram
+    polish gives the near-equal pairs it leaves exact rotations: the
+    reference test's criterion (test/psvd.jl:29), the singular values
+    against numpy's to the rank threshold, orthonormal U and V."""
+    m, n, rate, kmin = shape
+    A = decaying(m, n, rate, 12)
     rtol = 1e-10
     F = lra.psvdfact(A, lra.LRAOptions(rtol=rtol, precision="mixed", seed=3))
-    assert F.k >= 1024
+    assert F.k >= kmin
     E = (np.asarray(F.U) * F.S) @ np.asarray(F.Vt)
     assert np.linalg.norm(A - E) < 100 * rtol * np.linalg.norm(A)
     s = np.linalg.svd(A, compute_uv=False)
