@@ -3017,19 +3017,36 @@ lra_psvd* psvd_dev(lra_ctx* ctx, const lra_opts& o, char trans, int64_t m, int64
   const int64_t k = F.k;
   Stage st(ctx, 3);
   const int64_t ldq = std::max<int64_t>(M, 1), ldk = std::max<int64_t>(k, 1);
+  // LRA_TRACE: the post-processing's phases (each waits for the device)
+  const bool tr = trace_on();
+  auto tnow = [] { return std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now().time_since_epoch()).count(); };
+  double tl = tr ? tnow() : 0;
+  auto tmark = [&](const char* what) {
+    if (!tr) return;
+    LRA_CUDA(cudaStreamSynchronize(ctx->stream));
+    const double t = tnow();
+    std::fprintf(stderr, "[lra] psvd post k=%lld %s %.3f ms\n", (long long)k, what, t - tl);
+    tl = t;
+  };
   {
     // GEMM-shaped route: A[:, sk] = Q R_A, V^T = Q_v R_v, SVD(R_A R_v^T)
     const ArenaMark mk = ctx->arena.mark();
     T* Q = getcols<T>(ctx, trans, m, n, dA, F.jpvt, k);
     T* RA = ctx->arena.alloc_n<T>((size_t)ldk * ldk);
     T* Rv = ctx->arena.alloc_n<T>((size_t)ldk * ldk);
-    if (skeleton_qr<T>(ctx, F, M, Q, RA, dtype) && chol_v<T>(ctx, k, N - k, F.T_, Rv)) {
+    tmark("gather");
+    bool ok = skeleton_qr<T>(ctx, F, M, Q, RA, dtype);
+    tmark("skeleton cholesky qr");
+    ok = ok && chol_v<T>(ctx, k, N - k, F.T_, Rv);
+    tmark("chol(I + T T')");
+    if (ok) {
       T* Mm = ctx->arena.alloc_n<T>((size_t)ldk * ldk);
       gemm<T>(ctx, 'n', 't', k, k, k, T(1), RA, ldk, Rv, ldk, T(0), Mm, ldk);
       T* UM = ctx->arena.alloc_n<T>((size_t)ldk * ldk);
       T* VM = ctx->arena.alloc_n<T>((size_t)ldk * ldk);
       T* S = ctx->arena.alloc_n<T>(ldk);
       std::vector<T> hS = small_svd<T>(ctx, k, Mm, UM, VM, S);
+      tmark("core svd");
       std::vector<double> sd(hS.begin(), hS.end());
       const int64_t kk = psvdrank(sd, o), lkk = std::max<int64_t>(kk, 1);
       lra_psvd* r = static_cast<lra_psvd*>(hmalloc(sizeof(lra_psvd)));
@@ -3049,11 +3066,13 @@ lra_psvd* psvd_dev(lra_ctx* ctx, const lra_opts& o, char trans, int64_t m, int64
       if (N > k) gemm<T>(ctx, 't', 'n', kk, N - k, k, T(1), VM, ldk, F.T_, ldk, T(0), Vp + k * lkk, lkk);
       T* Vt = ctx->arena.alloc_n<T>((size_t)lkk * std::max<int64_t>(N, 1));
       scatter_cols(ctx, kk, N, Vp, lkk, F.jpvt, Vt, lkk);
+      tmark("factors");
       r->U = hmalloc(sizeof(T) * std::max<int64_t>(M * kk, 1));
       r->Vt = hmalloc(sizeof(T) * std::max<int64_t>(kk * N, 1));
       to_host(ctx, r->U, U, (size_t)M * kk);
       to_host(ctx, r->Vt, Vt, (size_t)kk * N);
       LRA_CUDA(cudaStreamSynchronize(ctx->stream));
+      tmark("to host");
       return r;
     }
     ctx->arena.release(mk);
