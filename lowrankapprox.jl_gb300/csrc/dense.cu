@@ -11,7 +11,10 @@
 
 #include <algorithm>
 #include <cstdio>
+#include <cstdlib>
 #include <cmath>
+#include <mutex>
+#include <set>
 #include <vector>
 
 #include "common.cuh"
@@ -567,6 +570,248 @@ __global__ void __launch_bounds__(JBT * 32) jacobi_block_kernel(JacParams<float>
   if (blockIdx.x == 0 && threadIdx.x == 0) *P.sweeps_out = sweep;
 }
 
+// ---- FP32 one-sided Jacobi in one thread-block cluster ---------------------------
+// Every column pair sits in the registers of one warp (X and V, RPL rows a
+// lane), the whole n x n matrix across the CTAs of one cluster.  Each step
+// rotates all nn/2 pairs at once; then the columns move one position along
+// the round-robin tournament (slot 0 fixed, slot i <- slot i + 1, slot nn - 1
+// <- slot 1), which pairs every two columns once in nn - 1 steps and brings
+// every column back to its slot at the end of a sweep.  A column moves by the
+// sender's stores into the receiver's shared-memory mailbox (distributed
+// shared memory across the cluster), double-buffered by step parity, so one
+// cluster barrier a step orders the stores before the receiver's loads and
+// after its previous reads.  Warp w owns slots w (top) and nn - 1 - w
+// (bottom): its top moves to warp w - 1's top (warp 1's to warp 0's bottom,
+// warp 0's stays), its bottom to warp w + 1's bottom (the last warp's to its
+// own top).  The rotation of a pair is that of jacobi_block_kernel.
+__device__ __forceinline__ unsigned cluster_rank() {
+  unsigned r;
+  asm volatile("mov.u32 %0, %%cluster_ctarank;" : "=r"(r));
+  return r;
+}
+__device__ __forceinline__ void cluster_barrier() {
+  asm volatile("barrier.cluster.arrive.release.aligned;\n\tbarrier.cluster.wait.acquire.aligned;" ::: "memory");
+}
+// shared::cluster address of the same shared-memory offset in CTA `rank`
+__device__ __forceinline__ uint32_t dsmem_addr(const void* local, unsigned rank) {
+  uint32_t r;
+  asm volatile("mapa.shared::cluster.u32 %0, %1, %2;"
+               : "=r"(r)
+               : "r"((uint32_t)__cvta_generic_to_shared(local)), "r"(rank));
+  return r;
+}
+// two FP32 values in one 64-bit register pair, for the packed FP32 pipe
+// (fma/mul .f32x2: one instruction for both halves)
+typedef unsigned long long f2_t;
+__device__ __forceinline__ f2_t f2_pack(float lo, float hi) {
+  f2_t d;
+  asm("mov.b64 %0, {%1, %2};" : "=l"(d) : "f"(lo), "f"(hi));
+  return d;
+}
+__device__ __forceinline__ float f2_lo(f2_t v) { return __uint_as_float((unsigned)v); }
+__device__ __forceinline__ float f2_hi(f2_t v) { return __uint_as_float((unsigned)(v >> 32)); }
+__device__ __forceinline__ f2_t f2_fma(f2_t a, f2_t b, f2_t c) {
+  f2_t d;
+  asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(d) : "l"(a), "l"(b), "l"(c));
+  return d;
+}
+__device__ __forceinline__ f2_t f2_mul(f2_t a, f2_t b) {
+  f2_t d;
+  asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
+  return d;
+}
+// 16 bytes into this CTA's shared memory (local) or another's of the cluster
+__device__ __forceinline__ void mbox_st4(bool local, uint32_t a, f2_t x, f2_t y) {
+  if (local)
+    asm volatile("st.shared.v2.b64 [%0], {%1, %2};" ::"r"(a), "l"(x), "l"(y) : "memory");
+  else
+    asm volatile("st.shared::cluster.v2.b64 [%0], {%1, %2};" ::"r"(a), "l"(x), "l"(y) : "memory");
+}
+__device__ __forceinline__ void mbox_st2(bool local, uint32_t a, f2_t x) {
+  if (local)
+    asm volatile("st.shared.b64 [%0], %1;" ::"r"(a), "l"(x) : "memory");
+  else
+    asm volatile("st.shared::cluster.b64 [%0], %1;" ::"r"(a), "l"(x) : "memory");
+}
+
+// A column in a mailbox: rows lane + 32 t of lane `lane` as 16-byte chunks
+// (t = 4q .. 4q + 3 at float offset 4 (32 q + lane)), and when RPL is not a
+// multiple of 4 the last two at 4 32 (RPL / 4) + 2 lane.  In registers the
+// rows come in pairs: pair p holds t = 2p (low half) and 2p + 1 (high).
+template <int RPL>
+__device__ __forceinline__ void mbox_send(bool local, uint32_t base, int lane, const f2_t (&c)[RPL / 2]) {
+#pragma unroll
+  for (int q = 0; q < RPL / 4; ++q) mbox_st4(local, base + (uint32_t)((q * 32 + lane) * 16), c[2 * q], c[2 * q + 1]);
+  if constexpr (RPL % 4 == 2) mbox_st2(local, base + (uint32_t)((RPL / 4) * 512 + lane * 8), c[RPL / 2 - 1]);
+}
+template <int RPL>
+__device__ __forceinline__ void mbox_recv(const float* box, int lane, f2_t (&c)[RPL / 2]) {
+  const ulonglong2* b4 = reinterpret_cast<const ulonglong2*>(box);
+#pragma unroll
+  for (int q = 0; q < RPL / 4; ++q) {
+    const ulonglong2 v = b4[q * 32 + lane];
+    c[2 * q] = v.x;
+    c[2 * q + 1] = v.y;
+  }
+  if constexpr (RPL % 4 == 2) c[RPL / 2 - 1] = reinterpret_cast<const f2_t*>(box + (RPL / 4) * 128)[lane];
+}
+
+template <int RPL>
+__global__ void __launch_bounds__(512, 1) jacobi_cluster_kernel(JacParams<float> P, int nn) {
+  static_assert(RPL % 2 == 0, "rows of a lane go in pairs");
+  constexpr int NP = RPL / 2;
+  extern __shared__ float4 jc_smem4[];
+  float* mbox = reinterpret_cast<float*>(jc_smem4);
+  __shared__ unsigned offv[3];  // the sweep's largest cosine (bits of a float >= 0), CTA 0's copy counts
+  constexpr int COL = RPL * 32;  // floats of one column in a mailbox
+  const int lane = threadIdx.x & 31, wl = threadIdx.x >> 5;
+  const int NW = blockDim.x >> 5;
+  const unsigned rank = cluster_rank();
+  const int w = (int)rank * NW + wl;
+  const int PW = nn / 2;
+  const int n = (int)P.n;
+  const float tol = (float)P.tol;
+  // mailbox of local warp l, buffer b, slot s (0 top, 1 bottom), X (0) / V (1)
+  auto box = [&](int b, int l, int sl, int xv) { return mbox + ((((size_t)b * NW + l) * 2 + sl) * 2 + xv) * COL; };
+  f2_t xt[NP], xb[NP], vt[NP], vb[NP];
+  {
+    const int ct = w, cb = nn - 1 - w;
+    auto ld = [&](const float* M, int64_t ldm, int col, int t) -> float {
+      const int i = lane + 32 * t;
+      return i < n && col < n ? M[i + (int64_t)col * ldm] : 0.0f;
+    };
+#pragma unroll
+    for (int p = 0; p < NP; ++p) {
+      xt[p] = f2_pack(ld(P.X, P.ldx, ct, 2 * p), ld(P.X, P.ldx, ct, 2 * p + 1));
+      vt[p] = f2_pack(ld(P.V, P.ldv, ct, 2 * p), ld(P.V, P.ldv, ct, 2 * p + 1));
+      xb[p] = f2_pack(ld(P.X, P.ldx, cb, 2 * p), ld(P.X, P.ldx, cb, 2 * p + 1));
+      vb[p] = f2_pack(ld(P.V, P.ldv, cb, 2 * p), ld(P.V, P.ldv, cb, 2 * p + 1));
+    }
+  }
+  if (threadIdx.x < 3) offv[threadIdx.x] = 0u;
+  // destinations of this warp's top and bottom columns
+  int dt_w = -1, dt_s = 0;  // warp 0's top stays
+  if (w >= 2) {
+    dt_w = w - 1;
+    dt_s = 0;
+  } else if (w == 1) {
+    dt_w = 0;
+    dt_s = 1;
+  }
+  const int db_w = w <= PW - 2 ? w + 1 : w, db_s = w <= PW - 2 ? 1 : 0;
+  const unsigned dt_r = dt_w >= 0 ? (unsigned)(dt_w / NW) : rank, db_r = (unsigned)(db_w / NW);
+  const uint32_t off_remote = dsmem_addr(offv, 0);
+  cluster_barrier();  // every CTA of the cluster runs before any remote store
+  int sweep = 0;
+  unsigned step_par = 0;
+  for (; sweep < P.max_sweeps; ++sweep) {
+    if (rank == 0 && threadIdx.x == 0) offv[(sweep + 1) % 3] = 0u;
+    float off = 0;
+    for (int step = 0; step < nn - 1; ++step) {
+      f2_t a2 = 0, b2 = 0, g2 = 0;
+#pragma unroll
+      for (int p = 0; p < NP; ++p) {
+        a2 = f2_fma(xt[p], xt[p], a2);
+        b2 = f2_fma(xb[p], xb[p], b2);
+        g2 = f2_fma(xt[p], xb[p], g2);
+      }
+      float a = warp_sum(f2_lo(a2) + f2_hi(a2));
+      float b = warp_sum(f2_lo(b2) + f2_hi(b2));
+      float g = warp_sum(f2_lo(g2) + f2_hi(g2));
+      if (a != 0 && b != 0) {
+        const float rel = fabsf(g) * rsqrtf(a * b);
+        if (rel > tol) {
+          off = fmaxf(off, rel);
+          // the angle need not be correctly rounded: (c, s) is a rotation
+          // to rounding whatever t is
+          const float zeta = __fdividef(b - a, 2.0f * g);
+          const float tn = copysignf(__fdividef(1.0f, fabsf(zeta) + sqrtf(fmaf(zeta, zeta, 1.0f))), zeta);
+          const float c = rsqrtf(fmaf(tn, tn, 1.0f));
+          const float sn = c * tn;
+          const f2_t cc = f2_pack(c, c), ss = f2_pack(sn, sn), ns = f2_pack(-sn, -sn);
+#pragma unroll
+          for (int p = 0; p < NP; ++p) {
+            const f2_t u = xt[p], v = xb[p];
+            xt[p] = f2_fma(ns, v, f2_mul(cc, u));
+            xb[p] = f2_fma(cc, v, f2_mul(ss, u));
+            const f2_t pu = vt[p], pv = vb[p];
+            vt[p] = f2_fma(ns, pv, f2_mul(cc, pu));
+            vb[p] = f2_fma(cc, pv, f2_mul(ss, pu));
+          }
+        }
+      }
+      if (step == nn - 2 && lane == 0) {
+        const uint32_t oa = off_remote + (uint32_t)((sweep % 3) * sizeof(unsigned));
+        asm volatile("red.shared::cluster.max.u32 [%0], %1;" ::"r"(oa), "r"(__float_as_uint(off)) : "memory");
+      }
+      const int buf = (int)(step_par & 1u);
+      if (dt_w >= 0) {
+        const bool local = dt_r == rank;
+        const uint32_t bx = (uint32_t)__cvta_generic_to_shared(box(buf, dt_w % NW, dt_s, 0));
+        const uint32_t bv = (uint32_t)__cvta_generic_to_shared(box(buf, dt_w % NW, dt_s, 1));
+        mbox_send<RPL>(local, local ? bx : dsmem_addr(box(buf, dt_w % NW, dt_s, 0), dt_r), lane, xt);
+        mbox_send<RPL>(local, local ? bv : dsmem_addr(box(buf, dt_w % NW, dt_s, 1), dt_r), lane, vt);
+      }
+      {
+        const bool local = db_r == rank;
+        const uint32_t bx = (uint32_t)__cvta_generic_to_shared(box(buf, db_w % NW, db_s, 0));
+        const uint32_t bv = (uint32_t)__cvta_generic_to_shared(box(buf, db_w % NW, db_s, 1));
+        mbox_send<RPL>(local, local ? bx : dsmem_addr(box(buf, db_w % NW, db_s, 0), db_r), lane, xb);
+        mbox_send<RPL>(local, local ? bv : dsmem_addr(box(buf, db_w % NW, db_s, 1), db_r), lane, vb);
+      }
+      cluster_barrier();
+      if (w != 0) {
+        mbox_recv<RPL>(box(buf, wl, 0, 0), lane, xt);
+        mbox_recv<RPL>(box(buf, wl, 0, 1), lane, vt);
+      }
+      mbox_recv<RPL>(box(buf, wl, 1, 0), lane, xb);
+      mbox_recv<RPL>(box(buf, wl, 1, 1), lane, vb);
+      ++step_par;
+    }
+    // the barrier of the sweep's last step ordered every warp's maximum
+    unsigned mb;
+    asm volatile("ld.shared::cluster.u32 %0, [%1];"
+                 : "=r"(mb)
+                 : "r"(off_remote + (uint32_t)((sweep % 3) * sizeof(unsigned)))
+                 : "memory");
+    if ((double)__uint_as_float(mb) <= P.stop) {
+      ++sweep;
+      break;
+    }
+  }
+  // every column is back in its slot: slot c holds column c
+  {
+    const int ct = w, cb = nn - 1 - w;
+    double st = 0, sb = 0;
+#pragma unroll
+    for (int t = 0; t < RPL; ++t) {
+      const int i = lane + 32 * t;
+      const float x0 = t & 1 ? f2_hi(xt[t / 2]) : f2_lo(xt[t / 2]);
+      const float x1 = t & 1 ? f2_hi(xb[t / 2]) : f2_lo(xb[t / 2]);
+      if (i < n) {
+        if (ct < n) {
+          P.X[i + (int64_t)ct * P.ldx] = x0;
+          P.V[i + (int64_t)ct * P.ldv] = t & 1 ? f2_hi(vt[t / 2]) : f2_lo(vt[t / 2]);
+        }
+        if (cb < n) {
+          P.X[i + (int64_t)cb * P.ldx] = x1;
+          P.V[i + (int64_t)cb * P.ldv] = t & 1 ? f2_hi(vb[t / 2]) : f2_lo(vb[t / 2]);
+        }
+      }
+      st = fma((double)x0, (double)x0, st);
+      sb = fma((double)x1, (double)x1, sb);
+    }
+    st = warp_sum(st);
+    sb = warp_sum(sb);
+    if (lane == 0) {
+      if (ct < n) P.S[ct] = (float)sqrt(st);
+      if (cb < n) P.S[cb] = (float)sqrt(sb);
+    }
+  }
+  if (rank == 0 && threadIdx.x == 0) *P.sweeps_out = sweep;
+  cluster_barrier();  // no CTA leaves while another may still read its shared memory
+}
+
 // Double-float block Jacobi: the polish sweeps of the mixed-precision path,
 // the same block-pair schedule as jacobi_block_kernel with X and V held as
 // float pairs (df64.cuh) and every dot, rotation and update done in
@@ -849,6 +1094,78 @@ __global__ void symcheck_kernel(int64_t n, const T* __restrict__ A, int64_t lda,
 
 }  // namespace
 
+// LRA_JACOBI_CLUSTER=0 keeps the FP32 sweeps on the block-pair kernel even
+// where the matrix fits one cluster (both variants stay testable)
+static bool jacobi_cluster_enabled() {
+  static const bool on = [] {
+    const char* e = std::getenv("LRA_JACOBI_CLUSTER");
+    return !(e && *e == '0');
+  }();
+  return on;
+}
+
+// The FP32 sweeps in one cluster (jacobi_cluster_kernel) when the columns fit
+// the registers of its warps: false when they do not (or no cluster of the
+// size needed can be scheduled), the caller then takes the block-pair kernel.
+static bool jacobi_cluster(lra_ctx* ctx, JacParams<float>& P) {
+  const int64_t n = P.n;
+  if (!jacobi_cluster_enabled() || n < 64 || n > 32 * 14) return false;
+  const int rpl = n <= 128 ? 4 : n <= 256 ? 8 : 14;
+  const void* kern = rpl == 4   ? (const void*)jacobi_cluster_kernel<4>
+                     : rpl == 8 ? (const void*)jacobi_cluster_kernel<8>
+                                : (const void*)jacobi_cluster_kernel<14>;
+  int optin = 0;
+  LRA_CUDA(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, ctx->device));
+  const size_t per_warp = (size_t)1024 * rpl;  // two buffers x two slots x (X, V) x 32 rpl floats
+  const int nw_max = (int)std::min<size_t>(16, ((size_t)optin - 64) / per_warp);
+  const int64_t need = (n + 1) / 2;  // column pairs
+  raise_smem_limit(ctx, kern);
+  static std::mutex mu;
+  static std::set<std::pair<const void*, int>> portable_set;
+  {
+    std::lock_guard<std::mutex> lk(mu);
+    if (!portable_set.count({kern, ctx->device})) {
+      LRA_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeNonPortableClusterSizeAllowed, 1));
+      portable_set.insert({kern, ctx->device});
+    }
+  }
+  if (ctx->tuning.jacobi_cluster == 1) return false;
+  const int c_max = ctx->tuning.jacobi_cluster > 1 ? ctx->tuning.jacobi_cluster : 16;
+  for (int c = c_max; c >= 2; --c) {
+    const int64_t nw = (need + c - 1) / c;
+    if (nw > nw_max || nw < 1) break;  // fewer CTAs only need more warps each
+    const int pw = (int)(c * nw);
+    if (pw < 2) continue;
+    const size_t smem = per_warp * (size_t)nw;
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3((unsigned)c);
+    cfg.blockDim = dim3((unsigned)(nw * 32));
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = ctx->stream;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeClusterDimension;
+    attr[0].val.clusterDim.x = (unsigned)c;
+    attr[0].val.clusterDim.y = 1;
+    attr[0].val.clusterDim.z = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    int clusters = 0;
+    if (cudaOccupancyMaxActiveClusters(&clusters, kern, &cfg) != cudaSuccess) {
+      cudaGetLastError();
+      continue;
+    }
+    if (clusters < 1) continue;
+    int nn = 2 * pw;
+    void* args[] = {&P, &nn};
+    LRA_CUDA(cudaLaunchKernelExC(&cfg, kern, args));
+    post_launch(ctx, "jacobi_cluster_kernel");
+    if (trace_on()) std::fprintf(stderr, "[lra] jacobi f32 cluster n=%lld ctas=%d warps=%lld slots=%d\n", (long long)n,
+                                 c, (long long)nw, nn);
+    return true;
+  }
+  return false;
+}
+
 template <typename T>
 void jacobi_svd(lra_ctx* ctx, int64_t n, T* X, int64_t ldx, T* V, int64_t ldv, T* S, bool quadratic_stop,
                 double stop) {
@@ -914,6 +1231,18 @@ void jacobi_svd(lra_ctx* ctx, int64_t n, T* X, int64_t ldx, T* V, int64_t ldv, T
   P.part = ctx->arena.alloc_n<double>(grid);
   P.bar = reinterpret_cast<GridBar*>(ctx->arena.alloc(sizeof(GridBar)));
   P.sweeps_out = ctx->arena.alloc_n<int>(1);
+  if constexpr (sizeof(T) == 4) {
+    if (jacobi_cluster(ctx, P)) {
+      int sweeps = 0;
+      if (trace_on()) {
+        LRA_CUDA(cudaMemcpyAsync(&sweeps, P.sweeps_out, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+        LRA_CUDA(cudaStreamSynchronize(ctx->stream));
+        std::fprintf(stderr, "[lra] jacobi f32 cluster n=%lld sweeps=%d\n", (long long)n, sweeps);
+      }
+      ctx->arena.release(mk);
+      return;
+    }
+  }
   LRA_CUDA(cudaMemsetAsync(P.bar, 0, sizeof(GridBar), ctx->stream));
   void* args[] = {&P};
   LRA_CUDA(cudaLaunchCooperativeKernel(kern, dim3(grid), dim3(nt), args, smem, ctx->stream));
@@ -1115,30 +1444,28 @@ __global__ void __launch_bounds__(256) potrf_coop_kernel(int64_t k, T* G, int64_
     if (!grid_sync(bar)) return;
     const int64_t rest = k - j0 - jb;
     if (rest <= 0) break;
-    // ---- 2. the block row: R_{b,>b} = R_bb^{-T} G_{b,>b}, a thread per column ----
+    // ---- 2. the block row: R_{b,>b} = R_bb^{-T} G_{b,>b}, a warp per column ----
+    // (lane i holds x_i; the columns are dealt out over the warps of the whole
+    // grid, since the FP64 pipe of one SM retires only a few FMAs a clock)
     for (int t = threadIdx.x; t < jb * jb; t += blockDim.x) a[t % jb][t / jb] = __ldcg(Gjj + t % jb + (t / jb) * ldg);
     __syncthreads();
     if (threadIdx.x < jb) rinv[threadIdx.x] = T(1) / a[threadIdx.x][threadIdx.x];
     __syncthreads();
-    for (int64_t col = gt; col < rest; col += GT) {
-      T* p = G + j0 + (j0 + jb + col) * ldg;
-      T x[CB];
-#pragma unroll
-      for (int i = 0; i < CB; ++i)
-        if (i < jb) x[i] = __ldcg(p + i);
-#pragma unroll
-      for (int i = 0; i < CB; ++i) {
-        if (i < jb) {
-          T s = x[i];
-#pragma unroll
-          for (int q = 0; q < CB; ++q)
-            if (q < i) s -= a[q][i] * x[q];
-          x[i] = s * rinv[i];
+    {
+      const int lane = threadIdx.x & 31;
+      const int64_t gw = (int64_t)(threadIdx.x >> 5) * gridDim.x + blockIdx.x;
+      const int64_t GW = (int64_t)gridDim.x * (blockDim.x >> 5);
+      for (int64_t col = gw; col < rest; col += GW) {
+        T* p = G + j0 + (j0 + jb + col) * ldg;
+        T x = lane < jb ? __ldcg(p + lane) : T(0);
+        // x_i = (g_i - sum_{q<i} R_qi x_q) / R_ii, the sums accumulated lane-wise
+        for (int i = 0; i < jb; ++i) {
+          const T xi = __shfl_sync(0xffffffffu, x, i) * rinv[i];
+          if (lane == i) x = xi;
+          if (lane > i && lane < jb) x -= a[i][lane] * xi;
         }
+        if (lane < jb) p[lane] = x;
       }
-#pragma unroll
-      for (int i = 0; i < CB; ++i)
-        if (i < jb) p[i] = x[i];
     }
     if (!grid_sync(bar)) return;
     // ---- 3. trailing upper triangle: G(i, j) -= sum_q R(q, i) R(q, j), j0+jb <= i <= j ----

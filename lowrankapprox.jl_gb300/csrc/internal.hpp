@@ -85,6 +85,9 @@ struct lra_tuning {
   int tc_split;
   // columns per block of the FP32 block Jacobi (4, 8, 16, 32; 0: by size)
   int jacobi_jb;
+  // largest cluster of the cluster-resident FP32 Jacobi (2..16; 0: the
+  // largest that can be scheduled; 1: never, the block-pair kernel instead)
+  int jacobi_cluster;
   // largest cosine, in units of 1e-4, at which the FP32 sweeps hand the
   // core SVD to the Gram polish (0: min(3e-2, 12 / n))
   int gram_start;
