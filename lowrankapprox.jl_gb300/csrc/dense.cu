@@ -656,7 +656,81 @@ __device__ __forceinline__ void mbox_recv(const float* box, int lane, f2_t (&c)[
   if constexpr (RPL % 4 == 2) c[RPL / 2 - 1] = reinterpret_cast<const f2_t*>(box + (RPL / 4) * 128)[lane];
 }
 
+// Point-to-point exchange: a remote store that counts its bytes on the
+// receiver's mbarrier (st.async ... complete_tx), a release arrival for a
+// sender in the receiver's own CTA, and the receiver's bounded wait.
+__device__ __forceinline__ void st_async16(uint32_t a, f2_t x, f2_t y, uint32_t mbar) {
+  asm volatile(
+      "{\n\t.reg .b32 x0, x1, y0, y1;\n\tmov.b64 {x0, x1}, %1;\n\tmov.b64 {y0, y1}, %2;\n\t"
+      "st.async.shared::cluster.mbarrier::complete_tx::bytes.v4.b32 [%0], {x0, x1, y0, y1}, [%3];\n}" ::"r"(a),
+      "l"(x), "l"(y), "r"(mbar)
+      : "memory");
+}
+__device__ __forceinline__ void st_async8(uint32_t a, f2_t x, uint32_t mbar) {
+  asm volatile("st.async.shared::cluster.mbarrier::complete_tx::bytes.b64 [%0], %1, [%2];" ::"r"(a), "l"(x), "r"(mbar)
+               : "memory");
+}
 template <int RPL>
+__device__ __forceinline__ void mbox_send_async(uint32_t base, uint32_t mbar, int lane, const f2_t (&c)[RPL / 2]) {
+#pragma unroll
+  for (int q = 0; q < RPL / 4; ++q) st_async16(base + (uint32_t)((q * 32 + lane) * 16), c[2 * q], c[2 * q + 1], mbar);
+  if constexpr (RPL % 4 == 2) st_async8(base + (uint32_t)((RPL / 4) * 512 + lane * 8), c[RPL / 2 - 1], mbar);
+}
+__device__ __forceinline__ void jc_mbar_init(uint64_t* bar, unsigned count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"((uint32_t)__cvta_generic_to_shared(bar)), "r"(count)
+               : "memory");
+}
+__device__ __forceinline__ void jc_arrive_tx(uint64_t* bar, unsigned bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(
+                   (uint32_t)__cvta_generic_to_shared(bar)),
+               "r"(bytes)
+               : "memory");
+}
+__device__ __forceinline__ void jc_arrive(uint64_t* bar) {
+  asm volatile("mbarrier.arrive.release.cta.shared::cta.b64 _, [%0];" ::"r"((uint32_t)__cvta_generic_to_shared(bar))
+               : "memory");
+}
+__device__ __forceinline__ bool jc_try_wait(uint64_t* bar, unsigned parity) {
+  unsigned ok;
+  asm volatile(
+      "{\n .reg .pred p;\n mbarrier.try_wait.parity.acquire.cluster.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, "
+      "p;\n}\n"
+      : "=r"(ok)
+      : "r"((uint32_t)__cvta_generic_to_shared(bar)), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+// Wait for a phase of `bar`, bounded: a wait that outlasts the limit, or an
+// error word already set, sets / keeps the error and gives up.  Returns
+// whether the data arrived; the whole warp agrees.
+__device__ __forceinline__ bool jc_wait(uint64_t* bar, unsigned parity, int* err) {
+  bool ok = true;
+  if (*((volatile int*)err) != 0) {
+    ok = false;
+  } else {
+    uint64_t t0 = 0;
+    int spins = 0;
+    while (!jc_try_wait(bar, parity)) {
+      if (++spins < 64) continue;
+      spins = 0;
+      if (*((volatile int*)err) != 0) {
+        ok = false;
+        break;
+      }
+      const uint64_t t = globaltimer_ns();
+      if (t0 == 0) {
+        t0 = t;
+      } else if (t - t0 > wait_limit_ns()) {
+        atomicCAS(err, 0, 6);
+        ok = false;
+        break;
+      }
+    }
+  }
+  return __all_sync(0xffffffffu, ok);
+}
+
+template <int RPL, bool P2P>
 __global__ void __launch_bounds__(512, 1) jacobi_cluster_kernel(JacParams<float> P, int nn) {
   static_assert(RPL % 2 == 0, "rows of a lane go in pairs");
   constexpr int NP = RPL / 2;
@@ -701,13 +775,37 @@ __global__ void __launch_bounds__(512, 1) jacobi_cluster_kernel(JacParams<float>
   const int db_w = w <= PW - 2 ? w + 1 : w, db_s = w <= PW - 2 ? 1 : 0;
   const unsigned dt_r = dt_w >= 0 ? (unsigned)(dt_w / NW) : rank, db_r = (unsigned)(db_w / NW);
   const uint32_t off_remote = dsmem_addr(offv, 0);
-  cluster_barrier();  // every CTA of the cluster runs before any remote store
+  // Point-to-point: full[b][l] completes a phase when the columns of local
+  // warp l for a step of parity b have arrived -- its own arrival with the
+  // bytes the remote senders store (st.async counts them), plus one release
+  // arrival from each sender in this CTA.  A sender never overwrites a
+  // buffer before its receiver has read it: every receiver of a warp also
+  // sends to it each step, so data of step s + 1 from the receiver means
+  // step s was read before step s + 2 reuses the buffer.
+  __shared__ __align__(8) uint64_t full[2][16];
+  const int ts_w = w == 0 ? -1 : (w == PW - 1 ? w : w + 1);  // sender of this warp's top
+  const int bs_w = w >= 1 ? w - 1 : 1;                       // of its bottom
+  const bool ts_local = ts_w >= 0 && ts_w / NW == (int)rank, bs_local = bs_w / NW == (int)rank;
+  const unsigned remote_bytes = (unsigned)(((ts_w >= 0 && !ts_local) ? 1 : 0) + (bs_local ? 0 : 1)) * 2u * 128u * RPL;
+  if constexpr (P2P) {
+    if (lane == 0) {
+      const unsigned cnt = 1u + (ts_local ? 1u : 0u) + (bs_local ? 1u : 0u);
+      jc_mbar_init(&full[0][wl], cnt);
+      jc_mbar_init(&full[1][wl], cnt);
+      asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+  }
+  cluster_barrier();  // every CTA of the cluster runs (its barriers set up) before any remote store
   int sweep = 0;
   unsigned step_par = 0;
+  bool alive = true;  // P2P: no wait has given up
   for (; sweep < P.max_sweeps; ++sweep) {
     if (rank == 0 && threadIdx.x == 0) offv[(sweep + 1) % 3] = 0u;
     float off = 0;
     for (int step = 0; step < nn - 1; ++step) {
+      if constexpr (P2P) {
+        if (lane == 0) jc_arrive_tx(&full[step_par & 1u][wl], remote_bytes);
+      }
       f2_t a2 = 0, b2 = 0, g2 = 0;
 #pragma unroll
       for (int p = 0; p < NP; ++p) {
@@ -745,21 +843,50 @@ __global__ void __launch_bounds__(512, 1) jacobi_cluster_kernel(JacParams<float>
         asm volatile("red.shared::cluster.max.u32 [%0], %1;" ::"r"(oa), "r"(__float_as_uint(off)) : "memory");
       }
       const int buf = (int)(step_par & 1u);
-      if (dt_w >= 0) {
-        const bool local = dt_r == rank;
-        const uint32_t bx = (uint32_t)__cvta_generic_to_shared(box(buf, dt_w % NW, dt_s, 0));
-        const uint32_t bv = (uint32_t)__cvta_generic_to_shared(box(buf, dt_w % NW, dt_s, 1));
-        mbox_send<RPL>(local, local ? bx : dsmem_addr(box(buf, dt_w % NW, dt_s, 0), dt_r), lane, xt);
-        mbox_send<RPL>(local, local ? bv : dsmem_addr(box(buf, dt_w % NW, dt_s, 1), dt_r), lane, vt);
+      if constexpr (P2P) {
+        // a local receiver's arrival releases the whole warp's stores
+        if (alive && dt_w >= 0) {
+          if (dt_r == rank) {
+            mbox_send<RPL>(true, (uint32_t)__cvta_generic_to_shared(box(buf, dt_w % NW, dt_s, 0)), lane, xt);
+            mbox_send<RPL>(true, (uint32_t)__cvta_generic_to_shared(box(buf, dt_w % NW, dt_s, 1)), lane, vt);
+            __syncwarp();
+            if (lane == 0) jc_arrive(&full[buf][dt_w % NW]);
+          } else {
+            const uint32_t mb = dsmem_addr(&full[buf][dt_w % NW], dt_r);
+            mbox_send_async<RPL>(dsmem_addr(box(buf, dt_w % NW, dt_s, 0), dt_r), mb, lane, xt);
+            mbox_send_async<RPL>(dsmem_addr(box(buf, dt_w % NW, dt_s, 1), dt_r), mb, lane, vt);
+          }
+        }
+        if (alive) {
+          if (db_r == rank) {
+            mbox_send<RPL>(true, (uint32_t)__cvta_generic_to_shared(box(buf, db_w % NW, db_s, 0)), lane, xb);
+            mbox_send<RPL>(true, (uint32_t)__cvta_generic_to_shared(box(buf, db_w % NW, db_s, 1)), lane, vb);
+            __syncwarp();
+            if (lane == 0) jc_arrive(&full[buf][db_w % NW]);
+          } else {
+            const uint32_t mb = dsmem_addr(&full[buf][db_w % NW], db_r);
+            mbox_send_async<RPL>(dsmem_addr(box(buf, db_w % NW, db_s, 0), db_r), mb, lane, xb);
+            mbox_send_async<RPL>(dsmem_addr(box(buf, db_w % NW, db_s, 1), db_r), mb, lane, vb);
+          }
+        }
+        if (alive) alive = jc_wait(&full[buf][wl], (step_par >> 1) & 1u, &P.bar->err);
+      } else {
+        if (dt_w >= 0) {
+          const bool local = dt_r == rank;
+          const uint32_t bx = (uint32_t)__cvta_generic_to_shared(box(buf, dt_w % NW, dt_s, 0));
+          const uint32_t bv = (uint32_t)__cvta_generic_to_shared(box(buf, dt_w % NW, dt_s, 1));
+          mbox_send<RPL>(local, local ? bx : dsmem_addr(box(buf, dt_w % NW, dt_s, 0), dt_r), lane, xt);
+          mbox_send<RPL>(local, local ? bv : dsmem_addr(box(buf, dt_w % NW, dt_s, 1), dt_r), lane, vt);
+        }
+        {
+          const bool local = db_r == rank;
+          const uint32_t bx = (uint32_t)__cvta_generic_to_shared(box(buf, db_w % NW, db_s, 0));
+          const uint32_t bv = (uint32_t)__cvta_generic_to_shared(box(buf, db_w % NW, db_s, 1));
+          mbox_send<RPL>(local, local ? bx : dsmem_addr(box(buf, db_w % NW, db_s, 0), db_r), lane, xb);
+          mbox_send<RPL>(local, local ? bv : dsmem_addr(box(buf, db_w % NW, db_s, 1), db_r), lane, vb);
+        }
+        cluster_barrier();
       }
-      {
-        const bool local = db_r == rank;
-        const uint32_t bx = (uint32_t)__cvta_generic_to_shared(box(buf, db_w % NW, db_s, 0));
-        const uint32_t bv = (uint32_t)__cvta_generic_to_shared(box(buf, db_w % NW, db_s, 1));
-        mbox_send<RPL>(local, local ? bx : dsmem_addr(box(buf, db_w % NW, db_s, 0), db_r), lane, xb);
-        mbox_send<RPL>(local, local ? bv : dsmem_addr(box(buf, db_w % NW, db_s, 1), db_r), lane, vb);
-      }
-      cluster_barrier();
       if (w != 0) {
         mbox_recv<RPL>(box(buf, wl, 0, 0), lane, xt);
         mbox_recv<RPL>(box(buf, wl, 0, 1), lane, vt);
@@ -768,13 +895,17 @@ __global__ void __launch_bounds__(512, 1) jacobi_cluster_kernel(JacParams<float>
       mbox_recv<RPL>(box(buf, wl, 1, 1), lane, vb);
       ++step_par;
     }
-    // the barrier of the sweep's last step ordered every warp's maximum
+    // the barrier of the sweep's last step ordered every warp's maximum (a
+    // cluster barrier a sweep on the point-to-point path); a wait that gave
+    // up anywhere ends the sweeps everywhere at the same point
+    if constexpr (P2P) cluster_barrier();
     unsigned mb;
     asm volatile("ld.shared::cluster.u32 %0, [%1];"
                  : "=r"(mb)
                  : "r"(off_remote + (uint32_t)((sweep % 3) * sizeof(unsigned)))
                  : "memory");
-    if ((double)__uint_as_float(mb) <= P.stop) {
+    const bool failed = P2P && *((volatile int*)&P.bar->err) != 0;
+    if ((double)__uint_as_float(mb) <= P.stop || failed) {
       ++sweep;
       break;
     }
@@ -1111,13 +1242,19 @@ static bool jacobi_cluster(lra_ctx* ctx, JacParams<float>& P) {
   const int64_t n = P.n;
   if (!jacobi_cluster_enabled() || n < 64 || n > 32 * 14) return false;
   const int rpl = n <= 128 ? 4 : n <= 256 ? 8 : 14;
-  const void* kern = rpl == 4   ? (const void*)jacobi_cluster_kernel<4>
-                     : rpl == 8 ? (const void*)jacobi_cluster_kernel<8>
-                                : (const void*)jacobi_cluster_kernel<14>;
+  // the columns move point to point (mbarriers) unless LRA_JACOBI_P2P=0
+  // asks for a cluster barrier every step
+  static const bool p2p = [] {
+    const char* e = std::getenv("LRA_JACOBI_P2P");
+    return !(e && *e == '0');
+  }();
+  const void* kern = rpl == 4   ? (p2p ? (const void*)jacobi_cluster_kernel<4, true> : (const void*)jacobi_cluster_kernel<4, false>)
+                     : rpl == 8 ? (p2p ? (const void*)jacobi_cluster_kernel<8, true> : (const void*)jacobi_cluster_kernel<8, false>)
+                                : (p2p ? (const void*)jacobi_cluster_kernel<14, true> : (const void*)jacobi_cluster_kernel<14, false>);
   int optin = 0;
   LRA_CUDA(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, ctx->device));
   const size_t per_warp = (size_t)1024 * rpl;  // two buffers x two slots x (X, V) x 32 rpl floats
-  const int nw_max = (int)std::min<size_t>(16, ((size_t)optin - 64) / per_warp);
+  const int nw_max = (int)std::min<size_t>(16, ((size_t)optin - 1024) / per_warp);  // static smem below 1 KB
   const int64_t need = (n + 1) / 2;  // column pairs
   raise_smem_limit(ctx, kern);
   static std::mutex mu;
@@ -1231,19 +1368,21 @@ void jacobi_svd(lra_ctx* ctx, int64_t n, T* X, int64_t ldx, T* V, int64_t ldv, T
   P.part = ctx->arena.alloc_n<double>(grid);
   P.bar = reinterpret_cast<GridBar*>(ctx->arena.alloc(sizeof(GridBar)));
   P.sweeps_out = ctx->arena.alloc_n<int>(1);
+  LRA_CUDA(cudaMemsetAsync(P.bar, 0, sizeof(GridBar), ctx->stream));
   if constexpr (sizeof(T) == 4) {
     if (jacobi_cluster(ctx, P)) {
       int sweeps = 0;
-      if (trace_on()) {
+      GridBar hb;
+      LRA_CUDA(cudaMemcpyAsync(&hb, P.bar, sizeof(GridBar), cudaMemcpyDeviceToHost, ctx->stream));
+      if (trace_on())
         LRA_CUDA(cudaMemcpyAsync(&sweeps, P.sweeps_out, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
-        LRA_CUDA(cudaStreamSynchronize(ctx->stream));
-        std::fprintf(stderr, "[lra] jacobi f32 cluster n=%lld sweeps=%d\n", (long long)n, sweeps);
-      }
+      LRA_CUDA(cudaStreamSynchronize(ctx->stream));
       ctx->arena.release(mk);
+      if (hb.err != 0) fail(LRA_ETIMEDOUT, "jacobi: a column exchange between the cluster's CTAs timed out");
+      if (trace_on()) std::fprintf(stderr, "[lra] jacobi f32 cluster n=%lld sweeps=%d\n", (long long)n, sweeps);
       return;
     }
   }
-  LRA_CUDA(cudaMemsetAsync(P.bar, 0, sizeof(GridBar), ctx->stream));
   void* args[] = {&P};
   LRA_CUDA(cudaLaunchCooperativeKernel(kern, dim3(grid), dim3(nt), args, smem, ctx->stream));
   post_launch(ctx, pair_cta ? "jacobi_pair_kernel" : (block ? "jacobi_block_kernel" : "jacobi_kernel"));
