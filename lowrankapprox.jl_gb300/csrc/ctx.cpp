@@ -158,6 +158,7 @@ bool trace_on() {
 //   tc_split <most K parts of the tensor-core sketch; 0: as many as fill the SMs>
 //   jacobi_jb <columns per FP32 Jacobi block: 4, 8, 16, 32; 0: by size>
 //   jacobi_cluster <largest cluster of the in-cluster FP32 Jacobi, 2..16; 0: largest schedulable; 1: off>
+//   trsm_inv <0: FP64 triangular solves on the tensor-core path by the explicit inverse; 1: substitution>
 //   gram_start <cosine x 1e4 where the FP32 Jacobi sweeps stop; 0: min(3e-2, 12 / n)>
 // lowrankapprox/autotune.py writes it from its sweeps; unknown keys and
 // out-of-range values are ignored, so an old table never breaks a newer
@@ -173,6 +174,7 @@ static void tuning_defaults(lra_tuning* t) {
   t->tc_split = 0;
   t->jacobi_jb = 0;
   t->jacobi_cluster = 0;
+  t->trsm_inv = 0;
   t->gram_start = 0;
 }
 
@@ -210,6 +212,11 @@ bool set_tuning(lra_tuning* t, const char* key, int64_t index, int64_t value) {
   if (!std::strcmp(key, "gram_start")) {
     if (value < 0 || value > 5000) return false;
     t->gram_start = (int)value;
+    return true;
+  }
+  if (!std::strcmp(key, "trsm_inv")) {
+    if (value != 0 && value != 1) return false;
+    t->trsm_inv = (int)value;
     return true;
   }
   if (!std::strcmp(key, "jacobi_cluster")) {
@@ -261,7 +268,7 @@ void load_tuning(lra_tuning* t, std::string* source) {
       int64_t lb = -1, v = 0;
       if (in >> lb >> v) used += set_tuning(t, "srft_wide", lb, v);
     } else if (key == "qr_steps" || key == "qr_sms" || key == "tc_split" || key == "jacobi_jb" ||
-               key == "jacobi_cluster" || key == "gram_start") {
+               key == "jacobi_cluster" || key == "trsm_inv" || key == "gram_start") {
       int64_t v = 0;
       if (in >> v) used += set_tuning(t, key.c_str(), 0, v);
     }
@@ -280,6 +287,7 @@ std::string tuning_text(const lra_tuning& t) {
   o << "tc_split " << t.tc_split << '\n';
   o << "jacobi_jb " << t.jacobi_jb << '\n';
   o << "jacobi_cluster " << t.jacobi_cluster << '\n';
+  o << "trsm_inv " << t.trsm_inv << '\n';
   o << "gram_start " << t.gram_start << '\n';
   return o.str();
 }

@@ -1784,11 +1784,134 @@ void trsm_left_diag(lra_ctx* ctx, int jb, int64_t nrhs, const T* R, int64_t ldr,
   post_launch(ctx, "trsm_left_diag_kernel");
 }
 
+namespace {
+
+// Y = R^-1 D with D = diag(R), the inverse of the unit upper triangular
+// D^-1 R (k x k, strictly lower part zero), a CTA per column: column j
+// solves R y = R_jj e_j by column-oriented back substitution -- y_j = 1,
+// then a_i -= R_iq y_q for i < q and y_q = a_q / R_qq from q = j down --
+// with the partial sums a_i in the registers of the thread owning row i
+// (rows tid + 128 u) and the finished y in shared memory; the column of R a
+// step needs is loaded one step ahead.  A graded R (|R_iq| <= |R_ii|, as a
+// pivoted QR leaves it) has an inverse whose rows span its whole diagonal
+// range, which a GEMM that scales each row by its largest entry would
+// truncate; R^-1 D has entries of order one.
+constexpr int kTiNT = 128;
+constexpr int kTiRows = 16;  // rows a thread: k up to 2048
+
+template <typename T>
+__global__ void __launch_bounds__(kTiNT) tri_inv_upper_kernel(int64_t k, const T* __restrict__ R, int64_t ldr,
+                                                              T* __restrict__ Y, int64_t ldy) {
+  extern __shared__ unsigned char ti_smem[];
+  T* ys = reinterpret_cast<T*>(ti_smem);  // k
+  const int tid = threadIdx.x;
+  const int U = (int)((k + kTiNT - 1) / kTiNT);
+  for (int64_t j = blockIdx.x; j < k; j += gridDim.x) {
+    T a[kTiRows], rc[kTiRows];
+#pragma unroll
+    for (int u = 0; u < kTiRows; ++u) {
+      const int64_t i = tid + (int64_t)kTiNT * u;
+      a[u] = T(0);
+      rc[u] = u < U && i < j ? R[i + j * ldr] : T(0);
+    }
+    if (tid == 0) ys[j] = T(1);
+    __syncthreads();
+    for (int64_t q = j; q > 0; --q) {
+      const T yq = ys[q];
+      const T rqq = R[(q - 1) + (q - 1) * ldr];
+      T rn[kTiRows];
+#pragma unroll
+      for (int u = 0; u < kTiRows; ++u) {
+        const int64_t i = tid + (int64_t)kTiNT * u;
+        rn[u] = u < U && i < q - 1 ? R[i + (q - 1) * ldr] : T(0);
+      }
+#pragma unroll
+      for (int u = 0; u < kTiRows; ++u) {
+        const int64_t i = tid + (int64_t)kTiNT * u;
+        if (u < U && i < q) {
+          a[u] = fma(-rc[u], yq, a[u]);
+          if (i == q - 1) ys[q - 1] = a[u] / rqq;
+        }
+        rc[u] = rn[u];
+      }
+      __syncthreads();
+    }
+    for (int64_t i = tid; i < k; i += kTiNT) Y[i + j * ldy] = i <= j ? ys[i] : T(0);
+    __syncthreads();  // ys is rewritten for the next column
+  }
+}
+
+// dst = src with row i (side 'l') or column j (side 'r') divided by R's
+// diagonal entry, as the substitution divides
+template <typename T>
+__global__ void div_by_diag_kernel(int64_t m, int64_t n, const T* __restrict__ R, int64_t ldr, bool rows,
+                                   const T* __restrict__ src, int64_t lds, T* __restrict__ dst, int64_t ldd) {
+  const int64_t total = m * n;
+  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < total; t += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t i = t % m, j = t / m;
+    const int64_t d = rows ? i : j;
+    dst[i + j * ldd] = src[i + j * lds] / R[d + d * ldr];
+  }
+}
+
+}  // namespace
+
+template <typename T>
+void div_by_diag(lra_ctx* ctx, int64_t m, int64_t n, const T* R, int64_t ldr, char side, const T* src, int64_t lds,
+                 T* dst, int64_t ldd) {
+  if (m <= 0 || n <= 0) return;
+  const unsigned g = (unsigned)std::max<int64_t>(1, std::min<int64_t>((m * n + 255) / 256, ctx->num_sms * 8));
+  div_by_diag_kernel<T><<<g, 256, 0, ctx->stream>>>(m, n, R, ldr, side == 'l', src, lds, dst, ldd);
+  post_launch(ctx, "div_by_diag_kernel");
+}
+template void div_by_diag<float>(lra_ctx*, int64_t, int64_t, const float*, int64_t, char, const float*, int64_t,
+                                 float*, int64_t);
+template void div_by_diag<double>(lra_ctx*, int64_t, int64_t, const double*, int64_t, char, const double*, int64_t,
+                                  double*, int64_t);
+
+template <typename T>
+bool tri_inv_upper(lra_ctx* ctx, int64_t k, const T* R, int64_t ldr, T* Y, int64_t ldy) {
+  if (k <= 0) return true;
+  if (k > (int64_t)kTiNT * kTiRows) return false;
+  const size_t smem = (size_t)k * sizeof(T);
+  if (smem > 48 * 1024) raise_smem_limit(ctx, (const void*)tri_inv_upper_kernel<T>);
+  tri_inv_upper_kernel<T><<<(unsigned)k, kTiNT, smem, ctx->stream>>>(k, R, ldr, Y, ldy);
+  post_launch(ctx, "tri_inv_upper_kernel");
+  return true;
+}
+
+template bool tri_inv_upper<float>(lra_ctx*, int64_t, const float*, int64_t, float*, int64_t);
+template bool tri_inv_upper<double>(lra_ctx*, int64_t, const double*, int64_t, double*, int64_t);
+
+// Whether a triangular solve with a k x k factor and `other` right-hand
+// sides should multiply by the explicit inverse instead: on the tensor-core
+// path for FP64, where the substitution's diagonal blocks run on the FP64
+// pipe (a few FMAs a clock per SM) and the inverse costs one GEMM
+template <typename T>
+bool trsm_by_inverse(const lra_ctx* ctx, int64_t k, int64_t other) {
+  if (sizeof(T) != 8 || !ctx->gemm_tc || ctx->tuning.trsm_inv == 1) return false;
+  return k > 2 * CB && k <= (int64_t)kTiNT * kTiRows && tc_gemm_worthwhile(other, k, k);
+}
+template bool trsm_by_inverse<float>(const lra_ctx*, int64_t, int64_t);
+template bool trsm_by_inverse<double>(const lra_ctx*, int64_t, int64_t);
+
 // X <- X triu(R)^{-1}, recursive like trsm_upper: the leading half, a GEMM
-// update of the trailing columns, the trailing half
+// update of the trailing columns, the trailing half; on the tensor-core
+// path X times the explicit inverse
 template <typename T>
 void trsm_right_upper(lra_ctx* ctx, int64_t m, int64_t k, const T* R, int64_t ldr, T* X, int64_t ldx) {
   if (m <= 0 || k <= 0) return;
+  if (trsm_by_inverse<T>(ctx, k, m)) {
+    const ArenaMark mk = ctx->arena.mark();
+    T* Y = ctx->arena.alloc_n<T>((size_t)k * k);
+    T* W = ctx->arena.alloc_n<T>((size_t)m * k);
+    // X R^-1 = (X Y) D^-1 with Y = R^-1 D
+    tri_inv_upper<T>(ctx, k, R, ldr, Y, k);
+    gemm<T>(ctx, 'n', 'n', m, k, k, T(1), X, ldx, Y, k, T(0), W, m);
+    div_by_diag<T>(ctx, m, k, R, ldr, 'r', W, m, X, ldx);
+    ctx->arena.release(mk);  // stream-ordered reuse
+    return;
+  }
   if (k <= CB) {
     const unsigned g = (unsigned)std::max<int64_t>(1, std::min<int64_t>((m + 127) / 128, ctx->num_sms * 8));
     trsm_right_diag_kernel<T><<<g, 128, 0, ctx->stream>>>(m, (int)k, R, ldr, X, ldx);

@@ -88,6 +88,9 @@ struct lra_tuning {
   // largest cluster of the cluster-resident FP32 Jacobi (2..16; 0: the
   // largest that can be scheduled; 1: never, the block-pair kernel instead)
   int jacobi_cluster;
+  // FP64 triangular solves on the tensor-core path: 0 multiply by the
+  // explicit inverse (k from 65 to 2048), 1 blocked substitution
+  int trsm_inv;
   // largest cosine, in units of 1e-4, at which the FP32 sweeps hand the
   // core SVD to the Gram polish (0: min(3e-2, 12 / n))
   int gram_start;
@@ -284,9 +287,20 @@ void jacobi_svd(lra_ctx* ctx, int64_t n, T* X, int64_t ldx, T* V, int64_t ldv, T
 // not numerically positive definite
 template <typename T>
 bool potrf_upper(lra_ctx* ctx, int64_t k, T* G, int64_t ldg);
-// X (m x k) <- X triu(R)^{-1}, blocked
+// X (m x k) <- X triu(R)^{-1}, blocked (or times the explicit inverse, see
+// trsm_by_inverse)
 template <typename T>
 void trsm_right_upper(lra_ctx* ctx, int64_t m, int64_t k, const T* R, int64_t ldr, T* X, int64_t ldx);
+// Y = triu(R)^{-1} diag(R) (k x k, ld ldy); false when k is beyond the
+// kernel (2048)
+template <typename T>
+bool tri_inv_upper(lra_ctx* ctx, int64_t k, const T* R, int64_t ldr, T* Y, int64_t ldy);
+// dst = src with rows (side 'l') or columns ('r') divided by diag(R)
+template <typename T>
+void div_by_diag(lra_ctx* ctx, int64_t m, int64_t n, const T* R, int64_t ldr, char side, const T* src, int64_t lds,
+                 T* dst, int64_t ldd);
+template <typename T>
+bool trsm_by_inverse(const lra_ctx* ctx, int64_t k, int64_t other);
 
 // post.cu: X (m x k) <- X Rpre^{-1} (if Rpre), then `passes` Cholesky QR
 // passes; on exit X is orthonormal and the input equals X Rc Rpre.  False

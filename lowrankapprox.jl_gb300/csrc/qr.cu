@@ -3150,6 +3150,18 @@ int64_t geqp3_adap(lra_ctx* ctx, int64_t m, int64_t n, T* A, int64_t lda, int64_
 template <typename T>
 void trsm_upper(lra_ctx* ctx, int64_t k, int64_t nrhs, const T* R, int64_t ldr, T* X, int64_t ldx) {
   if (k <= 0 || nrhs <= 0) return;
+  if (trsm_by_inverse<T>(ctx, k, nrhs)) {
+    // R^-1 X = Y (D^-1 X) with Y = R^-1 D (entries of order one), a
+    // tensor-core GEMM
+    const ArenaMark mk = ctx->arena.mark();
+    T* Y = ctx->arena.alloc_n<T>((size_t)k * k);
+    T* W = ctx->arena.alloc_n<T>((size_t)k * nrhs);
+    tri_inv_upper<T>(ctx, k, R, ldr, Y, k);
+    div_by_diag<T>(ctx, k, nrhs, R, ldr, 'l', X, ldx, W, k);
+    gemm<T>(ctx, 'n', 'n', k, nrhs, k, T(1), Y, k, W, k, T(0), X, ldx);
+    ctx->arena.release(mk);
+    return;
+  }
   if (k <= 32) {
     trsm_left_diag(ctx, (int)k, nrhs, R, ldr, X, ldx);
     return;
