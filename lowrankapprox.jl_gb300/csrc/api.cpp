@@ -862,6 +862,23 @@ bool skeleton_qr(lra_ctx* ctx, const Fact<T>& F, int64_t M, T* Ask, T* RA, int d
   return true;
 }
 
+// skeleton_qr and R_v = chol(I + T T^T) (chol_v); with one Cholesky QR
+// pass the two factorizations share a launch
+template <typename T>
+bool skeleton_qr_v(lra_ctx* ctx, const Fact<T>& F, int64_t M, T* Ask, T* RA, int64_t nr, T* Rv, int dtype) {
+  const int64_t k = F.k, kk = std::max<int64_t>(k, 1);
+  if (F.swaps > 0) return false;
+  if (!(dtype == LRA_F64 && F.embed)) return skeleton_qr<T>(ctx, F, M, Ask, RA, dtype) && chol_v<T>(ctx, k, nr, F.T_, Rv);
+  T* Rc = ctx->arena.alloc_n<T>((size_t)kk * kk);
+  if (!cholqr1_and_chol_v<T>(ctx, M, k, Ask, std::max<int64_t>(M, 1), F.B, F.ld, Rc, nr, F.T_, Rv)) return false;
+  // R_A = Rc R11
+  T* R11 = ctx->arena.alloc_n<T>((size_t)kk * kk);
+  copy_matrix(ctx, k, k, F.B, F.ld, R11, kk);
+  zero_lower(ctx, k, k, R11, kk);
+  gemm<T>(ctx, 'n', 'n', k, k, k, T(1), Rc, kk, R11, kk, T(0), RA, kk);
+  return true;
+}
+
 // getcols(trans, A, idx): M x k device matrix
 template <typename T>
 T* getcols(lra_ctx* ctx, char trans, int64_t m, int64_t n, const DMat<T>& A, const int64_t* idx, int64_t k) {
@@ -3035,10 +3052,8 @@ lra_psvd* psvd_dev(lra_ctx* ctx, const lra_opts& o, char trans, int64_t m, int64
     T* RA = ctx->arena.alloc_n<T>((size_t)ldk * ldk);
     T* Rv = ctx->arena.alloc_n<T>((size_t)ldk * ldk);
     tmark("gather");
-    bool ok = skeleton_qr<T>(ctx, F, M, Q, RA, dtype);
-    tmark("skeleton cholesky qr");
-    ok = ok && chol_v<T>(ctx, k, N - k, F.T_, Rv);
-    tmark("chol(I + T T')");
+    const bool ok = skeleton_qr_v<T>(ctx, F, M, Q, RA, N - k, Rv, dtype);
+    tmark("skeleton cholesky qr, chol(I + T T')");
     if (ok) {
       T* Mm = ctx->arena.alloc_n<T>((size_t)ldk * ldk);
       gemm<T>(ctx, 'n', 't', k, k, k, T(1), RA, ldk, Rv, ldk, T(0), Mm, ldk);

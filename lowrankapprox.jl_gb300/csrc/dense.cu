@@ -1531,87 +1531,120 @@ __global__ void potrf_diag_kernel(int jb, T* G, int64_t ldg, int* bad) {
   }
 }
 
-// The whole blocked right-looking Cholesky in one cooperative launch: for
-// each 32-wide diagonal block, CTA 0 factors the block in shared memory (as
-// potrf_diag_kernel), the grid solves the block row with a thread per column
-// (as potrf_panel_kernel) and updates the upper trailing triangle, with a
-// bounded grid barrier between the phases.  Three barriers per block
-// instead of three launches and a GEMM.
+// The whole blocked right-looking Cholesky in one cooperative launch, of
+// one matrix or two independent ones at once (their sequential diagonal
+// blocks then overlap): for each 32-wide diagonal block, CTA m factors
+// matrix m's block in shared memory (as potrf_diag_kernel), the grid solves
+// the block rows with a warp per column (lane i holds x_i; the columns of
+// both matrices dealt out over every warp, since the FP64 pipe of one SM
+// retires only a few FMAs a clock) and updates the upper trailing
+// triangles, with a bounded grid barrier between the phases.
 template <typename T>
-__global__ void __launch_bounds__(256) potrf_coop_kernel(int64_t k, T* G, int64_t ldg, int* bad, GridBar* bar) {
-  __shared__ T a[CB][CB + 1];
-  __shared__ T rinv[CB];
+struct PotrfJobs {
+  int n;           // 1 or 2
+  int64_t k[2];
+  T* G[2];
+  int64_t ldg[2];
+  int* bad;        // one flag per matrix
+};
+
+template <typename T>
+__global__ void __launch_bounds__(256) potrf_coop_kernel(PotrfJobs<T> J, GridBar* bar) {
+  __shared__ T a[2][CB][CB + 1];
+  __shared__ T rinv[2][CB];
   __shared__ T s_inv;
   const int64_t gt = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   const int64_t GT = (int64_t)gridDim.x * blockDim.x;
-  for (int64_t j0 = 0; j0 < k; j0 += CB) {
-    const int jb = (int)min((int64_t)CB, k - j0);
-    T* Gjj = G + j0 + j0 * ldg;
-    // ---- 1. the diagonal block, CTA 0 ----
-    if (blockIdx.x == 0) {
+  const int64_t kmax = J.n > 1 ? max(J.k[0], J.k[1]) : J.k[0];
+  for (int64_t j0 = 0; j0 < kmax; j0 += CB) {
+    // ---- 1. the diagonal blocks, CTA m for matrix m ----
+    for (int m = 0; m < J.n; ++m) {
+      if ((int)blockIdx.x != m % (int)gridDim.x || j0 >= J.k[m]) continue;
+      const int jb = (int)min((int64_t)CB, J.k[m] - j0);
+      const int64_t ldg = J.ldg[m];
+      T* Gjj = J.G[m] + j0 + j0 * ldg;
       // every read of G goes around L1: other CTAs wrote it in earlier phases
       for (int t = threadIdx.x; t < jb * jb; t += blockDim.x)
-        a[t % jb][t / jb] = __ldcg(Gjj + t % jb + (t / jb) * ldg);
+        a[m][t % jb][t / jb] = __ldcg(Gjj + t % jb + (t / jb) * ldg);
       __syncthreads();
       for (int c = 0; c < jb; ++c) {
         if (threadIdx.x == 0) {
-          T d = a[c][c];
+          T d = a[m][c][c];
           if (!(d > T(0))) {
-            atomicExch(bad, 1);
+            atomicExch(J.bad + m, 1);
             d = T(1);
           }
           const T r = sqrt(d);
-          a[c][c] = r;
+          a[m][c][c] = r;
           s_inv = T(1) / r;
         }
         __syncthreads();
         const T inv = s_inv;
-        for (int j = c + 1 + threadIdx.x; j < jb; j += blockDim.x) a[c][j] *= inv;
+        for (int j = c + 1 + threadIdx.x; j < jb; j += blockDim.x) a[m][c][j] *= inv;
         __syncthreads();
         const int w = jb - c - 1;
         for (int t = threadIdx.x; t < w * w; t += blockDim.x) {
           const int i = c + 1 + t % w, j = c + 1 + t / w;
-          if (i <= j) a[i][j] -= a[c][i] * a[c][j];
+          if (i <= j) a[m][i][j] -= a[m][c][i] * a[m][c][j];
         }
         __syncthreads();
       }
       for (int t = threadIdx.x; t < jb * jb; t += blockDim.x) {
         const int i = t % jb, j = t / jb;
-        if (i <= j) Gjj[i + j * ldg] = a[i][j];
+        if (i <= j) Gjj[i + j * ldg] = a[m][i][j];
       }
     }
     if (!grid_sync(bar)) return;
-    const int64_t rest = k - j0 - jb;
-    if (rest <= 0) break;
-    // ---- 2. the block row: R_{b,>b} = R_bb^{-T} G_{b,>b}, a warp per column ----
-    // (lane i holds x_i; the columns are dealt out over the warps of the whole
-    // grid, since the FP64 pipe of one SM retires only a few FMAs a clock)
-    for (int t = threadIdx.x; t < jb * jb; t += blockDim.x) a[t % jb][t / jb] = __ldcg(Gjj + t % jb + (t / jb) * ldg);
+    int64_t rest[2] = {0, 0};
+    int jbm[2] = {0, 0};
+    for (int m = 0; m < J.n; ++m) {
+      if (j0 >= J.k[m]) continue;
+      jbm[m] = (int)min((int64_t)CB, J.k[m] - j0);
+      rest[m] = J.k[m] - j0 - jbm[m];
+    }
+    if (rest[0] + rest[1] <= 0) break;
+    // ---- 2. the block rows: R_{b,>b} = R_bb^{-T} G_{b,>b}, a warp per column ----
+    for (int m = 0; m < J.n; ++m) {
+      if (rest[m] <= 0) continue;
+      const int jb = jbm[m];
+      const T* Gjj = J.G[m] + j0 + j0 * J.ldg[m];
+      for (int t = threadIdx.x; t < jb * jb; t += blockDim.x)
+        a[m][t % jb][t / jb] = __ldcg(Gjj + t % jb + (t / jb) * J.ldg[m]);
+    }
     __syncthreads();
-    if (threadIdx.x < jb) rinv[threadIdx.x] = T(1) / a[threadIdx.x][threadIdx.x];
+    for (int m = 0; m < J.n; ++m)
+      if (rest[m] > 0 && threadIdx.x < jbm[m]) rinv[m][threadIdx.x] = T(1) / a[m][threadIdx.x][threadIdx.x];
     __syncthreads();
     {
       const int lane = threadIdx.x & 31;
       const int64_t gw = (int64_t)(threadIdx.x >> 5) * gridDim.x + blockIdx.x;
       const int64_t GW = (int64_t)gridDim.x * (blockDim.x >> 5);
-      for (int64_t col = gw; col < rest; col += GW) {
-        T* p = G + j0 + (j0 + jb + col) * ldg;
+      for (int64_t cc = gw; cc < rest[0] + rest[1]; cc += GW) {
+        const int m = cc < rest[0] ? 0 : 1;
+        const int64_t col = m == 0 ? cc : cc - rest[0];
+        const int jb = jbm[m];
+        T* p = J.G[m] + j0 + (j0 + jb + col) * J.ldg[m];
         T x = lane < jb ? __ldcg(p + lane) : T(0);
         // x_i = (g_i - sum_{q<i} R_qi x_q) / R_ii, the sums accumulated lane-wise
         for (int i = 0; i < jb; ++i) {
-          const T xi = __shfl_sync(0xffffffffu, x, i) * rinv[i];
+          const T xi = __shfl_sync(0xffffffffu, x, i) * rinv[m][i];
           if (lane == i) x = xi;
-          if (lane > i && lane < jb) x -= a[i][lane] * xi;
+          if (lane > i && lane < jb) x -= a[m][i][lane] * xi;
         }
         if (lane < jb) p[lane] = x;
       }
     }
     if (!grid_sync(bar)) return;
-    // ---- 3. trailing upper triangle: G(i, j) -= sum_q R(q, i) R(q, j), j0+jb <= i <= j ----
-    const int64_t o = j0 + jb;
-    for (int64_t t = gt; t < rest * rest; t += GT) {
-      const int64_t i = t % rest, j = t / rest;
+    // ---- 3. trailing upper triangles: G(i, j) -= sum_q R(q, i) R(q, j), j0+jb <= i <= j ----
+    const int64_t n0 = rest[0] * rest[0];
+    for (int64_t t = gt; t < n0 + rest[1] * rest[1]; t += GT) {
+      const int m = t < n0 ? 0 : 1;
+      const int64_t tt = m == 0 ? t : t - n0, r = rest[m];
+      const int64_t i = tt % r, j = tt / r;
       if (i > j) continue;
+      const int jb = jbm[m];
+      const int64_t ldg = J.ldg[m], o = j0 + jb;
+      T* G = J.G[m];
       const T* ri = G + j0 + (o + i) * ldg;
       const T* rj = G + j0 + (o + j) * ldg;
       T s = 0;
@@ -1727,32 +1760,63 @@ __global__ void trsm_left_diag_kernel(int jb, int64_t nrhs, const T* Rbb, int64_
 
 }  // namespace
 
+// one or two Cholesky factorizations G_m = R_m^T R_m in place (upper R,
+// lower part zeroed) in one cooperative launch; ok[m] false when G_m is not
+// numerically positive definite
 template <typename T>
-bool potrf_upper(lra_ctx* ctx, int64_t k, T* G, int64_t ldg) {
-  if (k <= 0) return true;
+void potrf_upper_batch(lra_ctx* ctx, int n, const int64_t* k, T* const* G, const int64_t* ldg, bool* ok) {
   const ArenaMark mk = ctx->arena.mark();
-  int* bad = ctx->arena.alloc_n<int>(1);
-  LRA_CUDA(cudaMemsetAsync(bad, 0, sizeof(int), ctx->stream));
-  if (k > CB) {
+  int* bad = ctx->arena.alloc_n<int>(2);
+  LRA_CUDA(cudaMemsetAsync(bad, 0, 2 * sizeof(int), ctx->stream));
+  PotrfJobs<T> J{};
+  J.n = 0;
+  J.bad = bad;
+  int slot[2] = {-1, -1};
+  for (int m = 0; m < n; ++m) {
+    ok[m] = true;
+    if (k[m] <= 0) continue;
+    slot[m] = J.n;
+    J.k[J.n] = k[m];
+    J.G[J.n] = G[m];
+    J.ldg[J.n] = ldg[m];
+    ++J.n;
+  }
+  if (J.n > 0) {
     int per_sm = 0;
     LRA_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, potrf_coop_kernel<T>, 256, 0));
-    const int grid = std::max(1, std::min(ctx->num_sms, ctx->num_sms * per_sm));
+    const int grid = std::max(J.n, std::min(ctx->num_sms, ctx->num_sms * per_sm));
     GridBar* bar = reinterpret_cast<GridBar*>(ctx->arena.alloc(sizeof(GridBar)));
     LRA_CUDA(cudaMemsetAsync(bar, 0, sizeof(GridBar), ctx->stream));
-    void* args[] = {&k, &G, &ldg, &bad, &bar};
+    void* args[] = {&J, &bar};
     LRA_CUDA(cudaLaunchCooperativeKernel((const void*)potrf_coop_kernel<T>, dim3(grid), dim3(256), args, 0,
                                          ctx->stream));
     post_launch(ctx, "potrf_coop_kernel");
-    zero_lower(ctx, k, k, G, ldg);
-    int h = 0;
+    for (int m = 0; m < J.n; ++m) zero_lower(ctx, J.k[m], J.k[m], J.G[m], J.ldg[m]);
+    int h[2] = {0, 0};
     GridBar hb;
-    LRA_CUDA(cudaMemcpyAsync(&h, bad, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+    LRA_CUDA(cudaMemcpyAsync(h, bad, 2 * sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
     LRA_CUDA(cudaMemcpyAsync(&hb, bar, sizeof(GridBar), cudaMemcpyDeviceToHost, ctx->stream));
     LRA_CUDA(cudaStreamSynchronize(ctx->stream));
     ctx->arena.release(mk);
     if (hb.err != 0) fail(LRA_ETIMEDOUT, "potrf: a grid barrier timed out");
-    return h == 0;
+    for (int m = 0; m < n; ++m)
+      if (slot[m] >= 0) ok[m] = h[slot[m]] == 0;
+    return;
   }
+  ctx->arena.release(mk);
+}
+
+template <typename T>
+bool potrf_upper(lra_ctx* ctx, int64_t k, T* G, int64_t ldg) {
+  if (k <= 0) return true;
+  if (k > CB) {
+    bool ok = true;
+    potrf_upper_batch<T>(ctx, 1, &k, &G, &ldg, &ok);
+    return ok;
+  }
+  const ArenaMark mk = ctx->arena.mark();
+  int* bad = ctx->arena.alloc_n<int>(1);
+  LRA_CUDA(cudaMemsetAsync(bad, 0, sizeof(int), ctx->stream));
   for (int64_t j0 = 0; j0 < k; j0 += CB) {
     const int jb = (int)std::min<int64_t>(CB, k - j0);
     T* Gjj = G + j0 + j0 * ldg;
@@ -1926,6 +1990,8 @@ void trsm_right_upper(lra_ctx* ctx, int64_t m, int64_t k, const T* R, int64_t ld
 
 template bool potrf_upper<float>(lra_ctx*, int64_t, float*, int64_t);
 template bool potrf_upper<double>(lra_ctx*, int64_t, double*, int64_t);
+template void potrf_upper_batch<float>(lra_ctx*, int, const int64_t*, float* const*, const int64_t*, bool*);
+template void potrf_upper_batch<double>(lra_ctx*, int, const int64_t*, double* const*, const int64_t*, bool*);
 template void trsm_right_upper<float>(lra_ctx*, int64_t, int64_t, const float*, int64_t, float*, int64_t);
 template void trsm_right_upper<double>(lra_ctx*, int64_t, int64_t, const double*, int64_t, double*, int64_t);
 // ---- T = R11^{-1} R12 by back substitution, a thread per right-hand side -------

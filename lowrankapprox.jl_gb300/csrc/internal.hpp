@@ -287,6 +287,13 @@ void jacobi_svd(lra_ctx* ctx, int64_t n, T* X, int64_t ldx, T* V, int64_t ldv, T
 // not numerically positive definite
 template <typename T>
 bool potrf_upper(lra_ctx* ctx, int64_t k, T* G, int64_t ldg);
+// n (1 or 2) independent factorizations as potrf_upper, in one launch
+template <typename T>
+void potrf_upper_batch(lra_ctx* ctx, int n, const int64_t* k, T* const* G, const int64_t* ldg, bool* ok);
+// cholqr_pre with one pass and chol_v at once (their factorizations batched)
+template <typename T>
+bool cholqr1_and_chol_v(lra_ctx* ctx, int64_t m, int64_t k, T* X, int64_t ldx, const T* Rpre, int64_t ldr, T* Rc,
+                        int64_t nr, const T* Tm, T* Rv);
 // X (m x k) <- X triu(R)^{-1}, blocked (or times the explicit inverse, see
 // trsm_by_inverse)
 template <typename T>

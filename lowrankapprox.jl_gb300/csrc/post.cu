@@ -55,6 +55,31 @@ bool cholqr_pre(lra_ctx* ctx, int64_t m, int64_t k, T* X, int64_t ldx, const T* 
   return ok;
 }
 
+// X (m x k) <- X Rpre^{-1} and one Cholesky QR pass (Rc = its triangular
+// factor), together with R_v = chol(I + T T^T) (T k x nr, ld k): the two
+// k x k Cholesky factorizations in one launch.  False on a breakdown of
+// either.
+template <typename T>
+bool cholqr1_and_chol_v(lra_ctx* ctx, int64_t m, int64_t k, T* X, int64_t ldx, const T* Rpre, int64_t ldr, T* Rc,
+                        int64_t nr, const T* Tm, T* Rv) {
+  const int64_t kk = std::max<int64_t>(k, 1);
+  set_identity(ctx, k, k, Rv, kk);
+  if (k == 0) {
+    set_identity(ctx, k, k, Rc, kk);
+    return true;
+  }
+  if (nr > 0) gemm<T>(ctx, 'n', 't', k, k, nr, T(1), Tm, kk, Tm, kk, T(1), Rv, kk);
+  trsm_right_upper(ctx, m, k, Rpre, ldr, X, ldx);
+  gemm<T>(ctx, 't', 'n', k, k, m, T(1), X, ldx, X, ldx, T(0), Rc, kk);
+  const int64_t ks[2] = {k, k}, lds[2] = {kk, kk};
+  T* Gs[2] = {Rc, Rv};
+  bool ok[2] = {true, true};
+  potrf_upper_batch<T>(ctx, 2, ks, Gs, lds, ok);
+  if (!ok[0] || !ok[1]) return false;
+  trsm_right_upper(ctx, m, k, Rc, kk, X, ldx);
+  return true;
+}
+
 // R_v = chol(I + T T^T), T k x nr (ld k); false on breakdown
 template <typename T>
 bool chol_v(lra_ctx* ctx, int64_t k, int64_t nr, const T* Tm, T* Rv) {
@@ -114,6 +139,10 @@ std::vector<T> small_svd(lra_ctx* ctx, int64_t k, const T* Mm, T* U, T* V, T* S)
 template bool cholqr_pre<float>(lra_ctx*, int64_t, int64_t, float*, int64_t, const float*, int64_t, int, float*);
 template bool cholqr_pre<double>(lra_ctx*, int64_t, int64_t, double*, int64_t, const double*, int64_t, int,
                                  double*);
+template bool cholqr1_and_chol_v<float>(lra_ctx*, int64_t, int64_t, float*, int64_t, const float*, int64_t, float*,
+                                        int64_t, const float*, float*);
+template bool cholqr1_and_chol_v<double>(lra_ctx*, int64_t, int64_t, double*, int64_t, const double*, int64_t,
+                                         double*, int64_t, const double*, double*);
 template bool chol_v<float>(lra_ctx*, int64_t, int64_t, const float*, float*);
 template bool chol_v<double>(lra_ctx*, int64_t, int64_t, const double*, double*);
 template std::vector<float> small_svd<float>(lra_ctx*, int64_t, const float*, float*, float*, float*);
