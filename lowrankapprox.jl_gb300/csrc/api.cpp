@@ -982,6 +982,19 @@ using namespace lra;
 
 namespace {
 
+// the context's error word, after the stream has drained: a kernel whose
+// bounded wait gave up during this call fails the call
+void check_dev_err(lra_ctx* ctx) {
+  if (!ctx->dev_err_armed) return;
+  ctx->dev_err_armed = false;
+  int h = 0;
+  LRA_CUDA(cudaMemcpy(&h, ctx->dev_err, sizeof(int), cudaMemcpyDeviceToHost));
+  if (h != 0) {
+    LRA_CUDA(cudaMemset(ctx->dev_err, 0, sizeof(int)));
+    fail(LRA_ETIMEDOUT, "tc_gemm: a bounded wait timed out");
+  }
+}
+
 template <class Fn>
 int guarded(lra_ctx* ctx, Fn&& fn) {
   if (!ctx) return LRA_EINVAL;
@@ -995,6 +1008,7 @@ int guarded(lra_ctx* ctx, Fn&& fn) {
     ctx->gemm_tc = false;
     ctx->mixed_rtol = 0;
     LRA_CUDA(cudaStreamSynchronize(ctx->stream));
+    check_dev_err(ctx);
     ctx->last_error.clear();
     return LRA_OK;
   } catch (const lra::Error& e) {
@@ -1003,6 +1017,11 @@ int guarded(lra_ctx* ctx, Fn&& fn) {
     ctx->last_error = e.msg;
     cudaStreamSynchronize(ctx->stream);
     cudaGetLastError();
+    if (ctx->dev_err) {
+      cudaMemset(ctx->dev_err, 0, sizeof(int));
+      ctx->dev_err_armed = false;
+      cudaGetLastError();
+    }
     return e.status;
   } catch (const std::bad_alloc&) {
     ctx->last_error = "host allocation failed";
@@ -2344,6 +2363,7 @@ void lra_ctx_destroy(lra_ctx* ctx) {
   for (cudaEvent_t e : ctx->aux_ev)
     if (e) cudaEventDestroy(e);
   if (ctx->own_stream) cudaStreamDestroy(ctx->stream);
+  if (ctx->dev_err) cudaFree(ctx->dev_err);
   delete ctx;
 }
 

@@ -97,6 +97,11 @@ struct lra_tuning {
 };
 
 struct lra_ctx {
+  // device word that kernels with bounded waits set when one gave up,
+  // read once at the end of the library call (tc_gemm arms it instead of
+  // waiting for its own launch)
+  int* dev_err = nullptr;
+  bool dev_err_armed = false;
   int device = 0;
   int num_sms = 0;
   cudaStream_t stream = nullptr;

@@ -1039,8 +1039,14 @@ void tc_gemm(lra_ctx* ctx, char ta, char tb, int64_t m, int64_t n, int64_t k, do
   const int chunks = (kb_per + G_CHUNK - 1) / G_CHUNK;
   int tsh = 1;
   while ((1 << (tsh - 1)) < chunks) ++tsh;
-  int* err = ctx->arena.alloc_n<int>(1);
-  LRA_CUDA(cudaMemsetAsync(err, 0, sizeof(int), ctx->stream));
+  // a timed-out wait is reported when the library call ends (the context's
+  // error word), so that consecutive GEMMs queue without a host round trip
+  if (!ctx->dev_err) {
+    LRA_CUDA(cudaMalloc(&ctx->dev_err, sizeof(int)));
+    LRA_CUDA(cudaMemsetAsync(ctx->dev_err, 0, sizeof(int), ctx->stream));
+  }
+  ctx->dev_err_armed = true;
+  int* err = ctx->dev_err;
   TgParams P;
   P.M = m;
   P.N = n;
@@ -1072,11 +1078,7 @@ void tc_gemm(lra_ctx* ctx, char ta, char tb, int64_t m, int64_t n, int64_t k, do
     tc_gemm_reduce_kernel<<<g, 256, 0, ctx->stream>>>(m, n, nsplit, ws, alpha, beta, C, ldc);
     post_launch(ctx, "tc_gemm_reduce_kernel");
   }
-  int herr = 0;
-  LRA_CUDA(cudaMemcpyAsync(&herr, err, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
-  LRA_CUDA(cudaStreamSynchronize(ctx->stream));
-  ctx->arena.release(mk);
-  if (herr) fail(LRA_ETIMEDOUT, "tc_gemm: a bounded wait timed out");
+  ctx->arena.release(mk);  // stream-ordered reuse
 }
 
 template void tc_split<float>(lra_ctx*, char, int64_t, int64_t, const float*, int64_t, int, TcSplit*, bool);
