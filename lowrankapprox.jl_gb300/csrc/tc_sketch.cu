@@ -1030,9 +1030,11 @@ void tc_gemm(lra_ctx* ctx, char ta, char tb, int64_t m, int64_t n, int64_t k, do
   }
   const int nkb = (int)((k + KBLK - 1) / KBLK);
   const int64_t tiles = ((m + G_TILE_M - 1) / G_TILE_M) * ((n + G_TILE_N - 1) / G_TILE_N);
-  // split K while the tiles alone leave SMs idle, at least 4 K blocks each
+  // split K while the tiles alone leave SMs idle (down to one K block each:
+  // a k x k product of the post-processing has few tiles and few K blocks,
+  // and one CTA per tile would run its K blocks one stage at a time)
   int64_t nsplit = 1;
-  if (tiles < ctx->num_sms) nsplit = std::max<int64_t>(1, std::min<int64_t>((ctx->num_sms + tiles - 1) / tiles, nkb / 4));
+  if (tiles < ctx->num_sms) nsplit = std::max<int64_t>(1, std::min<int64_t>((ctx->num_sms + tiles - 1) / tiles, nkb));
   const int kb_per = (int)((nkb + nsplit - 1) / nsplit);
   nsplit = (nkb + kb_per - 1) / kb_per;
   // |X| <= chunks * 2^(24 + 40 - t) (1 + 2^-7 + ...): t = ceil(log2(chunks)) + 1
