@@ -42,6 +42,9 @@ struct JacParams {
   // block Jacobi: V stays in global memory (only X's block pair in shared
   // memory), so that longer columns fit 8-column blocks
   int vglobal = 0;
+  // LRA_TRACE: CTA 0's time in each phase of the block kernel, summed over
+  // its block pairs (ns): load, local rounds, V, write-back, barrier
+  unsigned long long* phase_ns = nullptr;
 };
 
 constexpr int JCH = 16;  // rows per lane per register chunk (512 rows)
@@ -346,6 +349,26 @@ __global__ void __launch_bounds__(NT) jacobi_pair_kernel(JacParams<T> P) {
   if (blockIdx.x == 0 && threadIdx.x == 0) *P.sweeps_out = sweep;
 }
 
+// two FP32 values in one 64-bit register pair, for the packed FP32 pipe
+// (fma/mul .f32x2: one instruction for both halves)
+typedef unsigned long long f2_t;
+__device__ __forceinline__ f2_t f2_pack(float lo, float hi) {
+  f2_t d;
+  asm("mov.b64 %0, {%1, %2};" : "=l"(d) : "f"(lo), "f"(hi));
+  return d;
+}
+__device__ __forceinline__ float f2_lo(f2_t v) { return __uint_as_float((unsigned)v); }
+__device__ __forceinline__ float f2_hi(f2_t v) { return __uint_as_float((unsigned)(v >> 32)); }
+__device__ __forceinline__ f2_t f2_fma(f2_t a, f2_t b, f2_t c) {
+  f2_t d;
+  asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(d) : "l"(a), "l"(b), "l"(c));
+  return d;
+}
+__device__ __forceinline__ f2_t f2_mul(f2_t a, f2_t b) {
+  f2_t d;
+  asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
+  return d;
+}
 // Block one-sided Jacobi for the FP32 sweeps: the columns are grouped in
 // blocks of JB; each grid-wide round pairs the blocks round-robin, and the
 // CTA holding a block pair loads its 2 JB columns of X and V into shared
@@ -358,7 +381,14 @@ __global__ void __launch_bounds__(NT) jacobi_pair_kernel(JacParams<T> P) {
 // local rounds.
 constexpr int JB = 8;
 constexpr int JB_RPL = 16;  // rows per lane in registers (columns up to 512 long)
+constexpr int JB_QMAX = 16;  // 16-byte chunks a lane holds in the inter-block steps (columns up to 2048 long)
 
+// 16 bytes, of which the first `bytes` come from src and the rest are zero
+__device__ __forceinline__ void cp_async16z(float* dst, const float* src, int bytes) {
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;" ::"r"((uint32_t)__cvta_generic_to_shared(dst)), "l"(src),
+               "r"(bytes)
+               : "memory");
+}
 __device__ __forceinline__ void cp_async4(float* dst, const float* src) {
   asm volatile("cp.async.ca.shared.global [%0], [%1], 4;" ::"r"((uint32_t)__cvta_generic_to_shared(dst)), "l"(src)
                : "memory");
@@ -368,12 +398,18 @@ template <int JBT>
 __global__ void __launch_bounds__(JBT * 32) jacobi_block_kernel(JacParams<float> P) {
   extern __shared__ float jb_smem[];
   __shared__ double red[32];
-  __shared__ float Ql[2 * JBT][2 * JBT];  // column k of the block's local rotation at Ql[k][.]
+  __shared__ __align__(16) float Ql[2 * JBT][2 * JBT];  // column k of the block's local rotation at Ql[k][.]
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
   const int64_t n = P.n;
-  float* Xs = jb_smem;                       // [2 JBT][n]
-  float* Vs = jb_smem + (size_t)2 * JBT * n;  // [2 JBT][n], unless V stays in global memory
+  // column stride in shared memory: n rounded up to 16 bytes, the padding
+  // rows zero, so that long columns move in 16-byte vectors
+  const int64_t ld = (n + 3) & ~(int64_t)3;
+  float* Xs = jb_smem;                        // [2 JBT][ld]
+  float* Vs = jb_smem + (size_t)2 * JBT * ld;  // [2 JBT][ld], unless V stays in global memory
   const bool vg = P.vglobal != 0;
+  // columns that start on 16 bytes move as 16-byte vectors
+  const bool vec16 = (P.ldx & 3) == 0 && ((uintptr_t)P.X & 15) == 0 &&
+                     (vg || ((P.ldv & 3) == 0 && ((uintptr_t)P.V & 15) == 0));
   const int64_t nblk = (n + JBT - 1) / JBT;
   const int64_t nbb = nblk + (nblk & 1);
   const float tol = (float)P.tol;
@@ -382,6 +418,14 @@ __global__ void __launch_bounds__(JBT * 32) jacobi_block_kernel(JacParams<float>
     float off = 0;
     for (int64_t r = 0; r < nbb - 1; ++r) {
       for (int64_t s = blockIdx.x; s < nbb / 2; s += gridDim.x) {
+        const bool stamp = P.phase_ns && blockIdx.x == 0 && threadIdx.x == 0;
+        uint64_t t_ph = stamp ? globaltimer_ns() : 0;
+        auto phase = [&](int i) {
+          if (!stamp) return;
+          const uint64_t t = globaltimer_ns();
+          P.phase_ns[i] += t - t_ph;
+          t_ph = t;
+        };
         int64_t b1, b2;
         rr_pair(r, s, nbb, b1, b2);
         // local column k < JBT is column b1 JBT + k, k >= JBT is b2 JBT + k - JBT
@@ -391,16 +435,26 @@ __global__ void __launch_bounds__(JBT * 32) jacobi_block_kernel(JacParams<float>
           const int64_t j = b * JBT + (k % JBT);
           return j < n ? j : -1;
         };
-        // all 4 JBT n elements in flight at once (asynchronous copies)
+        // all 4 JBT n elements in flight at once (asynchronous copies), in
+        // 16-byte vectors when the columns start on 16 bytes (the rows past n
+        // zero-filled)
         for (int k = 0; k < 2 * JBT; ++k) {
           const int64_t j = gcol(k);
-          for (int64_t i = threadIdx.x; i < n; i += JBT * 32) {
-            if (j >= 0) {
-              cp_async4(Xs + k * n + i, P.X + i + j * P.ldx);
-              if (!vg) cp_async4(Vs + k * n + i, P.V + i + j * P.ldv);
+          if (vec16) {
+            for (int64_t i = 4 * (int64_t)threadIdx.x; i < ld; i += 4 * JBT * 32) {
+              const int bytes = j >= 0 ? (int)(4 * min((int64_t)4, n - i)) : 0;
+              cp_async16z(Xs + k * ld + i, P.X + (j >= 0 ? i + j * P.ldx : 0), bytes);
+              if (!vg) cp_async16z(Vs + k * ld + i, P.V + (j >= 0 ? i + j * P.ldv : 0), bytes);
+            }
+            continue;
+          }
+          for (int64_t i = threadIdx.x; i < ld; i += JBT * 32) {
+            if (j >= 0 && i < n) {
+              cp_async4(Xs + k * ld + i, P.X + i + j * P.ldx);
+              if (!vg) cp_async4(Vs + k * ld + i, P.V + i + j * P.ldv);
             } else {
-              Xs[k * n + i] = 0.0f;
-              if (!vg) Vs[k * n + i] = 0.0f;
+              Xs[k * ld + i] = 0.0f;
+              if (!vg) Vs[k * ld + i] = 0.0f;
             }
           }
         }
@@ -408,41 +462,57 @@ __global__ void __launch_bounds__(JBT * 32) jacobi_block_kernel(JacParams<float>
           Ql[e / (2 * JBT)][e % (2 * JBT)] = e / (2 * JBT) == e % (2 * JBT) ? 1.0f : 0.0f;
         asm volatile("cp.async.wait_all;" ::: "memory");
         __syncthreads();
+        phase(0);
         unsigned long long vmask = 0;  // local columns that exist
 #pragma unroll
         for (int k = 0; k < 2 * JBT; ++k) vmask |= (gcol(k) >= 0 ? 1ull : 0ull) << k;
         const int ni = (int)n;
-        for (int lr = 0; lr < 2 * JBT - 1; ++lr) {
-          // round-robin pair of this warp among the 2 JBT local columns
-          auto lpos = [&](int i) { return i == 0 ? 0 : 1 + (i - 1 + lr) % (2 * JBT - 1); };
-          int p = lpos(wid), q = lpos(2 * JBT - 1 - wid);
-          if (p > q) {
-            const int t = p;
-            p = q;
-            q = t;
+        // Past the first round of a sweep (whose full local sweeps also
+        // rotate the pairs inside each block, once a sweep), the block pair
+        // of long columns takes inter-block steps only: warp w keeps column w
+        // of block b1 in registers and meets column (w + step) mod JBT of
+        // block b2, which moves from warp to warp through shared memory --
+        // every inter-block pair once, in JBT steps that read and write one
+        // column a warp instead of 2 JBT - 1 rounds that read and write all.
+        // (registers for up to 2048 rows with 8-column blocks and fewer;
+        // larger blocks have too few registers a thread)
+        constexpr int QM = JBT <= 8 ? JB_QMAX : 1;
+        const bool inter = r > 0 && ni > 32 * JB_RPL && ld <= (int64_t)4 * 32 * QM;
+        if (inter) {
+          const int p = wid;
+          const int nq = (int)(ld / 4);
+          const ulonglong2 z2 = make_ulonglong2(0ull, 0ull);
+          ulonglong2* tp = reinterpret_cast<ulonglong2*>(Xs + p * ld);
+          ulonglong2 top[QM];
+#pragma unroll
+          for (int c = 0; c < QM; ++c) {
+            const int v = lane + 32 * c;
+            top[c] = v < nq ? tp[v] : z2;
           }
-          if (((vmask >> p) & 1ull) && ((vmask >> q) & 1ull)) {
-            float* xp = Xs + p * ni;
-            float* xq = Xs + q * ni;
-            float a = 0, b = 0, g = 0;
-            if (ni <= 32 * JB_RPL) {
-              // both columns in registers for the dots and the update
-              float u[JB_RPL], w[JB_RPL];
+          const bool pe = (vmask >> p) & 1ull;
+          for (int st = 0; st < JBT; ++st) {
+            const int q = JBT + (wid + st) % JBT;
+            if (pe && ((vmask >> q) & 1ull)) {
+              ulonglong2* qp = reinterpret_cast<ulonglong2*>(Xs + q * ld);
+              ulonglong2 bot[QM];
 #pragma unroll
-              for (int t = 0; t < JB_RPL; ++t) {
-                const int i = lane + 32 * t;
-                u[t] = i < ni ? xp[i] : 0.0f;
-                w[t] = i < ni ? xq[i] : 0.0f;
+              for (int c = 0; c < QM; ++c) {
+                const int v = lane + 32 * c;
+                bot[c] = v < nq ? qp[v] : z2;
               }
+              f2_t a2 = 0, b2 = 0, g2 = 0;
 #pragma unroll
-              for (int t = 0; t < JB_RPL; ++t) {
-                a = fmaf(u[t], u[t], a);
-                b = fmaf(w[t], w[t], b);
-                g = fmaf(u[t], w[t], g);
+              for (int c = 0; c < QM; ++c) {
+                a2 = f2_fma(top[c].x, top[c].x, a2);
+                a2 = f2_fma(top[c].y, top[c].y, a2);
+                b2 = f2_fma(bot[c].x, bot[c].x, b2);
+                b2 = f2_fma(bot[c].y, bot[c].y, b2);
+                g2 = f2_fma(top[c].x, bot[c].x, g2);
+                g2 = f2_fma(top[c].y, bot[c].y, g2);
               }
-              a = warp_sum(a);
-              b = warp_sum(b);
-              g = warp_sum(g);
+              const float a = warp_sum(f2_lo(a2) + f2_hi(a2));
+              const float b = warp_sum(f2_lo(b2) + f2_hi(b2));
+              const float g = warp_sum(f2_lo(g2) + f2_hi(g2));
               if (a != 0 && b != 0) {
                 const float rel = fabsf(g) * rsqrtf(a * b);
                 if (rel > tol) {
@@ -451,43 +521,16 @@ __global__ void __launch_bounds__(JBT * 32) jacobi_block_kernel(JacParams<float>
                   const float t = copysignf(1.0f, zeta) / (fabsf(zeta) + sqrtf(1.0f + zeta * zeta));
                   const float c = rsqrtf(1.0f + t * t);
                   const float sn = c * t;
+                  const f2_t cc = f2_pack(c, c), ss = f2_pack(sn, sn), ns = f2_pack(-sn, -sn);
 #pragma unroll
-                  for (int tt = 0; tt < JB_RPL; ++tt) {
-                    const int i = lane + 32 * tt;
-                    if (i < ni) {
-                      xp[i] = c * u[tt] - sn * w[tt];
-                      xq[i] = sn * u[tt] + c * w[tt];
-                    }
-                  }
-                  for (int l = lane; l < 2 * JBT; l += 32) {
-                    const float qu = Ql[p][l], qw = Ql[q][l];
-                    Ql[p][l] = c * qu - sn * qw;
-                    Ql[q][l] = sn * qu + c * qw;
-                  }
-                }
-              }
-            } else {
-              for (int i = lane; i < ni; i += 32) {
-                const float u = xp[i], w = xq[i];
-                a = fmaf(u, u, a);
-                b = fmaf(w, w, b);
-                g = fmaf(u, w, g);
-              }
-              a = warp_sum(a);
-              b = warp_sum(b);
-              g = warp_sum(g);
-              if (a != 0 && b != 0) {
-                const float rel = fabsf(g) * rsqrtf(a * b);
-                if (rel > tol) {
-                  off = fmaxf(off, rel);
-                  const float zeta = (b - a) / (2.0f * g);
-                  const float t = copysignf(1.0f, zeta) / (fabsf(zeta) + sqrtf(1.0f + zeta * zeta));
-                  const float c = rsqrtf(1.0f + t * t);
-                  const float sn = c * t;
-                  for (int i = lane; i < ni; i += 32) {
-                    const float u = xp[i], w = xq[i];
-                    xp[i] = c * u - sn * w;
-                    xq[i] = sn * u + c * w;
+                  for (int k = 0; k < QM; ++k) {
+                    const ulonglong2 u = top[k], w = bot[k];
+                    top[k].x = f2_fma(ns, w.x, f2_mul(cc, u.x));
+                    top[k].y = f2_fma(ns, w.y, f2_mul(cc, u.y));
+                    bot[k].x = f2_fma(cc, w.x, f2_mul(ss, u.x));
+                    bot[k].y = f2_fma(cc, w.y, f2_mul(ss, u.y));
+                    const int v = lane + 32 * k;
+                    if (v < nq) qp[v] = bot[k];
                   }
                   for (int l = lane; l < 2 * JBT; l += 32) {
                     const float qu = Ql[p][l], qw = Ql[q][l];
@@ -497,51 +540,239 @@ __global__ void __launch_bounds__(JBT * 32) jacobi_block_kernel(JacParams<float>
                 }
               }
             }
+            __syncthreads();
+          }
+#pragma unroll
+          for (int c = 0; c < QM; ++c) {
+            const int v = lane + 32 * c;
+            if (v < nq) tp[v] = top[c];
           }
           __syncthreads();
+        } else {
+          for (int lr = 0; lr < 2 * JBT - 1; ++lr) {
+            // round-robin pair of this warp among the 2 JBT local columns
+            auto lpos = [&](int i) { return i == 0 ? 0 : 1 + (i - 1 + lr) % (2 * JBT - 1); };
+            int p = lpos(wid), q = lpos(2 * JBT - 1 - wid);
+            if (p > q) {
+              const int t = p;
+              p = q;
+              q = t;
+            }
+            if (((vmask >> p) & 1ull) && ((vmask >> q) & 1ull)) {
+              float* xp = Xs + p * ld;
+              float* xq = Xs + q * ld;
+              float a = 0, b = 0, g = 0;
+              if (ni <= 32 * JB_RPL) {
+                // both columns in registers for the dots and the update
+                float u[JB_RPL], w[JB_RPL];
+  #pragma unroll
+                for (int t = 0; t < JB_RPL; ++t) {
+                  const int i = lane + 32 * t;
+                  u[t] = i < ni ? xp[i] : 0.0f;
+                  w[t] = i < ni ? xq[i] : 0.0f;
+                }
+  #pragma unroll
+                for (int t = 0; t < JB_RPL; ++t) {
+                  a = fmaf(u[t], u[t], a);
+                  b = fmaf(w[t], w[t], b);
+                  g = fmaf(u[t], w[t], g);
+                }
+                a = warp_sum(a);
+                b = warp_sum(b);
+                g = warp_sum(g);
+                if (a != 0 && b != 0) {
+                  const float rel = fabsf(g) * rsqrtf(a * b);
+                  if (rel > tol) {
+                    off = fmaxf(off, rel);
+                    const float zeta = (b - a) / (2.0f * g);
+                    const float t = copysignf(1.0f, zeta) / (fabsf(zeta) + sqrtf(1.0f + zeta * zeta));
+                    const float c = rsqrtf(1.0f + t * t);
+                    const float sn = c * t;
+  #pragma unroll
+                    for (int tt = 0; tt < JB_RPL; ++tt) {
+                      const int i = lane + 32 * tt;
+                      if (i < ni) {
+                        xp[i] = c * u[tt] - sn * w[tt];
+                        xq[i] = sn * u[tt] + c * w[tt];
+                      }
+                    }
+                    for (int l = lane; l < 2 * JBT; l += 32) {
+                      const float qu = Ql[p][l], qw = Ql[q][l];
+                      Ql[p][l] = c * qu - sn * qw;
+                      Ql[q][l] = sn * qu + c * qw;
+                    }
+                  }
+                }
+              } else {
+                // long columns: 16-byte vectors (rows 4v .. 4v + 3 in lane v
+                // mod 32) and the packed FP32 pipe, two accumulators a value
+                const ulonglong2* vp = reinterpret_cast<const ulonglong2*>(xp);
+                const ulonglong2* vq = reinterpret_cast<const ulonglong2*>(xq);
+                const int nv = (int)(ld / 4);
+                f2_t a2 = 0, b2 = 0, g2 = 0;
+  #pragma unroll 4
+                for (int v = lane; v < nv; v += 32) {
+                  const ulonglong2 u = vp[v], w = vq[v];
+                  a2 = f2_fma(u.x, u.x, a2);
+                  a2 = f2_fma(u.y, u.y, a2);
+                  b2 = f2_fma(w.x, w.x, b2);
+                  b2 = f2_fma(w.y, w.y, b2);
+                  g2 = f2_fma(u.x, w.x, g2);
+                  g2 = f2_fma(u.y, w.y, g2);
+                }
+                a = warp_sum(f2_lo(a2) + f2_hi(a2));
+                b = warp_sum(f2_lo(b2) + f2_hi(b2));
+                g = warp_sum(f2_lo(g2) + f2_hi(g2));
+                if (a != 0 && b != 0) {
+                  const float rel = fabsf(g) * rsqrtf(a * b);
+                  if (rel > tol) {
+                    off = fmaxf(off, rel);
+                    const float zeta = (b - a) / (2.0f * g);
+                    const float t = copysignf(1.0f, zeta) / (fabsf(zeta) + sqrtf(1.0f + zeta * zeta));
+                    const float c = rsqrtf(1.0f + t * t);
+                    const float sn = c * t;
+                    const f2_t cc = f2_pack(c, c), ss = f2_pack(sn, sn), ns = f2_pack(-sn, -sn);
+                    ulonglong2* wp = reinterpret_cast<ulonglong2*>(xp);
+                    ulonglong2* wq = reinterpret_cast<ulonglong2*>(xq);
+  #pragma unroll 4
+                    for (int v = lane; v < nv; v += 32) {
+                      const ulonglong2 u = wp[v], w = wq[v];
+                      ulonglong2 up, uq;
+                      up.x = f2_fma(ns, w.x, f2_mul(cc, u.x));
+                      up.y = f2_fma(ns, w.y, f2_mul(cc, u.y));
+                      uq.x = f2_fma(cc, w.x, f2_mul(ss, u.x));
+                      uq.y = f2_fma(cc, w.y, f2_mul(ss, u.y));
+                      wp[v] = up;
+                      wq[v] = uq;
+                    }
+                    for (int l = lane; l < 2 * JBT; l += 32) {
+                      const float qu = Ql[p][l], qw = Ql[q][l];
+                      Ql[p][l] = c * qu - sn * qw;
+                      Ql[q][l] = sn * qu + c * qw;
+                    }
+                  }
+                }
+              }
+            }
+            __syncthreads();
+          }
         }
+        phase(1);
         // the block's columns of V times the gathered rotation, a thread per
         // row (rows of V read and written in place, coalesced, when V stays
         // in global memory)
-        for (int i = threadIdx.x; i < ni; i += JBT * 32) {
-          float acc[2 * JBT];
+        if constexpr (JBT <= 8) {
+          // two rows a thread at once: their 4 JBT entries are loaded
+          // together (the latencies overlap), and each 16-byte read of the
+          // rotation (which the compiler may not hoist out of the row loop)
+          // serves both
+          constexpr int NT = JBT * 32;
+          for (int i = threadIdx.x; i < ni; i += 2 * NT) {
+            const int i2 = i + NT;
+            const bool two = i2 < ni;
+            float v0[2 * JBT], v1[2 * JBT];
 #pragma unroll
-          for (int k = 0; k < 2 * JBT; ++k) acc[k] = 0.0f;
-#pragma unroll 1
-          for (int j = 0; j < 2 * JBT; ++j) {  // (not unrolled: Ql would be hoisted into registers)
-            float v;
-            if (vg) {
-              const int64_t gj = gcol(j);
-              v = gj >= 0 ? P.V[i + gj * P.ldv] : 0.0f;
-            } else {
-              v = Vs[j * ni + i];
+            for (int j = 0; j < 2 * JBT; ++j) {
+              if (vg) {
+                const int64_t gj = gcol(j);
+                v0[j] = gj >= 0 ? P.V[i + gj * P.ldv] : 0.0f;
+                v1[j] = gj >= 0 && two ? P.V[i2 + gj * P.ldv] : 0.0f;
+              } else {
+                v0[j] = Vs[j * ld + i];
+                v1[j] = two ? Vs[j * ld + i2] : 0.0f;
+              }
             }
-#pragma unroll
-            for (int k = 0; k < 2 * JBT; ++k) acc[k] = fmaf(v, Ql[k][j], acc[k]);
-          }
-          if (vg) {
 #pragma unroll
             for (int k = 0; k < 2 * JBT; ++k) {
-              const int64_t gk = gcol(k);
-              if (gk >= 0) P.V[i + gk * P.ldv] = acc[k];
-            }
-          } else {
+              float s0 = 0.0f, s1 = 0.0f;
 #pragma unroll
-            for (int k = 0; k < 2 * JBT; ++k) Vs[k * ni + i] = acc[k];
+              for (int j = 0; j < 2 * JBT; j += 4) {
+                float4 q;
+                asm volatile("ld.shared.v4.f32 {%0, %1, %2, %3}, [%4];"
+                             : "=f"(q.x), "=f"(q.y), "=f"(q.z), "=f"(q.w)
+                             : "r"((uint32_t)__cvta_generic_to_shared(&Ql[k][j])));
+                s0 = fmaf(v0[j], q.x, s0);
+                s0 = fmaf(v0[j + 1], q.y, s0);
+                s0 = fmaf(v0[j + 2], q.z, s0);
+                s0 = fmaf(v0[j + 3], q.w, s0);
+                s1 = fmaf(v1[j], q.x, s1);
+                s1 = fmaf(v1[j + 1], q.y, s1);
+                s1 = fmaf(v1[j + 2], q.z, s1);
+                s1 = fmaf(v1[j + 3], q.w, s1);
+              }
+              if (vg) {
+                const int64_t gk = gcol(k);
+                if (gk >= 0) {
+                  P.V[i + gk * P.ldv] = s0;
+                  if (two) P.V[i2 + gk * P.ldv] = s1;
+                }
+              } else {
+                Vs[k * ld + i] = s0;
+                if (two) Vs[k * ld + i2] = s1;
+              }
+            }
+          }
+        } else {
+          for (int i = threadIdx.x; i < ni; i += JBT * 32) {
+            float acc[2 * JBT];
+#pragma unroll
+            for (int k = 0; k < 2 * JBT; ++k) acc[k] = 0.0f;
+#pragma unroll 1
+            for (int j = 0; j < 2 * JBT; ++j) {  // (not unrolled: Ql would be hoisted into registers)
+              float v;
+              if (vg) {
+                const int64_t gj = gcol(j);
+                v = gj >= 0 ? P.V[i + gj * P.ldv] : 0.0f;
+              } else {
+                v = Vs[j * ld + i];
+              }
+#pragma unroll
+              for (int k = 0; k < 2 * JBT; ++k) acc[k] = fmaf(v, Ql[k][j], acc[k]);
+            }
+            if (vg) {
+#pragma unroll
+              for (int k = 0; k < 2 * JBT; ++k) {
+                const int64_t gk = gcol(k);
+                if (gk >= 0) P.V[i + gk * P.ldv] = acc[k];
+              }
+            } else {
+#pragma unroll
+              for (int k = 0; k < 2 * JBT; ++k) Vs[k * ld + i] = acc[k];
+            }
           }
         }
         __syncthreads();
+        phase(2);
         for (int k = 0; k < 2 * JBT; ++k) {
           const int64_t j = gcol(k);
           if (j < 0) continue;
+          if (vec16) {
+            // whole vectors up to the last full one, the rest by element
+            const int64_t n4 = n & ~(int64_t)3;
+            for (int64_t i = 4 * (int64_t)threadIdx.x; i < n4; i += 4 * JBT * 32) {
+              *reinterpret_cast<float4*>(P.X + i + j * P.ldx) = *reinterpret_cast<const float4*>(Xs + k * ld + i);
+              if (!vg)
+                *reinterpret_cast<float4*>(P.V + i + j * P.ldv) = *reinterpret_cast<const float4*>(Vs + k * ld + i);
+            }
+            for (int64_t i = n4 + threadIdx.x; i < n; i += JBT * 32) {
+              P.X[i + j * P.ldx] = Xs[k * ld + i];
+              if (!vg) P.V[i + j * P.ldv] = Vs[k * ld + i];
+            }
+            continue;
+          }
           for (int64_t i = threadIdx.x; i < n; i += JBT * 32) {
-            P.X[i + j * P.ldx] = Xs[k * n + i];
-            if (!vg) P.V[i + j * P.ldv] = Vs[k * n + i];
+            P.X[i + j * P.ldx] = Xs[k * ld + i];
+            if (!vg) P.V[i + j * P.ldv] = Vs[k * ld + i];
           }
         }
         __syncthreads();
+        phase(3);
       }
-      if (!grid_sync(P.bar)) return;
+      {
+        const uint64_t t0 = P.phase_ns && blockIdx.x == 0 && threadIdx.x == 0 ? globaltimer_ns() : 0;
+        if (!grid_sync(P.bar)) return;
+        if (t0) P.phase_ns[4] += globaltimer_ns() - t0;
+      }
     }
     const double offd = block_max((double)off, red);
     if (threadIdx.x == 0) P.part[blockIdx.x] = offd;
@@ -599,26 +830,6 @@ __device__ __forceinline__ uint32_t dsmem_addr(const void* local, unsigned rank)
                : "=r"(r)
                : "r"((uint32_t)__cvta_generic_to_shared(local)), "r"(rank));
   return r;
-}
-// two FP32 values in one 64-bit register pair, for the packed FP32 pipe
-// (fma/mul .f32x2: one instruction for both halves)
-typedef unsigned long long f2_t;
-__device__ __forceinline__ f2_t f2_pack(float lo, float hi) {
-  f2_t d;
-  asm("mov.b64 %0, {%1, %2};" : "=l"(d) : "f"(lo), "f"(hi));
-  return d;
-}
-__device__ __forceinline__ float f2_lo(f2_t v) { return __uint_as_float((unsigned)v); }
-__device__ __forceinline__ float f2_hi(f2_t v) { return __uint_as_float((unsigned)(v >> 32)); }
-__device__ __forceinline__ f2_t f2_fma(f2_t a, f2_t b, f2_t c) {
-  f2_t d;
-  asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(d) : "l"(a), "l"(b), "l"(c));
-  return d;
-}
-__device__ __forceinline__ f2_t f2_mul(f2_t a, f2_t b) {
-  f2_t d;
-  asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
-  return d;
 }
 // 16 bytes into this CTA's shared memory (local) or another's of the cluster
 __device__ __forceinline__ void mbox_st4(bool local, uint32_t a, f2_t x, f2_t y) {
@@ -1322,14 +1533,15 @@ void jacobi_svd(lra_ctx* ctx, int64_t n, T* X, int64_t ldx, T* V, int64_t ldv, T
   // longer columns V stays in global memory (read and written once per block
   // pair), up to about 3400 rows; beyond, a warp per pair
   int jbt = 8;
-  bool vglobal = (size_t)4 * jbt * n * sizeof(float) > blk_cap;
+  const int64_t nld = (n + 3) & ~(int64_t)3;  // the kernel's padded column stride
+  bool vglobal = (size_t)4 * jbt * nld * sizeof(float) > blk_cap;
   // the tuning table may ask for another block size (when it fits)
   const int want = ctx->tuning.jacobi_jb;
-  if ((want == 4 || want == 8 || want == 16 || want == 32) && (size_t)2 * want * n * sizeof(float) <= blk_cap) {
+  if ((want == 4 || want == 8 || want == 16 || want == 32) && (size_t)2 * want * nld * sizeof(float) <= blk_cap) {
     jbt = want;
-    vglobal = (size_t)4 * jbt * n * sizeof(float) > blk_cap;
+    vglobal = (size_t)4 * jbt * nld * sizeof(float) > blk_cap;
   }
-  const size_t blk_smem = (size_t)(vglobal ? 2 : 4) * jbt * n * sizeof(float);
+  const size_t blk_smem = (size_t)(vglobal ? 2 : 4) * jbt * nld * sizeof(float);
   const bool block = !pair_cta && n >= 4 * jbt && blk_smem <= blk_cap;
   const void* kern = pair_cta ? (const void*)jacobi_pair_kernel<T, NT>
                      : !block ? (const void*)jacobi_kernel<T, NT>
@@ -1368,6 +1580,10 @@ void jacobi_svd(lra_ctx* ctx, int64_t n, T* X, int64_t ldx, T* V, int64_t ldv, T
   P.part = ctx->arena.alloc_n<double>(grid);
   P.bar = reinterpret_cast<GridBar*>(ctx->arena.alloc(sizeof(GridBar)));
   P.sweeps_out = ctx->arena.alloc_n<int>(1);
+  if (trace_on() && block) {
+    P.phase_ns = ctx->arena.alloc_n<unsigned long long>(5);
+    LRA_CUDA(cudaMemsetAsync(P.phase_ns, 0, 5 * sizeof(unsigned long long), ctx->stream));
+  }
   LRA_CUDA(cudaMemsetAsync(P.bar, 0, sizeof(GridBar), ctx->stream));
   if constexpr (sizeof(T) == 4) {
     if (jacobi_cluster(ctx, P)) {
@@ -1388,12 +1604,17 @@ void jacobi_svd(lra_ctx* ctx, int64_t n, T* X, int64_t ldx, T* V, int64_t ldv, T
   post_launch(ctx, pair_cta ? "jacobi_pair_kernel" : (block ? "jacobi_block_kernel" : "jacobi_kernel"));
   GridBar hb;
   int sweeps = 0;
+  unsigned long long ph[5] = {0, 0, 0, 0, 0};
   LRA_CUDA(cudaMemcpyAsync(&hb, P.bar, sizeof(GridBar), cudaMemcpyDeviceToHost, ctx->stream));
   if (trace_on())
     LRA_CUDA(cudaMemcpyAsync(&sweeps, P.sweeps_out, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+  if (P.phase_ns) LRA_CUDA(cudaMemcpyAsync(ph, P.phase_ns, sizeof(ph), cudaMemcpyDeviceToHost, ctx->stream));
   LRA_CUDA(cudaStreamSynchronize(ctx->stream));
   ctx->arena.release(mk);
   if (hb.err != 0) fail(LRA_ETIMEDOUT, "jacobi: a grid barrier timed out");
+  if (P.phase_ns)
+    std::fprintf(stderr, "[lra] jacobi block CTA 0 ms: load %.2f local %.2f V %.2f write %.2f barrier %.2f\n",
+                 ph[0] * 1e-6, ph[1] * 1e-6, ph[2] * 1e-6, ph[3] * 1e-6, ph[4] * 1e-6);
   if (trace_on())
     std::fprintf(stderr, "[lra] jacobi %s%s n=%lld sweeps=%d grid=%d\n", sizeof(T) == 8 ? "f64" : "f32",
                  block ? " block" : "", (long long)n, sweeps, grid);

@@ -549,24 +549,27 @@ void jacobi_svd_fast(lra_ctx* ctx, int64_t n, T* X, int64_t ldx, T* V, int64_t l
     }
     scale = std::ldexp(1.0, -std::ilogb(hm));
   }
-  float* X32 = ctx->arena.alloc_n<float>((size_t)n * n);
-  float* V32 = ctx->arena.alloc_n<float>((size_t)n * n);
+  // leading dimension a multiple of 4 floats: the Jacobi kernels move whole
+  // 16-byte vectors of a column
+  const int64_t ld32 = (n + 3) & ~(int64_t)3;
+  float* X32 = ctx->arena.alloc_n<float>((size_t)ld32 * n);
+  float* V32 = ctx->arena.alloc_n<float>((size_t)ld32 * n);
   float* S32 = ctx->arena.alloc_n<float>(n);
-  cast<T, float>(ctx, n, n, X, ldx, X32, n, scale);
+  cast<T, float>(ctx, n, n, X, ldx, X32, ld32, scale);
   // the Gram polish converges quadratically from cosines of a few 1e-3 (the
   // FP32 sweeps stop there); the pairwise FP64 sweeps want them near 1e-6
   // (neighbouring singular values of a smooth spectrum of n are ~1/n apart
   // relative to each other, and the simultaneous rotations converge only
   // from cosines below that gap: the start level falls with n)
   const double start = ctx->tuning.gram_start > 0 ? 1e-4 * ctx->tuning.gram_start : std::min(kGramStart, 12.0 / (double)n);
-  jacobi_svd<float>(ctx, n, X32, n, V32, n, S32, true, df_polish ? start : 0.0);
+  jacobi_svd<float>(ctx, n, X32, ld32, V32, ld32, S32, true, df_polish ? start : 0.0);
   // 2. the rotation in FP64, re-orthonormalized by two Newton-Schulz steps
   //    W <- W (3 I - W'W) / 2: with |I - W'W| near 1e-6 from the FP32
   //    sweeps the error squares each step, to rounding level after two
   T* W = ctx->arena.alloc_n<T>((size_t)n * n);
   T* G = ctx->arena.alloc_n<T>((size_t)n * n);
   T* W2 = ctx->arena.alloc_n<T>((size_t)n * n);
-  cast<float, T>(ctx, n, n, V32, n, W, n);
+  cast<float, T>(ctx, n, n, V32, ld32, W, n);
   for (int it = 0; it < 2; ++it) {
     gemm<T>(ctx, 't', 'n', n, n, n, T(1), W, n, W, n, T(0), G, n);
     copy_matrix(ctx, n, n, W, n, W2, n);
