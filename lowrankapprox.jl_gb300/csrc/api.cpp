@@ -527,6 +527,9 @@ struct Fact {
   // updated R1 (k x k, ld k; R above, reflectors below) and its tau
   T* r1 = nullptr;
   T* r1tau = nullptr;
+  // R11^-1 diag(R11) (k x k, ld k) when the solve for T computed it, for the
+  // post-processing's division by R11 (valid while swaps == 0)
+  T* r11inv = nullptr;
 };
 
 template <typename T>
@@ -788,10 +791,15 @@ void postproc_t(lra_ctx* ctx, const lra_opts& o, Fact<T>& F, bool want_t) {
   F.T_ = ctx->arena.alloc_n<T>((size_t)std::max<int64_t>(k, 1) * std::max<int64_t>(nr, 1));
   if (k > 0 && nr > 0) {
     copy_matrix(ctx, k, nr, F.B + k * F.ld, F.ld, F.T_, k);
-    if (k <= kBsMax)
+    if (k <= kBsMax) {
       trsm_bs(ctx, k, nr, F.B, F.ld, F.T_, k);
-    else
-      trsm_upper(ctx, k, nr, F.B, F.ld, F.T_, k);
+    } else {
+      if (trsm_by_inverse<T>(ctx, k, nr)) {
+        F.r11inv = ctx->arena.alloc_n<T>((size_t)k * k);
+        tri_inv_upper<T>(ctx, k, F.B, F.ld, F.r11inv, k);
+      }
+      trsm_upper(ctx, k, nr, F.B, F.ld, F.T_, k, F.r11inv);
+    }
   }
   if (maxdet) maxdet_dev<T>(ctx, o, F);
 }
@@ -870,7 +878,8 @@ bool skeleton_qr_v(lra_ctx* ctx, const Fact<T>& F, int64_t M, T* Ask, T* RA, int
   if (F.swaps > 0) return false;
   if (!(dtype == LRA_F64 && F.embed)) return skeleton_qr<T>(ctx, F, M, Ask, RA, dtype) && chol_v<T>(ctx, k, nr, F.T_, Rv);
   T* Rc = ctx->arena.alloc_n<T>((size_t)kk * kk);
-  if (!cholqr1_and_chol_v<T>(ctx, M, k, Ask, std::max<int64_t>(M, 1), F.B, F.ld, Rc, nr, F.T_, Rv)) return false;
+  if (!cholqr1_and_chol_v<T>(ctx, M, k, Ask, std::max<int64_t>(M, 1), F.B, F.ld, Rc, nr, F.T_, Rv, F.r11inv))
+    return false;
   // R_A = Rc R11
   T* R11 = ctx->arena.alloc_n<T>((size_t)kk * kk);
   copy_matrix(ctx, k, k, F.B, F.ld, R11, kk);

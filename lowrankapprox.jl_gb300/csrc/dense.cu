@@ -2077,7 +2077,10 @@ namespace {
 // then a_i -= R_iq y_q for i < q and y_q = a_q / R_qq from q = j down --
 // with the partial sums a_i in the registers of the thread owning row i
 // (rows tid + 128 u) and the finished y in shared memory; the column of R a
-// step needs is loaded one step ahead.  A graded R (|R_iq| <= |R_ii|, as a
+// step needs is loaded one step ahead, and 1 / R_qq is computed for every q
+// first, so that no FP64 division sits on a step's critical path (a product
+// with the reciprocal instead, within an ulp of the quotient).  A graded R
+// (|R_iq| <= |R_ii|, as a
 // pivoted QR leaves it) has an inverse whose rows span its whole diagonal
 // range, which a GEMM that scales each row by its largest entry would
 // truncate; R^-1 D has entries of order one.
@@ -2089,8 +2092,11 @@ __global__ void __launch_bounds__(kTiNT) tri_inv_upper_kernel(int64_t k, const T
                                                               T* __restrict__ Y, int64_t ldy) {
   extern __shared__ unsigned char ti_smem[];
   T* ys = reinterpret_cast<T*>(ti_smem);  // k
+  T* rdi = ys + k;                        // 1 / R_qq, off the per-step critical path
   const int tid = threadIdx.x;
   const int U = (int)((k + kTiNT - 1) / kTiNT);
+  for (int64_t q = tid; q < k; q += kTiNT) rdi[q] = T(1) / R[q + q * ldr];
+  __syncthreads();
   for (int64_t j = blockIdx.x; j < k; j += gridDim.x) {
     T a[kTiRows], rc[kTiRows];
 #pragma unroll
@@ -2103,7 +2109,7 @@ __global__ void __launch_bounds__(kTiNT) tri_inv_upper_kernel(int64_t k, const T
     __syncthreads();
     for (int64_t q = j; q > 0; --q) {
       const T yq = ys[q];
-      const T rqq = R[(q - 1) + (q - 1) * ldr];
+      const T rqq = rdi[q - 1];
       T rn[kTiRows];
 #pragma unroll
       for (int u = 0; u < kTiRows; ++u) {
@@ -2115,7 +2121,7 @@ __global__ void __launch_bounds__(kTiNT) tri_inv_upper_kernel(int64_t k, const T
         const int64_t i = tid + (int64_t)kTiNT * u;
         if (u < U && i < q) {
           a[u] = fma(-rc[u], yq, a[u]);
-          if (i == q - 1) ys[q - 1] = a[u] / rqq;
+          if (i == q - 1) ys[q - 1] = a[u] * rqq;
         }
         rc[u] = rn[u];
       }
@@ -2158,7 +2164,7 @@ template <typename T>
 bool tri_inv_upper(lra_ctx* ctx, int64_t k, const T* R, int64_t ldr, T* Y, int64_t ldy) {
   if (k <= 0) return true;
   if (k > (int64_t)kTiNT * kTiRows) return false;
-  const size_t smem = (size_t)k * sizeof(T);
+  const size_t smem = (size_t)2 * k * sizeof(T);
   if (smem > 48 * 1024) raise_smem_limit(ctx, (const void*)tri_inv_upper_kernel<T>);
   tri_inv_upper_kernel<T><<<(unsigned)k, kTiNT, smem, ctx->stream>>>(k, R, ldr, Y, ldy);
   post_launch(ctx, "tri_inv_upper_kernel");
@@ -2184,15 +2190,15 @@ template bool trsm_by_inverse<double>(const lra_ctx*, int64_t, int64_t);
 // update of the trailing columns, the trailing half; on the tensor-core
 // path X times the explicit inverse
 template <typename T>
-void trsm_right_upper(lra_ctx* ctx, int64_t m, int64_t k, const T* R, int64_t ldr, T* X, int64_t ldx) {
+void trsm_right_upper(lra_ctx* ctx, int64_t m, int64_t k, const T* R, int64_t ldr, T* X, int64_t ldx, const T* Yd) {
   if (m <= 0 || k <= 0) return;
   if (trsm_by_inverse<T>(ctx, k, m)) {
     const ArenaMark mk = ctx->arena.mark();
-    T* Y = ctx->arena.alloc_n<T>((size_t)k * k);
+    T* Y = Yd ? nullptr : ctx->arena.alloc_n<T>((size_t)k * k);
     T* W = ctx->arena.alloc_n<T>((size_t)m * k);
-    // X R^-1 = (X Y) D^-1 with Y = R^-1 D
-    tri_inv_upper<T>(ctx, k, R, ldr, Y, k);
-    gemm<T>(ctx, 'n', 'n', m, k, k, T(1), X, ldx, Y, k, T(0), W, m);
+    // X R^-1 = (X Y) D^-1 with Y = R^-1 D (Yd when the caller has it)
+    if (Y) tri_inv_upper<T>(ctx, k, R, ldr, Y, k);
+    gemm<T>(ctx, 'n', 'n', m, k, k, T(1), X, ldx, Yd ? Yd : Y, k, T(0), W, m);
     div_by_diag<T>(ctx, m, k, R, ldr, 'r', W, m, X, ldx);
     ctx->arena.release(mk);  // stream-ordered reuse
     return;
@@ -2213,8 +2219,10 @@ template bool potrf_upper<float>(lra_ctx*, int64_t, float*, int64_t);
 template bool potrf_upper<double>(lra_ctx*, int64_t, double*, int64_t);
 template void potrf_upper_batch<float>(lra_ctx*, int, const int64_t*, float* const*, const int64_t*, bool*);
 template void potrf_upper_batch<double>(lra_ctx*, int, const int64_t*, double* const*, const int64_t*, bool*);
-template void trsm_right_upper<float>(lra_ctx*, int64_t, int64_t, const float*, int64_t, float*, int64_t);
-template void trsm_right_upper<double>(lra_ctx*, int64_t, int64_t, const double*, int64_t, double*, int64_t);
+template void trsm_right_upper<float>(lra_ctx*, int64_t, int64_t, const float*, int64_t, float*, int64_t,
+                                      const float*);
+template void trsm_right_upper<double>(lra_ctx*, int64_t, int64_t, const double*, int64_t, double*, int64_t,
+                                       const double*);
 // ---- T = R11^{-1} R12 by back substitution, a thread per right-hand side -------
 // The ID's solve (src/id.jl:447, R11 \ R12) for ranks up to kBsMax: row
 // i of x is (x_i - sum_{j > i} R_ij x_j) / R_ii, the sum taken from j = i+1

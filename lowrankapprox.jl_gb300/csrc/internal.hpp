@@ -269,7 +269,7 @@ struct PackItem {
 void pack_results(lra_ctx* ctx, int64_t count, const PackItem* items, char* out);
 template <typename T>
 void trsm_upper(lra_ctx* ctx, int64_t k, int64_t nrhs, const T* R, int64_t ldr, T* X,
-                int64_t ldx);
+                int64_t ldx, const T* Yd = nullptr);
 
 // Householder vectors (below the diagonal of V, m x k) applied to X
 // (m x nc): X <- Q X (trans 'n') or Q^T X (trans 't').
@@ -298,11 +298,12 @@ void potrf_upper_batch(lra_ctx* ctx, int n, const int64_t* k, T* const* G, const
 // cholqr_pre with one pass and chol_v at once (their factorizations batched)
 template <typename T>
 bool cholqr1_and_chol_v(lra_ctx* ctx, int64_t m, int64_t k, T* X, int64_t ldx, const T* Rpre, int64_t ldr, T* Rc,
-                        int64_t nr, const T* Tm, T* Rv);
+                        int64_t nr, const T* Tm, T* Rv, const T* Rpre_inv = nullptr);
 // X (m x k) <- X triu(R)^{-1}, blocked (or times the explicit inverse, see
 // trsm_by_inverse)
 template <typename T>
-void trsm_right_upper(lra_ctx* ctx, int64_t m, int64_t k, const T* R, int64_t ldr, T* X, int64_t ldx);
+void trsm_right_upper(lra_ctx* ctx, int64_t m, int64_t k, const T* R, int64_t ldr, T* X, int64_t ldx,
+                      const T* Yd = nullptr);
 // Y = triu(R)^{-1} diag(R) (k x k, ld ldy); false when k is beyond the
 // kernel (2048)
 template <typename T>

@@ -61,7 +61,7 @@ bool cholqr_pre(lra_ctx* ctx, int64_t m, int64_t k, T* X, int64_t ldx, const T* 
 // either.
 template <typename T>
 bool cholqr1_and_chol_v(lra_ctx* ctx, int64_t m, int64_t k, T* X, int64_t ldx, const T* Rpre, int64_t ldr, T* Rc,
-                        int64_t nr, const T* Tm, T* Rv) {
+                        int64_t nr, const T* Tm, T* Rv, const T* Rpre_inv) {
   const int64_t kk = std::max<int64_t>(k, 1);
   set_identity(ctx, k, k, Rv, kk);
   if (k == 0) {
@@ -69,7 +69,7 @@ bool cholqr1_and_chol_v(lra_ctx* ctx, int64_t m, int64_t k, T* X, int64_t ldx, c
     return true;
   }
   if (nr > 0) gemm<T>(ctx, 'n', 't', k, k, nr, T(1), Tm, kk, Tm, kk, T(1), Rv, kk);
-  trsm_right_upper(ctx, m, k, Rpre, ldr, X, ldx);
+  trsm_right_upper(ctx, m, k, Rpre, ldr, X, ldx, Rpre_inv);
   gemm<T>(ctx, 't', 'n', k, k, m, T(1), X, ldx, X, ldx, T(0), Rc, kk);
   const int64_t ks[2] = {k, k}, lds[2] = {kk, kk};
   T* Gs[2] = {Rc, Rv};
@@ -140,9 +140,9 @@ template bool cholqr_pre<float>(lra_ctx*, int64_t, int64_t, float*, int64_t, con
 template bool cholqr_pre<double>(lra_ctx*, int64_t, int64_t, double*, int64_t, const double*, int64_t, int,
                                  double*);
 template bool cholqr1_and_chol_v<float>(lra_ctx*, int64_t, int64_t, float*, int64_t, const float*, int64_t, float*,
-                                        int64_t, const float*, float*);
+                                        int64_t, const float*, float*, const float*);
 template bool cholqr1_and_chol_v<double>(lra_ctx*, int64_t, int64_t, double*, int64_t, const double*, int64_t,
-                                         double*, int64_t, const double*, double*);
+                                         double*, int64_t, const double*, double*, const double*);
 template bool chol_v<float>(lra_ctx*, int64_t, int64_t, const float*, float*);
 template bool chol_v<double>(lra_ctx*, int64_t, int64_t, const double*, double*);
 template std::vector<float> small_svd<float>(lra_ctx*, int64_t, const float*, float*, float*, float*);

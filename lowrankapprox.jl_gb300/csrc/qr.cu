@@ -3148,17 +3148,18 @@ int64_t geqp3_adap(lra_ctx* ctx, int64_t m, int64_t n, T* A, int64_t lda, int64_
 // most 32 rows are solved by trsm_left_diag_kernel (a thread per right-hand
 // side, back substitution in registers)
 template <typename T>
-void trsm_upper(lra_ctx* ctx, int64_t k, int64_t nrhs, const T* R, int64_t ldr, T* X, int64_t ldx) {
+void trsm_upper(lra_ctx* ctx, int64_t k, int64_t nrhs, const T* R, int64_t ldr, T* X, int64_t ldx, const T* Yd) {
   if (k <= 0 || nrhs <= 0) return;
   if (trsm_by_inverse<T>(ctx, k, nrhs)) {
-    // R^-1 X = Y (D^-1 X) with Y = R^-1 D (entries of order one), a
-    // tensor-core GEMM
+    // R^-1 X = Y (D^-1 X) with Y = R^-1 D (entries of order one; Yd when the
+    // caller has it already), a tensor-core GEMM
     const ArenaMark mk = ctx->arena.mark();
-    T* Y = ctx->arena.alloc_n<T>((size_t)k * k);
+    T* Y = Yd ? nullptr : ctx->arena.alloc_n<T>((size_t)k * k);
     T* W = ctx->arena.alloc_n<T>((size_t)k * nrhs);
-    tri_inv_upper<T>(ctx, k, R, ldr, Y, k);
+    if (Y) tri_inv_upper<T>(ctx, k, R, ldr, Y, k);
+    const T* Yu = Yd ? Yd : Y;
     div_by_diag<T>(ctx, k, nrhs, R, ldr, 'l', X, ldx, W, k);
-    gemm<T>(ctx, 'n', 'n', k, nrhs, k, T(1), Y, k, W, k, T(0), X, ldx);
+    gemm<T>(ctx, 'n', 'n', k, nrhs, k, T(1), Yu, k, W, k, T(0), X, ldx);
     ctx->arena.release(mk);
     return;
   }
@@ -3376,7 +3377,7 @@ template int64_t geqp3_adap_noalloc<double>(lra_ctx*, int64_t, int64_t, double*,
 #define INST(T)                                                                                   \
   template int64_t geqp3_adap<T>(lra_ctx*, int64_t, int64_t, T*, int64_t, int64_t*, T*, int64_t,  \
                                  int64_t, double, double, bool);                                 \
-  template void trsm_upper<T>(lra_ctx*, int64_t, int64_t, const T*, int64_t, T*, int64_t);       \
+  template void trsm_upper<T>(lra_ctx*, int64_t, int64_t, const T*, int64_t, T*, int64_t, const T*); \
   template void apply_q<T>(lra_ctx*, char, int64_t, int64_t, const T*, int64_t, const T*, T*,    \
                            int64_t, int64_t);                                                    \
   template void orgqr<T>(lra_ctx*, int64_t, int64_t, T*, int64_t, const T*);                      \
