@@ -22,7 +22,10 @@ def _psvd(lra, A, opts, cluster):
     return F, launches
 
 
-@pytest.mark.parametrize("rate", [7.0, 20.0, 30.0, 41.0, 44.0])
+# core orders from about 70 to 450: the kernel's three register tiles (rows
+# a lane 4, 8, 14 for orders up to 128, 256, 448) and both sides of each
+# boundary, odd and even orders alike
+@pytest.mark.parametrize("rate", [7.0, 12.3, 13.1, 20.0, 24.9, 25.9, 30.0, 41.0, 44.0])
 def test_cluster_jacobi_mixed(lra, rate):
     m, n = 1400, 1000
     A = decaying(m, n, rate, 31)
