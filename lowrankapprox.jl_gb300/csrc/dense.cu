@@ -808,10 +808,11 @@ __global__ void __launch_bounds__(JBT * 32) jacobi_block_kernel(JacParams<float>
 // the round-robin tournament (slot 0 fixed, slot i <- slot i + 1, slot nn - 1
 // <- slot 1), which pairs every two columns once in nn - 1 steps and brings
 // every column back to its slot at the end of a sweep.  A column moves by the
-// sender's stores into the receiver's shared-memory mailbox (distributed
-// shared memory across the cluster), double-buffered by step parity, so one
-// cluster barrier a step orders the stores before the receiver's loads and
-// after its previous reads.  Warp w owns slots w (top) and nn - 1 - w
+// sender's stores into the receiver's shared-memory mailbox, double-buffered
+// by step parity: within a CTA plain stores and a release arrival on the
+// receiver's mbarrier, across CTAs stores into its distributed shared memory
+// that count their bytes on that mbarrier (st.async); the receiver waits for
+// the mbarrier's phase, with no barrier across the cluster per step.  Warp w owns slots w (top) and nn - 1 - w
 // (bottom): its top moves to warp w - 1's top (warp 1's to warp 0's bottom,
 // warp 0's stays), its bottom to warp w + 1's bottom (the last warp's to its
 // own top).  The rotation of a pair is that of jacobi_block_kernel.
@@ -831,18 +832,12 @@ __device__ __forceinline__ uint32_t dsmem_addr(const void* local, unsigned rank)
                : "r"((uint32_t)__cvta_generic_to_shared(local)), "r"(rank));
   return r;
 }
-// 16 bytes into this CTA's shared memory (local) or another's of the cluster
-__device__ __forceinline__ void mbox_st4(bool local, uint32_t a, f2_t x, f2_t y) {
-  if (local)
-    asm volatile("st.shared.v2.b64 [%0], {%1, %2};" ::"r"(a), "l"(x), "l"(y) : "memory");
-  else
-    asm volatile("st.shared::cluster.v2.b64 [%0], {%1, %2};" ::"r"(a), "l"(x), "l"(y) : "memory");
+// 16 / 8 bytes into this CTA's shared memory
+__device__ __forceinline__ void mbox_st4(uint32_t a, f2_t x, f2_t y) {
+  asm volatile("st.shared.v2.b64 [%0], {%1, %2};" ::"r"(a), "l"(x), "l"(y) : "memory");
 }
-__device__ __forceinline__ void mbox_st2(bool local, uint32_t a, f2_t x) {
-  if (local)
-    asm volatile("st.shared.b64 [%0], %1;" ::"r"(a), "l"(x) : "memory");
-  else
-    asm volatile("st.shared::cluster.b64 [%0], %1;" ::"r"(a), "l"(x) : "memory");
+__device__ __forceinline__ void mbox_st2(uint32_t a, f2_t x) {
+  asm volatile("st.shared.b64 [%0], %1;" ::"r"(a), "l"(x) : "memory");
 }
 
 // A column in a mailbox: rows lane + 32 t of lane `lane` as 16-byte chunks
@@ -850,10 +845,10 @@ __device__ __forceinline__ void mbox_st2(bool local, uint32_t a, f2_t x) {
 // multiple of 4 the last two at 4 32 (RPL / 4) + 2 lane.  In registers the
 // rows come in pairs: pair p holds t = 2p (low half) and 2p + 1 (high).
 template <int RPL>
-__device__ __forceinline__ void mbox_send(bool local, uint32_t base, int lane, const f2_t (&c)[RPL / 2]) {
+__device__ __forceinline__ void mbox_send(uint32_t base, int lane, const f2_t (&c)[RPL / 2]) {
 #pragma unroll
-  for (int q = 0; q < RPL / 4; ++q) mbox_st4(local, base + (uint32_t)((q * 32 + lane) * 16), c[2 * q], c[2 * q + 1]);
-  if constexpr (RPL % 4 == 2) mbox_st2(local, base + (uint32_t)((RPL / 4) * 512 + lane * 8), c[RPL / 2 - 1]);
+  for (int q = 0; q < RPL / 4; ++q) mbox_st4(base + (uint32_t)((q * 32 + lane) * 16), c[2 * q], c[2 * q + 1]);
+  if constexpr (RPL % 4 == 2) mbox_st2(base + (uint32_t)((RPL / 4) * 512 + lane * 8), c[RPL / 2 - 1]);
 }
 template <int RPL>
 __device__ __forceinline__ void mbox_recv(const float* box, int lane, f2_t (&c)[RPL / 2]) {
@@ -941,7 +936,7 @@ __device__ __forceinline__ bool jc_wait(uint64_t* bar, unsigned parity, int* err
   return __all_sync(0xffffffffu, ok);
 }
 
-template <int RPL, bool P2P>
+template <int RPL>
 __global__ void __launch_bounds__(512, 1) jacobi_cluster_kernel(JacParams<float> P, int nn) {
   static_assert(RPL % 2 == 0, "rows of a lane go in pairs");
   constexpr int NP = RPL / 2;
@@ -998,25 +993,21 @@ __global__ void __launch_bounds__(512, 1) jacobi_cluster_kernel(JacParams<float>
   const int bs_w = w >= 1 ? w - 1 : 1;                       // of its bottom
   const bool ts_local = ts_w >= 0 && ts_w / NW == (int)rank, bs_local = bs_w / NW == (int)rank;
   const unsigned remote_bytes = (unsigned)(((ts_w >= 0 && !ts_local) ? 1 : 0) + (bs_local ? 0 : 1)) * 2u * 128u * RPL;
-  if constexpr (P2P) {
-    if (lane == 0) {
-      const unsigned cnt = 1u + (ts_local ? 1u : 0u) + (bs_local ? 1u : 0u);
-      jc_mbar_init(&full[0][wl], cnt);
-      jc_mbar_init(&full[1][wl], cnt);
-      asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
-    }
+  if (lane == 0) {
+    const unsigned cnt = 1u + (ts_local ? 1u : 0u) + (bs_local ? 1u : 0u);
+    jc_mbar_init(&full[0][wl], cnt);
+    jc_mbar_init(&full[1][wl], cnt);
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
   cluster_barrier();  // every CTA of the cluster runs (its barriers set up) before any remote store
   int sweep = 0;
   unsigned step_par = 0;
-  bool alive = true;  // P2P: no wait has given up
+  bool alive = true;  // no wait has given up
   for (; sweep < P.max_sweeps; ++sweep) {
     if (rank == 0 && threadIdx.x == 0) offv[(sweep + 1) % 3] = 0u;
     float off = 0;
     for (int step = 0; step < nn - 1; ++step) {
-      if constexpr (P2P) {
-        if (lane == 0) jc_arrive_tx(&full[step_par & 1u][wl], remote_bytes);
-      }
+      if (lane == 0) jc_arrive_tx(&full[step_par & 1u][wl], remote_bytes);
       f2_t a2 = 0, b2 = 0, g2 = 0;
 #pragma unroll
       for (int p = 0; p < NP; ++p) {
@@ -1054,50 +1045,32 @@ __global__ void __launch_bounds__(512, 1) jacobi_cluster_kernel(JacParams<float>
         asm volatile("red.shared::cluster.max.u32 [%0], %1;" ::"r"(oa), "r"(__float_as_uint(off)) : "memory");
       }
       const int buf = (int)(step_par & 1u);
-      if constexpr (P2P) {
-        // a local receiver's arrival releases the whole warp's stores
-        if (alive && dt_w >= 0) {
-          if (dt_r == rank) {
-            mbox_send<RPL>(true, (uint32_t)__cvta_generic_to_shared(box(buf, dt_w % NW, dt_s, 0)), lane, xt);
-            mbox_send<RPL>(true, (uint32_t)__cvta_generic_to_shared(box(buf, dt_w % NW, dt_s, 1)), lane, vt);
-            __syncwarp();
-            if (lane == 0) jc_arrive(&full[buf][dt_w % NW]);
-          } else {
-            const uint32_t mb = dsmem_addr(&full[buf][dt_w % NW], dt_r);
-            mbox_send_async<RPL>(dsmem_addr(box(buf, dt_w % NW, dt_s, 0), dt_r), mb, lane, xt);
-            mbox_send_async<RPL>(dsmem_addr(box(buf, dt_w % NW, dt_s, 1), dt_r), mb, lane, vt);
-          }
+      // a local receiver's arrival releases the whole warp's stores
+      if (alive && dt_w >= 0) {
+        if (dt_r == rank) {
+          mbox_send<RPL>((uint32_t)__cvta_generic_to_shared(box(buf, dt_w % NW, dt_s, 0)), lane, xt);
+          mbox_send<RPL>((uint32_t)__cvta_generic_to_shared(box(buf, dt_w % NW, dt_s, 1)), lane, vt);
+          __syncwarp();
+          if (lane == 0) jc_arrive(&full[buf][dt_w % NW]);
+        } else {
+          const uint32_t mb = dsmem_addr(&full[buf][dt_w % NW], dt_r);
+          mbox_send_async<RPL>(dsmem_addr(box(buf, dt_w % NW, dt_s, 0), dt_r), mb, lane, xt);
+          mbox_send_async<RPL>(dsmem_addr(box(buf, dt_w % NW, dt_s, 1), dt_r), mb, lane, vt);
         }
-        if (alive) {
-          if (db_r == rank) {
-            mbox_send<RPL>(true, (uint32_t)__cvta_generic_to_shared(box(buf, db_w % NW, db_s, 0)), lane, xb);
-            mbox_send<RPL>(true, (uint32_t)__cvta_generic_to_shared(box(buf, db_w % NW, db_s, 1)), lane, vb);
-            __syncwarp();
-            if (lane == 0) jc_arrive(&full[buf][db_w % NW]);
-          } else {
-            const uint32_t mb = dsmem_addr(&full[buf][db_w % NW], db_r);
-            mbox_send_async<RPL>(dsmem_addr(box(buf, db_w % NW, db_s, 0), db_r), mb, lane, xb);
-            mbox_send_async<RPL>(dsmem_addr(box(buf, db_w % NW, db_s, 1), db_r), mb, lane, vb);
-          }
-        }
-        if (alive) alive = jc_wait(&full[buf][wl], (step_par >> 1) & 1u, &P.bar->err);
-      } else {
-        if (dt_w >= 0) {
-          const bool local = dt_r == rank;
-          const uint32_t bx = (uint32_t)__cvta_generic_to_shared(box(buf, dt_w % NW, dt_s, 0));
-          const uint32_t bv = (uint32_t)__cvta_generic_to_shared(box(buf, dt_w % NW, dt_s, 1));
-          mbox_send<RPL>(local, local ? bx : dsmem_addr(box(buf, dt_w % NW, dt_s, 0), dt_r), lane, xt);
-          mbox_send<RPL>(local, local ? bv : dsmem_addr(box(buf, dt_w % NW, dt_s, 1), dt_r), lane, vt);
-        }
-        {
-          const bool local = db_r == rank;
-          const uint32_t bx = (uint32_t)__cvta_generic_to_shared(box(buf, db_w % NW, db_s, 0));
-          const uint32_t bv = (uint32_t)__cvta_generic_to_shared(box(buf, db_w % NW, db_s, 1));
-          mbox_send<RPL>(local, local ? bx : dsmem_addr(box(buf, db_w % NW, db_s, 0), db_r), lane, xb);
-          mbox_send<RPL>(local, local ? bv : dsmem_addr(box(buf, db_w % NW, db_s, 1), db_r), lane, vb);
-        }
-        cluster_barrier();
       }
+      if (alive) {
+        if (db_r == rank) {
+          mbox_send<RPL>((uint32_t)__cvta_generic_to_shared(box(buf, db_w % NW, db_s, 0)), lane, xb);
+          mbox_send<RPL>((uint32_t)__cvta_generic_to_shared(box(buf, db_w % NW, db_s, 1)), lane, vb);
+          __syncwarp();
+          if (lane == 0) jc_arrive(&full[buf][db_w % NW]);
+        } else {
+          const uint32_t mb = dsmem_addr(&full[buf][db_w % NW], db_r);
+          mbox_send_async<RPL>(dsmem_addr(box(buf, db_w % NW, db_s, 0), db_r), mb, lane, xb);
+          mbox_send_async<RPL>(dsmem_addr(box(buf, db_w % NW, db_s, 1), db_r), mb, lane, vb);
+        }
+      }
+      if (alive) alive = jc_wait(&full[buf][wl], (step_par >> 1) & 1u, &P.bar->err);
       if (w != 0) {
         mbox_recv<RPL>(box(buf, wl, 0, 0), lane, xt);
         mbox_recv<RPL>(box(buf, wl, 0, 1), lane, vt);
@@ -1106,16 +1079,15 @@ __global__ void __launch_bounds__(512, 1) jacobi_cluster_kernel(JacParams<float>
       mbox_recv<RPL>(box(buf, wl, 1, 1), lane, vb);
       ++step_par;
     }
-    // the barrier of the sweep's last step ordered every warp's maximum (a
-    // cluster barrier a sweep on the point-to-point path); a wait that gave
-    // up anywhere ends the sweeps everywhere at the same point
-    if constexpr (P2P) cluster_barrier();
+    // a cluster barrier a sweep orders every warp's maximum; a wait that
+    // gave up anywhere ends the sweeps everywhere at the same point
+    cluster_barrier();
     unsigned mb;
     asm volatile("ld.shared::cluster.u32 %0, [%1];"
                  : "=r"(mb)
                  : "r"(off_remote + (uint32_t)((sweep % 3) * sizeof(unsigned)))
                  : "memory");
-    const bool failed = P2P && *((volatile int*)&P.bar->err) != 0;
+    const bool failed = *((volatile int*)&P.bar->err) != 0;
     if ((double)__uint_as_float(mb) <= P.stop || failed) {
       ++sweep;
       break;
@@ -1453,15 +1425,9 @@ static bool jacobi_cluster(lra_ctx* ctx, JacParams<float>& P) {
   const int64_t n = P.n;
   if (!jacobi_cluster_enabled() || n < 64 || n > 32 * 14) return false;
   const int rpl = n <= 128 ? 4 : n <= 256 ? 8 : 14;
-  // the columns move point to point (mbarriers) unless LRA_JACOBI_P2P=0
-  // asks for a cluster barrier every step
-  static const bool p2p = [] {
-    const char* e = std::getenv("LRA_JACOBI_P2P");
-    return !(e && *e == '0');
-  }();
-  const void* kern = rpl == 4   ? (p2p ? (const void*)jacobi_cluster_kernel<4, true> : (const void*)jacobi_cluster_kernel<4, false>)
-                     : rpl == 8 ? (p2p ? (const void*)jacobi_cluster_kernel<8, true> : (const void*)jacobi_cluster_kernel<8, false>)
-                                : (p2p ? (const void*)jacobi_cluster_kernel<14, true> : (const void*)jacobi_cluster_kernel<14, false>);
+  const void* kern = rpl == 4   ? (const void*)jacobi_cluster_kernel<4>
+                     : rpl == 8 ? (const void*)jacobi_cluster_kernel<8>
+                                : (const void*)jacobi_cluster_kernel<14>;
   int optin = 0;
   LRA_CUDA(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, ctx->device));
   const size_t per_warp = (size_t)1024 * rpl;  // two buffers x two slots x (X, V) x 32 rpl floats
