@@ -1951,7 +1951,73 @@ __global__ void trsm_left_diag_kernel(int jb, int64_t nrhs, const T* Rbb, int64_
 // lower part zeroed) in one cooperative launch; ok[m] false when G_m is not
 // numerically positive definite
 template <typename T>
+void potrf_upper_batch(lra_ctx* ctx, int n, const int64_t* k, T* const* G, const int64_t* ldg, bool* ok);
+
+// Blocked right-looking Cholesky on the tensor-core path for orders past
+// kPotrfPanel * 2: per panel of kPotrfPanel columns the diagonal blocks of
+// all matrices factored in one cooperative launch, the block rows R12 =
+// R11^-T G12 = Dr^-1 (Y^T G12) with Y = R11^-1 Dr (tri_inv_upper), and the
+// trailing G22 -= R12^T R12 as a tensor-core GEMM; the cooperative kernel's
+// FP64 trailing updates (k^3 / 3 FMAs on the FP64 pipe) are the cost this
+// removes.
+constexpr int64_t kPotrfPanel = 256;
+
+template <typename T>
+void potrf_upper_blocked(lra_ctx* ctx, int n, const int64_t* k, T* const* G, const int64_t* ldg, bool* ok) {
+  int64_t kmax = 0;
+  for (int m = 0; m < n; ++m) {
+    ok[m] = true;
+    kmax = std::max(kmax, k[m]);
+  }
+  for (int64_t j0 = 0; j0 < kmax; j0 += kPotrfPanel) {
+    int64_t kb[2] = {0, 0}, lb[2] = {1, 1};
+    T* Gb[2] = {nullptr, nullptr};
+    bool okb[2] = {true, true};
+    int idx[2] = {-1, -1}, nb = 0;
+    for (int m = 0; m < n; ++m) {
+      if (!ok[m] || j0 >= k[m]) continue;
+      idx[nb] = m;
+      kb[nb] = std::min(kPotrfPanel, k[m] - j0);
+      Gb[nb] = G[m] + j0 + j0 * ldg[m];
+      lb[nb] = ldg[m];
+      ++nb;
+    }
+    if (nb == 0) break;
+    potrf_upper_batch<T>(ctx, nb, kb, Gb, lb, okb);
+    for (int b = 0; b < nb; ++b) {
+      const int m = idx[b];
+      if (!okb[b]) {
+        ok[m] = false;
+        continue;
+      }
+      const int64_t jb = kb[b], rest = k[m] - j0 - jb, ld = ldg[m];
+      if (rest <= 0) continue;
+      const ArenaMark mk = ctx->arena.mark();
+      T* Y = ctx->arena.alloc_n<T>((size_t)jb * jb);
+      T* W = ctx->arena.alloc_n<T>((size_t)jb * rest);
+      tri_inv_upper<T>(ctx, jb, Gb[b], ld, Y, jb);
+      T* G12 = G[m] + j0 + (j0 + jb) * ld;
+      gemm<T>(ctx, 't', 'n', jb, rest, jb, T(1), Y, jb, G12, ld, T(0), W, jb);
+      div_by_diag<T>(ctx, jb, rest, Gb[b], ld, 'l', W, jb, G12, ld);
+      T* G22 = G[m] + (j0 + jb) + (j0 + jb) * ld;
+      gemm<T>(ctx, 't', 'n', rest, rest, jb, T(-1), G12, ld, G12, ld, T(1), G22, ld);
+      ctx->arena.release(mk);  // stream-ordered reuse
+    }
+  }
+  for (int m = 0; m < n; ++m)
+    if (k[m] > 0) zero_lower(ctx, k[m], k[m], G[m], ldg[m]);
+}
+
+template <typename T>
 void potrf_upper_batch(lra_ctx* ctx, int n, const int64_t* k, T* const* G, const int64_t* ldg, bool* ok) {
+  if (sizeof(T) == 8 && ctx->gemm_tc) {
+    int64_t kmax = 0;
+    for (int m = 0; m < n; ++m) kmax = std::max(kmax, k[m]);
+    if (kmax > 2 * kPotrfPanel) {
+      potrf_upper_blocked<T>(ctx, n, k, G, ldg, ok);
+      return;
+    }
+  }
   const ArenaMark mk = ctx->arena.mark();
   int* bad = ctx->arena.alloc_n<int>(2);
   LRA_CUDA(cudaMemsetAsync(bad, 0, 2 * sizeof(int), ctx->stream));
@@ -2051,7 +2117,8 @@ namespace {
 // range, which a GEMM that scales each row by its largest entry would
 // truncate; R^-1 D has entries of order one.
 constexpr int kTiNT = 128;
-constexpr int kTiRows = 16;  // rows a thread: k up to 2048
+constexpr int kTiRows = 16;   // rows a thread: k up to 2048
+constexpr int kTiLeaf = 512;  // larger orders split in two on the tensor-core path
 
 template <typename T>
 __global__ void __launch_bounds__(kTiNT) tri_inv_upper_kernel(int64_t k, const T* __restrict__ R, int64_t ldr,
@@ -2130,6 +2197,25 @@ template <typename T>
 bool tri_inv_upper(lra_ctx* ctx, int64_t k, const T* R, int64_t ldr, T* Y, int64_t ldy) {
   if (k <= 0) return true;
   if (k > (int64_t)kTiNT * kTiRows) return false;
+  if (sizeof(T) == 8 && ctx->gemm_tc && k > kTiLeaf) {
+    // Recursive on the tensor-core path: with R = [A B; 0 C] and D = diag(R),
+    // R^-1 D = [Ya, -Ya (Da^-1 B) Yc; 0, Yc] for Ya = A^-1 Da, Yc = C^-1 Dc.
+    // Every factor has entries of order one (Da^-1 B because |R_iq| <=
+    // |R_ii| in a pivoted QR's R), so the two products are accurate on the
+    // tensor cores; the leaves' column substitutions are shorter.
+    const int64_t k1 = (k / 2 + 31) / 32 * 32, k2 = k - k1;
+    tri_inv_upper<T>(ctx, k1, R, ldr, Y, ldy);
+    tri_inv_upper<T>(ctx, k2, R + k1 + k1 * ldr, ldr, Y + k1 + k1 * ldy, ldy);
+    const ArenaMark mk = ctx->arena.mark();
+    T* W = ctx->arena.alloc_n<T>((size_t)k1 * k2);
+    T* W2 = ctx->arena.alloc_n<T>((size_t)k1 * k2);
+    div_by_diag<T>(ctx, k1, k2, R, ldr, 'l', R + k1 * ldr, ldr, W, k1);
+    gemm<T>(ctx, 'n', 'n', k1, k2, k2, T(1), W, k1, Y + k1 + k1 * ldy, ldy, T(0), W2, k1);
+    gemm<T>(ctx, 'n', 'n', k1, k2, k1, T(-1), Y, ldy, W2, k1, T(0), Y + k1 * ldy, ldy);
+    zero_lower(ctx, k, k, Y, ldy);  // the block below the diagonal
+    ctx->arena.release(mk);  // stream-ordered reuse
+    return true;
+  }
   const size_t smem = (size_t)2 * k * sizeof(T);
   if (smem > 48 * 1024) raise_smem_limit(ctx, (const void*)tri_inv_upper_kernel<T>);
   tri_inv_upper_kernel<T><<<(unsigned)k, kTiNT, smem, ctx->stream>>>(k, R, ldr, Y, ldy);

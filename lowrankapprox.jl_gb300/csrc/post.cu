@@ -19,6 +19,7 @@
 // k x k SVD / eigenproblem is iterative.
 
 #include <algorithm>
+#include <chrono>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -68,15 +69,32 @@ bool cholqr1_and_chol_v(lra_ctx* ctx, int64_t m, int64_t k, T* X, int64_t ldx, c
     set_identity(ctx, k, k, Rc, kk);
     return true;
   }
+  // LRA_TRACE: the phases (each waits for the device)
+  const bool tr = trace_on();
+  auto tnow = [] { return std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now().time_since_epoch()).count(); };
+  double tl = tr ? tnow() : 0;
+  auto tmark = [&](const char* what) {
+    if (!tr) return;
+    LRA_CUDA(cudaStreamSynchronize(ctx->stream));
+    const double t = tnow();
+    std::fprintf(stderr, "[lra] cholqr k=%lld %s %.3f ms\n", (long long)k, what, t - tl);
+    tl = t;
+  };
+  tmark("start");
   if (nr > 0) gemm<T>(ctx, 'n', 't', k, k, nr, T(1), Tm, kk, Tm, kk, T(1), Rv, kk);
+  tmark("I + T T'");
   trsm_right_upper(ctx, m, k, Rpre, ldr, X, ldx, Rpre_inv);
+  tmark("X / R11");
   gemm<T>(ctx, 't', 'n', k, k, m, T(1), X, ldx, X, ldx, T(0), Rc, kk);
+  tmark("gram");
   const int64_t ks[2] = {k, k}, lds[2] = {kk, kk};
   T* Gs[2] = {Rc, Rv};
   bool ok[2] = {true, true};
   potrf_upper_batch<T>(ctx, 2, ks, Gs, lds, ok);
+  tmark("two cholesky");
   if (!ok[0] || !ok[1]) return false;
   trsm_right_upper(ctx, m, k, Rc, kk, X, ldx);
+  tmark("X / Rc");
   return true;
 }
 
