@@ -76,7 +76,7 @@ def main():
             out[f"qr/{tag}/tau"] = tau[:k]
     np.savez_compressed(os.path.join(HERE, "laqps_cases.npz"), **out)
 
-    # Hilbert 1024 idfact (BASELINE's CPU-runnable case), rtol 1e-12 and the
+    # Hilbert 1024 idfact (the reference README's CPU-sized case), rtol 1e-12 and the
     # default 5 eps; 40 x 1024 lattice-Gaussian sketch from seed 0.
     A = O.hilb(1024)
     s = lattice_gauss(0, 40 * 1024 * 2)

@@ -92,7 +92,7 @@ def test_status_strings(lib):
 
 def test_python_options_mirror():
     import lowrankapprox as L
-    o = L.LRAOptions(sketch="subs", rank=5)   # BASELINE's :subs spelling means :sub
+    o = L.LRAOptions(sketch="subs", rank=5)   # the :subs spelling means :sub
     assert o.sketch == "sub" and o.rank == 5
     o2 = o.copy(rtol=1e-3)
     assert o2.rtol == 1e-3 and o.rtol != 1e-3

@@ -1,5 +1,6 @@
 """GPU parity against the oracle at the benchmarked workloads, on the same
-sketch (the benchmark spec's bar, with the tolerances written here):
+sketch (ranks and skeletons equal outside near-ties, errors within 2x of the
+oracle's, with the tolerances written here):
 
 * psvdfact of the dense 8192 x 8192 Float64 matrix U diag(10^(-i/40)) V'
   at rtol 1e-10 on the mixed-precision path (the headline workload);
