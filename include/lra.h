@@ -207,7 +207,16 @@ int lra_ctx_stage_ms(const lra_ctx* ctx, double out[4]);
    from the table LRA_TUNING names or the one beside liblra.so
    (tuning_gb300.txt, written by lowrankapprox/autotune.py).  set overrides
    one entry of this context (keys "tc_tile_n" with index dtype * 16 +
-   ceil(log2 order), "qr_seq_len", "srft_wide" with index log2 l');
+   ceil(log2 order), "qr_seq_len", "srft_wide" with index log2 l'; index 0
+   for the rest: "qr_steps" (adaptive steps a pivoted-QR launch may hold,
+   1..8), "qr_sms" (SMs a QR launch may take, 0 all), "tc_split" (most K
+   parts of the tensor-core sketch, 0 as many as fill the SMs),
+   "jacobi_jb" (FP32 Jacobi block columns 4, 8, 16, 32; 0 by size),
+   "jacobi_cluster" (largest cluster of the in-cluster FP32 Jacobi, 2..16;
+   0 the largest schedulable, 1 never), "trsm_inv" (1: FP64 triangular
+   solves on the tensor-core path by substitution instead of the
+   unit-diagonal inverse), "gram_start" (cosine x 1e4 where the FP32 sweeps
+   hand over to the Gram polish, 0 by order));
    get writes the table in force and its source as text and returns the
    length it needs (with the terminating zero).  No counterpart in the
    reference, whose BLAS picks its own blocking.                           */
